@@ -1,0 +1,311 @@
+"""Benchmark: residual + RK4 throughput of the shock-fitted CPG cylinder at 800 x 400.
+
+One step = one explicit RK4 step (ADVECT_FLOW_EXPLICIT: 4 residual stages, shock
+fitting, CFL dt on the device) over the 800 x 400 cylinder = 1.28 M cell-stages.
+Metric: Mcell-stage/s (cells x 4 stages x steps / time), FP64.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Device timing: CUDA events on the library's stream around each step; every step is
+preceded (outside its timed window) by a 512 MiB write that evicts the 129 MB L2.
+e2e: the same metric through the public API with host buffers: per step, the state
+is uploaded from pinned host memory (hymor_set_state), advanced (hymor_step) and
+read back (hymor_get_state), timed on the host clock.
+With --gpus N > 1 (torchrun) every rank advances its own replica of the case (the
+path has no cross-GPU exchange); value = all ranks' cell-stages / max rank time.
+--impl reference times the CPU restatement of the reference path (the oracle,
+OpenMP over every host core) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NCHI, NETA = 800, 400
+CELLS = NCHI * NETA
+STAGES = 4
+BYTES_PER_CELL_STAGE = 216   # algorithmic bytes of residual + RK4 stage (2-D CPG)
+FLUSH_BYTES = 512 << 20
+METRIC = "Mcell-RK4-stages/s"
+UNIT = "Mcell-stage/s"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_numbers():
+    """Per-launch DRAM traffic and FP64 work of the flux kernel from the committed ncu
+    summary (profiles/k_flux_cylinder_800x400.md), or None."""
+    path = os.path.join(ROOT, "profiles", "k_flux_cylinder_800x400.md")
+    out = {}
+    try:
+        for line in open(path):
+            for key in ("traffic_bytes_per_launch", "fp64_flop_per_launch"):
+                if line.strip().startswith(key + ":"):
+                    out[key] = float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def init_dist(world, backend):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def max_over_ranks(dist, value: float) -> float:
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64)
+    if dist.get_backend() == "nccl":
+        t = t.cuda()
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def make_case():
+    from hymor_gb300 import case as C
+    cfg = C.cylinder_config(NCHI, NETA)
+    return cfg, C.initial_state(cfg)
+
+
+def cpu_baseline_sample(cs, budget_s: float = 12.0):
+    """Oracle (CPU restatement of the reference path, OpenMP) on a bounded sample of the
+    same workload: whole RK4 steps of the 800 x 400 cylinder until ~budget_s."""
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    O.lib().orc_set_threads(threads)
+    o = O.Oracle(cs)
+    o.advect(1)  # warm-up
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        o.advect(1)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el > budget_s or steps >= 200:
+            break
+    return {"value": CELLS * STAGES * steps / el / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{steps} RK4 steps of the {NCHI}x{NETA} cylinder ({el:.1f} s)"}
+
+
+def run_reference(args, world, rank):
+    """--impl reference: the reference's CPU path (restated, the oracle) on host cores."""
+    if rank != 0:
+        return 0
+    cfg, cs = make_case()
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    O.lib().orc_set_threads(threads)
+    o = O.Oracle(cs)
+    for _ in range(args.warmup):
+        o.advect(1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.advect(1)
+    el = time.perf_counter() - t0
+    v = CELLS * STAGES * args.steps / el / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"shock-fitted CPG cylinder {NCHI}x{NETA}, M5 Re1e4, residual + RK4 step",
+                   "cells": CELLS, "stages_per_step": STAGES, "parallelism": "cpu"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} RK4 steps of the {NCHI}x{NETA} cylinder"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference is Julia (not installable here); its hot path restated in C++ "
+                "(oracle/hymor_oracle.cpp) is timed instead",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="hymor", choices=["hymor", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+
+    dist = init_dist(world, "nccl")
+    import torch
+    torch.cuda.set_device(local)
+    from hymor_gb300 import solver as S
+    from hymor_gb300._lib import dp, ip
+
+    cfg, cs = make_case()
+    sol = S.Solution(cs)
+    L, h = sol.ctx.L, sol.ctx.h
+    # warm-up (graph capture happens on the first step)
+    ms = ctypes.c_float()
+    sol.ctx.check(L.hymor_bench_steps(h, args.warmup, FLUSH_BYTES, ctypes.byref(ms)))
+    # timed region: K steps, flux-kernel events on
+    sol.ctx.check(L.hymor_profile_flux(h, 1, None, None))
+    torch.cuda.synchronize()
+    barrier(dist)
+    with ClockSampler(local) as clk:
+        sol.ctx.check(L.hymor_bench_steps(h, args.steps, FLUSH_BYTES, ctypes.byref(ms)))
+    torch.cuda.synchronize()
+    barrier(dist)
+    flux_ms, flux_n = ctypes.c_float(), ctypes.c_int32()
+    sol.ctx.check(L.hymor_profile_flux(h, 0, ctypes.byref(flux_ms), ctypes.byref(flux_n)))
+    t_dev = max_over_ranks(dist, ms.value / 1e3)
+    total_cell_stages = CELLS * STAGES * args.steps * world
+    value = total_cell_stages / t_dev / 1e6
+
+    # end-to-end through the public API with pinned host buffers
+    G = (NCHI + 2) * (NETA + 2)
+    q_host = torch.empty(4 * G, dtype=torch.float64, pin_memory=True)
+    q_host.numpy()[:] = cs.q_flat()
+    st = sol.get_state()
+    pts = [np.ascontiguousarray(st[k]) for k in ("pts_x", "pts_y", "pts_chi", "pts_eta")]
+    ci = np.ascontiguousarray(st["cell_idx"])
+    qp = ctypes.cast(q_host.data_ptr(), ctypes.POINTER(ctypes.c_double))
+    sol.set_state(q_host.numpy(), *pts, ci, st["t"])
+    torch.cuda.synchronize()
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        sol.ctx.check(L.hymor_set_state(h, qp, dp(pts[0]), dp(pts[1]), dp(pts[2]), dp(pts[3]), ip(ci), 0.0, None))
+        sol.ctx.check(L.hymor_step(h, 1))
+        sol.ctx.check(L.hymor_get_state(h, qp, dp(pts[0]), dp(pts[1]), dp(pts[2]), dp(pts[3]), ip(ci), None, None))
+    t_e2e = max_over_ranks(dist, time.perf_counter() - t0)
+    e2e_value = CELLS * STAGES * args.e2e_steps * world / t_e2e / 1e6
+    h2d = 4 * G * 8 + 4 * NCHI * 8 + NCHI * 4
+    d2h = h2d
+
+    if rank == 0:
+        hbm, kind = peaks()
+        flux_avg_s = flux_ms.value / 1e3 / max(flux_n.value, 1)
+        achieved = BYTES_PER_CELL_STAGE * CELLS / flux_avg_s / 1e9
+        prof = profile_numbers()
+        roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                    "frac": achieved / hbm, "traffic": prof.get("traffic_bytes_per_launch"),
+                    "kernel": "k_flux (residual, one RK stage)", "peak_kind": kind,
+                    "flux_kernel_ms": flux_avg_s * 1e3, "flux_launches": flux_n.value}
+        if "fp64_flop_per_launch" in prof:
+            fp = prof["fp64_flop_per_launch"] / flux_avg_s / 1e12
+            roofline["fp64"] = {"achieved_tflops": fp, "peak_tflops": 1.2, "frac": fp / 1.2,
+                                "peak_kind": "measured DFMA microbenchmark"}
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"shock-fitted CPG cylinder {NCHI}x{NETA}, M5 Re1e4, residual + RK4 step",
+                       "cells": CELLS, "stages_per_step": STAGES, "parallelism": f"replicas x{world}",
+                       "l2": "512 MiB flush before every timed step"},
+            "roofline": roofline,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": 20 * args.steps,
+            "clocks": clk.summary(),
+        }
+        if not args.no_cpu_baseline and world == 1:
+            line["cpu_baseline"] = cpu_baseline_sample(cs)
+        elif world > 1:
+            line["cpu_baseline"] = None
+        print(json.dumps(line), flush=True)
+    sol.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,658 @@
+// C ABI of libhymor: context, state transfer, residual, RK4 step (CUDA graph),
+// CFL, timing. Declarations and reference citations: include/hymor.h.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+
+namespace hymor {
+void flux_kernel_setup();
+}
+
+using namespace hymor;
+
+struct hymor_ctx_s {
+  DevCtx d;
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  std::string err;
+  std::vector<void*> allocs;
+  // step graph
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  // flux-kernel profiling: 8 event-record nodes (start/stop of the 4 flux launches)
+  bool profile = false;
+  cudaGraphNode_t ev_nodes[8] = {};
+  cudaEvent_t cap_ev[8] = {};
+  std::vector<cudaEvent_t> prof_ev;  // 8 per profiled step
+  int prof_steps = 0;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  int timer_running = 0;
+  // L2 flush scratch of hymor_bench_steps
+  void* flush_buf = nullptr;
+  uint64_t flush_bytes = 0;
+};
+
+namespace {
+
+int fail(hymor_ctx* c, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return code;
+}
+
+#define CU(call)                                                                    \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess)                                                          \
+      return fail(ctx, HYMOR_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                  __FILE__, __LINE__);                                              \
+  } while (0)
+
+template <typename T>
+int dalloc(hymor_ctx* ctx, T** p, size_t count) {
+  void* v = nullptr;
+  CU(cudaMalloc(&v, count * sizeof(T) + 16));
+  CU(cudaMemset(v, 0, count * sizeof(T) + 16));
+  ctx->allocs.push_back(v);
+  *p = static_cast<T*>(v);
+  return 0;
+}
+
+#define TRY(x)            \
+  do {                    \
+    int r_ = (x);         \
+    if (r_) return r_;    \
+  } while (0)
+
+int check_config(hymor_ctx* ctx, const hymor_config* c) {
+  if (c->nchi < 3 || c->neta < 4) return fail(ctx, HYMOR_ERR_INVALID, "grid too small: %d x %d", c->nchi, c->neta);
+  if (c->nchi > 4096) return fail(ctx, HYMOR_ERR_INVALID, "Nchi = %d exceeds 4096 (shock spline workspace)", c->nchi);
+  if ((long)(c->nchi + 2) * (c->neta + 2) > (1L << 31) / 2) return fail(ctx, HYMOR_ERR_INVALID, "grid too large");
+  const int bcs[4] = {c->bc_chi0, c->bc_chi1, c->bc_eta0, c->bc_eta1};
+  for (int e = 0; e < 4; ++e) {
+    if (bcs[e] < 0 || bcs[e] > HYMOR_BC_SHOCK) return fail(ctx, HYMOR_ERR_INVALID, "unknown boundary condition %d", bcs[e]);
+    if (bcs[e] == HYMOR_BC_SHOCK && e != 3)
+      return fail(ctx, HYMOR_ERR_INVALID, "Non defined Boundary-condition: shock is only valid on eta1");
+  }
+  if (c->shock_enabled && c->bc_eta1 != HYMOR_BC_SHOCK)
+    return fail(ctx, HYMOR_ERR_INVALID, "shock fitting needs boundary_eta1 = shock");
+  if (c->shock_interp < 1 || c->shock_interp > 3) return fail(ctx, HYMOR_ERR_INVALID, "Invalid shock.interpolate");
+  if (!(c->gamma > 1)) return fail(ctx, HYMOR_ERR_INVALID, "freestream.gamma must be > 1");
+  if (!(c->Re > 0) || !(c->Pr > 0)) return fail(ctx, HYMOR_ERR_INVALID, "Re and Pr must be positive");
+  if (c->mapping < 0 || c->mapping > 3) return fail(ctx, HYMOR_ERR_INVALID, "unknown mapping %d", c->mapping);
+  if (c->rk_variant < 0 || c->rk_variant > 1) return fail(ctx, HYMOR_ERR_INVALID, "unknown rk_variant");
+  if (c->viscosity_model < 0 || c->viscosity_model > 1) return fail(ctx, HYMOR_ERR_INVALID, "unknown viscosity model");
+  if (c->shock_enabled && !(c->spline_param > 0 && c->spline_param <= 1))
+    return fail(ctx, HYMOR_ERR_INVALID, "spline_param must be in (0, 1]");
+  return 0;
+}
+
+int upload(hymor_ctx* ctx, double** dst, const double* src, size_t n, const char* name) {
+  if (!src) return fail(ctx, HYMOR_ERR_INVALID, "mesh array %s is NULL", name);
+  TRY(dalloc(ctx, dst, n));
+  CU(cudaMemcpy(*dst, src, n * sizeof(double), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+// Geometry planes of the flux kernel (see common.cuh), computed once per mesh on the
+// host in FP64 from the reference's mesh arrays (VISCOUS_FLUX.jl:72-95).
+void face_geometry(const hymor_config& c, const hymor_mesh& m, std::vector<double>& lrg,
+                   std::vector<double>& btg, std::vector<double>& rvol, std::vector<double>& rxl,
+                   std::vector<double>& rxb) {
+  const int nchi = c.nchi, neta = c.neta;
+  const long NLR = (long)(nchi + 1) * neta, NBT = (long)nchi * (neta + 1), N = (long)nchi * neta;
+  lrg.assign(kGeoPlanes * NLR, 0.0);
+  btg.assign(kGeoPlanes * NBT, 0.0);
+  rvol.assign(N, 0.0);
+  rxl.assign(NLR, 0.0);
+  rxb.assign(NBT, 0.0);
+  auto X = [&](int i, int j) { return m.x_ext[i + (long)j * (nchi + 2)]; };
+  auto Y = [&](int i, int j) { return m.y_ext[i + (long)j * (nchi + 2)]; };
+  auto xc = [&](int i, int j) { return m.x_corner[i + (long)j * (nchi + 1)]; };
+  auto yc = [&](int i, int j) { return m.y_corner[i + (long)j * (nchi + 1)]; };
+  for (int j = 0; j < neta; ++j)
+    for (int i = 0; i <= nchi; ++i) {
+      const long f = i + (long)j * (nchi + 1);
+      const double nx = m.lr_xn[f], ny = m.lr_yn[f];
+      const double dX = X(i + 1, j + 1) - X(i, j + 1), dY = Y(i + 1, j + 1) - Y(i, j + 1);
+      const double cld = std::sqrt(dY * dY + dX * dX);
+      const double c1x = -dX / cld, c1y = -dY / cld;
+      const double Cnn = -c1x * nx - c1y * ny;
+      const double Cft = c1x * ny - c1y * nx;
+      const double lx = xc(i, j + 1) - xc(i, j), ly = yc(i, j + 1) - yc(i, j);
+      const double len = std::sqrt(lx * lx + ly * ly);
+      lrg[0 * NLR + f] = nx;
+      lrg[1 * NLR + f] = ny;
+      lrg[2 * NLR + f] = m.lr_a[f];
+      lrg[3 * NLR + f] = -1.0 / (cld * Cnn);
+      lrg[4 * NLR + f] = -Cft / (len * Cnn);
+      lrg[5 * NLR + f] = 1.0 / len;
+      rxl[f] = 1.0 / ((X(i + 1, j + 1) + X(i, j + 1)) / 2);
+    }
+  for (int j = 0; j <= neta; ++j)
+    for (int i = 0; i < nchi; ++i) {
+      const long f = i + (long)j * nchi;
+      const double nx = m.bt_xn[f], ny = m.bt_yn[f];
+      const double dX = X(i + 1, j + 1) - X(i + 1, j), dY = Y(i + 1, j + 1) - Y(i + 1, j);
+      const double cbd = std::sqrt(dY * dY + dX * dX);
+      const double c2x = dX / cbd, c2y = dY / cbd;
+      const double Cnn = c2x * nx + c2y * ny;
+      const double Cft = c2x * ny - c2y * nx;
+      const double lx = xc(i + 1, j) - xc(i, j), ly = yc(i + 1, j) - yc(i, j);
+      const double len = std::sqrt(lx * lx + ly * ly);
+      btg[0 * NBT + f] = nx;
+      btg[1 * NBT + f] = ny;
+      btg[2 * NBT + f] = m.bt_a[f];
+      btg[3 * NBT + f] = 1.0 / (cbd * Cnn);
+      btg[4 * NBT + f] = Cft / (len * Cnn);
+      btg[5 * NBT + f] = 1.0 / len;
+      rxb[f] = 1.0 / ((X(i + 1, j + 1) + X(i + 1, j)) / 2);
+    }
+  for (long k = 0; k < N; ++k) rvol[k] = 1.0 / m.vol[k];
+}
+
+int enqueue_step(hymor_ctx* ctx, bool with_events) {
+  DevCtx& d = ctx->d;
+  cudaStream_t st = ctx->stream;
+  const hymor_config& c = d.cfg;
+  const bool shock = c.shock_enabled;
+  CU(cudaMemsetAsync(d.scal + kCmax, 0, 3 * sizeof(double), st));
+  if (shock) launch_flow_cells(d, st);
+  launch_sound_cmax(d, shock, st);
+  launch_cfl(d, st);
+  const double wA[4] = {1.0 / 6, 1.0 / 3, 1.0 / 3, 1.0 / 6};
+  const double wY[4] = {0.5, 0.5, 1.0, 0.0};
+  double* const F[4] = {d.F[0], d.F[1], d.F[2], d.F[3]};
+  auto flux = [&](int k) -> int {
+    if (with_events) CU(cudaEventRecord(ctx->cap_ev[2 * k], st));
+    launch_flux(d, false, F, st);
+    if (with_events) CU(cudaEventRecord(ctx->cap_ev[2 * k + 1], st));
+    return 0;
+  };
+  if (c.rk_variant == 0) {
+    launch_update_thermo(d, 0, 0, 0, st);
+    launch_shock_bc(d, false, true, shock, wY[0], wA[0], 0, st);
+    TRY(flux(0));
+    for (int k = 1; k < 4; ++k) {
+      launch_update_thermo(d, 1, wY[k - 1], wA[k - 1], st);
+      launch_shock_bc(d, false, false, shock, wY[k], wA[k], 0, st);
+      TRY(flux(k));
+    }
+  } else {
+    launch_snapshot(d, st);
+    launch_update_thermo(d, 0, 0, 0, st);
+    launch_shock_bc(d, false, true, shock, 0.0, wA[0], 0, st);
+    TRY(flux(0));
+    for (int k = 1; k < 4; ++k) {
+      launch_classical_stage(d, wY[k - 1], st);
+      launch_update_thermo(d, 5, 0, wA[k - 1], st);
+      launch_shock_bc(d, false, false, shock, 0.0, wA[k], 0, st);
+      TRY(flux(k));
+    }
+  }
+  launch_update_thermo(d, 2, 0, wA[3], st);
+  launch_shock_bc(d, true, false, false, 0, 0, 1, st);
+  launch_fill_minrho(d, true, st);
+  CU(cudaGetLastError());
+  return 0;
+}
+
+int build_graph(hymor_ctx* ctx) {
+  if (ctx->gexec) return 0;
+  CU(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  int r = enqueue_step(ctx, true);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  if (r) return r;
+  if (e != cudaSuccess) return fail(ctx, HYMOR_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+  ctx->graph = g;
+  CU(cudaGraphInstantiate(&ctx->gexec, g, 0));
+  // map the event-record nodes to their flux-launch slots
+  size_t nn = 0;
+  CU(cudaGraphGetNodes(g, nullptr, &nn));
+  std::vector<cudaGraphNode_t> nodes(nn);
+  CU(cudaGraphGetNodes(g, nodes.data(), &nn));
+  for (auto n : nodes) {
+    cudaGraphNodeType ty;
+    CU(cudaGraphNodeGetType(n, &ty));
+    if (ty != cudaGraphNodeTypeEventRecord) continue;
+    cudaEvent_t ev;
+    CU(cudaGraphEventRecordNodeGetEvent(n, &ev));
+    for (int k = 0; k < 8; ++k)
+      if (ctx->cap_ev[k] == ev) ctx->ev_nodes[k] = n;
+  }
+  return 0;
+}
+
+int read_err(hymor_ctx* ctx) {
+  unsigned h[kErrCount];
+  CU(cudaMemcpyAsync(h, ctx->d.err, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  if (h[kErrFlags] & kBitShockRange)
+    return fail(ctx, HYMOR_ERR_SHOCK_RANGE, "shocked cell outside rows 2..Neta-1 (the shock left the mesh)");
+  if (h[kErrFlags] & kBitNumeric)
+    return fail(ctx, HYMOR_ERR_NUMERIC, "non-positive density or pressure, or NaN, in the flow field");
+  if (h[kErrFlags] & kBitTimeout) return fail(ctx, HYMOR_ERR_TIMEOUT, "bounded device wait gave up");
+  return 0;
+}
+
+int set_device(hymor_ctx* ctx) {
+  CU(cudaSetDevice(ctx->device));
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx** out) {
+  if (!out) return HYMOR_ERR_INVALID;
+  *out = nullptr;
+  if (!cfg || !mesh) return HYMOR_ERR_INVALID;
+  hymor_ctx* ctx = new hymor_ctx_s();
+  auto bail = [&](int r) {
+    // keep the context so the caller can read the message, then let them destroy it
+    *out = ctx;
+    return r;
+  };
+  int r = check_config(ctx, cfg);
+  if (r) return bail(r);
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1)
+    return bail(fail(ctx, HYMOR_ERR_CUDA, "no CUDA device visible"));
+  cudaGetDevice(&ctx->device);
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(ctx, HYMOR_ERR_CUDA, "stream creation failed"));
+  flux_kernel_setup();
+  DevCtx& d = ctx->d;
+  d.cfg = *cfg;
+  d.nchi = cfg->nchi;
+  d.neta = cfg->neta;
+  d.NI = d.nchi + 2;
+  d.NJ = d.neta + 2;
+  d.G = (long)d.NI * d.NJ;
+  d.N = (long)d.nchi * d.neta;
+  d.NLR = (long)(d.nchi + 1) * d.neta;
+  d.NBT = (long)d.nchi * (d.neta + 1);
+  const long NC = (long)(d.nchi + 1) * (d.neta + 1);
+  DevMesh& m = d.m;
+  m.nchi = d.nchi;
+  m.neta = d.neta;
+  double* tmp;
+#define UP(field, n)                                                  \
+  do {                                                                \
+    if ((r = upload(ctx, &tmp, mesh->field, (n), #field))) return bail(r); \
+    m.field = tmp;                                                    \
+  } while (0)
+  UP(lr_xn, d.NLR); UP(lr_yn, d.NLR); UP(lr_a, d.NLR);
+  UP(bt_xn, d.NBT); UP(bt_yn, d.NBT); UP(bt_a, d.NBT);
+  UP(vol, d.N); UP(x_ext, d.G); UP(y_ext, d.G);
+  UP(x_corner, NC); UP(y_corner, NC); UP(chi1, d.nchi);
+  if (cfg->axisymmetric) {
+    UP(fb_area, d.N);
+  } else {
+    m.fb_area = nullptr;
+  }
+#undef UP
+  m.fb_yn_front = mesh->fb_yn_front;
+  m.fb_yn_back = mesh->fb_yn_back;
+  {
+    std::vector<double> lrg, btg, rvol, rxl, rxb;
+    face_geometry(*cfg, *mesh, lrg, btg, rvol, rxl, rxb);
+    double *p1, *p2, *p3, *p4, *p5;
+    if ((r = upload(ctx, &p1, lrg.data(), lrg.size(), "lr geometry"))) return bail(r);
+    if ((r = upload(ctx, &p2, btg.data(), btg.size(), "bt geometry"))) return bail(r);
+    if ((r = upload(ctx, &p3, rvol.data(), rvol.size(), "1/vol"))) return bail(r);
+    if ((r = upload(ctx, &p4, rxl.data(), rxl.size(), "1/x lr"))) return bail(r);
+    if ((r = upload(ctx, &p5, rxb.data(), rxb.size(), "1/x bt"))) return bail(r);
+    m.lrg = p1; m.btg = p2; m.rvol = p3; m.rx_lr = p4; m.rx_bt = p5;
+  }
+  auto cons = [&](Cons& q) -> int {
+    TRY(dalloc(ctx, &q.rho, d.G)); TRY(dalloc(ctx, &q.ru, d.G));
+    TRY(dalloc(ctx, &q.rv, d.G)); TRY(dalloc(ctx, &q.rE, d.G));
+    return 0;
+  };
+  auto pts = [&](ShockPts& s) -> int {
+    TRY(dalloc(ctx, &s.x, d.nchi)); TRY(dalloc(ctx, &s.y, d.nchi));
+    TRY(dalloc(ctx, &s.chi, d.nchi)); TRY(dalloc(ctx, &s.eta, d.nchi));
+    return 0;
+  };
+  if ((r = cons(d.S)) || (r = cons(d.Y))) return bail(r);
+  if (cfg->rk_variant == 1) {
+    if ((r = cons(d.Yc)) || (r = pts(d.Ycp))) return bail(r);
+  } else {
+    d.Yc = d.S;
+    d.Ycp = ShockPts{};
+  }
+  if ((r = dalloc(ctx, &d.p, d.G)) || (r = dalloc(ctx, &d.T, d.G)) || (r = dalloc(ctx, &d.aS, d.G)) ||
+      (r = dalloc(ctx, &d.aY, d.G)))
+    return bail(r);
+  for (int v = 0; v < 4; ++v)
+    if ((r = dalloc(ctx, &d.F[v], d.N)) || (r = dalloc(ctx, &d.SF[v], d.N))) return bail(r);
+  if ((r = pts(d.Sp)) || (r = pts(d.Yp))) return bail(r);
+  if ((r = dalloc(ctx, &d.cell_idx, d.nchi)) || (r = dalloc(ctx, &d.beta, d.nchi)) ||
+      (r = dalloc(ctx, &d.speed_x, d.nchi)) || (r = dalloc(ctx, &d.speed_y, d.nchi)) ||
+      (r = dalloc(ctx, &d.rel, d.nchi)) || (r = dalloc(ctx, &d.spl, 8 * (long)d.nchi + 8)) ||
+      (r = dalloc(ctx, &d.scal, (long)kCount)) || (r = dalloc(ctx, &d.err, (long)kErrCount)))
+    return bail(r);
+  d.coef = nullptr;
+  d.jwork = nullptr;
+  for (int k = 0; k < 8; ++k)
+    if (cudaEventCreate(&ctx->cap_ev[k]) != cudaSuccess) return bail(fail(ctx, HYMOR_ERR_CUDA, "event"));
+  cudaEventCreate(&ctx->t0);
+  cudaEventCreate(&ctx->t1);
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return bail(fail(ctx, HYMOR_ERR_CUDA, "create: %s", cudaGetErrorString(e)));
+  *out = ctx;
+  return 0;
+}
+
+int hymor_ctx_destroy(hymor_ctx* ctx) {
+  if (!ctx) return HYMOR_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+  if (ctx->graph) cudaGraphDestroy(ctx->graph);
+  for (auto e : ctx->cap_ev)
+    if (e) cudaEventDestroy(e);
+  for (auto e : ctx->prof_ev) cudaEventDestroy(e);
+  if (ctx->t0) cudaEventDestroy(ctx->t0);
+  if (ctx->t1) cudaEventDestroy(ctx->t1);
+  for (void* p : ctx->allocs) cudaFree(p);
+  if (ctx->flush_buf) cudaFree(ctx->flush_buf);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return 0;
+}
+
+const char* hymor_last_error(const hymor_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int hymor_set_state(hymor_ctx* ctx, const double* q, const double* pts_x, const double* pts_y,
+                    const double* pts_chi, const double* pts_eta, const int32_t* cell_idx, double t,
+                    const double* a) {
+  if (!ctx) return HYMOR_ERR_INVALID;
+  if (!q) return fail(ctx, HYMOR_ERR_INVALID, "q is NULL");
+  TRY(set_device(ctx));
+  DevCtx& d = ctx->d;
+  const size_t G = d.G, n = d.nchi;
+  const bool shock = d.cfg.shock_enabled;
+  if (shock && (!pts_x || !pts_y || !pts_chi || !pts_eta || !cell_idx))
+    return fail(ctx, HYMOR_ERR_INVALID, "shock fitting needs the shock points and cell indices");
+  std::vector<int32_t> ci(n, d.neta + 1);
+  if (cell_idx) {
+    for (size_t i = 0; i < n; ++i) {
+      ci[i] = cell_idx[i];
+      if (shock && (ci[i] < 2 || ci[i] > d.neta - 1))
+        return fail(ctx, HYMOR_ERR_SHOCK_RANGE, "cell_idx[%zu] = %d outside 2..Neta-1", i, ci[i]);
+    }
+  }
+  cudaStream_t st = ctx->stream;
+  CU(cudaMemcpyAsync(d.S.rho, q, G * 8, cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(d.S.ru, q + G, G * 8, cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(d.S.rv, q + 2 * G, G * 8, cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(d.S.rE, q + 3 * G, G * 8, cudaMemcpyHostToDevice, st));
+  if (pts_x) CU(cudaMemcpyAsync(d.Sp.x, pts_x, n * 8, cudaMemcpyHostToDevice, st));
+  if (pts_y) CU(cudaMemcpyAsync(d.Sp.y, pts_y, n * 8, cudaMemcpyHostToDevice, st));
+  if (pts_chi) CU(cudaMemcpyAsync(d.Sp.chi, pts_chi, n * 8, cudaMemcpyHostToDevice, st));
+  if (pts_eta) CU(cudaMemcpyAsync(d.Sp.eta, pts_eta, n * 8, cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(d.cell_idx, ci.data(), n * 4, cudaMemcpyHostToDevice, st));
+  double sc[kCount] = {0};
+  sc[kT] = t;
+  CU(cudaMemcpyAsync(d.scal, sc, sizeof sc, cudaMemcpyHostToDevice, st));
+  if (a) {
+    CU(cudaMemcpyAsync(d.aS, a, G * 8, cudaMemcpyHostToDevice, st));
+  } else {
+    launch_sound_cmax(d, true, st);
+  }
+  CU(cudaStreamSynchronize(st));
+  CU(cudaGetLastError());
+  return 0;
+}
+
+int hymor_get_state(hymor_ctx* ctx, double* q, double* pts_x, double* pts_y, double* pts_chi,
+                    double* pts_eta, int32_t* cell_idx, double* t, double* dt) {
+  if (!ctx) return HYMOR_ERR_INVALID;
+  TRY(set_device(ctx));
+  DevCtx& d = ctx->d;
+  const size_t G = d.G, n = d.nchi;
+  cudaStream_t st = ctx->stream;
+  if (q) {
+    CU(cudaMemcpyAsync(q, d.S.rho, G * 8, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(q + G, d.S.ru, G * 8, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(q + 2 * G, d.S.rv, G * 8, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(q + 3 * G, d.S.rE, G * 8, cudaMemcpyDeviceToHost, st));
+  }
+  if (pts_x) CU(cudaMemcpyAsync(pts_x, d.Sp.x, n * 8, cudaMemcpyDeviceToHost, st));
+  if (pts_y) CU(cudaMemcpyAsync(pts_y, d.Sp.y, n * 8, cudaMemcpyDeviceToHost, st));
+  if (pts_chi) CU(cudaMemcpyAsync(pts_chi, d.Sp.chi, n * 8, cudaMemcpyDeviceToHost, st));
+  if (pts_eta) CU(cudaMemcpyAsync(pts_eta, d.Sp.eta, n * 8, cudaMemcpyDeviceToHost, st));
+  if (cell_idx) CU(cudaMemcpyAsync(cell_idx, d.cell_idx, n * 4, cudaMemcpyDeviceToHost, st));
+  double sc[kCount];
+  CU(cudaMemcpyAsync(sc, d.scal, sizeof sc, cudaMemcpyDeviceToHost, st));
+  CU(cudaStreamSynchronize(st));
+  if (t) *t = sc[kT];
+  if (dt) *dt = sc[kDt];
+  return 0;
+}
+
+int hymor_residual(hymor_ctx* ctx, double* flux) {
+  if (!ctx) return HYMOR_ERR_INVALID;
+  TRY(set_device(ctx));
+  DevCtx& d = ctx->d;
+  cudaStream_t st = ctx->stream;
+  launch_update_thermo(d, 3, 0, 0, st);
+  launch_sound_cmax(d, true, st);
+  launch_shock_bc(d, true, false, false, 0, 0, 1, st);
+  double* const SF[4] = {d.SF[0], d.SF[1], d.SF[2], d.SF[3]};
+  launch_flux(d, true, SF, st);
+  CU(cudaGetLastError());
+  if (flux)
+    for (int v = 0; v < 4; ++v)
+      CU(cudaMemcpyAsync(flux + v * d.N, d.SF[v], d.N * 8, cudaMemcpyDeviceToHost, st));
+  return read_err(ctx);
+}
+
+int hymor_set_flux(hymor_ctx* ctx, const double* flux) {
+  if (!ctx || !flux) return HYMOR_ERR_INVALID;
+  TRY(set_device(ctx));
+  for (int v = 0; v < 4; ++v)
+    CU(cudaMemcpyAsync(ctx->d.SF[v], flux + v * ctx->d.N, ctx->d.N * 8, cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return 0;
+}
+
+int hymor_step(hymor_ctx* ctx, int nsteps) {
+  if (!ctx) return HYMOR_ERR_INVALID;
+  if (nsteps < 0) return fail(ctx, HYMOR_ERR_INVALID, "nsteps < 0");
+  TRY(set_device(ctx));
+  TRY(build_graph(ctx));
+  for (int s = 0; s < nsteps; ++s) {
+    if (ctx->profile) {
+      const size_t base = ctx->prof_ev.size();
+      for (int k = 0; k < 8; ++k) {
+        cudaEvent_t ev;
+        CU(cudaEventCreate(&ev));
+        ctx->prof_ev.push_back(ev);
+        if (ctx->ev_nodes[k]) CU(cudaGraphExecEventRecordNodeSetEvent(ctx->gexec, ctx->ev_nodes[k], ev));
+      }
+      (void)base;
+      ctx->prof_steps++;
+    }
+    CU(cudaGraphLaunch(ctx->gexec, ctx->stream));
+  }
+  return read_err(ctx);
+}
+
+int hymor_bench_steps(hymor_ctx* ctx, int nsteps, uint64_t flush_bytes, float* ms) {
+  if (!ctx || nsteps < 0) return HYMOR_ERR_INVALID;
+  TRY(set_device(ctx));
+  TRY(build_graph(ctx));
+  if (flush_bytes > ctx->flush_bytes) {
+    if (ctx->flush_buf) CU(cudaFree(ctx->flush_buf));
+    ctx->flush_buf = nullptr;
+    CU(cudaMalloc(&ctx->flush_buf, flush_bytes));
+    ctx->flush_bytes = flush_bytes;
+  }
+  std::vector<cudaEvent_t> ev(2 * (size_t)nsteps);
+  for (auto& e : ev) CU(cudaEventCreate(&e));
+  for (int s = 0; s < nsteps; ++s) {
+    if (flush_bytes) CU(cudaMemsetAsync(ctx->flush_buf, s & 0xff, flush_bytes, ctx->stream));
+    if (ctx->profile) {
+      for (int k = 0; k < 8; ++k) {
+        cudaEvent_t e;
+        CU(cudaEventCreate(&e));
+        ctx->prof_ev.push_back(e);
+        if (ctx->ev_nodes[k]) CU(cudaGraphExecEventRecordNodeSetEvent(ctx->gexec, ctx->ev_nodes[k], e));
+      }
+      ctx->prof_steps++;
+    }
+    CU(cudaEventRecord(ev[2 * s], ctx->stream));
+    CU(cudaGraphLaunch(ctx->gexec, ctx->stream));
+    CU(cudaEventRecord(ev[2 * s + 1], ctx->stream));
+  }
+  CU(cudaStreamSynchronize(ctx->stream));
+  double tot = 0;
+  for (int s = 0; s < nsteps; ++s) {
+    float v = 0;
+    CU(cudaEventElapsedTime(&v, ev[2 * s], ev[2 * s + 1]));
+    tot += v;
+  }
+  for (auto e : ev) cudaEventDestroy(e);
+  if (ms) *ms = (float)tot;
+  return read_err(ctx);
+}
+
+int hymor_update_flow_cells(hymor_ctx* ctx) {
+  if (!ctx) return HYMOR_ERR_INVALID;
+  TRY(set_device(ctx));
+  if (ctx->d.cfg.shock_enabled) {
+    launch_flow_cells(ctx->d, ctx->stream);
+    launch_sound_cmax(ctx->d, true, ctx->stream);
+  }
+  CU(cudaGetLastError());
+  return read_err(ctx);
+}
+
+int hymor_cfl_timestep(hymor_ctx* ctx, double* dt) {
+  if (!ctx) return HYMOR_ERR_INVALID;
+  TRY(set_device(ctx));
+  DevCtx& d = ctx->d;
+  CU(cudaMemsetAsync(d.scal + kCmax, 0, 3 * sizeof(double), ctx->stream));
+  launch_sound_cmax(d, false, ctx->stream);
+  launch_cfl(d, ctx->stream);
+  CU(cudaGetLastError());
+  double sc[kCount];
+  CU(cudaMemcpyAsync(sc, d.scal, sizeof sc, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  if (dt) *dt = sc[kDt];
+  return 0;
+}
+
+int hymor_counters(hymor_ctx* ctx, int32_t* rho_limited, int32_t* rh_warnings) {
+  if (!ctx) return HYMOR_ERR_INVALID;
+  TRY(set_device(ctx));
+  unsigned h[kErrCount];
+  CU(cudaMemcpyAsync(h, ctx->d.err, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  if (rho_limited) *rho_limited = (int32_t)h[kRhoLimited];
+  if (rh_warnings) *rh_warnings = (int32_t)h[kRhWarn];
+  return 0;
+}
+
+int hymor_timer_start(hymor_ctx* ctx) {
+  if (!ctx) return HYMOR_ERR_INVALID;
+  CU(cudaEventRecord(ctx->t0, ctx->stream));
+  ctx->timer_running = 1;
+  return 0;
+}
+
+int hymor_timer_stop(hymor_ctx* ctx, float* ms) {
+  if (!ctx || !ctx->timer_running) return HYMOR_ERR_INVALID;
+  CU(cudaEventRecord(ctx->t1, ctx->stream));
+  CU(cudaEventSynchronize(ctx->t1));
+  ctx->timer_running = 0;
+  float v = 0;
+  CU(cudaEventElapsedTime(&v, ctx->t0, ctx->t1));
+  if (ms) *ms = v;
+  return 0;
+}
+
+int hymor_profile_flux(hymor_ctx* ctx, int enable, float* total_ms, int32_t* launches) {
+  if (!ctx) return HYMOR_ERR_INVALID;
+  TRY(set_device(ctx));
+  if (total_ms || launches) {
+    CU(cudaStreamSynchronize(ctx->stream));
+    double tot = 0;
+    int n = 0;
+    for (size_t s = 0; s + 8 <= ctx->prof_ev.size(); s += 8)
+      for (int k = 0; k < 4; ++k) {
+        float v = 0;
+        CU(cudaEventElapsedTime(&v, ctx->prof_ev[s + 2 * k], ctx->prof_ev[s + 2 * k + 1]));
+        tot += v;
+        ++n;
+      }
+    if (total_ms) *total_ms = (float)tot;
+    if (launches) *launches = n;
+  }
+  for (auto e : ctx->prof_ev) cudaEventDestroy(e);
+  ctx->prof_ev.clear();
+  ctx->prof_steps = 0;
+  if (ctx->gexec) {
+    for (int k = 0; k < 8; ++k)
+      if (ctx->ev_nodes[k]) CU(cudaGraphExecEventRecordNodeSetEvent(ctx->gexec, ctx->ev_nodes[k], ctx->cap_ev[k]));
+  }
+  ctx->profile = enable != 0;
+  return 0;
+}
+
+int hymor_synchronize(hymor_ctx* ctx) {
+  if (!ctx) return HYMOR_ERR_INVALID;
+  CU(cudaStreamSynchronize(ctx->stream));
+  return read_err(ctx);
+}
+
+int hymor_device_alloc(hymor_ctx* ctx, uint64_t bytes, void** dptr) {
+  if (!ctx || !dptr) return HYMOR_ERR_INVALID;
+  TRY(set_device(ctx));
+  CU(cudaMalloc(dptr, bytes));
+  return 0;
+}
+
+int hymor_device_free(hymor_ctx* ctx, void* dptr) {
+  if (!ctx) return HYMOR_ERR_INVALID;
+  CU(cudaFree(dptr));
+  return 0;
+}
+
+int hymor_memcpy_h2d(hymor_ctx* ctx, void* dst, const void* src, uint64_t bytes) {
+  if (!ctx) return HYMOR_ERR_INVALID;
+  CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return 0;
+}
+
+int hymor_memcpy_d2h(hymor_ctx* ctx, void* dst, const void* src, uint64_t bytes) {
+  if (!ctx) return HYMOR_ERR_INVALID;
+  CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return 0;
+}
+
+}  // extern "C"
+
+// DevCtx accessor for linear.cu
+namespace hymor {
+DevCtx& ctx_dev(hymor_ctx* c) { return c->d; }
+cudaStream_t ctx_stream(hymor_ctx* c) { return c->stream; }
+int ctx_fail(hymor_ctx* c, int code, const char* msg) { return fail(c, code, "%s", msg); }
+std::vector<void*>& ctx_allocs(hymor_ctx* c) { return c->allocs; }
+}  // namespace hymor

@@ -1,0 +1,1307 @@
+// Residual, shock fitting, boundary conditions and time-marching kernels (sm_103a).
+//
+// One RK4 step (ADVECT_FLOW_EXPLICIT, utils/Time_marching/ADVECT_FLOW_EXPLICIT.jl:36-81)
+// is this launch sequence on one stream (captured once into a CUDA graph):
+//
+//   flow_cells      UPDATE_FLOW_CELLS on S: shocked-cell detection, upstream fill,
+//                   extrapolation (one thread per chi column)
+//   sound_cmax      sound speed of S, max|a|                       (all ghosted cells)
+//   cfl             CFL_TIMESTEP maxima, dt on the device           (all cells)
+//   4 x { update_thermo   stage update of Y and S, p/T of Y       (all ghosted cells)
+//         shock_bc        spline + R-H jump + extrapolation + MOVE_SHOCK, then the
+//                         ghost-cell boundary conditions           (one CTA)
+//         flux            FV residual of Y                         (31x8-cell tiles) }
+//   update_thermo   last S update, p/T of S
+//   shock_bc        UPDATE_SHOCK_BC + APPLY_BOUNDARY_CONDITIONS on S (one CTA)
+//   fill_minrho     UPDATE_FIELD_UPSTREAM + MIN_RHO on S, t += dt
+//
+// The flux kernel dominates. It is FP64-bound on GB300 (about 1.9 DFMA/clk/SM):
+// geometry-only factors are precomputed per face (common.cuh), every face flux is
+// evaluated once per tile in shared memory, and divisions are replaced by
+// reciprocal multiplies (frcp).
+#include <cmath>
+#include <cstdio>
+
+#include "kernels.h"
+
+namespace hymor {
+
+namespace {
+
+constexpr int TX = 31;           // cells per tile along chi (TX + 1 = 32 lr faces per row)
+constexpr int TY = 8;            // cells per tile along eta
+constexpr int HX = TX + 2, HY = TY + 2, NH = HX * HY;
+constexpr int CX = TX + 1, CY = TY + 1, NCOR = CX * CY;
+constexpr int NLRF = (TX + 1) * TY;  // 256
+constexpr int NBTF = TX * (TY + 1);  // 279
+constexpr int kFluxThreads = 256;
+
+__device__ __forceinline__ bool flow_at(const int* cell_idx, bool shock, int i, int j1) {
+  // j1: 1-based interior row; flow cells are rows below the shocked row
+  return !shock || j1 < cell_idx[i];
+}
+
+// ---------------------------------------------------------------------------
+// Stage update + thermodynamic state (INTEGRATION.jl:53-71 followed by
+// UPDATE_THERMODYNAMIC_PROPERTIES.jl:22-31, CPG: cv* = 1).
+struct UpdArgs {
+  Cons S, Y, Yc;
+  const double* F0;
+  const double* F1;
+  const double* F2;
+  const double* F3;
+  double *p, *T;
+  const int* cell_idx;
+  const double* scal;
+  unsigned* err;
+  double cY, cS, gm1;
+  int nchi, neta, mode, shock;
+};
+
+__global__ void __launch_bounds__(256) k_update_thermo(UpdArgs a) {
+  const int NI = a.nchi + 2, NJ = a.neta + 2;
+  const long G = (long)NI * NJ;
+  const double dt = a.scal[kDt];
+  const double wY = a.cY * dt, wS = a.cS * dt;
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < G; k += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(k % NI), j = (int)(k / NI);
+    const bool interior = i >= 1 && i <= a.nchi && j >= 1 && j <= a.neta;
+    double r, u, v, e;
+    const Cons& tgt = (a.mode == 2 || a.mode == 3) ? a.S : a.Y;
+    if (a.mode == 0) {
+      r = a.S.rho[k]; u = a.S.ru[k]; v = a.S.rv[k]; e = a.S.rE[k];
+      a.Y.rho[k] = r; a.Y.ru[k] = u; a.Y.rv[k] = v; a.Y.rE[k] = e;
+    } else {
+      r = tgt.rho[k]; u = tgt.ru[k]; v = tgt.rv[k]; e = tgt.rE[k];
+      if (interior && (a.mode == 1 || a.mode == 2 || a.mode == 5)) {
+        const long c = (long)(i - 1) + (long)(j - 1) * a.nchi;
+        if (flow_at(a.cell_idx, a.shock, i - 1, j)) {
+          const double f0 = a.F0[c], f1 = a.F1[c], f2 = a.F2[c], f3 = a.F3[c];
+          // S (accumulator) += wS * k
+          a.S.rho[k] = fma(wS, f0, a.S.rho[k]);
+          a.S.ru[k] = fma(wS, f1, a.S.ru[k]);
+          a.S.rv[k] = fma(wS, f2, a.S.rv[k]);
+          a.S.rE[k] = fma(wS, f3, a.S.rE[k]);
+          if (a.mode == 1) {  // Y (stage) += wY * k
+            r = fma(wY, f0, r); u = fma(wY, f1, u); v = fma(wY, f2, v); e = fma(wY, f3, e);
+            a.Y.rho[k] = r; a.Y.ru[k] = u; a.Y.rv[k] = v; a.Y.rE[k] = e;
+          } else if (a.mode == 2) {
+            r = a.S.rho[k]; u = a.S.ru[k]; v = a.S.rv[k]; e = a.S.rE[k];
+          }
+        }
+      }
+    }
+    // e = (rho_E - (rho_u^2 + rho_v^2) / rho / 2) / rho ; p = rho e (gamma - 1) ; T = e
+    const double ir = frcp(r);
+    const double ke = fma(u, u, v * v) * ir;
+    const double eint = fma(-0.5, ke, e);
+    const double p = eint * a.gm1;
+    const double T = eint * ir;
+    a.p[k] = p;
+    a.T[k] = T;
+    if (interior && !(r > 0 && p > 0)) atomicOr(&a.err[kErrFlags], kBitNumeric);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Shock fitting + boundary conditions, one CTA.
+
+struct ShockArgs {
+  hymor_config cfg;
+  Cons tgt;          // array being evaluated
+  double *p, *T;     // its ghosted thermodynamic state
+  double* a_bc;      // sound speed used by the LODI outflow condition (ghosted)
+  bool compute_a;    // fill a_bc's edge-adjacent lines from p and rho first
+  ShockPts pts;      // shock points of tgt
+  ShockPts pS;       // shock points of S (MOVE_SHOCK of the accumulator)
+  bool copy_pts, move, on_S, do_shock, do_bc;
+  double cY, cS;
+  const int* cell_idx;
+  double *beta, *speed_x, *speed_y, *rel;
+  double* spl;       // workspace: 8 * nchi doubles
+  const double* scal;
+  unsigned* err;
+  DevMesh m;
+};
+
+// Element-space coordinates (utils/Mesh/GO_TO_ELEMENT_SPACE.jl:28-140).
+__device__ void element_space(const hymor_config& c, double x, double y, double& chi, double& eta) {
+  if (c.mapping == HYMOR_MAP_CIRCLE) {
+    const double angle_min = -c.circle_angle_extra, angle_max = M_PI / 2;
+    double t = atan2(-x, y) + M_PI / 2;
+    double mm = fmod(t, 2 * M_PI);
+    if (mm < 0) mm += 2 * M_PI;
+    const double angle = mm - M_PI / 2;
+    const double ch = (angle_max - angle) / (angle_max - angle_min);
+    const double r = sqrt(x * x + y * y);
+    const double dmax = c.dRs + (c.dRe - c.dRs) * (ch * ch);
+    chi = ch;
+    eta = (r - c.R) / dmax;
+  } else if (c.mapping == HYMOR_MAP_BLUNT_CONE) {
+    const double Lm = c.L, Rm = c.R, th = c.theta, ib = c.initial_beta;
+    const double s_Straight = ((Lm - Rm) + Rm * cos(th)) / sin(th);
+    const double s_Curve = 2 * th * Rm;
+    const double s_tot = s_Curve + 2 * s_Straight;
+    const double s_Str_sh = ((Lm - Rm) + Rm * cos(ib)) / sin(ib);
+    const double s_Crv_sh = ib * Rm;
+    const double s_tot_sh = 2 * s_Crv_sh + 2 * s_Str_sh;
+    const double slope = sin(th - ib);
+    const double x_body = y, y_body = -x;
+    const double tang = (y_body - (Lm - Rm)) / x_body;
+    double eta_phys, chi_arc;
+    if ((tang < tan(M_PI / 2 - th)) && (x_body > 0)) {
+      eta_phys = y_body * cos(th) + x_body * sin(th) - Rm - (Lm - Rm) * cos(th);
+      const double lambda = (x_body / cos(th) - (eta_phys * sin(th) + Rm * sin(th)) / cos(th)) / s_tot;
+      chi_arc = s_Straight / s_tot - lambda;
+    } else if ((-tan(M_PI / 2 - th) < tang) && (x_body < 0)) {
+      eta_phys = y_body * cos(th) - x_body * sin(th) - Rm - (Lm - Rm) * cos(th);
+      const double lambda = (-x_body / cos(th) - (eta_phys * sin(th) + Rm * sin(th)) / cos(th)) / s_tot;
+      chi_arc = (s_Straight + s_Curve) / s_tot + lambda;
+    } else {
+      const double angle = atan2((y_body + Rm - Lm), x_body);
+      eta_phys = x_body / cos(angle) - Rm;
+      chi_arc = (angle - M_PI / 2 + th) / (2 * th * s_tot / s_Curve) + s_Straight / s_tot;
+    }
+    chi = 1 - 2 * chi_arc;
+    const double dmax = (chi_arc < s_Str_sh / s_tot_sh) ? c.dRs + (s_Str_sh - chi_arc * s_tot_sh) * slope : c.dRs;
+    eta = eta_phys / dmax;
+  } else if (c.mapping == HYMOR_MAP_CHANNEL) {
+    const double p = c.eta_refinement_power;
+    chi = (x * cos(c.channel_angle) + y * sin(c.channel_angle)) / c.Lx;
+    const double er = (-x * sin(c.channel_angle) + y * cos(c.channel_angle)) / c.Ly;
+    eta = er <= 0.5 ? pow(er / pow(2.0, p - 1), 1 / p) : 1 - pow((1 - er) / pow(2.0, p - 1), 1 / p);
+  } else {
+    chi = 1 - y / c.Lx;
+    const double dmax = c.dRs + (c.dRe - c.dRs) * (1 - chi);
+    eta = -x / dmax;
+  }
+}
+
+// Natural smoothing spline (Reinsch): factor the pentadiagonal system once and solve
+// for the x and y ordinates (single thread; the system is n-2 unknowns). Objective
+// Σ (y_i - f(x_i))² + λ ∫ f''², the one BSplineKit's fit(BSplineOrder(4), x, y, λ)
+// minimises (utils/Shock_fitting/LEAST_SQUARES_SHOCK_POINTS.jl:52-58).
+// Outputs: gx, gy (fitted values), cx, cy (second derivatives), all length n.
+__device__ void spline_fit2(int n, const double* xs, const double* yx, const double* yy, double lam,
+                            double* gx, double* gy, double* cx, double* cy, double* w0, double* w1,
+                            double* w2) {
+  for (int k = 0; k < n; ++k) { cx[k] = 0; cy[k] = 0; gx[k] = yx[k]; gy[k] = yy[k]; }
+  if (n < 3) return;
+  const int m = n - 2;
+  // bands of A = R + lam Q^T Q and its Cholesky factor, computed on the fly
+  double l1_prev = 0, l2_prev = 0, l2_prev2 = 0, l1_prev2 = 0;
+  (void)l1_prev2;
+  for (int jj = 0; jj < m; ++jj) {
+    const int j = jj + 1;
+    const double hm = xs[j] - xs[j - 1], h0 = xs[j + 1] - xs[j];
+    const double qm = 1.0 / hm, qp = 1.0 / h0, q0 = -qm - qp;
+    double d0 = (hm + h0) / 3 + lam * (qm * qm + q0 * q0 + qp * qp);
+    double d1 = 0, d2 = 0;
+    if (jj + 1 < m) {
+      const double h1 = xs[j + 2] - xs[j + 1];
+      const double qm1 = 1.0 / h0, qp1 = 1.0 / h1, q01 = -qm1 - qp1;
+      d1 = h0 / 6 + lam * (q0 * qm1 + qp * q01);
+    }
+    if (jj + 2 < m) d2 = lam * (qp * (1.0 / (xs[j + 2] - xs[j + 1])));
+    // Cholesky rows: l0 = sqrt(d0 - l1[j-1]^2 - l2[j-2]^2), l1 = (d1 - l2[j-1] l1[j-1]) / l0, l2 = d2 / l0
+    double a = d0 - l1_prev * l1_prev - l2_prev2 * l2_prev2;
+    const double l0 = sqrt(a);
+    const double il0 = 1.0 / l0;
+    const double l1 = (d1 - l2_prev * l1_prev) * il0;
+    const double l2 = d2 * il0;
+    w0[jj] = l0;
+    w1[jj] = l1;
+    w2[jj] = l2;
+    // forward substitution for both right-hand sides: rhs = Q^T y
+    const double rx = qm * yx[j - 1] + q0 * yx[j] + qp * yx[j + 1];
+    const double ry = qm * yy[j - 1] + q0 * yy[j] + qp * yy[j + 1];
+    double zx = rx, zy = ry;
+    if (jj >= 1) { zx -= w1[jj - 1] * cx[jj]; zy -= w1[jj - 1] * cy[jj]; }
+    if (jj >= 2) { zx -= w2[jj - 2] * cx[jj - 1]; zy -= w2[jj - 2] * cy[jj - 1]; }
+    cx[jj + 1] = zx * il0;  // z stored in place, shifted by one
+    cy[jj + 1] = zy * il0;
+    l2_prev2 = l2_prev;
+    l2_prev = l2;
+    l1_prev = l1;
+  }
+  // back substitution (gamma at indices 1..n-2), reading z from the same slots
+  for (int jj = m - 1; jj >= 0; --jj) {
+    double vx = cx[jj + 1], vy = cy[jj + 1];
+    if (jj + 1 < m) { vx -= w1[jj] * cx[jj + 2]; vy -= w1[jj] * cy[jj + 2]; }
+    if (jj + 2 < m) { vx -= w2[jj] * cx[jj + 3]; vy -= w2[jj] * cy[jj + 3]; }
+    const double il0 = 1.0 / w0[jj];
+    cx[jj + 1] = vx * il0;
+    cy[jj + 1] = vy * il0;
+  }
+  cx[0] = cx[n - 1] = 0;
+  cy[0] = cy[n - 1] = 0;
+}
+
+// g = y - lam Q gamma (one point per thread)
+__device__ double spline_g(int n, const double* xs, const double* ys, const double* gam, double lam, int r) {
+  double qg = 0;
+  if (r - 1 >= 1 && r - 1 <= n - 2) qg += (1.0 / (xs[r] - xs[r - 1])) * gam[r - 1];
+  if (r >= 1 && r <= n - 2) {
+    const double qm = 1.0 / (xs[r] - xs[r - 1]), qp = 1.0 / (xs[r + 1] - xs[r]);
+    qg += (-qm - qp) * gam[r];
+  }
+  if (r + 1 >= 1 && r + 1 <= n - 2) qg += (1.0 / (xs[r + 1] - xs[r])) * gam[r + 1];
+  return ys[r] - lam * qg;
+}
+
+__device__ int spline_interval(int n, const double* xs, double t) {
+  if (t <= xs[0]) return 0;
+  if (t >= xs[n - 1]) return n - 2;
+  int lo = 0, hi = n - 1;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (xs[mid] <= t) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+__device__ void spline_eval(int n, const double* xs, const double* g, const double* gam, double t,
+                            double& val, double& der) {
+  auto in_val = [&](int k, double tt) {
+    const double h = xs[k + 1] - xs[k], a = xs[k + 1] - tt, b = tt - xs[k];
+    return (a * g[k] + b * g[k + 1]) / h + ((a * a * a - h * h * a) * gam[k] + (b * b * b - h * h * b) * gam[k + 1]) / (6 * h);
+  };
+  auto in_der = [&](int k, double tt) {
+    const double h = xs[k + 1] - xs[k], a = xs[k + 1] - tt, b = tt - xs[k];
+    return (g[k + 1] - g[k]) / h + ((h * h - 3 * a * a) * gam[k] + (3 * b * b - h * h) * gam[k + 1]) / (6 * h);
+  };
+  if (n < 2) { val = g[0]; der = 0; return; }
+  if (t < xs[0]) { der = in_der(0, xs[0]); val = g[0] + der * (t - xs[0]); return; }
+  if (t > xs[n - 1]) { der = in_der(n - 2, xs[n - 1]); val = g[n - 1] + der * (t - xs[n - 1]); return; }
+  const int k = spline_interval(n, xs, t);
+  val = in_val(k, t);
+  der = in_der(k, t);
+}
+
+// Freestream state seen by shock point i (COMPUTE_UPSTREAM_CONDITIONS.jl:31-112).
+__device__ void upstream(const hymor_config& c, double t, double px, double py, bool first, double& p_inf,
+                         double& u_inf, double& v_inf, double& rho_inf) {
+  const double u_y = c.rho_v_0 / c.rho_0, u_x = c.rho_u_0 / c.rho_0;
+  const double pert = cos(2.0 * M_PI * c.dist_ky * (py - u_y * t)) * sin(2.0 * M_PI * c.dist_kx * (px - u_x * t));
+  const double rho = c.rho_0 + pert * c.dist_amp[0];
+  const double ru = c.rho_u_0 + pert * c.dist_amp[1];
+  double rv = c.rho_v_0 + pert * c.dist_amp[2];
+  const double rE = c.rho_E_0 + pert * c.dist_amp[3];
+  if (c.axisymmetric && first) rv = 0;
+  v_inf = rv / rho;
+  u_inf = ru / rho;
+  const double um = sqrt(v_inf * v_inf + u_inf * u_inf);
+  const double e_inf = (rE - rho * (um * um) * 0.5) / rho;
+  p_inf = e_inf * rho * (c.gamma - 1.0);
+  rho_inf = rho;
+}
+
+// Ghost-cell boundary condition of one edge at position k (0-based along the
+// ghosted edge), APPLY_BOUNDARY_CONDITIONS.jl:1-828.
+struct EdgeCtx {
+  int edge, bc, NI, NJ, nchi, neta;
+};
+
+__device__ __forceinline__ int at(const EdgeCtx& e, int depth, int k) {
+  if (e.edge == 0) return gidx(depth, k, e.nchi);
+  if (e.edge == 1) return gidx(e.NI - 1 - depth, k, e.nchi);
+  if (e.edge == 2) return gidx(k, depth, e.nchi);
+  return gidx(k, e.NJ - 1 - depth, e.nchi);
+}
+__device__ __forceinline__ int at_per(const EdgeCtx& e, int k) {
+  if (e.edge == 0) return gidx(e.NI - 2, k, e.nchi);
+  if (e.edge == 1) return gidx(1, k, e.nchi);
+  if (e.edge == 2) return gidx(k, e.NJ - 2, e.nchi);
+  return gidx(k, 1, e.nchi);
+}
+
+__device__ void edge_normal(const EdgeCtx& e, const DevMesh& m, int k, double& nx, double& ny) {
+  // k is the 0-based ghosted position (interior positions 1..len-2)
+  if (e.edge == 0) { const long f = (long)0 + (long)(k - 1) * (e.nchi + 1); nx = m.lr_xn[f]; ny = m.lr_yn[f]; }
+  else if (e.edge == 1) { const long f = (long)e.nchi + (long)(k - 1) * (e.nchi + 1); nx = m.lr_xn[f]; ny = m.lr_yn[f]; }
+  else if (e.edge == 2) { const long f = (long)(k - 1); nx = m.bt_xn[f]; ny = m.bt_yn[f]; }
+  else { const long f = (long)(k - 1) + (long)e.neta * e.nchi; nx = m.bt_xn[f]; ny = m.bt_yn[f]; }
+}
+
+// First pass of one edge: everything but the symmetry end copies.
+__device__ void edge_bc_point(const hymor_config& c, const EdgeCtx& e, const DevMesh& m, Cons q,
+                              double* P, double* Tt, const double* A, int k, int len) {
+  const int g = at(e, 0, k), a1 = at(e, 1, k), a2 = at(e, 2, k);
+  double* R = q.rho;
+  double* U = q.ru;
+  double* V = q.rv;
+  double* E = q.rE;
+  auto copy = [&](double* X) { X[g] = X[a1]; };
+  auto neg = [&](double* X) { X[g] = -X[a1]; };
+  auto extrap = [&](double* X) { X[g] = 2 * X[a1] - X[a2]; };
+  const bool inner = k >= 1 && k <= len - 2;
+  switch (e.bc) {
+    case HYMOR_BC_INFLOW_SUBSONIC:
+      R[g] = c.rho_0; U[g] = c.rho_u_0; V[g] = c.rho_v_0; extrap(E); extrap(P);
+      break;
+    case HYMOR_BC_INFLOW_SUPERSONIC:
+      R[g] = c.rho_0; U[g] = c.rho_u_0; V[g] = c.rho_v_0; E[g] = c.rho_E_0; P[g] = c.p_0;
+      break;
+    case HYMOR_BC_NO_SLIP_ADIABATIC:
+      copy(R); neg(U); neg(V); extrap(E); extrap(P); copy(Tt);
+      break;
+    case HYMOR_BC_NO_SLIP_ISOTHERMAL: {
+      copy(R); neg(U); neg(V); extrap(E); extrap(P);
+      const double Tw = (e.edge <= 1) ? c.Tw_chi0 : (e.edge == 2 ? c.Tw_eta0 : c.Tw_eta1);
+      const double T_w = Tw * c.cv / c.energy_factor;
+      Tt[g] = 2 * T_w - Tt[a1];
+      break;
+    }
+    case HYMOR_BC_OUTFLOW_SUBSONIC:
+      extrap(R); extrap(E); extrap(U); extrap(V); copy(P);
+      if (e.edge != 1) copy(Tt);
+      break;
+    case HYMOR_BC_OUTFLOW_SUPERSONIC:
+      extrap(R); extrap(E); extrap(U); extrap(V); extrap(P); copy(Tt);
+      break;
+    case HYMOR_BC_OUTFLOW_SUPERSONIC_1ST:
+      copy(U); copy(V); copy(R); copy(E); copy(P); copy(Tt);
+      break;
+    case HYMOR_BC_OUTFLOW_NRCBC: {
+      extrap(R); extrap(U); extrap(V); extrap(E); extrap(P); copy(Tt);
+      if (inner) {
+        double nx, ny;
+        edge_normal(e, m, k, nx, ny);
+        const double a = A[a1];
+        const double rho_int = R[a1];
+        double ung = (U[g] * nx + V[g] * ny) / R[g];
+        double uni = (U[a1] * nx + V[a1] * ny) / rho_int;
+        if (e.edge == 0 || e.edge == 2) { ung = -ung; uni = -uni; }
+        if (ung < a) {
+          const double p_lodi = P[a1] + rho_int * a * (ung - uni);
+          P[g] = p_lodi;
+          const double rho_e = P[g] / (c.gamma - 1);
+          E[g] = rho_e + 0.5 * (U[g] * U[g] + V[g] * V[g]) / R[g];
+        }
+      }
+      break;
+    }
+    case HYMOR_BC_PERIODIC: {
+      const int s = at_per(e, k);
+      U[g] = U[s]; V[g] = V[s]; R[g] = R[s]; E[g] = E[s]; P[g] = P[s]; Tt[g] = Tt[s];
+      break;
+    }
+    case HYMOR_BC_SYMMETRY: {
+      copy(R); copy(P);
+      if (inner) {
+        double nx, ny;
+        edge_normal(e, m, k, nx, ny);
+        const double fv = U[a1] * nx + V[a1] * ny;
+        U[g] = U[a1] - 2 * fv * nx;
+        V[g] = V[a1] - 2 * fv * ny;
+      }
+      copy(E); copy(Tt);
+      break;
+    }
+    default:
+      break;
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_shock_bc(ShockArgs A) {
+  const hymor_config& c = A.cfg;
+  const int nchi = c.nchi, neta = c.neta, NI = nchi + 2, NJ = neta + 2;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const double dt = A.scal[kDt];
+  const double t = A.scal[kT];
+  Cons q = A.tgt;
+
+  // (0) sound speed of the edge-adjacent lines, before the shock update
+  //     (UPDATE_SOUND_SPEED.jl:31-36 precedes UPDATE_SHOCK_BC in PDE.jl:20-26)
+  if (A.compute_a) {
+    const int bcs[4] = {c.bc_chi0, c.bc_chi1, c.bc_eta0, c.bc_eta1};
+    for (int ed = 0; ed < 4; ++ed) {
+      if (bcs[ed] != HYMOR_BC_OUTFLOW_NRCBC) continue;
+      const int len = ed <= 1 ? NJ : NI;
+      EdgeCtx e{ed, bcs[ed], NI, NJ, nchi, neta};
+      for (int k = tid; k < len; k += nt) {
+        const int a1 = at(e, 1, k);
+        A.a_bc[a1] = sqrt(c.gamma * A.p[a1] / q.rho[a1]);
+      }
+    }
+  }
+
+  if (c.shock_enabled && A.do_shock) {
+    extern __shared__ double sh[];
+    double* xs = sh;              // knots (pts_chi)
+    double* vx = xs + nchi;       // ordinates x
+    double* vy = vx + nchi;       // ordinates y
+    double* gamx = vy + nchi;
+    double* gamy = gamx + nchi;
+    double* gxs = gamy + nchi;    // fitted values
+    double* gys = gxs + nchi;
+    double* w0 = A.spl;           // Cholesky bands (global workspace)
+    double* w1 = w0 + nchi;
+    double* w2 = w1 + nchi;
+    if (A.copy_pts) {
+      for (int i = tid; i < nchi; i += nt) {
+        A.pts.x[i] = A.pS.x[i]; A.pts.y[i] = A.pS.y[i];
+        A.pts.chi[i] = A.pS.chi[i]; A.pts.eta[i] = A.pS.eta[i];
+      }
+      __syncthreads();
+    }
+    for (int i = tid; i < nchi; i += nt) { xs[i] = A.pts.chi[i]; vx[i] = A.pts.x[i]; vy[i] = A.pts.y[i]; }
+    __syncthreads();
+    const double ps = c.spline_param;
+    const double lam = (1 - ps) / ps;
+    if (tid == 0) spline_fit2(nchi, xs, vx, vy, lam, gxs, gys, gamx, gamy, w0, w1, w2);
+    __syncthreads();
+    // fitted values g = y - lam Q gamma
+    for (int i = tid; i < nchi; i += nt) {
+      gxs[i] = spline_g(nchi, xs, vx, gamx, lam, i);
+      gys[i] = spline_g(nchi, xs, vy, gamy, lam, i);
+    }
+    __syncthreads();
+    // (1) resample at mesh chi, element space, beta (LEAST_SQUARES_SHOCK_POINTS.jl:60-70,
+    //     COMPUTE_BETA.jl:37-50)
+    for (int i = tid; i < nchi; i += nt) {
+      const double tc = A.m.chi1[i];
+      double xv, xd, yv, yd;
+      spline_eval(nchi, xs, gxs, gamx, tc, xv, xd);
+      spline_eval(nchi, xs, gys, gamy, tc, yv, yd);
+      double ch, et;
+      element_space(c, xv, yv, ch, et);
+      A.pts.x[i] = xv; A.pts.y[i] = yv; A.pts.chi[i] = ch; A.pts.eta[i] = et;
+      double p_inf, u_inf, v_inf, rho_inf;
+      upstream(c, t, xv, yv, i == 0, p_inf, u_inf, v_inf, rho_inf);
+      const double cross = xd * v_inf - yd * u_inf;
+      const double dot = xd * u_inf + yd * v_inf;
+      double b = atan2(fabs(cross), fabs(dot));
+      if (i == 0 && c.bc_chi0 == HYMOR_BC_SYMMETRY) b = M_PI / 2;  // UPDATE_SHOCK_BC.jl:31-34
+      A.beta[i] = b;
+    }
+    __syncthreads();
+    // (2) Rankine-Hugoniot jump at the shock, shocked-cell and auxiliary-cell values
+    //     (UPDATE_SHOCK_JUMP_PROPERTIES.jl:324-522, EXTRAPOLATE_CELLS_SHOCK.jl:39-176)
+    for (int i = tid; i < nchi; i += nt) {
+      const int sc = A.cell_idx[i];
+      if (sc < 2 || sc > neta - 1) {
+        atomicOr(&A.err[kErrFlags], kBitShockRange);
+        continue;
+      }
+      const int I = i + 1;  // ghosted column
+      const double x0 = A.m.x_ext[gidx(I, sc, nchi)], y0 = A.m.y_ext[gidx(I, sc, nchi)];
+      const double x1 = A.m.x_ext[gidx(I, sc - 1, nchi)], y1 = A.m.y_ext[gidx(I, sc - 1, nchi)];
+      const double x2 = A.m.x_ext[gidx(I, sc - 2, nchi)], y2 = A.m.y_ext[gidx(I, sc - 2, nchi)];
+      const double xsh = A.pts.x[i], ysh = A.pts.y[i];
+      const double dist01 = sqrt((x0 - x1) * (x0 - x1) + (y0 - y1) * (y0 - y1));
+      const double dist12 = sqrt((x1 - x2) * (x1 - x2) + (y1 - y2) * (y1 - y2));
+      const double dist1s = ((xsh - x1) * (x1 - x2) + (ysh - y1) * (y1 - y2)) / dist12;
+      const double dist0s = ((xsh - x0) * (x0 - x1) + (ysh - y0) * (y0 - y1)) / dist01;
+      const int g0 = gidx(I, sc, nchi), g1 = gidx(I, sc - 1, nchi), g2 = gidx(I, sc - 2, nchi);
+      const double p_1 = A.p[g1];
+      double p_2 = A.p[g2];
+      if (sc - 2 == 0 && c.bc_eta0 == HYMOR_BC_NO_SLIP_ISOTHERMAL)
+        p_2 = 2 * A.p[gidx(I, 1, nchi)] - A.p[gidx(I, 2, nchi)];  // UPDATE_THERMODYNAMIC_PROPERTIES.jl:28-31
+      const double slope_p = (p_1 - p_2) / dist12;
+      const double slope_rho = (q.rho[g1] - q.rho[g2]) / dist12;
+      const double slope_ru = (q.ru[g1] - q.ru[g2]) / dist12;
+      const double slope_rv = (q.rv[g1] - q.rv[g2]) / dist12;
+      const double slope_rE = (q.rE[g1] - q.rE[g2]) / dist12;
+      const double p_s = slope_p * dist1s + p_1;
+      double p_inf, u_inf, v_inf, rho_inf;
+      upstream(c, t, xsh, ysh, i == 0, p_inf, u_inf, v_inf, rho_inf);
+      const double yr = p_s / p_inf;
+      if (yr < 1) atomicAdd(&A.err[kRhWarn], 1u);
+      const double gs = c.gamma, gi = c.gamma;
+      const double Acoef = (gs + 1) / (gs - 1), Bcoef = (gi + 1) / (gi - 1);
+      const double rho_s = rho_inf * (yr * Acoef + 1) / (yr + Bcoef);
+      const double e_s = p_s / ((gs - 1) * rho_s);
+      const double b = A.beta[i];
+      const double ang_inf = b - atan2(v_inf, u_inf);
+      const double vmag = sqrt(u_inf * u_inf + v_inf * v_inf);
+      const double vn_inf = sin(ang_inf) * vmag;
+      const double temp1 = 2 * yr / (gs - 1) - 2 / (gi - 1);
+      const double temp2 = yr * Acoef + 1;
+      const double temp3 = p_inf * (yr - 1) / rho_inf;
+      const double rel = -vn_inf + sqrt(temp3 * temp2 / temp1);
+      A.rel[i] = rel;
+      const double vt_s = cos(ang_inf) * vmag;
+      const double vn_s = -rel + rho_inf / rho_s * (rel + vn_inf);
+      const double sb = sin(b), cb = cos(b);
+      if (!c.shock_eulerian) {
+        A.speed_x[i] = -rel * sb;
+        A.speed_y[i] = rel * cb;
+      } else {
+        const double sx = -rel * sb, sy = rel * cb;
+        A.speed_x[i] = sx - sy * tan(M_PI / 2 - b);
+        A.speed_y[i] = 0.0;
+      }
+      const double ru_s = rho_s * (vn_s * sb + vt_s * cb);
+      const double rv_s = rho_s * (-vn_s * cb + vt_s * sb);
+      const double rE_s = e_s * rho_s + (ru_s * ru_s + rv_s * rv_s) / (2 * rho_s);
+      q.rho[g0] = -slope_rho * dist0s + rho_s;
+      q.ru[g0] = -slope_ru * dist0s + ru_s;
+      q.rv[g0] = -slope_rv * dist0s + rv_s;
+      q.rE[g0] = -slope_rE * dist0s + rE_s;
+      A.p[g0] = -slope_p * dist0s + p_s;
+      // EXTRAPOLATE_CELLS_SHOCK: idx_1 = sc+1, idx_2 = sc+2 (0-based ghosted rows)
+      const int i1 = gidx(I, sc + 1, nchi), i2 = gidx(I, sc + 2, nchi);
+      const int im1 = g1, im2 = g2;
+      double* arr[5] = {q.rho, q.ru, q.rv, q.rE, A.p};
+      if (c.shock_interp == 1) {
+        for (int v = 0; v < 5; ++v) { arr[v][i1] = arr[v][g0]; arr[v][i2] = arr[v][g0]; }
+      } else if (c.shock_interp == 2) {
+        for (int v = 0; v < 5; ++v) arr[v][i1] = 2 * arr[v][g0] - arr[v][im1];
+        for (int v = 0; v < 4; ++v) arr[v][i2] = 2 * arr[v][i1] - arr[v][g0];
+      } else {
+        const double pm2 = (sc - 2 == 0 && c.bc_eta0 == HYMOR_BC_NO_SLIP_ISOTHERMAL) ? p_2 : A.p[im2];
+        for (int v = 0; v < 4; ++v) arr[v][i1] = 3 * arr[v][g0] - 3 * arr[v][im1] + arr[v][im2];
+        A.p[i1] = 3 * A.p[g0] - 3 * A.p[im1] + pm2;
+        for (int v = 0; v < 4; ++v) arr[v][i2] = 3 * arr[v][i1] - 3 * arr[v][g0] + arr[v][im1];
+      }
+    }
+    __syncthreads();
+    // (3) MOVE_SHOCK (MOVE_SHOCK.jl:29-49) on S (cS) and on the stage points (cY)
+    if (A.move) {
+      const double wS = A.cS * dt * c.relaxation, wY = A.cY * dt * c.relaxation;
+      for (int i = tid; i < nchi; i += nt) {
+        A.pS.x[i] = A.pS.x[i] + A.speed_x[i] * wS;
+        A.pS.y[i] = A.pS.y[i] + A.speed_y[i] * wS;
+        if (!A.on_S) {
+          A.pts.x[i] = A.pts.x[i] + A.speed_x[i] * wY;
+          A.pts.y[i] = A.pts.y[i] + A.speed_y[i] * wY;
+        }
+      }
+      __syncthreads();
+      if (tid == 0 && c.bc_chi0 == HYMOR_BC_SYMMETRY && nchi >= 2) {
+        A.pS.x[0] = A.pS.x[1];
+        if (!A.on_S) A.pts.x[0] = A.pts.x[1];
+      }
+    }
+  }
+  __syncthreads();
+
+  // (4) boundary conditions, edges in the reference order chi0, chi1, eta0, eta1
+  const int bcs[4] = {c.bc_chi0, c.bc_chi1, c.bc_eta0, c.bc_eta1};
+  for (int ed = 0; ed < 4 && A.do_bc; ++ed) {
+    const int len = ed <= 1 ? NJ : NI;
+    EdgeCtx e{ed, bcs[ed], NI, NJ, nchi, neta};
+    if (e.bc != HYMOR_BC_SHOCK) {
+      for (int k = tid; k < len; k += nt) edge_bc_point(c, e, A.m, q, A.p, A.T, A.a_bc, k, len);
+      __syncthreads();
+      if (e.bc == HYMOR_BC_SYMMETRY && tid == 0) {
+        // ends of the ghost line copy their neighbours along the line
+        q.ru[at(e, 0, 0)] = q.ru[at(e, 0, 1)];
+        q.rv[at(e, 0, 0)] = q.rv[at(e, 0, 1)];
+        q.ru[at(e, 0, len - 1)] = q.ru[at(e, 0, len - 2)];
+        q.rv[at(e, 0, len - 1)] = q.rv[at(e, 0, len - 2)];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Residual: FLUX_MASS/MOMENTUM/TOTAL_ENERGY + VISCOUS_FLUX (and the *_3D forms),
+// fused and face-centric, one 31x8-cell tile per CTA.
+struct FluxArgs {
+  const double *rho, *ru, *rv, *rE, *p, *T;
+  double *o0, *o1, *o2, *o3;
+  const int* cell_idx;
+  DevMesh m;
+  double mre, kq;          // mu/Re and k gamma/(Re Pr) for constant transport
+  double inv_Re, gk;       // 1/Re and gamma/(Re Pr) for Sutherland faces
+  double suthS, Tinf_inv;
+  int nchi, neta;
+  int mask;                // shock fitting with feedback: zero flux at j >= sc
+  int shock;
+};
+
+template <bool AXI, bool SUTH>
+__global__ void __launch_bounds__(kFluxThreads, 2) k_flux(FluxArgs a) {
+  extern __shared__ double sm[];
+  double* s_r = sm;
+  double* s_u = s_r + NH;   // u = rho_u / rho
+  double* s_v = s_u + NH;
+  double* s_ru = s_v + NH;
+  double* s_rv = s_ru + NH;
+  double* s_rE = s_rv + NH;
+  double* s_p = s_rE + NH;
+  double* s_T = s_p + NH;
+  double* s_mu = s_T + NH;                   // SUTH only
+  double* s_uc = s_mu + (SUTH ? NH : 0);
+  double* s_vc = s_uc + NCOR;
+  double* s_Tc = s_vc + NCOR;
+  double* f_lr = s_Tc + NCOR;                // 4 x NLRF
+  double* f_bt = f_lr + 4 * NLRF;            // 4 x NBTF
+  double* t_lr = f_bt + 4 * NBTF;            // AXI hoop stress on faces
+  double* t_bt = t_lr + (AXI ? NLRF : 0);
+
+  const int nchi = a.nchi, neta = a.neta;
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;  // first interior cell (0-based)
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+  // whole tile at or above the shocked rows: flux is zero (NON_LINEAR_DYNAMICS mask)
+  if (a.mask) {
+    int sc = 0;
+    if (lane < TX && i0 + lane < nchi) sc = a.cell_idx[i0 + lane];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sc = max(sc, __shfl_xor_sync(0xffffffffu, sc, o));
+    if (j0 + 1 >= sc) {
+      const int ci = i0 + lane, cj = j0 + warp;
+      if (lane < TX && ci < nchi && cj < neta) {
+        const long c = (long)ci + (long)cj * nchi;
+        a.o0[c] = 0; a.o1[c] = 0; a.o2[c] = 0; a.o3[c] = 0;
+      }
+      return;
+    }
+  }
+
+  // (1) halo cells: ghosted (i0 + hx, j0 + hy)
+  for (int h = tid; h < NH; h += kFluxThreads) {
+    const int hx = h % HX, hy = h / HX;
+    const int gi = i0 + hx, gj = j0 + hy;
+    if (gi <= nchi + 1 && gj <= neta + 1) {
+      const long g = (long)gi + (long)gj * (nchi + 2);
+      const double r = a.rho[g], ru = a.ru[g], rv = a.rv[g];
+      const double ir = frcp(r);
+      s_r[h] = r; s_ru[h] = ru; s_rv[h] = rv; s_rE[h] = a.rE[g];
+      s_u[h] = ru * ir; s_v[h] = rv * ir;
+      s_p[h] = a.p[g];
+      const double T = a.T[g];
+      s_T[h] = T;
+      if (SUTH) {
+        const double Ts = T * a.Tinf_inv;
+        s_mu[h] = Ts * sqrt(Ts) * (1 + a.suthS) * frcp(Ts + a.suthS);
+      }
+    }
+  }
+  __syncthreads();
+  // (2) corner averages (VISCOUS_FLUX.jl:67-70, 184-185)
+  for (int cidx = tid; cidx < NCOR; cidx += kFluxThreads) {
+    const int cx = cidx % CX, cy = cidx / CX;
+    if (i0 + cx <= nchi && j0 + cy <= neta) {
+      const int h00 = cx + cy * HX, h10 = h00 + 1, h01 = h00 + HX, h11 = h01 + 1;
+      s_uc[cidx] = (s_u[h00] + s_u[h10] + s_u[h01] + s_u[h11]) * 0.25;
+      s_vc[cidx] = (s_v[h00] + s_v[h10] + s_v[h01] + s_v[h11]) * 0.25;
+      s_Tc[cidx] = (s_T[h00] + s_T[h10] + s_T[h01] + s_T[h11]) * 0.25;
+    }
+  }
+  __syncthreads();
+  const long NLR = (long)(nchi + 1) * neta, NBT = (long)nchi * (neta + 1);
+  // (3a) lr faces: warp = tile row fy, lane = fx (32 faces per row)
+  {
+    const int fx = lane, fy = warp;
+    const int gi = i0 + fx, gj = j0 + fy;  // face (gi, gj) 0-based: between ghosted (gi, gj+1), (gi+1, gj+1)
+    if (gi <= nchi && gj < neta) {
+      const long f = (long)gi + (long)gj * (nchi + 1);
+      const double nx = a.m.lrg[f], ny = a.m.lrg[NLR + f], Af = a.m.lrg[2 * NLR + f];
+      const double g1 = a.m.lrg[3 * NLR + f], g2 = a.m.lrg[4 * NLR + f], il = a.m.lrg[5 * NLR + f];
+      const int L = fx + (fy + 1) * HX, R = L + 1;
+      const int clo = fx + fy * CX, chi_ = clo + CX;
+      const double Sr = s_r[L] + s_r[R], Su = s_ru[L] + s_ru[R], Sv = s_rv[L] + s_rv[R];
+      const double SE = s_rE[L] + s_rE[R], Sp = s_p[L] + s_p[R];
+      const double ir = frcp(Sr);
+      const double m2 = fma(Su, nx, Sv * ny);
+      const double Vn = m2 * ir;
+      // viscous (VISCOUS_FLUX.jl:98-133)
+      const double dUc = s_uc[chi_] - s_uc[clo], dVc = s_vc[chi_] - s_vc[clo], dTc = s_Tc[chi_] - s_Tc[clo];
+      const double du_dn = fma(g1, s_u[R] - s_u[L], g2 * dUc);
+      const double dv_dn = fma(g1, s_v[R] - s_v[L], g2 * dVc);
+      const double dT_dn = fma(g1, s_T[R] - s_T[L], g2 * dTc);
+      const double du_dt = dUc * il, dv_dt = dVc * il;
+      const double dun_dn = fma(-du_dn, nx, -dv_dn * ny);
+      const double dut_dn = fma(du_dn, ny, -dv_dn * nx);
+      const double dun_dt = fma(-du_dt, nx, -dv_dt * ny);
+      const double dut_dt = fma(du_dt, ny, -dv_dt * nx);
+      double div = dut_dt + dun_dn;
+      double mre = a.mre, kq = a.kq;
+      if (SUTH) {
+        const double mu_f = (s_mu[R] + s_mu[L]) * 0.5;
+        mre = mu_f * a.inv_Re;
+        kq = mu_f * a.gk;
+      }
+      double uf = 0, rx = 0;
+      if (AXI) {
+        rx = a.m.rx_lr[f];
+        uf = (s_u[R] + s_u[L]) * 0.5;
+        div = fma(uf, rx, div);
+      }
+      const double tau11 = mre * fma(-2.0 / 3.0, div, 2 * dun_dn);
+      const double tau12 = mre * (dun_dt + dut_dn);
+      const double tx = fma(tau12, ny, -tau11 * nx);
+      const double ty = -fma(tau11, ny, tau12 * nx);
+      const double w = fma(Su * ir, tx, (Sv * ir) * ty);
+      const double qn = kq * dT_dn;
+      const double Ah = 0.5 * Af;
+      const int o = fx + fy * (TX + 1);
+      f_lr[o] = m2 * Ah;
+      f_lr[NLRF + o] = fma(fma(Su, Vn, Sp * nx), Ah, tx * Af);
+      f_lr[2 * NLRF + o] = fma(fma(Sv, Vn, Sp * ny), Ah, ty * Af);
+      f_lr[3 * NLRF + o] = fma((SE + Sp) * Vn, Ah, (w + qn) * Af);
+      if (AXI) t_lr[o] = mre * fma(-2.0 / 3.0, div, 2 * uf * rx);
+    }
+  }
+  // (3b) bt faces: TX x (TY + 1)
+  for (int b = tid; b < (TX + 1) * (TY + 1); b += kFluxThreads) {
+    const int fx = b & 31, fy = b >> 5;
+    if (fx >= TX) continue;
+    const int gi = i0 + fx, gj = j0 + fy;  // face (gi, gj): between ghosted (gi+1, gj), (gi+1, gj+1)
+    if (gi < nchi && gj <= neta) {
+      const long f = (long)gi + (long)gj * nchi;
+      const double nx = a.m.btg[f], ny = a.m.btg[NBT + f], Af = a.m.btg[2 * NBT + f];
+      const double h1 = a.m.btg[3 * NBT + f], h2 = a.m.btg[4 * NBT + f], il = a.m.btg[5 * NBT + f];
+      const int B = (fx + 1) + fy * HX, Tt = B + HX;
+      const int clo = fx + fy * CX, chi_ = clo + 1;
+      const double Sr = s_r[B] + s_r[Tt], Su = s_ru[B] + s_ru[Tt], Sv = s_rv[B] + s_rv[Tt];
+      const double SE = s_rE[B] + s_rE[Tt], Sp = s_p[B] + s_p[Tt];
+      const double ir = frcp(Sr);
+      const double m2 = fma(Su, nx, Sv * ny);
+      const double Vn = m2 * ir;
+      const double dUc = s_uc[chi_] - s_uc[clo], dVc = s_vc[chi_] - s_vc[clo], dTc = s_Tc[chi_] - s_Tc[clo];
+      const double du_dn = fma(h1, s_u[Tt] - s_u[B], h2 * dUc);
+      const double dv_dn = fma(h1, s_v[Tt] - s_v[B], h2 * dVc);
+      const double dT_dn = fma(h1, s_T[Tt] - s_T[B], h2 * dTc);
+      const double du_dt = -dUc * il, dv_dt = -dVc * il;
+      const double dut_dt = fma(du_dt, ny, -dv_dt * nx);
+      const double dun_dt = fma(du_dt, nx, dv_dt * ny);
+      const double dut_dn = fma(du_dn, ny, -dv_dn * nx);
+      const double dun_dn = fma(du_dn, nx, dv_dn * ny);
+      double div = dut_dt + dun_dn;
+      double mre = a.mre, kq = a.kq;
+      if (SUTH) {
+        const double mu_f = (s_mu[Tt] + s_mu[B]) * 0.5;
+        mre = mu_f * a.inv_Re;
+        kq = mu_f * a.gk;
+      }
+      double uf = 0, rx = 0;
+      if (AXI) {
+        rx = a.m.rx_bt[f];
+        uf = (s_u[Tt] + s_u[B]) * 0.5;
+        div = fma(uf, rx, div);
+      }
+      const double tau22 = mre * fma(-2.0 / 3.0, div, 2 * dun_dn);
+      const double tau21 = mre * (dut_dn + dun_dt);
+      const double tx = fma(tau22, nx, tau21 * ny);
+      const double ty = fma(tau22, ny, -tau21 * nx);
+      const double w = fma(Su * ir, tx, (Sv * ir) * ty);
+      const double qn = kq * dT_dn;
+      const double Ah = 0.5 * Af;
+      const int o = fx + fy * TX;
+      f_bt[o] = m2 * Ah;
+      f_bt[NBTF + o] = fma(fma(Su, Vn, Sp * nx), Ah, -tx * Af);
+      f_bt[2 * NBTF + o] = fma(fma(Sv, Vn, Sp * ny), Ah, -ty * Af);
+      f_bt[3 * NBTF + o] = fma((SE + Sp) * Vn, Ah, -(w + qn) * Af);
+      if (AXI) t_bt[o] = mre * fma(-2.0 / 3.0, div, 2 * uf * rx);
+    }
+  }
+  __syncthreads();
+  // (4) cells: warp = tile row, lane = column
+  {
+    const int cx = lane, cy = warp;
+    const int ci = i0 + cx, cj = j0 + cy;
+    if (cx < TX && ci < nchi && cj < neta) {
+      const long c = (long)ci + (long)cj * nchi;
+      double r0 = 0, r1 = 0, r2 = 0, r3 = 0;
+      const bool active = !a.mask || (cj + 1 < a.cell_idx[ci]);
+      if (active) {
+        const int w = cx + cy * (TX + 1), e = w + 1;
+        const int s = cx + cy * TX, n = s + TX;
+        const double rv = a.m.rvol[c];
+        r0 = (f_lr[w] - f_lr[e] + f_bt[s] - f_bt[n]) * rv;
+        r1 = (f_lr[NLRF + w] - f_lr[NLRF + e] + f_bt[NBTF + s] - f_bt[NBTF + n]) * rv;
+        double v2 = f_lr[2 * NLRF + w] - f_lr[2 * NLRF + e] + f_bt[2 * NBTF + s] - f_bt[2 * NBTF + n];
+        if (AXI) {
+          // FLUX_MOMENTUM_3D.jl:120-122: front/back pressure with sign(y) of the cell centre
+          const double pc = s_p[(cx + 1) + (cy + 1) * HX];
+          const double ycell = a.m.y_ext[(long)(ci + 1) + (long)(cj + 1) * (nchi + 2)];
+          v2 += (pc * a.m.fb_yn_front - pc * a.m.fb_yn_back) * a.m.fb_area[c] * jsign(ycell);
+          // VISCOUS_FLUX_3D.jl:154-177: hoop stress, radius = x of the cell centre
+          const double tth = (t_lr[w] + t_lr[e] + t_bt[s] + t_bt[n]) * 0.25;
+          const double xcell = a.m.x_ext[(long)(ci + 1) + (long)(cj + 1) * (nchi + 2)];
+          r1 -= tth * frcp(xcell);
+        }
+        r2 = v2 * rv;
+        r3 = (f_lr[3 * NLRF + w] - f_lr[3 * NLRF + e] + f_bt[3 * NBTF + s] - f_bt[3 * NBTF + n]) * rv;
+      }
+      a.o0[c] = r0; a.o1[c] = r1; a.o2[c] = r2; a.o3[c] = r3;
+    }
+  }
+}
+
+template <bool AXI, bool SUTH>
+size_t flux_smem() {
+  return sizeof(double) * (8 * NH + (SUTH ? NH : 0) + 3 * NCOR + 4 * NLRF + 4 * NBTF + (AXI ? NLRF + NBTF : 0));
+}
+
+// ---------------------------------------------------------------------------
+// UPDATE_FLOW_CELLS on S: DETECT_CELLS_SHOCKED (DETECT_CELLS_SHOCKED.jl:50-65),
+// UPDATE_FIELD_UPSTREAM (UPDATE_FIELD_UPSTREAM.jl:93-109), EXTRAPOLATE_CELLS_SHOCK.
+__device__ void fill_column_upstream(const hymor_config& c, const DevMesh& m, Cons q, int i, int sc, double t) {
+  const int nchi = c.nchi, NJ = c.neta + 2;
+  const double u_y = c.rho_v_0 / c.rho_0, u_x = c.rho_u_0 / c.rho_0;
+  const bool dist = c.dist_amp[0] != 0 || c.dist_amp[1] != 0 || c.dist_amp[2] != 0 || c.dist_amp[3] != 0;
+  for (int jg = sc + 2; jg < NJ; ++jg) {  // 0-based ghosted rows >= sc + 2
+    const long k = gidx(i + 1, jg, nchi);
+    double pert = 0;
+    if (dist)
+      pert = cos(2.0 * M_PI * c.dist_ky * (m.y_ext[k] - u_y * t)) * sin(2.0 * M_PI * c.dist_kx * (m.x_ext[k] - u_x * t));
+    q.rho[k] = c.rho_0 + pert * c.dist_amp[0];
+    q.ru[k] = c.rho_u_0 + pert * c.dist_amp[1];
+    q.rv[k] = c.rho_v_0 + pert * c.dist_amp[2];
+    q.rE[k] = c.rho_E_0 + pert * c.dist_amp[3];
+  }
+}
+
+__device__ void extrapolate_column(const hymor_config& c, Cons q, int i, int sc) {
+  const int nchi = c.nchi, I = i + 1;
+  const int g0 = gidx(I, sc, nchi), i1 = gidx(I, sc + 1, nchi), i2 = gidx(I, sc + 2, nchi);
+  const int im1 = gidx(I, sc - 1, nchi), im2 = gidx(I, sc - 2, nchi);
+  double* arr[4] = {q.rho, q.ru, q.rv, q.rE};
+  if (c.shock_interp == 1) {
+    for (int v = 0; v < 4; ++v) { arr[v][i1] = arr[v][g0]; arr[v][i2] = arr[v][g0]; }
+  } else if (c.shock_interp == 2) {
+    for (int v = 0; v < 4; ++v) arr[v][i1] = 2 * arr[v][g0] - arr[v][im1];
+    for (int v = 0; v < 4; ++v) arr[v][i2] = 2 * arr[v][i1] - arr[v][g0];
+  } else {
+    for (int v = 0; v < 4; ++v) arr[v][i1] = 3 * arr[v][g0] - 3 * arr[v][im1] + arr[v][im2];
+    for (int v = 0; v < 4; ++v) arr[v][i2] = 3 * arr[v][i1] - 3 * arr[v][g0] + arr[v][im1];
+  }
+}
+
+struct FlowArgs {
+  hymor_config cfg;
+  DevMesh m;
+  Cons S;
+  ShockPts pS;
+  int* cell_idx;
+  const double* scal;
+  unsigned* err;
+};
+
+__global__ void k_flow_cells(FlowArgs A) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const hymor_config& c = A.cfg;
+  if (i >= c.nchi) return;
+  const int nchi = c.nchi, neta = c.neta;
+  const double px = A.pS.x[i], py = A.pS.y[i];
+  double best = INFINITY;
+  int bj = 1;
+  for (int j = 1; j <= neta; ++j) {
+    const long k = gidx(i + 1, j, nchi);
+    const double dx = px - A.m.x_ext[k], dy = py - A.m.y_ext[k];
+    const double d = dx * dx + dy * dy;
+    if (d < best) { best = d; bj = j; }
+  }
+  A.cell_idx[i] = bj;
+  if (bj < 2 || bj > neta - 1) {
+    atomicOr(&A.err[kErrFlags], kBitShockRange);
+    return;
+  }
+  fill_column_upstream(c, A.m, A.S, i, bj, A.scal[kT]);
+  extrapolate_column(c, A.S, i, bj);
+}
+
+// Sound speed of S, max |a| over every ghosted cell (CFL_TIMESTEP.jl:80).
+struct SoundArgs {
+  Cons S;
+  double* aS;
+  double* scal;
+  double gamma;
+  int nchi, neta, recompute, isothermal_eta0;
+};
+
+__global__ void __launch_bounds__(256) k_sound_cmax(SoundArgs A) {
+  const int NI = A.nchi + 2, NJ = A.neta + 2;
+  const long G = (long)NI * NJ;
+  double mx = 0;
+  const double gm1 = A.gamma - 1;
+  auto pres = [&](long k) {
+    const double r = A.S.rho[k], u = A.S.ru[k], v = A.S.rv[k], e = A.S.rE[k];
+    const double eint = e - (u * u + v * v) / r / 2;
+    return eint * gm1;
+  };
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < G; k += (long)gridDim.x * blockDim.x) {
+    double a;
+    if (A.recompute) {
+      const int i = (int)(k % NI), j = (int)(k / NI);
+      double p;
+      if (j == 0 && A.isothermal_eta0)
+        p = 2 * pres(gidx(i, 1, A.nchi)) - pres(gidx(i, 2, A.nchi));
+      else
+        p = pres(k);
+      a = sqrt(A.gamma * p / A.S.rho[k]);
+      A.aS[k] = a;
+    } else {
+      a = A.aS[k];
+    }
+    mx = fmax(mx, fabs(a));
+  }
+  mx = warp_max(mx);
+  __shared__ double red[32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    v = warp_max(v);
+    if (threadIdx.x == 0) atomic_max_nonneg(&A.scal[kCmax], v);
+  }
+}
+
+// CFL maxima (CFL_TIMESTEP.jl:80-130) and dt.
+struct CflArgs {
+  Cons S;
+  const double* SF0;
+  const double* SF1;
+  const double* SF2;
+  const double* SF3;
+  DevMesh m;
+  const int* cell_idx;
+  double* scal;
+  double gamma, Pr, Re;
+  int nchi, neta, shock;
+};
+
+__global__ void __launch_bounds__(256) k_cfl(CflArgs A) {
+  const int nchi = A.nchi, neta = A.neta;
+  const long N = (long)nchi * neta;
+  const double cmax = A.scal[kCmax];
+  double mlam = 0, mflux = 0;
+  const double nu_c = fmax(4.0 / 3.0, A.gamma / A.Pr);
+  for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N; c += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(c % nchi), j = (int)(c / nchi);
+    const bool flow = !A.shock || (j + 1 < A.cell_idx[i]);
+    auto lam_lr = [&](int fi) {
+      const long L = gidx(fi, j + 1, nchi), R = L + 1;
+      const long f = fi + (long)j * (nchi + 1);
+      const double rs = A.S.rho[L] + A.S.rho[R];
+      const double uf = (A.S.ru[L] + A.S.ru[R]) / rs, vf = (A.S.rv[L] + A.S.rv[R]) / rs;
+      return (fabs(uf * A.m.lr_xn[f] + vf * A.m.lr_yn[f]) + cmax) * A.m.lr_a[f];
+    };
+    auto lam_bt = [&](int fj) {
+      const long B = gidx(i + 1, fj, nchi), Tt = B + (nchi + 2);
+      const long f = i + (long)fj * nchi;
+      const double rs = A.S.rho[B] + A.S.rho[Tt];
+      const double uf = (A.S.ru[B] + A.S.ru[Tt]) / rs, vf = (A.S.rv[B] + A.S.rv[Tt]) / rs;
+      return (fabs(uf * A.m.bt_xn[f] + vf * A.m.bt_yn[f]) + cmax) * A.m.bt_a[f];
+    };
+    if (flow) {
+      const double lam_c = fmax(lam_lr(i), lam_lr(i + 1)) + fmax(lam_bt(j), lam_bt(j + 1));
+      const long g = gidx(i + 1, j + 1, nchi);
+      const double Axi = 0.5 * (A.m.lr_a[i + (long)j * (nchi + 1)] + A.m.lr_a[i + 1 + (long)j * (nchi + 1)]);
+      const double Aeta = 0.5 * (A.m.bt_a[i + (long)j * nchi] + A.m.bt_a[i + (long)(j + 1) * nchi]);
+      const double vol = A.m.vol[c];
+      const double nu_eff = nu_c / (A.S.rho[g] * A.Re);
+      const double lam_v = 2 * nu_eff * (Axi * Axi + Aeta * Aeta) / vol;
+      mlam = fmax(mlam, (lam_c + lam_v) / vol);
+      const double r = A.S.rho[g];
+      const double t_u = (fabs(A.SF2[c]) + fabs(A.SF1[c])) / r;
+      const double t_r = fabs(A.SF0[c] / r);
+      const double t_E = fabs(A.SF3[c] / A.S.rE[g]);
+      mflux = fmax(mflux, fmax(t_u, fmax(t_r, t_E)));
+    }
+  }
+  mlam = warp_max(mlam);
+  mflux = warp_max(mflux);
+  __shared__ double r1[32], r2[32];
+  if ((threadIdx.x & 31) == 0) { r1[threadIdx.x >> 5] = mlam; r2[threadIdx.x >> 5] = mflux; }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const bool ok = threadIdx.x < (blockDim.x >> 5);
+    double v1 = ok ? r1[threadIdx.x] : 0.0, v2 = ok ? r2[threadIdx.x] : 0.0;
+    v1 = warp_max(v1);
+    v2 = warp_max(v2);
+    if (threadIdx.x == 0) {
+      atomic_max_nonneg(&A.scal[kMaxLam], v1);
+      atomic_max_nonneg(&A.scal[kMaxFlux], v2);
+    }
+  }
+}
+
+__global__ void k_cfl_final(double* scal, double CFL, double max_dt) {
+  const double dt1 = CFL / scal[kMaxLam];
+  const double dt2 = CFL / scal[kMaxFlux];  // +inf when the stored flux is zero
+  scal[kDt] = fmin(dt1, fmin(dt2, max_dt));
+}
+
+// Step end on S: UPDATE_FIELD_UPSTREAM (after APPLY_BOUNDARY_CONDITIONS), MIN_RHO, t += dt.
+struct FillArgs {
+  hymor_config cfg;
+  DevMesh m;
+  Cons S;
+  const int* cell_idx;
+  double* scal;
+  unsigned* err;
+  int advance;
+};
+
+__global__ void __launch_bounds__(256) k_fill_minrho(FillArgs A) {
+  const hymor_config& c = A.cfg;
+  const int nchi = c.nchi, neta = c.neta, NI = nchi + 2;
+  const long G = (long)NI * (neta + 2);
+  const double t = A.scal[kT];
+  const double u_y = c.rho_v_0 / c.rho_0, u_x = c.rho_u_0 / c.rho_0;
+  const bool dist = c.dist_amp[0] != 0 || c.dist_amp[1] != 0 || c.dist_amp[2] != 0 || c.dist_amp[3] != 0;
+  unsigned limited = 0;
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < G; k += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(k % NI), j = (int)(k / NI);
+    if (i < 1 || i > nchi) continue;
+    if (c.shock_enabled && j >= A.cell_idx[i - 1] + 2) {
+      double pert = 0;
+      if (dist)
+        pert = cos(2.0 * M_PI * c.dist_ky * (A.m.y_ext[k] - u_y * t)) * sin(2.0 * M_PI * c.dist_kx * (A.m.x_ext[k] - u_x * t));
+      A.S.rho[k] = c.rho_0 + pert * c.dist_amp[0];
+      A.S.ru[k] = c.rho_u_0 + pert * c.dist_amp[1];
+      A.S.rv[k] = c.rho_v_0 + pert * c.dist_amp[2];
+      A.S.rE[k] = c.rho_E_0 + pert * c.dist_amp[3];
+    }
+    if (j >= 1 && j <= neta && A.S.rho[k] < c.rho_min) {  // MIN_RHO.jl:16-23
+      A.S.rho[k] = c.rho_min;
+      ++limited;
+    }
+  }
+  if (limited) atomicAdd(&A.err[kRhoLimited], limited);
+}
+
+__global__ void k_advance_time(double* scal) { scal[kT] = scal[kT] + scal[kDt]; }
+
+// Classical RK4 helpers (value-semantics stages of the MATLAB twin).
+struct SnapArgs {
+  Cons S, Yc;
+  ShockPts pS, pYc;
+  long G;
+  int nchi;
+};
+__global__ void k_snapshot(SnapArgs A) {
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < A.G; k += (long)gridDim.x * blockDim.x) {
+    A.Yc.rho[k] = A.S.rho[k]; A.Yc.ru[k] = A.S.ru[k]; A.Yc.rv[k] = A.S.rv[k]; A.Yc.rE[k] = A.S.rE[k];
+    if (k < A.nchi) {
+      A.pYc.x[k] = A.pS.x[k]; A.pYc.y[k] = A.pS.y[k]; A.pYc.chi[k] = A.pS.chi[k]; A.pYc.eta[k] = A.pS.eta[k];
+    }
+  }
+}
+
+struct ClassArgs {
+  Cons Y, Yc;
+  ShockPts pY, pYc;
+  const double* F0;
+  const double* F1;
+  const double* F2;
+  const double* F3;
+  const double* speed_x;
+  const double* speed_y;
+  const int* cell_idx;
+  const double* scal;
+  double cY, relax;
+  int nchi, neta, shock, sym;
+};
+__global__ void k_classical_stage(ClassArgs A) {
+  const int NI = A.nchi + 2;
+  const long G = (long)NI * (A.neta + 2);
+  const double w = A.cY * A.scal[kDt];
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < G; k += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(k % NI), j = (int)(k / NI);
+    double r = A.Yc.rho[k], u = A.Yc.ru[k], v = A.Yc.rv[k], e = A.Yc.rE[k];
+    if (i >= 1 && i <= A.nchi && j >= 1 && j <= A.neta && flow_at(A.cell_idx, A.shock, i - 1, j)) {
+      const long c = (long)(i - 1) + (long)(j - 1) * A.nchi;
+      r = fma(w, A.F0[c], r); u = fma(w, A.F1[c], u); v = fma(w, A.F2[c], v); e = fma(w, A.F3[c], e);
+    }
+    A.Y.rho[k] = r; A.Y.ru[k] = u; A.Y.rv[k] = v; A.Y.rE[k] = e;
+    if (A.shock && k < A.nchi) {
+      const double wr = w * A.relax;
+      A.pY.x[k] = A.pYc.x[k] + A.speed_x[k] * wr;
+      A.pY.y[k] = A.pYc.y[k] + A.speed_y[k] * wr;
+      A.pY.chi[k] = A.pYc.chi[k];
+      A.pY.eta[k] = A.pYc.eta[k];
+    }
+  }
+}
+// symmetry fix of the classical stage points runs after the stage kernel
+__global__ void k_sym_fix(ShockPts p) { p.x[0] = p.x[1]; }
+
+int grid_for(long n, int threads) {
+  long b = (n + threads - 1) / threads;
+  const long cap = 152L * 16;
+  return (int)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+}  // namespace
+
+// ===========================================================================
+// launchers
+
+void launch_update_thermo(const DevCtx& d, int mode, double cY, double cS, cudaStream_t st) {
+  UpdArgs a;
+  a.S = d.S;
+  a.Y = d.Y;
+  a.Yc = d.Yc;
+  a.F0 = d.F[0]; a.F1 = d.F[1]; a.F2 = d.F[2]; a.F3 = d.F[3];
+  a.p = d.p;
+  a.T = d.T;
+  a.cell_idx = d.cell_idx;
+  a.scal = d.scal;
+  a.err = d.err;
+  a.cY = cY;
+  a.cS = cS;
+  a.gm1 = d.cfg.gamma - 1;
+  a.nchi = d.nchi;
+  a.neta = d.neta;
+  a.mode = mode;
+  a.shock = d.cfg.shock_enabled;
+  k_update_thermo<<<grid_for(d.G, 256), 256, 0, st>>>(a);
+}
+
+static void launch_shock_bc_impl(const DevCtx& d, bool on_S, bool copy_pts, bool move, double cY, double cS,
+                                 int a_mode, bool do_shock, bool do_bc, cudaStream_t st) {
+  ShockArgs A;
+  A.do_shock = do_shock;
+  A.do_bc = do_bc;
+  A.cfg = d.cfg;
+  A.tgt = on_S ? d.S : d.Y;
+  A.p = d.p;
+  A.T = d.T;
+  A.compute_a = (a_mode == 0);
+  A.a_bc = (a_mode == 0) ? d.aY : d.aS;
+  A.pts = on_S ? d.Sp : d.Yp;
+  A.pS = d.Sp;
+  A.copy_pts = copy_pts;
+  A.move = move;
+  A.on_S = on_S;
+  A.cY = cY;
+  A.cS = cS;
+  A.cell_idx = d.cell_idx;
+  A.beta = d.beta;
+  A.speed_x = d.speed_x;
+  A.speed_y = d.speed_y;
+  A.rel = d.rel;
+  A.spl = d.spl;
+  A.scal = d.scal;
+  A.err = d.err;
+  A.m = d.m;
+  const size_t smem = d.cfg.shock_enabled ? sizeof(double) * 7 * d.nchi : 0;
+  k_shock_bc<<<1, 1024, smem, st>>>(A);
+}
+
+void launch_shock_bc(const DevCtx& d, bool on_S, bool copy_pts, bool move, double cY, double cS,
+                     int a_mode, cudaStream_t st) {
+  launch_shock_bc_impl(d, on_S, copy_pts, move, cY, cS, a_mode, true, true, st);
+}
+
+void launch_shock_bc_flags(const DevCtx& d, bool on_S, bool copy_pts, bool do_shock, bool do_bc, int a_mode,
+                           cudaStream_t st) {
+  launch_shock_bc_impl(d, on_S, copy_pts, false, 0, 0, a_mode, do_shock, do_bc, st);
+}
+
+void launch_flux(const DevCtx& d, bool on_S, double* const out[4], cudaStream_t st) {
+  FluxArgs a;
+  const Cons& q = on_S ? d.S : d.Y;
+  a.rho = q.rho; a.ru = q.ru; a.rv = q.rv; a.rE = q.rE;
+  a.p = d.p;
+  a.T = d.T;
+  a.o0 = out[0]; a.o1 = out[1]; a.o2 = out[2]; a.o3 = out[3];
+  a.cell_idx = d.cell_idx;
+  a.m = d.m;
+  const hymor_config& c = d.cfg;
+  a.mre = ((1.0 + 1.0) / 2) / c.Re;
+  a.kq = (1.0 + 1.0) / 2 * c.gamma / c.Re / c.Pr;
+  a.inv_Re = 1.0 / c.Re;
+  a.gk = c.gamma / c.Re / c.Pr;
+  a.suthS = c.sutherland_S;
+  a.Tinf_inv = c.energy_factor / c.cv;
+  a.nchi = d.nchi;
+  a.neta = d.neta;
+  a.shock = c.shock_enabled;
+  a.mask = c.shock_enabled && c.shock_feedback;
+  dim3 grid((d.nchi + TX - 1) / TX, (d.neta + TY - 1) / TY);
+  const bool axi = c.axisymmetric, suth = c.viscosity_model == 1;
+  if (!axi && !suth) k_flux<false, false><<<grid, kFluxThreads, flux_smem<false, false>(), st>>>(a);
+  else if (axi && !suth) k_flux<true, false><<<grid, kFluxThreads, flux_smem<true, false>(), st>>>(a);
+  else if (!axi && suth) k_flux<false, true><<<grid, kFluxThreads, flux_smem<false, true>(), st>>>(a);
+  else k_flux<true, true><<<grid, kFluxThreads, flux_smem<true, true>(), st>>>(a);
+}
+
+void flux_kernel_setup() {
+  cudaFuncSetAttribute(k_flux<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem<false, false>());
+  cudaFuncSetAttribute(k_flux<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem<true, false>());
+  cudaFuncSetAttribute(k_flux<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem<false, true>());
+  cudaFuncSetAttribute(k_flux<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem<true, true>());
+  cudaFuncSetAttribute(k_shock_bc, cudaFuncAttributeMaxDynamicSharedMemorySize, 7 * 8 * 4096);
+}
+
+void launch_flow_cells(const DevCtx& d, cudaStream_t st) {
+  FlowArgs A;
+  A.cfg = d.cfg;
+  A.m = d.m;
+  A.S = d.S;
+  A.pS = d.Sp;
+  A.cell_idx = d.cell_idx;
+  A.scal = d.scal;
+  A.err = d.err;
+  k_flow_cells<<<(d.nchi + 127) / 128, 128, 0, st>>>(A);
+}
+
+void launch_sound_cmax(const DevCtx& d, bool recompute, cudaStream_t st) {
+  SoundArgs A;
+  A.S = d.S;
+  A.aS = d.aS;
+  A.scal = d.scal;
+  A.gamma = d.cfg.gamma;
+  A.nchi = d.nchi;
+  A.neta = d.neta;
+  A.recompute = recompute;
+  A.isothermal_eta0 = d.cfg.bc_eta0 == HYMOR_BC_NO_SLIP_ISOTHERMAL;
+  k_sound_cmax<<<grid_for(d.G, 256), 256, 0, st>>>(A);
+}
+
+void launch_cfl(const DevCtx& d, cudaStream_t st) {
+  CflArgs A;
+  A.S = d.S;
+  A.SF0 = d.SF[0]; A.SF1 = d.SF[1]; A.SF2 = d.SF[2]; A.SF3 = d.SF[3];
+  A.m = d.m;
+  A.cell_idx = d.cell_idx;
+  A.scal = d.scal;
+  A.gamma = d.cfg.gamma;
+  A.Pr = d.cfg.Pr;
+  A.Re = d.cfg.Re;
+  A.nchi = d.nchi;
+  A.neta = d.neta;
+  A.shock = d.cfg.shock_enabled;
+  k_cfl<<<grid_for(d.N, 256), 256, 0, st>>>(A);
+  k_cfl_final<<<1, 1, 0, st>>>(d.scal, d.cfg.CFL, d.cfg.max_dt);
+}
+
+void launch_fill_minrho(const DevCtx& d, bool advance_time, cudaStream_t st) {
+  FillArgs A;
+  A.cfg = d.cfg;
+  A.m = d.m;
+  A.S = d.S;
+  A.cell_idx = d.cell_idx;
+  A.scal = d.scal;
+  A.err = d.err;
+  A.advance = 0;
+  k_fill_minrho<<<grid_for(d.G, 256), 256, 0, st>>>(A);
+  if (advance_time) k_advance_time<<<1, 1, 0, st>>>(d.scal);
+}
+
+void launch_snapshot(const DevCtx& d, cudaStream_t st) {
+  SnapArgs A{d.S, d.Yc, d.Sp, d.Ycp, d.G, d.nchi};
+  k_snapshot<<<grid_for(d.G, 256), 256, 0, st>>>(A);
+}
+
+void launch_classical_stage(const DevCtx& d, double cY, cudaStream_t st) {
+  ClassArgs A;
+  A.Y = d.Y;
+  A.Yc = d.Yc;
+  A.pY = d.Yp;
+  A.pYc = d.Ycp;
+  A.F0 = d.F[0]; A.F1 = d.F[1]; A.F2 = d.F[2]; A.F3 = d.F[3];
+  A.speed_x = d.speed_x;
+  A.speed_y = d.speed_y;
+  A.cell_idx = d.cell_idx;
+  A.scal = d.scal;
+  A.cY = cY;
+  A.relax = d.cfg.relaxation;
+  A.nchi = d.nchi;
+  A.neta = d.neta;
+  A.shock = d.cfg.shock_enabled;
+  k_classical_stage<<<grid_for(d.G, 256), 256, 0, st>>>(A);
+  if (d.cfg.shock_enabled && d.cfg.bc_chi0 == HYMOR_BC_SYMMETRY && d.nchi >= 2) k_sym_fix<<<1, 1, 0, st>>>(d.Yp);
+}
+
+}  // namespace hymor

@@ -1,0 +1,65 @@
+// Host-side launchers of the libhymor kernels (core.cu, linear.cu).
+#pragma once
+
+#include "common.cuh"
+
+namespace hymor {
+
+struct DevCtx {
+  hymor_config cfg;
+  int nchi, neta, NI, NJ;
+  long G, N, NLR, NBT;
+  DevMesh m;
+  Cons S;          // the solution (reference `s`)
+  Cons Y;          // the stage solution (reference `solution_0` / `temp`)
+  Cons Yc;         // classical-RK4 snapshot of y_n
+  double *p, *T;   // ghosted work arrays (thermodynamic state of the array being evaluated)
+  double* aS;      // ghosted sound speed of S (persistent like s["var"]["a"])
+  double* aY;      // ghosted sound speed of the stage array (edge-adjacent lines only)
+  double* F[4];    // stage flux
+  double* SF[4];   // persistent flux of S (s["flux"])
+  ShockPts Sp, Yp, Ycp;  // shock points of S, Y and the classical snapshot
+  int* cell_idx;   // 1-based shocked rows (Nchi)
+  double *beta, *speed_x, *speed_y, *rel;  // Nchi
+  double* spl;     // spline workspace (device, sized for Nchi)
+  double* scal;    // Scalar block
+  unsigned* err;   // ErrWord block
+  // Jacobian
+  double* coef;    // N * 144 stencil blocks (or null)
+  double* jwork;   // linearisation workspace
+};
+
+// ---- core.cu ----
+// mode: 0 = Y <- S (all ghosted cells), thermo(Y); 1 = Y += wY F, S += wS F (interior,
+// masked), thermo(Y); 2 = S += wS F, thermo(S); 3 = thermo(S); 4 = thermo(Y).
+// Stage weights are read from the device dt: wY = cY * dt, wS = cS * dt.
+void launch_update_thermo(const DevCtx& d, int mode, double cY, double cS, cudaStream_t st);
+// Shock fitting + boundary conditions on `tgt` (S when on_S, else Y).
+//   copy_pts: copy S's shock points into Y first (stage 1)
+//   move: apply MOVE_SHOCK to S (weight cS*dt) and Y (weight cY*dt)
+//   a_mode: 0 = compute the edge-adjacent sound speed of tgt into aY before the shock
+//           update and use it (PDE); 1 = use the persistent aS (ADVECT_FLOW step end)
+void launch_shock_bc(const DevCtx& d, bool on_S, bool copy_pts, bool move, double cY, double cS,
+                     int a_mode, cudaStream_t st);
+// Flux (residual) of tgt into out[4] (masked by the flow cells when feedback is on).
+void launch_flux(const DevCtx& d, bool on_S, double* const out[4], cudaStream_t st);
+// UPDATE_FLOW_CELLS part 1: detect shocked cells, upstream fill, extrapolation (on S).
+void launch_flow_cells(const DevCtx& d, cudaStream_t st);
+// Sound speed of S (recompute) and max|a| into scal[kCmax]; recompute=false only reduces aS.
+void launch_sound_cmax(const DevCtx& d, bool recompute, cudaStream_t st);
+// CFL maxima and dt (scal[kDt]).
+void launch_cfl(const DevCtx& d, cudaStream_t st);
+// Step end: upstream fill + MIN_RHO on S, t += dt.
+void launch_fill_minrho(const DevCtx& d, bool advance_time, cudaStream_t st);
+// Classical RK4: snapshot S -> Yc (cells and shock points); restore Y <- Yc + c*dt*F.
+void launch_snapshot(const DevCtx& d, cudaStream_t st);
+void launch_classical_stage(const DevCtx& d, double cY, cudaStream_t st);
+
+// ---- linear.cu ----
+void launch_jacobian_assemble(DevCtx& d, cudaStream_t st);
+void launch_matvec(const DevCtx& d, int k, const double* X, double* Y, int transpose, double scale,
+                   cudaStream_t st);
+void launch_expm(const DevCtx& d, int k, double dt, int nsteps, int order, const double* X,
+                 double* Y, int transpose, double* work, cudaStream_t st);
+
+}  // namespace hymor

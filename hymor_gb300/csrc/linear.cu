@@ -1,0 +1,459 @@
+// Linearised residual on the device: coloured finite-difference Jacobian assembly
+// into stencil blocks, the block-stencil matvec (and its transpose) and the
+// Taylor propagator exp(A dt)^n used by the exponential-transform eigen solvers.
+//
+// Device layout of the Jacobian: 144 planes of N doubles (plane (q*4 + vout)*4 + vin,
+// q = neighbour slot), so that consecutive threads (cells) read consecutive
+// addresses. hymor_jacobian_get/set convert to the per-cell block layout of
+// include/hymor.h.
+#include <cmath>
+#include <vector>
+
+#include "kernels.h"
+
+namespace hymor {
+DevCtx& ctx_dev(hymor_ctx* c);
+cudaStream_t ctx_stream(hymor_ctx* c);
+int ctx_fail(hymor_ctx* c, int code, const char* msg);
+std::vector<void*>& ctx_allocs(hymor_ctx* c);
+void launch_shock_bc_flags(const DevCtx& d, bool on_S, bool copy_pts, bool do_shock, bool do_bc, int a_mode,
+                           cudaStream_t st);
+
+namespace {
+
+constexpr int kMvThreads = 256;
+constexpr int kVecChunk = 4;
+
+struct Wrap {
+  int nchi, neta, per_chi, per_eta;
+  // input cell of output (i, j) at offset (a, b); -1 if the reference assembles no entry
+  __device__ __forceinline__ long nbr(int i, int j, int a, int b) const {
+    int ii = i + a, jj = j + b;
+    const bool wi = ii < 0 || ii >= nchi, wj = jj < 0 || jj >= neta;
+    if ((wi && !per_chi) || (wj && !per_eta) || (wi && wj)) return -1;
+    if (wi) ii = ii < 0 ? ii + nchi : ii - nchi;
+    if (wj) jj = jj < 0 ? jj + neta : jj - neta;
+    return (long)ii + (long)jj * nchi;
+  }
+};
+
+Wrap make_wrap(const hymor_config& c) {
+  return Wrap{c.nchi, c.neta, c.bc_chi0 == HYMOR_BC_PERIODIC && c.bc_chi1 == HYMOR_BC_PERIODIC,
+              c.bc_eta0 == HYMOR_BC_PERIODIC && c.bc_eta1 == HYMOR_BC_PERIODIC};
+}
+
+// Y = S with variable `var` of every interior cell of colour `colour` (1..9, the
+// pattern of GET_PERTURBATION_MATRIX, LINEARIZE_EQUATIONS_NO_DISCONTINUITY.jl:959-983)
+// raised by flow_cells * eps; then p, T of Y.
+struct PertArgs {
+  Cons S, Y;
+  double *p, *T;
+  const int* cell_idx;
+  double eps, gm1;
+  int nchi, neta, var, colour, shock;
+};
+
+__global__ void k_perturb_thermo(PertArgs a) {
+  const int NI = a.nchi + 2;
+  const long G = (long)NI * (a.neta + 2);
+  const int si = (a.colour % 3 == 0) ? 3 : a.colour % 3;  // 1-based start in chi
+  const int sj = (a.colour + 2) / 3;                       // 1-based start in eta
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < G; k += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(k % NI), j = (int)(k / NI);
+    double v[4] = {a.S.rho[k], a.S.ru[k], a.S.rv[k], a.S.rE[k]};
+    if (a.var >= 0 && i >= 1 && i <= a.nchi && j >= 1 && j <= a.neta) {
+      const bool hit = (i >= si) && ((i - si) % 3 == 0) && (j >= sj) && ((j - sj) % 3 == 0);
+      const double flow = (!a.shock || j < a.cell_idx[i - 1]) ? 1.0 : 0.0;
+      v[a.var] = v[a.var] + flow * (hit ? 1.0 : 0.0) * a.eps;
+    }
+    a.Y.rho[k] = v[0]; a.Y.ru[k] = v[1]; a.Y.rv[k] = v[2]; a.Y.rE[k] = v[3];
+    const double ir = 1.0 / v[0];
+    const double ke = fma(v[1], v[1], v[2] * v[2]) * ir;
+    const double eint = fma(-0.5, ke, v[3]);
+    a.p[k] = eint * a.gm1;
+    a.T[k] = eint * ir;
+  }
+}
+
+// coef[plane(q, vo, var)][m] = (Fp[vo][m] - Fb[vo][m]) / eps for every slot q whose
+// input cell m + offset(q) has the perturbed colour (GET_OUTPUT_INDEXING_A11,
+// LINEARIZE_EQUATIONS_NO_DISCONTINUITY.jl:306-788; REMOVE_BASE_OUTPUT :935-946).
+struct ScatArgs {
+  const double* Fp[4];
+  const double* Fb[4];
+  double* coef;
+  Wrap w;
+  double inv_eps_dummy;
+  double eps;
+  int var, colour;
+  long N;
+};
+
+__global__ void k_scatter(ScatArgs a) {
+  const long N = a.N;
+  const int si = (a.colour % 3 == 0) ? 3 : a.colour % 3;
+  const int sj = (a.colour + 2) / 3;
+  for (long m = blockIdx.x * (long)blockDim.x + threadIdx.x; m < N; m += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(m % a.w.nchi), j = (int)(m / a.w.nchi);
+    double d[4];
+#pragma unroll
+    for (int vo = 0; vo < 4; ++vo) d[vo] = (a.Fp[vo][m] - a.Fb[vo][m]) / a.eps;
+#pragma unroll
+    for (int b = -1; b <= 1; ++b)
+#pragma unroll
+      for (int aa = -1; aa <= 1; ++aa) {
+        const long n = a.w.nbr(i, j, aa, b);
+        if (n < 0) continue;
+        const int ni = (int)(n % a.w.nchi) + 1, nj = (int)(n / a.w.nchi) + 1;  // 1-based
+        const bool hit = (ni >= si) && ((ni - si) % 3 == 0) && (nj >= sj) && ((nj - sj) % 3 == 0);
+        if (!hit) continue;
+        const int q = (b + 1) * 3 + (aa + 1);
+#pragma unroll
+        for (int vo = 0; vo < 4; ++vo) a.coef[((long)(q * 4 + vo) * 4 + a.var) * N + m] = d[vo];
+      }
+  }
+}
+
+// y_j = scale * (L x_j) (transpose 0) or scale * (Lᵀ x_j) (transpose 1); optionally
+// acc_j += c_acc * y_j. Vectors: 4N each, column-major batch.
+struct MvArgs {
+  const double* coef;
+  const double* X;
+  double* Y;
+  double* acc;
+  double scale, c_acc;
+  Wrap w;
+  long N;
+  int k, transpose;
+};
+
+__global__ void __launch_bounds__(kMvThreads) k_matvec(MvArgs a) {
+  const long N = a.N;
+  const long n4 = 4 * N;
+  for (long m = blockIdx.x * (long)blockDim.x + threadIdx.x; m < N; m += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(m % a.w.nchi), j = (int)(m / a.w.nchi);
+    for (int v0 = 0; v0 < a.k; v0 += kVecChunk) {
+      const int nv = min(kVecChunk, a.k - v0);
+      double y[kVecChunk][4];
+#pragma unroll
+      for (int v = 0; v < kVecChunk; ++v)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) y[v][c] = 0;
+#pragma unroll
+      for (int b = -1; b <= 1; ++b)
+#pragma unroll
+        for (int aa = -1; aa <= 1; ++aa) {
+          long n;
+          long cell;  // cell that owns the block
+          int q;
+          if (!a.transpose) {
+            n = a.w.nbr(i, j, aa, b);
+            cell = m;
+            q = (b + 1) * 3 + (aa + 1);
+          } else {
+            // m is the input cell of output cell n = m - (aa, b); block slot of (aa, b)
+            n = a.w.nbr(i, j, -aa, -b);
+            cell = n;
+            q = (b + 1) * 3 + (aa + 1);
+          }
+          if (n < 0) continue;
+          double B[16];
+#pragma unroll
+          for (int e = 0; e < 16; ++e) B[e] = a.coef[(long)(q * 16 + e) * N + cell];
+          for (int v = 0; v < nv; ++v) {
+            const double* x = a.X + (long)(v0 + v) * n4;
+            const double x0 = x[n], x1 = x[N + n], x2 = x[2 * N + n], x3 = x[3 * N + n];
+            if (!a.transpose) {
+#pragma unroll
+              for (int vo = 0; vo < 4; ++vo)
+                y[v][vo] = fma(B[vo * 4 + 0], x0, fma(B[vo * 4 + 1], x1, fma(B[vo * 4 + 2], x2, fma(B[vo * 4 + 3], x3, y[v][vo]))));
+            } else {
+#pragma unroll
+              for (int vi = 0; vi < 4; ++vi)
+                y[v][vi] = fma(B[0 * 4 + vi], x0, fma(B[1 * 4 + vi], x1, fma(B[2 * 4 + vi], x2, fma(B[3 * 4 + vi], x3, y[v][vi]))));
+            }
+          }
+        }
+      for (int v = 0; v < nv; ++v) {
+        double* yo = a.Y + (long)(v0 + v) * n4;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const double val = a.scale * y[v][c];
+          yo[c * N + m] = val;
+          if (a.acc) {
+            double* ac = a.acc + (long)(v0 + v) * n4;
+            ac[c * N + m] = fma(val, a.c_acc, ac[c * N + m]);
+          }
+        }
+      }
+    }
+  }
+}
+
+__global__ void k_copy(const double* __restrict__ s, double* __restrict__ d, long n) {
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) d[k] = s[k];
+}
+
+// per-cell block layout <-> plane layout
+__global__ void k_blocks_to_planes(const double* blk, double* pl, long N) {
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < N * 144; t += (long)gridDim.x * blockDim.x) {
+    const long m = t / 144;
+    const int e = (int)(t % 144);
+    pl[(long)e * N + m] = blk[t];
+  }
+}
+__global__ void k_planes_to_blocks(const double* pl, double* blk, long N) {
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < N * 144; t += (long)gridDim.x * blockDim.x) {
+    const long m = t / 144;
+    const int e = (int)(t % 144);
+    blk[t] = pl[(long)e * N + m];
+  }
+}
+
+int grid_for(long n, int threads) {
+  long b = (n + threads - 1) / threads;
+  const long cap = 152L * 16;
+  return (int)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+}  // namespace
+
+void launch_matvec(const DevCtx& d, int k, const double* X, double* Y, int transpose, double scale,
+                   cudaStream_t st) {
+  MvArgs a;
+  a.coef = d.coef;
+  a.X = X;
+  a.Y = Y;
+  a.acc = nullptr;
+  a.scale = scale;
+  a.c_acc = 0;
+  a.w = make_wrap(d.cfg);
+  a.N = d.N;
+  a.k = k;
+  a.transpose = transpose;
+  k_matvec<<<grid_for(d.N, kMvThreads), kMvThreads, 0, st>>>(a);
+}
+
+// POWER_METHOD! (Eigenvalues/ARNOLDI_POWER_GPU.jl:64-82): per step vout = v,
+// term_j = (A dt) term_{j-1}, vout += term_j / j!, v = vout.
+void launch_expm(const DevCtx& d, int k, double dt, int nsteps, int order, const double* X, double* Yout,
+                 int transpose, double* work, cudaStream_t st) {
+  const long n = 4 * d.N * (long)k;
+  double* v = work;
+  double* t1 = work + n;
+  double* t2 = work + 2 * n;
+  double* vout = Yout;
+  k_copy<<<grid_for(n, 256), 256, 0, st>>>(X, v, n);
+  k_copy<<<grid_for(n, 256), 256, 0, st>>>(X, vout, n);
+  MvArgs a;
+  a.coef = d.coef;
+  a.w = make_wrap(d.cfg);
+  a.N = d.N;
+  a.k = k;
+  a.transpose = transpose;
+  a.scale = dt;
+  a.acc = vout;
+  for (int s = 0; s < nsteps; ++s) {
+    const double* src = v;
+    long fact = 1;
+    for (int j = 1; j <= order; ++j) {
+      fact *= j;
+      double* dst = (j % 2) ? t1 : t2;
+      a.X = src;
+      a.Y = dst;
+      a.c_acc = 1.0 / (double)fact;
+      k_matvec<<<grid_for(d.N, kMvThreads), kMvThreads, 0, st>>>(a);
+      src = dst;
+    }
+    k_copy<<<grid_for(n, 256), 256, 0, st>>>(vout, v, n);
+  }
+}
+
+void launch_jacobian_assemble(DevCtx& d, cudaStream_t st) {
+  const hymor_config& c = d.cfg;
+  const long N = d.N;
+  double* Fb[4];
+  double* Fp[4];
+  for (int v = 0; v < 4; ++v) {
+    Fb[v] = d.jwork + v * N;
+    Fp[v] = d.jwork + (4 + v) * N;
+  }
+  PertArgs pa;
+  pa.S = d.S;
+  pa.Y = d.Y;
+  pa.p = d.p;
+  pa.T = d.T;
+  pa.cell_idx = d.cell_idx;
+  pa.eps = c.perturbation_magnitude;
+  pa.gm1 = c.gamma - 1;
+  pa.nchi = d.nchi;
+  pa.neta = d.neta;
+  pa.shock = c.shock_enabled;
+  // base output: NON_LINEAR_DYNAMICS(deepcopy(s))
+  pa.var = -1;
+  pa.colour = 1;
+  k_perturb_thermo<<<grid_for(d.G, 256), 256, 0, st>>>(pa);
+  launch_shock_bc_flags(d, false, true, c.shock_enabled, true, 0, st);
+  launch_flux(d, false, Fb, st);
+  cudaMemsetAsync(d.coef, 0, sizeof(double) * 144 * N, st);
+  ScatArgs sa;
+  for (int v = 0; v < 4; ++v) { sa.Fp[v] = Fp[v]; sa.Fb[v] = Fb[v]; }
+  sa.coef = d.coef;
+  sa.w = make_wrap(c);
+  sa.eps = c.perturbation_magnitude;
+  sa.N = N;
+  for (int var = 0; var < 4; ++var)
+    for (int colour = 1; colour <= 9; ++colour) {
+      pa.var = var;
+      pa.colour = colour;
+      k_perturb_thermo<<<grid_for(d.G, 256), 256, 0, st>>>(pa);
+      launch_shock_bc_flags(d, false, true, c.shock_enabled, true, 0, st);
+      launch_flux(d, false, Fp, st);
+      sa.var = var;
+      sa.colour = colour;
+      k_scatter<<<grid_for(N, 256), 256, 0, st>>>(sa);
+    }
+}
+
+}  // namespace hymor
+
+using namespace hymor;
+
+namespace {
+int ensure_linear(hymor_ctx* ctx) {
+  DevCtx& d = ctx_dev(ctx);
+  if (!d.coef) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, sizeof(double) * 144 * d.N) != cudaSuccess)
+      return ctx_fail(ctx, HYMOR_ERR_CUDA, "Jacobian allocation failed");
+    ctx_allocs(ctx).push_back(p);
+    d.coef = static_cast<double*>(p);
+    if (cudaMalloc(&p, sizeof(double) * 8 * d.N) != cudaSuccess)
+      return ctx_fail(ctx, HYMOR_ERR_CUDA, "Jacobian workspace allocation failed");
+    ctx_allocs(ctx).push_back(p);
+    d.jwork = static_cast<double*>(p);
+  }
+  return 0;
+}
+
+int cuda_check(hymor_ctx* ctx, cudaError_t e) {
+  if (e != cudaSuccess) return ctx_fail(ctx, HYMOR_ERR_CUDA, cudaGetErrorString(e));
+  return 0;
+}
+}  // namespace
+
+extern "C" {
+
+int hymor_linearize(hymor_ctx* ctx) {
+  if (!ctx) return HYMOR_ERR_INVALID;
+  int r = ensure_linear(ctx);
+  if (r) return r;
+  DevCtx& d = ctx_dev(ctx);
+  cudaStream_t st = ctx_stream(ctx);
+  // LINEARIZE_L.jl:43-56: flow cells and shock BC, thermo, sound speed, boundary conditions
+  if (d.cfg.shock_enabled) {
+    launch_flow_cells(d, st);
+    launch_update_thermo(d, 3, 0, 0, st);
+    launch_sound_cmax(d, true, st);
+    launch_shock_bc_flags(d, true, false, true, false, 1, st);
+  }
+  launch_update_thermo(d, 3, 0, 0, st);
+  launch_sound_cmax(d, true, st);
+  launch_shock_bc_flags(d, true, false, false, true, 1, st);
+  launch_jacobian_assemble(d, st);
+  if ((r = cuda_check(ctx, cudaGetLastError()))) return r;
+  return cuda_check(ctx, cudaStreamSynchronize(st));
+}
+
+int hymor_jacobian_get(hymor_ctx* ctx, double* coef) {
+  if (!ctx || !coef) return HYMOR_ERR_INVALID;
+  DevCtx& d = ctx_dev(ctx);
+  if (!d.coef) return ctx_fail(ctx, HYMOR_ERR_NOT_READY, "no Jacobian: call hymor_linearize or hymor_jacobian_set");
+  cudaStream_t st = ctx_stream(ctx);
+  double* tmp = nullptr;
+  int r;
+  if ((r = cuda_check(ctx, cudaMallocAsync((void**)&tmp, sizeof(double) * 144 * d.N, st)))) return r;
+  k_planes_to_blocks<<<grid_for(d.N * 144, 256), 256, 0, st>>>(d.coef, tmp, d.N);
+  r = cuda_check(ctx, cudaMemcpyAsync(coef, tmp, sizeof(double) * 144 * d.N, cudaMemcpyDeviceToHost, st));
+  cudaFreeAsync(tmp, st);
+  if (r) return r;
+  return cuda_check(ctx, cudaStreamSynchronize(st));
+}
+
+int hymor_jacobian_set(hymor_ctx* ctx, const double* coef) {
+  if (!ctx || !coef) return HYMOR_ERR_INVALID;
+  int r = ensure_linear(ctx);
+  if (r) return r;
+  DevCtx& d = ctx_dev(ctx);
+  cudaStream_t st = ctx_stream(ctx);
+  double* tmp = nullptr;
+  if ((r = cuda_check(ctx, cudaMallocAsync((void**)&tmp, sizeof(double) * 144 * d.N, st)))) return r;
+  r = cuda_check(ctx, cudaMemcpyAsync(tmp, coef, sizeof(double) * 144 * d.N, cudaMemcpyHostToDevice, st));
+  k_blocks_to_planes<<<grid_for(d.N * 144, 256), 256, 0, st>>>(tmp, d.coef, d.N);
+  cudaFreeAsync(tmp, st);
+  if (r) return r;
+  return cuda_check(ctx, cudaStreamSynchronize(st));
+}
+
+int hymor_matvec_dev(hymor_ctx* ctx, int k, const double* dX, double* dY, int transpose) {
+  if (!ctx || k < 1 || !dX || !dY) return HYMOR_ERR_INVALID;
+  DevCtx& d = ctx_dev(ctx);
+  if (!d.coef) return ctx_fail(ctx, HYMOR_ERR_NOT_READY, "no Jacobian: call hymor_linearize or hymor_jacobian_set");
+  launch_matvec(d, k, dX, dY, transpose, 1.0, ctx_stream(ctx));
+  return cuda_check(ctx, cudaGetLastError());
+}
+
+int hymor_matvec(hymor_ctx* ctx, int k, const double* X, double* Y, int transpose) {
+  if (!ctx || k < 1 || !X || !Y) return HYMOR_ERR_INVALID;
+  DevCtx& d = ctx_dev(ctx);
+  if (!d.coef) return ctx_fail(ctx, HYMOR_ERR_NOT_READY, "no Jacobian: call hymor_linearize or hymor_jacobian_set");
+  cudaStream_t st = ctx_stream(ctx);
+  const size_t bytes = sizeof(double) * 4 * d.N * (size_t)k;
+  double *dx = nullptr, *dy = nullptr;
+  int r;
+  if ((r = cuda_check(ctx, cudaMallocAsync((void**)&dx, bytes, st)))) return r;
+  if ((r = cuda_check(ctx, cudaMallocAsync((void**)&dy, bytes, st)))) return r;
+  cudaMemcpyAsync(dx, X, bytes, cudaMemcpyHostToDevice, st);
+  launch_matvec(d, k, dx, dy, transpose, 1.0, st);
+  cudaMemcpyAsync(Y, dy, bytes, cudaMemcpyDeviceToHost, st);
+  cudaFreeAsync(dx, st);
+  cudaFreeAsync(dy, st);
+  if ((r = cuda_check(ctx, cudaGetLastError()))) return r;
+  return cuda_check(ctx, cudaStreamSynchronize(st));
+}
+
+int hymor_expm_apply_dev(hymor_ctx* ctx, int k, double dt, int nsteps, int order, const double* dX, double* dY,
+                         int transpose) {
+  if (!ctx || k < 1 || nsteps < 0 || order < 1 || order > 20 || !dX || !dY) return HYMOR_ERR_INVALID;
+  DevCtx& d = ctx_dev(ctx);
+  if (!d.coef) return ctx_fail(ctx, HYMOR_ERR_NOT_READY, "no Jacobian: call hymor_linearize or hymor_jacobian_set");
+  cudaStream_t st = ctx_stream(ctx);
+  const size_t n = 4 * d.N * (size_t)k;
+  double* work = nullptr;
+  int r;
+  if ((r = cuda_check(ctx, cudaMallocAsync((void**)&work, 3 * n * sizeof(double), st)))) return r;
+  launch_expm(d, k, dt, nsteps, order, dX, dY, transpose, work, st);
+  cudaFreeAsync(work, st);
+  return cuda_check(ctx, cudaGetLastError());
+}
+
+int hymor_expm_apply(hymor_ctx* ctx, int k, double dt, int nsteps, int order, const double* X, double* Y,
+                     int transpose) {
+  if (!ctx || k < 1 || !X || !Y) return HYMOR_ERR_INVALID;
+  DevCtx& d = ctx_dev(ctx);
+  cudaStream_t st = ctx_stream(ctx);
+  const size_t bytes = sizeof(double) * 4 * d.N * (size_t)k;
+  double *dx = nullptr, *dy = nullptr;
+  int r;
+  if ((r = cuda_check(ctx, cudaMallocAsync((void**)&dx, bytes, st)))) return r;
+  if ((r = cuda_check(ctx, cudaMallocAsync((void**)&dy, bytes, st)))) return r;
+  cudaMemcpyAsync(dx, X, bytes, cudaMemcpyHostToDevice, st);
+  r = hymor_expm_apply_dev(ctx, k, dt, nsteps, order, dx, dy, transpose);
+  if (!r) cudaMemcpyAsync(Y, dy, bytes, cudaMemcpyDeviceToHost, st);
+  cudaFreeAsync(dx, st);
+  cudaFreeAsync(dy, st);
+  if (r) return r;
+  return cuda_check(ctx, cudaStreamSynchronize(st));
+}
+
+}  // extern "C"

@@ -1,0 +1,173 @@
+/*
+ * hymor.h — C ABI of the GB300-native HYMOR hot path (libhymor.so).
+ *
+ * The reference (AdrianAA00/HYMOR) is Julia; its hot path is the Julia API
+ * below, which a Julia host binds with `ccall`. Every entry
+ * point returns 0 on success or a negative HYMOR_ERR_* code; hymor_last_error()
+ * gives the message. Arrays use the reference layout: column-major with chi (i)
+ * fastest; conserved variables are ghosted (Nchi+2) x (Neta+2) and stored back
+ * to back as [rho; rho_u; rho_v; rho_E]; fluxes are 4 x Nchi*Neta; linear
+ * vectors are [rho; rho_u; rho_v; rho_E] x Nchi*Neta (4N).
+ *
+ * One context = one GPU, one CUDA stream, one solution. Contexts are not
+ * thread-safe: calls on one context must not overlap.
+ */
+#ifndef HYMOR_H
+#define HYMOR_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HYMOR_OK 0
+#define HYMOR_ERR_INVALID (-1)      /* bad argument / size / configuration          */
+#define HYMOR_ERR_CUDA (-2)         /* CUDA runtime error                           */
+#define HYMOR_ERR_NUMERIC (-3)      /* NaN / non-positive density or pressure seen  */
+#define HYMOR_ERR_SHOCK_RANGE (-4)  /* shocked cell too close to the domain top     */
+#define HYMOR_ERR_TIMEOUT (-5)      /* a bounded device wait gave up                */
+#define HYMOR_ERR_NOT_READY (-6)    /* e.g. matvec before a Jacobian exists         */
+
+/* Boundary conditions (names of utils/Operators/APPLY_BOUNDARY_CONDITIONS.jl). */
+enum {
+  HYMOR_BC_SYMMETRY = 0,
+  HYMOR_BC_NO_SLIP_ADIABATIC = 1,
+  HYMOR_BC_NO_SLIP_ISOTHERMAL = 2,
+  HYMOR_BC_OUTFLOW_SUPERSONIC = 3,
+  HYMOR_BC_OUTFLOW_SUPERSONIC_1ST = 4,
+  HYMOR_BC_OUTFLOW_SUBSONIC = 5,
+  HYMOR_BC_OUTFLOW_NRCBC = 6,
+  HYMOR_BC_INFLOW_SUPERSONIC = 7,
+  HYMOR_BC_INFLOW_SUBSONIC = 8,
+  HYMOR_BC_PERIODIC = 9,
+  HYMOR_BC_SHOCK = 10
+};
+
+/* Curvilinear mappings (utils/Mesh/GO_TO_ELEMENT_SPACE.jl). */
+enum { HYMOR_MAP_CIRCLE = 0, HYMOR_MAP_BLUNT_CONE = 1, HYMOR_MAP_CHANNEL = 2, HYMOR_MAP_WEDGE = 3 };
+
+/* The fields of the reference's input Dict that the hot path reads. */
+typedef struct {
+  int32_t nchi, neta;
+  int32_t axisymmetric;                 /* PDE_dimension: 0 "2D", 1 "3D-axisymmetric"        */
+  int32_t bc_chi0, bc_chi1, bc_eta0, bc_eta1;
+  int32_t shock_enabled, shock_feedback;
+  int32_t shock_interp;                 /* 1, 2, 3 = "1st", "2nd", "3rd"                     */
+  int32_t shock_eulerian;               /* 0 Lagrangian, 1 Eulerian                          */
+  int32_t mapping;                      /* HYMOR_MAP_*                                       */
+  int32_t rk_variant;                   /* 0 reference Julia stages, 1 classical RK4         */
+  int32_t viscosity_model;              /* 0 constant (reference CPG), 1 Sutherland          */
+  int32_t pad0;
+  double gamma, Pr, Re, Mach;
+  double Tw_chi0, Tw_eta0, Tw_eta1;     /* wall temperature / freestream temperature         */
+  double cv, energy_factor;             /* freestream cv, energy factor                      */
+  double rho_0, rho_u_0, rho_v_0, rho_E_0, p_0;   /* non-dimensional freestream              */
+  double dist_kx, dist_ky, dist_amp[4]; /* freestream disturbance                            */
+  double relaxation, spline_param;
+  double R, dRs, dRe, circle_angle_extra;
+  double L, theta, initial_beta;
+  double Lx, Ly, channel_angle, eta_refinement_power;
+  double rho_min;
+  double CFL, max_dt;
+  double perturbation_magnitude;        /* finite-difference step of the Jacobian            */
+  double sutherland_S;                  /* S / T_inf of the Sutherland law                   */
+} hymor_config;
+
+/* Mesh arrays, host pointers in the reference layout (copied to the device). */
+typedef struct {
+  const double *lr_xn, *lr_yn, *lr_a;   /* (Nchi+1) x Neta                                   */
+  const double *bt_xn, *bt_yn, *bt_a;   /* Nchi x (Neta+1)                                   */
+  const double *vol;                    /* Nchi x Neta                                       */
+  const double *x_ext, *y_ext;          /* (Nchi+2) x (Neta+2)                               */
+  const double *x_corner, *y_corner;    /* (Nchi+1) x (Neta+1)                               */
+  const double *chi1;                   /* Nchi: mesh["chi"][:, 1]                           */
+  const double *fb_area;                /* Nchi x Neta, axisymmetric only (else NULL)        */
+  double fb_yn_front, fb_yn_back;
+} hymor_mesh;
+
+typedef struct hymor_ctx_s hymor_ctx;
+
+/* Context: copies the mesh, builds the face geometry, allocates device state.
+ * Replaces the reference's solution Dict set-up (utils/Initialization/INITIALIZATION.jl:35-61
+ * leaves `s["mesh"]`, `s["var"]`, `s["shock"]` ready for the hot path). */
+int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx** out);
+int hymor_ctx_destroy(hymor_ctx* ctx);
+const char* hymor_last_error(const hymor_ctx* ctx);
+
+/* Solution state: q = 4 ghosted arrays; shock points (Nchi each); cell_idx
+ * 1-based shocked-cell rows (shock["cell_indices"], flow cells follow as
+ * j < cell_idx[i]); t = time; a = ghosted sound speed or NULL (then sqrt(gamma p / rho)
+ * of q). Any shock pointer may be NULL when shock fitting is off. */
+int hymor_set_state(hymor_ctx* ctx, const double* q, const double* pts_x, const double* pts_y,
+                    const double* pts_chi, const double* pts_eta, const int32_t* cell_idx,
+                    double t, const double* a);
+int hymor_get_state(hymor_ctx* ctx, double* q, double* pts_x, double* pts_y, double* pts_chi,
+                    double* pts_eta, int32_t* cell_idx, double* t, double* dt);
+
+/* NON_LINEAR_DYNAMICS_NO_DISCONTINUITY (utils/Operators/NON_LINEAR_DYNAMICS_NO_DISCONTINUITY.jl:1-28,
+ * calling PDE, utils/Operators/PDE.jl:1-47) on the context state, which it mutates
+ * like the reference mutates `s` (ghost cells, shocked cells, shock points). Writes
+ * the context's flux (read by the CFL dt2 term) and, if flux != NULL, copies it out. */
+int hymor_residual(hymor_ctx* ctx, double* flux);
+/* Sets the context's persistent flux arrays (the Dict's s["flux"]). */
+int hymor_set_flux(hymor_ctx* ctx, const double* flux);
+
+/* nsteps x ADVECT_FLOW (utils/Time_marching/ADVECT_FLOW.jl:30-39 ->
+ * ADVECT_FLOW_EXPLICIT.jl:36-81), all on the device (one CUDA graph per step). */
+int hymor_step(hymor_ctx* ctx, int nsteps);
+/* UPDATE_FLOW_CELLS (utils/Shock_fitting/UPDATE_FLOW_CELLS.jl:25-37). */
+int hymor_update_flow_cells(hymor_ctx* ctx);
+/* CFL_TIMESTEP (utils/Time_marching/CFL_TIMESTEP.jl:41-138) on the current state. */
+int hymor_cfl_timestep(hymor_ctx* ctx, double* dt);
+/* Counters: MIN_RHO activations and Rankine-Hugoniot y < 1 warnings since creation. */
+int hymor_counters(hymor_ctx* ctx, int32_t* rho_limited, int32_t* rh_warnings);
+
+/* Device timing on the context stream (CUDA events): start, then stop returns ms. */
+int hymor_timer_start(hymor_ctx* ctx);
+int hymor_timer_stop(hymor_ctx* ctx, float* ms);
+/* Per-kernel device time of the residual (flux) kernel inside the last hymor_step
+ * call: total ms and number of launches (measured with CUDA events on the stream). */
+int hymor_profile_flux(hymor_ctx* ctx, int enable, float* total_ms, int32_t* launches);
+int hymor_synchronize(hymor_ctx* ctx);
+/* Benchmark helper (no reference counterpart): nsteps x ADVECT_FLOW, each step preceded,
+ * outside its timed window, by a write of flush_bytes to a scratch buffer (evicts the
+ * L2 cache). *ms = summed device time of the steps (CUDA events on the context stream). */
+int hymor_bench_steps(hymor_ctx* ctx, int nsteps, uint64_t flush_bytes, float* ms);
+
+/* ---- Linearised operator (stencil-block Jacobian) ----
+ * Storage per output cell m (chi-fastest), neighbour slot q = (b+1)*3 + (a+1) for the
+ * input cell at offset (a, b): coef[((m*9 + q)*4 + vout)*4 + vin] = L[(m,vout),(m+(a,b),vin)]. */
+
+/* LINEARIZE_L (utils/Stability_analysis/Modal_stability_analysis/LINEARIZE_L.jl:34-69 ->
+ * LINEARIZE_EQUATIONS_NO_DISCONTINUITY.jl:42-288): coloured finite-difference Jacobian of the
+ * residual on the device, 36 perturbed residuals batched. Keeps the blocks on the device. */
+int hymor_linearize(hymor_ctx* ctx);
+/* Copy the blocks out (Nchi*Neta*144 doubles) / in. */
+int hymor_jacobian_get(hymor_ctx* ctx, double* coef);
+int hymor_jacobian_set(hymor_ctx* ctx, const double* coef);
+/* Y = L X (transpose 0) or Lᵀ X (transpose 1) for k vectors (4N x k, column-major),
+ * host pointers. Replaces the CuSparse SpMV `mul!(term, A, v)` of
+ * Eigenvalues/ARNOLDI_POWER_GPU.jl:73 (and its transpose, TRANSIENT_GROWTH_DOWNSTREAM.jl:75). */
+int hymor_matvec(hymor_ctx* ctx, int k, const double* X, double* Y, int transpose);
+/* Same on device pointers (no copies). */
+int hymor_matvec_dev(hymor_ctx* ctx, int k, const double* dX, double* dY, int transpose);
+/* Y = (Σ_{j<=order} (A dt)^j / j!)^nsteps X for k vectors: POWER_METHOD!
+ * (Eigenvalues/ARNOLDI_POWER_GPU.jl:64-82); transpose uses (A dt)ᵀ (EXPONENTIAL!,
+ * Transient_growth_downstream/CONSTRUCT_C.jl:78-111). Host pointers. */
+int hymor_expm_apply(hymor_ctx* ctx, int k, double dt, int nsteps, int order, const double* X,
+                     double* Y, int transpose);
+int hymor_expm_apply_dev(hymor_ctx* ctx, int k, double dt, int nsteps, int order,
+                         const double* dX, double* dY, int transpose);
+
+/* Device buffer helpers for the *_dev entry points. */
+int hymor_device_alloc(hymor_ctx* ctx, uint64_t bytes, void** dptr);
+int hymor_device_free(hymor_ctx* ctx, void* dptr);
+int hymor_memcpy_h2d(hymor_ctx* ctx, void* dst, const void* src, uint64_t bytes);
+int hymor_memcpy_d2h(hymor_ctx* ctx, void* dst, const void* src, uint64_t bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HYMOR_H */

@@ -1,0 +1,173 @@
+"""GPU parity: libhymor (through the C ABI) against the CPU oracle on the same seeded
+inputs. Tolerance: residual 1e-12 norm-wise relative per conserved variable (the
+FP64 target of the hot path); marching and linear operators as stated per test."""
+import numpy as np
+import pytest
+
+from hymor_gb300 import case as C
+from hymor_gb300 import solver as S
+from oracle import oracle as O
+from tests.helpers import per_var_rel, rel_err
+
+pytestmark = pytest.mark.gpu
+
+RES_TOL = 1e-12
+
+
+def both(cfg, seed=1, noise=1e-6):
+    cs = C.initial_state(cfg, seed=seed, noise=noise)
+    return cs, S.Solution(cs), O.Oracle(cs)
+
+
+def compare_state(sol, orc, tol):
+    a, b = sol.get_state(), orc.get_state()
+    G = (sol.nchi + 2) * (sol.neta + 2)
+    errs = per_var_rel(a["q"], b["q"])
+    assert max(errs) < tol, errs
+    if sol.cfg.shock_enabled:
+        assert np.array_equal(a["cell_idx"], b["cell_idx"])
+        assert rel_err(a["pts_x"], b["pts_x"]) < tol
+        assert rel_err(a["pts_y"], b["pts_y"]) < tol
+        assert rel_err(a["pts_chi"], b["pts_chi"]) < tol
+    return errs
+
+
+CASES = {
+    "cylinder_100x80": lambda: C.cylinder_config(100, 80),
+    "cylinder_odd_33x17": lambda: C.cylinder_config(33, 17),
+    "cylinder_interp1_eulerian": lambda: C.cylinder_config(45, 30, shock_interp="1st", shock_formulation="Eulerian"),
+    "cylinder_interp3_adiabatic": lambda: C.cylinder_config(40, 30, shock_interp="3rd", bc_eta0="no_slip_adiabatic"),
+    "cylinder_sutherland": lambda: C.cylinder_config(64, 40, viscosity="sutherland"),
+    "cylinder_nofeedback": lambda: C.cylinder_config(50, 30, shock_feedback=False),
+    "channel_periodic": lambda: C.channel_config(36, 20),
+    "blunt_cone_axisym": lambda: C.blunt_cone_config(96, 40),
+    "cylinder_disturbed": lambda: C.cylinder_config(40, 30, disturbance_amplitude=(1e-3, 2e-3, -1e-3, 5e-3)),
+    "wall_symmetry_outflows": lambda: C.cylinder_config(
+        30, 24, shock_enabled=False, bc_chi0="symmetry", bc_chi1="outflow_subsonic", bc_eta0="no_slip_isothermal",
+        bc_eta1="outflow_supersonic"),
+    "inflow_edges": lambda: C.cylinder_config(
+        30, 24, shock_enabled=False, bc_chi0="inflow_subsonic", bc_chi1="outflow_supersonic_1st",
+        bc_eta0="no_slip_adiabatic", bc_eta1="inflow_supersonic"),
+}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_residual_parity(require_gpu, name):
+    """PDE / NON_LINEAR_DYNAMICS_NO_DISCONTINUITY: flux and the mutated state."""
+    cfg = CASES[name]()
+    cs, sol, orc = both(cfg)
+    fg = S.PDE(sol)
+    fo = orc.residual()
+    errs = per_var_rel(fg, fo)
+    assert max(errs) < RES_TOL, errs
+    compare_state(sol, orc, 1e-13)
+
+
+@pytest.mark.parametrize("name", ["cylinder_100x80", "cylinder_odd_33x17", "channel_periodic",
+                                  "blunt_cone_axisym", "cylinder_sutherland", "cylinder_interp3_adiabatic",
+                                  "cylinder_disturbed", "wall_symmetry_outflows"])
+def test_rk4_steps_parity(require_gpu, name):
+    """ADVECT_FLOW_EXPLICIT (reference Julia stage aliasing), 10 steps."""
+    cfg = CASES[name]()
+    cs, sol, orc = both(cfg)
+    S.ADVECT_FLOW(sol, 10)
+    orc.advect(10)
+    compare_state(sol, orc, 1e-11)
+    assert abs(sol.get_state()["t"] - orc.get_state()["t"]) < 1e-13 * max(1.0, orc.get_state()["t"])
+
+
+def test_rk4_classical_variant(require_gpu):
+    cfg = C.cylinder_config(40, 30, rk_variant="classical")
+    cs, sol, orc = both(cfg)
+    S.ADVECT_FLOW(sol, 10)
+    orc.advect(10)
+    compare_state(sol, orc, 1e-11)
+
+
+def test_cfl_timestep_parity(require_gpu):
+    cfg = C.cylinder_config(60, 40)
+    cs, sol, orc = both(cfg)
+    S.UPDATE_FLOW_CELLS(sol)
+    orc.update_flow_cells()
+    assert abs(S.CFL_TIMESTEP(sol) - orc.cfl()) < 1e-14 * orc.cfl()
+
+
+@pytest.mark.slow
+def test_cylinder_2000_steps_parity(require_gpu):
+    """The 100 x 80 shock-fitted cylinder marched 2000 RK4 steps at CFL 0.5: residual and
+    shock position match the oracle."""
+    cfg = C.cylinder_config(100, 80)
+    cs, sol, orc = both(cfg)
+    S.ADVECT_FLOW(sol, 2000)
+    orc.advect(2000)
+    errs = compare_state(sol, orc, 1e-9)
+    st = sol.get_state()
+    assert np.isfinite(st["q"]).all()
+    # residual of the marched state
+    fg, fo = S.PDE(sol), orc.residual()
+    assert max(per_var_rel(fg, fo)) < 1e-8, errs
+
+
+def test_jacobian_parity(require_gpu):
+    """LINEARIZE_L on the GPU against the oracle's coloured FD Jacobian. Entries are finite
+    differences with eps = 1e-8, so they agree to the FD rounding (~1e-6 of the entry
+    scale), and their action on a vector agrees far better."""
+    cfg = C.cylinder_config(36, 24)
+    cs, sol, orc = both(cfg)
+    _, L = S.LINEARIZE_L(sol)
+    cg = L.blocks()
+    co = orc.linearize()
+    assert rel_err(cg, co) < 1e-5
+    compare_state(sol, orc, 1e-13)
+
+
+@pytest.mark.parametrize("name", ["cylinder_odd_33x17", "channel_periodic"])
+def test_matvec_parity(require_gpu, name):
+    """Stencil-block matvec and transpose with the same blocks: 1e-13, and the dot-product
+    identity <L x, y> = <x, Lᵀ y> to 1e-12."""
+    cfg = CASES[name]()
+    cs, sol, orc = both(cfg)
+    co = orc.linearize()
+    L = S.LinearOperatorGPU(sol)
+    L.set_blocks(co)
+    rng = np.random.Generator(np.random.PCG64(2))
+    n = 4 * cfg.nchi * cfg.neta
+    X = rng.standard_normal((n, 5))
+    Yg = L @ X
+    for j in range(5):
+        assert rel_err(Yg[:, j], orc.matvec(co, X[:, j])) < 1e-13
+        assert rel_err((L.T @ X)[:, j], orc.matvec(co, X[:, j], transpose=True)) < 1e-13
+    x, y = X[:, 0], X[:, 1]
+    lhs, rhs = np.dot(L @ x, y), np.dot(x, L.T @ y)
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+
+
+def test_expm_parity(require_gpu):
+    """POWER_METHOD! Taylor-5 propagator: 20 steps, 3 vectors, vs the oracle."""
+    cfg = C.cylinder_config(30, 20)
+    cs, sol, orc = both(cfg)
+    co = orc.linearize()
+    L = S.LinearOperatorGPU(sol)
+    L.set_blocks(co)
+    rng = np.random.Generator(np.random.PCG64(3))
+    n = 4 * cfg.nchi * cfg.neta
+    X = rng.standard_normal((n, 3))
+    dt = 1e-4
+    Yg = L.expm(X, dt, 20)
+    for j in range(3):
+        assert rel_err(Yg[:, j], orc.expm(co, dt, 20, X[:, j])) < 1e-12
+    Yt = L.T.expm(X[:, 0], dt, 5)
+    assert rel_err(Yt, orc.expm(co, dt, 5, X[:, 0], transpose=True)) < 1e-12
+
+
+def test_shock_range_error_is_reported(require_gpu):
+    """A state whose shocked row sits at the top of the mesh is rejected with
+    HYMOR_ERR_SHOCK_RANGE, not written out of bounds."""
+    cfg = C.cylinder_config(24, 16)
+    cs = C.initial_state(cfg)
+    bad = cs.cell_idx.copy()
+    bad[3] = cfg.neta
+    with pytest.raises(S.HymorError) as e:
+        sol = S.Solution(cs)
+        sol.set_state(cs.q_flat(), cs.pts_x, cs.pts_y, cs.pts_chi, cs.pts_eta, bad, 0.0)
+    assert e.value.code == -4
