@@ -31,7 +31,8 @@ EXPORTS = [
     "hymor_timer_stop", "hymor_profile_flux", "hymor_synchronize", "hymor_linearize",
     "hymor_jacobian_get", "hymor_jacobian_set", "hymor_matvec", "hymor_matvec_dev",
     "hymor_expm_apply", "hymor_expm_apply_dev", "hymor_device_alloc", "hymor_device_free",
-    "hymor_memcpy_h2d", "hymor_memcpy_d2h", "hymor_bench_steps",
+    "hymor_memcpy_h2d", "hymor_memcpy_d2h", "hymor_bench_steps", "hymor_dot_dev",
+    "hymor_krylov_orthogonalize", "hymor_krylov_rotate", "hymor_block4_apply_dev", "hymor_memcpy_d2d",
 ]
 
 
@@ -82,7 +83,12 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "hymor_device_free": [vp, vp],
         "hymor_memcpy_h2d": [vp, vp, vp, ctypes.c_uint64],
         "hymor_memcpy_d2h": [vp, vp, vp, ctypes.c_uint64],
+        "hymor_memcpy_d2d": [vp, vp, vp, ctypes.c_uint64],
         "hymor_bench_steps": [vp, i, ctypes.c_uint64, ctypes.POINTER(ctypes.c_float)],
+        "hymor_dot_dev": [vp, ctypes.c_int64, i, vp, ctypes.c_int64, vp, dp],
+        "hymor_krylov_orthogonalize": [vp, ctypes.c_int64, i, vp, ctypes.c_int64, vp, dp, i],
+        "hymor_krylov_rotate": [vp, ctypes.c_int64, i, i, vp, ctypes.c_int64, dp],
+        "hymor_block4_apply_dev": [vp, i, vp, vp, vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)

@@ -173,9 +173,10 @@ int enqueue_step(hymor_ctx* ctx, bool with_events) {
   const double wY[4] = {0.5, 0.5, 1.0, 0.0};
   double* const F[4] = {d.F[0], d.F[1], d.F[2], d.F[3]};
   auto flux = [&](int k) -> int {
-    if (with_events) CU(cudaEventRecord(ctx->cap_ev[2 * k], st));
+    // cudaEventRecordExternal makes a real event-record node under stream capture
+    if (with_events) CU(cudaEventRecordWithFlags(ctx->cap_ev[2 * k], st, cudaEventRecordExternal));
     launch_flux(d, false, F, st);
-    if (with_events) CU(cudaEventRecord(ctx->cap_ev[2 * k + 1], st));
+    if (with_events) CU(cudaEventRecordWithFlags(ctx->cap_ev[2 * k + 1], st, cudaEventRecordExternal));
     return 0;
   };
   if (c.rk_variant == 0) {
@@ -603,13 +604,16 @@ int hymor_profile_flux(hymor_ctx* ctx, int enable, float* total_ms, int32_t* lau
     if (total_ms) *total_ms = (float)tot;
     if (launches) *launches = n;
   }
-  for (auto e : ctx->prof_ev) cudaEventDestroy(e);
-  ctx->prof_ev.clear();
-  ctx->prof_steps = 0;
+  // point the graph's event nodes back at the capture events before releasing the
+  // per-step events they reference
   if (ctx->gexec) {
     for (int k = 0; k < 8; ++k)
       if (ctx->ev_nodes[k]) CU(cudaGraphExecEventRecordNodeSetEvent(ctx->gexec, ctx->ev_nodes[k], ctx->cap_ev[k]));
   }
+  CU(cudaStreamSynchronize(ctx->stream));
+  for (auto e : ctx->prof_ev) cudaEventDestroy(e);
+  ctx->prof_ev.clear();
+  ctx->prof_steps = 0;
   ctx->profile = enable != 0;
   return 0;
 }
@@ -643,6 +647,13 @@ int hymor_memcpy_h2d(hymor_ctx* ctx, void* dst, const void* src, uint64_t bytes)
 int hymor_memcpy_d2h(hymor_ctx* ctx, void* dst, const void* src, uint64_t bytes) {
   if (!ctx) return HYMOR_ERR_INVALID;
   CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return 0;
+}
+
+int hymor_memcpy_d2d(hymor_ctx* ctx, void* dst, const void* src, uint64_t bytes) {
+  if (!ctx) return HYMOR_ERR_INVALID;
+  CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
   return 0;
 }

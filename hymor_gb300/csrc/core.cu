@@ -624,8 +624,7 @@ __global__ void __launch_bounds__(kFluxThreads, 2) k_flux(FluxArgs a) {
   double* s_rE = s_rv + NH;
   double* s_p = s_rE + NH;
   double* s_T = s_p + NH;
-  double* s_mu = s_T + NH;                   // SUTH only
-  double* s_uc = s_mu + (SUTH ? NH : 0);
+  double* s_uc = s_T + NH;
   double* s_vc = s_uc + NCOR;
   double* s_Tc = s_vc + NCOR;
   double* f_lr = s_Tc + NCOR;                // 4 x NLRF
@@ -666,10 +665,6 @@ __global__ void __launch_bounds__(kFluxThreads, 2) k_flux(FluxArgs a) {
       s_p[h] = a.p[g];
       const double T = a.T[g];
       s_T[h] = T;
-      if (SUTH) {
-        const double Ts = T * a.Tinf_inv;
-        s_mu[h] = Ts * sqrt(Ts) * (1 + a.suthS) * frcp(Ts + a.suthS);
-      }
     }
   }
   __syncthreads();
@@ -712,8 +707,9 @@ __global__ void __launch_bounds__(kFluxThreads, 2) k_flux(FluxArgs a) {
       const double dut_dt = fma(du_dt, ny, -dv_dt * nx);
       double div = dut_dt + dun_dn;
       double mre = a.mre, kq = a.kq;
-      if (SUTH) {
-        const double mu_f = (s_mu[R] + s_mu[L]) * 0.5;
+      if (SUTH) {  // Sutherland at the face temperature
+        const double Ts = (s_T[L] + s_T[R]) * 0.5 * a.Tinf_inv;
+        const double mu_f = Ts * sqrt(Ts) * (1 + a.suthS) * frcp(Ts + a.suthS);
         mre = mu_f * a.inv_Re;
         kq = mu_f * a.gk;
       }
@@ -766,7 +762,8 @@ __global__ void __launch_bounds__(kFluxThreads, 2) k_flux(FluxArgs a) {
       double div = dut_dt + dun_dn;
       double mre = a.mre, kq = a.kq;
       if (SUTH) {
-        const double mu_f = (s_mu[Tt] + s_mu[B]) * 0.5;
+        const double Ts = (s_T[B] + s_T[Tt]) * 0.5 * a.Tinf_inv;
+        const double mu_f = Ts * sqrt(Ts) * (1 + a.suthS) * frcp(Ts + a.suthS);
         mre = mu_f * a.inv_Re;
         kq = mu_f * a.gk;
       }
@@ -827,7 +824,7 @@ __global__ void __launch_bounds__(kFluxThreads, 2) k_flux(FluxArgs a) {
 
 template <bool AXI, bool SUTH>
 size_t flux_smem() {
-  return sizeof(double) * (8 * NH + (SUTH ? NH : 0) + 3 * NCOR + 4 * NLRF + 4 * NBTF + (AXI ? NLRF + NBTF : 0));
+  return sizeof(double) * (8 * NH + 3 * NCOR + 4 * NLRF + 4 * NBTF + (AXI ? NLRF + NBTF : 0));
 }
 
 // ---------------------------------------------------------------------------
@@ -954,8 +951,8 @@ struct CflArgs {
   DevMesh m;
   const int* cell_idx;
   double* scal;
-  double gamma, Pr, Re;
-  int nchi, neta, shock;
+  double gamma, Pr, Re, suthS, Tinf_inv;
+  int nchi, neta, shock, suth;
 };
 
 __global__ void __launch_bounds__(256) k_cfl(CflArgs A) {
@@ -987,7 +984,14 @@ __global__ void __launch_bounds__(256) k_cfl(CflArgs A) {
       const double Axi = 0.5 * (A.m.lr_a[i + (long)j * (nchi + 1)] + A.m.lr_a[i + 1 + (long)j * (nchi + 1)]);
       const double Aeta = 0.5 * (A.m.bt_a[i + (long)j * nchi] + A.m.bt_a[i + (long)(j + 1) * nchi]);
       const double vol = A.m.vol[c];
-      const double nu_eff = nu_c / (A.S.rho[g] * A.Re);
+      double Re_flow = A.Re;  // Re / mu* (UPDATE_CHEMISTRY_EQUILIBRIUM.jl:99-101); mu* = 1 for CPG
+      if (A.suth) {
+        const double r = A.S.rho[g];
+        const double e = (A.S.rE[g] - (A.S.ru[g] * A.S.ru[g] + A.S.rv[g] * A.S.rv[g]) / r / 2) / r;
+        const double Ts = e * A.Tinf_inv;
+        Re_flow = A.Re / (Ts * sqrt(Ts) * (1 + A.suthS) / (Ts + A.suthS));
+      }
+      const double nu_eff = nu_c / (A.S.rho[g] * Re_flow);
       const double lam_v = 2 * nu_eff * (Axi * Axi + Aeta * Aeta) / vol;
       mlam = fmax(mlam, (lam_c + lam_v) / vol);
       const double r = A.S.rho[g];
@@ -1259,6 +1263,9 @@ void launch_cfl(const DevCtx& d, cudaStream_t st) {
   A.gamma = d.cfg.gamma;
   A.Pr = d.cfg.Pr;
   A.Re = d.cfg.Re;
+  A.suthS = d.cfg.sutherland_S;
+  A.Tinf_inv = d.cfg.energy_factor / d.cfg.cv;
+  A.suth = d.cfg.viscosity_model == 1;
   A.nchi = d.nchi;
   A.neta = d.neta;
   A.shock = d.cfg.shock_enabled;

@@ -210,6 +210,98 @@ __global__ void k_planes_to_blocks(const double* pl, double* blk, long N) {
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// Krylov helpers on device-resident bases. Reductions are deterministic: stage 1
+// gives each (block, column) a fixed slice of rows and a fixed warp-shuffle tree,
+// stage 2 sums the block partials of a column in a fixed order.
+constexpr int kDotBlocks = 296;  // 2 x 148-152 SMs
+constexpr int kDotThreads = 256;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// partial[j * kDotBlocks + b] = Σ_{rows of block b} A[i + j lda] * w[i]
+__global__ void __launch_bounds__(kDotThreads) k_dot_stage1(const double* A, long lda, const double* w, long n,
+                                                            double* partial) {
+  const int j = blockIdx.y;
+  const double* a = A + (long)j * lda;
+  double acc = 0;
+  for (long i = blockIdx.x * (long)kDotThreads + threadIdx.x; i < n; i += (long)kDotBlocks * kDotThreads)
+    acc = fma(a[i], w[i], acc);
+  acc = warp_sum(acc);
+  __shared__ double red[kDotThreads / 32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < kDotThreads / 32 ? red[threadIdx.x] : 0.0;
+    v = warp_sum(v);
+    if (threadIdx.x == 0) partial[(long)j * kDotBlocks + blockIdx.x] = v;
+  }
+}
+
+// out[j] (+)= Σ_b partial[j * kDotBlocks + b]; mode 0 store, 1 add
+__global__ void k_dot_stage2(const double* partial, double* out, int mode) {
+  const int j = blockIdx.x;
+  double acc = 0;
+  for (int b = threadIdx.x; b < kDotBlocks; b += 32) acc += partial[(long)j * kDotBlocks + b];
+  acc = warp_sum(acc);
+  if (threadIdx.x == 0) out[j] = mode ? out[j] + acc : acc;
+}
+
+// w -= A[:, 0:m] h
+__global__ void __launch_bounds__(256) k_gemv_sub(const double* A, long lda, long n, int m, const double* h, double* w) {
+  extern __shared__ double sh[];
+  for (int j = threadIdx.x; j < m; j += blockDim.x) sh[j] = h[j];
+  __syncthreads();
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    double acc = 0;
+    for (int j = 0; j < m; ++j) acc = fma(A[i + (long)j * lda], sh[j], acc);
+    w[i] -= acc;
+  }
+}
+
+// dst = src / sqrt(nrm2[0])
+__global__ void k_normalize(const double* src, double* dst, long n, const double* nrm2) {
+  const double s = 1.0 / sqrt(nrm2[0]);
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) dst[i] = src[i] * s;
+}
+
+// out[:, c] = A[:, 0:m] Q[:, c] for c < k (Q column-major m x k, in global memory)
+__global__ void __launch_bounds__(128) k_rotate(const double* A, long lda, long n, int m, int k, const double* Q,
+                                                double* out, long ldo) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    for (int c0 = 0; c0 < k; c0 += 8) {
+      double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      const int nc = min(8, k - c0);
+      for (int j = 0; j < m; ++j) {
+        const double a = A[i + (long)j * lda];
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+          if (c < nc) acc[c] = fma(a, Q[j + (long)(c0 + c) * m], acc[c]);
+      }
+      for (int c = 0; c < nc; ++c) out[i + (long)(c0 + c) * ldo] = acc[c];
+    }
+  }
+}
+
+// y = blockdiag(B) x with B row-major 4x4 per cell (N x 16), vectors [v0; v1; v2; v3] x N, k columns
+__global__ void k_block4(const double* B, const double* x, double* y, long N, int k) {
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < N * k; t += (long)gridDim.x * blockDim.x) {
+    const long m = t % N;
+    const long col = t / N;
+    const double* xc = x + col * 4 * N;
+    double* yc = y + col * 4 * N;
+    const double x0 = xc[m], x1 = xc[N + m], x2 = xc[2 * N + m], x3 = xc[3 * N + m];
+    const double* b = B + m * 16;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) yc[r * N + m] = fma(b[4 * r], x0, fma(b[4 * r + 1], x1, fma(b[4 * r + 2], x2, b[4 * r + 3] * x3)));
+  }
+}
+
 int grid_for(long n, int threads) {
   long b = (n + threads - 1) / threads;
   const long cap = 152L * 16;
@@ -454,6 +546,117 @@ int hymor_expm_apply(hymor_ctx* ctx, int k, double dt, int nsteps, int order, co
   cudaFreeAsync(dy, st);
   if (r) return r;
   return cuda_check(ctx, cudaStreamSynchronize(st));
+}
+
+}  // extern "C"
+
+namespace {
+struct KrylovScratch {
+  double* partial = nullptr;
+  int cols = 0;
+  double* h = nullptr;  // device coefficients (2 x cols + 2)
+  double* tmp = nullptr;
+  long tmp_n = 0;
+};
+KrylovScratch& kscratch(hymor_ctx* ctx) {
+  static thread_local std::vector<std::pair<hymor_ctx*, KrylovScratch>> table;
+  for (auto& e : table)
+    if (e.first == ctx) return e.second;
+  table.emplace_back(ctx, KrylovScratch{});
+  return table.back().second;
+}
+int ensure_scratch(hymor_ctx* ctx, int cols, long tmp_n) {
+  KrylovScratch& k = kscratch(ctx);
+  if (cols > k.cols) {
+    void* p;
+    if (cudaMalloc(&p, sizeof(double) * (long)kDotBlocks * cols) != cudaSuccess)
+      return ctx_fail(ctx, HYMOR_ERR_CUDA, "Krylov scratch allocation failed");
+    ctx_allocs(ctx).push_back(p);
+    k.partial = static_cast<double*>(p);
+    if (cudaMalloc(&p, sizeof(double) * (2 * cols + 4)) != cudaSuccess)
+      return ctx_fail(ctx, HYMOR_ERR_CUDA, "Krylov scratch allocation failed");
+    ctx_allocs(ctx).push_back(p);
+    k.h = static_cast<double*>(p);
+    k.cols = cols;
+  }
+  if (tmp_n > k.tmp_n) {
+    void* p;
+    if (cudaMalloc(&p, sizeof(double) * tmp_n) != cudaSuccess)
+      return ctx_fail(ctx, HYMOR_ERR_CUDA, "Krylov scratch allocation failed");
+    ctx_allocs(ctx).push_back(p);
+    k.tmp = static_cast<double*>(p);
+    k.tmp_n = tmp_n;
+  }
+  return 0;
+}
+void dots(const double* A, long lda, int m, const double* w, long n, double* out, int mode, double* partial,
+          cudaStream_t st) {
+  k_dot_stage1<<<dim3(kDotBlocks, m), kDotThreads, 0, st>>>(A, lda, w, n, partial);
+  k_dot_stage2<<<m, 32, 0, st>>>(partial, out, mode);
+}
+}  // namespace
+
+extern "C" {
+
+int hymor_dot_dev(hymor_ctx* ctx, int64_t n, int m, const double* dA, int64_t lda, const double* dw, double* out) {
+  if (!ctx || n < 1 || m < 1 || !dA || !dw || !out) return HYMOR_ERR_INVALID;
+  int r = ensure_scratch(ctx, m + 1, 0);
+  if (r) return r;
+  KrylovScratch& k = kscratch(ctx);
+  cudaStream_t st = ctx_stream(ctx);
+  dots(dA, lda, m, dw, n, k.h, 0, k.partial, st);
+  cudaMemcpyAsync(out, k.h, sizeof(double) * m, cudaMemcpyDeviceToHost, st);
+  return cuda_check(ctx, cudaStreamSynchronize(st));
+}
+
+int hymor_krylov_orthogonalize(hymor_ctx* ctx, int64_t n, int m, double* dV, int64_t ldv, double* dw, double* h,
+                               int out_col) {
+  if (!ctx || n < 1 || m < 0 || !dV || !dw || !h) return HYMOR_ERR_INVALID;
+  int r = ensure_scratch(ctx, 2 * (m + 1), 0);
+  if (r) return r;
+  KrylovScratch& k = kscratch(ctx);
+  cudaStream_t st = ctx_stream(ctx);
+  const int gb = grid_for(n, 256);
+  double* h1 = k.h;           // m
+  double* nrm = k.h + 2 * (m + 1) - 1;
+  if (m > 0) {
+    for (int pass = 0; pass < 2; ++pass) {  // classical Gram-Schmidt, twice
+      double* hp = pass == 0 ? h1 : h1 + m;
+      dots(dV, ldv, m, dw, n, hp, 0, k.partial, st);
+      k_gemv_sub<<<gb, 256, sizeof(double) * m, st>>>(dV, ldv, n, m, hp, dw);
+    }
+  }
+  dots(dw, n, 1, dw, n, nrm, 0, k.partial, st);
+  if (out_col >= 0) k_normalize<<<gb, 256, 0, st>>>(dw, dV + (long)out_col * ldv, n, nrm);
+  std::vector<double> hh(2 * m + 1);
+  if (m > 0) cudaMemcpyAsync(hh.data(), h1, sizeof(double) * 2 * m, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(hh.data() + 2 * m, nrm, sizeof(double), cudaMemcpyDeviceToHost, st);
+  if ((r = cuda_check(ctx, cudaStreamSynchronize(st)))) return r;
+  for (int j = 0; j < m; ++j) h[j] = hh[j] + hh[m + j];
+  h[m] = std::sqrt(hh[2 * m]);
+  return cuda_check(ctx, cudaGetLastError());
+}
+
+int hymor_krylov_rotate(hymor_ctx* ctx, int64_t n, int m, int kk, double* dV, int64_t ldv, const double* Q) {
+  if (!ctx || n < 1 || m < 1 || kk < 1 || kk > m || !dV || !Q) return HYMOR_ERR_INVALID;
+  int r = ensure_scratch(ctx, 1, n * kk + (long)m * kk);
+  if (r) return r;
+  KrylovScratch& k = kscratch(ctx);
+  cudaStream_t st = ctx_stream(ctx);
+  double* dQ = k.tmp + n * kk;
+  cudaMemcpyAsync(dQ, Q, sizeof(double) * m * kk, cudaMemcpyHostToDevice, st);
+  k_rotate<<<grid_for(n, 128), 128, 0, st>>>(dV, ldv, n, m, kk, dQ, k.tmp, n);
+  for (int c = 0; c < kk; ++c)
+    cudaMemcpyAsync(dV + (long)c * ldv, k.tmp + (long)c * n, sizeof(double) * n, cudaMemcpyDeviceToDevice, st);
+  if ((r = cuda_check(ctx, cudaGetLastError()))) return r;
+  return cuda_check(ctx, cudaStreamSynchronize(st));
+}
+
+int hymor_block4_apply_dev(hymor_ctx* ctx, int k, const double* dB, const double* dX, double* dY) {
+  if (!ctx || k < 1 || !dB || !dX || !dY) return HYMOR_ERR_INVALID;
+  DevCtx& d = ctx_dev(ctx);
+  k_block4<<<grid_for(d.N * k, 256), 256, 0, ctx_stream(ctx)>>>(dB, dX, dY, d.N, k);
+  return cuda_check(ctx, cudaGetLastError());
 }
 
 }  // extern "C"

@@ -1,0 +1,123 @@
+"""Device-resident Krylov–Schur eigensolver over libhymor.
+
+The reference runs Arpack's implicitly restarted Arnoldi on the host and ships
+every Krylov vector host→device→host around a CuSparse propagation
+(Eigenvalues/EIGENVALUES.jl:153-159, ARNOLDI_POWER_GPU.jl:36-45). Here the Krylov
+basis stays in HBM: the operator, the classical Gram–Schmidt (twice) with
+deterministic device reductions and the restart rotation all run through the C
+ABI, and only the small projected matrix (<= ncv x ncv) comes back to the host,
+where its Schur form is computed (Stewart's Krylov–Schur restart, SIAM J. Matrix
+Anal. Appl. 23 (2001) 601-614).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import scipy.linalg as sla
+
+from ._lib import HymorError, dp
+
+
+class DeviceBuffer:
+    """A device allocation owned by a libhymor context."""
+
+    def __init__(self, ctx, nbytes: int):
+        self.ctx = ctx
+        self.ptr = ctypes.c_void_p()
+        ctx.check(ctx.L.hymor_device_alloc(ctx.h, int(nbytes), ctypes.byref(self.ptr)))
+        self.nbytes = nbytes
+
+    def addr(self, offset_doubles: int = 0) -> int:
+        return self.ptr.value + 8 * int(offset_doubles)
+
+    def upload(self, a: np.ndarray, offset_doubles: int = 0):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        self.ctx.check(self.ctx.L.hymor_memcpy_h2d(self.ctx.h, self.addr(offset_doubles), a.ctypes.data, a.nbytes))
+
+    def download(self, n: int, offset_doubles: int = 0) -> np.ndarray:
+        out = np.empty(n)
+        self.ctx.check(self.ctx.L.hymor_memcpy_d2h(self.ctx.h, out.ctypes.data, self.addr(offset_doubles), out.nbytes))
+        return out
+
+    def free(self):
+        if self.ptr.value:
+            self.ctx.L.hymor_device_free(self.ctx.h, self.ptr)
+            self.ptr = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def krylov_schur(ctx, n: int, apply_op, nev: int, ncv: int, tol: float = 1e-8, maxit: int = 200,
+                 seed: int = 3, symmetric: bool = False, v0: np.ndarray | None = None):
+    """Largest-magnitude eigenpairs of a real operator held on the device.
+
+    apply_op(src_addr, dst_addr) writes OP(v) for device vectors of length n.
+    Returns (theta, resid, nops): Ritz values, their residual norms ||OP x - theta x||
+    (x of unit norm) and the number of operator applications."""
+    if not (0 < nev < ncv):
+        raise HymorError(-1, "need 0 < nev < ncv")
+    L = ctx.L
+    V = DeviceBuffer(ctx, 8 * n * (ncv + 1))
+    w = DeviceBuffer(ctx, 8 * n)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    x0 = rng.standard_normal(n) if v0 is None else np.asarray(v0, dtype=np.float64)
+    V.upload(x0 / np.linalg.norm(x0))
+    H = np.zeros((ncv + 1, ncv))
+    h = np.empty(ncv + 2)
+    p = 0       # columns of the current Krylov decomposition already built
+    nops = 0
+    theta = resid = None
+    for it in range(maxit):
+        for j in range(p, ncv):
+            apply_op(V.addr(j * n), w.addr())
+            nops += 1
+            ctx.check(L.hymor_krylov_orthogonalize(ctx.h, n, j + 1, V.ptr, n, w.ptr, dp(h), j + 1))
+            H[: j + 1, j] = h[: j + 1]
+            H[j + 1, j] = h[j + 1]
+            if h[j + 1] == 0:
+                raise HymorError(-3, "Krylov breakdown (invariant subspace found)")
+        Hm = H[:ncv, :ncv]
+        b = H[ncv, :ncv]
+        if symmetric:
+            Hs = 0.5 * (Hm + Hm.T)
+            vals, Y = np.linalg.eigh(Hs)
+            order = np.argsort(-np.abs(vals))
+            vals, Y = vals[order], Y[:, order]
+            res = np.abs(b @ Y)
+        else:
+            vals, Y = np.linalg.eig(Hm)
+            order = np.argsort(-np.abs(vals))
+            vals, Y = vals[order], Y[:, order]
+            Y = Y / np.linalg.norm(Y, axis=0)
+            res = np.abs(b @ Y)
+        theta, resid = vals[:nev], res[:nev]
+        if np.all(resid <= tol * np.abs(theta)):
+            break
+        # Krylov-Schur restart: keep the wanted Schur vectors
+        keep = min(nev + max(2, (ncv - nev) // 2), ncv - 1)
+        if symmetric:
+            T = np.diag(vals[:keep])
+            Q = Y[:, :keep]
+        else:
+            thr = np.sort(np.abs(vals))[::-1][keep - 1]
+            Tfull, Qfull, sdim = sla.schur(Hm, output="real", sort=lambda re, im: np.hypot(re, im) >= thr * (1 - 1e-12))
+            keep = max(1, min(sdim, ncv - 1))
+            T = Tfull[:keep, :keep]
+            Q = Qfull[:, :keep]
+        Qc = np.asfortranarray(Q)
+        ctx.check(L.hymor_krylov_rotate(ctx.h, n, ncv, keep, V.ptr, n, dp(Qc)))
+        # the residual vector becomes column `keep`
+        ctx.check(L.hymor_memcpy_d2d(ctx.h, V.addr(keep * n), V.addr(ncv * n), 8 * n))
+        Hn = np.zeros_like(H)
+        Hn[:keep, :keep] = T
+        Hn[keep, :keep] = b @ Q
+        H = Hn
+        p = keep
+    V.free()
+    w.free()
+    return theta, resid, nops

@@ -175,3 +175,130 @@ def LINEARIZE_L(s: Solution):
     residual, assembled on the GPU. Returns (s, L)."""
     s.ctx.check(s.ctx.L.hymor_linearize(s.ctx.h))
     return s, LinearOperatorGPU(s)
+
+
+# ---------------------------------------------------------------------------
+# Stability drivers over the device-resident Krylov solver
+
+
+def _expm_op(s: Solution, dt: float, nsteps: int, order: int, transpose: int = 0):
+    L, h = s.ctx.L, s.ctx.h
+
+    def apply(src, dst):
+        s.ctx.check(L.hymor_expm_apply_dev(h, 1, float(dt), int(nsteps), int(order), src, dst, int(transpose)))
+    return apply
+
+
+def EIGENVALUES(L: LinearOperatorGPU, s: Solution, n_modes: int, T_ref: float = 0.5, ncv: int | None = None,
+                tol: float = 1e-8, order: int = 5, method: str = "device", seed: int = 3, maxit: int = 300):
+    """EIGENVALUES_GPU_ARNOLDI (Eigenvalues/EIGENVALUES.jl:112-205): the n_modes eigenvalues of
+    largest magnitude of exp(L T_ref) (Taylor-`order` steps of the CFL dt), mapped back as
+    lambda = log(mu) / (dt * timesteps).
+
+    method "device": Krylov-Schur with the basis in HBM (hymor_gb300/krylov.py).
+    method "host":   the reference's structure, ARPACK on the host calling one GPU
+                     propagation per Krylov vector with a host round trip."""
+    import time
+    dt = CFL_TIMESTEP(s)
+    timesteps = int(round(T_ref / dt))
+    n = 4 * s.N
+    ncv = ncv or max(2 * n_modes + 1, 20)
+    t0 = time.perf_counter()
+    if method == "device":
+        from .krylov import krylov_schur
+        mu, resid, nops = krylov_schur(s.ctx, n, _expm_op(s, dt, timesteps, order), n_modes, ncv, tol=tol,
+                                       maxit=maxit, seed=seed)
+    elif method == "host":
+        from scipy.sparse.linalg import LinearOperator, eigs
+        count = [0]
+
+        def mv(x):
+            count[0] += 1
+            return L.expm(np.ascontiguousarray(x, dtype=np.float64).ravel(), dt, timesteps, order)
+        rng = np.random.Generator(np.random.PCG64(seed))
+        mu = eigs(LinearOperator((n, n), matvec=mv, dtype=np.float64), k=n_modes, which="LM", tol=tol, ncv=ncv,
+                  v0=rng.standard_normal(n), maxiter=maxit * n_modes, return_eigenvectors=False)
+        mu = mu[np.argsort(-np.abs(mu))]
+        resid = np.full(len(mu), np.nan)
+        nops = count[0]
+    else:
+        raise HymorError(-1, f"unknown method {method!r}")
+    elapsed = time.perf_counter() - t0
+    lam = np.log(mu.astype(complex)) / (dt * timesteps)
+    return lam, dict(mu=mu, resid=resid, dt=dt, timesteps=timesteps, nops=nops, seconds=elapsed)
+
+
+def chu_blocks(s: Solution, norms=(1, 1, 1, 1)):
+    """Per-cell 4x4 blocks of C0 = R'MR and D = R'M^R (CONSTRUCT_R.jl:24-133, CONSTRUCT_M.jl:27-94,
+    CONSTRUCT_M_HAT.jl:25-105) from the current state; host-side set-up like the reference's."""
+    v = s.var()
+    g = s.cfg.gamma
+    rho = v["rho"][1:-1, 1:-1].ravel(order="F")
+    u = (v["rho_u"][1:-1, 1:-1] / v["rho"][1:-1, 1:-1]).ravel(order="F")
+    w = (v["rho_v"][1:-1, 1:-1] / v["rho"][1:-1, 1:-1]).ravel(order="F")
+    rE = v["rho_E"][1:-1, 1:-1].ravel(order="F")
+    p = (rE - (rho * u * u + rho * w * w) / 2) * (g - 1)
+    a = np.sqrt(g * p / rho)
+    N = s.N
+    R = np.zeros((N, 4, 4))
+    R[:, 0, 0] = (g - 1) * (u**2 + w**2) / 2
+    R[:, 0, 1] = -u * (g - 1)
+    R[:, 0, 2] = -w * (g - 1)
+    R[:, 0, 3] = g - 1
+    R[:, 1, 0] = -u / rho
+    R[:, 1, 1] = 1.0 / rho
+    R[:, 2, 0] = -w / rho
+    R[:, 2, 2] = 1.0 / rho
+    R[:, 3, 0] = (u**2 + w**2) / (2 * p) - g / (g - 1) / rho
+    R[:, 3, 1] = -u / p
+    R[:, 3, 2] = -w / p
+    R[:, 3, 3] = 1.0 / p
+    vol = s.case.mesh["vol"].ravel(order="F")
+    st = s.get_state()
+    flow = (np.arange(1, s.neta + 1)[None, :] < st["cell_idx"][:, None]).ravel(order="F") if s.cfg.shock_enabled \
+        else np.ones(N)
+    mh = np.stack([rho * a**2 / (2 * (g * p) ** 2), rho / 2, rho / 2, (g - 1) * p / (2 * g)], axis=1) * vol[:, None]
+    mh = mh * np.asarray(norms, dtype=float)[None, :]
+    m = mh * flow[:, None]
+    C0 = np.einsum("nki,nk,nkj->nij", R, m, R)
+    D = np.einsum("nki,nk,nkj->nij", R, mh, R)
+    return C0, D
+
+
+def TRANSIENT_GROWTH_DOWNSTREAM(L: LinearOperatorGPU, s: Solution, n_modes: int, T: float, ncv: int | None = None,
+                                tol: float = 1e-8, order: int = 5, seed: int = 4, maxit: int = 300):
+    """TRANSIENT_GROWTH_DOWNSTREAM (TRANSIENT_GROWTH_DOWNSTREAM.jl:34-153): optimal energy gains
+    G(T), the largest eigenvalues of exp(Lᵀ T) R'MR exp(L T) x = G R'M^R x. The generalised
+    symmetric problem is reduced with the per-cell Cholesky factor of R'M^R (D = K Kᵀ) to
+    K^{-1} Pᵀ C0 P K^{-ᵀ} y = G y and solved by Krylov-Schur (Lanczos with full
+    reorthogonalisation) on the device; the forward propagation P and its adjoint Pᵀ are
+    Taylor-`order` steps of dt = T / round(T / dt_CFL)."""
+    import time
+    from .krylov import DeviceBuffer, krylov_schur
+    dt_cfl = CFL_TIMESTEP(s)
+    n_t = int(round(T / dt_cfl))
+    dt = T / n_t
+    C0, D = chu_blocks(s)
+    K = np.linalg.cholesky(D)
+    Kinv = np.linalg.inv(K)
+    KinvT = np.transpose(Kinv, (0, 2, 1))
+    n = 4 * s.N
+    bufs = [DeviceBuffer(s.ctx, 8 * s.N * 16) for _ in range(3)]
+    for b, arr in zip(bufs, (C0, Kinv, KinvT)):
+        b.upload(np.ascontiguousarray(arr.reshape(-1)))
+    t1, t2 = DeviceBuffer(s.ctx, 8 * n), DeviceBuffer(s.ctx, 8 * n)
+    Lh, h = s.ctx.L, s.ctx.h
+
+    def apply(src, dst):
+        s.ctx.check(Lh.hymor_block4_apply_dev(h, 1, bufs[2].ptr, src, t1.ptr))            # x = K^-T y
+        s.ctx.check(Lh.hymor_expm_apply_dev(h, 1, dt, n_t, order, t1.ptr, t2.ptr, 0))      # P x
+        s.ctx.check(Lh.hymor_block4_apply_dev(h, 1, bufs[0].ptr, t2.ptr, t1.ptr))          # C0 P x
+        s.ctx.check(Lh.hymor_expm_apply_dev(h, 1, dt, n_t, order, t1.ptr, t2.ptr, 1))      # Pᵀ C0 P x
+        s.ctx.check(Lh.hymor_block4_apply_dev(h, 1, bufs[1].ptr, t2.ptr, dst))             # K^-1 (...)
+    ncv = ncv or max(2 * n_modes + 1, 16)
+    t0 = time.perf_counter()
+    gains, resid, nops = krylov_schur(s.ctx, n, apply, n_modes, ncv, tol=tol, maxit=maxit, seed=seed, symmetric=True)
+    elapsed = time.perf_counter() - t0
+    for b in bufs + [t1, t2]:
+        b.free()
+    return np.real(gains), dict(resid=resid, dt=dt, n_t=n_t, T_opt=n_t * dt, nops=nops, seconds=elapsed)

@@ -160,11 +160,31 @@ int hymor_expm_apply(hymor_ctx* ctx, int k, double dt, int nsteps, int order, co
 int hymor_expm_apply_dev(hymor_ctx* ctx, int k, double dt, int nsteps, int order,
                          const double* dX, double* dY, int transpose);
 
+/* ---- Device-resident Krylov building blocks (replace the host Arpack loop around the
+ * GPU matvec, Eigenvalues/EIGENVALUES.jl:159 and TRANSIENT_GROWTH_DOWNSTREAM.jl:103).
+ * Reductions are deterministic (fixed block partition, fixed-order trees). */
+/* out[j] = A[:, j] . w for j < m (A device, column stride lda); out on the host. */
+int hymor_dot_dev(hymor_ctx* ctx, int64_t n, int m, const double* dA, int64_t lda, const double* dw,
+                  double* out);
+/* Classical Gram-Schmidt twice of device vector w against V[:, 0:m]; h[0..m-1] = the
+ * coefficients, h[m] = ||w|| after orthogonalisation (host array of m+1); if out_col >= 0
+ * the normalised w is written to V[:, out_col]. */
+int hymor_krylov_orthogonalize(hymor_ctx* ctx, int64_t n, int m, double* dV, int64_t ldv,
+                               double* dw, double* h, int out_col);
+/* V[:, 0:k] = V[:, 0:m] Q with Q host, column-major m x k (Krylov-Schur restart). */
+int hymor_krylov_rotate(hymor_ctx* ctx, int64_t n, int m, int k, double* dV, int64_t ldv,
+                        const double* Q);
+/* Y = blockdiag(B) X for k 4N-vectors; B device, row-major 4x4 per cell (N x 16). Applies
+ * the Chu-norm weights R'MR and R'M^R of CONSTRUCT_R/M/M_HAT (Transient_growth_downstream/
+ * CONSTRUCT_R.jl:24-133, CONSTRUCT_M.jl:27-94, CONSTRUCT_M_HAT.jl:25-105). */
+int hymor_block4_apply_dev(hymor_ctx* ctx, int k, const double* dB, const double* dX, double* dY);
+
 /* Device buffer helpers for the *_dev entry points. */
 int hymor_device_alloc(hymor_ctx* ctx, uint64_t bytes, void** dptr);
 int hymor_device_free(hymor_ctx* ctx, void* dptr);
 int hymor_memcpy_h2d(hymor_ctx* ctx, void* dst, const void* src, uint64_t bytes);
 int hymor_memcpy_d2h(hymor_ctx* ctx, void* dst, const void* src, uint64_t bytes);
+int hymor_memcpy_d2d(hymor_ctx* ctx, void* dst, const void* src, uint64_t bytes);
 
 #ifdef __cplusplus
 }

@@ -756,23 +756,20 @@ void apply_boundary_conditions(const orc_config& c, const Mesh& m, State& s) {
 
 // ---------------------------------------------------------------------------
 // Transport coefficients: CPG constant mu* = k* = 1
-// (UPDATE_CHEMISTRY_EQUILIBRIUM.jl:103-124); the Sutherland extension evaluates
-// mu* = T*^{3/2} (1 + S*) / (T* + S*) with T* = T / T_inf, k* = mu*.
-void transport(const orc_config& c, const State& s, vec& mu, vec& kk) {
-  const int G = (c.nchi + 2) * (c.neta + 2);
-  mu.assign(G, 1.0);
-  kk.assign(G, 1.0);
-  if (c.viscosity_model == 1) {
-    const double T_inf = c.cv * 1.0 / c.energy_factor;  // non-dimensional freestream temperature
-    const double S = c.sutherland_S;
-    for (int k = 0; k < G; ++k) {
-      double Ts = s.T[k] / T_inf;
-      double v = Ts * std::sqrt(Ts) * (1 + S) / (Ts + S);
-      mu[k] = v;
-      kk[k] = v;
+// (UPDATE_CHEMISTRY_EQUILIBRIUM.jl:103-124), averaged to faces as in VISCOUS_FLUX.jl:136-137.
+// Sutherland extension: mu* = T*^{3/2} (1 + S*) / (T* + S*), k* = mu*, evaluated at the
+// face temperature T* = (T_L + T_R) / (2 T_inf) (on a wall face this is the wall value).
+struct Transport {
+  int model;
+  double S, Tinf_inv;
+  double face(double TL, double TR, double muL = 1.0, double muR = 1.0) const {
+    if (model == 1) {
+      double Ts = (TL + TR) / 2 * Tinf_inv;
+      return Ts * std::sqrt(Ts) * (1 + S) / (Ts + S);
     }
+    return (muR + muL) / 2;
   }
-}
+};
 
 // utils/Operators/FLUX_MASS.jl:1-44, FLUX_MOMENTUM.jl:1-75, FLUX_TOTAL_ENERGY.jl:1-55,
 // and the *_3D variants (FLUX_MOMENTUM_3D.jl:120-125 adds the front/back pressure term).
@@ -874,8 +871,7 @@ void viscous_flux(const orc_config& c, const Mesh& m, State& s) {
   const double Re_infty = c.Re, gamma_star_fs = c.gamma, Pr_fs = c.Pr;
   const int NI = nchi + 2, NJ = neta + 2;
   const int G = NI * NJ;
-  vec mu, kk;
-  transport(c, s, mu, kk);
+  const Transport tr{c.viscosity_model, c.sutherland_S, c.energy_factor / c.cv};
   vec u(G), v(G);
 #pragma omp parallel for schedule(static)
   for (int k = 0; k < G; ++k) { u[k] = s.rho_u[k] / s.rho[k]; v[k] = s.rho_v[k] / s.rho[k]; }
@@ -918,7 +914,7 @@ void viscous_flux(const orc_config& c, const Mesh& m, State& s) {
       double dut_dn1 = du_dn1 * yn - dv_dn1 * xn;
       double dun_dt1 = -du_dt1 * xn - dv_dt1 * yn;
       double dut_dt1 = du_dt1 * yn - dv_dt1 * xn;
-      double mu_1 = (mu[Rr] + mu[L]) / 2;
+      double mu_1 = tr.face(T[L], T[Rr]);
       double div_1 = dut_dt1 + dun_dn1;
       double u_face_1 = 0, x_face_1 = 1;
       if (c.axisymmetric) {
@@ -935,7 +931,7 @@ void viscous_flux(const orc_config& c, const Mesh& m, State& s) {
       double u_1 = (s.rho_u[L] + s.rho_u[Rr]) * inv_rho_1;
       double v_1 = (s.rho_v[L] + s.rho_v[Rr]) * inv_rho_1;
       w1[f] = u_1 * tau_1x[f] + v_1 * tau_1y[f];
-      double k_lr = (kk[Rr] + kk[L]) / 2 * gamma_star_fs / Re_infty / Pr_fs;
+      double k_lr = tr.face(T[L], T[Rr]) * gamma_star_fs / Re_infty / Pr_fs;
       double dT_dc1 = -(T[Rr] - T[L]) / cld;
       double dT_dt1 = (T_c[d.cni(i, j + 1)] - T_c[d.cni(i, j)]) / lr_dist;
       double dT_dn1 = (dT_dc1 - dT_dt1 * Cn1_Ft1) / divide1;
@@ -966,7 +962,7 @@ void viscous_flux(const orc_config& c, const Mesh& m, State& s) {
       double dun_dt2 = du_dt2 * xn + dv_dt2 * yn;
       double dut_dn2 = du_dn2 * yn - dv_dn2 * xn;
       double dun_dn2 = du_dn2 * xn + dv_dn2 * yn;
-      double mu_2 = (mu[Tt] + mu[B]) / 2;
+      double mu_2 = tr.face(T[B], T[Tt]);
       double div_2 = dut_dt2 + dun_dn2;
       double u_face_2 = 0, x_face_2 = 1;
       if (c.axisymmetric) {
@@ -983,7 +979,7 @@ void viscous_flux(const orc_config& c, const Mesh& m, State& s) {
       double u_2 = (s.rho_u[B] + s.rho_u[Tt]) * inv_rho_2;
       double v_2 = (s.rho_v[B] + s.rho_v[Tt]) * inv_rho_2;
       w2[f] = u_2 * tau_2x[f] + v_2 * tau_2y[f];
-      double k_bt = (kk[Tt] + kk[B]) / 2 * gamma_star_fs / Re_infty / Pr_fs;
+      double k_bt = tr.face(T[B], T[Tt]) * gamma_star_fs / Re_infty / Pr_fs;
       double dT_dc2 = (T[Tt] - T[B]) / cbd;
       double dT_dt2 = -(T_c[d.cni(i + 1, j)] - T_c[d.cni(i, j)]) / bt_dist;
       double dT_dn2 = (Cn2_Ft2 * dT_dt2 - dT_dc2) / divide;
@@ -1063,7 +1059,14 @@ double cfl_timestep(const orc_config& c, const Mesh& m, const State& s) {
       double lam_c = lam_xi + lam_eta;
       double A_xi = 0.5 * (m.lr_a[d.lri(i, j)] + m.lr_a[d.lri(i + 1, j)]);
       double A_eta = 0.5 * (m.bt_a[d.bti(i, j)] + m.bt_a[d.bti(i, j + 1)]);
-      double nu_eff = std::max(4.0 / 3.0, c.gamma / c.Pr) / (R[g] * c.Re);
+      // Re_flow = Re / mu* (UPDATE_CHEMISTRY_EQUILIBRIUM.jl:99-101); mu* = 1 for CPG
+      double Re_flow = c.Re;
+      if (c.viscosity_model == 1) {
+        double e = (s.rho_E[g] - (s.rho_u[g] * s.rho_u[g] + s.rho_v[g] * s.rho_v[g]) / R[g] / 2) / R[g];
+        double Ts = e / (c.cv / c.energy_factor);
+        Re_flow = c.Re / (Ts * std::sqrt(Ts) * (1 + c.sutherland_S) / (Ts + c.sutherland_S));
+      }
+      double nu_eff = std::max(4.0 / 3.0, c.gamma / c.Pr) / (R[g] * Re_flow);
       double lam_v = 2 * nu_eff * (A_xi * A_xi + A_eta * A_eta) / m.vol[k];
       double flowk = c.shock_enabled ? s.flow[k] : 1.0;
       double lov = (lam_c + lam_v) * flowk / m.vol[k];
