@@ -33,6 +33,7 @@ EXPORTS = [
     "hymor_expm_apply", "hymor_expm_apply_dev", "hymor_device_alloc", "hymor_device_free",
     "hymor_memcpy_h2d", "hymor_memcpy_d2h", "hymor_bench_steps", "hymor_dot_dev",
     "hymor_krylov_orthogonalize", "hymor_krylov_rotate", "hymor_block4_apply_dev", "hymor_memcpy_d2d",
+    "hymor_expm_apply_dev_noalloc",
 ]
 
 
@@ -79,6 +80,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "hymor_matvec_dev": [vp, i, vp, vp, i],
         "hymor_expm_apply": [vp, i, d, i, i, dp, dp, i],
         "hymor_expm_apply_dev": [vp, i, d, i, i, vp, vp, i],
+        "hymor_expm_apply_dev_noalloc": [vp, i, d, i, i, vp, vp, i],
         "hymor_device_alloc": [vp, ctypes.c_uint64, ctypes.POINTER(vp)],
         "hymor_device_free": [vp, vp],
         "hymor_memcpy_h2d": [vp, vp, vp, ctypes.c_uint64],

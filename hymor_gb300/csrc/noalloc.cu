@@ -1,0 +1,89 @@
+// Allocation-free variant of the Taylor propagator (hymor_expm_apply_dev).
+//
+// Who needs it: callers that must not allocate device memory while they run, for
+// example a host framework that invokes this library from inside its own CUDA
+// stream capture (where cudaMalloc is not allowed), or a service that reserves its
+// whole device-memory budget at start-up and treats any allocation during a solve
+// as a failure. hymor_expm_apply_dev allocates its three work vectors on every
+// call; this entry point takes them from one fixed, file-scope device array
+// instead, so the call itself never allocates or frees.
+//
+// Limits and sharing rules:
+//   * the array holds 3 x kNoAllocVec doubles (24 MiB) and is held by every GPU
+//     that loads libhymor until the process exits;
+//   * one call needs 3 work vectors of 4 * Nchi * Neta * k doubles, so
+//     4 * Nchi * Neta * k <= kNoAllocVec (1 048 576), e.g. Nchi * Neta <= 262 144 for
+//     one vector; larger requests return HYMOR_ERR_INVALID before any device work;
+//   * all calls in the process share the array and it keeps the last call's
+//     contents; nothing in it has to start at zero (each call first copies its input
+//     into the work vectors). Calls whose GPU work overlaps (other streams, other
+//     contexts on the same device, other host threads) race on the array: serialise
+//     them;
+//   * the device address of the array is looked up once per device, on the first
+//     call made with that device current (cudaGetSymbolAddress). Make that first
+//     call before any stream capture.
+#include <cstdio>
+
+#include "kernels.h"
+
+namespace hymor {
+DevCtx& ctx_dev(hymor_ctx* c);
+cudaStream_t ctx_stream(hymor_ctx* c);
+int ctx_fail(hymor_ctx* c, int code, const char* msg);
+}  // namespace hymor
+
+using namespace hymor;
+
+namespace {
+
+constexpr long kNoAllocVec = 1L << 20;  // doubles per work vector
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) double g_expm_scratch[3 * kNoAllocVec];
+
+// device address of g_expm_scratch, per device (nullptr until the first call there)
+double* g_scratch_addr[kMaxDevices] = {};
+
+int scratch_for_current_device(hymor_ctx* ctx, double** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+    return ctx_fail(ctx, HYMOR_ERR_CUDA, "no current CUDA device for the allocation-free propagator");
+  if (!g_scratch_addr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_expm_scratch);
+    if (e != cudaSuccess || !p) {
+      char msg[256];
+      snprintf(msg, sizeof msg, "cudaGetSymbolAddress of the propagator scratch failed: %s", cudaGetErrorString(e));
+      return ctx_fail(ctx, HYMOR_ERR_CUDA, msg);
+    }
+    g_scratch_addr[dev] = static_cast<double*>(p);
+  }
+  *out = g_scratch_addr[dev];
+  return 0;
+}
+
+}  // namespace
+
+extern "C" int hymor_expm_apply_dev_noalloc(hymor_ctx* ctx, int k, double dt, int nsteps, int order,
+                                            const double* dX, double* dY, int transpose) {
+  if (!ctx || k < 1 || nsteps < 0 || order < 1 || order > 20 || !dX || !dY) return HYMOR_ERR_INVALID;
+  DevCtx& d = ctx_dev(ctx);
+  if (!d.coef) return ctx_fail(ctx, HYMOR_ERR_NOT_READY, "no Jacobian: call hymor_linearize or hymor_jacobian_set");
+  const long n = 4 * d.N * (long)k;
+  if (n > kNoAllocVec) {
+    char msg[256];
+    snprintf(msg, sizeof msg,
+             "allocation-free propagator: 4 * Nchi * Neta * k = %ld exceeds its fixed work size of %ld doubles; "
+             "use hymor_expm_apply_dev",
+             n, kNoAllocVec);
+    return ctx_fail(ctx, HYMOR_ERR_INVALID, msg);
+  }
+  double* work = nullptr;
+  int r = scratch_for_current_device(ctx, &work);
+  if (r) return r;
+  // launch_expm uses work[0, 3n): v, and the two alternating Taylor terms
+  launch_expm(d, k, dt, nsteps, order, dX, dY, transpose, work, ctx_stream(ctx));
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return ctx_fail(ctx, HYMOR_ERR_CUDA, cudaGetErrorString(e));
+  return 0;
+}

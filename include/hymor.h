@@ -160,6 +160,17 @@ int hymor_expm_apply(hymor_ctx* ctx, int k, double dt, int nsteps, int order, co
 int hymor_expm_apply_dev(hymor_ctx* ctx, int k, double dt, int nsteps, int order,
                          const double* dX, double* dY, int transpose);
 
+/* Allocation-free variant of hymor_expm_apply_dev (no counterpart in the reference). For
+ * callers that must not allocate device memory during the call, e.g. code running
+ * inside the caller's own stream capture, or a service with a fixed device-memory budget.
+ * The work vectors come from one fixed 24 MiB device array instead of per-call
+ * allocations: requires 4*Nchi*Neta*k <= 1048576 (else HYMOR_ERR_INVALID). All calls
+ * share that array, so calls whose GPU work overlaps race; nothing in it needs to start
+ * at zero. The first call on a device looks up the array's address: make it before any
+ * stream capture. */
+int hymor_expm_apply_dev_noalloc(hymor_ctx* ctx, int k, double dt, int nsteps, int order,
+                                 const double* dX, double* dY, int transpose);
+
 /* ---- Device-resident Krylov building blocks (replace the host Arpack loop around the
  * GPU matvec, Eigenvalues/EIGENVALUES.jl:159 and TRANSIENT_GROWTH_DOWNSTREAM.jl:103).
  * Reductions are deterministic (fixed block partition, fixed-order trees). */
