@@ -11,6 +11,7 @@
 
 namespace hymor {
 void flux_kernel_setup();
+void expm_cache_release(void* p);
 }
 
 using namespace hymor;
@@ -18,23 +19,29 @@ using namespace hymor;
 struct hymor_ctx_s {
   DevCtx d;
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;      // high-priority stream of the shock/BC chain inside the step graph
+  cudaEvent_t fork_ev[8] = {}, join_ev[8] = {};
   int device = 0;
   std::string err;
   std::vector<void*> allocs;
   // step graph
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
-  // flux-kernel profiling: 8 event-record nodes (start/stop of the 4 flux launches)
+  // flux-kernel profiling: event-record nodes around the flux launches of the 4 stages
+  // (2 launches per stage: interior tiles, then the shock/boundary tiles)
   bool profile = false;
-  cudaGraphNode_t ev_nodes[8] = {};
-  cudaEvent_t cap_ev[8] = {};
-  std::vector<cudaEvent_t> prof_ev;  // 8 per profiled step
+  static constexpr int kEv = 16;
+  cudaGraphNode_t ev_nodes[kEv] = {};
+  cudaEvent_t cap_ev[kEv] = {};
+  std::vector<cudaEvent_t> prof_ev;  // kEv per profiled step
   int prof_steps = 0;
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   int timer_running = 0;
   // L2 flush scratch of hymor_bench_steps
   void* flush_buf = nullptr;
   uint64_t flush_bytes = 0;
+  // replayed propagator graphs and their buffers (linear.cu)
+  void* expm_cache = nullptr;
 };
 
 namespace {
@@ -107,7 +114,7 @@ int upload(hymor_ctx* ctx, double** dst, const double* src, size_t n, const char
 // host in FP64 from the reference's mesh arrays (VISCOUS_FLUX.jl:72-95).
 void face_geometry(const hymor_config& c, const hymor_mesh& m, std::vector<double>& lrg,
                    std::vector<double>& btg, std::vector<double>& rvol, std::vector<double>& rxl,
-                   std::vector<double>& rxb) {
+                   std::vector<double>& rxb, std::vector<double>& gvis) {
   const int nchi = c.nchi, neta = c.neta;
   const long NLR = (long)(nchi + 1) * neta, NBT = (long)nchi * (neta + 1), N = (long)nchi * neta;
   lrg.assign(kGeoPlanes * NLR, 0.0);
@@ -158,50 +165,94 @@ void face_geometry(const hymor_config& c, const hymor_mesh& m, std::vector<doubl
       rxb[f] = 1.0 / ((X(i + 1, j + 1) + X(i + 1, j)) / 2);
     }
   for (long k = 0; k < N; ++k) rvol[k] = 1.0 / m.vol[k];
+  gvis.assign(N, 0.0);
+  for (int j = 0; j < neta; ++j)
+    for (int i = 0; i < nchi; ++i) {
+      const long k = i + (long)j * nchi;
+      const double Axi = 0.5 * (m.lr_a[i + (long)j * (nchi + 1)] + m.lr_a[i + 1 + (long)j * (nchi + 1)]);
+      const double Aeta = 0.5 * (m.bt_a[i + (long)j * nchi] + m.bt_a[i + (long)(j + 1) * nchi]);
+      gvis[k] = 2 * (Axi * Axi + Aeta * Aeta) / m.vol[k];
+    }
 }
 
 int enqueue_step(hymor_ctx* ctx, bool with_events) {
   DevCtx& d = ctx->d;
-  cudaStream_t st = ctx->stream;
+  cudaStream_t st = ctx->stream, sx = ctx->side;
   const hymor_config& c = d.cfg;
   const bool shock = c.shock_enabled;
-  CU(cudaMemsetAsync(d.scal + kCmax, 0, 3 * sizeof(double), st));
-  if (shock) launch_flow_cells(d, st);
-  launch_sound_cmax(d, shock, st);
-  launch_cfl(d, st);
   const double wA[4] = {1.0 / 6, 1.0 / 3, 1.0 / 3, 1.0 / 6};
   const double wY[4] = {0.5, 0.5, 1.0, 0.0};
   double* const F[4] = {d.F[0], d.F[1], d.F[2], d.F[3]};
-  auto flux = [&](int k) -> int {
-    // cudaEventRecordExternal makes a real event-record node under stream capture
-    if (with_events) CU(cudaEventRecordWithFlags(ctx->cap_ev[2 * k], st, cudaEventRecordExternal));
-    launch_flux(d, false, F, st);
-    if (with_events) CU(cudaEventRecordWithFlags(ctx->cap_ev[2 * k + 1], st, cudaEventRecordExternal));
+  int nf = 0, nj = 0;
+  auto fork = [&]() -> int {  // side stream waits for the work enqueued so far on the main stream
+    CU(cudaEventRecord(ctx->fork_ev[nf], st));
+    CU(cudaStreamWaitEvent(sx, ctx->fork_ev[nf], 0));
+    ++nf;
     return 0;
   };
+  auto join = [&]() -> int {  // main stream waits for the side stream
+    CU(cudaEventRecord(ctx->join_ev[nj], sx));
+    CU(cudaStreamWaitEvent(st, ctx->join_ev[nj], 0));
+    ++nj;
+    return 0;
+  };
+  auto ev = [&](int k) -> int {
+    // cudaEventRecordExternal makes a real event-record node under stream capture
+    if (with_events) CU(cudaEventRecordWithFlags(ctx->cap_ev[k], st, cudaEventRecordExternal));
+    return 0;
+  };
+  CU(cudaMemsetAsync(d.scal + kCmax, 0, 3 * sizeof(double), st));
+  if (shock) launch_flow_cells(d, st);
   if (c.rk_variant == 0) {
+    // Side stream: the CFL reduction, and every smoothing-spline fit one stage early (a
+    // fit needs only the shock points, which the previous stage's jump kernel moved);
+    // then per stage the jump + boundary kernels beside the flux of the interior tiles.
+    TRY(fork());
+    launch_sound_cmax(d, shock, sx);
+    launch_cfl(d, sx);
+    launch_spline(d, false, true, sx);
     launch_update_thermo(d, 0, 0, 0, st);
-    launch_shock_bc(d, false, true, shock, wY[0], wA[0], 0, st);
-    TRY(flux(0));
-    for (int k = 1; k < 4; ++k) {
-      launch_update_thermo(d, 1, wY[k - 1], wA[k - 1], st);
-      launch_shock_bc(d, false, false, shock, wY[k], wA[k], 0, st);
-      TRY(flux(k));
+    for (int k = 0; k < 4; ++k) {
+      if (k > 0) launch_update_thermo(d, 1, wY[k - 1], wA[k - 1], st);
+      TRY(fork());
+      launch_columns_bc(d, false, shock, wY[k], wA[k], 0, true, true, sx);
+      TRY(ev(4 * k));
+      launch_flux_class(d, false, F, 0, st);
+      TRY(ev(4 * k + 1));
+      TRY(join());
+      // next fit (stage k+1 on Y, or the step-end fit on S) overlaps this stage's remaining work
+      launch_spline(d, k == 3, false, sx);
+      TRY(ev(4 * k + 2));
+      launch_flux_class(d, false, F, 1, st);
+      TRY(ev(4 * k + 3));
     }
+    launch_update_thermo(d, 2, 0, wA[3], st);
+    TRY(join());
+    launch_columns_bc(d, true, false, 0, 0, 1, true, true, st);
   } else {
+    launch_sound_cmax(d, shock, st);
+    launch_cfl(d, st);
     launch_snapshot(d, st);
     launch_update_thermo(d, 0, 0, 0, st);
     launch_shock_bc(d, false, true, shock, 0.0, wA[0], 0, st);
-    TRY(flux(0));
+    TRY(ev(0));
+    launch_flux(d, false, F, st);
+    TRY(ev(1));
+    TRY(ev(2));
+    TRY(ev(3));
     for (int k = 1; k < 4; ++k) {
       launch_classical_stage(d, wY[k - 1], st);
       launch_update_thermo(d, 5, 0, wA[k - 1], st);
       launch_shock_bc(d, false, false, shock, 0.0, wA[k], 0, st);
-      TRY(flux(k));
+      TRY(ev(4 * k));
+      launch_flux(d, false, F, st);
+      TRY(ev(4 * k + 1));
+      TRY(ev(4 * k + 2));
+      TRY(ev(4 * k + 3));
     }
+    launch_update_thermo(d, 2, 0, wA[3], st);
+    launch_shock_bc(d, true, false, false, 0, 0, 1, st);
   }
-  launch_update_thermo(d, 2, 0, wA[3], st);
-  launch_shock_bc(d, true, false, false, 0, 0, 1, st);
   launch_fill_minrho(d, true, st);
   CU(cudaGetLastError());
   return 0;
@@ -228,7 +279,7 @@ int build_graph(hymor_ctx* ctx) {
     if (ty != cudaGraphNodeTypeEventRecord) continue;
     cudaEvent_t ev;
     CU(cudaGraphEventRecordNodeGetEvent(n, &ev));
-    for (int k = 0; k < 8; ++k)
+    for (int k = 0; k < hymor_ctx_s::kEv; ++k)
       if (ctx->cap_ev[k] == ev) ctx->ev_nodes[k] = n;
   }
   return 0;
@@ -307,15 +358,16 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
   m.fb_yn_front = mesh->fb_yn_front;
   m.fb_yn_back = mesh->fb_yn_back;
   {
-    std::vector<double> lrg, btg, rvol, rxl, rxb;
-    face_geometry(*cfg, *mesh, lrg, btg, rvol, rxl, rxb);
-    double *p1, *p2, *p3, *p4, *p5;
+    std::vector<double> lrg, btg, rvol, rxl, rxb, gvis;
+    face_geometry(*cfg, *mesh, lrg, btg, rvol, rxl, rxb, gvis);
+    double *p1, *p2, *p3, *p4, *p5, *p6;
     if ((r = upload(ctx, &p1, lrg.data(), lrg.size(), "lr geometry"))) return bail(r);
     if ((r = upload(ctx, &p2, btg.data(), btg.size(), "bt geometry"))) return bail(r);
     if ((r = upload(ctx, &p3, rvol.data(), rvol.size(), "1/vol"))) return bail(r);
     if ((r = upload(ctx, &p4, rxl.data(), rxl.size(), "1/x lr"))) return bail(r);
     if ((r = upload(ctx, &p5, rxb.data(), rxb.size(), "1/x bt"))) return bail(r);
-    m.lrg = p1; m.btg = p2; m.rvol = p3; m.rx_lr = p4; m.rx_bt = p5;
+    if ((r = upload(ctx, &p6, gvis.data(), gvis.size(), "viscous CFL geometry"))) return bail(r);
+    m.lrg = p1; m.btg = p2; m.rvol = p3; m.rx_lr = p4; m.rx_bt = p5; m.gvis = p6;
   }
   auto cons = [&](Cons& q) -> int {
     TRY(dalloc(ctx, &q.rho, d.G)); TRY(dalloc(ctx, &q.ru, d.G));
@@ -342,13 +394,24 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
   if ((r = pts(d.Sp)) || (r = pts(d.Yp))) return bail(r);
   if ((r = dalloc(ctx, &d.cell_idx, d.nchi)) || (r = dalloc(ctx, &d.beta, d.nchi)) ||
       (r = dalloc(ctx, &d.speed_x, d.nchi)) || (r = dalloc(ctx, &d.speed_y, d.nchi)) ||
-      (r = dalloc(ctx, &d.rel, d.nchi)) || (r = dalloc(ctx, &d.spl, 8 * (long)d.nchi + 8)) ||
-      (r = dalloc(ctx, &d.scal, (long)kCount)) || (r = dalloc(ctx, &d.err, (long)kErrCount)))
+      (r = dalloc(ctx, &d.rel, d.nchi)) || (r = dalloc(ctx, &d.spl, 17 * (long)d.nchi + 16)) ||
+      (r = dalloc(ctx, &d.scal, (long)kCount)) || (r = dalloc(ctx, &d.err, (long)kErrCount)) ||
+      (r = dalloc(ctx, &d.cflw, d.NLR + d.NBT)))
     return bail(r);
   d.coef = nullptr;
   d.jwork = nullptr;
-  for (int k = 0; k < 8; ++k)
+  for (int k = 0; k < hymor_ctx_s::kEv; ++k)
     if (cudaEventCreate(&ctx->cap_ev[k]) != cudaSuccess) return bail(fail(ctx, HYMOR_ERR_CUDA, "event"));
+  for (int k = 0; k < 8; ++k)  // 5 forks and 5 joins per step
+    if (cudaEventCreateWithFlags(&ctx->fork_ev[k], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->join_ev[k], cudaEventDisableTiming) != cudaSuccess)
+      return bail(fail(ctx, HYMOR_ERR_CUDA, "event"));
+  {
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    if (cudaStreamCreateWithPriority(&ctx->side, cudaStreamNonBlocking, hi) != cudaSuccess)
+      return bail(fail(ctx, HYMOR_ERR_CUDA, "side stream creation failed"));
+  }
   cudaEventCreate(&ctx->t0);
   cudaEventCreate(&ctx->t1);
   cudaError_t e = cudaDeviceSynchronize();
@@ -361,10 +424,16 @@ int hymor_ctx_destroy(hymor_ctx* ctx) {
   if (!ctx) return HYMOR_ERR_INVALID;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  expm_cache_release(ctx->expm_cache);
   if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
   if (ctx->graph) cudaGraphDestroy(ctx->graph);
   for (auto e : ctx->cap_ev)
     if (e) cudaEventDestroy(e);
+  for (auto e : ctx->fork_ev)
+    if (e) cudaEventDestroy(e);
+  for (auto e : ctx->join_ev)
+    if (e) cudaEventDestroy(e);
+  if (ctx->side) cudaStreamDestroy(ctx->side);
   for (auto e : ctx->prof_ev) cudaEventDestroy(e);
   if (ctx->t0) cudaEventDestroy(ctx->t0);
   if (ctx->t1) cudaEventDestroy(ctx->t1);
@@ -478,14 +547,12 @@ int hymor_step(hymor_ctx* ctx, int nsteps) {
   TRY(build_graph(ctx));
   for (int s = 0; s < nsteps; ++s) {
     if (ctx->profile) {
-      const size_t base = ctx->prof_ev.size();
-      for (int k = 0; k < 8; ++k) {
+      for (int k = 0; k < hymor_ctx_s::kEv; ++k) {
         cudaEvent_t ev;
         CU(cudaEventCreate(&ev));
         ctx->prof_ev.push_back(ev);
         if (ctx->ev_nodes[k]) CU(cudaGraphExecEventRecordNodeSetEvent(ctx->gexec, ctx->ev_nodes[k], ev));
       }
-      (void)base;
       ctx->prof_steps++;
     }
     CU(cudaGraphLaunch(ctx->gexec, ctx->stream));
@@ -508,7 +575,7 @@ int hymor_bench_steps(hymor_ctx* ctx, int nsteps, uint64_t flush_bytes, float* m
   for (int s = 0; s < nsteps; ++s) {
     if (flush_bytes) CU(cudaMemsetAsync(ctx->flush_buf, s & 0xff, flush_bytes, ctx->stream));
     if (ctx->profile) {
-      for (int k = 0; k < 8; ++k) {
+      for (int k = 0; k < hymor_ctx_s::kEv; ++k) {
         cudaEvent_t e;
         CU(cudaEventCreate(&e));
         ctx->prof_ev.push_back(e);
@@ -594,11 +661,13 @@ int hymor_profile_flux(hymor_ctx* ctx, int enable, float* total_ms, int32_t* lau
     CU(cudaStreamSynchronize(ctx->stream));
     double tot = 0;
     int n = 0;
-    for (size_t s = 0; s + 8 <= ctx->prof_ev.size(); s += 8)
-      for (int k = 0; k < 4; ++k) {
-        float v = 0;
-        CU(cudaEventElapsedTime(&v, ctx->prof_ev[s + 2 * k], ctx->prof_ev[s + 2 * k + 1]));
-        tot += v;
+    const size_t E = hymor_ctx_s::kEv;
+    for (size_t s = 0; s + E <= ctx->prof_ev.size(); s += E)
+      for (int k = 0; k < 4; ++k) {  // one residual evaluation per stage, in two launches
+        float v1 = 0, v2 = 0;
+        CU(cudaEventElapsedTime(&v1, ctx->prof_ev[s + 4 * k], ctx->prof_ev[s + 4 * k + 1]));
+        CU(cudaEventElapsedTime(&v2, ctx->prof_ev[s + 4 * k + 2], ctx->prof_ev[s + 4 * k + 3]));
+        tot += v1 + v2;
         ++n;
       }
     if (total_ms) *total_ms = (float)tot;
@@ -607,7 +676,7 @@ int hymor_profile_flux(hymor_ctx* ctx, int enable, float* total_ms, int32_t* lau
   // point the graph's event nodes back at the capture events before releasing the
   // per-step events they reference
   if (ctx->gexec) {
-    for (int k = 0; k < 8; ++k)
+    for (int k = 0; k < hymor_ctx_s::kEv; ++k)
       if (ctx->ev_nodes[k]) CU(cudaGraphExecEventRecordNodeSetEvent(ctx->gexec, ctx->ev_nodes[k], ctx->cap_ev[k]));
   }
   CU(cudaStreamSynchronize(ctx->stream));
@@ -666,4 +735,5 @@ DevCtx& ctx_dev(hymor_ctx* c) { return c->d; }
 cudaStream_t ctx_stream(hymor_ctx* c) { return c->stream; }
 int ctx_fail(hymor_ctx* c, int code, const char* msg) { return fail(c, code, "%s", msg); }
 std::vector<void*>& ctx_allocs(hymor_ctx* c) { return c->allocs; }
+void*& ctx_expm_cache(hymor_ctx* c) { return c->expm_cache; }
 }  // namespace hymor

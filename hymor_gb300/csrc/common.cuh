@@ -37,6 +37,7 @@ struct DevMesh {
   const double* rvol;  // N
   const double* rx_lr;  // axisymmetric: 1 / x_face on lr faces (NLR)
   const double* rx_bt;  // axisymmetric: 1 / x_face on bt faces (NBT)
+  const double* gvis;   // 2 (A_xi^2 + A_eta^2) / vol per cell (viscous CFL rate, CFL_TIMESTEP.jl:110-113)
 };
 
 struct Cons {

@@ -54,8 +54,10 @@ struct UpdArgs {
   const int* cell_idx;
   const double* scal;
   unsigned* err;
+  double* aY;        // sound speed of the lines next to outflow_NRCBC edges (LODI input)
   double cY, cS, gm1;
   int nchi, neta, mode, shock;
+  int nrcbc;         // bit e set: edge e (chi0, chi1, eta0, eta1) is outflow_NRCBC
 };
 
 __global__ void __launch_bounds__(256) k_update_thermo(UpdArgs a) {
@@ -99,6 +101,12 @@ __global__ void __launch_bounds__(256) k_update_thermo(UpdArgs a) {
     const double T = eint * ir;
     a.p[k] = p;
     a.T[k] = T;
+    if (a.nrcbc) {
+      // UPDATE_SOUND_SPEED.jl:31-36 for the cells the LODI outflow condition reads
+      const bool nb = ((a.nrcbc & 1) && i == 1) || ((a.nrcbc & 2) && i == NI - 2) ||
+                      ((a.nrcbc & 4) && j == 1) || ((a.nrcbc & 8) && j == NJ - 2);
+      if (nb) a.aY[k] = sqrt((a.gm1 + 1) * p / r);
+    }
     if (interior && !(r > 0 && p > 0)) atomicOr(&a.err[kErrFlags], kBitNumeric);
   }
 }
@@ -106,31 +114,13 @@ __global__ void __launch_bounds__(256) k_update_thermo(UpdArgs a) {
 // ---------------------------------------------------------------------------
 // Shock fitting + boundary conditions, one CTA.
 
-struct ShockArgs {
-  hymor_config cfg;
-  Cons tgt;          // array being evaluated
-  double *p, *T;     // its ghosted thermodynamic state
-  double* a_bc;      // sound speed used by the LODI outflow condition (ghosted)
-  bool compute_a;    // fill a_bc's edge-adjacent lines from p and rho first
-  ShockPts pts;      // shock points of tgt
-  ShockPts pS;       // shock points of S (MOVE_SHOCK of the accumulator)
-  bool copy_pts, move, on_S, do_shock, do_bc;
-  double cY, cS;
-  const int* cell_idx;
-  double *beta, *speed_x, *speed_y, *rel;
-  double* spl;       // workspace: 8 * nchi doubles
-  const double* scal;
-  unsigned* err;
-  DevMesh m;
-};
-
 // Element-space coordinates (utils/Mesh/GO_TO_ELEMENT_SPACE.jl:28-140).
 __device__ void element_space(const hymor_config& c, double x, double y, double& chi, double& eta) {
   if (c.mapping == HYMOR_MAP_CIRCLE) {
     const double angle_min = -c.circle_angle_extra, angle_max = M_PI / 2;
-    double t = atan2(-x, y) + M_PI / 2;
-    double mm = fmod(t, 2 * M_PI);
-    if (mm < 0) mm += 2 * M_PI;
+    // mod(t, 2 pi) for t = atan2(-x, y) + pi/2 in (-pi/2, 3 pi/2] (Julia's mod: result in [0, 2 pi))
+    const double t = atan2(-x, y) + M_PI / 2;
+    const double mm = t < 0 ? t + 2 * M_PI : (t >= 2 * M_PI ? t - 2 * M_PI : t);
     const double angle = mm - M_PI / 2;
     const double ch = (angle_max - angle) / (angle_max - angle_min);
     const double r = sqrt(x * x + y * y);
@@ -177,105 +167,13 @@ __device__ void element_space(const hymor_config& c, double x, double y, double&
   }
 }
 
-// Natural smoothing spline (Reinsch): factor the pentadiagonal system once and solve
-// for the x and y ordinates (single thread; the system is n-2 unknowns). Objective
-// Σ (y_i - f(x_i))² + λ ∫ f''², the one BSplineKit's fit(BSplineOrder(4), x, y, λ)
-// minimises (utils/Shock_fitting/LEAST_SQUARES_SHOCK_POINTS.jl:52-58).
-// Outputs: gx, gy (fitted values), cx, cy (second derivatives), all length n.
-__device__ void spline_fit2(int n, const double* xs, const double* yx, const double* yy, double lam,
-                            double* gx, double* gy, double* cx, double* cy, double* w0, double* w1,
-                            double* w2) {
-  for (int k = 0; k < n; ++k) { cx[k] = 0; cy[k] = 0; gx[k] = yx[k]; gy[k] = yy[k]; }
-  if (n < 3) return;
-  const int m = n - 2;
-  // bands of A = R + lam Q^T Q and its Cholesky factor, computed on the fly
-  double l1_prev = 0, l2_prev = 0, l2_prev2 = 0, l1_prev2 = 0;
-  (void)l1_prev2;
-  for (int jj = 0; jj < m; ++jj) {
-    const int j = jj + 1;
-    const double hm = xs[j] - xs[j - 1], h0 = xs[j + 1] - xs[j];
-    const double qm = 1.0 / hm, qp = 1.0 / h0, q0 = -qm - qp;
-    double d0 = (hm + h0) / 3 + lam * (qm * qm + q0 * q0 + qp * qp);
-    double d1 = 0, d2 = 0;
-    if (jj + 1 < m) {
-      const double h1 = xs[j + 2] - xs[j + 1];
-      const double qm1 = 1.0 / h0, qp1 = 1.0 / h1, q01 = -qm1 - qp1;
-      d1 = h0 / 6 + lam * (q0 * qm1 + qp * q01);
-    }
-    if (jj + 2 < m) d2 = lam * (qp * (1.0 / (xs[j + 2] - xs[j + 1])));
-    // Cholesky rows: l0 = sqrt(d0 - l1[j-1]^2 - l2[j-2]^2), l1 = (d1 - l2[j-1] l1[j-1]) / l0, l2 = d2 / l0
-    double a = d0 - l1_prev * l1_prev - l2_prev2 * l2_prev2;
-    const double l0 = sqrt(a);
-    const double il0 = 1.0 / l0;
-    const double l1 = (d1 - l2_prev * l1_prev) * il0;
-    const double l2 = d2 * il0;
-    w0[jj] = l0;
-    w1[jj] = l1;
-    w2[jj] = l2;
-    // forward substitution for both right-hand sides: rhs = Q^T y
-    const double rx = qm * yx[j - 1] + q0 * yx[j] + qp * yx[j + 1];
-    const double ry = qm * yy[j - 1] + q0 * yy[j] + qp * yy[j + 1];
-    double zx = rx, zy = ry;
-    if (jj >= 1) { zx -= w1[jj - 1] * cx[jj]; zy -= w1[jj - 1] * cy[jj]; }
-    if (jj >= 2) { zx -= w2[jj - 2] * cx[jj - 1]; zy -= w2[jj - 2] * cy[jj - 1]; }
-    cx[jj + 1] = zx * il0;  // z stored in place, shifted by one
-    cy[jj + 1] = zy * il0;
-    l2_prev2 = l2_prev;
-    l2_prev = l2;
-    l1_prev = l1;
-  }
-  // back substitution (gamma at indices 1..n-2), reading z from the same slots
-  for (int jj = m - 1; jj >= 0; --jj) {
-    double vx = cx[jj + 1], vy = cy[jj + 1];
-    if (jj + 1 < m) { vx -= w1[jj] * cx[jj + 2]; vy -= w1[jj] * cy[jj + 2]; }
-    if (jj + 2 < m) { vx -= w2[jj] * cx[jj + 3]; vy -= w2[jj] * cy[jj + 3]; }
-    const double il0 = 1.0 / w0[jj];
-    cx[jj + 1] = vx * il0;
-    cy[jj + 1] = vy * il0;
-  }
-  cx[0] = cx[n - 1] = 0;
-  cy[0] = cy[n - 1] = 0;
-}
-
-// g = y - lam Q gamma (one point per thread)
-__device__ double spline_g(int n, const double* xs, const double* ys, const double* gam, double lam, int r) {
+// g = y - lam Q gamma (one point per thread); ih[k] = 1 / (x[k+1] - x[k])
+__device__ double spline_g(int n, const double* ih, const double* ys, const double* gam, double lam, int r) {
   double qg = 0;
-  if (r - 1 >= 1 && r - 1 <= n - 2) qg += (1.0 / (xs[r] - xs[r - 1])) * gam[r - 1];
-  if (r >= 1 && r <= n - 2) {
-    const double qm = 1.0 / (xs[r] - xs[r - 1]), qp = 1.0 / (xs[r + 1] - xs[r]);
-    qg += (-qm - qp) * gam[r];
-  }
-  if (r + 1 >= 1 && r + 1 <= n - 2) qg += (1.0 / (xs[r + 1] - xs[r])) * gam[r + 1];
+  if (r - 1 >= 1 && r - 1 <= n - 2) qg += ih[r - 1] * gam[r - 1];
+  if (r >= 1 && r <= n - 2) qg += (-ih[r - 1] - ih[r]) * gam[r];
+  if (r + 1 >= 1 && r + 1 <= n - 2) qg += ih[r] * gam[r + 1];
   return ys[r] - lam * qg;
-}
-
-__device__ int spline_interval(int n, const double* xs, double t) {
-  if (t <= xs[0]) return 0;
-  if (t >= xs[n - 1]) return n - 2;
-  int lo = 0, hi = n - 1;
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (xs[mid] <= t) lo = mid; else hi = mid;
-  }
-  return lo;
-}
-
-__device__ void spline_eval(int n, const double* xs, const double* g, const double* gam, double t,
-                            double& val, double& der) {
-  auto in_val = [&](int k, double tt) {
-    const double h = xs[k + 1] - xs[k], a = xs[k + 1] - tt, b = tt - xs[k];
-    return (a * g[k] + b * g[k + 1]) / h + ((a * a * a - h * h * a) * gam[k] + (b * b * b - h * h * b) * gam[k + 1]) / (6 * h);
-  };
-  auto in_der = [&](int k, double tt) {
-    const double h = xs[k + 1] - xs[k], a = xs[k + 1] - tt, b = tt - xs[k];
-    return (g[k + 1] - g[k]) / h + ((h * h - 3 * a * a) * gam[k] + (3 * b * b - h * h) * gam[k + 1]) / (6 * h);
-  };
-  if (n < 2) { val = g[0]; der = 0; return; }
-  if (t < xs[0]) { der = in_der(0, xs[0]); val = g[0] + der * (t - xs[0]); return; }
-  if (t > xs[n - 1]) { der = in_der(n - 2, xs[n - 1]); val = g[n - 1] + der * (t - xs[n - 1]); return; }
-  const int k = spline_interval(n, xs, t);
-  val = in_val(k, t);
-  der = in_der(k, t);
 }
 
 // Freestream state seen by shock point i (COMPUTE_UPSTREAM_CONDITIONS.jl:31-112).
@@ -369,14 +267,15 @@ __device__ void edge_bc_point(const hymor_config& c, const EdgeCtx& e, const Dev
         edge_normal(e, m, k, nx, ny);
         const double a = A[a1];
         const double rho_int = R[a1];
-        double ung = (U[g] * nx + V[g] * ny) / R[g];
-        double uni = (U[a1] * nx + V[a1] * ny) / rho_int;
+        const double irg = frcp(R[g]);
+        double ung = (U[g] * nx + V[g] * ny) * irg;
+        double uni = (U[a1] * nx + V[a1] * ny) * frcp(rho_int);
         if (e.edge == 0 || e.edge == 2) { ung = -ung; uni = -uni; }
         if (ung < a) {
           const double p_lodi = P[a1] + rho_int * a * (ung - uni);
           P[g] = p_lodi;
-          const double rho_e = P[g] / (c.gamma - 1);
-          E[g] = rho_e + 0.5 * (U[g] * U[g] + V[g] * V[g]) / R[g];
+          const double rho_e = P[g] * (1.0 / (c.gamma - 1));
+          E[g] = rho_e + 0.5 * (U[g] * U[g] + V[g] * V[g]) * irg;
         }
       }
       break;
@@ -403,197 +302,453 @@ __device__ void edge_bc_point(const hymor_config& c, const EdgeCtx& e, const Dev
   }
 }
 
-__global__ void __launch_bounds__(1024) k_shock_bc(ShockArgs A) {
-  const hymor_config& c = A.cfg;
-  const int nchi = c.nchi, neta = c.neta, NI = nchi + 2, NJ = neta + 2;
-  const int tid = threadIdx.x, nt = blockDim.x;
-  const double dt = A.scal[kDt];
-  const double t = A.scal[kT];
-  Cons q = A.tgt;
+// ---------------------------------------------------------------------------
+// Shock fitting split over the GPU:
+//   k_spline_fit     one CTA: the serial banded factorisation of the smoothing
+//                    spline (the only O(Nchi) recurrence), both ordinates at once
+//   k_shock_columns  one thread per chi column: resample, element space, beta,
+//                    Rankine-Hugoniot jump, extrapolation, MOVE_SHOCK
+//   k_bc_chi / k_bc_eta  the two boundary phases (chi edges, then eta edges, whose
+//                    corners read the chi ghosts), one thread per edge point
+// Spline workspace (units of n = Nchi doubles): 0 knots, 1-2 ordinates x/y, 3-4
+// second derivatives x/y, 5-6 fitted values x/y, 7-11 per-row d0 d1 d2 rhs_x rhs_y,
+// 15 interval reciprocals 1/(x[k+1] - x[k]).
 
-  // (0) sound speed of the edge-adjacent lines, before the shock update
-  //     (UPDATE_SOUND_SPEED.jl:31-36 precedes UPDATE_SHOCK_BC in PDE.jl:20-26)
-  if (A.compute_a) {
-    const int bcs[4] = {c.bc_chi0, c.bc_chi1, c.bc_eta0, c.bc_eta1};
-    for (int ed = 0; ed < 4; ++ed) {
-      if (bcs[ed] != HYMOR_BC_OUTFLOW_NRCBC) continue;
-      const int len = ed <= 1 ? NJ : NI;
-      EdgeCtx e{ed, bcs[ed], NI, NJ, nchi, neta};
-      for (int k = tid; k < len; k += nt) {
-        const int a1 = at(e, 1, k);
-        A.a_bc[a1] = sqrt(c.gamma * A.p[a1] / q.rho[a1]);
-      }
+// 1/sqrt(a): hardware seed (rsqrt.approx.ftz.f64) refined by two Newton-Raphson
+// steps y <- y (3 - a y^2) / 2 (quadratic convergence, ~2^-80 before rounding).
+__device__ __forceinline__ double frsqrt(double a) {
+  double y;
+  asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(a));
+  double h = 0.5 * a;
+  y = y * fma(-h * y, y, 1.5);
+  y = y * fma(-h * y, y, 1.5);
+  return y;
+}
+
+struct SplineArgs {
+  ShockPts pts, pS;
+  double* ws;
+  double lam;
+  int n, copy_pts;
+};
+
+// Per-row bands of A = R + lam Q^T Q, right-hand sides Q^T y and interval reciprocals,
+// one thread per row (the rows are independent), after copying the shock points of S
+// into the stage array at stage 1.
+__global__ void __launch_bounds__(128) k_spline_rows(SplineArgs A) {
+  const int n = A.n;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double* xs = A.ws;
+  double* yx = xs + n;
+  double* yy = yx + n;
+  double* d0 = A.ws + 7 * n;
+  double* d1 = d0 + n;
+  double* d2 = d1 + n;
+  double* rx = d2 + n;
+  double* ry = rx + n;
+  double* ih = A.ws + 15 * n;  // 1 / (x[k+1] - x[k])
+  const ShockPts& src = A.copy_pts ? A.pS : A.pts;
+  const double lam = A.lam;
+  auto X = [&](int k) { return src.chi[k]; };
+  xs[i] = src.chi[i];
+  yx[i] = src.x[i];
+  yy[i] = src.y[i];
+  if (A.copy_pts) {
+    A.pts.x[i] = A.pS.x[i]; A.pts.y[i] = A.pS.y[i];
+    A.pts.chi[i] = A.pS.chi[i]; A.pts.eta[i] = A.pS.eta[i];
+  }
+  if (i + 1 < n) ih[i] = 1.0 / (X(i + 1) - X(i));
+  const int m = n - 2;
+  const int jj = i;
+  if (jj < m) {
+    const int j = jj + 1;
+    const double hm = X(j) - X(j - 1), h0 = X(j + 1) - X(j);
+    const double qm = 1.0 / hm, qp = 1.0 / h0, q0 = -qm - qp;
+    d0[jj] = (hm + h0) / 3 + lam * (qm * qm + q0 * q0 + qp * qp);
+    double e1 = 0, e2 = 0;
+    if (jj + 1 < m) {
+      const double h1 = X(j + 2) - X(j + 1);
+      const double qm1 = 1.0 / h0, qp1 = 1.0 / h1, q01 = -qm1 - qp1;
+      e1 = h0 / 6 + lam * (q0 * qm1 + qp * q01);
+    }
+    if (jj + 2 < m) e2 = lam * (qp * (1.0 / (X(j + 2) - X(j + 1))));
+    d1[jj] = e1;
+    d2[jj] = e2;
+    rx[jj] = qm * src.x[j - 1] + q0 * src.x[j] + qp * src.x[j + 1];
+    ry[jj] = qm * src.y[j - 1] + q0 * src.y[j] + qp * src.y[j + 1];
+  }
+}
+
+// Solves A gamma = Q^T y for the x and y ordinates (one CTA). GB300 runs a dependent
+// FP64 instruction in ~64 cycles and an FP32 one in ~4.5, so the inherently serial
+// banded Cholesky factorisation and the two triangular sweeps run in FP32, and
+// mixed-precision iterative refinement (FP64 residual r = b - A x, FP32 correction
+// solve, x += e; Moler, J. ACM 14 (1967) 316-321) brings the solution to FP64
+// accuracy: A is diagonally dominant (condition number ~4), so each refinement step
+// contracts the error by ~1e-6 and two steps reach the FP64 rounding level.
+constexpr int kRefineSteps = 2;
+
+constexpr int kChunk = 8;  // rows loaded into registers ahead of each serial sweep block
+
+// Forward and backward FP32 sweeps of L L^T x = r for two right-hand sides.
+//   forward:  z_j = c_j - a_j z_{j-1} - b_j z_{j-2}, with c_j = r_j / l0_j given in cx/cy
+//   backward: x_j = z_j / l0_j - p_j x_{j+1} - q_j x_{j+2}
+// Inputs and outputs are separate __restrict__ arrays so that the loads of a block of
+// rows issue before the dependent FMA chain (one FMA per row on the critical path).
+__device__ __forceinline__ void tri_solve_f32(int m, const float* __restrict__ fa, const float* __restrict__ fb,
+                                              const float* __restrict__ fil, const float* __restrict__ fp,
+                                              const float* __restrict__ fq, const float* __restrict__ cx,
+                                              const float* __restrict__ cy, float* __restrict__ zx,
+                                              float* __restrict__ zy, float* __restrict__ ox,
+                                              float* __restrict__ oy) {
+  float zx1 = 0.f, zx2 = 0.f, zy1 = 0.f, zy2 = 0.f;
+  int j = 0;
+  for (; j + kChunk <= m; j += kChunk) {
+    float ra[kChunk], rb[kChunk], rx[kChunk], ry[kChunk], ri[kChunk];
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u) { ra[u] = fa[j + u]; rb[u] = fb[j + u]; rx[u] = cx[j + u]; ry[u] = cy[j + u]; ri[u] = fil[j + u]; }
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u) {
+      const float a = fmaf(-ra[u], zx1, fmaf(-rb[u], zx2, rx[u]));
+      const float b = fmaf(-ra[u], zy1, fmaf(-rb[u], zy2, ry[u]));
+      zx[j + u] = a * ri[u];
+      zy[j + u] = b * ri[u];
+      zx2 = zx1; zx1 = a; zy2 = zy1; zy1 = b;
     }
   }
+  for (; j < m; ++j) {
+    const float a = fmaf(-fa[j], zx1, fmaf(-fb[j], zx2, cx[j]));
+    const float b = fmaf(-fa[j], zy1, fmaf(-fb[j], zy2, cy[j]));
+    zx[j] = a * fil[j];
+    zy[j] = b * fil[j];
+    zx2 = zx1; zx1 = a; zy2 = zy1; zy1 = b;
+  }
+  float x1 = 0.f, x2 = 0.f, y1 = 0.f, y2 = 0.f;
+  j = m - 1;
+  for (; j - kChunk + 1 >= 0; j -= kChunk) {
+    float rp[kChunk], rq[kChunk], rz[kChunk], rw[kChunk];
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u) { rp[u] = fp[j - u]; rq[u] = fq[j - u]; rz[u] = zx[j - u]; rw[u] = zy[j - u]; }
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u) {
+      const float a = fmaf(-rp[u], x1, fmaf(-rq[u], x2, rz[u]));
+      const float b = fmaf(-rp[u], y1, fmaf(-rq[u], y2, rw[u]));
+      ox[j - u] = a;
+      oy[j - u] = b;
+      x2 = x1; x1 = a; y2 = y1; y1 = b;
+    }
+  }
+  for (; j >= 0; --j) {
+    const float a = fmaf(-fp[j], x1, fmaf(-fq[j], x2, zx[j]));
+    const float b = fmaf(-fp[j], y1, fmaf(-fq[j], y2, zy[j]));
+    ox[j] = a;
+    oy[j] = b;
+    x2 = x1; x1 = a; y2 = y1; y1 = b;
+  }
+}
 
-  if (c.shock_enabled && A.do_shock) {
-    extern __shared__ double sh[];
-    double* xs = sh;              // knots (pts_chi)
-    double* vx = xs + nchi;       // ordinates x
-    double* vy = vx + nchi;       // ordinates y
-    double* gamx = vy + nchi;
-    double* gamy = gamx + nchi;
-    double* gxs = gamy + nchi;    // fitted values
-    double* gys = gxs + nchi;
-    double* w0 = A.spl;           // Cholesky bands (global workspace)
-    double* w1 = w0 + nchi;
-    double* w2 = w1 + nchi;
-    if (A.copy_pts) {
-      for (int i = tid; i < nchi; i += nt) {
-        A.pts.x[i] = A.pS.x[i]; A.pts.y[i] = A.pS.y[i];
-        A.pts.chi[i] = A.pS.chi[i]; A.pts.eta[i] = A.pS.eta[i];
-      }
-      __syncthreads();
+// FP32 banded Cholesky: il_j = 1 / l0_j, l1_j, l2_j of A ~ L L^T (one thread).
+__device__ __forceinline__ void chol_f32(int m, const float* __restrict__ fd0, const float* __restrict__ fd1,
+                                         const float* __restrict__ fd2, float* __restrict__ fil,
+                                         float* __restrict__ fl1, float* __restrict__ fl2) {
+  float l1p = 0.f, l2p = 0.f, l2pp = 0.f;
+  int j = 0;
+  for (; j + kChunk <= m; j += kChunk) {
+    float r0[kChunk], r1[kChunk], r2[kChunk];
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u) { r0[u] = fd0[j + u]; r1[u] = fd1[j + u]; r2[u] = fd2[j + u]; }
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u) {
+      const float a = fmaf(-l1p, l1p, fmaf(-l2pp, l2pp, r0[u]));
+      const float il = rsqrtf(a);
+      const float nl1 = fmaf(-l2p, l1p, r1[u]) * il;
+      const float nl2 = r2[u] * il;
+      fil[j + u] = il; fl1[j + u] = nl1; fl2[j + u] = nl2;
+      l2pp = l2p; l2p = nl2; l1p = nl1;
     }
-    for (int i = tid; i < nchi; i += nt) { xs[i] = A.pts.chi[i]; vx[i] = A.pts.x[i]; vy[i] = A.pts.y[i]; }
+  }
+  for (; j < m; ++j) {
+    const float a = fmaf(-l1p, l1p, fmaf(-l2pp, l2pp, fd0[j]));
+    const float il = rsqrtf(a);
+    const float nl1 = fmaf(-l2p, l1p, fd1[j]) * il;
+    const float nl2 = fd2[j] * il;
+    fil[j] = il; fl1[j] = nl1; fl2[j] = nl2;
+    l2pp = l2p; l2p = nl2; l1p = nl1;
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_spline_fit(SplineArgs A) {
+  extern __shared__ float shf[];
+  const int n = A.n, m = n - 2, tid = threadIdx.x, nt = blockDim.x;
+  double* xs = A.ws;
+  double* yx = xs + n;
+  double* yy = yx + n;
+  double* cx = yy + n;
+  double* cy = cx + n;
+  double* gx = cy + n;
+  double* gy = gx + n;
+  const double* d0 = A.ws + 7 * n;
+  const double* d1 = d0 + n;
+  const double* d2 = d1 + n;
+  const double* rx = d2 + n;
+  const double* ry = rx + n;
+  float* fil = shf;          // 1 / l0 (FP32)
+  float* fl1 = fil + m;
+  float* fl2 = fl1 + m;
+  float* fa = fl2 + m;       // l1_{j-1} / l0_j
+  float* fb = fa + m;        // l2_{j-2} / l0_j
+  float* fp = fb + m;        // l1_j / l0_j
+  float* fq = fp + m;        // l2_j / l0_j
+  float* wx = fq + m;        // right-hand sides c = r / l0
+  float* wy = wx + m;
+  float* fd0 = wy + m;       // FP32 bands (factorisation input), then forward results
+  float* fd1 = fd0 + m;
+  float* fd2 = fd1 + m;
+  float* ex = fd2 + m;       // corrections
+  float* ey = ex + m;
+  const double lam = A.lam;
+  for (int i = tid; i < n; i += nt) { cx[i] = 0; cy[i] = 0; }
+  if (m <= 0) {
     __syncthreads();
-    const double ps = c.spline_param;
-    const double lam = (1 - ps) / ps;
-    if (tid == 0) spline_fit2(nchi, xs, vx, vy, lam, gxs, gys, gamx, gamy, w0, w1, w2);
-    __syncthreads();
-    // fitted values g = y - lam Q gamma
-    for (int i = tid; i < nchi; i += nt) {
-      gxs[i] = spline_g(nchi, xs, vx, gamx, lam, i);
-      gys[i] = spline_g(nchi, xs, vy, gamy, lam, i);
-    }
-    __syncthreads();
-    // (1) resample at mesh chi, element space, beta (LEAST_SQUARES_SHOCK_POINTS.jl:60-70,
-    //     COMPUTE_BETA.jl:37-50)
-    for (int i = tid; i < nchi; i += nt) {
-      const double tc = A.m.chi1[i];
-      double xv, xd, yv, yd;
-      spline_eval(nchi, xs, gxs, gamx, tc, xv, xd);
-      spline_eval(nchi, xs, gys, gamy, tc, yv, yd);
-      double ch, et;
-      element_space(c, xv, yv, ch, et);
-      A.pts.x[i] = xv; A.pts.y[i] = yv; A.pts.chi[i] = ch; A.pts.eta[i] = et;
-      double p_inf, u_inf, v_inf, rho_inf;
-      upstream(c, t, xv, yv, i == 0, p_inf, u_inf, v_inf, rho_inf);
-      const double cross = xd * v_inf - yd * u_inf;
-      const double dot = xd * u_inf + yd * v_inf;
-      double b = atan2(fabs(cross), fabs(dot));
-      if (i == 0 && c.bc_chi0 == HYMOR_BC_SYMMETRY) b = M_PI / 2;  // UPDATE_SHOCK_BC.jl:31-34
-      A.beta[i] = b;
-    }
-    __syncthreads();
-    // (2) Rankine-Hugoniot jump at the shock, shocked-cell and auxiliary-cell values
-    //     (UPDATE_SHOCK_JUMP_PROPERTIES.jl:324-522, EXTRAPOLATE_CELLS_SHOCK.jl:39-176)
-    for (int i = tid; i < nchi; i += nt) {
-      const int sc = A.cell_idx[i];
-      if (sc < 2 || sc > neta - 1) {
-        atomicOr(&A.err[kErrFlags], kBitShockRange);
-        continue;
-      }
-      const int I = i + 1;  // ghosted column
-      const double x0 = A.m.x_ext[gidx(I, sc, nchi)], y0 = A.m.y_ext[gidx(I, sc, nchi)];
-      const double x1 = A.m.x_ext[gidx(I, sc - 1, nchi)], y1 = A.m.y_ext[gidx(I, sc - 1, nchi)];
-      const double x2 = A.m.x_ext[gidx(I, sc - 2, nchi)], y2 = A.m.y_ext[gidx(I, sc - 2, nchi)];
-      const double xsh = A.pts.x[i], ysh = A.pts.y[i];
-      const double dist01 = sqrt((x0 - x1) * (x0 - x1) + (y0 - y1) * (y0 - y1));
-      const double dist12 = sqrt((x1 - x2) * (x1 - x2) + (y1 - y2) * (y1 - y2));
-      const double dist1s = ((xsh - x1) * (x1 - x2) + (ysh - y1) * (y1 - y2)) / dist12;
-      const double dist0s = ((xsh - x0) * (x0 - x1) + (ysh - y0) * (y0 - y1)) / dist01;
-      const int g0 = gidx(I, sc, nchi), g1 = gidx(I, sc - 1, nchi), g2 = gidx(I, sc - 2, nchi);
-      const double p_1 = A.p[g1];
-      double p_2 = A.p[g2];
-      if (sc - 2 == 0 && c.bc_eta0 == HYMOR_BC_NO_SLIP_ISOTHERMAL)
-        p_2 = 2 * A.p[gidx(I, 1, nchi)] - A.p[gidx(I, 2, nchi)];  // UPDATE_THERMODYNAMIC_PROPERTIES.jl:28-31
-      const double slope_p = (p_1 - p_2) / dist12;
-      const double slope_rho = (q.rho[g1] - q.rho[g2]) / dist12;
-      const double slope_ru = (q.ru[g1] - q.ru[g2]) / dist12;
-      const double slope_rv = (q.rv[g1] - q.rv[g2]) / dist12;
-      const double slope_rE = (q.rE[g1] - q.rE[g2]) / dist12;
-      const double p_s = slope_p * dist1s + p_1;
-      double p_inf, u_inf, v_inf, rho_inf;
-      upstream(c, t, xsh, ysh, i == 0, p_inf, u_inf, v_inf, rho_inf);
-      const double yr = p_s / p_inf;
-      if (yr < 1) atomicAdd(&A.err[kRhWarn], 1u);
-      const double gs = c.gamma, gi = c.gamma;
-      const double Acoef = (gs + 1) / (gs - 1), Bcoef = (gi + 1) / (gi - 1);
-      const double rho_s = rho_inf * (yr * Acoef + 1) / (yr + Bcoef);
-      const double e_s = p_s / ((gs - 1) * rho_s);
-      const double b = A.beta[i];
-      const double ang_inf = b - atan2(v_inf, u_inf);
-      const double vmag = sqrt(u_inf * u_inf + v_inf * v_inf);
-      const double vn_inf = sin(ang_inf) * vmag;
-      const double temp1 = 2 * yr / (gs - 1) - 2 / (gi - 1);
-      const double temp2 = yr * Acoef + 1;
-      const double temp3 = p_inf * (yr - 1) / rho_inf;
-      const double rel = -vn_inf + sqrt(temp3 * temp2 / temp1);
-      A.rel[i] = rel;
-      const double vt_s = cos(ang_inf) * vmag;
-      const double vn_s = -rel + rho_inf / rho_s * (rel + vn_inf);
-      const double sb = sin(b), cb = cos(b);
-      if (!c.shock_eulerian) {
-        A.speed_x[i] = -rel * sb;
-        A.speed_y[i] = rel * cb;
-      } else {
-        const double sx = -rel * sb, sy = rel * cb;
-        A.speed_x[i] = sx - sy * tan(M_PI / 2 - b);
-        A.speed_y[i] = 0.0;
-      }
-      const double ru_s = rho_s * (vn_s * sb + vt_s * cb);
-      const double rv_s = rho_s * (-vn_s * cb + vt_s * sb);
-      const double rE_s = e_s * rho_s + (ru_s * ru_s + rv_s * rv_s) / (2 * rho_s);
-      q.rho[g0] = -slope_rho * dist0s + rho_s;
-      q.ru[g0] = -slope_ru * dist0s + ru_s;
-      q.rv[g0] = -slope_rv * dist0s + rv_s;
-      q.rE[g0] = -slope_rE * dist0s + rE_s;
-      A.p[g0] = -slope_p * dist0s + p_s;
-      // EXTRAPOLATE_CELLS_SHOCK: idx_1 = sc+1, idx_2 = sc+2 (0-based ghosted rows)
-      const int i1 = gidx(I, sc + 1, nchi), i2 = gidx(I, sc + 2, nchi);
-      const int im1 = g1, im2 = g2;
-      double* arr[5] = {q.rho, q.ru, q.rv, q.rE, A.p};
-      if (c.shock_interp == 1) {
-        for (int v = 0; v < 5; ++v) { arr[v][i1] = arr[v][g0]; arr[v][i2] = arr[v][g0]; }
-      } else if (c.shock_interp == 2) {
-        for (int v = 0; v < 5; ++v) arr[v][i1] = 2 * arr[v][g0] - arr[v][im1];
-        for (int v = 0; v < 4; ++v) arr[v][i2] = 2 * arr[v][i1] - arr[v][g0];
-      } else {
-        const double pm2 = (sc - 2 == 0 && c.bc_eta0 == HYMOR_BC_NO_SLIP_ISOTHERMAL) ? p_2 : A.p[im2];
-        for (int v = 0; v < 4; ++v) arr[v][i1] = 3 * arr[v][g0] - 3 * arr[v][im1] + arr[v][im2];
-        A.p[i1] = 3 * A.p[g0] - 3 * A.p[im1] + pm2;
-        for (int v = 0; v < 4; ++v) arr[v][i2] = 3 * arr[v][i1] - 3 * arr[v][g0] + arr[v][im1];
-      }
-    }
-    __syncthreads();
-    // (3) MOVE_SHOCK (MOVE_SHOCK.jl:29-49) on S (cS) and on the stage points (cY)
-    if (A.move) {
-      const double wS = A.cS * dt * c.relaxation, wY = A.cY * dt * c.relaxation;
-      for (int i = tid; i < nchi; i += nt) {
-        A.pS.x[i] = A.pS.x[i] + A.speed_x[i] * wS;
-        A.pS.y[i] = A.pS.y[i] + A.speed_y[i] * wS;
-        if (!A.on_S) {
-          A.pts.x[i] = A.pts.x[i] + A.speed_x[i] * wY;
-          A.pts.y[i] = A.pts.y[i] + A.speed_y[i] * wY;
-        }
-      }
-      __syncthreads();
-      if (tid == 0 && c.bc_chi0 == HYMOR_BC_SYMMETRY && nchi >= 2) {
-        A.pS.x[0] = A.pS.x[1];
-        if (!A.on_S) A.pts.x[0] = A.pts.x[1];
-      }
-    }
+    for (int i = tid; i < n; i += nt) { gx[i] = yx[i]; gy[i] = yy[i]; }
+    return;
+  }
+  for (int j = tid; j < m; j += nt) { fd0[j] = (float)d0[j]; fd1[j] = (float)d1[j]; fd2[j] = (float)d2[j]; }
+  __syncthreads();
+  if (tid == 0) chol_f32(m, fd0, fd1, fd2, fil, fl1, fl2);
+  __syncthreads();
+  for (int j = tid; j < m; j += nt) {
+    fa[j] = j >= 1 ? fl1[j - 1] * fil[j] : 0.f;
+    fb[j] = j >= 2 ? fl2[j - 2] * fil[j] : 0.f;
+    fp[j] = fl1[j] * fil[j];
+    fq[j] = fl2[j] * fil[j];
+    wx[j] = (float)rx[j] * fil[j];
+    wy[j] = (float)ry[j] * fil[j];
   }
   __syncthreads();
-
-  // (4) boundary conditions, edges in the reference order chi0, chi1, eta0, eta1
-  const int bcs[4] = {c.bc_chi0, c.bc_chi1, c.bc_eta0, c.bc_eta1};
-  for (int ed = 0; ed < 4 && A.do_bc; ++ed) {
-    const int len = ed <= 1 ? NJ : NI;
-    EdgeCtx e{ed, bcs[ed], NI, NJ, nchi, neta};
-    if (e.bc != HYMOR_BC_SHOCK) {
-      for (int k = tid; k < len; k += nt) edge_bc_point(c, e, A.m, q, A.p, A.T, A.a_bc, k, len);
-      __syncthreads();
-      if (e.bc == HYMOR_BC_SYMMETRY && tid == 0) {
-        // ends of the ghost line copy their neighbours along the line
-        q.ru[at(e, 0, 0)] = q.ru[at(e, 0, 1)];
-        q.rv[at(e, 0, 0)] = q.rv[at(e, 0, 1)];
-        q.ru[at(e, 0, len - 1)] = q.ru[at(e, 0, len - 2)];
-        q.rv[at(e, 0, len - 1)] = q.rv[at(e, 0, len - 2)];
-      }
+  // fd0/fd1 are free now: forward-sweep scratch
+  float* zx = fd0;
+  float* zy = fd1;
+  for (int pass = 0; pass <= kRefineSteps; ++pass) {
+    if (tid == 0) tri_solve_f32(m, fa, fb, fil, fp, fq, wx, wy, zx, zy, ex, ey);
+    __syncthreads();
+    // x += e (FP64), then the FP64 residual of the next pass
+    for (int j = tid; j < m; j += nt) { cx[j + 1] += (double)ex[j]; cy[j + 1] += (double)ey[j]; }
+    __syncthreads();
+    if (pass == kRefineSteps) break;
+    for (int j = tid; j < m; j += nt) {
+      // (A x)_j = d2_{j-2} x_{j-2} + d1_{j-1} x_{j-1} + d0_j x_j + d1_j x_{j+1} + d2_j x_{j+2}
+      double ax = d0[j] * cx[j + 1], ay = d0[j] * cy[j + 1];
+      if (j >= 1) { ax = fma(d1[j - 1], cx[j], ax); ay = fma(d1[j - 1], cy[j], ay); }
+      if (j >= 2) { ax = fma(d2[j - 2], cx[j - 1], ax); ay = fma(d2[j - 2], cy[j - 1], ay); }
+      if (j + 1 < m) { ax = fma(d1[j], cx[j + 2], ax); ay = fma(d1[j], cy[j + 2], ay); }
+      if (j + 2 < m) { ax = fma(d2[j], cx[j + 3], ax); ay = fma(d2[j], cy[j + 3], ay); }
+      wx[j] = (float)(rx[j] - ax) * fil[j];
+      wy[j] = (float)(ry[j] - ay) * fil[j];
     }
     __syncthreads();
+  }
+  // fitted values g = y - lam Q gamma
+  const double* ih = A.ws + 15 * n;
+  for (int i = tid; i < n; i += nt) {
+    gx[i] = spline_g(n, ih, yx, cx, lam, i);
+    gy[i] = spline_g(n, ih, yy, cy, lam, i);
+  }
+}
+
+struct ColArgs {
+  hymor_config cfg;
+  Cons tgt;
+  double* p;
+  ShockPts pts, pS;
+  const double* ws;
+  const int* cell_idx;
+  double *beta, *speed_x, *speed_y, *rel;
+  const double* scal;
+  unsigned* err;
+  DevMesh m;
+  double cY, cS;
+  int move, on_S;
+  int disturbed;                          // any freestream disturbance amplitude non-zero
+  double p_inf, u_inf, v_inf, rho_inf;    // undisturbed freestream (COMPUTE_UPSTREAM_CONDITIONS.jl)
+};
+
+// value and slope of the fitted spline at t (Linear() extrapolation outside the knots)
+__device__ void spline_at(int n, const double* xs, const double* g, const double* gam, const double* ih, double t,
+                          int guess, double& val, double& der) {
+  auto in_der = [&](int k, double tt) {
+    const double h = xs[k + 1] - xs[k], a = xs[k + 1] - tt, b = tt - xs[k];
+    return (g[k + 1] - g[k]) * ih[k] + ((h * h - 3 * a * a) * gam[k] + (3 * b * b - h * h) * gam[k + 1]) * (ih[k] * (1.0 / 6));
+  };
+  if (t < xs[0]) { der = in_der(0, xs[0]); val = g[0] + der * (t - xs[0]); return; }
+  if (t > xs[n - 1]) { der = in_der(n - 2, xs[n - 1]); val = g[n - 1] + der * (t - xs[n - 1]); return; }
+  // the knots stay close to the mesh abscissae, so walk from the column's own interval
+  int k = guess < 0 ? 0 : (guess > n - 2 ? n - 2 : guess);
+  while (k > 0 && xs[k] > t) --k;
+  while (k < n - 2 && xs[k + 1] <= t) ++k;
+  const double h = xs[k + 1] - xs[k], a = xs[k + 1] - t, b = t - xs[k];
+  val = (a * g[k] + b * g[k + 1]) * ih[k] + ((a * a * a - h * h * a) * gam[k] + (b * b * b - h * h * b) * gam[k + 1]) * (ih[k] * (1.0 / 6));
+  der = in_der(k, t);
+}
+
+__global__ void __launch_bounds__(128) k_shock_columns(ColArgs A) {
+  const hymor_config& c = A.cfg;
+  const int nchi = c.nchi, neta = c.neta;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nchi) return;
+  const double* xs = A.ws;
+  const double* cxs = A.ws + 3 * nchi;
+  const double* cys = A.ws + 4 * nchi;
+  const double* gxs = A.ws + 5 * nchi;
+  const double* gys = A.ws + 6 * nchi;
+  const double* ih = A.ws + 15 * nchi;
+  const double t = A.scal[kT], dt = A.scal[kDt];
+  Cons q = A.tgt;
+  // LEAST_SQUARES_SHOCK_POINTS.jl:60-70, COMPUTE_BETA.jl:37-50
+  const double tc = A.m.chi1[i];
+  double xv, xd, yv, yd;
+  spline_at(nchi, xs, gxs, cxs, ih, tc, i - 1, xv, xd);
+  spline_at(nchi, xs, gys, cys, ih, tc, i - 1, yv, yd);
+  double ch, et;
+  element_space(c, xv, yv, ch, et);
+  A.pts.x[i] = xv; A.pts.y[i] = yv; A.pts.chi[i] = ch; A.pts.eta[i] = et;
+  double p_inf = A.p_inf, u_inf = A.u_inf, v_inf = A.v_inf, rho_inf = A.rho_inf;
+  if (A.disturbed || (c.axisymmetric && i == 0)) upstream(c, t, xv, yv, i == 0, p_inf, u_inf, v_inf, rho_inf);
+  const double cross = xd * v_inf - yd * u_inf;
+  const double dot = xd * u_inf + yd * v_inf;
+  // beta = atan2(|cross|, |dot|) enters only through its sine and cosine, |cross| / r and |dot| / r
+  double sb, cb;
+  {
+    const double ir = frsqrt(cross * cross + dot * dot);
+    sb = fabs(cross) * ir;
+    cb = fabs(dot) * ir;
+  }
+  if (i == 0 && c.bc_chi0 == HYMOR_BC_SYMMETRY) { sb = 1.0; cb = 0.0; }  // beta = pi/2, UPDATE_SHOCK_BC.jl:31-34
+  // UPDATE_SHOCK_JUMP_PROPERTIES.jl:324-522 and EXTRAPOLATE_CELLS_SHOCK.jl:39-176
+  const int sc = A.cell_idx[i];
+  if (sc < 2 || sc > neta - 1) {
+    atomicOr(&A.err[kErrFlags], kBitShockRange);
+    return;
+  }
+  const int I = i + 1;
+  const double x0 = A.m.x_ext[gidx(I, sc, nchi)], y0 = A.m.y_ext[gidx(I, sc, nchi)];
+  const double x1 = A.m.x_ext[gidx(I, sc - 1, nchi)], y1 = A.m.y_ext[gidx(I, sc - 1, nchi)];
+  const double x2 = A.m.x_ext[gidx(I, sc - 2, nchi)], y2 = A.m.y_ext[gidx(I, sc - 2, nchi)];
+  const double i01 = frsqrt((x0 - x1) * (x0 - x1) + (y0 - y1) * (y0 - y1));  // 1 / dist01
+  const double i12 = frsqrt((x1 - x2) * (x1 - x2) + (y1 - y2) * (y1 - y2));  // 1 / dist12
+  const double dist1s = ((xv - x1) * (x1 - x2) + (yv - y1) * (y1 - y2)) * i12;
+  const double dist0s = ((xv - x0) * (x0 - x1) + (yv - y0) * (y0 - y1)) * i01;
+  const int g0 = gidx(I, sc, nchi), g1 = gidx(I, sc - 1, nchi), g2 = gidx(I, sc - 2, nchi);
+  const double p_1 = A.p[g1];
+  double p_2 = A.p[g2];
+  if (sc - 2 == 0 && c.bc_eta0 == HYMOR_BC_NO_SLIP_ISOTHERMAL)
+    p_2 = 2 * A.p[gidx(I, 1, nchi)] - A.p[gidx(I, 2, nchi)];  // UPDATE_THERMODYNAMIC_PROPERTIES.jl:28-31
+  const double slope_p = (p_1 - p_2) * i12;
+  const double slope_rho = (q.rho[g1] - q.rho[g2]) * i12;
+  const double slope_ru = (q.ru[g1] - q.ru[g2]) * i12;
+  const double slope_rv = (q.rv[g1] - q.rv[g2]) * i12;
+  const double slope_rE = (q.rE[g1] - q.rE[g2]) * i12;
+  const double p_s = slope_p * dist1s + p_1;
+  const double yr = p_s * frcp(p_inf);
+  if (yr < 1) atomicAdd(&A.err[kRhWarn], 1u);
+  const double gs = c.gamma, gi = c.gamma;
+  const double Acoef = (gs + 1) / (gs - 1), Bcoef = (gi + 1) / (gi - 1);
+  const double rho_s = rho_inf * (yr * Acoef + 1) * frcp(yr + Bcoef);
+  const double irho_s = frcp(rho_s);
+  const double e_s = p_s * (1.0 / (gs - 1)) * irho_s;
+  // ang_inf = beta - atan2(v_inf, u_inf): sine and cosine by the angle-difference identity
+  const double vmag = sqrt(u_inf * u_inf + v_inf * v_inf);
+  const double ivm = frcp(vmag);
+  const double cph = u_inf * ivm, sph = v_inf * ivm;
+  const double sa = sb * cph - cb * sph, ca = cb * cph + sb * sph;
+  const double vn_inf = sa * vmag;
+  const double temp1 = 2 * yr * (1.0 / (gs - 1)) - 2 / (gi - 1);
+  const double temp2 = yr * Acoef + 1;
+  const double temp3 = p_inf * (yr - 1) * frcp(rho_inf);
+  const double rel = -vn_inf + sqrt(temp3 * temp2 * frcp(temp1));
+  A.rel[i] = rel;
+  const double vt_s = ca * vmag;
+  const double vn_s = -rel + rho_inf * irho_s * (rel + vn_inf);
+  double spx, spy;
+  if (!c.shock_eulerian) {
+    spx = -rel * sb;
+    spy = rel * cb;
+  } else {
+    const double sx = -rel * sb, sy = rel * cb;
+    spx = sx - sy * (cb * frcp(sb));  // tan(pi/2 - beta) = cos(beta) / sin(beta)
+    spy = 0.0;
+  }
+  A.speed_x[i] = spx;
+  A.speed_y[i] = spy;
+  const double ru_s = rho_s * (vn_s * sb + vt_s * cb);
+  const double rv_s = rho_s * (-vn_s * cb + vt_s * sb);
+  const double rE_s = e_s * rho_s + (ru_s * ru_s + rv_s * rv_s) * (0.5 * irho_s);
+  q.rho[g0] = -slope_rho * dist0s + rho_s;
+  q.ru[g0] = -slope_ru * dist0s + ru_s;
+  q.rv[g0] = -slope_rv * dist0s + rv_s;
+  q.rE[g0] = -slope_rE * dist0s + rE_s;
+  A.p[g0] = -slope_p * dist0s + p_s;
+  const int i1 = gidx(I, sc + 1, nchi), i2 = gidx(I, sc + 2, nchi);
+  const int im1 = g1, im2 = g2;
+  double* arr[5] = {q.rho, q.ru, q.rv, q.rE, A.p};
+  if (c.shock_interp == 1) {
+    for (int v = 0; v < 5; ++v) { arr[v][i1] = arr[v][g0]; arr[v][i2] = arr[v][g0]; }
+  } else if (c.shock_interp == 2) {
+    for (int v = 0; v < 5; ++v) arr[v][i1] = 2 * arr[v][g0] - arr[v][im1];
+    for (int v = 0; v < 4; ++v) arr[v][i2] = 2 * arr[v][i1] - arr[v][g0];
+  } else {
+    for (int v = 0; v < 4; ++v) arr[v][i1] = 3 * arr[v][g0] - 3 * arr[v][im1] + arr[v][im2];
+    A.p[i1] = 3 * A.p[g0] - 3 * A.p[im1] + p_2;
+    for (int v = 0; v < 4; ++v) arr[v][i2] = 3 * arr[v][i1] - 3 * arr[v][g0] + arr[v][im1];
+  }
+  // MOVE_SHOCK (MOVE_SHOCK.jl:29-49); the symmetry copy pts_x[1] -> pts_x[0] runs in k_bc_edges
+  if (A.move) {
+    const double wS = A.cS * dt * c.relaxation, wY = A.cY * dt * c.relaxation;
+    A.pS.x[i] = A.pS.x[i] + spx * wS;
+    A.pS.y[i] = A.pS.y[i] + spy * wS;
+    if (!A.on_S) {
+      A.pts.x[i] = A.pts.x[i] + spx * wY;
+      A.pts.y[i] = A.pts.y[i] + spy * wY;
+    }
+  }
+}
+
+struct BcArgs {
+  hymor_config cfg;
+  Cons q;
+  double *p, *T;
+  const double* a_bc;
+  DevMesh m;
+  ShockPts pts, pS;
+  int phase;     // 0: chi edges, 1: eta edges
+  int fix_pts;   // MOVE_SHOCK symmetry copy (phase 0, thread 0)
+  int on_S;
+};
+
+__global__ void __launch_bounds__(256) k_bc_edges(BcArgs A) {
+  const hymor_config& c = A.cfg;
+  const int nchi = c.nchi, neta = c.neta, NI = nchi + 2, NJ = neta + 2;
+  const int len = A.phase == 0 ? NJ : NI;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (A.fix_pts && t == 0 && A.phase == 0 && nchi >= 2) {
+    A.pS.x[0] = A.pS.x[1];
+    if (!A.on_S) A.pts.x[0] = A.pts.x[1];
+  }
+  if (t >= 2 * len) return;
+  const int side = t / len, k = t % len;
+  const int edge = 2 * A.phase + side;
+  const int bc = edge == 0 ? c.bc_chi0 : edge == 1 ? c.bc_chi1 : edge == 2 ? c.bc_eta0 : c.bc_eta1;
+  if (bc == HYMOR_BC_SHOCK) return;
+  EdgeCtx e{edge, bc, NI, NJ, nchi, neta};
+  edge_bc_point(c, e, A.m, A.q, A.p, A.T, A.a_bc, k, len);
+  if (bc == HYMOR_BC_SYMMETRY) {
+    // ends of the ghost line copy their neighbours along the line
+    if (k == 1) { A.q.ru[at(e, 0, 0)] = A.q.ru[at(e, 0, 1)]; A.q.rv[at(e, 0, 0)] = A.q.rv[at(e, 0, 1)]; }
+    if (k == len - 2) {
+      A.q.ru[at(e, 0, len - 1)] = A.q.ru[at(e, 0, len - 2)];
+      A.q.rv[at(e, 0, len - 1)] = A.q.rv[at(e, 0, len - 2)];
+    }
   }
 }
 
@@ -611,6 +766,7 @@ struct FluxArgs {
   int nchi, neta;
   int mask;                // shock fitting with feedback: zero flux at j >= sc
   int shock;
+  int tile_class;          // -1 all tiles; 0 tiles reading nothing the shock/BC kernels write; 1 the others
 };
 
 template <bool AXI, bool SUTH>
@@ -635,6 +791,23 @@ __global__ void __launch_bounds__(kFluxThreads, 2) k_flux(FluxArgs a) {
   const int nchi = a.nchi, neta = a.neta;
   const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;  // first interior cell (0-based)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+  if (a.tile_class >= 0) {
+    // the halo (ghosted columns i0..i0+TX+1, rows j0..j0+TY+1) avoids every ghost cell and
+    // stays below the shocked rows sc..sc+2 of its columns -> independent of shock/BC work
+    bool inner = i0 >= 1 && i0 + TX + 1 <= nchi && j0 >= 1 && j0 + TY + 1 <= neta;
+    if (a.shock) {
+      int scmin = 0x7fffffff;
+      for (int c = lane; c < TX + 2; c += 32) {
+        const int col = i0 - 1 + c;  // interior column of halo column
+        if (col >= 0 && col < nchi) scmin = min(scmin, a.cell_idx[col]);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) scmin = min(scmin, __shfl_xor_sync(0xffffffffu, scmin, o));
+      inner = inner && (j0 + TY + 1 < scmin);
+    }
+    if (inner != (a.tile_class == 0)) return;
+  }
 
   // whole tile at or above the shocked rows: flux is zero (NON_LINEAR_DYNAMICS mask)
   if (a.mask) {
@@ -830,22 +1003,6 @@ size_t flux_smem() {
 // ---------------------------------------------------------------------------
 // UPDATE_FLOW_CELLS on S: DETECT_CELLS_SHOCKED (DETECT_CELLS_SHOCKED.jl:50-65),
 // UPDATE_FIELD_UPSTREAM (UPDATE_FIELD_UPSTREAM.jl:93-109), EXTRAPOLATE_CELLS_SHOCK.
-__device__ void fill_column_upstream(const hymor_config& c, const DevMesh& m, Cons q, int i, int sc, double t) {
-  const int nchi = c.nchi, NJ = c.neta + 2;
-  const double u_y = c.rho_v_0 / c.rho_0, u_x = c.rho_u_0 / c.rho_0;
-  const bool dist = c.dist_amp[0] != 0 || c.dist_amp[1] != 0 || c.dist_amp[2] != 0 || c.dist_amp[3] != 0;
-  for (int jg = sc + 2; jg < NJ; ++jg) {  // 0-based ghosted rows >= sc + 2
-    const long k = gidx(i + 1, jg, nchi);
-    double pert = 0;
-    if (dist)
-      pert = cos(2.0 * M_PI * c.dist_ky * (m.y_ext[k] - u_y * t)) * sin(2.0 * M_PI * c.dist_kx * (m.x_ext[k] - u_x * t));
-    q.rho[k] = c.rho_0 + pert * c.dist_amp[0];
-    q.ru[k] = c.rho_u_0 + pert * c.dist_amp[1];
-    q.rv[k] = c.rho_v_0 + pert * c.dist_amp[2];
-    q.rE[k] = c.rho_E_0 + pert * c.dist_amp[3];
-  }
-}
-
 __device__ void extrapolate_column(const hymor_config& c, Cons q, int i, int sc) {
   const int nchi = c.nchi, I = i + 1;
   const int g0 = gidx(I, sc, nchi), i1 = gidx(I, sc + 1, nchi), i2 = gidx(I, sc + 2, nchi);
@@ -872,27 +1029,50 @@ struct FlowArgs {
   unsigned* err;
 };
 
-__global__ void k_flow_cells(FlowArgs A) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(256) k_flow_cells(FlowArgs A) {
   const hymor_config& c = A.cfg;
-  if (i >= c.nchi) return;
-  const int nchi = c.nchi, neta = c.neta;
+  const int nchi = c.nchi, neta = c.neta, NJ = neta + 2;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (i >= nchi) return;
   const double px = A.pS.x[i], py = A.pS.y[i];
+  // nearest cell centre along the column; ties go to the smallest row, like the
+  // reference's sequential scan with a strict comparison
   double best = INFINITY;
-  int bj = 1;
-  for (int j = 1; j <= neta; ++j) {
+  int bj = 0x7fffffff;
+  for (int j = 1 + lane; j <= neta; j += 32) {
     const long k = gidx(i + 1, j, nchi);
     const double dx = px - A.m.x_ext[k], dy = py - A.m.y_ext[k];
     const double d = dx * dx + dy * dy;
     if (d < best) { best = d; bj = j; }
   }
-  A.cell_idx[i] = bj;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+    const int oj = __shfl_xor_sync(0xffffffffu, bj, o);
+    if (ob < best || (ob == best && oj < bj)) { best = ob; bj = oj; }
+  }
+  if (bj == 0x7fffffff) bj = 1;
+  if (lane == 0) A.cell_idx[i] = bj;
   if (bj < 2 || bj > neta - 1) {
-    atomicOr(&A.err[kErrFlags], kBitShockRange);
+    if (lane == 0) atomicOr(&A.err[kErrFlags], kBitShockRange);
     return;
   }
-  fill_column_upstream(c, A.m, A.S, i, bj, A.scal[kT]);
-  extrapolate_column(c, A.S, i, bj);
+  // UPDATE_FIELD_UPSTREAM: ghosted rows >= sc + 2 of this column
+  const double t = A.scal[kT];
+  const double u_y = c.rho_v_0 / c.rho_0, u_x = c.rho_u_0 / c.rho_0;
+  const bool dist = c.dist_amp[0] != 0 || c.dist_amp[1] != 0 || c.dist_amp[2] != 0 || c.dist_amp[3] != 0;
+  for (int jg = bj + 2 + lane; jg < NJ; jg += 32) {
+    const long k = gidx(i + 1, jg, nchi);
+    double pert = 0;
+    if (dist)
+      pert = cos(2.0 * M_PI * c.dist_ky * (A.m.y_ext[k] - u_y * t)) * sin(2.0 * M_PI * c.dist_kx * (A.m.x_ext[k] - u_x * t));
+    A.S.rho[k] = c.rho_0 + pert * c.dist_amp[0];
+    A.S.ru[k] = c.rho_u_0 + pert * c.dist_amp[1];
+    A.S.rv[k] = c.rho_v_0 + pert * c.dist_amp[2];
+    A.S.rE[k] = c.rho_E_0 + pert * c.dist_amp[3];
+  }
+  __syncwarp();
+  if (lane == 0) extrapolate_column(c, A.S, i, bj);
 }
 
 // Sound speed of S, max |a| over every ghosted cell (CFL_TIMESTEP.jl:80).
@@ -911,8 +1091,7 @@ __global__ void __launch_bounds__(256) k_sound_cmax(SoundArgs A) {
   const double gm1 = A.gamma - 1;
   auto pres = [&](long k) {
     const double r = A.S.rho[k], u = A.S.ru[k], v = A.S.rv[k], e = A.S.rE[k];
-    const double eint = e - (u * u + v * v) / r / 2;
-    return eint * gm1;
+    return fma(-0.5, fma(u, u, v * v) * frcp(r), e) * gm1;
   };
   for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < G; k += (long)gridDim.x * blockDim.x) {
     double a;
@@ -923,7 +1102,7 @@ __global__ void __launch_bounds__(256) k_sound_cmax(SoundArgs A) {
         p = 2 * pres(gidx(i, 1, A.nchi)) - pres(gidx(i, 2, A.nchi));
       else
         p = pres(k);
-      a = sqrt(A.gamma * p / A.S.rho[k]);
+      a = sqrt(A.gamma * p * frcp(A.S.rho[k]));
       A.aS[k] = a;
     } else {
       a = A.aS[k];
@@ -941,7 +1120,11 @@ __global__ void __launch_bounds__(256) k_sound_cmax(SoundArgs A) {
   }
 }
 
-// CFL maxima (CFL_TIMESTEP.jl:80-130) and dt.
+// CFL maxima (CFL_TIMESTEP.jl:80-130) and dt. k_cfl_faces evaluates the convective
+// face rate (|V_n| + c) A once per face; k_cfl takes, per cell, the max over opposite
+// faces, adds the viscous rate 2 max(4/3, gamma/Pr) (A_xi^2 + A_eta^2) / (rho Re_flow vol)
+// (the mesh factor 2 (A_xi^2 + A_eta^2) / vol is precomputed), divides by the volume and
+// reduces the maxima of the rates and of the stored-flux terms of dt2.
 struct CflArgs {
   Cons S;
   const double* SF0;
@@ -951,53 +1134,63 @@ struct CflArgs {
   DevMesh m;
   const int* cell_idx;
   double* scal;
+  double* lam_lr;   // face rates, lr then bt
+  double* lam_bt;
   double gamma, Pr, Re, suthS, Tinf_inv;
   int nchi, neta, shock, suth;
 };
 
+__global__ void __launch_bounds__(256) k_cfl_faces(CflArgs A) {
+  const int nchi = A.nchi, neta = A.neta;
+  const long NLR = (long)(nchi + 1) * neta, NBT = (long)nchi * (neta + 1);
+  const double cmax = A.scal[kCmax];
+  for (long f = blockIdx.x * (long)blockDim.x + threadIdx.x; f < NLR + NBT; f += (long)gridDim.x * blockDim.x) {
+    long L, R;
+    double nx, ny, Af;
+    if (f < NLR) {
+      const int i = (int)(f % (nchi + 1)), j = (int)(f / (nchi + 1));
+      L = gidx(i, j + 1, nchi);
+      R = L + 1;
+      nx = A.m.lr_xn[f]; ny = A.m.lr_yn[f]; Af = A.m.lr_a[f];
+    } else {
+      const long g = f - NLR;
+      const int i = (int)(g % nchi), j = (int)(g / nchi);
+      L = gidx(i + 1, j, nchi);
+      R = L + (nchi + 2);
+      nx = A.m.bt_xn[g]; ny = A.m.bt_yn[g]; Af = A.m.bt_a[g];
+    }
+    const double rs = A.S.rho[L] + A.S.rho[R];
+    const double Vn = fabs(fma(A.S.ru[L] + A.S.ru[R], nx, (A.S.rv[L] + A.S.rv[R]) * ny)) * frcp(rs);
+    const double lam = (Vn + cmax) * Af;
+    if (f < NLR) A.lam_lr[f] = lam; else A.lam_bt[f - NLR] = lam;
+  }
+}
+
 __global__ void __launch_bounds__(256) k_cfl(CflArgs A) {
   const int nchi = A.nchi, neta = A.neta;
   const long N = (long)nchi * neta;
-  const double cmax = A.scal[kCmax];
   double mlam = 0, mflux = 0;
-  const double nu_c = fmax(4.0 / 3.0, A.gamma / A.Pr);
+  const double kv = fmax(4.0 / 3.0, A.gamma / A.Pr) / A.Re;
   for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N; c += (long)gridDim.x * blockDim.x) {
     const int i = (int)(c % nchi), j = (int)(c / nchi);
     const bool flow = !A.shock || (j + 1 < A.cell_idx[i]);
-    auto lam_lr = [&](int fi) {
-      const long L = gidx(fi, j + 1, nchi), R = L + 1;
-      const long f = fi + (long)j * (nchi + 1);
-      const double rs = A.S.rho[L] + A.S.rho[R];
-      const double uf = (A.S.ru[L] + A.S.ru[R]) / rs, vf = (A.S.rv[L] + A.S.rv[R]) / rs;
-      return (fabs(uf * A.m.lr_xn[f] + vf * A.m.lr_yn[f]) + cmax) * A.m.lr_a[f];
-    };
-    auto lam_bt = [&](int fj) {
-      const long B = gidx(i + 1, fj, nchi), Tt = B + (nchi + 2);
-      const long f = i + (long)fj * nchi;
-      const double rs = A.S.rho[B] + A.S.rho[Tt];
-      const double uf = (A.S.ru[B] + A.S.ru[Tt]) / rs, vf = (A.S.rv[B] + A.S.rv[Tt]) / rs;
-      return (fabs(uf * A.m.bt_xn[f] + vf * A.m.bt_yn[f]) + cmax) * A.m.bt_a[f];
-    };
     if (flow) {
-      const double lam_c = fmax(lam_lr(i), lam_lr(i + 1)) + fmax(lam_bt(j), lam_bt(j + 1));
+      const long fw = i + (long)j * (nchi + 1), fs = i + (long)j * nchi;
+      const double lam_c = fmax(A.lam_lr[fw], A.lam_lr[fw + 1]) + fmax(A.lam_bt[fs], A.lam_bt[fs + nchi]);
       const long g = gidx(i + 1, j + 1, nchi);
-      const double Axi = 0.5 * (A.m.lr_a[i + (long)j * (nchi + 1)] + A.m.lr_a[i + 1 + (long)j * (nchi + 1)]);
-      const double Aeta = 0.5 * (A.m.bt_a[i + (long)j * nchi] + A.m.bt_a[i + (long)(j + 1) * nchi]);
-      const double vol = A.m.vol[c];
-      double Re_flow = A.Re;  // Re / mu* (UPDATE_CHEMISTRY_EQUILIBRIUM.jl:99-101); mu* = 1 for CPG
-      if (A.suth) {
-        const double r = A.S.rho[g];
-        const double e = (A.S.rE[g] - (A.S.ru[g] * A.S.ru[g] + A.S.rv[g] * A.S.rv[g]) / r / 2) / r;
-        const double Ts = e * A.Tinf_inv;
-        Re_flow = A.Re / (Ts * sqrt(Ts) * (1 + A.suthS) / (Ts + A.suthS));
-      }
-      const double nu_eff = nu_c / (A.S.rho[g] * Re_flow);
-      const double lam_v = 2 * nu_eff * (Axi * Axi + Aeta * Aeta) / vol;
-      mlam = fmax(mlam, (lam_c + lam_v) / vol);
       const double r = A.S.rho[g];
-      const double t_u = (fabs(A.SF2[c]) + fabs(A.SF1[c])) / r;
-      const double t_r = fabs(A.SF0[c] / r);
-      const double t_E = fabs(A.SF3[c] / A.S.rE[g]);
+      const double ir = frcp(r);
+      double mu = 1.0;  // Re_flow = Re / mu* (UPDATE_CHEMISTRY_EQUILIBRIUM.jl:99-101); mu* = 1 for CPG
+      if (A.suth) {
+        const double e = fma(-0.5, fma(A.S.ru[g], A.S.ru[g], A.S.rv[g] * A.S.rv[g]) * ir, A.S.rE[g]) * ir;
+        const double Ts = e * A.Tinf_inv;
+        mu = Ts * sqrt(Ts) * (1 + A.suthS) * frcp(Ts + A.suthS);
+      }
+      const double lam_v = kv * A.m.gvis[c] * ir * mu;
+      mlam = fmax(mlam, (lam_c + lam_v) * A.m.rvol[c]);
+      const double t_u = (fabs(A.SF2[c]) + fabs(A.SF1[c])) * ir;
+      const double t_r = fabs(A.SF0[c] * ir);
+      const double t_E = fabs(A.SF3[c] * frcp(A.S.rE[g]));
       mflux = fmax(mflux, fmax(t_u, fmax(t_r, t_E)));
     }
   }
@@ -1148,38 +1341,97 @@ void launch_update_thermo(const DevCtx& d, int mode, double cY, double cS, cudaS
   a.neta = d.neta;
   a.mode = mode;
   a.shock = d.cfg.shock_enabled;
+  a.aY = d.aY;
+  a.nrcbc = (d.cfg.bc_chi0 == HYMOR_BC_OUTFLOW_NRCBC) | ((d.cfg.bc_chi1 == HYMOR_BC_OUTFLOW_NRCBC) << 1) |
+            ((d.cfg.bc_eta0 == HYMOR_BC_OUTFLOW_NRCBC) << 2) | ((d.cfg.bc_eta1 == HYMOR_BC_OUTFLOW_NRCBC) << 3);
   k_update_thermo<<<grid_for(d.G, 256), 256, 0, st>>>(a);
+}
+
+void launch_spline(const DevCtx& d, bool on_S, bool copy_pts, cudaStream_t st) {
+  const hymor_config& c = d.cfg;
+  if (!c.shock_enabled) return;
+  SplineArgs sa;
+  sa.pts = on_S ? d.Sp : d.Yp;
+  sa.pS = d.Sp;
+  sa.ws = d.spl;
+  sa.lam = (1 - c.spline_param) / c.spline_param;
+  sa.n = d.nchi;
+  sa.copy_pts = copy_pts;
+  k_spline_rows<<<(d.nchi + 127) / 128, 128, 0, st>>>(sa);
+  k_spline_fit<<<1, 1024, sizeof(float) * 14 * d.nchi, st>>>(sa);
+}
+
+void launch_columns_bc(const DevCtx& d, bool on_S, bool move, double cY, double cS, int a_mode, bool do_shock,
+                       bool do_bc, cudaStream_t st) {
+  const hymor_config& c = d.cfg;
+  const Cons& tgt = on_S ? d.S : d.Y;
+  const ShockPts& pts = on_S ? d.Sp : d.Yp;
+  const bool shock = c.shock_enabled && do_shock;
+  if (shock) {
+    ColArgs ca;
+    ca.cfg = c;
+    ca.tgt = tgt;
+    ca.p = d.p;
+    ca.pts = pts;
+    ca.pS = d.Sp;
+    ca.ws = d.spl;
+    ca.cell_idx = d.cell_idx;
+    ca.beta = d.beta;
+    ca.speed_x = d.speed_x;
+    ca.speed_y = d.speed_y;
+    ca.rel = d.rel;
+    ca.scal = d.scal;
+    ca.err = d.err;
+    ca.m = d.m;
+    ca.cY = cY;
+    ca.cS = cS;
+    ca.move = move;
+    ca.on_S = on_S;
+    ca.disturbed = c.dist_amp[0] != 0 || c.dist_amp[1] != 0 || c.dist_amp[2] != 0 || c.dist_amp[3] != 0;
+    {
+      const double rho = c.rho_0, ru = c.rho_u_0, rv = c.rho_v_0, rE = c.rho_E_0;
+      const double vi = rv / rho, ui = ru / rho;
+      const double um = std::sqrt(vi * vi + ui * ui);
+      const double e_inf = (rE - rho * (um * um) * 0.5) / rho;
+      ca.p_inf = e_inf * rho * (c.gamma - 1.0);
+      ca.u_inf = ui;
+      ca.v_inf = vi;
+      ca.rho_inf = rho;
+    }
+    k_shock_columns<<<(d.nchi + 127) / 128, 128, 0, st>>>(ca);
+  }
+  const bool fix = shock && move && c.bc_chi0 == HYMOR_BC_SYMMETRY;
+  if (do_bc || fix) {
+    BcArgs ba;
+    ba.cfg = c;
+    ba.q = tgt;
+    ba.p = d.p;
+    ba.T = d.T;
+    ba.a_bc = (a_mode == 0) ? d.aY : d.aS;
+    ba.m = d.m;
+    ba.pts = pts;
+    ba.pS = d.Sp;
+    ba.on_S = on_S;
+    ba.fix_pts = fix;
+    if (!do_bc) {
+      // only the shock-point symmetry copy
+      ba.cfg.bc_chi0 = HYMOR_BC_SHOCK;
+      ba.cfg.bc_chi1 = HYMOR_BC_SHOCK;
+    }
+    ba.phase = 0;
+    k_bc_edges<<<(2 * d.NJ + 255) / 256, 256, 0, st>>>(ba);
+    if (do_bc) {
+      ba.phase = 1;
+      ba.fix_pts = 0;
+      k_bc_edges<<<(2 * d.NI + 255) / 256, 256, 0, st>>>(ba);
+    }
+  }
 }
 
 static void launch_shock_bc_impl(const DevCtx& d, bool on_S, bool copy_pts, bool move, double cY, double cS,
                                  int a_mode, bool do_shock, bool do_bc, cudaStream_t st) {
-  ShockArgs A;
-  A.do_shock = do_shock;
-  A.do_bc = do_bc;
-  A.cfg = d.cfg;
-  A.tgt = on_S ? d.S : d.Y;
-  A.p = d.p;
-  A.T = d.T;
-  A.compute_a = (a_mode == 0);
-  A.a_bc = (a_mode == 0) ? d.aY : d.aS;
-  A.pts = on_S ? d.Sp : d.Yp;
-  A.pS = d.Sp;
-  A.copy_pts = copy_pts;
-  A.move = move;
-  A.on_S = on_S;
-  A.cY = cY;
-  A.cS = cS;
-  A.cell_idx = d.cell_idx;
-  A.beta = d.beta;
-  A.speed_x = d.speed_x;
-  A.speed_y = d.speed_y;
-  A.rel = d.rel;
-  A.spl = d.spl;
-  A.scal = d.scal;
-  A.err = d.err;
-  A.m = d.m;
-  const size_t smem = d.cfg.shock_enabled ? sizeof(double) * 7 * d.nchi : 0;
-  k_shock_bc<<<1, 1024, smem, st>>>(A);
+  if (do_shock) launch_spline(d, on_S, copy_pts, st);
+  launch_columns_bc(d, on_S, move, cY, cS, a_mode, do_shock, do_bc, st);
 }
 
 void launch_shock_bc(const DevCtx& d, bool on_S, bool copy_pts, bool move, double cY, double cS,
@@ -1192,8 +1444,9 @@ void launch_shock_bc_flags(const DevCtx& d, bool on_S, bool copy_pts, bool do_sh
   launch_shock_bc_impl(d, on_S, copy_pts, false, 0, 0, a_mode, do_shock, do_bc, st);
 }
 
-void launch_flux(const DevCtx& d, bool on_S, double* const out[4], cudaStream_t st) {
+void launch_flux_class(const DevCtx& d, bool on_S, double* const out[4], int tile_class, cudaStream_t st) {
   FluxArgs a;
+  a.tile_class = tile_class;
   const Cons& q = on_S ? d.S : d.Y;
   a.rho = q.rho; a.ru = q.ru; a.rv = q.rv; a.rE = q.rE;
   a.p = d.p;
@@ -1220,12 +1473,16 @@ void launch_flux(const DevCtx& d, bool on_S, double* const out[4], cudaStream_t 
   else k_flux<true, true><<<grid, kFluxThreads, flux_smem<true, true>(), st>>>(a);
 }
 
+void launch_flux(const DevCtx& d, bool on_S, double* const out[4], cudaStream_t st) {
+  launch_flux_class(d, on_S, out, -1, st);
+}
+
 void flux_kernel_setup() {
   cudaFuncSetAttribute(k_flux<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem<false, false>());
   cudaFuncSetAttribute(k_flux<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem<true, false>());
   cudaFuncSetAttribute(k_flux<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem<false, true>());
   cudaFuncSetAttribute(k_flux<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem<true, true>());
-  cudaFuncSetAttribute(k_shock_bc, cudaFuncAttributeMaxDynamicSharedMemorySize, 7 * 8 * 4096);
+  cudaFuncSetAttribute(k_spline_fit, cudaFuncAttributeMaxDynamicSharedMemorySize, 14 * 4 * 4096);
 }
 
 void launch_flow_cells(const DevCtx& d, cudaStream_t st) {
@@ -1237,7 +1494,7 @@ void launch_flow_cells(const DevCtx& d, cudaStream_t st) {
   A.cell_idx = d.cell_idx;
   A.scal = d.scal;
   A.err = d.err;
-  k_flow_cells<<<(d.nchi + 127) / 128, 128, 0, st>>>(A);
+  k_flow_cells<<<(d.nchi * 32 + 255) / 256, 256, 0, st>>>(A);
 }
 
 void launch_sound_cmax(const DevCtx& d, bool recompute, cudaStream_t st) {
@@ -1269,6 +1526,9 @@ void launch_cfl(const DevCtx& d, cudaStream_t st) {
   A.nchi = d.nchi;
   A.neta = d.neta;
   A.shock = d.cfg.shock_enabled;
+  A.lam_lr = d.cflw;
+  A.lam_bt = d.cflw + d.NLR;
+  k_cfl_faces<<<grid_for(d.NLR + d.NBT, 256), 256, 0, st>>>(A);
   k_cfl<<<grid_for(d.N, 256), 256, 0, st>>>(A);
   k_cfl_final<<<1, 1, 0, st>>>(d.scal, d.cfg.CFL, d.cfg.max_dt);
 }

@@ -22,6 +22,7 @@ struct DevCtx {
   int* cell_idx;   // 1-based shocked rows (Nchi)
   double *beta, *speed_x, *speed_y, *rel;  // Nchi
   double* spl;     // spline workspace (device, sized for Nchi)
+  double* cflw;    // CFL face rates (NLR + NBT)
   double* scal;    // Scalar block
   unsigned* err;   // ErrWord block
   // Jacobian
@@ -41,8 +42,15 @@ void launch_update_thermo(const DevCtx& d, int mode, double cY, double cS, cudaS
 //           update and use it (PDE); 1 = use the persistent aS (ADVECT_FLOW step end)
 void launch_shock_bc(const DevCtx& d, bool on_S, bool copy_pts, bool move, double cY, double cS,
                      int a_mode, cudaStream_t st);
+// The two halves of launch_shock_bc: the smoothing-spline fit of the shock points
+// (depends only on the points) and the per-column jump + boundary conditions.
+void launch_spline(const DevCtx& d, bool on_S, bool copy_pts, cudaStream_t st);
+void launch_columns_bc(const DevCtx& d, bool on_S, bool move, double cY, double cS, int a_mode, bool do_shock,
+                       bool do_bc, cudaStream_t st);
 // Flux (residual) of tgt into out[4] (masked by the flow cells when feedback is on).
 void launch_flux(const DevCtx& d, bool on_S, double* const out[4], cudaStream_t st);
+// tile_class 0: only tiles whose halo no shock/BC kernel writes; 1: the other tiles
+void launch_flux_class(const DevCtx& d, bool on_S, double* const out[4], int tile_class, cudaStream_t st);
 // UPDATE_FLOW_CELLS part 1: detect shocked cells, upstream fill, extrapolation (on S).
 void launch_flow_cells(const DevCtx& d, cudaStream_t st);
 // Sound speed of S (recompute) and max|a| into scal[kCmax]; recompute=false only reduces aS.

@@ -16,6 +16,7 @@ DevCtx& ctx_dev(hymor_ctx* c);
 cudaStream_t ctx_stream(hymor_ctx* c);
 int ctx_fail(hymor_ctx* c, int code, const char* msg);
 std::vector<void*>& ctx_allocs(hymor_ctx* c);
+void*& ctx_expm_cache(hymor_ctx* c);
 void launch_shock_bc_flags(const DevCtx& d, bool on_S, bool copy_pts, bool do_shock, bool do_bc, int a_mode,
                            cudaStream_t st);
 
@@ -48,6 +49,8 @@ Wrap make_wrap(const hymor_config& c) {
 struct PertArgs {
   Cons S, Y;
   double *p, *T;
+  double* aY;
+  int nrcbc;
   const int* cell_idx;
   double eps, gm1;
   int nchi, neta, var, colour, shock;
@@ -72,6 +75,12 @@ __global__ void k_perturb_thermo(PertArgs a) {
     const double eint = fma(-0.5, ke, v[3]);
     a.p[k] = eint * a.gm1;
     a.T[k] = eint * ir;
+    if (a.nrcbc) {
+      const int NJ = a.neta + 2;
+      const bool nb = ((a.nrcbc & 1) && i == 1) || ((a.nrcbc & 2) && i == NI - 2) ||
+                      ((a.nrcbc & 4) && j == 1) || ((a.nrcbc & 8) && j == NJ - 2);
+      if (nb) a.aY[k] = sqrt((a.gm1 + 1) * (eint * a.gm1) / v[0]);
+    }
   }
 }
 
@@ -327,16 +336,11 @@ void launch_matvec(const DevCtx& d, int k, const double* X, double* Y, int trans
 }
 
 // POWER_METHOD! (Eigenvalues/ARNOLDI_POWER_GPU.jl:64-82): per step vout = v,
-// term_j = (A dt) term_{j-1}, vout += term_j / j!, v = vout.
-void launch_expm(const DevCtx& d, int k, double dt, int nsteps, int order, const double* X, double* Yout,
-                 int transpose, double* work, cudaStream_t st) {
+// term_j = (A dt) term_{j-1}, vout += term_j / j!, v = vout. The body assumes v and vout
+// already hold the input.
+static void launch_expm_body(const DevCtx& d, int k, double dt, int nsteps, int order, double* v, double* t1,
+                             double* t2, double* vout, int transpose, cudaStream_t st) {
   const long n = 4 * d.N * (long)k;
-  double* v = work;
-  double* t1 = work + n;
-  double* t2 = work + 2 * n;
-  double* vout = Yout;
-  k_copy<<<grid_for(n, 256), 256, 0, st>>>(X, v, n);
-  k_copy<<<grid_for(n, 256), 256, 0, st>>>(X, vout, n);
   MvArgs a;
   a.coef = d.coef;
   a.w = make_wrap(d.cfg);
@@ -361,6 +365,17 @@ void launch_expm(const DevCtx& d, int k, double dt, int nsteps, int order, const
   }
 }
 
+void launch_expm(const DevCtx& d, int k, double dt, int nsteps, int order, const double* X, double* Yout,
+                 int transpose, double* work, cudaStream_t st) {
+  const long n = 4 * d.N * (long)k;
+  double* v = work;
+  double* t1 = work + n;
+  double* t2 = work + 2 * n;
+  k_copy<<<grid_for(n, 256), 256, 0, st>>>(X, v, n);
+  k_copy<<<grid_for(n, 256), 256, 0, st>>>(X, Yout, n);
+  launch_expm_body(d, k, dt, nsteps, order, v, t1, t2, Yout, transpose, st);
+}
+
 void launch_jacobian_assemble(DevCtx& d, cudaStream_t st) {
   const hymor_config& c = d.cfg;
   const long N = d.N;
@@ -381,6 +396,9 @@ void launch_jacobian_assemble(DevCtx& d, cudaStream_t st) {
   pa.nchi = d.nchi;
   pa.neta = d.neta;
   pa.shock = c.shock_enabled;
+  pa.aY = d.aY;
+  pa.nrcbc = (c.bc_chi0 == HYMOR_BC_OUTFLOW_NRCBC) | ((c.bc_chi1 == HYMOR_BC_OUTFLOW_NRCBC) << 1) |
+             ((c.bc_eta0 == HYMOR_BC_OUTFLOW_NRCBC) << 2) | ((c.bc_eta1 == HYMOR_BC_OUTFLOW_NRCBC) << 3);
   // base output: NON_LINEAR_DYNAMICS(deepcopy(s))
   pa.var = -1;
   pa.colour = 1;
@@ -432,7 +450,94 @@ int cuda_check(hymor_ctx* ctx, cudaError_t e) {
   if (e != cudaSuccess) return ctx_fail(ctx, HYMOR_ERR_CUDA, cudaGetErrorString(e));
   return 0;
 }
+
+// Replayed propagations: the nsteps * (order + 1) launches of one propagation are captured
+// once into a CUDA graph over four fixed context buffers (v, two Taylor terms, vout); a
+// call copies its input into v and vout, launches the graph and copies vout out. This
+// removes the per-launch overhead that dominates small grids (a 200 x 100 stencil matvec is
+// ~5 us of FP64 work).
+struct ExpmGraph {
+  cudaGraphExec_t exec = nullptr;
+  int k = 0, nsteps = 0, order = 0, transpose = 0;
+  double dt = 0;
+  double* buf = nullptr;
+};
+struct ExpmCache {
+  double* buf = nullptr;
+  long cap = 0;  // doubles
+  std::vector<ExpmGraph> graphs;
+};
+ExpmCache& expm_cache(hymor_ctx* ctx) {
+  void*& slot = ctx_expm_cache(ctx);
+  if (!slot) slot = new ExpmCache();
+  return *static_cast<ExpmCache*>(slot);
+}
+constexpr int kExpmGraphMinLaunches = 16;
+constexpr size_t kExpmGraphCacheSize = 4;
+
+int expm_via_graph(hymor_ctx* ctx, int k, double dt, int nsteps, int order, const double* dX, double* dY,
+                   int transpose) {
+  DevCtx& d = ctx_dev(ctx);
+  cudaStream_t st = ctx_stream(ctx);
+  ExpmCache& c = expm_cache(ctx);
+  const long n = 4 * d.N * (long)k;
+  int r;
+  if (4 * n > c.cap) {
+    if ((r = cuda_check(ctx, cudaStreamSynchronize(st)))) return r;
+    for (auto& g : c.graphs) cudaGraphExecDestroy(g.exec);
+    c.graphs.clear();
+    if (c.buf) cudaFree(c.buf);
+    c.buf = nullptr;
+    c.cap = 0;
+    void* p = nullptr;
+    if ((r = cuda_check(ctx, cudaMalloc(&p, sizeof(double) * 4 * n)))) return r;
+    c.buf = static_cast<double*>(p);
+    c.cap = 4 * n;
+  }
+  double* v = c.buf;
+  double* t1 = c.buf + n;
+  double* t2 = c.buf + 2 * n;
+  double* vout = c.buf + 3 * n;
+  ExpmGraph* g = nullptr;
+  for (auto& e : c.graphs)
+    if (e.k == k && e.nsteps == nsteps && e.order == order && e.transpose == transpose && e.dt == dt && e.buf == c.buf)
+      g = &e;
+  if (!g) {
+    if (c.graphs.size() >= kExpmGraphCacheSize) {
+      if ((r = cuda_check(ctx, cudaStreamSynchronize(st)))) return r;
+      cudaGraphExecDestroy(c.graphs.front().exec);
+      c.graphs.erase(c.graphs.begin());
+    }
+    cudaGraph_t graph = nullptr;
+    if ((r = cuda_check(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal)))) return r;
+    launch_expm_body(d, k, dt, nsteps, order, v, t1, t2, vout, transpose, st);
+    const cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if ((r = cuda_check(ctx, e))) return r;
+    ExpmGraph ng;
+    ng.k = k; ng.nsteps = nsteps; ng.order = order; ng.transpose = transpose; ng.dt = dt; ng.buf = c.buf;
+    r = cuda_check(ctx, cudaGraphInstantiate(&ng.exec, graph, 0));
+    cudaGraphDestroy(graph);
+    if (r) return r;
+    c.graphs.push_back(ng);
+    g = &c.graphs.back();
+  }
+  if ((r = cuda_check(ctx, cudaMemcpyAsync(v, dX, sizeof(double) * n, cudaMemcpyDeviceToDevice, st)))) return r;
+  if ((r = cuda_check(ctx, cudaMemcpyAsync(vout, dX, sizeof(double) * n, cudaMemcpyDeviceToDevice, st)))) return r;
+  if ((r = cuda_check(ctx, cudaGraphLaunch(g->exec, st)))) return r;
+  return cuda_check(ctx, cudaMemcpyAsync(dY, vout, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+}
 }  // namespace
+
+namespace hymor {
+// Called by hymor_ctx_destroy after its stream has drained.
+void expm_cache_release(void* p) {
+  if (!p) return;
+  ExpmCache* c = static_cast<ExpmCache*>(p);
+  for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+  if (c->buf) cudaFree(c->buf);
+  delete c;
+}
+}  // namespace hymor
 
 extern "C" {
 
@@ -520,6 +625,7 @@ int hymor_expm_apply_dev(hymor_ctx* ctx, int k, double dt, int nsteps, int order
   DevCtx& d = ctx_dev(ctx);
   if (!d.coef) return ctx_fail(ctx, HYMOR_ERR_NOT_READY, "no Jacobian: call hymor_linearize or hymor_jacobian_set");
   cudaStream_t st = ctx_stream(ctx);
+  if ((long)nsteps * (order + 1) >= kExpmGraphMinLaunches) return expm_via_graph(ctx, k, dt, nsteps, order, dX, dY, transpose);
   const size_t n = 4 * d.N * (size_t)k;
   double* work = nullptr;
   int r;

@@ -7,8 +7,9 @@ module keeps those names and argument meanings: a :class:`Solution` plays the
 Dict (its arrays live on the GPU), and the functions mutate it in place and
 return it, exactly as the reference mutates and returns `s`.
 
-Every call goes through the C ABI (include/hymor.h); nothing here computes
-flow quantities on the CPU.
+Every hot-path call goes through the C ABI (include/hymor.h). The host side only
+assembles small set-up data, as the reference's host code does: the Chu-norm weight
+blocks of transient growth and the projected Krylov matrices (<= ncv x ncv).
 """
 from __future__ import annotations
 
@@ -229,17 +230,28 @@ def EIGENVALUES(L: LinearOperatorGPU, s: Solution, n_modes: int, T_ref: float = 
 
 
 def chu_blocks(s: Solution, norms=(1, 1, 1, 1)):
-    """Per-cell 4x4 blocks of C0 = R'MR and D = R'M^R (CONSTRUCT_R.jl:24-133, CONSTRUCT_M.jl:27-94,
-    CONSTRUCT_M_HAT.jl:25-105) from the current state; host-side set-up like the reference's."""
-    v = s.var()
-    g = s.cfg.gamma
-    rho = v["rho"][1:-1, 1:-1].ravel(order="F")
-    u = (v["rho_u"][1:-1, 1:-1] / v["rho"][1:-1, 1:-1]).ravel(order="F")
-    w = (v["rho_v"][1:-1, 1:-1] / v["rho"][1:-1, 1:-1]).ravel(order="F")
-    rE = v["rho_E"][1:-1, 1:-1].ravel(order="F")
-    p = (rE - (rho * u * u + rho * w * w) / 2) * (g - 1)
+    """Per-cell 4x4 blocks of C0 = R'MR and D = R'M^R for the current state of `s`."""
+    st = s.get_state()
+    return chu_blocks_from_state(s.cfg, s.case.mesh["vol"], st["q"], st["cell_idx"], norms)
+
+
+def chu_blocks_from_state(cfg, vol, qflat, cell_idx, norms=(1, 1, 1, 1)):
+    """CONSTRUCT_R.jl:24-133 (conserved -> (p, u, v, S)), CONSTRUCT_M.jl:27-94 (Chu weights
+    masked by the flow cells) and CONSTRUCT_M_HAT.jl:25-105 (unmasked), as per-cell 4x4
+    blocks of C0 = R'MR and D = R'M^R. Host-side set-up of the transient-growth operator,
+    like the reference's sparse constructions."""
+    nchi, neta = cfg.nchi, cfg.neta
+    g = cfg.gamma
+    q = np.asarray(qflat).reshape(4, nchi + 2, neta + 2, order="C")
+    q = np.asarray(qflat).reshape(4, -1)
+    shape = (nchi + 2, neta + 2)
+    rho_G, ru_G, rv_G, rE_G = (q[k].reshape(shape, order="F")[1:-1, 1:-1].ravel(order="F") for k in range(4))
+    rho = rho_G
+    u = ru_G / rho
+    w = rv_G / rho
+    p = (rE_G - (ru_G**2 + rv_G**2) / rho / 2) * (g - 1)
     a = np.sqrt(g * p / rho)
-    N = s.N
+    N = nchi * neta
     R = np.zeros((N, 4, 4))
     R[:, 0, 0] = (g - 1) * (u**2 + w**2) / 2
     R[:, 0, 1] = -u * (g - 1)
@@ -253,11 +265,12 @@ def chu_blocks(s: Solution, norms=(1, 1, 1, 1)):
     R[:, 3, 1] = -u / p
     R[:, 3, 2] = -w / p
     R[:, 3, 3] = 1.0 / p
-    vol = s.case.mesh["vol"].ravel(order="F")
-    st = s.get_state()
-    flow = (np.arange(1, s.neta + 1)[None, :] < st["cell_idx"][:, None]).ravel(order="F") if s.cfg.shock_enabled \
-        else np.ones(N)
-    mh = np.stack([rho * a**2 / (2 * (g * p) ** 2), rho / 2, rho / 2, (g - 1) * p / (2 * g)], axis=1) * vol[:, None]
+    v = np.asarray(vol).ravel(order="F")
+    if cfg.shock_enabled:
+        flow = (np.arange(1, neta + 1)[None, :] < np.asarray(cell_idx)[:, None]).ravel(order="F").astype(float)
+    else:
+        flow = np.ones(N)
+    mh = np.stack([rho * a**2 / (2 * (g * p) ** 2), rho / 2, rho / 2, (g - 1) * p / (2 * g)], axis=1) * v[:, None]
     mh = mh * np.asarray(norms, dtype=float)[None, :]
     m = mh * flow[:, None]
     C0 = np.einsum("nki,nk,nkj->nij", R, m, R)

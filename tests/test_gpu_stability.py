@@ -1,0 +1,113 @@
+"""GPU stability drivers: the exponential-transform eigen solver and transient growth
+(device-resident Krylov-Schur) against ARPACK on the oracle's propagator, with the same
+Jacobian blocks, plus the adjoint identities of the propagator and the FD check of the
+linearisation."""
+import numpy as np
+import pytest
+
+from hymor_gb300 import case as C
+from hymor_gb300 import solver as S
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(nchi, neta, steps=20):
+    cfg = C.cylinder_config(nchi, neta)
+    cs = C.initial_state(cfg)
+    sol, orc = S.Solution(cs), O.Oracle(cs)
+    S.ADVECT_FLOW(sol, steps)
+    orc.advect(steps)
+    return cfg, cs, sol, orc
+
+
+def test_eigenvalues_device_vs_oracle(require_gpu):
+    sla = pytest.importorskip("scipy.sparse.linalg")
+    cfg, cs, sol, orc = _setup(30, 20)
+    _, L = S.LINEARIZE_L(sol)
+    co = orc.linearize()
+    L.set_blocks(co)
+    lam, info = S.EIGENVALUES(L, sol, 4, T_ref=0.02, ncv=24, tol=1e-11)
+    dt, nt = info["dt"], info["timesteps"]
+    n = 4 * cfg.nchi * cfg.neta
+    op = sla.LinearOperator((n, n), matvec=lambda x: orc.expm(co, dt, nt, np.ascontiguousarray(x).ravel()),
+                            dtype=np.float64)
+    mu = sla.eigs(op, k=4, which="LM", tol=1e-13, ncv=24, return_eigenvectors=False)
+    mu = mu[np.argsort(-np.abs(mu))]
+    lam_o = np.log(mu.astype(complex)) / (dt * nt)
+    for a in lam:
+        assert np.min(np.abs(lam_o - a)) <= 1e-8 * np.max(np.abs(lam_o))
+    assert np.all(info["resid"] <= 1e-11 * np.abs(info["mu"]))
+    # the reference's structure (host ARPACK, one GPU propagation per vector) agrees
+    lam_h, _ = S.EIGENVALUES(L, sol, 4, T_ref=0.02, ncv=24, tol=1e-12, method="host")
+    for a in lam:
+        assert np.min(np.abs(lam_h - a)) <= 1e-8 * np.max(np.abs(lam_o))
+
+
+def test_transient_growth_device_vs_oracle(require_gpu):
+    sla = pytest.importorskip("scipy.sparse.linalg")
+    cfg, cs, sol, orc = _setup(24, 24)
+    _, L = S.LINEARIZE_L(sol)
+    co = orc.linearize()
+    L.set_blocks(co)
+    T = 0.01
+    G, info = S.TRANSIENT_GROWTH_DOWNSTREAM(L, sol, 2, T, ncv=16, tol=1e-11)
+    st = sol.get_state()
+    C0, D = S.chu_blocks_from_state(cfg, cs.mesh["vol"], st["q"], st["cell_idx"])
+    K = np.linalg.cholesky(D)
+    Ki = np.linalg.inv(K)
+    N = cfg.nchi * cfg.neta
+
+    def blk(B, x):
+        X = x.reshape(4, N).T
+        return np.einsum("nij,nj->ni", B, X).T.ravel()
+    dt, nt = info["dt"], info["n_t"]
+
+    def mv(y):
+        x = blk(np.transpose(Ki, (0, 2, 1)), np.ascontiguousarray(y).ravel())
+        z = orc.expm(co, dt, nt, x)
+        z = blk(C0, z)
+        z = orc.expm(co, dt, nt, z, transpose=True)
+        return blk(Ki, z)
+    op = sla.LinearOperator((4 * N, 4 * N), matvec=mv, dtype=np.float64)
+    Go = np.sort(sla.eigsh(op, k=2, which="LA", tol=1e-13, return_eigenvectors=False))[::-1]
+    assert np.allclose(np.sort(G)[::-1], Go, rtol=1e-6, atol=0)
+
+
+def test_propagator_adjoint_identity(require_gpu):
+    """<P x, y> = <x, Pᵀ y> for the Taylor propagator and its adjoint (the dot-product test)."""
+    cfg, cs, sol, orc = _setup(30, 20, steps=5)
+    _, L = S.LINEARIZE_L(sol)
+    rng = np.random.Generator(np.random.PCG64(4))
+    n = 4 * cfg.nchi * cfg.neta
+    x, y = rng.standard_normal(n), rng.standard_normal(n)
+    dt = S.CFL_TIMESTEP(sol)
+    Px = L.expm(x, dt, 25)
+    Pty = L.T.expm(y, dt, 25)
+    lhs, rhs = np.dot(Px, y), np.dot(x, Pty)
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+
+
+def test_linearisation_matches_residual_differences(require_gpu):
+    """CHECK_LINEARIZATION_L.jl:33-130 on the GPU: L q ~ f(x + q) - f(x) (central, h = 1e-7)."""
+    cfg, cs, sol, orc = _setup(30, 20, steps=10)
+    _, L = S.LINEARIZE_L(sol)
+    st = sol.get_state()
+    N = cfg.nchi * cfg.neta
+    rng = np.random.Generator(np.random.PCG64(5))
+    flow = (np.arange(1, cfg.neta + 1)[None, :] < st["cell_idx"][:, None]).ravel(order="F")
+    dq = rng.standard_normal(4 * N) * np.tile(flow, 4)
+    h = 1e-7
+
+    def residual_at(sign):
+        q = st["q"].copy().reshape(4, -1)
+        for v in range(4):
+            blk = q[v].reshape(cfg.nchi + 2, cfg.neta + 2, order="F")
+            blk[1:-1, 1:-1] += sign * h * dq[v * N:(v + 1) * N].reshape(cfg.nchi, cfg.neta, order="F")
+            q[v] = blk.ravel(order="F")
+        s2 = S.Solution(cs)
+        s2.set_state(q.ravel(), st["pts_x"], st["pts_y"], st["pts_chi"], st["pts_eta"], st["cell_idx"], st["t"])
+        return S.PDE(s2)
+    df = (residual_at(+1) - residual_at(-1)) / (2 * h)
+    Lq = L @ dq
+    assert np.linalg.norm(Lq - df) / np.linalg.norm(df) < 1e-3
