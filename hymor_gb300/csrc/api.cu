@@ -11,7 +11,7 @@
 
 namespace hymor {
 void flux_kernel_setup();
-void expm_cache_release(void* p);
+void linear_state_release(void* p);
 }
 
 using namespace hymor;
@@ -20,13 +20,16 @@ struct hymor_ctx_s {
   DevCtx d;
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;      // high-priority stream of the shock/BC chain inside the step graph
+  cudaStream_t fit = nullptr;       // the step's first spline fit, beside the flow cells and the CFL
   cudaEvent_t fork_ev[8] = {}, join_ev[8] = {};
+  cudaEvent_t fit_fork = nullptr, fit_join = nullptr;
   int device = 0;
   std::string err;
   std::vector<void*> allocs;
   // step graph
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
+  int step_kernels = 0;  // kernel nodes of the step graph
   // flux-kernel profiling: event-record nodes around the flux launches of the 4 stages
   // (2 launches per stage: interior tiles, then the shock/boundary tiles)
   bool profile = false;
@@ -40,8 +43,8 @@ struct hymor_ctx_s {
   // L2 flush scratch of hymor_bench_steps
   void* flush_buf = nullptr;
   uint64_t flush_bytes = 0;
-  // replayed propagator graphs and their buffers (linear.cu)
-  void* expm_cache = nullptr;
+  // state of the linear entry points: replayed propagator graphs, Krylov scratch (linear.cu)
+  void* linear_state = nullptr;
 };
 
 namespace {
@@ -202,15 +205,22 @@ int enqueue_step(hymor_ctx* ctx, bool with_events) {
     return 0;
   };
   CU(cudaMemsetAsync(d.scal + kCmax, 0, 3 * sizeof(double), st));
-  if (shock) launch_flow_cells(d, st);
   if (c.rk_variant == 0) {
-    // Side stream: the CFL reduction, and every smoothing-spline fit one stage early (a
-    // fit needs only the shock points, which the previous stage's jump kernel moved);
-    // then per stage the jump + boundary kernels beside the flux of the interior tiles.
+    // Third stream: the first fit reads only the shock points of S, which nothing before
+    // the first jump kernel changes, so it runs beside the flow cells and the CFL.
+    CU(cudaEventRecord(ctx->fit_fork, st));
+    CU(cudaStreamWaitEvent(ctx->fit, ctx->fit_fork, 0));
+    launch_spline(d, false, true, ctx->fit);
+    CU(cudaEventRecord(ctx->fit_join, ctx->fit));
+    if (shock) launch_flow_cells(d, st);
+    // Side stream: the CFL reduction, and every later smoothing-spline fit one stage
+    // early (a fit needs only the shock points, which the previous stage's jump kernel
+    // moved); then per stage the jump + boundary kernels beside the flux of the
+    // interior tiles.
     TRY(fork());
     launch_sound_cmax(d, shock, sx);
     launch_cfl(d, sx);
-    launch_spline(d, false, true, sx);
+    CU(cudaStreamWaitEvent(sx, ctx->fit_join, 0));
     launch_update_thermo(d, 0, 0, 0, st);
     for (int k = 0; k < 4; ++k) {
       if (k > 0) launch_update_thermo(d, 1, wY[k - 1], wA[k - 1], st);
@@ -230,6 +240,7 @@ int enqueue_step(hymor_ctx* ctx, bool with_events) {
     TRY(join());
     launch_columns_bc(d, true, false, 0, 0, 1, true, true, st);
   } else {
+    if (shock) launch_flow_cells(d, st);
     launch_sound_cmax(d, shock, st);
     launch_cfl(d, st);
     launch_snapshot(d, st);
@@ -273,9 +284,11 @@ int build_graph(hymor_ctx* ctx) {
   CU(cudaGraphGetNodes(g, nullptr, &nn));
   std::vector<cudaGraphNode_t> nodes(nn);
   CU(cudaGraphGetNodes(g, nodes.data(), &nn));
+  ctx->step_kernels = 0;
   for (auto n : nodes) {
     cudaGraphNodeType ty;
     CU(cudaGraphNodeGetType(n, &ty));
+    if (ty == cudaGraphNodeTypeKernel) ++ctx->step_kernels;
     if (ty != cudaGraphNodeTypeEventRecord) continue;
     cudaEvent_t ev;
     CU(cudaGraphEventRecordNodeGetEvent(n, &ev));
@@ -409,8 +422,12 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
   {
     int lo = 0, hi = 0;
     cudaDeviceGetStreamPriorityRange(&lo, &hi);
-    if (cudaStreamCreateWithPriority(&ctx->side, cudaStreamNonBlocking, hi) != cudaSuccess)
+    if (cudaStreamCreateWithPriority(&ctx->side, cudaStreamNonBlocking, hi) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&ctx->fit, cudaStreamNonBlocking, hi) != cudaSuccess)
       return bail(fail(ctx, HYMOR_ERR_CUDA, "side stream creation failed"));
+    if (cudaEventCreateWithFlags(&ctx->fit_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->fit_join, cudaEventDisableTiming) != cudaSuccess)
+      return bail(fail(ctx, HYMOR_ERR_CUDA, "event"));
   }
   cudaEventCreate(&ctx->t0);
   cudaEventCreate(&ctx->t1);
@@ -424,7 +441,7 @@ int hymor_ctx_destroy(hymor_ctx* ctx) {
   if (!ctx) return HYMOR_ERR_INVALID;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  expm_cache_release(ctx->expm_cache);
+  linear_state_release(ctx->linear_state);
   if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
   if (ctx->graph) cudaGraphDestroy(ctx->graph);
   for (auto e : ctx->cap_ev)
@@ -433,7 +450,10 @@ int hymor_ctx_destroy(hymor_ctx* ctx) {
     if (e) cudaEventDestroy(e);
   for (auto e : ctx->join_ev)
     if (e) cudaEventDestroy(e);
+  if (ctx->fit_fork) cudaEventDestroy(ctx->fit_fork);
+  if (ctx->fit_join) cudaEventDestroy(ctx->fit_join);
   if (ctx->side) cudaStreamDestroy(ctx->side);
+  if (ctx->fit) cudaStreamDestroy(ctx->fit);
   for (auto e : ctx->prof_ev) cudaEventDestroy(e);
   if (ctx->t0) cudaEventDestroy(ctx->t0);
   if (ctx->t1) cudaEventDestroy(ctx->t1);
@@ -636,6 +656,14 @@ int hymor_counters(hymor_ctx* ctx, int32_t* rho_limited, int32_t* rh_warnings) {
   return 0;
 }
 
+int hymor_step_kernels(hymor_ctx* ctx, int32_t* n) {
+  if (!ctx || !n) return HYMOR_ERR_INVALID;
+  TRY(set_device(ctx));
+  TRY(build_graph(ctx));
+  *n = ctx->step_kernels;
+  return 0;
+}
+
 int hymor_timer_start(hymor_ctx* ctx) {
   if (!ctx) return HYMOR_ERR_INVALID;
   CU(cudaEventRecord(ctx->t0, ctx->stream));
@@ -735,5 +763,5 @@ DevCtx& ctx_dev(hymor_ctx* c) { return c->d; }
 cudaStream_t ctx_stream(hymor_ctx* c) { return c->stream; }
 int ctx_fail(hymor_ctx* c, int code, const char* msg) { return fail(c, code, "%s", msg); }
 std::vector<void*>& ctx_allocs(hymor_ctx* c) { return c->allocs; }
-void*& ctx_expm_cache(hymor_ctx* c) { return c->expm_cache; }
+void*& ctx_linear_state(hymor_ctx* c) { return c->linear_state; }
 }  // namespace hymor

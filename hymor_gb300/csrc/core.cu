@@ -312,7 +312,8 @@ __device__ void edge_bc_point(const hymor_config& c, const EdgeCtx& e, const Dev
 //                    corners read the chi ghosts), one thread per edge point
 // Spline workspace (units of n = Nchi doubles): 0 knots, 1-2 ordinates x/y, 3-4
 // second derivatives x/y, 5-6 fitted values x/y, 7-11 per-row d0 d1 d2 rhs_x rhs_y,
-// 15 interval reciprocals 1/(x[k+1] - x[k]).
+// 12-14 FP64 Cholesky factors of the fallback solve, 15 interval reciprocals
+// 1/(x[k+1] - x[k]).
 
 // 1/sqrt(a): hardware seed (rsqrt.approx.ftz.f64) refined by two Newton-Raphson
 // steps y <- y (3 - a y^2) / 2 (quadratic convergence, ~2^-80 before rounding).
@@ -385,66 +386,73 @@ __global__ void __launch_bounds__(128) k_spline_rows(SplineArgs A) {
 // banded Cholesky factorisation and the two triangular sweeps run in FP32, and
 // mixed-precision iterative refinement (FP64 residual r = b - A x, FP32 correction
 // solve, x += e; Moler, J. ACM 14 (1967) 316-321) brings the solution to FP64
-// accuracy: A is diagonally dominant (condition number ~4), so each refinement step
-// contracts the error by ~1e-6 and two steps reach the FP64 rounding level.
-constexpr int kRefineSteps = 2;
+// accuracy. Each refinement step contracts the error by about cond(A) * 2^-24; with the
+// default smoothing parameter A is diagonally dominant (condition number ~4) and two
+// steps reach the FP64 rounding level. The loop stops once the correction, scaled by
+// the observed contraction, is below 2^-50 of the solution; when it contracts slower
+// than 1/2 (a heavily smoothed fit whose condition number defeats the FP32 factors) or
+// has not converged after kMaxRefine steps, the fit is redone by a serial FP64
+// Cholesky solve.
+constexpr int kMaxRefine = 8;
 
 constexpr int kChunk = 8;  // rows loaded into registers ahead of each serial sweep block
 
-// Forward and backward FP32 sweeps of L L^T x = r for two right-hand sides.
-//   forward:  z_j = c_j - a_j z_{j-1} - b_j z_{j-2}, with c_j = r_j / l0_j given in cx/cy
-//   backward: x_j = z_j / l0_j - p_j x_{j+1} - q_j x_{j+2}
-// Inputs and outputs are separate __restrict__ arrays so that the loads of a block of
-// rows issue before the dependent FMA chain (one FMA per row on the critical path).
-__device__ __forceinline__ void tri_solve_f32(int m, const float* __restrict__ fa, const float* __restrict__ fb,
-                                              const float* __restrict__ fil, const float* __restrict__ fp,
-                                              const float* __restrict__ fq, const float* __restrict__ cx,
-                                              const float* __restrict__ cy, float* __restrict__ zx,
-                                              float* __restrict__ zy, float* __restrict__ ox,
-                                              float* __restrict__ oy) {
-  float zx1 = 0.f, zx2 = 0.f, zy1 = 0.f, zy2 = 0.f;
+// 8 consecutive floats through two 16-byte shared-memory accesses (p 16-byte aligned).
+__device__ __forceinline__ void ld8(float (&r)[kChunk], const float* __restrict__ p) {
+  const float4 a = reinterpret_cast<const float4*>(p)[0], b = reinterpret_cast<const float4*>(p)[1];
+  r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w; r[4] = b.x; r[5] = b.y; r[6] = b.z; r[7] = b.w;
+}
+__device__ __forceinline__ void st8(float* __restrict__ p, const float (&r)[kChunk]) {
+  reinterpret_cast<float4*>(p)[0] = make_float4(r[0], r[1], r[2], r[3]);
+  reinterpret_cast<float4*>(p)[1] = make_float4(r[4], r[5], r[6], r[7]);
+}
+
+// Forward and backward FP32 sweeps of L L^T x = r for one right-hand side (the two
+// ordinates run on two warps, so that each serial chain issues half the instructions):
+//   forward:  s_j = c_j - a_j s_{j-1} - b_j s_{j-2}, z_j = s_j / l0_j, with c_j = r_j / l0_j
+//   backward: x_j = z_j - p_j x_{j+1} - q_j x_{j+2}
+// Blocks of kChunk rows are loaded with 16-byte accesses (row offsets of the blocks are
+// multiples of 8, the arrays 16-byte aligned) before the dependent FMA chain, which has
+// one FMA per row on its critical path.
+__device__ __forceinline__ void tri_solve1_f32(int m, const float* __restrict__ fa, const float* __restrict__ fb,
+                                               const float* __restrict__ fil, const float* __restrict__ fp,
+                                               const float* __restrict__ fq, const float* __restrict__ c,
+                                               float* __restrict__ z, float* __restrict__ o) {
+  float s1 = 0.f, s2 = 0.f;
   int j = 0;
   for (; j + kChunk <= m; j += kChunk) {
-    float ra[kChunk], rb[kChunk], rx[kChunk], ry[kChunk], ri[kChunk];
-#pragma unroll
-    for (int u = 0; u < kChunk; ++u) { ra[u] = fa[j + u]; rb[u] = fb[j + u]; rx[u] = cx[j + u]; ry[u] = cy[j + u]; ri[u] = fil[j + u]; }
+    float ra[kChunk], rb[kChunk], rc[kChunk], ri[kChunk], rz[kChunk];
+    ld8(ra, fa + j); ld8(rb, fb + j); ld8(rc, c + j); ld8(ri, fil + j);
 #pragma unroll
     for (int u = 0; u < kChunk; ++u) {
-      const float a = fmaf(-ra[u], zx1, fmaf(-rb[u], zx2, rx[u]));
-      const float b = fmaf(-ra[u], zy1, fmaf(-rb[u], zy2, ry[u]));
-      zx[j + u] = a * ri[u];
-      zy[j + u] = b * ri[u];
-      zx2 = zx1; zx1 = a; zy2 = zy1; zy1 = b;
+      const float v = fmaf(-ra[u], s1, fmaf(-rb[u], s2, rc[u]));
+      rz[u] = v * ri[u];
+      s2 = s1; s1 = v;
     }
+    st8(z + j, rz);
   }
   for (; j < m; ++j) {
-    const float a = fmaf(-fa[j], zx1, fmaf(-fb[j], zx2, cx[j]));
-    const float b = fmaf(-fa[j], zy1, fmaf(-fb[j], zy2, cy[j]));
-    zx[j] = a * fil[j];
-    zy[j] = b * fil[j];
-    zx2 = zx1; zx1 = a; zy2 = zy1; zy1 = b;
+    const float v = fmaf(-fa[j], s1, fmaf(-fb[j], s2, c[j]));
+    z[j] = v * fil[j];
+    s2 = s1; s1 = v;
   }
-  float x1 = 0.f, x2 = 0.f, y1 = 0.f, y2 = 0.f;
-  j = m - 1;
-  for (; j - kChunk + 1 >= 0; j -= kChunk) {
-    float rp[kChunk], rq[kChunk], rz[kChunk], rw[kChunk];
+  float x1 = 0.f, x2 = 0.f;
+  const int top = m & ~(kChunk - 1);
+  for (j = m - 1; j >= top; --j) {
+    const float v = fmaf(-fp[j], x1, fmaf(-fq[j], x2, z[j]));
+    o[j] = v;
+    x2 = x1; x1 = v;
+  }
+  for (int j0 = top - kChunk; j0 >= 0; j0 -= kChunk) {
+    float rp[kChunk], rq[kChunk], rz[kChunk], ro[kChunk];
+    ld8(rp, fp + j0); ld8(rq, fq + j0); ld8(rz, z + j0);
 #pragma unroll
-    for (int u = 0; u < kChunk; ++u) { rp[u] = fp[j - u]; rq[u] = fq[j - u]; rz[u] = zx[j - u]; rw[u] = zy[j - u]; }
-#pragma unroll
-    for (int u = 0; u < kChunk; ++u) {
-      const float a = fmaf(-rp[u], x1, fmaf(-rq[u], x2, rz[u]));
-      const float b = fmaf(-rp[u], y1, fmaf(-rq[u], y2, rw[u]));
-      ox[j - u] = a;
-      oy[j - u] = b;
-      x2 = x1; x1 = a; y2 = y1; y1 = b;
+    for (int u = kChunk - 1; u >= 0; --u) {
+      const float v = fmaf(-rp[u], x1, fmaf(-rq[u], x2, rz[u]));
+      ro[u] = v;
+      x2 = x1; x1 = v;
     }
-  }
-  for (; j >= 0; --j) {
-    const float a = fmaf(-fp[j], x1, fmaf(-fq[j], x2, zx[j]));
-    const float b = fmaf(-fp[j], y1, fmaf(-fq[j], y2, zy[j]));
-    ox[j] = a;
-    oy[j] = b;
-    x2 = x1; x1 = a; y2 = y1; y1 = b;
+    st8(o + j0, ro);
   }
 }
 
@@ -455,18 +463,18 @@ __device__ __forceinline__ void chol_f32(int m, const float* __restrict__ fd0, c
   float l1p = 0.f, l2p = 0.f, l2pp = 0.f;
   int j = 0;
   for (; j + kChunk <= m; j += kChunk) {
-    float r0[kChunk], r1[kChunk], r2[kChunk];
-#pragma unroll
-    for (int u = 0; u < kChunk; ++u) { r0[u] = fd0[j + u]; r1[u] = fd1[j + u]; r2[u] = fd2[j + u]; }
+    float r0[kChunk], r1[kChunk], r2[kChunk], o0[kChunk], o1[kChunk], o2[kChunk];
+    ld8(r0, fd0 + j); ld8(r1, fd1 + j); ld8(r2, fd2 + j);
 #pragma unroll
     for (int u = 0; u < kChunk; ++u) {
       const float a = fmaf(-l1p, l1p, fmaf(-l2pp, l2pp, r0[u]));
       const float il = rsqrtf(a);
       const float nl1 = fmaf(-l2p, l1p, r1[u]) * il;
       const float nl2 = r2[u] * il;
-      fil[j + u] = il; fl1[j + u] = nl1; fl2[j + u] = nl2;
+      o0[u] = il; o1[u] = nl1; o2[u] = nl2;
       l2pp = l2p; l2p = nl2; l1p = nl1;
     }
+    st8(fil + j, o0); st8(fl1 + j, o1); st8(fl2 + j, o2);
   }
   for (; j < m; ++j) {
     const float a = fmaf(-l1p, l1p, fmaf(-l2pp, l2pp, fd0[j]));
@@ -478,9 +486,78 @@ __device__ __forceinline__ void chol_f32(int m, const float* __restrict__ fd0, c
   }
 }
 
+// Serial FP64 banded Cholesky solve of A x = r for both ordinates (one thread); the
+// factors go to the workspace slots l0inv, l1, l2 and x overwrites the 1-offset
+// solution arrays gx_, gy_ (gx_[j + 1] = x_j).
+__device__ void chol_solve_f64(int m, const double* __restrict__ d0, const double* __restrict__ d1,
+                               const double* __restrict__ d2, const double* __restrict__ rx,
+                               const double* __restrict__ ry, double* __restrict__ il0, double* __restrict__ l1,
+                               double* __restrict__ l2, double* __restrict__ gx_, double* __restrict__ gy_) {
+  double l1p = 0, l2p = 0, l2pp = 0, zx1 = 0, zx2 = 0, zy1 = 0, zy2 = 0, l1pp = 0;
+  for (int j = 0; j < m; ++j) {
+    const double a = d0[j] - l1p * l1p - l2pp * l2pp;
+    const double il = frsqrt(a);
+    const double nl1 = (d1[j] - l2p * l1p) * il;
+    const double nl2 = d2[j] * il;
+    // forward: l0_j z_j = r_j - l1_{j-1} z_{j-1} - l2_{j-2} z_{j-2}
+    const double zx = (rx[j] - l1p * zx1 - l2pp * zx2) * il;
+    const double zy = (ry[j] - l1p * zy1 - l2pp * zy2) * il;
+    il0[j] = il; l1[j] = nl1; l2[j] = nl2;
+    gx_[j + 1] = zx; gy_[j + 1] = zy;
+    zx2 = zx1; zx1 = zx; zy2 = zy1; zy1 = zy;
+    l2pp = l2p; l2p = nl2; l1pp = l1p; l1p = nl1;
+  }
+  (void)l1pp;
+  // backward: l0_j x_j = z_j - l1_j x_{j+1} - l2_j x_{j+2}
+  double x1 = 0, x2 = 0, y1 = 0, y2 = 0;
+  for (int j = m - 1; j >= 0; --j) {
+    const double xv = (gx_[j + 1] - l1[j] * x1 - l2[j] * x2) * il0[j];
+    const double yv = (gy_[j + 1] - l1[j] * y1 - l2[j] * y2) * il0[j];
+    gx_[j + 1] = xv; gy_[j + 1] = yv;
+    x2 = x1; x1 = xv; y2 = y1; y1 = yv;
+  }
+}
+
+// Block-wide maxima of two non-negative floats (NaN counts as +inf); every thread gets
+// both. red holds 66 floats.
+__device__ __forceinline__ void block_max2_f32(float& v, float& w, float* red) {
+  if (!(v == v)) v = __int_as_float(0x7f800000);
+  if (!(w == w)) w = __int_as_float(0x7f800000);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    w = fmaxf(w, __shfl_xor_sync(0xffffffffu, w, o));
+  }
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) { red[wp] = v; red[32 + wp] = w; }
+  __syncthreads();
+  if (wp == 0) {
+    const bool in = lane < (int)(blockDim.x >> 5);
+    float a = in ? red[lane] : 0.f, b = in ? red[32 + lane] : 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, o));
+      b = fmaxf(b, __shfl_xor_sync(0xffffffffu, b, o));
+    }
+    if (lane == 0) { red[64] = a; red[65] = b; }
+  }
+  __syncthreads();
+  v = red[64];
+  w = red[65];
+}
+
+// Padded row stride of the FP32 arrays of k_spline_fit (a multiple of 4 floats, so that
+// every array starts on a 16-byte boundary).
+__host__ __device__ inline int spline_stride(int n) { return (n - 2 + 3) & ~3; }
+constexpr int kSplineArrays = 14;
+
 __global__ void __launch_bounds__(1024) k_spline_fit(SplineArgs A) {
-  extern __shared__ float shf[];
+  __shared__ float red[66];
+  extern __shared__ float4 shf4[];
+  float* shf = reinterpret_cast<float*>(shf4);
   const int n = A.n, m = n - 2, tid = threadIdx.x, nt = blockDim.x;
+  const int mp = spline_stride(n);
   double* xs = A.ws;
   double* yx = xs + n;
   double* yy = yx + n;
@@ -493,20 +570,20 @@ __global__ void __launch_bounds__(1024) k_spline_fit(SplineArgs A) {
   const double* d2 = d1 + n;
   const double* rx = d2 + n;
   const double* ry = rx + n;
-  float* fil = shf;          // 1 / l0 (FP32)
-  float* fl1 = fil + m;
-  float* fl2 = fl1 + m;
-  float* fa = fl2 + m;       // l1_{j-1} / l0_j
-  float* fb = fa + m;        // l2_{j-2} / l0_j
-  float* fp = fb + m;        // l1_j / l0_j
-  float* fq = fp + m;        // l2_j / l0_j
-  float* wx = fq + m;        // right-hand sides c = r / l0
-  float* wy = wx + m;
-  float* fd0 = wy + m;       // FP32 bands (factorisation input), then forward results
-  float* fd1 = fd0 + m;
-  float* fd2 = fd1 + m;
-  float* ex = fd2 + m;       // corrections
-  float* ey = ex + m;
+  float* fil = shf;           // 1 / l0 (FP32)
+  float* fl1 = fil + mp;
+  float* fl2 = fl1 + mp;
+  float* fa = fl2 + mp;       // l1_{j-1} / l0_j
+  float* fb = fa + mp;        // l2_{j-2} / l0_j
+  float* fp = fb + mp;        // l1_j / l0_j
+  float* fq = fp + mp;        // l2_j / l0_j
+  float* wx = fq + mp;        // right-hand sides c = r / l0
+  float* wy = wx + mp;
+  float* fd0 = wy + mp;       // FP32 bands (factorisation input), then forward results
+  float* fd1 = fd0 + mp;
+  float* fd2 = fd1 + mp;
+  float* ex = fd2 + mp;       // corrections
+  float* ey = ex + mp;
   const double lam = A.lam;
   for (int i = tid; i < n; i += nt) { cx[i] = 0; cy[i] = 0; }
   if (m <= 0) {
@@ -530,13 +607,28 @@ __global__ void __launch_bounds__(1024) k_spline_fit(SplineArgs A) {
   // fd0/fd1 are free now: forward-sweep scratch
   float* zx = fd0;
   float* zy = fd1;
-  for (int pass = 0; pass <= kRefineSteps; ++pass) {
-    if (tid == 0) tri_solve_f32(m, fa, fb, fil, fp, fq, wx, wy, zx, zy, ex, ey);
+  bool direct = false;
+  float prev = 0.f;
+  for (int pass = 0;; ++pass) {
+    if (tid == 0) tri_solve1_f32(m, fa, fb, fil, fp, fq, wx, zx, ex);
+    if (tid == kWarp) tri_solve1_f32(m, fa, fb, fil, fp, fq, wy, zy, ey);
     __syncthreads();
     // x += e (FP64), then the FP64 residual of the next pass
-    for (int j = tid; j < m; j += nt) { cx[j + 1] += (double)ex[j]; cy[j + 1] += (double)ey[j]; }
-    __syncthreads();
-    if (pass == kRefineSteps) break;
+    float emax = 0.f, xmax = 0.f;
+    for (int j = tid; j < m; j += nt) {
+      const double vx = cx[j + 1] + (double)ex[j], vy = cy[j + 1] + (double)ey[j];
+      cx[j + 1] = vx; cy[j + 1] = vy;
+      emax = fmaxf(emax, fmaxf(fabsf(ex[j]), fabsf(ey[j])));
+      xmax = fmaxf(xmax, (float)fmax(fabs(vx), fabs(vy)));
+    }
+    block_max2_f32(emax, xmax, red);
+    if (!(emax <= xmax)) { direct = true; break; }  // NaN or a diverging FP32 solve
+    if (pass >= 1) {
+      const float rho = emax / fmaxf(prev, 1e-37f);
+      if (rho * emax <= 0x1p-50f * xmax || emax <= 0x1p-52f * xmax) break;
+      if (rho > 0.5f || pass == kMaxRefine) { direct = true; break; }
+    }
+    prev = emax;
     for (int j = tid; j < m; j += nt) {
       // (A x)_j = d2_{j-2} x_{j-2} + d1_{j-1} x_{j-1} + d0_j x_j + d1_j x_{j+1} + d2_j x_{j+2}
       double ax = d0[j] * cx[j + 1], ay = d0[j] * cy[j + 1];
@@ -547,6 +639,11 @@ __global__ void __launch_bounds__(1024) k_spline_fit(SplineArgs A) {
       wx[j] = (float)(rx[j] - ax) * fil[j];
       wy[j] = (float)(ry[j] - ay) * fil[j];
     }
+    __syncthreads();
+  }
+  if (direct) {
+    if (tid == 0)
+      chol_solve_f64(m, d0, d1, d2, rx, ry, A.ws + 12 * n, A.ws + 13 * n, A.ws + 14 * n, cx, cy);
     __syncthreads();
   }
   // fitted values g = y - lam Q gamma
@@ -1358,7 +1455,7 @@ void launch_spline(const DevCtx& d, bool on_S, bool copy_pts, cudaStream_t st) {
   sa.n = d.nchi;
   sa.copy_pts = copy_pts;
   k_spline_rows<<<(d.nchi + 127) / 128, 128, 0, st>>>(sa);
-  k_spline_fit<<<1, 1024, sizeof(float) * 14 * d.nchi, st>>>(sa);
+  k_spline_fit<<<1, 1024, sizeof(float) * kSplineArrays * spline_stride(d.nchi), st>>>(sa);
 }
 
 void launch_columns_bc(const DevCtx& d, bool on_S, bool move, double cY, double cS, int a_mode, bool do_shock,
@@ -1482,7 +1579,8 @@ void flux_kernel_setup() {
   cudaFuncSetAttribute(k_flux<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem<true, false>());
   cudaFuncSetAttribute(k_flux<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem<false, true>());
   cudaFuncSetAttribute(k_flux<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem<true, true>());
-  cudaFuncSetAttribute(k_spline_fit, cudaFuncAttributeMaxDynamicSharedMemorySize, 14 * 4 * 4096);
+  cudaFuncSetAttribute(k_spline_fit, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sizeof(float) * kSplineArrays * spline_stride(4096));
 }
 
 void launch_flow_cells(const DevCtx& d, cudaStream_t st) {

@@ -16,7 +16,7 @@ DevCtx& ctx_dev(hymor_ctx* c);
 cudaStream_t ctx_stream(hymor_ctx* c);
 int ctx_fail(hymor_ctx* c, int code, const char* msg);
 std::vector<void*>& ctx_allocs(hymor_ctx* c);
-void*& ctx_expm_cache(hymor_ctx* c);
+void*& ctx_linear_state(hymor_ctx* c);
 void launch_shock_bc_flags(const DevCtx& d, bool on_S, bool copy_pts, bool do_shock, bool do_bc, int a_mode,
                            cudaStream_t st);
 
@@ -467,11 +467,25 @@ struct ExpmCache {
   long cap = 0;  // doubles
   std::vector<ExpmGraph> graphs;
 };
-ExpmCache& expm_cache(hymor_ctx* ctx) {
-  void*& slot = ctx_expm_cache(ctx);
-  if (!slot) slot = new ExpmCache();
-  return *static_cast<ExpmCache*>(slot);
+struct KrylovScratch {
+  double* partial = nullptr;
+  int cols = 0;
+  double* h = nullptr;  // device coefficients (2 x cols + 2)
+  double* tmp = nullptr;
+  long tmp_n = 0;
+};
+// Per-context state of the linear entry points, owned by the context (created on first
+// use, released by hymor_ctx_destroy).
+struct LinearState {
+  ExpmCache expm;
+  KrylovScratch kry;
+};
+LinearState& linear_state(hymor_ctx* ctx) {
+  void*& slot = ctx_linear_state(ctx);
+  if (!slot) slot = new LinearState();
+  return *static_cast<LinearState*>(slot);
 }
+ExpmCache& expm_cache(hymor_ctx* ctx) { return linear_state(ctx).expm; }
 constexpr int kExpmGraphMinLaunches = 16;
 constexpr size_t kExpmGraphCacheSize = 4;
 
@@ -530,12 +544,12 @@ int expm_via_graph(hymor_ctx* ctx, int k, double dt, int nsteps, int order, cons
 
 namespace hymor {
 // Called by hymor_ctx_destroy after its stream has drained.
-void expm_cache_release(void* p) {
+void linear_state_release(void* p) {
   if (!p) return;
-  ExpmCache* c = static_cast<ExpmCache*>(p);
-  for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
-  if (c->buf) cudaFree(c->buf);
-  delete c;
+  LinearState* s = static_cast<LinearState*>(p);
+  for (auto& g : s->expm.graphs) cudaGraphExecDestroy(g.exec);
+  if (s->expm.buf) cudaFree(s->expm.buf);
+  delete s;  // the Krylov buffers are context allocations, freed with the context
 }
 }  // namespace hymor
 
@@ -657,20 +671,7 @@ int hymor_expm_apply(hymor_ctx* ctx, int k, double dt, int nsteps, int order, co
 }  // extern "C"
 
 namespace {
-struct KrylovScratch {
-  double* partial = nullptr;
-  int cols = 0;
-  double* h = nullptr;  // device coefficients (2 x cols + 2)
-  double* tmp = nullptr;
-  long tmp_n = 0;
-};
-KrylovScratch& kscratch(hymor_ctx* ctx) {
-  static thread_local std::vector<std::pair<hymor_ctx*, KrylovScratch>> table;
-  for (auto& e : table)
-    if (e.first == ctx) return e.second;
-  table.emplace_back(ctx, KrylovScratch{});
-  return table.back().second;
-}
+KrylovScratch& kscratch(hymor_ctx* ctx) { return linear_state(ctx).kry; }
 int ensure_scratch(hymor_ctx* ctx, int cols, long tmp_n) {
   KrylovScratch& k = kscratch(ctx);
   if (cols > k.cols) {

@@ -77,6 +77,12 @@ class Solution:
         self.ctx.check(self.ctx.L.hymor_counters(self.ctx.h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
 
+    def step_kernels(self) -> int:
+        """Kernel launches one ADVECT_FLOW step makes (the kernel nodes of its graph)."""
+        n = ctypes.c_int32()
+        self.ctx.check(self.ctx.L.hymor_step_kernels(self.ctx.h, ctypes.byref(n)))
+        return n.value
+
     def close(self):
         self.ctx.close()
 

@@ -122,6 +122,9 @@ int hymor_update_flow_cells(hymor_ctx* ctx);
 int hymor_cfl_timestep(hymor_ctx* ctx, double* dt);
 /* Counters: MIN_RHO activations and Rankine-Hugoniot y < 1 warnings since creation. */
 int hymor_counters(hymor_ctx* ctx, int32_t* rho_limited, int32_t* rh_warnings);
+/* Number of kernel launches one hymor_step makes (the kernel nodes of its CUDA graph),
+ * for launch accounting. No counterpart in the reference. */
+int hymor_step_kernels(hymor_ctx* ctx, int32_t* n);
 
 /* Device timing on the context stream (CUDA events): start, then stop returns ms. */
 int hymor_timer_start(hymor_ctx* ctx);

@@ -31,6 +31,7 @@
 #include <cstdint>
 #include <cstring>
 #include <limits>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -456,8 +457,21 @@ void update_field_upstream(const orc_config& c, const Mesh& m, State& s) {
   }
 }
 
+// The shock chain reads rows sc-1 .. sc+2 of each column (UPDATE_SHOCK_JUMP_PROPERTIES.jl,
+// EXTRAPOLATE_CELLS_SHOCK.jl), so a shocked row outside 2..Neta-1 is a Julia BoundsError
+// in the reference; the oracle raises it as an exception instead of indexing past its arrays.
+void check_shock_rows(const orc_config& c, const State& s) {
+  for (int i = 0; i < c.nchi; ++i) {
+    const int sc = s.cell_idx[i];
+    if (sc < 2 || sc > c.neta - 1)
+      throw std::out_of_range("shocked row " + std::to_string(sc) + " of column " + std::to_string(i + 1) +
+                              " outside 2.." + std::to_string(c.neta - 1));
+  }
+}
+
 // utils/Shock_fitting/EXTRAPOLATE_CELLS_SHOCK.jl:39-176.
 void extrapolate_cells_shock(const orc_config& c, State& s) {
+  check_shock_rows(c, s);
   const Dims d{c.nchi, c.neta};
   for (int i = 1; i <= c.nchi; ++i) {
     int j = s.cell_idx[i - 1];
@@ -479,6 +493,7 @@ void extrapolate_cells_shock(const orc_config& c, State& s) {
 // utils/Shock_fitting/UPDATE_SHOCK_JUMP_PROPERTIES.jl:324-522
 // (UPDATE_SHOCK_JUMP_PROPERTIES_PRESSURE_3, CPG branch).
 void update_shock_jump_properties(const orc_config& c, const Mesh& m, State& s) {
+  check_shock_rows(c, s);
   const Dims d{c.nchi, c.neta};
   const int n = c.nchi;
   vec p_inf, u_inf, v_inf, rho_inf;
@@ -1399,8 +1414,7 @@ void orc_get_derived(orc_ctx* c, double* p, double* T, double* a, double* beta, 
 
 // NON_LINEAR_DYNAMICS_NO_DISCONTINUITY on the context state, in place (the state
 // is mutated exactly as the reference mutates `s`); flux = 4 x Nchi*Neta.
-void orc_residual(orc_ctx* c, double* flux) {
-  non_linear_dynamics(c->c, c->m, c->s);
+static void copy_flux_out(orc_ctx* c, double* flux) {
   const size_t N = (size_t)c->c.nchi * c->c.neta;
   if (flux) {
     std::memcpy(flux, c->s.flux_rho.data(), N * 8);
@@ -1409,6 +1423,24 @@ void orc_residual(orc_ctx* c, double* flux) {
     std::memcpy(flux + 3 * N, c->s.flux_rho_E.data(), N * 8);
   }
 }
+
+// The entry points that run the shock chain return 0, or -1 with orc_last_error() set
+// when the reference would have raised (a shocked row out of range).
+static thread_local std::string g_orc_error;
+const char* orc_last_error() { return g_orc_error.c_str(); }
+#define ORC_GUARD(body)                     \
+  try {                                     \
+    body;                                   \
+  } catch (const std::exception& e) {       \
+    g_orc_error = e.what();                 \
+    return -1;                              \
+  }                                         \
+  return 0
+
+int orc_residual(orc_ctx* c, double* flux) {
+  ORC_GUARD(non_linear_dynamics(c->c, c->m, c->s); copy_flux_out(c, flux));
+}
+
 
 // Sets the Dict's persistent flux arrays (read by CFL_TIMESTEP's dt2 term).
 void orc_set_flux(orc_ctx* c, const double* flux) {
@@ -1419,17 +1451,15 @@ void orc_set_flux(orc_ctx* c, const double* flux) {
   std::memcpy(c->s.flux_rho_E.data(), flux + 3 * N, N * 8);
 }
 
-void orc_update_flow_cells(orc_ctx* c) { update_flow_cells(c->c, c->m, c->s); }
-void orc_update_shock_bc(orc_ctx* c) {
-  update_thermo(c->c, c->s);
-  update_shock_bc(c->c, c->m, c->s);
+int orc_update_flow_cells(orc_ctx* c) { ORC_GUARD(update_flow_cells(c->c, c->m, c->s)); }
+int orc_update_shock_bc(orc_ctx* c) {
+  ORC_GUARD(update_thermo(c->c, c->s); update_shock_bc(c->c, c->m, c->s));
 }
 double orc_cfl_timestep(orc_ctx* c) { return cfl_timestep(c->c, c->m, c->s); }
 
-// `nsteps` calls of ADVECT_FLOW (explicit RK4). Returns 0.
+// `nsteps` calls of ADVECT_FLOW (explicit RK4).
 int orc_advect(orc_ctx* c, int nsteps) {
-  for (int k = 0; k < nsteps; ++k) advect_flow_explicit(c->c, c->m, c->s);
-  return 0;
+  ORC_GUARD(for (int k = 0; k < nsteps; ++k) advect_flow_explicit(c->c, c->m, c->s));
 }
 
 void orc_counters(orc_ctx* c, int32_t* rho_limited, int32_t* rh_warnings) {
@@ -1457,7 +1487,7 @@ void orc_element_space(const orc_config* cfg, int n, const double* x, const doub
 // LINEARIZE_L.jl:34-69 preparation (flow cells, shock BC, thermo, BCs; no remesh)
 // followed by the coloured finite-difference assembly into stencil blocks
 // (Nchi*Neta*144 doubles).
-void orc_linearize(orc_ctx* c, double* coef) {
+static void linearize_prepared(orc_ctx* c, double* coef) {
   if (c->c.shock_enabled) {
     update_flow_cells(c->c, c->m, c->s);
     update_thermo(c->c, c->s);
@@ -1468,6 +1498,7 @@ void orc_linearize(orc_ctx* c, double* coef) {
   apply_boundary_conditions(c->c, c->m, c->s);
   linearize_equations(c->c, c->m, c->s, coef);
 }
+int orc_linearize(orc_ctx* c, double* coef) { ORC_GUARD(linearize_prepared(c, coef)); }
 
 // Assembly only, on the current state (no preparation).
 void orc_jacobian(orc_ctx* c, double* coef) { linearize_equations(c->c, c->m, c->s, coef); }

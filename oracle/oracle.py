@@ -30,6 +30,7 @@ def lib() -> ctypes.CDLL:
         L.orc_get_state.argtypes = [vp, dp, dp, dp, dp, dp, ip, dp, dp]
         L.orc_get_derived.argtypes = [vp, dp, dp, dp, dp, dp, dp]
         L.orc_residual.argtypes = [vp, dp]
+        L.orc_last_error.restype = ctypes.c_char_p
         L.orc_set_flux.argtypes = [vp, dp]
         L.orc_update_flow_cells.argtypes = [vp]
         L.orc_update_shock_bc.argtypes = [vp]
@@ -47,6 +48,11 @@ def lib() -> ctypes.CDLL:
         L.orc_set_threads.argtypes = [ctypes.c_int]
         _lib = L
     return _lib
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise RuntimeError(lib().orc_last_error().decode())
 
 
 def _ip(a):
@@ -105,7 +111,7 @@ class Oracle:
 
     def residual(self) -> np.ndarray:
         f = np.empty(4 * self.N)
-        lib().orc_residual(self.h, dptr(f))
+        _check(lib().orc_residual(self.h, dptr(f)))
         return f
 
     def set_flux(self, f):
@@ -113,10 +119,10 @@ class Oracle:
         lib().orc_set_flux(self.h, dptr(f))
 
     def advect(self, nsteps: int):
-        lib().orc_advect(self.h, int(nsteps))
+        _check(lib().orc_advect(self.h, int(nsteps)))
 
     def update_flow_cells(self):
-        lib().orc_update_flow_cells(self.h)
+        _check(lib().orc_update_flow_cells(self.h))
 
     def cfl(self) -> float:
         return lib().orc_cfl_timestep(self.h)
@@ -128,7 +134,7 @@ class Oracle:
 
     def linearize(self) -> np.ndarray:
         coef = np.empty(self.N * 144)
-        lib().orc_linearize(self.h, dptr(coef))
+        _check(lib().orc_linearize(self.h, dptr(coef)))
         return coef
 
     def jacobian(self) -> np.ndarray:

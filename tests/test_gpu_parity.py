@@ -5,13 +5,19 @@ import numpy as np
 import pytest
 
 from hymor_gb300 import case as C
+from hymor_gb300 import krylov as K
 from hymor_gb300 import solver as S
+from hymor_gb300._lib import dp
 from oracle import oracle as O
 from tests.helpers import per_var_rel, rel_err, residual_rel, state_rel
 
 pytestmark = pytest.mark.gpu
 
 RES_TOL = 1e-12
+# The shock points come from a smoothing-spline solve; with condition number ~8e5 two
+# backward-stable FP64 solvers agree only to ~cond * 2^-53 ~ 1e-10 in the spline
+# coefficients, which reaches the mutated state at ~1e-12.
+STATE_TOL = {"cylinder_smooth_800": 1e-11}
 
 
 def both(cfg, seed=1, noise=1e-6):
@@ -54,6 +60,10 @@ CASES = {
     "eta_periodic": lambda: C.channel_config(
         20, 18, bc_chi0="no_slip_isothermal", bc_chi1="no_slip_isothermal", bc_eta0="periodic",
         bc_eta1="periodic", Tw_chi0=1.0),
+    # heavier smoothing (p = 1 - 1e-4): the spline system's condition number is ~1.6e3 at
+    # 100 columns (several FP32 refinement steps) and ~8e5 at 800 (the FP64 fallback solve)
+    "cylinder_smooth_100": lambda: C.cylinder_config(100, 40, spline_param=1 - 1e-4),
+    "cylinder_smooth_800": lambda: C.cylinder_config(800, 40, spline_param=1 - 1e-4),
 }
 
 
@@ -66,13 +76,14 @@ def test_residual_parity(require_gpu, name):
     fo = orc.residual()
     errs = residual_rel(fg, fo, cs)
     assert max(errs) < RES_TOL, errs
-    compare_state(sol, orc, 1e-13)
+    compare_state(sol, orc, STATE_TOL.get(name, 1e-13))
 
 
 @pytest.mark.parametrize("name", ["cylinder_100x80", "cylinder_odd_33x17", "channel_periodic",
                                   "blunt_cone_axisym", "cylinder_sutherland", "cylinder_interp3_adiabatic",
                                   "cylinder_disturbed", "wall_symmetry_outflows", "nrcbc_edges",
-                                  "eta_periodic", "inflow_edges"])
+                                  "eta_periodic", "inflow_edges", "cylinder_smooth_100",
+                                  "cylinder_smooth_800"])
 def test_rk4_steps_parity(require_gpu, name):
     """ADVECT_FLOW_EXPLICIT (reference Julia stage aliasing), 10 steps."""
     cfg = CASES[name]()
@@ -167,10 +178,60 @@ def test_expm_parity(require_gpu):
     assert rel_err(Yt, orc.expm(co, dt, 5, X[:, 0], transpose=True)) < 1e-12
 
 
+def test_expm_replayed_graphs(require_gpu):
+    """Repeated propagations replay a cached CUDA graph over fixed buffers: new inputs on
+    the same graph, more (dt, nsteps) combinations than the cache holds, an aliased
+    output, and a larger block that reallocates the buffers all match the oracle."""
+    cfg = C.cylinder_config(30, 20)
+    cs, sol, orc = both(cfg)
+    co = orc.linearize()
+    L = S.LinearOperatorGPU(sol)
+    L.set_blocks(co)
+    rng = np.random.Generator(np.random.PCG64(5))
+    n = 4 * cfg.nchi * cfg.neta
+    for trial, (dt, steps) in enumerate([(1e-4, 10), (1e-4, 10), (2e-4, 10), (1e-4, 12), (3e-4, 4),
+                                         (5e-5, 6), (1e-4, 10)]):
+        x = rng.standard_normal(n)
+        assert rel_err(L.expm(x, dt, steps), orc.expm(co, dt, steps, x)) < 1e-12, trial
+    X = rng.standard_normal((n, 4))
+    Y = L.expm(X, 1e-4, 10)
+    for j in range(4):
+        assert rel_err(Y[:, j], orc.expm(co, 1e-4, 10, X[:, j])) < 1e-12
+    x = rng.standard_normal(n)
+    assert rel_err(L.T.expm(x, 1e-4, 10), orc.expm(co, 1e-4, 10, x, transpose=True)) < 1e-12
+
+
+def test_contexts_recreated_keep_no_stale_scratch(require_gpu):
+    """The Krylov scratch and the propagator graphs belong to their context: contexts
+    created and destroyed in turn (often at the same address) each get their own."""
+    cfg = C.cylinder_config(30, 20)
+    cs = C.initial_state(cfg)
+    orc = O.Oracle(cs)
+    co = orc.linearize()
+    rng = np.random.Generator(np.random.PCG64(6))
+    n = 4 * cfg.nchi * cfg.neta
+    for _ in range(4):
+        sol = S.Solution(cs)
+        L = S.LinearOperatorGPU(sol)
+        L.set_blocks(co)
+        x = rng.standard_normal(n)
+        assert rel_err(L.expm(x, 1e-4, 8), orc.expm(co, 1e-4, 8, x)) < 1e-12
+        V = rng.standard_normal((3, n))  # three columns of length n, back to back
+        dV, dw = K.DeviceBuffer(sol.ctx, 8 * V.size), K.DeviceBuffer(sol.ctx, 8 * n)
+        dV.upload(V.ravel())
+        dw.upload(x)
+        out = np.empty(3)
+        sol.ctx.check(sol.ctx.L.hymor_dot_dev(sol.ctx.h, n, 3, dV.ptr, n, dw.ptr, dp(out)))
+        assert np.allclose(out, V @ x, rtol=1e-13, atol=1e-12)
+        dV.free()
+        dw.free()
+        sol.close()
+
+
 def test_shock_range_error_is_reported(require_gpu):
     """A state whose shocked row sits at the top of the mesh is rejected with
     HYMOR_ERR_SHOCK_RANGE, not written out of bounds."""
-    cfg = C.cylinder_config(24, 16)
+    cfg = C.cylinder_config(30, 20)  # initial shocked rows 19 = Neta - 1, in range
     cs = C.initial_state(cfg)
     bad = cs.cell_idx.copy()
     bad[3] = cfg.neta

@@ -160,3 +160,13 @@ def test_dot_product_identity():
     # and against the scattered CSR matrix
     L = O.stencil_to_csr(cfg, coef)
     assert np.max(np.abs(L @ x - o.matvec(coef, x))) < 1e-10 * np.max(np.abs(L @ x))
+
+
+def test_shock_leaving_the_mesh_raises():
+    """A shocked row outside 2..Neta-1 is a BoundsError in the reference's shock chain;
+    the oracle raises it instead of indexing past its arrays. Heavy smoothing (p = 0.9)
+    straightens the bow shock until its ends leave the 100 x 80 cylinder mesh."""
+    cfg = C.cylinder_config(100, 80, spline_param=0.9)
+    orc = O.Oracle(C.initial_state(cfg))
+    with pytest.raises(RuntimeError, match="outside 2..79"):
+        orc.advect(10)
