@@ -142,10 +142,10 @@ void face_geometry(const hymor_config& c, const hymor_mesh& m, std::vector<doubl
       const double len = std::sqrt(lx * lx + ly * ly);
       lrg[0 * NLR + f] = nx;
       lrg[1 * NLR + f] = ny;
-      lrg[2 * NLR + f] = m.lr_a[f];
+      lrg[2 * NLR + f] = 0.5 * m.lr_a[f];
       lrg[3 * NLR + f] = -1.0 / (cld * Cnn);
-      lrg[4 * NLR + f] = -Cft / (len * Cnn);
-      lrg[5 * NLR + f] = 1.0 / len;
+      lrg[4 * NLR + f] = 0.25 * (-Cft / (len * Cnn));
+      lrg[5 * NLR + f] = 0.25 * (1.0 / len);
       rxl[f] = 1.0 / ((X(i + 1, j + 1) + X(i, j + 1)) / 2);
     }
   for (int j = 0; j <= neta; ++j)
@@ -161,10 +161,10 @@ void face_geometry(const hymor_config& c, const hymor_mesh& m, std::vector<doubl
       const double len = std::sqrt(lx * lx + ly * ly);
       btg[0 * NBT + f] = nx;
       btg[1 * NBT + f] = ny;
-      btg[2 * NBT + f] = m.bt_a[f];
+      btg[2 * NBT + f] = 0.5 * m.bt_a[f];
       btg[3 * NBT + f] = 1.0 / (cbd * Cnn);
-      btg[4 * NBT + f] = Cft / (len * Cnn);
-      btg[5 * NBT + f] = 1.0 / len;
+      btg[4 * NBT + f] = 0.25 * (Cft / (len * Cnn));
+      btg[5 * NBT + f] = 0.25 * (1.0 / len);
       rxb[f] = 1.0 / ((X(i + 1, j + 1) + X(i + 1, j)) / 2);
     }
   for (long k = 0; k < N; ++k) rvol[k] = 1.0 / m.vol[k];

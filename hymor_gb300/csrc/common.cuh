@@ -19,12 +19,14 @@ constexpr int kWarp = 32;
 
 // Face geometry planes (precomputed once per mesh, hymor_ctx_create):
 //   lr face (i, j), between ghosted cells (i, j+1) and (i+1, j+1):
-//     0 nx, 1 ny, 2 A, 3 g1 = -1 / (cld * Cn1_Fn1), 4 g2 = -Cn1_Ft1 / (len * Cn1_Fn1), 5 1/len
+//     0 nx, 1 ny, 2 A/2, 3 g1 = -1 / (cld * Cn1_Fn1), 4 g2/4 = -Cn1_Ft1 / (4 len Cn1_Fn1), 5 1/(4 len)
 //   bt face (i, j), between ghosted cells (i+1, j) and (i+1, j+1):
-//     0 nx, 1 ny, 2 A, 3 h1 = 1 / (cbd * Cn2_Fn2),  4 h2 = Cn2_Ft2 / (len * Cn2_Fn2),  5 1/len
-// so that (VISCOUS_FLUX.jl:98-127)
-//   du_dn1 = g1 * (u_R - u_L) + g2 * (u_c(i, j+1) - u_c(i, j)),  du_dt1 =  (u_c(i,j+1) - u_c(i,j)) / len
-//   du_dn2 = h1 * (u_T - u_B) + h2 * (u_c(i+1, j) - u_c(i, j)),  du_dt2 = -(u_c(i+1,j) - u_c(i,j)) / len
+//     0 nx, 1 ny, 2 A/2, 3 h1 = 1 / (cbd * Cn2_Fn2),  4 h2/4 = Cn2_Ft2 / (4 len Cn2_Fn2),   5 1/(4 len)
+// so that, with U_c = 4 u_c the sum of the four cells around a corner (VISCOUS_FLUX.jl:98-127),
+//   du_dn1 = g1 * (u_R - u_L) + (g2/4) * (U_c(i, j+1) - U_c(i, j)),  du_dt1 =  (U_c(i,j+1) - U_c(i,j)) / (4 len)
+//   du_dn2 = h1 * (u_T - u_B) + (h2/4) * (U_c(i+1, j) - U_c(i, j)),  du_dt2 = -(U_c(i+1,j) - U_c(i,j)) / (4 len)
+// Every factor 1/2 and 1/4 is a power of two, so the folded products round exactly as
+// the unfolded ones.
 constexpr int kGeoPlanes = 6;
 
 struct DevMesh {
