@@ -392,13 +392,14 @@ __global__ void __launch_bounds__(128) k_spline_rows(SplineArgs A) {
 // banded Cholesky factorisation and the two triangular sweeps run in FP32, and
 // mixed-precision iterative refinement (FP64 residual r = b - A x, FP32 correction
 // solve, x += e; Moler, J. ACM 14 (1967) 316-321) brings the solution to FP64
-// accuracy. Each refinement step contracts the error by about cond(A) * 2^-24; with the
-// default smoothing parameter A is diagonally dominant (condition number ~4) and two
-// steps reach the FP64 rounding level. The loop stops once the correction, scaled by
-// the observed contraction, is below 2^-50 of the solution; when it contracts slower
-// than 1/2 (a heavily smoothed fit whose condition number defeats the FP32 factors) or
-// has not converged after kMaxRefine steps, the fit is redone by a serial FP64
-// Cholesky solve.
+// accuracy. Each refinement step contracts the error by about cond(A) * 2^-24 (the
+// observed ratio rho of successive corrections). The loop stops once the remaining
+// error rho * |e| either is below 2^-50 of the solution gamma, or moves the fitted
+// values g = y - lam Q gamma by less than 2^-56 of max|y| (|Q|_inf <= max 2 (1/h_{k-1} +
+// 1/h_k)); with the default smoothing parameter lam |Q| is ~1e-7, so one refinement step
+// suffices. When the corrections contract slower than 1/2 (a heavily smoothed fit
+// whose condition number defeats the FP32 factors) or have not converged after
+// kMaxRefine steps, the fit is redone by a serial FP64 Cholesky solve.
 constexpr int kMaxRefine = 8;
 
 constexpr int kChunk = 8;  // rows loaded into registers ahead of each serial sweep block
@@ -524,33 +525,35 @@ __device__ void chol_solve_f64(int m, const double* __restrict__ d0, const doubl
   }
 }
 
-// Block-wide maxima of two non-negative floats (NaN counts as +inf); every thread gets
-// both. red holds 66 floats.
-__device__ __forceinline__ void block_max2_f32(float& v, float& w, float* red) {
-  if (!(v == v)) v = __int_as_float(0x7f800000);
-  if (!(w == w)) w = __int_as_float(0x7f800000);
+// Block-wide maxima of K non-negative floats (NaN counts as +inf); every thread gets
+// them. red holds 33 K floats.
+template <int K>
+__device__ __forceinline__ void block_max_f32(float (&v)[K], float* red) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-    w = fmaxf(w, __shfl_xor_sync(0xffffffffu, w, o));
+  for (int q = 0; q < K; ++q) {
+    if (!(v[q] == v[q])) v[q] = __int_as_float(0x7f800000);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[q] = fmaxf(v[q], __shfl_xor_sync(0xffffffffu, v[q], o));
   }
   const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
   __syncthreads();
-  if (lane == 0) { red[wp] = v; red[32 + wp] = w; }
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < K; ++q) red[32 * q + wp] = v[q];
   __syncthreads();
   if (wp == 0) {
     const bool in = lane < (int)(blockDim.x >> 5);
-    float a = in ? red[lane] : 0.f, b = in ? red[32 + lane] : 0.f;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, o));
-      b = fmaxf(b, __shfl_xor_sync(0xffffffffu, b, o));
+    for (int q = 0; q < K; ++q) {
+      float a = in ? red[32 * q + lane] : 0.f;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, o));
+      if (lane == 0) red[32 * K + q] = a;
     }
-    if (lane == 0) { red[64] = a; red[65] = b; }
   }
   __syncthreads();
-  v = red[64];
-  w = red[65];
+#pragma unroll
+  for (int q = 0; q < K; ++q) v[q] = red[32 * K + q];
 }
 
 // Padded row stride of the FP32 arrays of k_spline_fit (a multiple of 4 floats, so that
@@ -559,7 +562,7 @@ __host__ __device__ inline int spline_stride(int n) { return (n - 2 + 3) & ~3; }
 constexpr int kSplineArrays = 14;
 
 __global__ void __launch_bounds__(1024) k_spline_fit(SplineArgs A) {
-  __shared__ float red[66];
+  __shared__ float red[33 * 4];
   extern __shared__ float4 shf4[];
   float* shf = reinterpret_cast<float*>(shf4);
   const int n = A.n, m = n - 2, tid = threadIdx.x, nt = blockDim.x;
@@ -597,7 +600,13 @@ __global__ void __launch_bounds__(1024) k_spline_fit(SplineArgs A) {
     for (int i = tid; i < n; i += nt) { gx[i] = yx[i]; gy[i] = yy[i]; }
     return;
   }
-  for (int j = tid; j < m; j += nt) { fd0[j] = (float)d0[j]; fd1[j] = (float)d1[j]; fd2[j] = (float)d2[j]; }
+  const double* ih = A.ws + 15 * n;
+  float qloc = 0.f, yloc = 0.f;  // max 2 (1/h_{k-1} + 1/h_k) and max |y| over this thread's rows
+  for (int j = tid; j < m; j += nt) {
+    fd0[j] = (float)d0[j]; fd1[j] = (float)d1[j]; fd2[j] = (float)d2[j];
+    qloc = fmaxf(qloc, 2.f * ((float)ih[j] + (float)ih[j + 1]));
+  }
+  for (int i = tid; i < n; i += nt) yloc = fmaxf(yloc, fmaxf(fabsf((float)yx[i]), fabsf((float)yy[i])));
   __syncthreads();
   if (tid == 0) chol_f32(m, fd0, fd1, fd2, fil, fl1, fl2);
   __syncthreads();
@@ -620,18 +629,20 @@ __global__ void __launch_bounds__(1024) k_spline_fit(SplineArgs A) {
     if (tid == kWarp) tri_solve1_f32(m, fa, fb, fil, fp, fq, wy, zy, ey);
     __syncthreads();
     // x += e (FP64), then the FP64 residual of the next pass
-    float emax = 0.f, xmax = 0.f;
+    float mx[4] = {0.f, 0.f, qloc, yloc};  // |e|, |gamma|, |Q| bound, |y|
     for (int j = tid; j < m; j += nt) {
       const double vx = cx[j + 1] + (double)ex[j], vy = cy[j + 1] + (double)ey[j];
       cx[j + 1] = vx; cy[j + 1] = vy;
-      emax = fmaxf(emax, fmaxf(fabsf(ex[j]), fabsf(ey[j])));
-      xmax = fmaxf(xmax, (float)fmax(fabs(vx), fabs(vy)));
+      mx[0] = fmaxf(mx[0], fmaxf(fabsf(ex[j]), fabsf(ey[j])));
+      mx[1] = fmaxf(mx[1], fmaxf(fabsf((float)vx), fabsf((float)vy)));
     }
-    block_max2_f32(emax, xmax, red);
+    block_max_f32<4>(mx, red);
+    const float emax = mx[0], xmax = mx[1];
     if (!(emax <= xmax)) { direct = true; break; }  // NaN or a diverging FP32 solve
     if (pass >= 1) {
       const float rho = emax / fmaxf(prev, 1e-37f);
-      if (rho * emax <= 0x1p-50f * xmax || emax <= 0x1p-52f * xmax) break;
+      const float rem = rho * emax;  // error left in gamma
+      if (rem <= 0x1p-50f * xmax || emax <= 0x1p-52f * xmax || (float)lam * mx[2] * rem <= 0x1p-56f * mx[3]) break;
       if (rho > 0.5f || pass == kMaxRefine) { direct = true; break; }
     }
     prev = emax;
@@ -653,7 +664,6 @@ __global__ void __launch_bounds__(1024) k_spline_fit(SplineArgs A) {
     __syncthreads();
   }
   // fitted values g = y - lam Q gamma
-  const double* ih = A.ws + 15 * n;
   for (int i = tid; i < n; i += nt) {
     gx[i] = spline_g(n, ih, yx, cx, lam, i);
     gy[i] = spline_g(n, ih, yy, cy, lam, i);
@@ -883,7 +893,7 @@ struct FluxArgs {
 };
 
 template <bool AXI, bool SUTH>
-__global__ void __launch_bounds__(kFluxThreads, 2) k_flux(FluxArgs a) {
+__global__ void __launch_bounds__(kFluxThreads, 3) k_flux(FluxArgs a) {
   extern __shared__ double sm[];
   double* s_r = sm;
   double* s_u = s_r + NH;   // u = rho_u / rho
