@@ -882,9 +882,9 @@ struct FluxArgs {
   DevMesh m;
   double mre, kq;          // mu/Re and k gamma/(Re Pr) for constant transport
   double inv_Re, gk;       // 1/Re and gamma/(Re Pr) for Sutherland faces
-  // the same scaled by powers of two (exact): the face kernel forms twice the viscous
-  // traction and heat flux so that both halves of the flux multiply the stored A/2
-  double mre2, mre4, kq2, inv_Re2, inv_Re4, gk2;
+  // the same doubled (exact): the face kernel forms twice the viscous traction and heat
+  // flux so that both halves of the flux multiply the stored A/2
+  double mre2, kq2, inv_Re2, gk2;
   double suthS, Tinf_inv;
   int nchi, neta;
   int mask;                // shock fitting with feedback: zero flux at j >= sc
@@ -998,18 +998,21 @@ __global__ void __launch_bounds__(kFluxThreads, 3) k_flux(FluxArgs a) {
       const double dv_dn = fma(g1, s_v[R] - s_v[L], g2 * dVc);
       const double dT_dn = fma(g1, s_T[R] - s_T[L], g2 * dTc);
       const double du_dt = dUc * il, dv_dt = dVc * il;
-      const double dun_dn = fma(-du_dn, nx, -dv_dn * ny);
-      const double dut_dn = fma(du_dn, ny, -dv_dn * nx);
-      const double dun_dt = fma(-du_dt, nx, -dv_dt * ny);
-      const double dut_dt = fma(du_dt, ny, -dv_dt * nx);
-      double div = dut_dt + dun_dn;
-      double mre = a.mre, mre2 = a.mre2, mre4 = a.mre4, kq2 = a.kq2;
+      // With D = (du_dn, dv_dn), E = (du_dt, dv_dt), n and t = (ny, -nx) the face frame of
+      // VISCOUS_FLUX.jl:98-133 has dun_dn = -D.n, dut_dn = D.t, dun_dt = -E.n, dut_dt = E.t,
+      // and the traction t = -tau11 n + tau12 t with tau11 = mu (2 dun_dn - 2/3 div),
+      // tau12 = mu (dun_dt + dut_dn) is, expanding D in the (n, t) basis,
+      //   t = mu (D + (D.n + 2/3 div) n - (E.n) t),   div = E.t - D.n (+ u/x axisymmetric)
+      const double Dn = fma(du_dn, nx, dv_dn * ny);
+      const double En = fma(du_dt, nx, dv_dt * ny);
+      const double Et = fma(du_dt, ny, -dv_dt * nx);
+      double div = Et - Dn;
+      double mre = a.mre, mre2 = a.mre2, kq2 = a.kq2;
       if (SUTH) {  // Sutherland at the face temperature
         const double Ts = (s_T[L] + s_T[R]) * 0.5 * a.Tinf_inv;
         const double mu_f = Ts * sqrt(Ts) * (1 + a.suthS) * frcp(Ts + a.suthS);
         if (AXI) mre = mu_f * a.inv_Re;
         mre2 = mu_f * a.inv_Re2;
-        mre4 = mu_f * a.inv_Re4;
         kq2 = mu_f * a.gk2;
       }
       double uf = 0, rx = 0;
@@ -1018,19 +1021,17 @@ __global__ void __launch_bounds__(kFluxThreads, 3) k_flux(FluxArgs a) {
         uf = (s_u[R] + s_u[L]) * 0.5;
         div = fma(uf, rx, div);
       }
-      // twice tau11 = mu (2 dun_dn - 2/3 div) and tau12, hence twice the traction (t2x, t2y),
-      // the work and the heat flux: (2 t) (A/2) = t A exactly
-      const double tau11 = mre4 * fma(-1.0 / 3.0, div, dun_dn);
-      const double tau12 = mre2 * (dun_dt + dut_dn);
-      const double tx = fma(tau12, ny, -tau11 * nx);
-      const double ty = -fma(tau11, ny, tau12 * nx);
-      const double w = fma(Su * ir, tx, (Sv * ir) * ty);
+      // twice the traction, the work and the heat flux: (2 t) (A/2) = t A
+      const double al = fma(2.0 / 3.0, div, Dn);
+      const double tx = mre2 * fma(al, nx, fma(-En, ny, du_dn));
+      const double ty = mre2 * fma(al, ny, fma(En, nx, dv_dn));
+      const double w = fma(Su, tx, Sv * ty) * ir;
       const double qn = kq2 * dT_dn;
       const int o = fx + fy * (TX + 1);
       f_lr[o] = m2 * Ah;
-      f_lr[NLRF + o] = fma(fma(Su, Vn, Sp * nx), Ah, tx * Ah);
-      f_lr[2 * NLRF + o] = fma(fma(Sv, Vn, Sp * ny), Ah, ty * Ah);
-      f_lr[3 * NLRF + o] = fma((SE + Sp) * Vn, Ah, (w + qn) * Ah);
+      f_lr[NLRF + o] = fma(Su, Vn, fma(Sp, nx, tx)) * Ah;
+      f_lr[2 * NLRF + o] = fma(Sv, Vn, fma(Sp, ny, ty)) * Ah;
+      f_lr[3 * NLRF + o] = fma(SE + Sp, Vn, w + qn) * Ah;
       if (AXI) t_lr[o] = mre * fma(-2.0 / 3.0, div, 2 * uf * rx);
     }
   }
@@ -1055,18 +1056,18 @@ __global__ void __launch_bounds__(kFluxThreads, 3) k_flux(FluxArgs a) {
       const double dv_dn = fma(h1, s_v[Tt] - s_v[B], h2 * dVc);
       const double dT_dn = fma(h1, s_T[Tt] - s_T[B], h2 * dTc);
       const double du_dt = -dUc * il, dv_dt = -dVc * il;
-      const double dut_dt = fma(du_dt, ny, -dv_dt * nx);
-      const double dun_dt = fma(du_dt, nx, dv_dt * ny);
-      const double dut_dn = fma(du_dn, ny, -dv_dn * nx);
-      const double dun_dn = fma(du_dn, nx, dv_dn * ny);
-      double div = dut_dt + dun_dn;
-      double mre = a.mre, mre2 = a.mre2, mre4 = a.mre4, kq2 = a.kq2;
+      // bt frame: dun_dn = D.n, dut_dn = D.t, dun_dt = E.n, dut_dt = E.t, traction
+      // tau22 n + tau21 t = mu (D + (D.n - 2/3 div) n + (E.n) t), div = E.t + D.n
+      const double Dn = fma(du_dn, nx, dv_dn * ny);
+      const double En = fma(du_dt, nx, dv_dt * ny);
+      const double Et = fma(du_dt, ny, -dv_dt * nx);
+      double div = Et + Dn;
+      double mre = a.mre, mre2 = a.mre2, kq2 = a.kq2;
       if (SUTH) {
         const double Ts = (s_T[B] + s_T[Tt]) * 0.5 * a.Tinf_inv;
         const double mu_f = Ts * sqrt(Ts) * (1 + a.suthS) * frcp(Ts + a.suthS);
         if (AXI) mre = mu_f * a.inv_Re;
         mre2 = mu_f * a.inv_Re2;
-        mre4 = mu_f * a.inv_Re4;
         kq2 = mu_f * a.gk2;
       }
       double uf = 0, rx = 0;
@@ -1075,17 +1076,16 @@ __global__ void __launch_bounds__(kFluxThreads, 3) k_flux(FluxArgs a) {
         uf = (s_u[Tt] + s_u[B]) * 0.5;
         div = fma(uf, rx, div);
       }
-      const double tau22 = mre4 * fma(-1.0 / 3.0, div, dun_dn);  // twice tau22 and tau21
-      const double tau21 = mre2 * (dut_dn + dun_dt);
-      const double tx = fma(tau22, nx, tau21 * ny);
-      const double ty = fma(tau22, ny, -tau21 * nx);
-      const double w = fma(Su * ir, tx, (Sv * ir) * ty);
+      const double al = fma(-2.0 / 3.0, div, Dn);
+      const double tx = mre2 * fma(al, nx, fma(En, ny, du_dn));
+      const double ty = mre2 * fma(al, ny, fma(-En, nx, dv_dn));
+      const double w = fma(Su, tx, Sv * ty) * ir;
       const double qn = kq2 * dT_dn;
       const int o = fx + fy * TX;
       f_bt[o] = m2 * Ah;
-      f_bt[NBTF + o] = fma(fma(Su, Vn, Sp * nx), Ah, -tx * Ah);
-      f_bt[2 * NBTF + o] = fma(fma(Sv, Vn, Sp * ny), Ah, -ty * Ah);
-      f_bt[3 * NBTF + o] = fma((SE + Sp) * Vn, Ah, -(w + qn) * Ah);
+      f_bt[NBTF + o] = fma(Su, Vn, fma(Sp, nx, -tx)) * Ah;
+      f_bt[2 * NBTF + o] = fma(Sv, Vn, fma(Sp, ny, -ty)) * Ah;
+      f_bt[3 * NBTF + o] = fma(SE + Sp, Vn, -(w + qn)) * Ah;
       if (AXI) t_bt[o] = mre * fma(-2.0 / 3.0, div, 2 * uf * rx);
     }
   }
@@ -1606,10 +1606,8 @@ void launch_flux_class(const DevCtx& d, bool on_S, double* const out[4], int til
   a.inv_Re = 1.0 / c.Re;
   a.gk = c.gamma / c.Re / c.Pr;
   a.mre2 = 2 * a.mre;
-  a.mre4 = 4 * a.mre;
   a.kq2 = 2 * a.kq;
   a.inv_Re2 = 2 * a.inv_Re;
-  a.inv_Re4 = 4 * a.inv_Re;
   a.gk2 = 2 * a.gk;
   a.suthS = c.sutherland_S;
   a.Tinf_inv = c.energy_factor / c.cv;
