@@ -414,89 +414,130 @@ __device__ __forceinline__ void st8(float* __restrict__ p, const float (&r)[kChu
   reinterpret_cast<float4*>(p)[1] = make_float4(r[4], r[5], r[6], r[7]);
 }
 
-// Forward and backward FP32 sweeps of L L^T x = r for one right-hand side (the two
-// ordinates run on two warps, so that each serial chain issues half the instructions):
-//   forward:  s_j = c_j - a_j s_{j-1} - b_j s_{j-2}, z_j = s_j / l0_j, with c_j = r_j / l0_j
+// Forward and backward FP32 sweeps of L L^T x = r for one right-hand side, by one warp:
+//   forward:  v_j = c_j - a_j v_{j-1} - b_j v_{j-2}, z_j = v_j / l0_j (c_j = r_j / l0_j)
 //   backward: x_j = z_j - p_j x_{j+1} - q_j x_{j+2}
-// Blocks of kChunk rows are loaded with 16-byte accesses (row offsets of the blocks are
-// multiples of 8, the arrays 16-byte aligned) before the dependent FMA chain, which has
-// one FMA per row on its critical path.
-__device__ __forceinline__ void tri_solve1_f32(int m, const float* __restrict__ fa, const float* __restrict__ fb,
-                                               const float* __restrict__ fil, const float* __restrict__ fp,
-                                               const float* __restrict__ fq, const float* __restrict__ c,
-                                               float* __restrict__ z, float* __restrict__ o) {
-  float s1 = 0.f, s2 = 0.f;
-  int j = 0;
-  for (; j + kChunk <= m; j += kChunk) {
-    float ra[kChunk], rb[kChunk], rc[kChunk], ri[kChunk], rz[kChunk];
-    ld8(ra, fa + j); ld8(rb, fb + j); ld8(rc, c + j); ld8(ri, fil + j);
+// Each is a second-order linear recurrence, i.e. the state S_j = (v_j, v_{j-1}) follows
+// the affine map S_j = T_j(S_{j-1}) = (c_j - a_j S_0 - b_j S_1, S_0). Each lane composes
+// the maps of its L consecutive rows (L odd, so that the lanes' shared-memory rows fall
+// in distinct banks), a Kogge-Stone scan over the 32 lanes composes the segment maps
+// (Blelloch, "Prefix sums and their applications", 1990), and each lane then runs its
+// rows from the state the scan hands it: ~3 L + 10 dependent operations instead of m.
+struct Affine2 {  // S -> M S + g
+  float m00, m01, m10, m11, g0, g1;
+};
+__device__ __forceinline__ void affine_push(Affine2& A, float a, float b, float c) {  // A <- T ∘ A
+  const float n00 = fmaf(-a, A.m00, -b * A.m10), n01 = fmaf(-a, A.m01, -b * A.m11);
+  const float ng0 = fmaf(-a, A.g0, fmaf(-b, A.g1, c));
+  A.m10 = A.m00; A.m11 = A.m01; A.g1 = A.g0;
+  A.m00 = n00; A.m01 = n01; A.g0 = ng0;
+}
+// inclusive scan over the lanes: lane k ends with the composition of the maps of lanes
+// 0..k; returns the state entering lane k's segment (lane 0: S = 0)
+__device__ __forceinline__ void affine_scan(Affine2& A, int lane, float& s1, float& s2) {
 #pragma unroll
-    for (int u = 0; u < kChunk; ++u) {
-      const float v = fmaf(-ra[u], s1, fmaf(-rb[u], s2, rc[u]));
-      rz[u] = v * ri[u];
+  for (int d = 1; d < 32; d <<= 1) {
+    const float p00 = __shfl_up_sync(0xffffffffu, A.m00, d), p01 = __shfl_up_sync(0xffffffffu, A.m01, d);
+    const float p10 = __shfl_up_sync(0xffffffffu, A.m10, d), p11 = __shfl_up_sync(0xffffffffu, A.m11, d);
+    const float q0 = __shfl_up_sync(0xffffffffu, A.g0, d), q1 = __shfl_up_sync(0xffffffffu, A.g1, d);
+    if (lane >= d) {  // A <- A ∘ P
+      const float r00 = fmaf(A.m00, p00, A.m01 * p10), r01 = fmaf(A.m00, p01, A.m01 * p11);
+      const float r10 = fmaf(A.m10, p00, A.m11 * p10), r11 = fmaf(A.m10, p01, A.m11 * p11);
+      const float h0 = fmaf(A.m00, q0, fmaf(A.m01, q1, A.g0)), h1 = fmaf(A.m10, q0, fmaf(A.m11, q1, A.g1));
+      A.m00 = r00; A.m01 = r01; A.m10 = r10; A.m11 = r11; A.g0 = h0; A.g1 = h1;
+    }
+  }
+  s1 = __shfl_up_sync(0xffffffffu, A.g0, 1);
+  s2 = __shfl_up_sync(0xffffffffu, A.g1, 1);
+  if (lane == 0) { s1 = 0.f; s2 = 0.f; }
+}
+__device__ __forceinline__ void tri_solve_warp_f32(int m, const float* __restrict__ fa, const float* __restrict__ fb,
+                                                   const float* __restrict__ fil, const float* __restrict__ fp,
+                                                   const float* __restrict__ fq, const float* __restrict__ c,
+                                                   float* __restrict__ z, float* __restrict__ o) {
+  const int lane = threadIdx.x & 31;
+  const int L = ((m + 31) >> 5) | 1;
+  {  // forward, lane k on rows [k L, (k + 1) L)
+    const int lo = min(m, lane * L), hi = min(m, lo + L);
+    Affine2 A{1.f, 0.f, 0.f, 1.f, 0.f, 0.f};
+    for (int j = lo; j < hi; ++j) affine_push(A, fa[j], fb[j], c[j]);
+    float s1, s2;
+    affine_scan(A, lane, s1, s2);
+    for (int j = lo; j < hi; ++j) {
+      const float v = fmaf(-fa[j], s1, fmaf(-fb[j], s2, c[j]));
+      z[j] = v * fil[j];
       s2 = s1; s1 = v;
     }
-    st8(z + j, rz);
   }
-  for (; j < m; ++j) {
-    const float v = fmaf(-fa[j], s1, fmaf(-fb[j], s2, c[j]));
-    z[j] = v * fil[j];
-    s2 = s1; s1 = v;
-  }
-  float x1 = 0.f, x2 = 0.f;
-  const int top = m & ~(kChunk - 1);
-  for (j = m - 1; j >= top; --j) {
-    const float v = fmaf(-fp[j], x1, fmaf(-fq[j], x2, z[j]));
-    o[j] = v;
-    x2 = x1; x1 = v;
-  }
-  for (int j0 = top - kChunk; j0 >= 0; j0 -= kChunk) {
-    float rp[kChunk], rq[kChunk], rz[kChunk], ro[kChunk];
-    ld8(rp, fp + j0); ld8(rq, fq + j0); ld8(rz, z + j0);
-#pragma unroll
-    for (int u = kChunk - 1; u >= 0; --u) {
-      const float v = fmaf(-rp[u], x1, fmaf(-rq[u], x2, rz[u]));
-      ro[u] = v;
-      x2 = x1; x1 = v;
+  __syncwarp();
+  {  // backward, lane k on rows m - 1 - k L down to m - (k + 1) L
+    const int top = m - 1 - lane * L, bot = max(-1, top - L);
+    Affine2 A{1.f, 0.f, 0.f, 1.f, 0.f, 0.f};
+    for (int j = top; j > bot; --j) affine_push(A, fp[j], fq[j], z[j]);
+    float s1, s2;
+    affine_scan(A, lane, s1, s2);
+    for (int j = top; j > bot; --j) {
+      const float v = fmaf(-fp[j], s1, fmaf(-fq[j], s2, z[j]));
+      o[j] = v;
+      s2 = s1; s1 = v;
     }
-    st8(o + j0, ro);
   }
 }
 
-// FP32 banded Cholesky: il_j = 1 / l0_j, l1_j, l2_j of A ~ L L^T (one thread).
-__device__ __forceinline__ void chol_f32(int m, const float* __restrict__ fd0, const float* __restrict__ fd1,
-                                         const float* __restrict__ fd2, float* __restrict__ fil,
-                                         float* __restrict__ fl1, float* __restrict__ fl2) {
-  float l1p = 0.f, l2p = 0.f, l2pp = 0.f;
+__device__ __forceinline__ float rcp_approx_f32(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// Pivots of the FP32 banded factorisation A ~ L L^T (one thread). With l0_j^2 = a_j,
+// l1_j = t_j / l0_j, l2_j = d2_j / l0_j:
+//   a_j = d0_j - t_{j-1}^2 / a_{j-1} - d2_{j-2}^2 / a_{j-2},   t_j = d1_j - d2_{j-1} t_{j-1} / a_{j-1}
+// so that the serial chain of a row is one reciprocal and one FMA (the square roots are
+// taken afterwards, in parallel). The recurrence forgets its start geometrically when A is
+// diagonally dominant, so pivot_window first gets each row's pivot in parallel from the
+// kPivWindow rows before it, started at a ~ d0, t ~ d1; the serial form runs only when the
+// windowed pivots do not satisfy the recurrence to 2^-20.
+constexpr int kPivWindow = 32;
+
+__device__ __forceinline__ void pivot_window(int j, const float* __restrict__ fd0, const float* __restrict__ fd1,
+                                             const float* __restrict__ fd2, float& a, float& t) {
+  const int s = j > kPivWindow ? j - kPivWindow : 0;
+  float q1 = 0.f, q2 = 0.f, t1 = 0.f, e1 = 0.f, e2 = 0.f;
+  if (s >= 1) { q1 = rcp_approx_f32(fd0[s - 1]); t1 = fd1[s - 1]; e1 = fd2[s - 1]; }
+  if (s >= 2) { q2 = rcp_approx_f32(fd0[s - 2]); e2 = fd2[s - 2]; }
+  a = 0.f; t = 0.f;
+  for (int r = s; r <= j; ++r) {
+    a = fmaf(-t1 * t1, q1, fmaf(-e2 * e2, q2, fd0[r]));
+    t = fmaf(-e1 * t1, q1, fd1[r]);
+    q2 = q1; q1 = rcp_approx_f32(a); t1 = t; e2 = e1; e1 = fd2[r];
+  }
+}
+__device__ __forceinline__ void chol_pivots_f32(int m, const float* __restrict__ fd0, const float* __restrict__ fd1,
+                                                const float* __restrict__ fd2, float* __restrict__ pa,
+                                                float* __restrict__ pt) {
+  float q1 = 0.f, q2 = 0.f, t1 = 0.f, e1 = 0.f, e2 = 0.f;  // 1/a, t and d2 of rows j-1, j-2
+  auto row = [&](float d0, float d1, float d2, float& a, float& t) {
+    a = fmaf(-t1 * t1, q1, fmaf(-e2 * e2, q2, d0));
+    t = fmaf(-e1 * t1, q1, d1);
+    q2 = q1; q1 = rcp_approx_f32(a);
+    t1 = t; e2 = e1; e1 = d2;
+  };
   int j = 0;
   for (; j + kChunk <= m; j += kChunk) {
-    float r0[kChunk], r1[kChunk], r2[kChunk], o0[kChunk], o1[kChunk], o2[kChunk];
+    float r0[kChunk], r1[kChunk], r2[kChunk], oa[kChunk], ot[kChunk];
     ld8(r0, fd0 + j); ld8(r1, fd1 + j); ld8(r2, fd2 + j);
 #pragma unroll
-    for (int u = 0; u < kChunk; ++u) {
-      const float a = fmaf(-l1p, l1p, fmaf(-l2pp, l2pp, r0[u]));
-      const float il = rsqrtf(a);
-      const float nl1 = fmaf(-l2p, l1p, r1[u]) * il;
-      const float nl2 = r2[u] * il;
-      o0[u] = il; o1[u] = nl1; o2[u] = nl2;
-      l2pp = l2p; l2p = nl2; l1p = nl1;
-    }
-    st8(fil + j, o0); st8(fl1 + j, o1); st8(fl2 + j, o2);
+    for (int u = 0; u < kChunk; ++u) row(r0[u], r1[u], r2[u], oa[u], ot[u]);
+    st8(pa + j, oa); st8(pt + j, ot);
   }
-  for (; j < m; ++j) {
-    const float a = fmaf(-l1p, l1p, fmaf(-l2pp, l2pp, fd0[j]));
-    const float il = rsqrtf(a);
-    const float nl1 = fmaf(-l2p, l1p, fd1[j]) * il;
-    const float nl2 = fd2[j] * il;
-    fil[j] = il; fl1[j] = nl1; fl2[j] = nl2;
-    l2pp = l2p; l2p = nl2; l1p = nl1;
-  }
+  for (; j < m; ++j) row(fd0[j], fd1[j], fd2[j], pa[j], pt[j]);
 }
 
 // Serial FP64 banded Cholesky solve of A x = r for both ordinates (one thread); the
 // factors go to the workspace slots l0inv, l1, l2 and x overwrites the 1-offset
 // solution arrays gx_, gy_ (gx_[j + 1] = x_j).
-__device__ void chol_solve_f64(int m, const double* __restrict__ d0, const double* __restrict__ d1,
+__device__ __noinline__ void chol_solve_f64(int m, const double* __restrict__ d0, const double* __restrict__ d1,
                                const double* __restrict__ d2, const double* __restrict__ rx,
                                const double* __restrict__ ry, double* __restrict__ il0, double* __restrict__ l1,
                                double* __restrict__ l2, double* __restrict__ gx_, double* __restrict__ gy_) {
@@ -560,8 +601,11 @@ __device__ __forceinline__ void block_max_f32(float (&v)[K], float* red) {
 // every array starts on a 16-byte boundary).
 __host__ __device__ inline int spline_stride(int n) { return (n - 2 + 3) & ~3; }
 constexpr int kSplineArrays = 14;
+// 16 warps: enough to keep the FP64 pipes of the SM busy in the parallel phases, and
+// 128 registers per thread for the prefetched serial sweeps
+constexpr int kSplineThreads = 1024;
 
-__global__ void __launch_bounds__(1024) k_spline_fit(SplineArgs A) {
+__global__ void __launch_bounds__(kSplineThreads) k_spline_fit(SplineArgs A) {
   __shared__ float red[33 * 4];
   extern __shared__ float4 shf4[];
   float* shf = reinterpret_cast<float*>(shf4);
@@ -608,15 +652,31 @@ __global__ void __launch_bounds__(1024) k_spline_fit(SplineArgs A) {
   }
   for (int i = tid; i < n; i += nt) yloc = fmaxf(yloc, fmaxf(fabsf((float)yx[i]), fabsf((float)yy[i])));
   __syncthreads();
-  if (tid == 0) chol_f32(m, fd0, fd1, fd2, fil, fl1, fl2);
+  float* pa = fl1;  // pivots a_j = l0_j^2
+  float* pt = fl2;  // t_j = l0_j l1_j
+  for (int j = tid; j < m; j += nt) pivot_window(j, fd0, fd1, fd2, pa[j], pt[j]);
   __syncthreads();
+  int off = 0;
   for (int j = tid; j < m; j += nt) {
-    fa[j] = j >= 1 ? fl1[j - 1] * fil[j] : 0.f;
-    fb[j] = j >= 2 ? fl2[j - 2] * fil[j] : 0.f;
-    fp[j] = fl1[j] * fil[j];
-    fq[j] = fl2[j] * fil[j];
-    wx[j] = (float)rx[j] * fil[j];
-    wy[j] = (float)ry[j] * fil[j];
+    float ar = fd0[j], tr = fd1[j];
+    if (j >= 1) { const float q = rcp_approx_f32(pa[j - 1]); ar = fmaf(-pt[j - 1] * pt[j - 1], q, ar); tr = fmaf(-fd2[j - 1] * pt[j - 1], q, tr); }
+    if (j >= 2) ar = fmaf(-fd2[j - 2] * fd2[j - 2], rcp_approx_f32(pa[j - 2]), ar);
+    if (!(fabsf(pa[j] - ar) <= 0x1p-20f * fabsf(pa[j]) && fabsf(pt[j] - tr) <= 0x1p-20f * (fabsf(tr) + fabsf(fd1[j]))))
+      off = 1;
+  }
+  if (__syncthreads_or(off)) {
+    if (tid == 0) chol_pivots_f32(m, fd0, fd1, fd2, pa, pt);
+    __syncthreads();
+  }
+  for (int j = tid; j < m; j += nt) {
+    const float il = rsqrtf(pa[j]);
+    fil[j] = il;
+    fa[j] = j >= 1 ? pt[j - 1] * rsqrtf(pa[j - 1]) * il : 0.f;   // l1_{j-1} / l0_j
+    fb[j] = j >= 2 ? fd2[j - 2] * rsqrtf(pa[j - 2]) * il : 0.f;  // l2_{j-2} / l0_j
+    fp[j] = pt[j] * il * il;                                     // l1_j / l0_j
+    fq[j] = fd2[j] * il * il;                                    // l2_j / l0_j
+    wx[j] = (float)rx[j] * il;
+    wy[j] = (float)ry[j] * il;
   }
   __syncthreads();
   // fd0/fd1 are free now: forward-sweep scratch
@@ -625,8 +685,8 @@ __global__ void __launch_bounds__(1024) k_spline_fit(SplineArgs A) {
   bool direct = false;
   float prev = 0.f;
   for (int pass = 0;; ++pass) {
-    if (tid == 0) tri_solve1_f32(m, fa, fb, fil, fp, fq, wx, zx, ex);
-    if (tid == kWarp) tri_solve1_f32(m, fa, fb, fil, fp, fq, wy, zy, ey);
+    if (tid < kWarp) tri_solve_warp_f32(m, fa, fb, fil, fp, fq, wx, zx, ex);
+    else if (tid < 2 * kWarp) tri_solve_warp_f32(m, fa, fb, fil, fp, fq, wy, zy, ey);
     __syncthreads();
     // x += e (FP64), then the FP64 residual of the next pass
     float mx[4] = {0.f, 0.f, qloc, yloc};  // |e|, |gamma|, |Q| bound, |y|
@@ -1498,7 +1558,7 @@ void launch_spline(const DevCtx& d, bool on_S, bool copy_pts, cudaStream_t st) {
   sa.n = d.nchi;
   sa.copy_pts = copy_pts;
   k_spline_rows<<<(d.nchi + 127) / 128, 128, 0, st>>>(sa);
-  k_spline_fit<<<1, 1024, sizeof(float) * kSplineArrays * spline_stride(d.nchi), st>>>(sa);
+  k_spline_fit<<<1, kSplineThreads, sizeof(float) * kSplineArrays * spline_stride(d.nchi), st>>>(sa);
 }
 
 void launch_columns_bc(const DevCtx& d, bool on_S, bool move, double cY, double cS, int a_mode, bool do_shock,
