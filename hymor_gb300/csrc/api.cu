@@ -45,6 +45,12 @@ struct hymor_ctx_s {
   uint64_t flush_bytes = 0;
   // state of the linear entry points: replayed propagator graphs, Krylov scratch (linear.cu)
   void* linear_state = nullptr;
+  // pinned host staging of the small state arrays (shock points, cell indices, scalars),
+  // so that set_state / get_state move them by DMA instead of pageable staged copies
+  unsigned char* stage = nullptr;
+  // the persistent sound speed has not been computed for the state set last (set_state
+  // without it); the next call that reads it computes it first
+  bool a_stale = false;
 };
 
 namespace {
@@ -315,6 +321,17 @@ int set_device(hymor_ctx* ctx) {
   return 0;
 }
 
+// staging layout: pts x, y, chi, eta (n doubles each), scalars (kCount doubles), cell_idx (n int32)
+size_t stage_bytes(int n) { return (4 * (size_t)n + kCount) * sizeof(double) + (size_t)n * sizeof(int32_t); }
+
+// Computes the persistent sound speed of S if set_state left it stale, unless the work
+// about to be enqueued recomputes it before reading it.
+void refresh_sound(hymor_ctx* ctx, bool recomputed_anyway) {
+  if (!ctx->a_stale) return;
+  if (!recomputed_anyway) launch_sound_cmax(ctx->d, true, ctx->stream);
+  ctx->a_stale = false;
+}
+
 }  // namespace
 
 extern "C" {
@@ -429,6 +446,8 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
         cudaEventCreateWithFlags(&ctx->fit_join, cudaEventDisableTiming) != cudaSuccess)
       return bail(fail(ctx, HYMOR_ERR_CUDA, "event"));
   }
+  if (cudaMallocHost(&ctx->stage, stage_bytes(d.nchi)) != cudaSuccess)
+    return bail(fail(ctx, HYMOR_ERR_CUDA, "pinned staging allocation failed"));
   cudaEventCreate(&ctx->t0);
   cudaEventCreate(&ctx->t1);
   cudaError_t e = cudaDeviceSynchronize();
@@ -459,6 +478,7 @@ int hymor_ctx_destroy(hymor_ctx* ctx) {
   if (ctx->t1) cudaEventDestroy(ctx->t1);
   for (void* p : ctx->allocs) cudaFree(p);
   if (ctx->flush_buf) cudaFree(ctx->flush_buf);
+  if (ctx->stage) cudaFreeHost(ctx->stage);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return 0;
@@ -486,23 +506,28 @@ int hymor_set_state(hymor_ctx* ctx, const double* q, const double* pts_x, const 
     }
   }
   cudaStream_t st = ctx->stream;
+  CU(cudaStreamSynchronize(st));  // the staging buffer may still feed an earlier copy
   CU(cudaMemcpyAsync(d.S.rho, q, G * 8, cudaMemcpyHostToDevice, st));
   CU(cudaMemcpyAsync(d.S.ru, q + G, G * 8, cudaMemcpyHostToDevice, st));
   CU(cudaMemcpyAsync(d.S.rv, q + 2 * G, G * 8, cudaMemcpyHostToDevice, st));
   CU(cudaMemcpyAsync(d.S.rE, q + 3 * G, G * 8, cudaMemcpyHostToDevice, st));
-  if (pts_x) CU(cudaMemcpyAsync(d.Sp.x, pts_x, n * 8, cudaMemcpyHostToDevice, st));
-  if (pts_y) CU(cudaMemcpyAsync(d.Sp.y, pts_y, n * 8, cudaMemcpyHostToDevice, st));
-  if (pts_chi) CU(cudaMemcpyAsync(d.Sp.chi, pts_chi, n * 8, cudaMemcpyHostToDevice, st));
-  if (pts_eta) CU(cudaMemcpyAsync(d.Sp.eta, pts_eta, n * 8, cudaMemcpyHostToDevice, st));
-  CU(cudaMemcpyAsync(d.cell_idx, ci.data(), n * 4, cudaMemcpyHostToDevice, st));
-  double sc[kCount] = {0};
+  double* sp = reinterpret_cast<double*>(ctx->stage);
+  double* sc = sp + 4 * n;
+  int32_t* sci = reinterpret_cast<int32_t*>(sc + kCount);
+  const double* src[4] = {pts_x, pts_y, pts_chi, pts_eta};
+  double* dst[4] = {d.Sp.x, d.Sp.y, d.Sp.chi, d.Sp.eta};
+  for (int k = 0; k < 4; ++k)
+    if (src[k]) {
+      std::memcpy(sp + k * n, src[k], n * 8);
+      CU(cudaMemcpyAsync(dst[k], sp + k * n, n * 8, cudaMemcpyHostToDevice, st));
+    }
+  std::memcpy(sci, ci.data(), n * 4);
+  CU(cudaMemcpyAsync(d.cell_idx, sci, n * 4, cudaMemcpyHostToDevice, st));
+  for (int k = 0; k < kCount; ++k) sc[k] = 0;
   sc[kT] = t;
-  CU(cudaMemcpyAsync(d.scal, sc, sizeof sc, cudaMemcpyHostToDevice, st));
-  if (a) {
-    CU(cudaMemcpyAsync(d.aS, a, G * 8, cudaMemcpyHostToDevice, st));
-  } else {
-    launch_sound_cmax(d, true, st);
-  }
+  CU(cudaMemcpyAsync(d.scal, sc, kCount * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (a) CU(cudaMemcpyAsync(d.aS, a, G * 8, cudaMemcpyHostToDevice, st));
+  ctx->a_stale = !a;
   CU(cudaStreamSynchronize(st));
   CU(cudaGetLastError());
   return 0;
@@ -521,14 +546,19 @@ int hymor_get_state(hymor_ctx* ctx, double* q, double* pts_x, double* pts_y, dou
     CU(cudaMemcpyAsync(q + 2 * G, d.S.rv, G * 8, cudaMemcpyDeviceToHost, st));
     CU(cudaMemcpyAsync(q + 3 * G, d.S.rE, G * 8, cudaMemcpyDeviceToHost, st));
   }
-  if (pts_x) CU(cudaMemcpyAsync(pts_x, d.Sp.x, n * 8, cudaMemcpyDeviceToHost, st));
-  if (pts_y) CU(cudaMemcpyAsync(pts_y, d.Sp.y, n * 8, cudaMemcpyDeviceToHost, st));
-  if (pts_chi) CU(cudaMemcpyAsync(pts_chi, d.Sp.chi, n * 8, cudaMemcpyDeviceToHost, st));
-  if (pts_eta) CU(cudaMemcpyAsync(pts_eta, d.Sp.eta, n * 8, cudaMemcpyDeviceToHost, st));
-  if (cell_idx) CU(cudaMemcpyAsync(cell_idx, d.cell_idx, n * 4, cudaMemcpyDeviceToHost, st));
-  double sc[kCount];
-  CU(cudaMemcpyAsync(sc, d.scal, sizeof sc, cudaMemcpyDeviceToHost, st));
+  double* sp = reinterpret_cast<double*>(ctx->stage);
+  double* sc = sp + 4 * n;
+  int32_t* sci = reinterpret_cast<int32_t*>(sc + kCount);
+  double* out[4] = {pts_x, pts_y, pts_chi, pts_eta};
+  const double* src[4] = {d.Sp.x, d.Sp.y, d.Sp.chi, d.Sp.eta};
+  for (int k = 0; k < 4; ++k)
+    if (out[k]) CU(cudaMemcpyAsync(sp + k * n, src[k], n * 8, cudaMemcpyDeviceToHost, st));
+  if (cell_idx) CU(cudaMemcpyAsync(sci, d.cell_idx, n * 4, cudaMemcpyDeviceToHost, st));
+  CU(cudaMemcpyAsync(sc, d.scal, kCount * sizeof(double), cudaMemcpyDeviceToHost, st));
   CU(cudaStreamSynchronize(st));
+  for (int k = 0; k < 4; ++k)
+    if (out[k]) std::memcpy(out[k], sp + k * n, n * 8);
+  if (cell_idx) std::memcpy(cell_idx, sci, n * 4);
   if (t) *t = sc[kT];
   if (dt) *dt = sc[kDt];
   return 0;
@@ -541,6 +571,7 @@ int hymor_residual(hymor_ctx* ctx, double* flux) {
   cudaStream_t st = ctx->stream;
   launch_update_thermo(d, 3, 0, 0, st);
   launch_sound_cmax(d, true, st);
+  ctx->a_stale = false;
   launch_shock_bc(d, true, false, false, 0, 0, 1, st);
   double* const SF[4] = {d.SF[0], d.SF[1], d.SF[2], d.SF[3]};
   launch_flux(d, true, SF, st);
@@ -565,6 +596,7 @@ int hymor_step(hymor_ctx* ctx, int nsteps) {
   if (nsteps < 0) return fail(ctx, HYMOR_ERR_INVALID, "nsteps < 0");
   TRY(set_device(ctx));
   TRY(build_graph(ctx));
+  if (nsteps > 0) refresh_sound(ctx, ctx->d.cfg.shock_enabled);  // the step recomputes it with shock fitting
   for (int s = 0; s < nsteps; ++s) {
     if (ctx->profile) {
       for (int k = 0; k < hymor_ctx_s::kEv; ++k) {
@@ -590,6 +622,7 @@ int hymor_bench_steps(hymor_ctx* ctx, int nsteps, uint64_t flush_bytes, float* m
     CU(cudaMalloc(&ctx->flush_buf, flush_bytes));
     ctx->flush_bytes = flush_bytes;
   }
+  if (nsteps > 0) refresh_sound(ctx, ctx->d.cfg.shock_enabled);
   std::vector<cudaEvent_t> ev(2 * (size_t)nsteps);
   for (auto& e : ev) CU(cudaEventCreate(&e));
   for (int s = 0; s < nsteps; ++s) {
@@ -625,6 +658,7 @@ int hymor_update_flow_cells(hymor_ctx* ctx) {
   if (ctx->d.cfg.shock_enabled) {
     launch_flow_cells(ctx->d, ctx->stream);
     launch_sound_cmax(ctx->d, true, ctx->stream);
+    ctx->a_stale = false;
   }
   CU(cudaGetLastError());
   return read_err(ctx);
@@ -634,6 +668,7 @@ int hymor_cfl_timestep(hymor_ctx* ctx, double* dt) {
   if (!ctx) return HYMOR_ERR_INVALID;
   TRY(set_device(ctx));
   DevCtx& d = ctx->d;
+  refresh_sound(ctx, false);
   CU(cudaMemsetAsync(d.scal + kCmax, 0, 3 * sizeof(double), ctx->stream));
   launch_sound_cmax(d, false, ctx->stream);
   launch_cfl(d, ctx->stream);
