@@ -321,8 +321,13 @@ int set_device(hymor_ctx* ctx) {
   return 0;
 }
 
-// staging layout: pts x, y, chi, eta (n doubles each), scalars (kCount doubles), cell_idx (n int32)
-size_t stage_bytes(int n) { return (4 * (size_t)n + kCount) * sizeof(double) + (size_t)n * sizeof(int32_t); }
+// State layout shared by the device block and the pinned staging buffer: each plane is
+// padded to a multiple of 32 doubles (256 bytes).
+//   header: pts x, y, chi, eta (np doubles each), scalars (kScalPitch doubles), cell_idx (n int32)
+constexpr size_t kScalPitch = 32;
+size_t state_pitch(size_t n) { return (n + 31) & ~size_t(31); }
+size_t header_doubles(size_t n) { return 4 * state_pitch(n) + kScalPitch + (n + 1) / 2; }
+size_t stage_bytes(int n) { return header_doubles(n) * sizeof(double); }
 
 // Computes the persistent sound speed of S if set_state left it stale, unless the work
 // about to be enqueued recomputes it before reading it.
@@ -409,7 +414,13 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
     TRY(dalloc(ctx, &s.chi, d.nchi)); TRY(dalloc(ctx, &s.eta, d.nchi));
     return 0;
   };
-  if ((r = cons(d.S)) || (r = cons(d.Y))) return bail(r);
+  {  // S in one block (4 planes, each 256-byte aligned) so that a state moves in one 2-D copy
+    const size_t Gp = state_pitch(d.G);
+    double* b = nullptr;
+    if ((r = dalloc(ctx, &b, 4 * Gp))) return bail(r);
+    d.S = Cons{b, b + Gp, b + 2 * Gp, b + 3 * Gp};
+  }
+  if ((r = cons(d.Y))) return bail(r);
   if (cfg->rk_variant == 1) {
     if ((r = cons(d.Yc)) || (r = pts(d.Ycp))) return bail(r);
   } else {
@@ -421,11 +432,20 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
     return bail(r);
   for (int v = 0; v < 4; ++v)
     if ((r = dalloc(ctx, &d.F[v], d.N)) || (r = dalloc(ctx, &d.SF[v], d.N))) return bail(r);
-  if ((r = pts(d.Sp)) || (r = pts(d.Yp))) return bail(r);
-  if ((r = dalloc(ctx, &d.cell_idx, d.nchi)) || (r = dalloc(ctx, &d.beta, d.nchi)) ||
+  {  // shock points of S, the scalars and the cell indices in one block, laid out like the
+     // pinned staging buffer, so that they move in one copy
+    const size_t np = state_pitch(d.nchi);
+    double* b = nullptr;
+    if ((r = dalloc(ctx, &b, header_doubles(d.nchi)))) return bail(r);
+    d.Sp = ShockPts{b, b + np, b + 2 * np, b + 3 * np};
+    d.scal = b + 4 * np;
+    d.cell_idx = reinterpret_cast<int*>(b + 4 * np + kScalPitch);
+  }
+  if ((r = pts(d.Yp))) return bail(r);
+  if ((r = dalloc(ctx, &d.beta, d.nchi)) ||
       (r = dalloc(ctx, &d.speed_x, d.nchi)) || (r = dalloc(ctx, &d.speed_y, d.nchi)) ||
       (r = dalloc(ctx, &d.rel, d.nchi)) || (r = dalloc(ctx, &d.spl, 17 * (long)d.nchi + 16)) ||
-      (r = dalloc(ctx, &d.scal, (long)kCount)) || (r = dalloc(ctx, &d.err, (long)kErrCount)) ||
+      (r = dalloc(ctx, &d.err, (long)kErrCount)) ||
       (r = dalloc(ctx, &d.cflw, d.NLR + d.NBT)))
     return bail(r);
   d.coef = nullptr;
@@ -506,26 +526,26 @@ int hymor_set_state(hymor_ctx* ctx, const double* q, const double* pts_x, const 
     }
   }
   cudaStream_t st = ctx->stream;
-  CU(cudaStreamSynchronize(st));  // the staging buffer may still feed an earlier copy
-  CU(cudaMemcpyAsync(d.S.rho, q, G * 8, cudaMemcpyHostToDevice, st));
-  CU(cudaMemcpyAsync(d.S.ru, q + G, G * 8, cudaMemcpyHostToDevice, st));
-  CU(cudaMemcpyAsync(d.S.rv, q + 2 * G, G * 8, cudaMemcpyHostToDevice, st));
-  CU(cudaMemcpyAsync(d.S.rE, q + 3 * G, G * 8, cudaMemcpyHostToDevice, st));
-  double* sp = reinterpret_cast<double*>(ctx->stage);
-  double* sc = sp + 4 * n;
-  int32_t* sci = reinterpret_cast<int32_t*>(sc + kCount);
+  const size_t np = state_pitch(n), Gp = state_pitch(G);
+  CU(cudaMemcpy2DAsync(d.S.rho, Gp * 8, q, G * 8, G * 8, 4, cudaMemcpyHostToDevice, st));
+  double* sp = reinterpret_cast<double*>(ctx->stage);  // staged header, same layout as on the device
+  double* sc = sp + 4 * np;
+  int32_t* sci = reinterpret_cast<int32_t*>(sc + kScalPitch);
   const double* src[4] = {pts_x, pts_y, pts_chi, pts_eta};
   double* dst[4] = {d.Sp.x, d.Sp.y, d.Sp.chi, d.Sp.eta};
+  const bool all_pts = pts_x && pts_y && pts_chi && pts_eta;
   for (int k = 0; k < 4; ++k)
-    if (src[k]) {
-      std::memcpy(sp + k * n, src[k], n * 8);
-      CU(cudaMemcpyAsync(dst[k], sp + k * n, n * 8, cudaMemcpyHostToDevice, st));
-    }
+    if (src[k]) std::memcpy(sp + k * np, src[k], n * 8);
   std::memcpy(sci, ci.data(), n * 4);
-  CU(cudaMemcpyAsync(d.cell_idx, sci, n * 4, cudaMemcpyHostToDevice, st));
-  for (int k = 0; k < kCount; ++k) sc[k] = 0;
+  for (size_t k = 0; k < kScalPitch; ++k) sc[k] = 0;
   sc[kT] = t;
-  CU(cudaMemcpyAsync(d.scal, sc, kCount * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (all_pts) {
+    CU(cudaMemcpyAsync(d.Sp.x, sp, header_doubles(n) * 8, cudaMemcpyHostToDevice, st));
+  } else {  // keep the device copies of the points the caller did not pass
+    for (int k = 0; k < 4; ++k)
+      if (src[k]) CU(cudaMemcpyAsync(dst[k], sp + k * np, n * 8, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(d.scal, sc, (header_doubles(n) - 4 * np) * 8, cudaMemcpyHostToDevice, st));
+  }
   if (a) CU(cudaMemcpyAsync(d.aS, a, G * 8, cudaMemcpyHostToDevice, st));
   ctx->a_stale = !a;
   CU(cudaStreamSynchronize(st));
@@ -540,24 +560,16 @@ int hymor_get_state(hymor_ctx* ctx, double* q, double* pts_x, double* pts_y, dou
   DevCtx& d = ctx->d;
   const size_t G = d.G, n = d.nchi;
   cudaStream_t st = ctx->stream;
-  if (q) {
-    CU(cudaMemcpyAsync(q, d.S.rho, G * 8, cudaMemcpyDeviceToHost, st));
-    CU(cudaMemcpyAsync(q + G, d.S.ru, G * 8, cudaMemcpyDeviceToHost, st));
-    CU(cudaMemcpyAsync(q + 2 * G, d.S.rv, G * 8, cudaMemcpyDeviceToHost, st));
-    CU(cudaMemcpyAsync(q + 3 * G, d.S.rE, G * 8, cudaMemcpyDeviceToHost, st));
-  }
+  const size_t np = state_pitch(n), Gp = state_pitch(G);
+  if (q) CU(cudaMemcpy2DAsync(q, G * 8, d.S.rho, Gp * 8, G * 8, 4, cudaMemcpyDeviceToHost, st));
   double* sp = reinterpret_cast<double*>(ctx->stage);
-  double* sc = sp + 4 * n;
-  int32_t* sci = reinterpret_cast<int32_t*>(sc + kCount);
+  double* sc = sp + 4 * np;
+  int32_t* sci = reinterpret_cast<int32_t*>(sc + kScalPitch);
   double* out[4] = {pts_x, pts_y, pts_chi, pts_eta};
-  const double* src[4] = {d.Sp.x, d.Sp.y, d.Sp.chi, d.Sp.eta};
-  for (int k = 0; k < 4; ++k)
-    if (out[k]) CU(cudaMemcpyAsync(sp + k * n, src[k], n * 8, cudaMemcpyDeviceToHost, st));
-  if (cell_idx) CU(cudaMemcpyAsync(sci, d.cell_idx, n * 4, cudaMemcpyDeviceToHost, st));
-  CU(cudaMemcpyAsync(sc, d.scal, kCount * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CU(cudaMemcpyAsync(sp, d.Sp.x, header_doubles(n) * 8, cudaMemcpyDeviceToHost, st));
   CU(cudaStreamSynchronize(st));
   for (int k = 0; k < 4; ++k)
-    if (out[k]) std::memcpy(out[k], sp + k * n, n * 8);
+    if (out[k]) std::memcpy(out[k], sp + k * np, n * 8);
   if (cell_idx) std::memcpy(cell_idx, sci, n * 4);
   if (t) *t = sc[kT];
   if (dt) *dt = sc[kDt];
