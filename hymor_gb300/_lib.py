@@ -33,7 +33,7 @@ EXPORTS = [
     "hymor_expm_apply", "hymor_expm_apply_dev", "hymor_device_alloc", "hymor_device_free",
     "hymor_memcpy_h2d", "hymor_memcpy_d2h", "hymor_bench_steps", "hymor_dot_dev",
     "hymor_krylov_orthogonalize", "hymor_krylov_rotate", "hymor_block4_apply_dev", "hymor_memcpy_d2d",
-    "hymor_expm_apply_dev_noalloc", "hymor_step_kernels",
+    "hymor_expm_apply_dev_noalloc", "hymor_step_kernels", "hymor_fp64_peak",
 ]
 
 
@@ -70,6 +70,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "hymor_cfl_timestep": [vp, dp],
         "hymor_counters": [vp, ip, ip],
         "hymor_step_kernels": [vp, ip],
+        "hymor_fp64_peak": [vp, dp],
         "hymor_timer_start": [vp],
         "hymor_timer_stop": [vp, ctypes.POINTER(ctypes.c_float)],
         "hymor_profile_flux": [vp, i, ctypes.POINTER(ctypes.c_float), ip],

@@ -811,4 +811,5 @@ cudaStream_t ctx_stream(hymor_ctx* c) { return c->stream; }
 int ctx_fail(hymor_ctx* c, int code, const char* msg) { return fail(c, code, "%s", msg); }
 std::vector<void*>& ctx_allocs(hymor_ctx* c) { return c->allocs; }
 void*& ctx_linear_state(hymor_ctx* c) { return c->linear_state; }
+int ctx_select_device(hymor_ctx* c) { return cudaSetDevice(c->device) == cudaSuccess ? 0 : HYMOR_ERR_CUDA; }
 }  // namespace hymor

@@ -125,6 +125,10 @@ int hymor_counters(hymor_ctx* ctx, int32_t* rho_limited, int32_t* rh_warnings);
 /* Number of kernel launches one hymor_step makes (the kernel nodes of its CUDA graph),
  * for launch accounting. No counterpart in the reference. */
 int hymor_step_kernels(hymor_ctx* ctx, int32_t* n);
+/* FP64 FMA throughput of the context's GPU in TFLOP/s (independent DFMA chains over
+ * every SM, timed with CUDA events), the roofline denominator of the FP64-bound
+ * kernels. No counterpart in the reference. */
+int hymor_fp64_peak(hymor_ctx* ctx, double* tflops);
 
 /* Device timing on the context stream (CUDA events): start, then stop returns ms. */
 int hymor_timer_start(hymor_ctx* ctx);
