@@ -219,6 +219,7 @@ int enqueue_step(hymor_ctx* ctx, bool with_events) {
     launch_spline(d, false, true, ctx->fit);
     CU(cudaEventRecord(ctx->fit_join, ctx->fit));
     if (shock) launch_flow_cells(d, st);
+    launch_classify_tiles(d, st);
     // Side stream: the CFL reduction, and every later smoothing-spline fit one stage
     // early (a fit needs only the shock points, which the previous stage's jump kernel
     // moved); then per stage the jump + boundary kernels beside the flux of the
@@ -445,7 +446,7 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
   if ((r = dalloc(ctx, &d.beta, d.nchi)) ||
       (r = dalloc(ctx, &d.speed_x, d.nchi)) || (r = dalloc(ctx, &d.speed_y, d.nchi)) ||
       (r = dalloc(ctx, &d.rel, d.nchi)) || (r = dalloc(ctx, &d.spl, 17 * (long)d.nchi + 16)) ||
-      (r = dalloc(ctx, &d.err, (long)kErrCount)) ||
+      (r = dalloc(ctx, &d.err, (long)kErrCount)) || (r = dalloc(ctx, &d.tiles, 2 + 2 * (long)flux_tiles(d))) ||
       (r = dalloc(ctx, &d.cflw, d.NLR + d.NBT)))
     return bail(r);
   d.coef = nullptr;

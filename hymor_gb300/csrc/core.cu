@@ -950,7 +950,40 @@ struct FluxArgs {
   int mask;                // shock fitting with feedback: zero flux at j >= sc
   int shock;
   int tile_class;          // -1 all tiles; 0 tiles reading nothing the shock/BC kernels write; 1 the others
+  // compact tile list of one class (k_classify_tiles): block b processes tile list[b]
+  // when b < *count; null: the grid is the tile grid
+  const int* list;
+  const int* count;
+  int tiles_x;
 };
+
+// Tile classes of the RK step, once per step (the shocked rows are fixed within a step):
+// 0 = the halo (ghosted columns i0-1 .. i0+TX, rows j0 .. j0+TY+1) avoids every ghost cell
+// and stays below the shocked rows sc .. sc+2 of its columns, so its flux does not wait
+// for the shock/boundary kernels; 1 = the others; tiles wholly at or above the shocked
+// rows (zero flux under the NON_LINEAR_DYNAMICS mask, never read by the stage update)
+// are left out. lists: [count0, count1, class 0 tiles (ntiles), class 1 tiles (ntiles)].
+__global__ void k_classify_tiles(const int* __restrict__ cell_idx, int* lists, int nchi, int neta, int tiles_x,
+                                 int ntiles, int shock, int mask) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntiles) return;
+  const int i0 = (t % tiles_x) * TX, j0 = (t / tiles_x) * TY;
+  if (mask) {
+    int sc = 0;
+    for (int c = i0; c < i0 + TX && c < nchi; ++c) sc = max(sc, cell_idx[c]);
+    if (j0 + 1 >= sc) return;
+  }
+  bool inner = i0 >= 1 && i0 + TX + 1 <= nchi && j0 >= 1 && j0 + TY + 1 <= neta;
+  if (shock) {
+    int scmin = 0x7fffffff;
+    for (int c = i0 - 1; c <= i0 + TX; ++c)
+      if (c >= 0 && c < nchi) scmin = min(scmin, cell_idx[c]);
+    inner = inner && (j0 + TY + 1 < scmin);
+  }
+  const int cls = inner ? 0 : 1;
+  const int slot = atomicAdd(&lists[cls], 1);
+  lists[2 + cls * ntiles + slot] = t;
+}
 
 template <bool AXI, bool SUTH>
 __global__ void __launch_bounds__(kFluxThreads, 3) k_flux(FluxArgs a) {
@@ -972,10 +1005,17 @@ __global__ void __launch_bounds__(kFluxThreads, 3) k_flux(FluxArgs a) {
   double* t_bt = t_lr + (AXI ? NLRF : 0);
 
   const int nchi = a.nchi, neta = a.neta;
-  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;  // first interior cell (0-based)
+  int bx = blockIdx.x, by = blockIdx.y;
+  if (a.list) {
+    if ((int)blockIdx.x >= *a.count) return;
+    const int t = a.list[blockIdx.x];
+    bx = t % a.tiles_x;
+    by = t / a.tiles_x;
+  }
+  const int i0 = bx * TX, j0 = by * TY;  // first interior cell (0-based)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
-  if (a.tile_class >= 0) {
+  if (a.tile_class >= 0 && !a.list) {
     // the halo (ghosted columns i0..i0+TX+1, rows j0..j0+TY+1) avoids every ghost cell and
     // stays below the shocked rows sc..sc+2 of its columns -> independent of shock/BC work
     bool inner = i0 >= 1 && i0 + TX + 1 <= nchi && j0 >= 1 && j0 + TY + 1 <= neta;
@@ -1650,9 +1690,22 @@ void launch_shock_bc_flags(const DevCtx& d, bool on_S, bool copy_pts, bool do_sh
   launch_shock_bc_impl(d, on_S, copy_pts, false, 0, 0, a_mode, do_shock, do_bc, st);
 }
 
+int flux_tiles_x(const DevCtx& d) { return (d.nchi + TX - 1) / TX; }
+int flux_tiles(const DevCtx& d) { return flux_tiles_x(d) * ((d.neta + TY - 1) / TY); }
+
+void launch_classify_tiles(const DevCtx& d, cudaStream_t st) {
+  const int nt = flux_tiles(d);
+  cudaMemsetAsync(d.tiles, 0, 2 * sizeof(int), st);
+  k_classify_tiles<<<(nt + 127) / 128, 128, 0, st>>>(d.cell_idx, d.tiles, d.nchi, d.neta, flux_tiles_x(d), nt,
+                                                   d.cfg.shock_enabled, d.cfg.shock_enabled && d.cfg.shock_feedback);
+}
+
 void launch_flux_class(const DevCtx& d, bool on_S, double* const out[4], int tile_class, cudaStream_t st) {
   FluxArgs a;
   a.tile_class = tile_class;
+  a.list = nullptr;
+  a.count = nullptr;
+  a.tiles_x = flux_tiles_x(d);
   const Cons& q = on_S ? d.S : d.Y;
   a.rho = q.rho; a.ru = q.ru; a.rv = q.rv; a.rE = q.rE;
   a.p = d.p;
@@ -1676,6 +1729,12 @@ void launch_flux_class(const DevCtx& d, bool on_S, double* const out[4], int til
   a.shock = c.shock_enabled;
   a.mask = c.shock_enabled && c.shock_feedback;
   dim3 grid((d.nchi + TX - 1) / TX, (d.neta + TY - 1) / TY);
+  if (tile_class >= 0 && d.tiles) {  // the compact list of the class, one tile per block
+    const int nt = flux_tiles(d);
+    a.count = d.tiles + tile_class;
+    a.list = d.tiles + 2 + tile_class * nt;
+    grid = dim3(nt, 1);
+  }
   const bool axi = c.axisymmetric, suth = c.viscosity_model == 1;
   if (!axi && !suth) k_flux<false, false><<<grid, kFluxThreads, flux_smem<false, false>(), st>>>(a);
   else if (axi && !suth) k_flux<true, false><<<grid, kFluxThreads, flux_smem<true, false>(), st>>>(a);

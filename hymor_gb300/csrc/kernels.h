@@ -25,6 +25,7 @@ struct DevCtx {
   double* cflw;    // CFL face rates (NLR + NBT)
   double* scal;    // Scalar block
   unsigned* err;   // ErrWord block
+  int* tiles;      // flux tile lists of the RK step (launch_classify_tiles)
   // Jacobian
   double* coef;    // N * 144 stencil blocks (or null)
   double* jwork;   // linearisation workspace
@@ -49,8 +50,13 @@ void launch_columns_bc(const DevCtx& d, bool on_S, bool move, double cY, double 
                        bool do_bc, cudaStream_t st);
 // Flux (residual) of tgt into out[4] (masked by the flow cells when feedback is on).
 void launch_flux(const DevCtx& d, bool on_S, double* const out[4], cudaStream_t st);
-// tile_class 0: only tiles whose halo no shock/BC kernel writes; 1: the other tiles
+// tile_class 0: only tiles whose halo no shock/BC kernel writes; 1: the other tiles.
+// With the step's tile lists (d.tiles) each class runs over its compact list, and tiles
+// wholly above the shock are not evaluated (their flux is never read by the stage update).
 void launch_flux_class(const DevCtx& d, bool on_S, double* const out[4], int tile_class, cudaStream_t st);
+// Classifies the flux tiles of the current shocked rows into d.tiles.
+void launch_classify_tiles(const DevCtx& d, cudaStream_t st);
+int flux_tiles(const DevCtx& d);
 // UPDATE_FLOW_CELLS part 1: detect shocked cells, upstream fill, extrapolation (on S).
 void launch_flow_cells(const DevCtx& d, cudaStream_t st);
 // Sound speed of S (recompute) and max|a| into scal[kCmax]; recompute=false only reduces aS.

@@ -15,7 +15,7 @@ int ctx_select_device(hymor_ctx* c);
 namespace {
 
 constexpr int kPeakIlp = 8;       // independent chains per thread
-constexpr int kPeakIters = 4096;  // DFMA per chain
+constexpr int kPeakIters = 1024;  // DFMA per chain (~5 ms per launch on GB300)
 constexpr int kPeakThreads = 256;
 
 __global__ void __launch_bounds__(kPeakThreads) k_dfma_peak(double* out, double a, double b) {
