@@ -449,6 +449,8 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
       (r = dalloc(ctx, &d.err, (long)kErrCount)) || (r = dalloc(ctx, &d.tiles, 2 + 2 * (long)flux_tiles(d))) ||
       (r = dalloc(ctx, &d.cflw, d.NLR + d.NBT)))
     return bail(r);
+  if (cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess || d.sms < 1)
+    return bail(fail(ctx, HYMOR_ERR_CUDA, "multiprocessor count"));
   d.coef = nullptr;
   d.jwork = nullptr;
   for (int k = 0; k < hymor_ctx_s::kEv; ++k)

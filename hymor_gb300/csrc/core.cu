@@ -35,6 +35,8 @@ constexpr int CX = TX + 1, CY = TY + 1, NCOR = CX * CY;
 constexpr int NLRF = (TX + 1) * TY;  // 256
 constexpr int NBTF = TX * (TY + 1);  // 279
 constexpr int kFluxThreads = 256;
+// dynamic shared memory that leaves room for one flux block per SM (of 228 KB)
+constexpr size_t kFluxOneBlockSmem = 120 * 1024;
 
 // x > 0 (NaN excluded) on the integer pipe: the bit patterns of +0 .. +inf are ordered
 // as unsigned integers, and every NaN or negative pattern lies above +inf.
@@ -985,9 +987,9 @@ __global__ void k_classify_tiles(const int* __restrict__ cell_idx, int* lists, i
   lists[2 + cls * ntiles + slot] = t;
 }
 
+// One 31 x 8-cell tile (bx, by) of the residual; every thread of the block takes part.
 template <bool AXI, bool SUTH>
-__global__ void __launch_bounds__(kFluxThreads, 3) k_flux(FluxArgs a) {
-  extern __shared__ double sm[];
+__device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, double* sm) {
   double* s_r = sm;
   double* s_u = s_r + NH;   // u = rho_u / rho
   double* s_v = s_u + NH;
@@ -1005,13 +1007,6 @@ __global__ void __launch_bounds__(kFluxThreads, 3) k_flux(FluxArgs a) {
   double* t_bt = t_lr + (AXI ? NLRF : 0);
 
   const int nchi = a.nchi, neta = a.neta;
-  int bx = blockIdx.x, by = blockIdx.y;
-  if (a.list) {
-    if ((int)blockIdx.x >= *a.count) return;
-    const int t = a.list[blockIdx.x];
-    bx = t % a.tiles_x;
-    by = t / a.tiles_x;
-  }
   const int i0 = bx * TX, j0 = by * TY;  // first interior cell (0-based)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
@@ -1220,6 +1215,22 @@ __global__ void __launch_bounds__(kFluxThreads, 3) k_flux(FluxArgs a) {
       }
       a.o0[c] = r0; a.o1[c] = r1; a.o2[c] = r2; a.o3[c] = r3;
     }
+  }
+}
+
+// Tile grid (no list), or a persistent grid striding over the compact tile list of a class.
+template <bool AXI, bool SUTH>
+__global__ void __launch_bounds__(kFluxThreads, 4) k_flux(FluxArgs a) {
+  extern __shared__ double sm[];
+  if (!a.list) {
+    flux_tile<AXI, SUTH>(a, blockIdx.x, blockIdx.y, sm);
+    return;
+  }
+  const int n = *a.count;
+  for (int k = blockIdx.x; k < n; k += gridDim.x) {
+    const int t = a.list[k];
+    flux_tile<AXI, SUTH>(a, t % a.tiles_x, t / a.tiles_x, sm);
+    __syncthreads();  // the next tile reuses the shared arrays
   }
 }
 
@@ -1690,6 +1701,9 @@ void launch_shock_bc_flags(const DevCtx& d, bool on_S, bool copy_pts, bool do_sh
   launch_shock_bc_impl(d, on_S, copy_pts, false, 0, 0, a_mode, do_shock, do_bc, st);
 }
 
+// resident flux blocks per SM of each variant (index 2 axisymmetric + Sutherland)
+int g_flux_blocks_per_sm[4] = {3, 3, 3, 3};
+
 int flux_tiles_x(const DevCtx& d) { return (d.nchi + TX - 1) / TX; }
 int flux_tiles(const DevCtx& d) { return flux_tiles_x(d) * ((d.neta + TY - 1) / TY); }
 
@@ -1729,17 +1743,24 @@ void launch_flux_class(const DevCtx& d, bool on_S, double* const out[4], int til
   a.shock = c.shock_enabled;
   a.mask = c.shock_enabled && c.shock_feedback;
   dim3 grid((d.nchi + TX - 1) / TX, (d.neta + TY - 1) / TY);
-  if (tile_class >= 0 && d.tiles) {  // the compact list of the class, one tile per block
+  size_t extra = 0;
+  if (tile_class >= 0 && d.tiles) {
+    // the compact list of the class over a persistent grid: three blocks per SM for the
+    // interior tiles; one block per SM (the shared-memory request admits no second) for
+    // the few shock/boundary tiles, which would otherwise pile up on some SMs
     const int nt = flux_tiles(d);
     a.count = d.tiles + tile_class;
     a.list = d.tiles + 2 + tile_class * nt;
-    grid = dim3(nt, 1);
+    const bool axi = c.axisymmetric, suth = c.viscosity_model == 1;
+    grid = dim3(tile_class == 0 ? g_flux_blocks_per_sm[axi * 2 + suth] * d.sms : d.sms, 1);
+    if (tile_class == 1) extra = kFluxOneBlockSmem;
   }
   const bool axi = c.axisymmetric, suth = c.viscosity_model == 1;
-  if (!axi && !suth) k_flux<false, false><<<grid, kFluxThreads, flux_smem<false, false>(), st>>>(a);
-  else if (axi && !suth) k_flux<true, false><<<grid, kFluxThreads, flux_smem<true, false>(), st>>>(a);
-  else if (!axi && suth) k_flux<false, true><<<grid, kFluxThreads, flux_smem<false, true>(), st>>>(a);
-  else k_flux<true, true><<<grid, kFluxThreads, flux_smem<true, true>(), st>>>(a);
+  auto smem = [&](size_t need) { return need > extra ? need : extra; };
+  if (!axi && !suth) k_flux<false, false><<<grid, kFluxThreads, smem(flux_smem<false, false>()), st>>>(a);
+  else if (axi && !suth) k_flux<true, false><<<grid, kFluxThreads, smem(flux_smem<true, false>()), st>>>(a);
+  else if (!axi && suth) k_flux<false, true><<<grid, kFluxThreads, smem(flux_smem<false, true>()), st>>>(a);
+  else k_flux<true, true><<<grid, kFluxThreads, smem(flux_smem<true, true>()), st>>>(a);
 }
 
 void launch_flux(const DevCtx& d, bool on_S, double* const out[4], cudaStream_t st) {
@@ -1747,10 +1768,19 @@ void launch_flux(const DevCtx& d, bool on_S, double* const out[4], cudaStream_t 
 }
 
 void flux_kernel_setup() {
-  cudaFuncSetAttribute(k_flux<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem<false, false>());
-  cudaFuncSetAttribute(k_flux<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem<true, false>());
-  cudaFuncSetAttribute(k_flux<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem<false, true>());
-  cudaFuncSetAttribute(k_flux<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem<true, true>());
+  cudaFuncSetAttribute(k_flux<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxOneBlockSmem);
+  cudaFuncSetAttribute(k_flux<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxOneBlockSmem);
+  cudaFuncSetAttribute(k_flux<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxOneBlockSmem);
+  cudaFuncSetAttribute(k_flux<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxOneBlockSmem);
+  auto occ = [](auto kern, size_t smem) {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kFluxThreads, smem) != cudaSuccess || b < 1) b = 1;
+    return b;
+  };
+  g_flux_blocks_per_sm[0] = occ(k_flux<false, false>, flux_smem<false, false>());
+  g_flux_blocks_per_sm[1] = occ(k_flux<false, true>, flux_smem<false, true>());
+  g_flux_blocks_per_sm[2] = occ(k_flux<true, false>, flux_smem<true, false>());
+  g_flux_blocks_per_sm[3] = occ(k_flux<true, true>, flux_smem<true, true>());
   cudaFuncSetAttribute(k_spline_fit, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)sizeof(float) * kSplineArrays * spline_stride(4096));
 }

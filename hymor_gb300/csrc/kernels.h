@@ -8,6 +8,7 @@ namespace hymor {
 struct DevCtx {
   hymor_config cfg;
   int nchi, neta, NI, NJ;
+  int sms;         // streaming multiprocessors of the device
   long G, N, NLR, NBT;
   DevMesh m;
   Cons S;          // the solution (reference `s`)
