@@ -128,6 +128,9 @@ void face_geometry(const hymor_config& c, const hymor_mesh& m, std::vector<doubl
   const long NLR = (long)(nchi + 1) * neta, NBT = (long)nchi * (neta + 1), N = (long)nchi * neta;
   lrg.assign(kGeoPlanes * NLR, 0.0);
   btg.assign(kGeoPlanes * NBT, 0.0);
+  // the gradient planes carry 2 mu*/Re (mu* = 1 for CPG), so that the face kernel forms
+  // twice the viscous traction without a multiply (Sutherland faces scale it by mu_f)
+  const double vs = 2.0 / c.Re;
   rvol.assign(N, 0.0);
   rxl.assign(NLR, 0.0);
   rxb.assign(NBT, 0.0);
@@ -149,10 +152,10 @@ void face_geometry(const hymor_config& c, const hymor_mesh& m, std::vector<doubl
       lrg[0 * NLR + f] = nx;
       lrg[1 * NLR + f] = ny;
       lrg[2 * NLR + f] = 0.5 * m.lr_a[f];
-      lrg[3 * NLR + f] = -1.0 / (cld * Cnn);
-      lrg[4 * NLR + f] = 0.25 * (-Cft / (len * Cnn));
-      lrg[5 * NLR + f] = 0.25 * (1.0 / len);
-      rxl[f] = 1.0 / ((X(i + 1, j + 1) + X(i, j + 1)) / 2);
+      lrg[3 * NLR + f] = vs * (-1.0 / (cld * Cnn));
+      lrg[4 * NLR + f] = vs * (0.25 * (-Cft / (len * Cnn)));
+      lrg[5 * NLR + f] = vs * (0.25 * (1.0 / len));
+      rxl[f] = vs * (1.0 / ((X(i + 1, j + 1) + X(i, j + 1)) / 2));
     }
   for (int j = 0; j <= neta; ++j)
     for (int i = 0; i < nchi; ++i) {
@@ -168,10 +171,10 @@ void face_geometry(const hymor_config& c, const hymor_mesh& m, std::vector<doubl
       btg[0 * NBT + f] = nx;
       btg[1 * NBT + f] = ny;
       btg[2 * NBT + f] = 0.5 * m.bt_a[f];
-      btg[3 * NBT + f] = 1.0 / (cbd * Cnn);
-      btg[4 * NBT + f] = 0.25 * (Cft / (len * Cnn));
-      btg[5 * NBT + f] = 0.25 * (1.0 / len);
-      rxb[f] = 1.0 / ((X(i + 1, j + 1) + X(i + 1, j)) / 2);
+      btg[3 * NBT + f] = vs * (1.0 / (cbd * Cnn));
+      btg[4 * NBT + f] = vs * (0.25 * (Cft / (len * Cnn)));
+      btg[5 * NBT + f] = vs * (0.25 * (1.0 / len));
+      rxb[f] = vs * (1.0 / ((X(i + 1, j + 1) + X(i + 1, j)) / 2));
     }
   for (long k = 0; k < N; ++k) rvol[k] = 1.0 / m.vol[k];
   gvis.assign(N, 0.0);

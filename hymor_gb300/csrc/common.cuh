@@ -17,16 +17,16 @@ namespace hymor {
 
 constexpr int kWarp = 32;
 
-// Face geometry planes (precomputed once per mesh, hymor_ctx_create):
+// Face geometry planes (precomputed once per mesh, hymor_ctx_create), with s = 2 / Re:
 //   lr face (i, j), between ghosted cells (i, j+1) and (i+1, j+1):
-//     0 nx, 1 ny, 2 A/2, 3 g1 = -1 / (cld * Cn1_Fn1), 4 g2/4 = -Cn1_Ft1 / (4 len Cn1_Fn1), 5 1/(4 len)
+//     0 nx, 1 ny, 2 A/2, 3 s g1 = -s / (cld * Cn1_Fn1), 4 s g2/4 = -s Cn1_Ft1 / (4 len Cn1_Fn1), 5 s/(4 len)
 //   bt face (i, j), between ghosted cells (i+1, j) and (i+1, j+1):
-//     0 nx, 1 ny, 2 A/2, 3 h1 = 1 / (cbd * Cn2_Fn2),  4 h2/4 = Cn2_Ft2 / (4 len Cn2_Fn2),   5 1/(4 len)
-// so that, with U_c = 4 u_c the sum of the four cells around a corner (VISCOUS_FLUX.jl:98-127),
-//   du_dn1 = g1 * (u_R - u_L) + (g2/4) * (U_c(i, j+1) - U_c(i, j)),  du_dt1 =  (U_c(i,j+1) - U_c(i,j)) / (4 len)
-//   du_dn2 = h1 * (u_T - u_B) + (h2/4) * (U_c(i+1, j) - U_c(i, j)),  du_dt2 = -(U_c(i+1,j) - U_c(i,j)) / (4 len)
-// Every factor 1/2 and 1/4 is a power of two, so the folded products round exactly as
-// the unfolded ones.
+//     0 nx, 1 ny, 2 A/2, 3 s h1 = s / (cbd * Cn2_Fn2),  4 s h2/4 = s Cn2_Ft2 / (4 len Cn2_Fn2),   5 s/(4 len)
+// so that, with U_c = 4 u_c the sum of the four cells around a corner, the gradients of
+// VISCOUS_FLUX.jl:98-127 come out multiplied by s:
+//   s du_dn1 = (s g1) (u_R - u_L) + (s g2/4) (U_c(i, j+1) - U_c(i, j)),  s du_dt1 =  (s/(4 len)) (U_c(i,j+1) - U_c(i,j))
+//   s du_dn2 = (s h1) (u_T - u_B) + (s h2/4) (U_c(i+1, j) - U_c(i, j)),  s du_dt2 = -(s/(4 len)) (U_c(i+1,j) - U_c(i,j))
+// and the traction formed from them is twice mu/Re times the unit-viscosity traction.
 constexpr int kGeoPlanes = 6;
 
 struct DevMesh {
@@ -37,8 +37,8 @@ struct DevMesh {
   const double* lrg;   // kGeoPlanes x NLR
   const double* btg;   // kGeoPlanes x NBT
   const double* rvol;  // N
-  const double* rx_lr;  // axisymmetric: 1 / x_face on lr faces (NLR)
-  const double* rx_bt;  // axisymmetric: 1 / x_face on bt faces (NBT)
+  const double* rx_lr;  // axisymmetric: (2 / Re) / x_face on lr faces (NLR)
+  const double* rx_bt;  // axisymmetric: (2 / Re) / x_face on bt faces (NBT)
   const double* gvis;   // 2 (A_xi^2 + A_eta^2) / vol per cell (viscous CFL rate, CFL_TIMESTEP.jl:110-113)
 };
 

@@ -942,11 +942,10 @@ struct FluxArgs {
   double *o0, *o1, *o2, *o3;
   const int* cell_idx;
   DevMesh m;
-  double mre, kq;          // mu/Re and k gamma/(Re Pr) for constant transport
-  double inv_Re, gk;       // 1/Re and gamma/(Re Pr) for Sutherland faces
-  // the same doubled (exact): the face kernel forms twice the viscous traction and heat
-  // flux so that both halves of the flux multiply the stored A/2
-  double mre2, kq2, inv_Re2, gk2;
+  // The gradient planes carry 2 mu*/Re, so the face kernel forms twice the viscous
+  // traction (then multiplied by the stored A/2) and, with kpr = gamma / Pr, twice the
+  // heat flux k gamma / (Re Pr) dT/dn (CPG: mu* = k* = 1; Sutherland: both times mu_f).
+  double kpr;
   double suthS, Tinf_inv;
   int nchi, neta;
   int mask;                // shock fitting with feedback: zero flux at j >= sc
@@ -1102,13 +1101,12 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, dou
       const double En = fma(du_dt, nx, dv_dt * ny);
       const double Et = fma(du_dt, ny, -dv_dt * nx);
       double div = Et - Dn;
-      double mre = a.mre, mre2 = a.mre2, kq2 = a.kq2;
+      double kpr = a.kpr;  // gamma / Pr: the heat flux from the 2/Re-scaled temperature gradient
+      double mu_f = 1;
       if (SUTH) {  // Sutherland at the face temperature
         const double Ts = (s_T[L] + s_T[R]) * 0.5 * a.Tinf_inv;
-        const double mu_f = Ts * sqrt(Ts) * (1 + a.suthS) * frcp(Ts + a.suthS);
-        if (AXI) mre = mu_f * a.inv_Re;
-        mre2 = mu_f * a.inv_Re2;
-        kq2 = mu_f * a.gk2;
+        mu_f = Ts * sqrt(Ts) * (1 + a.suthS) * frcp(Ts + a.suthS);
+        kpr *= mu_f;
       }
       double uf = 0, rx = 0;
       if (AXI) {
@@ -1118,16 +1116,17 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, dou
       }
       // twice the traction, the work and the heat flux: (2 t) (A/2) = t A
       const double al = fma(2.0 / 3.0, div, Dn);
-      const double tx = mre2 * fma(al, nx, fma(-En, ny, du_dn));
-      const double ty = mre2 * fma(al, ny, fma(En, nx, dv_dn));
+      double tx = fma(al, nx, fma(-En, ny, du_dn));
+      double ty = fma(al, ny, fma(En, nx, dv_dn));
+      if (SUTH) { tx *= mu_f; ty *= mu_f; }
       const double w = fma(Su, tx, Sv * ty) * ir;
-      const double qn = kq2 * dT_dn;
+      const double qn = kpr * dT_dn;
       const int o = fx + fy * (TX + 1);
       f_lr[o] = m2 * Ah;
       f_lr[NLRF + o] = fma(Su, Vn, fma(Sp, nx, tx)) * Ah;
       f_lr[2 * NLRF + o] = fma(Sv, Vn, fma(Sp, ny, ty)) * Ah;
       f_lr[3 * NLRF + o] = fma(SE + Sp, Vn, w + qn) * Ah;
-      if (AXI) t_lr[o] = mre * fma(-2.0 / 3.0, div, 2 * uf * rx);
+      if (AXI) t_lr[o] = (0.5 * mu_f) * fma(-2.0 / 3.0, div, 2 * uf * rx);
     }
   }
   // (3b) bt faces: TX x (TY + 1)
@@ -1157,13 +1156,12 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, dou
       const double En = fma(du_dt, nx, dv_dt * ny);
       const double Et = fma(du_dt, ny, -dv_dt * nx);
       double div = Et + Dn;
-      double mre = a.mre, mre2 = a.mre2, kq2 = a.kq2;
+      double kpr = a.kpr;
+      double mu_f = 1;
       if (SUTH) {
         const double Ts = (s_T[B] + s_T[Tt]) * 0.5 * a.Tinf_inv;
-        const double mu_f = Ts * sqrt(Ts) * (1 + a.suthS) * frcp(Ts + a.suthS);
-        if (AXI) mre = mu_f * a.inv_Re;
-        mre2 = mu_f * a.inv_Re2;
-        kq2 = mu_f * a.gk2;
+        mu_f = Ts * sqrt(Ts) * (1 + a.suthS) * frcp(Ts + a.suthS);
+        kpr *= mu_f;
       }
       double uf = 0, rx = 0;
       if (AXI) {
@@ -1172,16 +1170,17 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, dou
         div = fma(uf, rx, div);
       }
       const double al = fma(-2.0 / 3.0, div, Dn);
-      const double tx = mre2 * fma(al, nx, fma(En, ny, du_dn));
-      const double ty = mre2 * fma(al, ny, fma(-En, nx, dv_dn));
+      double tx = fma(al, nx, fma(En, ny, du_dn));
+      double ty = fma(al, ny, fma(-En, nx, dv_dn));
+      if (SUTH) { tx *= mu_f; ty *= mu_f; }
       const double w = fma(Su, tx, Sv * ty) * ir;
-      const double qn = kq2 * dT_dn;
+      const double qn = kpr * dT_dn;
       const int o = fx + fy * TX;
       f_bt[o] = m2 * Ah;
       f_bt[NBTF + o] = fma(Su, Vn, fma(Sp, nx, -tx)) * Ah;
       f_bt[2 * NBTF + o] = fma(Sv, Vn, fma(Sp, ny, -ty)) * Ah;
       f_bt[3 * NBTF + o] = fma(SE + Sp, Vn, -(w + qn)) * Ah;
-      if (AXI) t_bt[o] = mre * fma(-2.0 / 3.0, div, 2 * uf * rx);
+      if (AXI) t_bt[o] = (0.5 * mu_f) * fma(-2.0 / 3.0, div, 2 * uf * rx);
     }
   }
   __syncthreads();
@@ -1728,14 +1727,7 @@ void launch_flux_class(const DevCtx& d, bool on_S, double* const out[4], int til
   a.cell_idx = d.cell_idx;
   a.m = d.m;
   const hymor_config& c = d.cfg;
-  a.mre = ((1.0 + 1.0) / 2) / c.Re;
-  a.kq = (1.0 + 1.0) / 2 * c.gamma / c.Re / c.Pr;
-  a.inv_Re = 1.0 / c.Re;
-  a.gk = c.gamma / c.Re / c.Pr;
-  a.mre2 = 2 * a.mre;
-  a.kq2 = 2 * a.kq;
-  a.inv_Re2 = 2 * a.inv_Re;
-  a.gk2 = 2 * a.gk;
+  a.kpr = c.gamma / c.Pr;
   a.suthS = c.sutherland_S;
   a.Tinf_inv = c.energy_factor / c.cv;
   a.nchi = d.nchi;
