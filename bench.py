@@ -58,7 +58,7 @@ def profile_numbers():
     out = {}
     try:
         for line in open(path):
-            for key in ("traffic_bytes_per_stage", "fp64_flop_per_stage"):
+            for key in ("traffic_bytes_per_stage", "fp64_flop_per_stage", "fp64_inst_per_stage"):
                 if line.strip().startswith(key + ":"):
                     out[key] = float(line.split(":", 1)[1].split()[0])
     except OSError:
@@ -291,6 +291,10 @@ def main():
             roofline["fp64"] = {"achieved_tflops": fp, "peak_tflops": fp64_peak.value, "unit": "TFLOP/s",
                                 "frac": fp / fp64_peak.value,
                                 "peak_kind": "DFMA throughput kernel timed in this run (hymor_fp64_peak)"}
+            if "fp64_inst_per_stage" in prof:
+                # the pipe issues one FP64 instruction (DFMA, DADD or DMUL) per lane-slot:
+                # instruction rate against the DFMA peak's instruction rate
+                roofline["fp64"]["inst_frac"] = (prof["fp64_inst_per_stage"] / flux_avg_s) / (fp64_peak.value * 1e12 / 2)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
