@@ -247,6 +247,8 @@ def main():
     torch.cuda.synchronize()
     barrier(dist)
     flux_ms, flux_n = ctypes.c_float(), ctypes.c_int32()
+    phases = (ctypes.c_float * 18)()
+    sol.ctx.check(L.hymor_profile_phases(h, phases))
     sol.ctx.check(L.hymor_profile_flux(h, 0, ctypes.byref(flux_ms), ctypes.byref(flux_n)))
     step_kernels = sol.step_kernels()
     t_dev = max_over_ranks(dist, ms.value / 1e3)
@@ -305,6 +307,12 @@ def main():
             "roofline": roofline,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": step_kernels * args.steps,
+            # main-stream phases of one step (us, averaged over the timed steps)
+            "step_phases_us": {"start": round(phases[0] * 1e3, 1),
+                               "stages": [[round(phases[1 + 4 * k + q] * 1e3, 1) for q in range(4)]
+                                          for k in range(4)],
+                               "stage_fields": ["update", "flux_interior", "wait_shock_bc", "flux_shock_bc"],
+                               "end": round(phases[17] * 1e3, 1)},
             "clocks": clk.summary(),
         }
         if not args.no_cpu_baseline and world == 1:

@@ -34,6 +34,7 @@ EXPORTS = [
     "hymor_memcpy_h2d", "hymor_memcpy_d2h", "hymor_bench_steps", "hymor_dot_dev",
     "hymor_krylov_orthogonalize", "hymor_krylov_rotate", "hymor_block4_apply_dev", "hymor_memcpy_d2d",
     "hymor_expm_apply_dev_noalloc", "hymor_step_kernels", "hymor_fp64_peak",
+    "hymor_profile_phases",
 ]
 
 
@@ -71,6 +72,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "hymor_counters": [vp, ip, ip],
         "hymor_step_kernels": [vp, ip],
         "hymor_fp64_peak": [vp, dp],
+        "hymor_profile_phases": [vp, ctypes.POINTER(ctypes.c_float)],
         "hymor_timer_start": [vp],
         "hymor_timer_stop": [vp, ctypes.POINTER(ctypes.c_float)],
         "hymor_profile_flux": [vp, i, ctypes.POINTER(ctypes.c_float), ip],

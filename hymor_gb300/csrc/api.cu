@@ -33,7 +33,9 @@ struct hymor_ctx_s {
   // flux-kernel profiling: event-record nodes around the flux launches of the 4 stages
   // (2 launches per stage: interior tiles, then the shock/boundary tiles)
   bool profile = false;
-  static constexpr int kEv = 16;
+  // 4 k .. 4 k + 3: around the two flux launches of stage k; 16 + k: start of stage k's
+  // stage update; 20: step start; 21: step end (main stream)
+  static constexpr int kEv = 22;
   cudaGraphNode_t ev_nodes[kEv] = {};
   cudaEvent_t cap_ev[kEv] = {};
   std::vector<cudaEvent_t> prof_ev;  // kEv per profiled step
@@ -214,6 +216,7 @@ int enqueue_step(hymor_ctx* ctx, bool with_events) {
     return 0;
   };
   CU(cudaMemsetAsync(d.scal + kCmax, 0, 3 * sizeof(double), st));
+  TRY(ev(20));
   if (c.rk_variant == 0) {
     // Third stream: the first fit reads only the shock points of S, which nothing before
     // the first jump kernel changes, so it runs beside the flow cells and the CFL.
@@ -231,9 +234,13 @@ int enqueue_step(hymor_ctx* ctx, bool with_events) {
     launch_sound_cmax(d, shock, sx);
     launch_cfl(d, sx);
     CU(cudaStreamWaitEvent(sx, ctx->fit_join, 0));
+    TRY(ev(16));
     launch_update_thermo(d, 0, 0, 0, st);
     for (int k = 0; k < 4; ++k) {
-      if (k > 0) launch_update_thermo(d, 1, wY[k - 1], wA[k - 1], st);
+      if (k > 0) {
+        TRY(ev(16 + k));
+        launch_update_thermo(d, 1, wY[k - 1], wA[k - 1], st);
+      }
       TRY(fork());
       launch_columns_bc(d, false, shock, wY[k], wA[k], 0, true, true, sx);
       TRY(ev(4 * k));
@@ -254,6 +261,7 @@ int enqueue_step(hymor_ctx* ctx, bool with_events) {
     launch_sound_cmax(d, shock, st);
     launch_cfl(d, st);
     launch_snapshot(d, st);
+    TRY(ev(16));
     launch_update_thermo(d, 0, 0, 0, st);
     launch_shock_bc(d, false, true, shock, 0.0, wA[0], 0, st);
     TRY(ev(0));
@@ -262,6 +270,7 @@ int enqueue_step(hymor_ctx* ctx, bool with_events) {
     TRY(ev(2));
     TRY(ev(3));
     for (int k = 1; k < 4; ++k) {
+      TRY(ev(16 + k));
       launch_classical_stage(d, wY[k - 1], st);
       launch_update_thermo(d, 5, 0, wA[k - 1], st);
       launch_shock_bc(d, false, false, shock, 0.0, wA[k], 0, st);
@@ -275,6 +284,7 @@ int enqueue_step(hymor_ctx* ctx, bool with_events) {
     launch_shock_bc(d, true, false, false, 0, 0, 1, st);
   }
   launch_fill_minrho(d, true, st);
+  TRY(ev(21));
   CU(cudaGetLastError());
   return 0;
 }
@@ -765,6 +775,34 @@ int hymor_profile_flux(hymor_ctx* ctx, int enable, float* total_ms, int32_t* lau
   ctx->prof_ev.clear();
   ctx->prof_steps = 0;
   ctx->profile = enable != 0;
+  return 0;
+}
+
+int hymor_profile_phases(hymor_ctx* ctx, float* ms) {
+  if (!ctx || !ms) return HYMOR_ERR_INVALID;
+  TRY(set_device(ctx));
+  CU(cudaStreamSynchronize(ctx->stream));
+  const size_t E = hymor_ctx_s::kEv;
+  for (int k = 0; k < 18; ++k) ms[k] = 0;
+  int steps = 0;
+  auto dt = [&](size_t s, int a, int b, float& acc) -> int {
+    float v = 0;
+    CU(cudaEventElapsedTime(&v, ctx->prof_ev[s + a], ctx->prof_ev[s + b]));
+    acc += v;
+    return 0;
+  };
+  for (size_t s = 0; s + E <= ctx->prof_ev.size(); s += E, ++steps) {
+    TRY(dt(s, 20, 16, ms[0]));
+    for (int k = 0; k < 4; ++k) {
+      TRY(dt(s, 16 + k, 4 * k, ms[1 + 4 * k]));          // stage update (+ fork)
+      TRY(dt(s, 4 * k, 4 * k + 1, ms[2 + 4 * k]));       // flux, interior tiles
+      TRY(dt(s, 4 * k + 1, 4 * k + 2, ms[3 + 4 * k]));   // wait for the shock/boundary kernels
+      TRY(dt(s, 4 * k + 2, 4 * k + 3, ms[4 + 4 * k]));   // flux, shock/boundary tiles
+    }
+    TRY(dt(s, 15, 21, ms[17]));
+  }
+  if (steps)
+    for (int k = 0; k < 18; ++k) ms[k] /= steps;
   return 0;
 }
 

@@ -35,6 +35,15 @@ constexpr int CX = TX + 1, CY = TY + 1, NCOR = CX * CY;
 constexpr int NLRF = (TX + 1) * TY;  // 256
 constexpr int NBTF = TX * (TY + 1);  // 279
 constexpr int kFluxThreads = 256;
+// Tile geometry of a 31 x TYV-cell flux tile (TYV warps, one per tile row).
+template <int TYV>
+struct TileGeo {
+  static constexpr int NH = HX * (TYV + 2);        // halo cells
+  static constexpr int NCOR = CX * (TYV + 1);      // corners
+  static constexpr int NLRF = (TX + 1) * TYV;      // lr faces
+  static constexpr int NBTF = TX * (TYV + 1);      // bt faces
+  static constexpr int THREADS = 32 * TYV;
+};
 // dynamic shared memory that leaves room for one flux block per SM (of 228 KB)
 constexpr size_t kFluxOneBlockSmem = 120 * 1024;
 
@@ -76,6 +85,11 @@ __global__ void __launch_bounds__(256) k_update_thermo(UpdArgs a) {
   for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < G; k += (long)gridDim.x * blockDim.x) {
     const int i = (int)(k % NI), j = (int)(k / NI);
     const bool interior = i >= 1 && i <= a.nchi && j >= 1 && j <= a.neta;
+    // Upstream of the shock band (interior rows >= sc + 3) nothing changes the stage array
+    // between the step's first update and its end (the flux is masked there and only the
+    // step-start / step-end fills write it), so p and T would be recomputed from the same
+    // values: the later stage updates skip those cells.
+    if (a.mode == 1 && a.shock && interior && j >= a.cell_idx[i - 1] + 3) continue;
     double r, u, v, e;
     const Cons& tgt = (a.mode == 2 || a.mode == 3) ? a.S : a.Y;
     if (a.mode == 0) {
@@ -982,37 +996,38 @@ __global__ void k_classify_tiles(const int* __restrict__ cell_idx, int* lists, i
     inner = inner && (j0 + TY + 1 < scmin);
   }
   const int cls = inner ? 0 : 1;
-  const int slot = atomicAdd(&lists[cls], 1);
-  lists[2 + cls * ntiles + slot] = t;
+  lists[2 + cls * ntiles + atomicAdd(&lists[cls], 1)] = t;
 }
 
-// One 31 x 8-cell tile (bx, by) of the residual; every thread of the block takes part.
-template <bool AXI, bool SUTH>
+// One 31 x TYV-cell tile (bx, by) of the residual, TYV warps (one per tile row); every
+// thread of the block takes part.
+template <bool AXI, bool SUTH, int TYV>
 __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, double* sm) {
+  using G = TileGeo<TYV>;
   double* s_r = sm;
-  double* s_u = s_r + NH;   // u = rho_u / rho
-  double* s_v = s_u + NH;
-  double* s_ru = s_v + NH;
-  double* s_rv = s_ru + NH;
-  double* s_rE = s_rv + NH;
-  double* s_p = s_rE + NH;
-  double* s_T = s_p + NH;
-  double* s_uc = s_T + NH;
-  double* s_vc = s_uc + NCOR;
-  double* s_Tc = s_vc + NCOR;
-  double* f_lr = s_Tc + NCOR;                // 4 x NLRF
-  double* f_bt = f_lr + 4 * NLRF;            // 4 x NBTF
-  double* t_lr = f_bt + 4 * NBTF;            // AXI hoop stress on faces
-  double* t_bt = t_lr + (AXI ? NLRF : 0);
+  double* s_u = s_r + G::NH;   // u = rho_u / rho
+  double* s_v = s_u + G::NH;
+  double* s_ru = s_v + G::NH;
+  double* s_rv = s_ru + G::NH;
+  double* s_rE = s_rv + G::NH;
+  double* s_p = s_rE + G::NH;
+  double* s_T = s_p + G::NH;
+  double* s_uc = s_T + G::NH;
+  double* s_vc = s_uc + G::NCOR;
+  double* s_Tc = s_vc + G::NCOR;
+  double* f_lr = s_Tc + G::NCOR;                // 4 x G::NLRF
+  double* f_bt = f_lr + 4 * G::NLRF;            // 4 x G::NBTF
+  double* t_lr = f_bt + 4 * G::NBTF;            // AXI hoop stress on faces
+  double* t_bt = t_lr + (AXI ? G::NLRF : 0);
 
   const int nchi = a.nchi, neta = a.neta;
-  const int i0 = bx * TX, j0 = by * TY;  // first interior cell (0-based)
+  const int i0 = bx * TX, j0 = by * TYV;  // first interior cell (0-based)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   if (a.tile_class >= 0 && !a.list) {
-    // the halo (ghosted columns i0..i0+TX+1, rows j0..j0+TY+1) avoids every ghost cell and
+    // the halo (ghosted columns i0..i0+TX+1, rows j0..j0+TYV+1) avoids every ghost cell and
     // stays below the shocked rows sc..sc+2 of its columns -> independent of shock/BC work
-    bool inner = i0 >= 1 && i0 + TX + 1 <= nchi && j0 >= 1 && j0 + TY + 1 <= neta;
+    bool inner = i0 >= 1 && i0 + TX + 1 <= nchi && j0 >= 1 && j0 + TYV + 1 <= neta;
     if (a.shock) {
       int scmin = 0x7fffffff;
       for (int c = lane; c < TX + 2; c += 32) {
@@ -1021,7 +1036,7 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, dou
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) scmin = min(scmin, __shfl_xor_sync(0xffffffffu, scmin, o));
-      inner = inner && (j0 + TY + 1 < scmin);
+      inner = inner && (j0 + TYV + 1 < scmin);
     }
     if (inner != (a.tile_class == 0)) return;
   }
@@ -1043,7 +1058,7 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, dou
   }
 
   // (1) halo cells: ghosted (i0 + hx, j0 + hy)
-  for (int h = tid; h < NH; h += kFluxThreads) {
+  for (int h = tid; h < G::NH; h += G::THREADS) {
     const int hx = h % HX, hy = h / HX;
     const int gi = i0 + hx, gj = j0 + hy;
     if (gi <= nchi + 1 && gj <= neta + 1) {
@@ -1059,7 +1074,7 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, dou
   }
   __syncthreads();
   // (2) corner averages (VISCOUS_FLUX.jl:67-70, 184-185)
-  for (int cidx = tid; cidx < NCOR; cidx += kFluxThreads) {
+  for (int cidx = tid; cidx < G::NCOR; cidx += G::THREADS) {
     const int cx = cidx % CX, cy = cidx / CX;
     if (i0 + cx <= nchi && j0 + cy <= neta) {
       const int h00 = cx + cy * HX, h10 = h00 + 1, h01 = h00 + HX, h11 = h01 + 1;
@@ -1123,14 +1138,14 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, dou
       const double qn = kpr * dT_dn;
       const int o = fx + fy * (TX + 1);
       f_lr[o] = m2 * Ah;
-      f_lr[NLRF + o] = fma(Su, Vn, fma(Sp, nx, tx)) * Ah;
-      f_lr[2 * NLRF + o] = fma(Sv, Vn, fma(Sp, ny, ty)) * Ah;
-      f_lr[3 * NLRF + o] = fma(SE + Sp, Vn, w + qn) * Ah;
+      f_lr[G::NLRF + o] = fma(Su, Vn, fma(Sp, nx, tx)) * Ah;
+      f_lr[2 * G::NLRF + o] = fma(Sv, Vn, fma(Sp, ny, ty)) * Ah;
+      f_lr[3 * G::NLRF + o] = fma(SE + Sp, Vn, w + qn) * Ah;
       if (AXI) t_lr[o] = (0.5 * mu_f) * fma(-2.0 / 3.0, div, 2 * uf * rx);
     }
   }
-  // (3b) bt faces: TX x (TY + 1)
-  for (int b = tid; b < (TX + 1) * (TY + 1); b += kFluxThreads) {
+  // (3b) bt faces: TX x (TYV + 1)
+  for (int b = tid; b < (TX + 1) * (TYV + 1); b += G::THREADS) {
     const int fx = b & 31, fy = b >> 5;
     if (fx >= TX) continue;
     const int gi = i0 + fx, gj = j0 + fy;  // face (gi, gj): between ghosted (gi+1, gj), (gi+1, gj+1)
@@ -1177,9 +1192,9 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, dou
       const double qn = kpr * dT_dn;
       const int o = fx + fy * TX;
       f_bt[o] = m2 * Ah;
-      f_bt[NBTF + o] = fma(Su, Vn, fma(Sp, nx, -tx)) * Ah;
-      f_bt[2 * NBTF + o] = fma(Sv, Vn, fma(Sp, ny, -ty)) * Ah;
-      f_bt[3 * NBTF + o] = fma(SE + Sp, Vn, -(w + qn)) * Ah;
+      f_bt[G::NBTF + o] = fma(Su, Vn, fma(Sp, nx, -tx)) * Ah;
+      f_bt[2 * G::NBTF + o] = fma(Sv, Vn, fma(Sp, ny, -ty)) * Ah;
+      f_bt[3 * G::NBTF + o] = fma(SE + Sp, Vn, -(w + qn)) * Ah;
       if (AXI) t_bt[o] = (0.5 * mu_f) * fma(-2.0 / 3.0, div, 2 * uf * rx);
     }
   }
@@ -1197,8 +1212,8 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, dou
         const int s = cx + cy * TX, n = s + TX;
         const double rv = a.m.rvol[c];
         r0 = (f_lr[w] - f_lr[e] + f_bt[s] - f_bt[n]) * rv;
-        r1 = (f_lr[NLRF + w] - f_lr[NLRF + e] + f_bt[NBTF + s] - f_bt[NBTF + n]) * rv;
-        double v2 = f_lr[2 * NLRF + w] - f_lr[2 * NLRF + e] + f_bt[2 * NBTF + s] - f_bt[2 * NBTF + n];
+        r1 = (f_lr[G::NLRF + w] - f_lr[G::NLRF + e] + f_bt[G::NBTF + s] - f_bt[G::NBTF + n]) * rv;
+        double v2 = f_lr[2 * G::NLRF + w] - f_lr[2 * G::NLRF + e] + f_bt[2 * G::NBTF + s] - f_bt[2 * G::NBTF + n];
         if (AXI) {
           // FLUX_MOMENTUM_3D.jl:120-122: front/back pressure with sign(y) of the cell centre
           const double pc = s_p[(cx + 1) + (cy + 1) * HX];
@@ -1210,7 +1225,7 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, dou
           r1 -= tth * frcp(xcell);
         }
         r2 = v2 * rv;
-        r3 = (f_lr[3 * NLRF + w] - f_lr[3 * NLRF + e] + f_bt[3 * NBTF + s] - f_bt[3 * NBTF + n]) * rv;
+        r3 = (f_lr[3 * G::NLRF + w] - f_lr[3 * G::NLRF + e] + f_bt[3 * G::NBTF + s] - f_bt[3 * G::NBTF + n]) * rv;
       }
       a.o0[c] = r0; a.o1[c] = r1; a.o2[c] = r2; a.o3[c] = r3;
     }
@@ -1218,24 +1233,25 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, dou
 }
 
 // Tile grid (no list), or a persistent grid striding over the compact tile list of a class.
-template <bool AXI, bool SUTH>
-__global__ void __launch_bounds__(kFluxThreads, 4) k_flux(FluxArgs a) {
+template <bool AXI, bool SUTH, int TYV>
+__global__ void __launch_bounds__(32 * TYV, 32 / TYV) k_flux(FluxArgs a) {
   extern __shared__ double sm[];
   if (!a.list) {
-    flux_tile<AXI, SUTH>(a, blockIdx.x, blockIdx.y, sm);
+    flux_tile<AXI, SUTH, TYV>(a, blockIdx.x, blockIdx.y, sm);
     return;
   }
   const int n = *a.count;
   for (int k = blockIdx.x; k < n; k += gridDim.x) {
     const int t = a.list[k];
-    flux_tile<AXI, SUTH>(a, t % a.tiles_x, t / a.tiles_x, sm);
+    flux_tile<AXI, SUTH, TYV>(a, t % a.tiles_x, t / a.tiles_x, sm);
     __syncthreads();  // the next tile reuses the shared arrays
   }
 }
 
-template <bool AXI, bool SUTH>
+template <bool AXI, bool SUTH, int TYV = TY>
 size_t flux_smem() {
-  return sizeof(double) * (8 * NH + 3 * NCOR + 4 * NLRF + 4 * NBTF + (AXI ? NLRF + NBTF : 0));
+  using G = TileGeo<TYV>;
+  return sizeof(double) * (8 * G::NH + 3 * G::NCOR + 4 * G::NLRF + 4 * G::NBTF + (AXI ? G::NLRF + G::NBTF : 0));
 }
 
 // ---------------------------------------------------------------------------
@@ -1713,6 +1729,17 @@ void launch_classify_tiles(const DevCtx& d, cudaStream_t st) {
                                                    d.cfg.shock_enabled, d.cfg.shock_enabled && d.cfg.shock_feedback);
 }
 
+template <bool AXI, bool SUTH>
+void flux_launch(const FluxArgs& a, int tile_class, dim3 grid, const DevCtx& d, cudaStream_t st) {
+  if (tile_class == 1 && a.list) {
+    // the shock/boundary class: one block per SM (the shared-memory request admits no
+    // second), so that its few tiles spread over every SM instead of piling up on some
+    k_flux<AXI, SUTH, TY><<<d.sms, kFluxThreads, kFluxOneBlockSmem, st>>>(a);
+  } else {
+    k_flux<AXI, SUTH, TY><<<grid, kFluxThreads, flux_smem<AXI, SUTH>(), st>>>(a);
+  }
+}
+
 void launch_flux_class(const DevCtx& d, bool on_S, double* const out[4], int tile_class, cudaStream_t st) {
   FluxArgs a;
   a.tile_class = tile_class;
@@ -1735,24 +1762,19 @@ void launch_flux_class(const DevCtx& d, bool on_S, double* const out[4], int til
   a.shock = c.shock_enabled;
   a.mask = c.shock_enabled && c.shock_feedback;
   dim3 grid((d.nchi + TX - 1) / TX, (d.neta + TY - 1) / TY);
-  size_t extra = 0;
+  const bool axi = c.axisymmetric, suth = c.viscosity_model == 1;
   if (tile_class >= 0 && d.tiles) {
-    // the compact list of the class over a persistent grid: three blocks per SM for the
-    // interior tiles; one block per SM (the shared-memory request admits no second) for
-    // the few shock/boundary tiles, which would otherwise pile up on some SMs
+    // the compact list of the class over a persistent grid (the interior tiles at full
+    // occupancy)
     const int nt = flux_tiles(d);
     a.count = d.tiles + tile_class;
     a.list = d.tiles + 2 + tile_class * nt;
-    const bool axi = c.axisymmetric, suth = c.viscosity_model == 1;
-    grid = dim3(tile_class == 0 ? g_flux_blocks_per_sm[axi * 2 + suth] * d.sms : d.sms, 1);
-    if (tile_class == 1) extra = kFluxOneBlockSmem;
+    grid = dim3(g_flux_blocks_per_sm[axi * 2 + suth] * d.sms, 1);
   }
-  const bool axi = c.axisymmetric, suth = c.viscosity_model == 1;
-  auto smem = [&](size_t need) { return need > extra ? need : extra; };
-  if (!axi && !suth) k_flux<false, false><<<grid, kFluxThreads, smem(flux_smem<false, false>()), st>>>(a);
-  else if (axi && !suth) k_flux<true, false><<<grid, kFluxThreads, smem(flux_smem<true, false>()), st>>>(a);
-  else if (!axi && suth) k_flux<false, true><<<grid, kFluxThreads, smem(flux_smem<false, true>()), st>>>(a);
-  else k_flux<true, true><<<grid, kFluxThreads, smem(flux_smem<true, true>()), st>>>(a);
+  if (!axi && !suth) flux_launch<false, false>(a, tile_class, grid, d, st);
+  else if (axi && !suth) flux_launch<true, false>(a, tile_class, grid, d, st);
+  else if (!axi && suth) flux_launch<false, true>(a, tile_class, grid, d, st);
+  else flux_launch<true, true>(a, tile_class, grid, d, st);
 }
 
 void launch_flux(const DevCtx& d, bool on_S, double* const out[4], cudaStream_t st) {
@@ -1760,19 +1782,19 @@ void launch_flux(const DevCtx& d, bool on_S, double* const out[4], cudaStream_t 
 }
 
 void flux_kernel_setup() {
-  cudaFuncSetAttribute(k_flux<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxOneBlockSmem);
-  cudaFuncSetAttribute(k_flux<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxOneBlockSmem);
-  cudaFuncSetAttribute(k_flux<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxOneBlockSmem);
-  cudaFuncSetAttribute(k_flux<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxOneBlockSmem);
+  cudaFuncSetAttribute(k_flux<false, false, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxOneBlockSmem);
+  cudaFuncSetAttribute(k_flux<true, false, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxOneBlockSmem);
+  cudaFuncSetAttribute(k_flux<false, true, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxOneBlockSmem);
+  cudaFuncSetAttribute(k_flux<true, true, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxOneBlockSmem);
   auto occ = [](auto kern, size_t smem) {
     int b = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kFluxThreads, smem) != cudaSuccess || b < 1) b = 1;
     return b;
   };
-  g_flux_blocks_per_sm[0] = occ(k_flux<false, false>, flux_smem<false, false>());
-  g_flux_blocks_per_sm[1] = occ(k_flux<false, true>, flux_smem<false, true>());
-  g_flux_blocks_per_sm[2] = occ(k_flux<true, false>, flux_smem<true, false>());
-  g_flux_blocks_per_sm[3] = occ(k_flux<true, true>, flux_smem<true, true>());
+  g_flux_blocks_per_sm[0] = occ(k_flux<false, false, TY>, flux_smem<false, false>());
+  g_flux_blocks_per_sm[1] = occ(k_flux<false, true, TY>, flux_smem<false, true>());
+  g_flux_blocks_per_sm[2] = occ(k_flux<true, false, TY>, flux_smem<true, false>());
+  g_flux_blocks_per_sm[3] = occ(k_flux<true, true, TY>, flux_smem<true, true>());
   cudaFuncSetAttribute(k_spline_fit, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)sizeof(float) * kSplineArrays * spline_stride(4096));
 }
