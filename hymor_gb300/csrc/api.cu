@@ -180,12 +180,15 @@ void face_geometry(const hymor_config& c, const hymor_mesh& m, std::vector<doubl
     }
   for (long k = 0; k < N; ++k) rvol[k] = 1.0 / m.vol[k];
   gvis.assign(N, 0.0);
+  // max(4/3, gamma/Pr) / Re times the viscous CFL factor, over the volume once more: the
+  // viscous rate the CFL kernel adds to the convective one before dividing by the volume
+  const double kv = std::fmax(4.0 / 3.0, c.gamma / c.Pr) / c.Re;
   for (int j = 0; j < neta; ++j)
     for (int i = 0; i < nchi; ++i) {
       const long k = i + (long)j * nchi;
       const double Axi = 0.5 * (m.lr_a[i + (long)j * (nchi + 1)] + m.lr_a[i + 1 + (long)j * (nchi + 1)]);
       const double Aeta = 0.5 * (m.bt_a[i + (long)j * nchi] + m.bt_a[i + (long)(j + 1) * nchi]);
-      gvis[k] = 2 * (Axi * Axi + Aeta * Aeta) / m.vol[k];
+      gvis[k] = kv * (2 * (Axi * Axi + Aeta * Aeta) / m.vol[k]) / m.vol[k];
     }
 }
 
@@ -231,7 +234,9 @@ int enqueue_step(hymor_ctx* ctx, bool with_events) {
     // moved); then per stage the jump + boundary kernels beside the flux of the
     // interior tiles.
     TRY(fork());
-    launch_sound_cmax(d, shock, sx);
+    // with shock fitting the step recomputes the sound speed for the CFL maximum only
+    // (and the outflow_NRCBC lines); the full field is recomputed when next needed
+    launch_sound_cmax(d, shock, sx, true);
     launch_cfl(d, sx);
     CU(cudaStreamWaitEvent(sx, ctx->fit_join, 0));
     TRY(ev(16));
@@ -343,6 +348,12 @@ size_t state_pitch(size_t n) { return (n + 31) & ~size_t(31); }
 size_t header_doubles(size_t n) { return 4 * state_pitch(n) + kScalPitch + (n + 1) / 2; }
 size_t stage_bytes(int n) { return header_doubles(n) * sizeof(double); }
 
+// A step with shock fitting (Julia RK4 variant) computes the sound speed only where it
+// reads it (its maximum and the outflow_NRCBC lines): the full field is stale afterwards.
+void mark_sound_after_steps(hymor_ctx* ctx, int nsteps) {
+  if (nsteps > 0 && ctx->d.cfg.shock_enabled && ctx->d.cfg.rk_variant == 0) ctx->a_stale = true;
+}
+
 // Computes the persistent sound speed of S if set_state left it stale, unless the work
 // about to be enqueued recomputes it before reading it.
 void refresh_sound(hymor_ctx* ctx, bool recomputed_anyway) {
@@ -417,6 +428,18 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
     if ((r = upload(ctx, &p5, rxb.data(), rxb.size(), "1/x bt"))) return bail(r);
     if ((r = upload(ctx, &p6, gvis.data(), gvis.size(), "viscous CFL geometry"))) return bail(r);
     m.lrg = p1; m.btg = p2; m.rvol = p3; m.rx_lr = p4; m.rx_bt = p5; m.gvis = p6;
+    // cell centres transposed (row index fastest), for scans along a chi column
+    const int NI = cfg->nchi + 2, NJ = cfg->neta + 2;
+    std::vector<double> xt((size_t)NI * NJ), yt((size_t)NI * NJ);
+    for (int j = 0; j < NJ; ++j)
+      for (int i = 0; i < NI; ++i) {
+        xt[(size_t)i * NJ + j] = mesh->x_ext[i + (size_t)j * NI];
+        yt[(size_t)i * NJ + j] = mesh->y_ext[i + (size_t)j * NI];
+      }
+    double *p7 = nullptr, *p8 = nullptr;
+    if ((r = upload(ctx, &p7, xt.data(), xt.size(), "x centres")) || (r = upload(ctx, &p8, yt.data(), yt.size(), "y centres")))
+      return bail(r);
+    m.xt = p7; m.yt = p8;
   }
   auto cons = [&](Cons& q) -> int {
     TRY(dalloc(ctx, &q.rho, d.G)); TRY(dalloc(ctx, &q.ru, d.G));
@@ -460,6 +483,7 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
       (r = dalloc(ctx, &d.speed_x, d.nchi)) || (r = dalloc(ctx, &d.speed_y, d.nchi)) ||
       (r = dalloc(ctx, &d.rel, d.nchi)) || (r = dalloc(ctx, &d.spl, 17 * (long)d.nchi + 16)) ||
       (r = dalloc(ctx, &d.err, (long)kErrCount)) || (r = dalloc(ctx, &d.tiles, 2 + 2 * (long)flux_tiles(d))) ||
+      (r = dalloc(ctx, &d.ticket, 2L)) ||
       (r = dalloc(ctx, &d.cflw, d.NLR + d.NBT)))
     return bail(r);
   if (cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess || d.sms < 1)
@@ -637,6 +661,7 @@ int hymor_step(hymor_ctx* ctx, int nsteps) {
     }
     CU(cudaGraphLaunch(ctx->gexec, ctx->stream));
   }
+  mark_sound_after_steps(ctx, nsteps);
   return read_err(ctx);
 }
 
@@ -668,6 +693,7 @@ int hymor_bench_steps(hymor_ctx* ctx, int nsteps, uint64_t flush_bytes, float* m
     CU(cudaGraphLaunch(ctx->gexec, ctx->stream));
     CU(cudaEventRecord(ev[2 * s + 1], ctx->stream));
   }
+  mark_sound_after_steps(ctx, nsteps);
   CU(cudaStreamSynchronize(ctx->stream));
   double tot = 0;
   for (int s = 0; s < nsteps; ++s) {

@@ -39,7 +39,9 @@ struct DevMesh {
   const double* rvol;  // N
   const double* rx_lr;  // axisymmetric: (2 / Re) / x_face on lr faces (NLR)
   const double* rx_bt;  // axisymmetric: (2 / Re) / x_face on bt faces (NBT)
-  const double* gvis;   // 2 (A_xi^2 + A_eta^2) / vol per cell (viscous CFL rate, CFL_TIMESTEP.jl:110-113)
+  const double* gvis;   // kv 2 (A_xi^2 + A_eta^2) / vol^2 per cell, kv = max(4/3, gamma/Pr) / Re
+                        // (viscous CFL rate over the volume, CFL_TIMESTEP.jl:110-113)
+  const double *xt, *yt;  // x_ext, y_ext transposed: ghosted (i, j) at i * (Neta + 2) + j
 };
 
 struct Cons {

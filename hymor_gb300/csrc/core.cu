@@ -86,10 +86,10 @@ __global__ void __launch_bounds__(256) k_update_thermo(UpdArgs a) {
     const int i = (int)(k % NI), j = (int)(k / NI);
     const bool interior = i >= 1 && i <= a.nchi && j >= 1 && j <= a.neta;
     // Upstream of the shock band (interior rows >= sc + 3) nothing changes the stage array
-    // between the step's first update and its end (the flux is masked there and only the
-    // step-start / step-end fills write it), so p and T would be recomputed from the same
-    // values: the later stage updates skip those cells.
-    if (a.mode == 1 && a.shock && interior && j >= a.cell_idx[i - 1] + 3) continue;
+    // or the solution between the step's first update and its end (the flux is masked
+    // there and only the step-start / step-end fills write it, with Y = S), so p and T
+    // would be recomputed from the same values: the later updates skip those cells.
+    if ((a.mode == 1 || a.mode == 2) && a.shock && interior && j >= a.cell_idx[i - 1] + 3) continue;
     double r, u, v, e;
     const Cons& tgt = (a.mode == 2 || a.mode == 3) ? a.S : a.Y;
     if (a.mode == 0) {
@@ -1291,12 +1291,15 @@ __global__ void __launch_bounds__(256) k_flow_cells(FlowArgs A) {
   const double px = A.pS.x[i], py = A.pS.y[i];
   // nearest cell centre along the column; ties go to the smallest row, like the
   // reference's sequential scan with a strict comparison
+  // (squared distance rounded like the reference's unfused dx^2 + dy^2, so that the
+  // nearest row is the same one; the transposed centres make the loads coalesced)
   double best = INFINITY;
   int bj = 0x7fffffff;
+  const double* xc = A.m.xt + (long)(i + 1) * NJ;
+  const double* yc = A.m.yt + (long)(i + 1) * NJ;
   for (int j = 1 + lane; j <= neta; j += 32) {
-    const long k = gidx(i + 1, j, nchi);
-    const double dx = px - A.m.x_ext[k], dy = py - A.m.y_ext[k];
-    const double d = dx * dx + dy * dy;
+    const double dx = px - xc[j], dy = py - yc[j];
+    const double d = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
     if (d < best) { best = d; bj = j; }
   }
 #pragma unroll
@@ -1334,12 +1337,18 @@ __global__ void __launch_bounds__(256) k_flow_cells(FlowArgs A) {
 }
 
 // Sound speed of S, max |a| over every ghosted cell (CFL_TIMESTEP.jl:80).
+//   mode 0: max over the stored sound speed
+//   mode 1: recompute a = sqrt(gamma p / rho) everywhere, and its max
+//   mode 2: the max only, as sqrt(max gamma p / rho) (sqrt is monotone and correctly
+//           rounded, so this is the max of the square roots exactly), storing a only on
+//           the lines the outflow_NRCBC condition reads; the last block takes the root
 struct SoundArgs {
   Cons S;
   double* aS;
   double* scal;
+  unsigned* ticket;  // blocks done (mode 2), reset by the last one
   double gamma;
-  int nchi, neta, recompute, isothermal_eta0;
+  int nchi, neta, mode, isothermal_eta0, nrcbc;
 };
 
 __global__ void __launch_bounds__(256) k_sound_cmax(SoundArgs A) {
@@ -1353,21 +1362,28 @@ __global__ void __launch_bounds__(256) k_sound_cmax(SoundArgs A) {
   };
   auto pres = [&](long k) { return pres_r(k, frcp(A.S.rho[k])); };
   for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < G; k += (long)gridDim.x * blockDim.x) {
-    double a;
-    if (A.recompute) {
-      const int i = (int)(k % NI), j = (int)(k / NI);
-      double p;
-      const double ir = frcp(A.S.rho[k]);
-      if (j == 0 && A.isothermal_eta0)
-        p = 2 * pres(gidx(i, 1, A.nchi)) - pres(gidx(i, 2, A.nchi));
-      else
-        p = pres_r(k, ir);
-      a = sqrt(A.gamma * p * ir);
-      A.aS[k] = a;
-    } else {
-      a = A.aS[k];
+    if (A.mode == 0) {
+      mx = fmax(mx, fabs(A.aS[k]));
+      continue;
     }
-    mx = fmax(mx, fabs(a));
+    const int i = (int)(k % NI), j = (int)(k / NI);
+    double p;
+    const double ir = frcp(A.S.rho[k]);
+    if (j == 0 && A.isothermal_eta0)
+      p = 2 * pres(gidx(i, 1, A.nchi)) - pres(gidx(i, 2, A.nchi));
+    else
+      p = pres_r(k, ir);
+    const double c2 = A.gamma * p * ir;
+    if (A.mode == 1) {
+      const double a = sqrt(c2);
+      A.aS[k] = a;
+      mx = fmax(mx, fabs(a));
+    } else {
+      const bool nb = ((A.nrcbc & 1) && i == 1) || ((A.nrcbc & 2) && i == NI - 2) ||
+                      ((A.nrcbc & 4) && j == 1) || ((A.nrcbc & 8) && j == NJ - 2);
+      if (nb) A.aS[k] = sqrt(c2);
+      mx = fmax(mx, c2);
+    }
   }
   mx = warp_max(mx);
   __shared__ double red[32];
@@ -1376,7 +1392,18 @@ __global__ void __launch_bounds__(256) k_sound_cmax(SoundArgs A) {
   if (threadIdx.x < 32) {
     double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
     v = warp_max(v);
-    if (threadIdx.x == 0) atomic_max_nonneg(&A.scal[kCmax], v);
+    if (threadIdx.x == 0) {
+      atomic_max_nonneg(&A.scal[kCmax], v);
+      if (A.mode == 2) {
+        __threadfence();
+        if (atomicAdd(A.ticket, 1u) == gridDim.x - 1) {  // every block's maximum is in
+          unsigned long long* bits = reinterpret_cast<unsigned long long*>(&A.scal[kCmax]);
+          const double c2max = __longlong_as_double((long long)atomicAdd(bits, 0ull));
+          A.scal[kCmax] = sqrt(c2max);
+          *A.ticket = 0;
+        }
+      }
+    }
   }
 }
 
@@ -1396,7 +1423,7 @@ struct CflArgs {
   double* scal;
   double* lam_lr;   // face rates, lr then bt
   double* lam_bt;
-  double gamma, kv, suthS, Tinf_inv;   // kv = max(4/3, gamma/Pr) / Re
+  double gamma, suthS, Tinf_inv;
   int nchi, neta, shock, suth;
 };
 
@@ -1411,13 +1438,14 @@ __global__ void __launch_bounds__(256) k_cfl_faces(CflArgs A) {
       const int i = (int)(f % (nchi + 1)), j = (int)(f / (nchi + 1));
       L = gidx(i, j + 1, nchi);
       R = L + 1;
-      nx = A.m.lr_xn[f]; ny = A.m.lr_yn[f]; Af = A.m.lr_a[f];
+      // the flux kernel's geometry planes (n_x, n_y, A/2), one copy of the face data
+      nx = A.m.lrg[f]; ny = A.m.lrg[NLR + f]; Af = 2 * A.m.lrg[2 * NLR + f];
     } else {
       const long g = f - NLR;
       const int i = (int)(g % nchi), j = (int)(g / nchi);
       L = gidx(i + 1, j, nchi);
       R = L + (nchi + 2);
-      nx = A.m.bt_xn[g]; ny = A.m.bt_yn[g]; Af = A.m.bt_a[g];
+      nx = A.m.btg[g]; ny = A.m.btg[NBT + g]; Af = 2 * A.m.btg[2 * NBT + g];
     }
     const double rs = A.S.rho[L] + A.S.rho[R];
     const double Vn = fabs(fma(A.S.ru[L] + A.S.ru[R], nx, (A.S.rv[L] + A.S.rv[R]) * ny)) * frcp(rs);
@@ -1430,7 +1458,6 @@ __global__ void __launch_bounds__(256) k_cfl(CflArgs A) {
   const int nchi = A.nchi, neta = A.neta;
   const long N = (long)nchi * neta;
   double mlam = 0, mflux = 0;
-  const double kv = A.kv;
   for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N; c += (long)gridDim.x * blockDim.x) {
     const int i = (int)(c % nchi), j = (int)(c / nchi);
     const bool flow = !A.shock || (j + 1 < A.cell_idx[i]);
@@ -1440,14 +1467,14 @@ __global__ void __launch_bounds__(256) k_cfl(CflArgs A) {
       const long g = gidx(i + 1, j + 1, nchi);
       const double r = A.S.rho[g];
       const double ir = frcp(r);
-      double mu = 1.0;  // Re_flow = Re / mu* (UPDATE_CHEMISTRY_EQUILIBRIUM.jl:99-101); mu* = 1 for CPG
-      if (A.suth) {
+      // viscous rate over the volume: gvis carries max(4/3, gamma/Pr) / Re and 1/vol^2
+      double lam_v = A.m.gvis[c] * ir;
+      if (A.suth) {  // Re_flow = Re / mu* (UPDATE_CHEMISTRY_EQUILIBRIUM.jl:99-101); mu* = 1 for CPG
         const double e = fma(-0.5, fma(A.S.ru[g], A.S.ru[g], A.S.rv[g] * A.S.rv[g]) * ir, A.S.rE[g]) * ir;
         const double Ts = e * A.Tinf_inv;
-        mu = Ts * sqrt(Ts) * (1 + A.suthS) * frcp(Ts + A.suthS);
+        lam_v *= Ts * sqrt(Ts) * (1 + A.suthS) * frcp(Ts + A.suthS);
       }
-      const double lam_v = kv * A.m.gvis[c] * ir * mu;
-      mlam = fmax(mlam, (lam_c + lam_v) * A.m.rvol[c]);
+      mlam = fmax(mlam, fma(lam_c, A.m.rvol[c], lam_v));
       const double t_u = (fabs(A.SF2[c]) + fabs(A.SF1[c])) * ir;
       const double t_r = fabs(A.SF0[c] * ir);
       const double t_E = fabs(A.SF3[c] * frcp(A.S.rE[g]));
@@ -1485,6 +1512,7 @@ struct FillArgs {
   const int* cell_idx;
   double* scal;
   unsigned* err;
+  unsigned* ticket;  // blocks done; the last one advances t (every block has read t by then)
   int advance;
 };
 
@@ -1520,9 +1548,18 @@ __global__ void __launch_bounds__(256) k_fill_minrho(FillArgs A) {
     }
   }
   if (limited) atomicAdd(&A.err[kRhoLimited], limited);
+  if (A.advance) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      if (atomicAdd(A.ticket, 1u) == gridDim.x - 1) {
+        A.scal[kT] = A.scal[kT] + A.scal[kDt];
+        *A.ticket = 0;
+      }
+    }
+  }
 }
 
-__global__ void k_advance_time(double* scal) { scal[kT] = scal[kT] + scal[kDt]; }
 
 // Classical RK4 helpers (value-semantics stages of the MATLAB twin).
 struct SnapArgs {
@@ -1811,15 +1848,18 @@ void launch_flow_cells(const DevCtx& d, cudaStream_t st) {
   k_flow_cells<<<(d.nchi * 32 + 255) / 256, 256, 0, st>>>(A);
 }
 
-void launch_sound_cmax(const DevCtx& d, bool recompute, cudaStream_t st) {
+void launch_sound_cmax(const DevCtx& d, bool recompute, cudaStream_t st, bool max_only) {
   SoundArgs A;
   A.S = d.S;
   A.aS = d.aS;
   A.scal = d.scal;
+  A.ticket = d.ticket;
   A.gamma = d.cfg.gamma;
   A.nchi = d.nchi;
   A.neta = d.neta;
-  A.recompute = recompute;
+  A.mode = recompute ? (max_only ? 2 : 1) : 0;
+  A.nrcbc = (d.cfg.bc_chi0 == HYMOR_BC_OUTFLOW_NRCBC) | ((d.cfg.bc_chi1 == HYMOR_BC_OUTFLOW_NRCBC) << 1) |
+            ((d.cfg.bc_eta0 == HYMOR_BC_OUTFLOW_NRCBC) << 2) | ((d.cfg.bc_eta1 == HYMOR_BC_OUTFLOW_NRCBC) << 3);
   A.isothermal_eta0 = d.cfg.bc_eta0 == HYMOR_BC_NO_SLIP_ISOTHERMAL;
   k_sound_cmax<<<grid_for(d.G, 256), 256, 0, st>>>(A);
 }
@@ -1832,7 +1872,6 @@ void launch_cfl(const DevCtx& d, cudaStream_t st) {
   A.cell_idx = d.cell_idx;
   A.scal = d.scal;
   A.gamma = d.cfg.gamma;
-  A.kv = std::fmax(4.0 / 3.0, d.cfg.gamma / d.cfg.Pr) / d.cfg.Re;
   A.suthS = d.cfg.sutherland_S;
   A.Tinf_inv = d.cfg.energy_factor / d.cfg.cv;
   A.suth = d.cfg.viscosity_model == 1;
@@ -1854,9 +1893,9 @@ void launch_fill_minrho(const DevCtx& d, bool advance_time, cudaStream_t st) {
   A.cell_idx = d.cell_idx;
   A.scal = d.scal;
   A.err = d.err;
-  A.advance = 0;
+  A.ticket = d.ticket + 1;
+  A.advance = advance_time;
   k_fill_minrho<<<grid_for(d.G, 256), 256, 0, st>>>(A);
-  if (advance_time) k_advance_time<<<1, 1, 0, st>>>(d.scal);
 }
 
 void launch_snapshot(const DevCtx& d, cudaStream_t st) {

@@ -27,6 +27,7 @@ struct DevCtx {
   double* scal;    // Scalar block
   unsigned* err;   // ErrWord block
   int* tiles;      // flux tile lists of the RK step (launch_classify_tiles)
+  unsigned* ticket;  // block counters: [0] k_sound_cmax (mode 2), [1] k_fill_minrho
   // Jacobian
   double* coef;    // N * 144 stencil blocks (or null)
   double* jwork;   // linearisation workspace
@@ -61,7 +62,8 @@ int flux_tiles(const DevCtx& d);
 // UPDATE_FLOW_CELLS part 1: detect shocked cells, upstream fill, extrapolation (on S).
 void launch_flow_cells(const DevCtx& d, cudaStream_t st);
 // Sound speed of S (recompute) and max|a| into scal[kCmax]; recompute=false only reduces aS.
-void launch_sound_cmax(const DevCtx& d, bool recompute, cudaStream_t st);
+// max_only (with recompute): the max, and a only on the lines outflow_NRCBC reads.
+void launch_sound_cmax(const DevCtx& d, bool recompute, cudaStream_t st, bool max_only = false);
 // CFL maxima and dt (scal[kDt]).
 void launch_cfl(const DevCtx& d, cudaStream_t st);
 // Step end: upstream fill + MIN_RHO on S, t += dt.
