@@ -617,8 +617,8 @@ __device__ __forceinline__ void block_max_f32(float (&v)[K], float* red) {
 // every array starts on a 16-byte boundary).
 __host__ __device__ inline int spline_stride(int n) { return (n - 2 + 3) & ~3; }
 constexpr int kSplineArrays = 14;
-// 16 warps: enough to keep the FP64 pipes of the SM busy in the parallel phases, and
-// 128 registers per thread for the prefetched serial sweeps
+// 32 warps: the parallel FP64 phases (residual, corrections, fitted values) spread over
+// every warp of the SM; the serial parts use one or two warps
 constexpr int kSplineThreads = 1024;
 
 __global__ void __launch_bounds__(kSplineThreads) k_spline_fit(SplineArgs A) {
