@@ -249,7 +249,9 @@ int enqueue_step(hymor_ctx* ctx, bool with_events) {
       TRY(fork());
       launch_columns_bc(d, false, shock, wY[k], wA[k], 0, true, true, sx);
       TRY(ev(4 * k));
-      launch_flux_class(d, false, F, 0, st);
+      // at the first stage the CFL chain and the first fit run beside the interior flux as
+      // well: it leaves them one block slot per SM
+      launch_flux_class(d, false, F, 0, st, k == 0 ? 1 : 0);
       TRY(ev(4 * k + 1));
       TRY(join());
       // next fit (stage k+1 on Y, or the step-end fit on S) overlaps this stage's remaining work
@@ -347,6 +349,23 @@ constexpr size_t kScalPitch = 32;
 size_t state_pitch(size_t n) { return (n + 31) & ~size_t(31); }
 size_t header_doubles(size_t n) { return 4 * state_pitch(n) + kScalPitch + (n + 1) / 2; }
 size_t stage_bytes(int n) { return header_doubles(n) * sizeof(double); }
+
+// The stored flux s["flux"] is no longer all zero: a step graph captured while it was
+// (whose CFL kernel skips the stored-flux term) is dropped and captured again.
+void stored_flux_written(hymor_ctx* ctx) {
+  if (!ctx->d.sf_zero) return;
+  ctx->d.sf_zero = 0;
+  if (ctx->gexec) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaGraphExecDestroy(ctx->gexec);
+    ctx->gexec = nullptr;
+  }
+  if (ctx->graph) {
+    cudaGraphDestroy(ctx->graph);
+    ctx->graph = nullptr;
+  }
+  for (auto& n : ctx->ev_nodes) n = nullptr;
+}
 
 // A step with shock fitting (Julia RK4 variant) computes the sound speed only where it
 // reads it (its maximum and the outflow_NRCBC lines): the full field is stale afterwards.
@@ -490,6 +509,7 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
     return bail(fail(ctx, HYMOR_ERR_CUDA, "multiprocessor count"));
   d.coef = nullptr;
   d.jwork = nullptr;
+  d.sf_zero = 1;  // the flux arrays are allocated zeroed
   for (int k = 0; k < hymor_ctx_s::kEv; ++k)
     if (cudaEventCreate(&ctx->cap_ev[k]) != cudaSuccess) return bail(fail(ctx, HYMOR_ERR_CUDA, "event"));
   for (int k = 0; k < 8; ++k)  // 5 forks and 5 joins per step
@@ -627,6 +647,7 @@ int hymor_residual(hymor_ctx* ctx, double* flux) {
   launch_shock_bc(d, true, false, false, 0, 0, 1, st);
   double* const SF[4] = {d.SF[0], d.SF[1], d.SF[2], d.SF[3]};
   launch_flux(d, true, SF, st);
+  stored_flux_written(ctx);
   CU(cudaGetLastError());
   if (flux)
     for (int v = 0; v < 4; ++v)
@@ -639,6 +660,7 @@ int hymor_set_flux(hymor_ctx* ctx, const double* flux) {
   TRY(set_device(ctx));
   for (int v = 0; v < 4; ++v)
     CU(cudaMemcpyAsync(ctx->d.SF[v], flux + v * ctx->d.N, ctx->d.N * 8, cudaMemcpyHostToDevice, ctx->stream));
+  stored_flux_written(ctx);
   CU(cudaStreamSynchronize(ctx->stream));
   return 0;
 }

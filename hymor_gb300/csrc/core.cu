@@ -1425,6 +1425,7 @@ struct CflArgs {
   double* lam_bt;
   double gamma, suthS, Tinf_inv;
   int nchi, neta, shock, suth;
+  int sf_zero;      // the stored flux is zero everywhere: its dt term is +inf, skip it
 };
 
 __global__ void __launch_bounds__(256) k_cfl_faces(CflArgs A) {
@@ -1475,10 +1476,12 @@ __global__ void __launch_bounds__(256) k_cfl(CflArgs A) {
         lam_v *= Ts * sqrt(Ts) * (1 + A.suthS) * frcp(Ts + A.suthS);
       }
       mlam = fmax(mlam, fma(lam_c, A.m.rvol[c], lam_v));
-      const double t_u = (fabs(A.SF2[c]) + fabs(A.SF1[c])) * ir;
-      const double t_r = fabs(A.SF0[c] * ir);
-      const double t_E = fabs(A.SF3[c] * frcp(A.S.rE[g]));
-      mflux = fmax(mflux, fmax(t_u, fmax(t_r, t_E)));
+      if (!A.sf_zero) {
+        const double t_u = (fabs(A.SF2[c]) + fabs(A.SF1[c])) * ir;
+        const double t_r = fabs(A.SF0[c] * ir);
+        const double t_E = fabs(A.SF3[c] * frcp(A.S.rE[g]));
+        mflux = fmax(mflux, fmax(t_u, fmax(t_r, t_E)));
+      }
     }
   }
   mlam = warp_max(mlam);
@@ -1777,7 +1780,8 @@ void flux_launch(const FluxArgs& a, int tile_class, dim3 grid, const DevCtx& d, 
   }
 }
 
-void launch_flux_class(const DevCtx& d, bool on_S, double* const out[4], int tile_class, cudaStream_t st) {
+void launch_flux_class(const DevCtx& d, bool on_S, double* const out[4], int tile_class, cudaStream_t st,
+                       int spare) {
   FluxArgs a;
   a.tile_class = tile_class;
   a.list = nullptr;
@@ -1806,7 +1810,8 @@ void launch_flux_class(const DevCtx& d, bool on_S, double* const out[4], int til
     const int nt = flux_tiles(d);
     a.count = d.tiles + tile_class;
     a.list = d.tiles + 2 + tile_class * nt;
-    grid = dim3(g_flux_blocks_per_sm[axi * 2 + suth] * d.sms, 1);
+    const int b = g_flux_blocks_per_sm[axi * 2 + suth];
+    grid = dim3((b > spare + 1 ? b - spare : 1) * d.sms, 1);
   }
   if (!axi && !suth) flux_launch<false, false>(a, tile_class, grid, d, st);
   else if (axi && !suth) flux_launch<true, false>(a, tile_class, grid, d, st);
@@ -1880,6 +1885,7 @@ void launch_cfl(const DevCtx& d, cudaStream_t st) {
   A.shock = d.cfg.shock_enabled;
   A.lam_lr = d.cflw;
   A.lam_bt = d.cflw + d.NLR;
+  A.sf_zero = d.sf_zero;
   k_cfl_faces<<<grid_for(d.NLR + d.NBT, 256), 256, 0, st>>>(A);
   k_cfl<<<grid_for(d.N, 256), 256, 0, st>>>(A);
   k_cfl_final<<<1, 1, 0, st>>>(d.scal, d.cfg.CFL, d.cfg.max_dt);

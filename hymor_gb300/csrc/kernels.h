@@ -19,6 +19,7 @@ struct DevCtx {
   double* aY;      // ghosted sound speed of the stage array (edge-adjacent lines only)
   double* F[4];    // stage flux
   double* SF[4];   // persistent flux of S (s["flux"])
+  int sf_zero;     // SF is still all zero (nothing has written it since creation)
   ShockPts Sp, Yp, Ycp;  // shock points of S, Y and the classical snapshot
   int* cell_idx;   // 1-based shocked rows (Nchi)
   double *beta, *speed_x, *speed_y, *rel;  // Nchi
@@ -55,7 +56,9 @@ void launch_flux(const DevCtx& d, bool on_S, double* const out[4], cudaStream_t 
 // tile_class 0: only tiles whose halo no shock/BC kernel writes; 1: the other tiles.
 // With the step's tile lists (d.tiles) each class runs over its compact list, and tiles
 // wholly above the shock are not evaluated (their flux is never read by the stage update).
-void launch_flux_class(const DevCtx& d, bool on_S, double* const out[4], int tile_class, cudaStream_t st);
+// spare: resident block slots per SM the persistent interior-tile grid leaves to other streams
+void launch_flux_class(const DevCtx& d, bool on_S, double* const out[4], int tile_class, cudaStream_t st,
+                       int spare = 0);
 // Classifies the flux tiles of the current shocked rows into d.tiles.
 void launch_classify_tiles(const DevCtx& d, cudaStream_t st);
 int flux_tiles(const DevCtx& d);

@@ -110,6 +110,22 @@ def test_cfl_timestep_parity(require_gpu):
     assert abs(S.CFL_TIMESTEP(sol) - orc.cfl()) < 1e-14 * orc.cfl()
 
 
+def test_stored_flux_enters_cfl_and_steps(require_gpu):
+    """The stored flux s["flux"] (set by PDE on the solution) enters CFL_TIMESTEP's dt2
+    term: steps taken before and after it is first written match the oracle (the step
+    graph captured while it was zero is captured again)."""
+    cfg = C.cylinder_config(40, 30)
+    cs, sol, orc = both(cfg)
+    S.ADVECT_FLOW(sol, 2)
+    orc.advect(2)
+    S.PDE(sol)
+    orc.residual()
+    assert abs(S.CFL_TIMESTEP(sol) - orc.cfl()) < 1e-13 * orc.cfl()
+    S.ADVECT_FLOW(sol, 3)
+    orc.advect(3)
+    compare_state(sol, orc, 1e-11)
+
+
 @pytest.mark.slow
 def test_cylinder_2000_steps_parity(require_gpu):
     """The 100 x 80 shock-fitted cylinder marched 2000 RK4 steps at CFL 0.5: residual and
