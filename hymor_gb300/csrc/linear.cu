@@ -9,7 +9,13 @@
 #include <cmath>
 #include <vector>
 
+#include <cooperative_groups.h>
+
+#include <algorithm>
+
 #include "kernels.h"
+
+namespace cg = cooperative_groups;
 
 namespace hymor {
 DevCtx& ctx_dev(hymor_ctx* c);
@@ -136,7 +142,8 @@ struct MvArgs {
   int k, transpose;
 };
 
-__global__ void __launch_bounds__(kMvThreads) k_matvec(MvArgs a) {
+// y = scale * A x (or A^T x) for the cells of this thread (grid-stride), acc += c_acc y.
+__device__ __forceinline__ void matvec_cells(const MvArgs& a) {
   const long N = a.N;
   const long n4 = 4 * N;
   for (long m = blockIdx.x * (long)blockDim.x + threadIdx.x; m < N; m += (long)gridDim.x * blockDim.x) {
@@ -196,6 +203,34 @@ __global__ void __launch_bounds__(kMvThreads) k_matvec(MvArgs a) {
         }
       }
     }
+  }
+}
+
+__global__ void __launch_bounds__(kMvThreads) k_matvec(MvArgs a) { matvec_cells(a); }
+
+// The whole Taylor propagation in one cooperative launch: the blocks are co-resident
+// (cudaLaunchCooperativeKernel) and meet at a grid barrier after every matvec, instead of
+// one kernel per matvec. Same per-cell arithmetic, in the same order, as launch_expm.
+__global__ void __launch_bounds__(kMvThreads) k_expm_coop(MvArgs base, int nsteps, int order, double* v, double* t1,
+                                                          double* t2, double* vout) {
+  cg::grid_group grid = cg::this_grid();
+  const long n = 4 * base.N * (long)base.k;
+  for (int s = 0; s < nsteps; ++s) {
+    const double* src = v;
+    long fact = 1;
+    for (int j = 1; j <= order; ++j) {
+      fact *= j;
+      MvArgs a = base;
+      a.X = src;
+      a.Y = (j % 2) ? t1 : t2;
+      a.acc = vout;
+      a.c_acc = 1.0 / (double)fact;
+      matvec_cells(a);
+      grid.sync();
+      src = a.Y;
+    }
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) v[q] = vout[q];
+    grid.sync();
   }
 }
 
@@ -451,21 +486,13 @@ int cuda_check(hymor_ctx* ctx, cudaError_t e) {
   return 0;
 }
 
-// Replayed propagations: the nsteps * (order + 1) launches of one propagation are captured
-// once into a CUDA graph over four fixed context buffers (v, two Taylor terms, vout); a
-// call copies its input into v and vout, launches the graph and copies vout out. This
-// removes the per-launch overhead that dominates small grids (a 200 x 100 stencil matvec is
-// ~5 us of FP64 work).
-struct ExpmGraph {
-  cudaGraphExec_t exec = nullptr;
-  int k = 0, nsteps = 0, order = 0, transpose = 0;
-  double dt = 0;
-  double* buf = nullptr;
-};
+// Propagations of more than a few launches run as one cooperative kernel (k_expm_coop)
+// over four context buffers (v, two Taylor terms, vout): a call copies its input into v
+// and vout, launches once and copies vout out. This removes the per-launch overhead that
+// dominates small grids (a 200 x 100 stencil matvec is ~5 us of FP64 work).
 struct ExpmCache {
   double* buf = nullptr;
   long cap = 0;  // doubles
-  std::vector<ExpmGraph> graphs;
 };
 struct KrylovScratch {
   double* partial = nullptr;
@@ -486,11 +513,10 @@ LinearState& linear_state(hymor_ctx* ctx) {
   return *static_cast<LinearState*>(slot);
 }
 ExpmCache& expm_cache(hymor_ctx* ctx) { return linear_state(ctx).expm; }
-constexpr int kExpmGraphMinLaunches = 16;
-constexpr size_t kExpmGraphCacheSize = 4;
+constexpr int kExpmCoopMinLaunches = 16;
 
-int expm_via_graph(hymor_ctx* ctx, int k, double dt, int nsteps, int order, const double* dX, double* dY,
-                   int transpose) {
+int expm_cooperative(hymor_ctx* ctx, int k, double dt, int nsteps, int order, const double* dX, double* dY,
+                     int transpose) {
   DevCtx& d = ctx_dev(ctx);
   cudaStream_t st = ctx_stream(ctx);
   ExpmCache& c = expm_cache(ctx);
@@ -498,8 +524,6 @@ int expm_via_graph(hymor_ctx* ctx, int k, double dt, int nsteps, int order, cons
   int r;
   if (4 * n > c.cap) {
     if ((r = cuda_check(ctx, cudaStreamSynchronize(st)))) return r;
-    for (auto& g : c.graphs) cudaGraphExecDestroy(g.exec);
-    c.graphs.clear();
     if (c.buf) cudaFree(c.buf);
     c.buf = nullptr;
     c.cap = 0;
@@ -512,32 +536,28 @@ int expm_via_graph(hymor_ctx* ctx, int k, double dt, int nsteps, int order, cons
   double* t1 = c.buf + n;
   double* t2 = c.buf + 2 * n;
   double* vout = c.buf + 3 * n;
-  ExpmGraph* g = nullptr;
-  for (auto& e : c.graphs)
-    if (e.k == k && e.nsteps == nsteps && e.order == order && e.transpose == transpose && e.dt == dt && e.buf == c.buf)
-      g = &e;
-  if (!g) {
-    if (c.graphs.size() >= kExpmGraphCacheSize) {
-      if ((r = cuda_check(ctx, cudaStreamSynchronize(st)))) return r;
-      cudaGraphExecDestroy(c.graphs.front().exec);
-      c.graphs.erase(c.graphs.begin());
-    }
-    cudaGraph_t graph = nullptr;
-    if ((r = cuda_check(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal)))) return r;
-    launch_expm_body(d, k, dt, nsteps, order, v, t1, t2, vout, transpose, st);
-    const cudaError_t e = cudaStreamEndCapture(st, &graph);
-    if ((r = cuda_check(ctx, e))) return r;
-    ExpmGraph ng;
-    ng.k = k; ng.nsteps = nsteps; ng.order = order; ng.transpose = transpose; ng.dt = dt; ng.buf = c.buf;
-    r = cuda_check(ctx, cudaGraphInstantiate(&ng.exec, graph, 0));
-    cudaGraphDestroy(graph);
-    if (r) return r;
-    c.graphs.push_back(ng);
-    g = &c.graphs.back();
-  }
+  static int blocks_per_sm = 0;  // co-resident blocks of k_expm_coop (same on every GB300)
+  if (!blocks_per_sm &&
+      (r = cuda_check(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_expm_coop, kMvThreads, 0))))
+    return r;
+  const long want = (d.N + kMvThreads - 1) / kMvThreads;
+  const int grid = (int)std::min<long>(want, (long)blocks_per_sm * d.sms);
+  MvArgs base;
+  base.coef = d.coef;
+  base.w = make_wrap(d.cfg);
+  base.N = d.N;
+  base.k = k;
+  base.transpose = transpose;
+  base.scale = dt;
+  base.X = nullptr;
+  base.Y = nullptr;
+  base.acc = nullptr;
+  base.c_acc = 0;
   if ((r = cuda_check(ctx, cudaMemcpyAsync(v, dX, sizeof(double) * n, cudaMemcpyDeviceToDevice, st)))) return r;
   if ((r = cuda_check(ctx, cudaMemcpyAsync(vout, dX, sizeof(double) * n, cudaMemcpyDeviceToDevice, st)))) return r;
-  if ((r = cuda_check(ctx, cudaGraphLaunch(g->exec, st)))) return r;
+  void* args[] = {&base, &nsteps, &order, &v, &t1, &t2, &vout};
+  if ((r = cuda_check(ctx, cudaLaunchCooperativeKernel((const void*)k_expm_coop, grid, kMvThreads, args, 0, st))))
+    return r;
   return cuda_check(ctx, cudaMemcpyAsync(dY, vout, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
 }
 }  // namespace
@@ -547,7 +567,6 @@ namespace hymor {
 void linear_state_release(void* p) {
   if (!p) return;
   LinearState* s = static_cast<LinearState*>(p);
-  for (auto& g : s->expm.graphs) cudaGraphExecDestroy(g.exec);
   if (s->expm.buf) cudaFree(s->expm.buf);
   delete s;  // the Krylov buffers are context allocations, freed with the context
 }
@@ -639,7 +658,7 @@ int hymor_expm_apply_dev(hymor_ctx* ctx, int k, double dt, int nsteps, int order
   DevCtx& d = ctx_dev(ctx);
   if (!d.coef) return ctx_fail(ctx, HYMOR_ERR_NOT_READY, "no Jacobian: call hymor_linearize or hymor_jacobian_set");
   cudaStream_t st = ctx_stream(ctx);
-  if ((long)nsteps * (order + 1) >= kExpmGraphMinLaunches) return expm_via_graph(ctx, k, dt, nsteps, order, dX, dY, transpose);
+  if ((long)nsteps * (order + 1) >= kExpmCoopMinLaunches) return expm_cooperative(ctx, k, dt, nsteps, order, dX, dY, transpose);
   const size_t n = 4 * d.N * (size_t)k;
   double* work = nullptr;
   int r;

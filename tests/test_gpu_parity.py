@@ -194,10 +194,10 @@ def test_expm_parity(require_gpu):
     assert rel_err(Yt, orc.expm(co, dt, 5, X[:, 0], transpose=True)) < 1e-12
 
 
-def test_expm_replayed_graphs(require_gpu):
-    """Repeated propagations replay a cached CUDA graph over fixed buffers: new inputs on
-    the same graph, more (dt, nsteps) combinations than the cache holds, an aliased
-    output, and a larger block that reallocates the buffers all match the oracle."""
+def test_expm_repeated_propagations(require_gpu):
+    """Repeated propagations through the cooperative single-launch path and its fixed
+    buffers: new inputs, several (dt, nsteps) combinations, a larger block that
+    reallocates the buffers, and the transpose all match the oracle."""
     cfg = C.cylinder_config(30, 20)
     cs, sol, orc = both(cfg)
     co = orc.linearize()
