@@ -557,7 +557,7 @@ __device__ __noinline__ void chol_solve_f64(int m, const double* __restrict__ d0
                                const double* __restrict__ d2, const double* __restrict__ rx,
                                const double* __restrict__ ry, double* __restrict__ il0, double* __restrict__ l1,
                                double* __restrict__ l2, double* __restrict__ gx_, double* __restrict__ gy_) {
-  double l1p = 0, l2p = 0, l2pp = 0, zx1 = 0, zx2 = 0, zy1 = 0, zy2 = 0, l1pp = 0;
+  double l1p = 0, l2p = 0, l2pp = 0, zx1 = 0, zx2 = 0, zy1 = 0, zy2 = 0;
   for (int j = 0; j < m; ++j) {
     const double a = d0[j] - l1p * l1p - l2pp * l2pp;
     const double il = frsqrt(a);
@@ -569,9 +569,8 @@ __device__ __noinline__ void chol_solve_f64(int m, const double* __restrict__ d0
     il0[j] = il; l1[j] = nl1; l2[j] = nl2;
     gx_[j + 1] = zx; gy_[j + 1] = zy;
     zx2 = zx1; zx1 = zx; zy2 = zy1; zy1 = zy;
-    l2pp = l2p; l2p = nl2; l1pp = l1p; l1p = nl1;
+    l2pp = l2p; l2p = nl2; l1p = nl1;
   }
-  (void)l1pp;
   // backward: l0_j x_j = z_j - l1_j x_{j+1} - l2_j x_{j+2}
   double x1 = 0, x2 = 0, y1 = 0, y2 = 0;
   for (int j = m - 1; j >= 0; --j) {
