@@ -8,9 +8,9 @@ Metric: Mcell-stage/s (cells x 4 stages x steps / time), FP64.
 
 Device timing: CUDA events on the library's stream around each step; every step is
 preceded (outside its timed window) by a 512 MiB write that evicts the 129 MB L2.
-e2e: the same metric through the public API with host buffers: per step, the state
-is uploaded from pinned host memory (hymor_set_state), advanced (hymor_step) and
-read back (hymor_get_state), timed on the host clock.
+e2e: the same metric through the public API with host buffers: per step, one
+hymor_advect call uploads the state from pinned host memory, advances it one step and
+writes it back, timed on the host clock.
 With --gpus N > 1 (torchrun) every rank advances its own replica of the case (the
 path has no cross-GPU exchange); value = all ranks' cell-stages / max rank time.
 --impl reference times the CPU restatement of the reference path (the oracle,
@@ -267,10 +267,11 @@ def main():
     torch.cuda.synchronize()
     barrier(dist)
     t0 = time.perf_counter()
+    t_state = ctypes.c_double(st["t"])
     for _ in range(args.e2e_steps):
-        sol.ctx.check(L.hymor_set_state(h, qp, dp(pts[0]), dp(pts[1]), dp(pts[2]), dp(pts[3]), ip(ci), 0.0, None))
-        sol.ctx.check(L.hymor_step(h, 1))
-        sol.ctx.check(L.hymor_get_state(h, qp, dp(pts[0]), dp(pts[1]), dp(pts[2]), dp(pts[3]), ip(ci), None, None))
+        # ADVECT_FLOW on the host-resident state: upload, one step, download (hymor_advect)
+        sol.ctx.check(L.hymor_advect(h, 1, qp, dp(pts[0]), dp(pts[1]), dp(pts[2]), dp(pts[3]), ip(ci),
+                                     ctypes.byref(t_state)))
     t_e2e = max_over_ranks(dist, time.perf_counter() - t0)
     e2e_value = CELLS * STAGES * args.e2e_steps * world / t_e2e / 1e6
     h2d = 4 * G * 8 + 4 * NCHI * 8 + NCHI * 4

@@ -34,7 +34,7 @@ EXPORTS = [
     "hymor_memcpy_h2d", "hymor_memcpy_d2h", "hymor_bench_steps", "hymor_dot_dev",
     "hymor_krylov_orthogonalize", "hymor_krylov_rotate", "hymor_block4_apply_dev", "hymor_memcpy_d2d",
     "hymor_expm_apply_dev_noalloc", "hymor_step_kernels", "hymor_fp64_peak",
-    "hymor_profile_phases",
+    "hymor_profile_phases", "hymor_advect",
 ]
 
 
@@ -67,6 +67,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "hymor_residual": [vp, dp],
         "hymor_set_flux": [vp, dp],
         "hymor_step": [vp, i],
+        "hymor_advect": [vp, i, dp, dp, dp, dp, dp, ip, dp],
         "hymor_update_flow_cells": [vp],
         "hymor_cfl_timestep": [vp, dp],
         "hymor_counters": [vp, ip, ip],

@@ -325,16 +325,20 @@ int build_graph(hymor_ctx* ctx) {
   return 0;
 }
 
-int read_err(hymor_ctx* ctx) {
-  unsigned h[kErrCount];
-  CU(cudaMemcpyAsync(h, ctx->d.err, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
-  CU(cudaStreamSynchronize(ctx->stream));
+int check_err_words(hymor_ctx* ctx, const unsigned* h) {
   if (h[kErrFlags] & kBitShockRange)
     return fail(ctx, HYMOR_ERR_SHOCK_RANGE, "shocked cell outside rows 2..Neta-1 (the shock left the mesh)");
   if (h[kErrFlags] & kBitNumeric)
     return fail(ctx, HYMOR_ERR_NUMERIC, "non-positive density or pressure, or NaN, in the flow field");
   if (h[kErrFlags] & kBitTimeout) return fail(ctx, HYMOR_ERR_TIMEOUT, "bounded device wait gave up");
   return 0;
+}
+
+int read_err(hymor_ctx* ctx) {
+  unsigned h[kErrCount];
+  CU(cudaMemcpyAsync(h, ctx->d.err, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return check_err_words(ctx, h);
 }
 
 int set_device(hymor_ctx* ctx) {
@@ -348,7 +352,7 @@ int set_device(hymor_ctx* ctx) {
 constexpr size_t kScalPitch = 32;
 size_t state_pitch(size_t n) { return (n + 31) & ~size_t(31); }
 size_t header_doubles(size_t n) { return 4 * state_pitch(n) + kScalPitch + (n + 1) / 2; }
-size_t stage_bytes(int n) { return header_doubles(n) * sizeof(double); }
+size_t stage_bytes(int n) { return header_doubles(n) * sizeof(double) + kErrCount * sizeof(unsigned); }
 
 // The stored flux s["flux"] is no longer all zero: a step graph captured while it was
 // (whose CFL kernel skips the stored-flux term) is dropped and captured again.
@@ -379,6 +383,76 @@ void refresh_sound(hymor_ctx* ctx, bool recomputed_anyway) {
   if (!ctx->a_stale) return;
   if (!recomputed_anyway) launch_sound_cmax(ctx->d, true, ctx->stream);
   ctx->a_stale = false;
+}
+
+// Validates a host state and enqueues its upload (no synchronisation): q in one 2-D copy,
+// the shock points, scalars and shocked rows through the pinned staging buffer.
+int enqueue_upload(hymor_ctx* ctx, const double* q, const double* pts_x, const double* pts_y,
+                   const double* pts_chi, const double* pts_eta, const int32_t* cell_idx, double t,
+                   const double* a) {
+  if (!q) return fail(ctx, HYMOR_ERR_INVALID, "q is NULL");
+  DevCtx& d = ctx->d;
+  const size_t G = d.G, n = d.nchi;
+  const bool shock = d.cfg.shock_enabled;
+  if (shock && (!pts_x || !pts_y || !pts_chi || !pts_eta || !cell_idx))
+    return fail(ctx, HYMOR_ERR_INVALID, "shock fitting needs the shock points and cell indices");
+  const size_t np = state_pitch(n), Gp = state_pitch(G);
+  double* sp = reinterpret_cast<double*>(ctx->stage);  // staged header, same layout as on the device
+  double* sc = sp + 4 * np;
+  int32_t* sci = reinterpret_cast<int32_t*>(sc + kScalPitch);
+  for (size_t i = 0; i < n; ++i) {
+    const int32_t v = cell_idx ? cell_idx[i] : d.neta + 1;
+    if (cell_idx && shock && (v < 2 || v > d.neta - 1))
+      return fail(ctx, HYMOR_ERR_SHOCK_RANGE, "cell_idx[%zu] = %d outside 2..Neta-1", i, v);
+    sci[i] = v;
+  }
+  cudaStream_t st = ctx->stream;
+  CU(cudaMemcpy2DAsync(d.S.rho, Gp * 8, q, G * 8, G * 8, 4, cudaMemcpyHostToDevice, st));
+  const double* src[4] = {pts_x, pts_y, pts_chi, pts_eta};
+  double* dst[4] = {d.Sp.x, d.Sp.y, d.Sp.chi, d.Sp.eta};
+  const bool all_pts = pts_x && pts_y && pts_chi && pts_eta;
+  for (int k = 0; k < 4; ++k)
+    if (src[k]) std::memcpy(sp + k * np, src[k], n * 8);
+  for (size_t k = 0; k < kScalPitch; ++k) sc[k] = 0;
+  sc[kT] = t;
+  if (all_pts) {
+    CU(cudaMemcpyAsync(d.Sp.x, sp, header_doubles(n) * 8, cudaMemcpyHostToDevice, st));
+  } else {  // keep the device copies of the points the caller did not pass
+    for (int k = 0; k < 4; ++k)
+      if (src[k]) CU(cudaMemcpyAsync(dst[k], sp + k * np, n * 8, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(d.scal, sc, (header_doubles(n) - 4 * np) * 8, cudaMemcpyHostToDevice, st));
+  }
+  if (a) CU(cudaMemcpyAsync(d.aS, a, G * 8, cudaMemcpyHostToDevice, st));
+  ctx->a_stale = !a;
+  return 0;
+}
+
+// Enqueues the download of S (if q) and of the header into the staging buffer (and of the
+// error word behind it, with_err); the caller synchronises and unpacks.
+int enqueue_download(hymor_ctx* ctx, double* q, bool with_err) {
+  DevCtx& d = ctx->d;
+  const size_t G = d.G, n = d.nchi, Gp = state_pitch(G);
+  cudaStream_t st = ctx->stream;
+  if (q) CU(cudaMemcpy2DAsync(q, G * 8, d.S.rho, Gp * 8, G * 8, 4, cudaMemcpyDeviceToHost, st));
+  CU(cudaMemcpyAsync(ctx->stage, d.Sp.x, header_doubles(n) * 8, cudaMemcpyDeviceToHost, st));
+  if (with_err)
+    CU(cudaMemcpyAsync(ctx->stage + header_doubles(n) * 8, d.err, kErrCount * sizeof(unsigned),
+                       cudaMemcpyDeviceToHost, st));
+  return 0;
+}
+
+void unpack_header(hymor_ctx* ctx, double* pts_x, double* pts_y, double* pts_chi, double* pts_eta,
+                   int32_t* cell_idx, double* t, double* dt) {
+  const size_t n = ctx->d.nchi, np = state_pitch(n);
+  const double* sp = reinterpret_cast<const double*>(ctx->stage);
+  const double* sc = sp + 4 * np;
+  const int32_t* sci = reinterpret_cast<const int32_t*>(sc + kScalPitch);
+  double* out[4] = {pts_x, pts_y, pts_chi, pts_eta};
+  for (int k = 0; k < 4; ++k)
+    if (out[k]) std::memcpy(out[k], sp + k * np, n * 8);
+  if (cell_idx) std::memcpy(cell_idx, sci, n * 4);
+  if (t) *t = sc[kT];
+  if (dt) *dt = sc[kDt];
 }
 
 }  // namespace
@@ -570,45 +644,9 @@ int hymor_set_state(hymor_ctx* ctx, const double* q, const double* pts_x, const 
                     const double* pts_chi, const double* pts_eta, const int32_t* cell_idx, double t,
                     const double* a) {
   if (!ctx) return HYMOR_ERR_INVALID;
-  if (!q) return fail(ctx, HYMOR_ERR_INVALID, "q is NULL");
   TRY(set_device(ctx));
-  DevCtx& d = ctx->d;
-  const size_t G = d.G, n = d.nchi;
-  const bool shock = d.cfg.shock_enabled;
-  if (shock && (!pts_x || !pts_y || !pts_chi || !pts_eta || !cell_idx))
-    return fail(ctx, HYMOR_ERR_INVALID, "shock fitting needs the shock points and cell indices");
-  std::vector<int32_t> ci(n, d.neta + 1);
-  if (cell_idx) {
-    for (size_t i = 0; i < n; ++i) {
-      ci[i] = cell_idx[i];
-      if (shock && (ci[i] < 2 || ci[i] > d.neta - 1))
-        return fail(ctx, HYMOR_ERR_SHOCK_RANGE, "cell_idx[%zu] = %d outside 2..Neta-1", i, ci[i]);
-    }
-  }
-  cudaStream_t st = ctx->stream;
-  const size_t np = state_pitch(n), Gp = state_pitch(G);
-  CU(cudaMemcpy2DAsync(d.S.rho, Gp * 8, q, G * 8, G * 8, 4, cudaMemcpyHostToDevice, st));
-  double* sp = reinterpret_cast<double*>(ctx->stage);  // staged header, same layout as on the device
-  double* sc = sp + 4 * np;
-  int32_t* sci = reinterpret_cast<int32_t*>(sc + kScalPitch);
-  const double* src[4] = {pts_x, pts_y, pts_chi, pts_eta};
-  double* dst[4] = {d.Sp.x, d.Sp.y, d.Sp.chi, d.Sp.eta};
-  const bool all_pts = pts_x && pts_y && pts_chi && pts_eta;
-  for (int k = 0; k < 4; ++k)
-    if (src[k]) std::memcpy(sp + k * np, src[k], n * 8);
-  std::memcpy(sci, ci.data(), n * 4);
-  for (size_t k = 0; k < kScalPitch; ++k) sc[k] = 0;
-  sc[kT] = t;
-  if (all_pts) {
-    CU(cudaMemcpyAsync(d.Sp.x, sp, header_doubles(n) * 8, cudaMemcpyHostToDevice, st));
-  } else {  // keep the device copies of the points the caller did not pass
-    for (int k = 0; k < 4; ++k)
-      if (src[k]) CU(cudaMemcpyAsync(dst[k], sp + k * np, n * 8, cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(d.scal, sc, (header_doubles(n) - 4 * np) * 8, cudaMemcpyHostToDevice, st));
-  }
-  if (a) CU(cudaMemcpyAsync(d.aS, a, G * 8, cudaMemcpyHostToDevice, st));
-  ctx->a_stale = !a;
-  CU(cudaStreamSynchronize(st));
+  TRY(enqueue_upload(ctx, q, pts_x, pts_y, pts_chi, pts_eta, cell_idx, t, a));
+  CU(cudaStreamSynchronize(ctx->stream));
   CU(cudaGetLastError());
   return 0;
 }
@@ -617,23 +655,26 @@ int hymor_get_state(hymor_ctx* ctx, double* q, double* pts_x, double* pts_y, dou
                     double* pts_eta, int32_t* cell_idx, double* t, double* dt) {
   if (!ctx) return HYMOR_ERR_INVALID;
   TRY(set_device(ctx));
-  DevCtx& d = ctx->d;
-  const size_t G = d.G, n = d.nchi;
-  cudaStream_t st = ctx->stream;
-  const size_t np = state_pitch(n), Gp = state_pitch(G);
-  if (q) CU(cudaMemcpy2DAsync(q, G * 8, d.S.rho, Gp * 8, G * 8, 4, cudaMemcpyDeviceToHost, st));
-  double* sp = reinterpret_cast<double*>(ctx->stage);
-  double* sc = sp + 4 * np;
-  int32_t* sci = reinterpret_cast<int32_t*>(sc + kScalPitch);
-  double* out[4] = {pts_x, pts_y, pts_chi, pts_eta};
-  CU(cudaMemcpyAsync(sp, d.Sp.x, header_doubles(n) * 8, cudaMemcpyDeviceToHost, st));
-  CU(cudaStreamSynchronize(st));
-  for (int k = 0; k < 4; ++k)
-    if (out[k]) std::memcpy(out[k], sp + k * np, n * 8);
-  if (cell_idx) std::memcpy(cell_idx, sci, n * 4);
-  if (t) *t = sc[kT];
-  if (dt) *dt = sc[kDt];
+  TRY(enqueue_download(ctx, q, false));
+  CU(cudaStreamSynchronize(ctx->stream));
+  unpack_header(ctx, pts_x, pts_y, pts_chi, pts_eta, cell_idx, t, dt);
   return 0;
+}
+
+int hymor_advect(hymor_ctx* ctx, int nsteps, double* q, double* pts_x, double* pts_y, double* pts_chi,
+                 double* pts_eta, int32_t* cell_idx, double* t) {
+  if (!ctx || !t) return HYMOR_ERR_INVALID;
+  if (nsteps < 0) return fail(ctx, HYMOR_ERR_INVALID, "nsteps < 0");
+  TRY(set_device(ctx));
+  TRY(build_graph(ctx));
+  TRY(enqueue_upload(ctx, q, pts_x, pts_y, pts_chi, pts_eta, cell_idx, *t, nullptr));
+  if (nsteps > 0) refresh_sound(ctx, ctx->d.cfg.shock_enabled);
+  for (int s = 0; s < nsteps; ++s) CU(cudaGraphLaunch(ctx->gexec, ctx->stream));
+  mark_sound_after_steps(ctx, nsteps);
+  TRY(enqueue_download(ctx, q, true));
+  CU(cudaStreamSynchronize(ctx->stream));
+  unpack_header(ctx, pts_x, pts_y, pts_chi, pts_eta, cell_idx, t, nullptr);
+  return check_err_words(ctx, reinterpret_cast<const unsigned*>(ctx->stage + header_doubles(ctx->d.nchi) * 8));
 }
 
 int hymor_residual(hymor_ctx* ctx, double* flux) {

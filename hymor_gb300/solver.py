@@ -66,6 +66,20 @@ class Solution:
         return dict(q=q, pts_x=px, pts_y=py, pts_chi=pc, pts_eta=pe, cell_idx=ci, t=t.value,
                     dt=dt.value)
 
+    def advect_host(self, q, px, py, pchi, peta, cell_idx, t: float, nsteps: int) -> float:
+        """ADVECT_FLOW of a host-resident state in one call (hymor_advect): the arrays are
+        uploaded, advanced `nsteps` steps and overwritten with the result; returns t."""
+        arrs = (q, px, py, pchi, peta)
+        for v in arrs:
+            if v.dtype != np.float64 or not v.flags.c_contiguous:
+                raise HymorError(-1, "advect_host needs contiguous float64 arrays (updated in place)")
+        if cell_idx.dtype != np.int32 or not cell_idx.flags.c_contiguous:
+            raise HymorError(-1, "advect_host needs contiguous int32 cell indices (updated in place)")
+        tt = ctypes.c_double(t)
+        self.ctx.check(self.ctx.L.hymor_advect(self.ctx.h, int(nsteps), *[dp(v) for v in arrs], ip(cell_idx),
+                                               ctypes.byref(tt)))
+        return tt.value
+
     def var(self) -> dict:
         """s["var"]: the four ghosted conserved arrays, (Nchi+2, Neta+2) column-major."""
         q = self.get_state()["q"].reshape(4, -1)

@@ -116,6 +116,13 @@ int hymor_set_flux(hymor_ctx* ctx, const double* flux);
 /* nsteps x ADVECT_FLOW (utils/Time_marching/ADVECT_FLOW.jl:30-39 ->
  * ADVECT_FLOW_EXPLICIT.jl:36-81), all on the device (one CUDA graph per step). */
 int hymor_step(hymor_ctx* ctx, int nsteps);
+/* ADVECT_FLOW on a host-resident solution, in one call: the state in q (4 x G, as
+ * hymor_set_state), the shock points, the shocked rows and t are uploaded, nsteps steps
+ * run, and the advanced state, points, rows and t are written back into the same buffers
+ * (the Dict mutated in place, ADVECT_FLOW.jl:30-39). One synchronisation per call; errors
+ * as hymor_step. Equivalent to hymor_set_state + hymor_step + hymor_get_state. */
+int hymor_advect(hymor_ctx* ctx, int nsteps, double* q, double* pts_x, double* pts_y, double* pts_chi,
+                 double* pts_eta, int32_t* cell_idx, double* t);
 /* UPDATE_FLOW_CELLS (utils/Shock_fitting/UPDATE_FLOW_CELLS.jl:25-37). */
 int hymor_update_flow_cells(hymor_ctx* ctx);
 /* CFL_TIMESTEP (utils/Time_marching/CFL_TIMESTEP.jl:41-138) on the current state. */

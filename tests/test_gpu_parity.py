@@ -110,6 +110,28 @@ def test_cfl_timestep_parity(require_gpu):
     assert abs(S.CFL_TIMESTEP(sol) - orc.cfl()) < 1e-14 * orc.cfl()
 
 
+def test_advect_host_matches_separate_calls(require_gpu):
+    """hymor_advect (upload, steps, download in one call) gives exactly what
+    hymor_set_state + hymor_step + hymor_get_state give."""
+    cfg = C.cylinder_config(40, 30)
+    cs = C.initial_state(cfg)
+    a = S.Solution(cs)
+    S.ADVECT_FLOW(a, 3)
+    ref = a.get_state()
+    b = S.Solution(cs)
+    st = b.get_state()
+    q = np.ascontiguousarray(st["q"])
+    pts = [np.ascontiguousarray(st[k]) for k in ("pts_x", "pts_y", "pts_chi", "pts_eta")]
+    ci = np.ascontiguousarray(st["cell_idx"])
+    t = b.advect_host(q, *pts, ci, st["t"], 3)
+    assert np.array_equal(q, ref["q"])
+    for k, v in zip(("pts_x", "pts_y", "pts_chi", "pts_eta"), pts):
+        assert np.array_equal(v, ref[k])
+    assert np.array_equal(ci, ref["cell_idx"]) and t == ref["t"]
+    a.close()
+    b.close()
+
+
 def test_stored_flux_enters_cfl_and_steps(require_gpu):
     """The stored flux s["flux"] (set by PDE on the solution) enters CFL_TIMESTEP's dt2
     term: steps taken before and after it is first written match the oracle (the step
