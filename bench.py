@@ -312,7 +312,7 @@ def main():
             "step_phases_us": {"start": round(phases[0] * 1e3, 1),
                                "stages": [[round(phases[1 + 4 * k + q] * 1e3, 1) for q in range(4)]
                                           for k in range(4)],
-                               "stage_fields": ["update", "flux_interior", "wait_shock_bc", "flux_shock_bc"],
+                               "stage_fields": ["update", "flux_interior", "start_shock_bc_after_interior", "flux_shock_bc"],
                                "end": round(phases[17] * 1e3, 1)},
             "clocks": clk.summary(),
         }

@@ -21,8 +21,10 @@ struct hymor_ctx_s {
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;      // high-priority stream of the shock/BC chain inside the step graph
   cudaStream_t fit = nullptr;       // the step's first spline fit, beside the flow cells and the CFL
+  cudaStream_t c1 = nullptr;        // the shock/boundary-class flux, beside the interior-class flux
   cudaEvent_t fork_ev[8] = {}, join_ev[8] = {};
   cudaEvent_t fit_fork = nullptr, fit_join = nullptr;
+  cudaEvent_t c1_fork[4] = {}, c1_join[4] = {};
   int device = 0;
   std::string err;
   std::vector<void*> allocs;
@@ -213,11 +215,12 @@ int enqueue_step(hymor_ctx* ctx, bool with_events) {
     ++nj;
     return 0;
   };
-  auto ev = [&](int k) -> int {
+  auto ev_on = [&](int k, cudaStream_t s) -> int {
     // cudaEventRecordExternal makes a real event-record node under stream capture
-    if (with_events) CU(cudaEventRecordWithFlags(ctx->cap_ev[k], st, cudaEventRecordExternal));
+    if (with_events) CU(cudaEventRecordWithFlags(ctx->cap_ev[k], s, cudaEventRecordExternal));
     return 0;
   };
+  auto ev = [&](int k) -> int { return ev_on(k, st); };
   CU(cudaMemsetAsync(d.scal + kCmax, 0, 3 * sizeof(double), st));
   TRY(ev(20));
   if (c.rk_variant == 0) {
@@ -248,17 +251,22 @@ int enqueue_step(hymor_ctx* ctx, bool with_events) {
       }
       TRY(fork());
       launch_columns_bc(d, false, shock, wY[k], wA[k], 0, true, true, sx);
-      TRY(ev(4 * k));
-      // at the first stage the CFL chain and the first fit run beside the interior flux as
-      // well: it leaves them one block slot per SM
-      launch_flux_class(d, false, F, 0, st, k == 0 ? 1 : 0);
-      TRY(ev(4 * k + 1));
-      TRY(join());
+      // the shock/boundary-class flux on its own stream as soon as the jump and boundary
+      // kernels are done, beside the rest of the interior-class flux
+      CU(cudaEventRecord(ctx->c1_fork[k], sx));
+      CU(cudaStreamWaitEvent(ctx->c1, ctx->c1_fork[k], 0));
+      TRY(ev_on(4 * k + 2, ctx->c1));
+      launch_flux_class(d, false, F, 1, ctx->c1);
+      TRY(ev_on(4 * k + 3, ctx->c1));
+      CU(cudaEventRecord(ctx->c1_join[k], ctx->c1));
       // next fit (stage k+1 on Y, or the step-end fit on S) overlaps this stage's remaining work
       launch_spline(d, k == 3, false, sx);
-      TRY(ev(4 * k + 2));
-      launch_flux_class(d, false, F, 1, st);
-      TRY(ev(4 * k + 3));
+      TRY(ev(4 * k));
+      // the interior flux leaves one block slot per SM to the side-stream kernels and the
+      // shock/boundary-class flux
+      launch_flux_class(d, false, F, 0, st, 1);
+      TRY(ev(4 * k + 1));
+      CU(cudaStreamWaitEvent(st, ctx->c1_join[k], 0));
     }
     launch_update_thermo(d, 2, 0, wA[3], st);
     TRY(join());
@@ -594,8 +602,13 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
     int lo = 0, hi = 0;
     cudaDeviceGetStreamPriorityRange(&lo, &hi);
     if (cudaStreamCreateWithPriority(&ctx->side, cudaStreamNonBlocking, hi) != cudaSuccess ||
-        cudaStreamCreateWithPriority(&ctx->fit, cudaStreamNonBlocking, hi) != cudaSuccess)
+        cudaStreamCreateWithPriority(&ctx->fit, cudaStreamNonBlocking, hi) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&ctx->c1, cudaStreamNonBlocking, hi) != cudaSuccess)
       return bail(fail(ctx, HYMOR_ERR_CUDA, "side stream creation failed"));
+    for (int k = 0; k < 4; ++k)
+      if (cudaEventCreateWithFlags(&ctx->c1_fork[k], cudaEventDisableTiming) != cudaSuccess ||
+          cudaEventCreateWithFlags(&ctx->c1_join[k], cudaEventDisableTiming) != cudaSuccess)
+        return bail(fail(ctx, HYMOR_ERR_CUDA, "event"));
     if (cudaEventCreateWithFlags(&ctx->fit_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->fit_join, cudaEventDisableTiming) != cudaSuccess)
       return bail(fail(ctx, HYMOR_ERR_CUDA, "event"));
@@ -625,8 +638,13 @@ int hymor_ctx_destroy(hymor_ctx* ctx) {
     if (e) cudaEventDestroy(e);
   if (ctx->fit_fork) cudaEventDestroy(ctx->fit_fork);
   if (ctx->fit_join) cudaEventDestroy(ctx->fit_join);
+  for (auto e : ctx->c1_fork)
+    if (e) cudaEventDestroy(e);
+  for (auto e : ctx->c1_join)
+    if (e) cudaEventDestroy(e);
   if (ctx->side) cudaStreamDestroy(ctx->side);
   if (ctx->fit) cudaStreamDestroy(ctx->fit);
+  if (ctx->c1) cudaStreamDestroy(ctx->c1);
   for (auto e : ctx->prof_ev) cudaEventDestroy(e);
   if (ctx->t0) cudaEventDestroy(ctx->t0);
   if (ctx->t1) cudaEventDestroy(ctx->t1);
@@ -844,10 +862,11 @@ int hymor_profile_flux(hymor_ctx* ctx, int enable, float* total_ms, int32_t* lau
     const size_t E = hymor_ctx_s::kEv;
     for (size_t s = 0; s + E <= ctx->prof_ev.size(); s += E)
       for (int k = 0; k < 4; ++k) {  // one residual evaluation per stage, in two launches
+        // from the start of the interior-class flux to the later end of the two classes
         float v1 = 0, v2 = 0;
         CU(cudaEventElapsedTime(&v1, ctx->prof_ev[s + 4 * k], ctx->prof_ev[s + 4 * k + 1]));
-        CU(cudaEventElapsedTime(&v2, ctx->prof_ev[s + 4 * k + 2], ctx->prof_ev[s + 4 * k + 3]));
-        tot += v1 + v2;
+        CU(cudaEventElapsedTime(&v2, ctx->prof_ev[s + 4 * k], ctx->prof_ev[s + 4 * k + 3]));
+        tot += v1 > v2 ? v1 : v2;
         ++n;
       }
     if (total_ms) *total_ms = (float)tot;
@@ -885,10 +904,15 @@ int hymor_profile_phases(hymor_ctx* ctx, float* ms) {
     for (int k = 0; k < 4; ++k) {
       TRY(dt(s, 16 + k, 4 * k, ms[1 + 4 * k]));          // stage update (+ fork)
       TRY(dt(s, 4 * k, 4 * k + 1, ms[2 + 4 * k]));       // flux, interior tiles
-      TRY(dt(s, 4 * k + 1, 4 * k + 2, ms[3 + 4 * k]));   // wait for the shock/boundary kernels
+      TRY(dt(s, 4 * k, 4 * k + 2, ms[3 + 4 * k]));       // start of the shock/boundary-tile flux,
+                                                          // after the interior flux's start
       TRY(dt(s, 4 * k + 2, 4 * k + 3, ms[4 + 4 * k]));   // flux, shock/boundary tiles
     }
-    TRY(dt(s, 15, 21, ms[17]));
+    // from the later end of the last stage's two flux launches to the step end
+    float e1 = 0, e2 = 0;
+    TRY(dt(s, 13, 21, e1));
+    TRY(dt(s, 15, 21, e2));
+    ms[17] += e1 < e2 ? e1 : e2;
   }
   if (steps)
     for (int k = 0; k < 18; ++k) ms[k] /= steps;

@@ -44,8 +44,8 @@ struct TileGeo {
   static constexpr int NBTF = TX * (TYV + 1);      // bt faces
   static constexpr int THREADS = 32 * TYV;
 };
-// dynamic shared memory that leaves room for one flux block per SM (of 228 KB)
-constexpr size_t kFluxOneBlockSmem = 120 * 1024;
+// ceiling of the flux kernels' dynamic shared memory (above the 48 KB default)
+constexpr size_t kFluxMaxSmem = 120 * 1024;
 
 // x > 0 (NaN excluded) on the integer pipe: the bit patterns of +0 .. +inf are ordered
 // as unsigned integers, and every NaN or negative pattern lies above +inf.
@@ -1771,9 +1771,8 @@ void launch_classify_tiles(const DevCtx& d, cudaStream_t st) {
 template <bool AXI, bool SUTH>
 void flux_launch(const FluxArgs& a, int tile_class, dim3 grid, const DevCtx& d, cudaStream_t st) {
   if (tile_class == 1 && a.list) {
-    // the shock/boundary class: one block per SM (the shared-memory request admits no
-    // second), so that its few tiles spread over every SM instead of piling up on some
-    k_flux<AXI, SUTH, TY><<<d.sms, kFluxThreads, kFluxOneBlockSmem, st>>>(a);
+    // the shock/boundary class: a persistent grid of one block per SM over its few tiles
+    k_flux<AXI, SUTH, TY><<<d.sms, kFluxThreads, flux_smem<AXI, SUTH>(), st>>>(a);
   } else {
     k_flux<AXI, SUTH, TY><<<grid, kFluxThreads, flux_smem<AXI, SUTH>(), st>>>(a);
   }
@@ -1823,10 +1822,10 @@ void launch_flux(const DevCtx& d, bool on_S, double* const out[4], cudaStream_t 
 }
 
 void flux_kernel_setup() {
-  cudaFuncSetAttribute(k_flux<false, false, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxOneBlockSmem);
-  cudaFuncSetAttribute(k_flux<true, false, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxOneBlockSmem);
-  cudaFuncSetAttribute(k_flux<false, true, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxOneBlockSmem);
-  cudaFuncSetAttribute(k_flux<true, true, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxOneBlockSmem);
+  cudaFuncSetAttribute(k_flux<false, false, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxMaxSmem);
+  cudaFuncSetAttribute(k_flux<true, false, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxMaxSmem);
+  cudaFuncSetAttribute(k_flux<false, true, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxMaxSmem);
+  cudaFuncSetAttribute(k_flux<true, true, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxMaxSmem);
   auto occ = [](auto kern, size_t smem) {
     int b = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kFluxThreads, smem) != cudaSuccess || b < 1) b = 1;

@@ -132,10 +132,11 @@ int hymor_counters(hymor_ctx* ctx, int32_t* rho_limited, int32_t* rh_warnings);
 /* Number of kernel launches one hymor_step makes (the kernel nodes of its CUDA graph),
  * for launch accounting. No counterpart in the reference. */
 int hymor_step_kernels(hymor_ctx* ctx, int32_t* n);
-/* Average main-stream phases (ms) of the steps profiled since hymor_profile_flux(ctx, 1, ..):
+/* Average phases (ms) of the steps profiled since hymor_profile_flux(ctx, 1, ..):
  * ms[0] step start to the first stage update; per stage k, ms[1 + 4k] the stage update,
- * ms[2 + 4k] the flux of the interior tiles, ms[3 + 4k] the wait for the shock/boundary
- * kernels, ms[4 + 4k] the flux of the shock/boundary tiles; ms[17] the step end.
+ * ms[2 + 4k] the flux of the interior tiles, ms[3 + 4k] the start of the flux of the
+ * shock/boundary tiles (its own stream) after the start of the interior flux, ms[4 + 4k]
+ * that flux; ms[17] the later end of the last stage's two flux launches to the step end.
  * Call before hymor_profile_flux(ctx, 0, ..), which releases the events. No counterpart
  * in the reference. */
 int hymor_profile_phases(hymor_ctx* ctx, float* ms);
