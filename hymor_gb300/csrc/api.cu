@@ -25,6 +25,7 @@ struct hymor_ctx_s {
   cudaEvent_t fork_ev[8] = {}, join_ev[8] = {};
   cudaEvent_t fit_fork = nullptr, fit_join = nullptr;
   cudaEvent_t c1_fork[4] = {}, c1_join[4] = {};
+  cudaEvent_t u0_ev = nullptr, cfl_ev = nullptr, cls_ev = nullptr;
   int device = 0;
   std::string err;
   std::vector<void*> allocs;
@@ -225,48 +226,64 @@ int enqueue_step(hymor_ctx* ctx, bool with_events) {
   TRY(ev(20));
   if (c.rk_variant == 0) {
     // Third stream: the first fit reads only the shock points of S, which nothing before
-    // the first jump kernel changes, so it runs beside the flow cells and the CFL.
+    // the first jump kernel changes, so it runs beside the flow cells and the CFL; the
+    // first stage's jump and boundary kernels follow it there.
     CU(cudaEventRecord(ctx->fit_fork, st));
     CU(cudaStreamWaitEvent(ctx->fit, ctx->fit_fork, 0));
     launch_spline(d, false, true, ctx->fit);
-    CU(cudaEventRecord(ctx->fit_join, ctx->fit));
     if (shock) launch_flow_cells(d, st);
-    launch_classify_tiles(d, st);
-    // Side stream: the CFL reduction, and every later smoothing-spline fit one stage
-    // early (a fit needs only the shock points, which the previous stage's jump kernel
-    // moved); then per stage the jump + boundary kernels beside the flux of the
-    // interior tiles.
+    // Side stream: the tile classes and the CFL reduction beside the first stage update,
+    // and every later smoothing-spline fit one stage early (a fit needs only the shock
+    // points, which the previous stage's jump kernel moved); then per stage the jump +
+    // boundary kernels beside the flux of the interior tiles.
     TRY(fork());
+    launch_classify_tiles(d, sx);
+    CU(cudaEventRecord(ctx->cls_ev, sx));
     // with shock fitting the step recomputes the sound speed for the CFL maximum only
     // (and the outflow_NRCBC lines); the full field is recomputed when next needed
     launch_sound_cmax(d, shock, sx, true);
     launch_cfl(d, sx);
-    CU(cudaStreamWaitEvent(sx, ctx->fit_join, 0));
+    CU(cudaEventRecord(ctx->cfl_ev, sx));
     TRY(ev(16));
     launch_update_thermo(d, 0, 0, 0, st);
     for (int k = 0; k < 4; ++k) {
-      if (k > 0) {
+      cudaStream_t sj = sx;  // the stream of this stage's jump and boundary kernels
+      if (k == 0) {
+        // The first stage's jump and boundary kernels need no time step (only MOVE_SHOCK
+        // does): they run on the fit stream beside the CFL, and the move follows the CFL.
+        sj = ctx->fit;
+        CU(cudaEventRecord(ctx->u0_ev, st));
+        CU(cudaStreamWaitEvent(sj, ctx->u0_ev, 0));
+        CU(cudaStreamWaitEvent(sj, ctx->cls_ev, 0));  // the tile lists, for the flux below
+        launch_columns_bc(d, false, false, wY[0], wA[0], 0, true, true, sj);
+      } else {
         TRY(ev(16 + k));
         launch_update_thermo(d, 1, wY[k - 1], wA[k - 1], st);
+        TRY(fork());
+        launch_columns_bc(d, false, shock, wY[k], wA[k], 0, true, true, sx);
       }
-      TRY(fork());
-      launch_columns_bc(d, false, shock, wY[k], wA[k], 0, true, true, sx);
       // the shock/boundary-class flux on its own stream as soon as the jump and boundary
       // kernels are done, beside the rest of the interior-class flux
-      CU(cudaEventRecord(ctx->c1_fork[k], sx));
+      CU(cudaEventRecord(ctx->c1_fork[k], sj));
       CU(cudaStreamWaitEvent(ctx->c1, ctx->c1_fork[k], 0));
       TRY(ev_on(4 * k + 2, ctx->c1));
       launch_flux_class(d, false, F, 1, ctx->c1);
       TRY(ev_on(4 * k + 3, ctx->c1));
       CU(cudaEventRecord(ctx->c1_join[k], ctx->c1));
+      if (k == 0) {
+        CU(cudaStreamWaitEvent(sx, ctx->c1_fork[0], 0));
+        launch_move_shock(d, false, wY[0], wA[0], sx);
+      }
       // next fit (stage k+1 on Y, or the step-end fit on S) overlaps this stage's remaining work
       launch_spline(d, k == 3, false, sx);
       TRY(ev(4 * k));
       // the interior flux leaves one block slot per SM to the side-stream kernels and the
       // shock/boundary-class flux
+      if (k == 0) CU(cudaStreamWaitEvent(st, ctx->cls_ev, 0));
       launch_flux_class(d, false, F, 0, st, 1);
       TRY(ev(4 * k + 1));
       CU(cudaStreamWaitEvent(st, ctx->c1_join[k], 0));
+      if (k == 0) CU(cudaStreamWaitEvent(st, ctx->cfl_ev, 0));  // dt, for the next stage update
     }
     launch_update_thermo(d, 2, 0, wA[3], st);
     TRY(join());
@@ -610,7 +627,10 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
           cudaEventCreateWithFlags(&ctx->c1_join[k], cudaEventDisableTiming) != cudaSuccess)
         return bail(fail(ctx, HYMOR_ERR_CUDA, "event"));
     if (cudaEventCreateWithFlags(&ctx->fit_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&ctx->fit_join, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&ctx->fit_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->u0_ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->cfl_ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->cls_ev, cudaEventDisableTiming) != cudaSuccess)
       return bail(fail(ctx, HYMOR_ERR_CUDA, "event"));
   }
   if (cudaMallocHost(&ctx->stage, stage_bytes(d.nchi)) != cudaSuccess)
@@ -638,6 +658,9 @@ int hymor_ctx_destroy(hymor_ctx* ctx) {
     if (e) cudaEventDestroy(e);
   if (ctx->fit_fork) cudaEventDestroy(ctx->fit_fork);
   if (ctx->fit_join) cudaEventDestroy(ctx->fit_join);
+  if (ctx->u0_ev) cudaEventDestroy(ctx->u0_ev);
+  if (ctx->cfl_ev) cudaEventDestroy(ctx->cfl_ev);
+  if (ctx->cls_ev) cudaEventDestroy(ctx->cls_ev);
   for (auto e : ctx->c1_fork)
     if (e) cudaEventDestroy(e);
   for (auto e : ctx->c1_join)

@@ -243,7 +243,9 @@ __device__ void edge_normal(const EdgeCtx& e, const DevMesh& m, int k, double& n
   else { const long f = (long)(k - 1) + (long)e.neta * e.nchi; nx = m.bt_xn[f]; ny = m.bt_yn[f]; }
 }
 
-// First pass of one edge: everything but the symmetry end copies.
+// First pass of one edge: everything but the symmetry end copies. Each case loads the
+// values it reads before it stores any: the compiler cannot tell the planes apart, so a
+// load after a store would wait for the store's own load to return.
 __device__ void edge_bc_point(const hymor_config& c, const EdgeCtx& e, const DevMesh& m, Cons q,
                               double* P, double* Tt, const double* A, int k, int len) {
   const int g = at(e, 0, k), a1 = at(e, 1, k), a2 = at(e, 2, k);
@@ -251,72 +253,91 @@ __device__ void edge_bc_point(const hymor_config& c, const EdgeCtx& e, const Dev
   double* U = q.ru;
   double* V = q.rv;
   double* E = q.rE;
-  auto copy = [&](double* X) { X[g] = X[a1]; };
-  auto neg = [&](double* X) { X[g] = -X[a1]; };
-  auto extrap = [&](double* X) { X[g] = 2 * X[a1] - X[a2]; };
   const bool inner = k >= 1 && k <= len - 2;
   switch (e.bc) {
-    case HYMOR_BC_INFLOW_SUBSONIC:
-      R[g] = c.rho_0; U[g] = c.rho_u_0; V[g] = c.rho_v_0; extrap(E); extrap(P);
+    case HYMOR_BC_INFLOW_SUBSONIC: {
+      const double e1 = E[a1], e2 = E[a2], p1 = P[a1], p2 = P[a2];
+      R[g] = c.rho_0; U[g] = c.rho_u_0; V[g] = c.rho_v_0; E[g] = 2 * e1 - e2; P[g] = 2 * p1 - p2;
       break;
+    }
     case HYMOR_BC_INFLOW_SUPERSONIC:
       R[g] = c.rho_0; U[g] = c.rho_u_0; V[g] = c.rho_v_0; E[g] = c.rho_E_0; P[g] = c.p_0;
       break;
-    case HYMOR_BC_NO_SLIP_ADIABATIC:
-      copy(R); neg(U); neg(V); extrap(E); extrap(P); copy(Tt);
-      break;
-    case HYMOR_BC_NO_SLIP_ISOTHERMAL: {
-      copy(R); neg(U); neg(V); extrap(E); extrap(P);
-      const double Tw = (e.edge <= 1) ? c.Tw_chi0 : (e.edge == 2 ? c.Tw_eta0 : c.Tw_eta1);
-      const double T_w = Tw * c.cv / c.energy_factor;
-      Tt[g] = 2 * T_w - Tt[a1];
+    case HYMOR_BC_NO_SLIP_ADIABATIC: {
+      const double r1 = R[a1], u1 = U[a1], v1 = V[a1], e1 = E[a1], e2 = E[a2];
+      const double p1 = P[a1], p2 = P[a2], t1 = Tt[a1];
+      R[g] = r1; U[g] = -u1; V[g] = -v1; E[g] = 2 * e1 - e2; P[g] = 2 * p1 - p2; Tt[g] = t1;
       break;
     }
-    case HYMOR_BC_OUTFLOW_SUBSONIC:
-      extrap(R); extrap(E); extrap(U); extrap(V); copy(P);
-      if (e.edge != 1) copy(Tt);
+    case HYMOR_BC_NO_SLIP_ISOTHERMAL: {
+      const double r1 = R[a1], u1 = U[a1], v1 = V[a1], e1 = E[a1], e2 = E[a2];
+      const double p1 = P[a1], p2 = P[a2], t1 = Tt[a1];
+      const double Tw = (e.edge <= 1) ? c.Tw_chi0 : (e.edge == 2 ? c.Tw_eta0 : c.Tw_eta1);
+      const double T_w = Tw * c.cv / c.energy_factor;
+      R[g] = r1; U[g] = -u1; V[g] = -v1; E[g] = 2 * e1 - e2; P[g] = 2 * p1 - p2;
+      Tt[g] = 2 * T_w - t1;
       break;
-    case HYMOR_BC_OUTFLOW_SUPERSONIC:
-      extrap(R); extrap(E); extrap(U); extrap(V); extrap(P); copy(Tt);
+    }
+    case HYMOR_BC_OUTFLOW_SUBSONIC: {
+      const double r1 = R[a1], r2 = R[a2], e1 = E[a1], e2 = E[a2], u1 = U[a1], u2 = U[a2];
+      const double v1 = V[a1], v2 = V[a2], p1 = P[a1], t1 = Tt[a1];
+      R[g] = 2 * r1 - r2; E[g] = 2 * e1 - e2; U[g] = 2 * u1 - u2; V[g] = 2 * v1 - v2; P[g] = p1;
+      if (e.edge != 1) Tt[g] = t1;
       break;
-    case HYMOR_BC_OUTFLOW_SUPERSONIC_1ST:
-      copy(U); copy(V); copy(R); copy(E); copy(P); copy(Tt);
+    }
+    case HYMOR_BC_OUTFLOW_SUPERSONIC: {
+      const double r1 = R[a1], r2 = R[a2], e1 = E[a1], e2 = E[a2], u1 = U[a1], u2 = U[a2];
+      const double v1 = V[a1], v2 = V[a2], p1 = P[a1], p2 = P[a2], t1 = Tt[a1];
+      R[g] = 2 * r1 - r2; E[g] = 2 * e1 - e2; U[g] = 2 * u1 - u2; V[g] = 2 * v1 - v2; P[g] = 2 * p1 - p2;
+      Tt[g] = t1;
       break;
+    }
+    case HYMOR_BC_OUTFLOW_SUPERSONIC_1ST: {
+      const double u1 = U[a1], v1 = V[a1], r1 = R[a1], e1 = E[a1], p1 = P[a1], t1 = Tt[a1];
+      U[g] = u1; V[g] = v1; R[g] = r1; E[g] = e1; P[g] = p1; Tt[g] = t1;
+      break;
+    }
     case HYMOR_BC_OUTFLOW_NRCBC: {
-      extrap(R); extrap(U); extrap(V); extrap(E); extrap(P); copy(Tt);
+      const double r1 = R[a1], r2 = R[a2], u1 = U[a1], u2 = U[a2], v1 = V[a1], v2 = V[a2];
+      const double e1 = E[a1], e2 = E[a2], p1 = P[a1], p2 = P[a2], t1 = Tt[a1];
+      const double rg = 2 * r1 - r2, ug = 2 * u1 - u2, vg = 2 * v1 - v2;
+      double eg = 2 * e1 - e2, pg = 2 * p1 - p2;
       if (inner) {
         double nx, ny;
         edge_normal(e, m, k, nx, ny);
         const double a = A[a1];
-        const double rho_int = R[a1];
-        const double irg = frcp(R[g]);
-        double ung = (U[g] * nx + V[g] * ny) * irg;
-        double uni = (U[a1] * nx + V[a1] * ny) * frcp(rho_int);
+        const double rho_int = r1;
+        const double irg = frcp(rg);
+        double ung = (ug * nx + vg * ny) * irg;
+        double uni = (u1 * nx + v1 * ny) * frcp(rho_int);
         if (e.edge == 0 || e.edge == 2) { ung = -ung; uni = -uni; }
         if (ung < a) {
-          const double p_lodi = P[a1] + rho_int * a * (ung - uni);
-          P[g] = p_lodi;
-          const double rho_e = P[g] * (1.0 / (c.gamma - 1));
-          E[g] = rho_e + 0.5 * (U[g] * U[g] + V[g] * V[g]) * irg;
+          const double p_lodi = p1 + rho_int * a * (ung - uni);
+          pg = p_lodi;
+          const double rho_e = pg * (1.0 / (c.gamma - 1));
+          eg = rho_e + 0.5 * (ug * ug + vg * vg) * irg;
         }
       }
+      R[g] = rg; U[g] = ug; V[g] = vg; E[g] = eg; P[g] = pg; Tt[g] = t1;
       break;
     }
     case HYMOR_BC_PERIODIC: {
       const int s = at_per(e, k);
-      U[g] = U[s]; V[g] = V[s]; R[g] = R[s]; E[g] = E[s]; P[g] = P[s]; Tt[g] = Tt[s];
+      const double us = U[s], vs = V[s], rs = R[s], es = E[s], ps = P[s], ts = Tt[s];
+      U[g] = us; V[g] = vs; R[g] = rs; E[g] = es; P[g] = ps; Tt[g] = ts;
       break;
     }
     case HYMOR_BC_SYMMETRY: {
-      copy(R); copy(P);
+      const double r1 = R[a1], p1 = P[a1], e1 = E[a1], t1 = Tt[a1];
       if (inner) {
+        const double u1 = U[a1], v1 = V[a1];
         double nx, ny;
         edge_normal(e, m, k, nx, ny);
-        const double fv = U[a1] * nx + V[a1] * ny;
-        U[g] = U[a1] - 2 * fv * nx;
-        V[g] = V[a1] - 2 * fv * ny;
+        const double fv = u1 * nx + v1 * ny;
+        U[g] = u1 - 2 * fv * nx;
+        V[g] = v1 - 2 * fv * ny;
       }
-      copy(E); copy(Tt);
+      R[g] = r1; P[g] = p1; E[g] = e1; Tt[g] = t1;
       break;
     }
     default:
@@ -329,9 +350,10 @@ __device__ void edge_bc_point(const hymor_config& c, const EdgeCtx& e, const Dev
 //   k_spline_fit     one CTA: the serial banded factorisation of the smoothing
 //                    spline (the only O(Nchi) recurrence), both ordinates at once
 //   k_shock_columns  one thread per chi column: resample, element space, beta,
-//                    Rankine-Hugoniot jump, extrapolation, MOVE_SHOCK
-//   k_bc_chi / k_bc_eta  the two boundary phases (chi edges, then eta edges, whose
-//                    corners read the chi ghosts), one thread per edge point
+//                    Rankine-Hugoniot jump, extrapolation, MOVE_SHOCK (or k_move_shock
+//                    after it, once the time step is known)
+//   k_bc_edges       the two boundary phases (chi edges, then eta edges, whose corners
+//                    read the chi ghosts), one launch each, one thread per edge point
 // Spline workspace (units of n = Nchi doubles): 0 knots, 1-2 ordinates x/y, 3-4
 // second derivatives x/y, 5-6 fitted values x/y, 7-11 per-row d0 d1 d2 rhs_x rhs_y,
 // 12-14 FP64 Cholesky factors of the fallback solve, 15 interval reciprocals
@@ -783,6 +805,20 @@ __device__ void spline_at(int n, const double* xs, const double* g, const double
   der = in_der(k, t);
 }
 
+// MOVE_SHOCK (MOVE_SHOCK.jl:29-49) of point i by its shock speed (spx, spy): the solution's
+// points by the accumulator weight, the stage points (on_S false) by the stage weight
+__device__ __forceinline__ void move_shock_point(const hymor_config& c, const ShockPts& pS, const ShockPts& pts,
+                                                 bool on_S, double cY, double cS, double dt, double spx,
+                                                 double spy, int i) {
+  const double wS = cS * dt * c.relaxation, wY = cY * dt * c.relaxation;
+  pS.x[i] = pS.x[i] + spx * wS;
+  pS.y[i] = pS.y[i] + spy * wS;
+  if (!on_S) {
+    pts.x[i] = pts.x[i] + spx * wY;
+    pts.y[i] = pts.y[i] + spy * wY;
+  }
+}
+
 __global__ void __launch_bounds__(128) k_shock_columns(ColArgs A) {
   const hymor_config& c = A.cfg;
   const int nchi = c.nchi, neta = c.neta;
@@ -897,15 +933,31 @@ __global__ void __launch_bounds__(128) k_shock_columns(ColArgs A) {
     A.p[i1] = 3 * A.p[g0] - 3 * A.p[im1] + p_2;
     for (int v = 0; v < 4; ++v) arr[v][i2] = 3 * arr[v][i1] - 3 * arr[v][g0] + arr[v][im1];
   }
-  // MOVE_SHOCK (MOVE_SHOCK.jl:29-49); the symmetry copy pts_x[1] -> pts_x[0] runs in k_bc_edges
-  if (A.move) {
-    const double wS = A.cS * dt * c.relaxation, wY = A.cY * dt * c.relaxation;
-    A.pS.x[i] = A.pS.x[i] + spx * wS;
-    A.pS.y[i] = A.pS.y[i] + spy * wS;
-    if (!A.on_S) {
-      A.pts.x[i] = A.pts.x[i] + spx * wY;
-      A.pts.y[i] = A.pts.y[i] + spy * wY;
-    }
+  // MOVE_SHOCK; the symmetry copy pts_x[1] -> pts_x[0] runs in k_bc_edges
+  if (A.move) move_shock_point(c, A.pS, A.pts, A.on_S, A.cY, A.cS, dt, spx, spy, i);
+}
+
+// MOVE_SHOCK on its own, after a k_shock_columns launch without it: one CTA moves every
+// point by the speeds that launch stored, then makes the symmetry copy pts_x[1] -> pts_x[0].
+// It lets the jump and boundary kernels of a step's first stage run before the time step
+// is known (only the move needs dt).
+struct MoveArgs {
+  hymor_config cfg;
+  ShockPts pts, pS;
+  const double *speed_x, *speed_y, *scal;
+  double cY, cS;
+  int on_S, fix;
+};
+
+__global__ void __launch_bounds__(1024) k_move_shock(MoveArgs A) {
+  const int n = A.cfg.nchi;
+  const double dt = A.scal[kDt];
+  for (int i = threadIdx.x; i < n; i += blockDim.x)
+    move_shock_point(A.cfg, A.pS, A.pts, A.on_S, A.cY, A.cS, dt, A.speed_x[i], A.speed_y[i], i);
+  __syncthreads();
+  if (A.fix && threadIdx.x == 0 && n >= 2) {
+    A.pS.x[0] = A.pS.x[1];
+    if (!A.on_S) A.pts.x[0] = A.pts.x[1];
   }
 }
 
@@ -921,18 +973,13 @@ struct BcArgs {
   int on_S;
 };
 
-__global__ void __launch_bounds__(256) k_bc_edges(BcArgs A) {
+// point t of the two edges of one phase (0: chi edges, 1: eta edges)
+__device__ __forceinline__ void bc_edge_point(const BcArgs& A, int phase, int t) {
   const hymor_config& c = A.cfg;
   const int nchi = c.nchi, neta = c.neta, NI = nchi + 2, NJ = neta + 2;
-  const int len = A.phase == 0 ? NJ : NI;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (A.fix_pts && t == 0 && A.phase == 0 && nchi >= 2) {
-    A.pS.x[0] = A.pS.x[1];
-    if (!A.on_S) A.pts.x[0] = A.pts.x[1];
-  }
-  if (t >= 2 * len) return;
+  const int len = phase == 0 ? NJ : NI;
   const int side = t / len, k = t % len;
-  const int edge = 2 * A.phase + side;
+  const int edge = 2 * phase + side;
   const int bc = edge == 0 ? c.bc_chi0 : edge == 1 ? c.bc_chi1 : edge == 2 ? c.bc_eta0 : c.bc_eta1;
   if (bc == HYMOR_BC_SHOCK) return;
   EdgeCtx e{edge, bc, NI, NJ, nchi, neta};
@@ -945,6 +992,18 @@ __global__ void __launch_bounds__(256) k_bc_edges(BcArgs A) {
       A.q.rv[at(e, 0, len - 1)] = A.q.rv[at(e, 0, len - 2)];
     }
   }
+}
+
+// One boundary phase, one thread per edge point: the chi edges, then (second launch) the
+// eta edges, whose corners read the chi ghosts.
+__global__ void __launch_bounds__(256) k_bc_edges(BcArgs A) {
+  const int len = A.phase == 0 ? A.cfg.neta + 2 : A.cfg.nchi + 2;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (A.fix_pts && t == 0 && A.phase == 0 && A.cfg.nchi >= 2) {
+    A.pS.x[0] = A.pS.x[1];
+    if (!A.on_S) A.pts.x[0] = A.pts.x[1];
+  }
+  if (t < 2 * len) bc_edge_point(A, A.phase, t);
 }
 
 // ---------------------------------------------------------------------------
@@ -1737,6 +1796,23 @@ void launch_columns_bc(const DevCtx& d, bool on_S, bool move, double cY, double 
       k_bc_edges<<<(2 * d.NI + 255) / 256, 256, 0, st>>>(ba);
     }
   }
+}
+
+void launch_move_shock(const DevCtx& d, bool on_S, double cY, double cS, cudaStream_t st) {
+  const hymor_config& c = d.cfg;
+  if (!c.shock_enabled) return;
+  MoveArgs a;
+  a.cfg = c;
+  a.pts = on_S ? d.Sp : d.Yp;
+  a.pS = d.Sp;
+  a.speed_x = d.speed_x;
+  a.speed_y = d.speed_y;
+  a.scal = d.scal;
+  a.cY = cY;
+  a.cS = cS;
+  a.on_S = on_S;
+  a.fix = c.bc_chi0 == HYMOR_BC_SYMMETRY;
+  k_move_shock<<<1, 1024, 0, st>>>(a);
 }
 
 static void launch_shock_bc_impl(const DevCtx& d, bool on_S, bool copy_pts, bool move, double cY, double cS,

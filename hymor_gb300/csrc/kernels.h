@@ -51,6 +51,9 @@ void launch_shock_bc(const DevCtx& d, bool on_S, bool copy_pts, bool move, doubl
 void launch_spline(const DevCtx& d, bool on_S, bool copy_pts, cudaStream_t st);
 void launch_columns_bc(const DevCtx& d, bool on_S, bool move, double cY, double cS, int a_mode, bool do_shock,
                        bool do_bc, cudaStream_t st);
+// MOVE_SHOCK after a launch_columns_bc(.., move = false, ..) with the same on_S, cY, cS:
+// moves the points by the stored shock speeds and makes the symmetry copy
+void launch_move_shock(const DevCtx& d, bool on_S, double cY, double cS, cudaStream_t st);
 // Flux (residual) of tgt into out[4] (masked by the flow cells when feedback is on).
 void launch_flux(const DevCtx& d, bool on_S, double* const out[4], cudaStream_t st);
 // tile_class 0: only tiles whose halo no shock/BC kernel writes; 1: the other tiles.
