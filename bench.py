@@ -15,6 +15,11 @@ With --gpus N > 1 (torchrun) every rank advances its own replica of the case (th
 path has no cross-GPU exchange); value = all ranks' cell-stages / max rank time.
 --impl reference times the CPU restatement of the reference path (the oracle,
 OpenMP over every host core) on the same workload.
+
+The line also carries "matvec": the second benchmark of the 800 x 400 case, the
+linearised-residual (stencil-block Jacobian) matvec applied to 64 seeded unit-norm
+vectors, batched in one launch and as 64 one-vector launches, against the FP64 and the
+HBM roofline, with the Jacobian assembly time and the oracle's matvec beside it.
 """
 from __future__ import annotations
 
@@ -38,6 +43,8 @@ CELLS = NCHI * NETA
 STAGES = 4
 BYTES_PER_CELL_STAGE = 216   # algorithmic bytes of residual + RK4 stage (2-D CPG)
 FLUSH_BYTES = 512 << 20
+MATVEC_VECTORS = 64          # seeded unit-norm perturbation vectors of the matvec benchmark
+MATVEC_FLOP = 288            # 144 FMA per cell-matvec (9 neighbour blocks of 4 x 4)
 METRIC = "Mcell-RK4-stages/s"
 UNIT = "Mcell-stage/s"
 
@@ -82,7 +89,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except OSError:
@@ -178,6 +185,127 @@ def cpu_baseline_sample(cs, budget_s: float = 12.0):
             "sample": f"{steps} RK4 steps of the {NCHI}x{NETA} cylinder ({el:.1f} s)"}
 
 
+def matvec_bytes(k: int) -> float:
+    """Algorithmic bytes per cell-matvec with k vectors per launch: the 144 coefficients
+    (1152 B) once per launch, x and y (64 B) per vector."""
+    return (1152 + 64 * k) / k
+
+
+def matvec_numbers(sol, cs, fp64_peak_tflops: float, hbm_gbs: float, cpu: bool, reps: int = 3):
+    """The linearised-residual matvec of the 800 x 400 case on 64 seeded unit-norm vectors
+    (numpy PCG64, seed 2): one batched launch against 64 one-vector launches (device time,
+    CUDA events on the library stream; the 369 MB of Jacobian blocks and the 655 MB of
+    vectors exceed L2, so no flush is needed), the device Jacobian assembly it needs
+    (hymor_linearize: 37 residual evaluations and the scatter, host clock), and the
+    oracle's single-vector matvec on the host."""
+    import torch
+    from hymor_gb300._lib import dp
+    L, h = sol.ctx.L, sol.ctx.h
+    t0 = time.perf_counter()
+    sol.ctx.check(L.hymor_linearize(h))
+    jac_s = time.perf_counter() - t0
+    k, n = MATVEC_VECTORS, 4 * CELLS
+    rng = np.random.Generator(np.random.PCG64(2))
+    X = rng.standard_normal((k, n))
+    X /= np.linalg.norm(X, axis=1, keepdims=True)
+    dX = torch.from_numpy(X.reshape(-1)).cuda()
+    dY = torch.empty_like(dX)
+    torch.cuda.synchronize()
+    xp, yp = ctypes.c_void_p(dX.data_ptr()), ctypes.c_void_p(dY.data_ptr())
+    ms = ctypes.c_float()
+    sol.ctx.check(L.hymor_bench_matvec(h, k, xp, yp, 0, 0, 1, ctypes.byref(ms)))  # warm-up
+    sol.ctx.check(L.hymor_bench_matvec(h, k, xp, yp, 0, 0, reps, ctypes.byref(ms)))
+    t_b = ms.value / 1e3 / reps
+    sol.ctx.check(L.hymor_bench_matvec(h, k, xp, yp, 0, 1, reps, ctypes.byref(ms)))
+    t_p = ms.value / 1e3 / reps
+    sol.ctx.check(L.hymor_bench_matvec(h, k, xp, yp, 1, 0, reps, ctypes.byref(ms)))
+    t_t = ms.value / 1e3 / reps
+    cell_mv = CELLS * k
+
+    def roof(t, kk):
+        fl = cell_mv * MATVEC_FLOP / t / 1e12
+        gbs = cell_mv * matvec_bytes(kk) / t / 1e9
+        return {"bound": "fp64", "achieved_tflops": fl, "peak_tflops": fp64_peak_tflops,
+                "frac": fl / fp64_peak_tflops, "hbm_algorithmic_gbs": gbs, "hbm_peak_gbs": hbm_gbs,
+                "hbm_frac": gbs / hbm_gbs, "bytes_per_cell_matvec": matvec_bytes(kk),
+                "flop_per_cell_matvec": MATVEC_FLOP}
+
+    out = {"workload": f"linearised-residual matvec, {k} seeded unit-norm vectors x {n} ({NCHI}x{NETA})",
+           "vectors": k, "batched_ms": t_b * 1e3, "plain_ms": t_p * 1e3, "transpose_batched_ms": t_t * 1e3,
+           "batched_speedup": t_p / t_b,
+           "per_vector_us": {"batched": t_b / k * 1e6, "plain": t_p / k * 1e6},
+           "roofline": roof(t_b, k), "plain_roofline": roof(t_p, 1),
+           "jacobian_assembly_s": jac_s, "gpu_launches": {"batched": reps, "plain": reps * k}}
+    if cpu:
+        from oracle import oracle as O
+        coef = np.empty(CELLS * 144)
+        sol.ctx.check(L.hymor_jacobian_get(h, dp(coef)))
+        o = O.Oracle(cs)
+        o.matvec(coef, X[0])  # warm-up
+        t0, nv = time.perf_counter(), 0
+        while nv < 3:
+            o.matvec(coef, X[nv])
+            nv += 1
+        el = (time.perf_counter() - t0) / nv
+        out["cpu_baseline"] = {"ms_per_vector": el * 1e3, "cores": 1, "kind": "port",
+                               "sample": f"{nv} vectors through the oracle's stencil matvec"}
+    del dX, dY
+    out["propagator"] = propagator_numbers(fp64_peak_tflops)
+    return out
+
+
+def propagator_numbers(fp64_peak_tflops: float, nchi: int = 100, neta: int = 80, k: int = 64,
+                       nsteps: int = 50, order: int = 5):
+    """Batched against one-vector propagation on the small cylinder (100 x 80, where one
+    matvec is ~2 us of FP64 work and the one-vector path is bound by latency): 50 Taylor
+    steps of degree 5 (250 matvecs) of exp(L dt), the building block of the Krylov solves,
+    for 64 seeded vectors (seed 3) in one call against 64 one-vector calls; host clock
+    around a device synchronisation."""
+    import torch
+    from hymor_gb300 import case as C
+    from hymor_gb300 import solver as S
+    cfg = C.cylinder_config(nchi, neta)
+    sol = S.Solution(C.initial_state(cfg))
+    L, h = sol.ctx.L, sol.ctx.h
+    sol.ctx.check(L.hymor_linearize(h))
+    dt = ctypes.c_double()
+    sol.ctx.check(L.hymor_cfl_timestep(h, ctypes.byref(dt)))
+    n = 4 * nchi * neta
+    rng = np.random.Generator(np.random.PCG64(3))
+    X = rng.standard_normal((k, n))
+    X /= np.linalg.norm(X, axis=1, keepdims=True)
+    dX = torch.from_numpy(X.reshape(-1)).cuda()
+    dY = torch.empty_like(dX)
+    xp, yp = dX.data_ptr(), dY.data_ptr()
+
+    def batched():
+        sol.ctx.check(L.hymor_expm_apply_dev(h, k, dt.value, nsteps, order, ctypes.c_void_p(xp),
+                                             ctypes.c_void_p(yp), 0))
+
+    def plain():
+        for v in range(k):
+            sol.ctx.check(L.hymor_expm_apply_dev(h, 1, dt.value, nsteps, order, ctypes.c_void_p(xp + 8 * n * v),
+                                                 ctypes.c_void_p(yp + 8 * n * v), 0))
+
+    res = {}
+    for name, fn in (("batched", batched), ("plain", plain)):
+        fn()  # warm-up (scratch allocation)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        res[name] = time.perf_counter() - t0
+    sol.close()
+    flop = float(nsteps * order) * nchi * neta * MATVEC_FLOP * k
+    return {"workload": f"exp(L dt): {nsteps} Taylor steps of degree {order}, {k} vectors x {n} ({nchi}x{neta})",
+            "batched_s": res["batched"], "plain_s": res["plain"],
+            "batched_speedup": res["plain"] / res["batched"],
+            "per_vector_ms": {"batched": res["batched"] / k * 1e3, "plain": res["plain"] / k * 1e3},
+            "fp64_frac": {"batched": flop / res["batched"] / 1e12 / fp64_peak_tflops,
+                          "plain": flop / res["plain"] / 1e12 / fp64_peak_tflops},
+            "gpu_launches": {"batched": 1, "plain": k}}
+
+
 def run_reference(args, world, rank):
     """--impl reference: the reference's CPU path (restated, the oracle) on host cores."""
     if rank != 0:
@@ -187,21 +315,26 @@ def run_reference(args, world, rank):
     threads = os.cpu_count() or 1
     O.lib().orc_set_threads(threads)
     o = O.Oracle(cs)
-    for _ in range(args.warmup):
+    for _ in range(min(args.warmup, 3)):
         o.advect(1)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
+    # a bounded sample: the requested steps, or as many as fit in ~60 s of host time
+    t0, done = time.perf_counter(), 0
+    while done < args.steps:
         o.advect(1)
+        done += 1
+        if time.perf_counter() - t0 > 60.0:
+            break
     el = time.perf_counter() - t0
-    v = CELLS * STAGES * args.steps / el / 1e6
+    v = CELLS * STAGES * done / el / 1e6
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": el / done * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"shock-fitted CPG cylinder {NCHI}x{NETA}, M5 Re1e4, residual + RK4 step",
                    "cells": CELLS, "stages_per_step": STAGES, "parallelism": "cpu"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{args.steps} RK4 steps of the {NCHI}x{NETA} cylinder"},
+                         "sample": f"{done} of the {args.steps} requested RK4 steps of the {NCHI}x{NETA} "
+                                   f"cylinder ({el:.1f} s)"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference is Julia (not installable here); its hot path restated in C++ "
                 "(oracle/hymor_oracle.cpp) is timed instead",
@@ -213,11 +346,13 @@ def run_reference(args, world, rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=60)
-    ap.add_argument("--warmup", type=int, default=5)
+    # 1000 timed steps (~0.6 s of device time) let the clock sampler see the timed region
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="hymor", choices=["hymor", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=100)
+    ap.add_argument("--no-matvec", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_env()
@@ -320,6 +455,9 @@ def main():
             line["cpu_baseline"] = cpu_baseline_sample(cs)
         elif world > 1:
             line["cpu_baseline"] = None
+        if not args.no_matvec:
+            line["matvec"] = matvec_numbers(sol, cs, fp64_peak.value, hbm,
+                                            cpu=not args.no_cpu_baseline and world == 1)
         print(json.dumps(line), flush=True)
     sol.close()
     if dist is not None:

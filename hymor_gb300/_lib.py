@@ -34,7 +34,7 @@ EXPORTS = [
     "hymor_memcpy_h2d", "hymor_memcpy_d2h", "hymor_bench_steps", "hymor_dot_dev",
     "hymor_krylov_orthogonalize", "hymor_krylov_rotate", "hymor_block4_apply_dev", "hymor_memcpy_d2d",
     "hymor_expm_apply_dev_noalloc", "hymor_step_kernels", "hymor_fp64_peak",
-    "hymor_profile_phases", "hymor_advect",
+    "hymor_profile_phases", "hymor_advect", "hymor_bench_matvec",
 ]
 
 
@@ -83,6 +83,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "hymor_jacobian_set": [vp, dp],
         "hymor_matvec": [vp, i, dp, dp, i],
         "hymor_matvec_dev": [vp, i, vp, vp, i],
+        "hymor_bench_matvec": [vp, i, vp, vp, i, i, i, ctypes.POINTER(ctypes.c_float)],
         "hymor_expm_apply": [vp, i, d, i, i, dp, dp, i],
         "hymor_expm_apply_dev": [vp, i, d, i, i, vp, vp, i],
         "hymor_expm_apply_dev_noalloc": [vp, i, d, i, i, vp, vp, i],

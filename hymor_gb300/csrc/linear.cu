@@ -142,13 +142,20 @@ struct MvArgs {
   int k, transpose;
 };
 
-// y = scale * A x (or A^T x) for the cells of this thread (grid-stride), acc += c_acc y.
+// y = scale * A x (or A^T x), acc += c_acc y. The work items are (cell, chunk of
+// kVecChunk vectors) pairs, cell fastest, over a grid-stride loop: a batch of vectors on
+// a small grid still spreads over every SM (a 100 x 80 grid is 8000 cells, 64 vectors are
+// 16 chunks of it), and neighbouring threads read neighbouring cells.
 __device__ __forceinline__ void matvec_cells(const MvArgs& a) {
   const long N = a.N;
   const long n4 = 4 * N;
-  for (long m = blockIdx.x * (long)blockDim.x + threadIdx.x; m < N; m += (long)gridDim.x * blockDim.x) {
+  const int chunks = (a.k + kVecChunk - 1) / kVecChunk;
+  const long items = N * chunks;
+  for (long w = blockIdx.x * (long)blockDim.x + threadIdx.x; w < items; w += (long)gridDim.x * blockDim.x) {
+    const long m = w % N;
     const int i = (int)(m % a.w.nchi), j = (int)(m / a.w.nchi);
-    for (int v0 = 0; v0 < a.k; v0 += kVecChunk) {
+    {
+      const int v0 = (int)(w / N) * kVecChunk;
       const int nv = min(kVecChunk, a.k - v0);
       double y[kVecChunk][4];
 #pragma unroll
@@ -367,7 +374,7 @@ void launch_matvec(const DevCtx& d, int k, const double* X, double* Y, int trans
   a.N = d.N;
   a.k = k;
   a.transpose = transpose;
-  k_matvec<<<grid_for(d.N, kMvThreads), kMvThreads, 0, st>>>(a);
+  k_matvec<<<grid_for(d.N * ((k + kVecChunk - 1) / kVecChunk), kMvThreads), kMvThreads, 0, st>>>(a);
 }
 
 // POWER_METHOD! (Eigenvalues/ARNOLDI_POWER_GPU.jl:64-82): per step vout = v,
@@ -393,7 +400,7 @@ static void launch_expm_body(const DevCtx& d, int k, double dt, int nsteps, int 
       a.X = src;
       a.Y = dst;
       a.c_acc = 1.0 / (double)fact;
-      k_matvec<<<grid_for(d.N, kMvThreads), kMvThreads, 0, st>>>(a);
+      k_matvec<<<grid_for(d.N * ((k + kVecChunk - 1) / kVecChunk), kMvThreads), kMvThreads, 0, st>>>(a);
       src = dst;
     }
     k_copy<<<grid_for(n, 256), 256, 0, st>>>(vout, v, n);
@@ -540,7 +547,7 @@ int expm_cooperative(hymor_ctx* ctx, int k, double dt, int nsteps, int order, co
   if (!blocks_per_sm &&
       (r = cuda_check(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_expm_coop, kMvThreads, 0))))
     return r;
-  const long want = (d.N + kMvThreads - 1) / kMvThreads;
+  const long want = (d.N * ((k + kVecChunk - 1) / kVecChunk) + kMvThreads - 1) / kMvThreads;
   const int grid = (int)std::min<long>(want, (long)blocks_per_sm * d.sms);
   MvArgs base;
   base.coef = d.coef;
@@ -650,6 +657,37 @@ int hymor_matvec(hymor_ctx* ctx, int k, const double* X, double* Y, int transpos
   cudaFreeAsync(dy, st);
   if ((r = cuda_check(ctx, cudaGetLastError()))) return r;
   return cuda_check(ctx, cudaStreamSynchronize(st));
+}
+
+int hymor_bench_matvec(hymor_ctx* ctx, int k, const double* dX, double* dY, int transpose, int per_vector,
+                       int reps, float* ms) {
+  if (!ctx || k < 1 || !dX || !dY || reps < 1 || !ms) return HYMOR_ERR_INVALID;
+  DevCtx& d = ctx_dev(ctx);
+  if (!d.coef) return ctx_fail(ctx, HYMOR_ERR_NOT_READY, "no Jacobian: call hymor_linearize or hymor_jacobian_set");
+  cudaStream_t st = ctx_stream(ctx);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int r;
+  if ((r = cuda_check(ctx, cudaEventCreate(&e0)))) return r;
+  if ((r = cuda_check(ctx, cudaEventCreate(&e1)))) {
+    cudaEventDestroy(e0);
+    return r;
+  }
+  const long n4 = 4 * d.N;
+  cudaEventRecord(e0, st);
+  for (int rep = 0; rep < reps; ++rep) {
+    if (per_vector) {
+      for (int v = 0; v < k; ++v) launch_matvec(d, 1, dX + v * n4, dY + v * n4, transpose, 1.0, st);
+    } else {
+      launch_matvec(d, k, dX, dY, transpose, 1.0, st);
+    }
+  }
+  cudaEventRecord(e1, st);
+  r = cuda_check(ctx, cudaEventSynchronize(e1));
+  if (!r) r = cuda_check(ctx, cudaEventElapsedTime(ms, e0, e1));
+  if (!r) r = cuda_check(ctx, cudaGetLastError());
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return r;
 }
 
 int hymor_expm_apply_dev(hymor_ctx* ctx, int k, double dt, int nsteps, int order, const double* dX, double* dY,

@@ -174,6 +174,12 @@ int hymor_jacobian_set(hymor_ctx* ctx, const double* coef);
 int hymor_matvec(hymor_ctx* ctx, int k, const double* X, double* Y, int transpose);
 /* Same on device pointers (no copies). */
 int hymor_matvec_dev(hymor_ctx* ctx, int k, const double* dX, double* dY, int transpose);
+/* Timing of hymor_matvec_dev (no counterpart in the reference): reps repetitions of one
+ * launch over the k vectors (per_vector 0), or of k launches of one vector each
+ * (per_vector 1, the one-vector path); *ms = their device time, CUDA events on the
+ * context stream. */
+int hymor_bench_matvec(hymor_ctx* ctx, int k, const double* dX, double* dY, int transpose, int per_vector,
+                       int reps, float* ms);
 /* Y = (Σ_{j<=order} (A dt)^j / j!)^nsteps X for k vectors: POWER_METHOD!
  * (Eigenvalues/ARNOLDI_POWER_GPU.jl:64-82); transpose uses (A dt)ᵀ (EXPONENTIAL!,
  * Transient_growth_downstream/CONSTRUCT_C.jl:78-111). Host pointers. */
