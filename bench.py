@@ -306,6 +306,40 @@ def propagator_numbers(fp64_peak_tflops: float, nchi: int = 100, neta: int = 80,
             "gpu_launches": {"batched": 1, "plain": k}}
 
 
+def solve_numbers(nchi: int = 100, neta: int = 80, n_modes: int = 4, T_ref: float = 0.5, tol: float = 1e-8,
+                  block: int = 8, steps: int = 20, maxit: int = 200):
+    """Solve level (--solve, minutes): the n_modes eigenvalues of largest magnitude of
+    exp(L T_ref) on the cylinder (after `steps` RK4 steps of the synthetic start), by the
+    block Krylov-Schur (`block` vectors per batched propagation) and by the one-vector
+    Krylov-Schur, both to Ritz residual tol or maxit restarts, from start vectors on the
+    flow cells (the masked operator's other directions only carry the trivial eigenvalue
+    0); host clock around each solve. Reports the residuals reached: on a clustered
+    spectrum neither solve may reach tol within maxit."""
+    from hymor_gb300 import case as C
+    from hymor_gb300 import solver as S
+    cfg = C.cylinder_config(nchi, neta)
+    sol = S.Solution(C.initial_state(cfg))
+    S.ADVECT_FLOW(sol, steps)
+    _, Lop = S.LINEARIZE_L(sol)
+    lam_b, info_b = S.EIGENVALUES(Lop, sol, n_modes, T_ref=T_ref, tol=tol, block=block, flow_start=True,
+                                  maxit=maxit)
+    lam_p, info_p = S.EIGENVALUES(Lop, sol, n_modes, T_ref=T_ref, tol=tol, flow_start=True, maxit=maxit)
+    scale = float(np.max(np.abs(lam_p)))
+    agree = max(float(np.min(np.abs(lam_p - a))) for a in lam_b) / scale
+    sol.close()
+    rel = {k: [float(r) for r in i["resid"] / np.abs(i["mu"])] for k, i in (("batched", info_b), ("plain", info_p))}
+    return {"workload": f"EIGENVALUES, {n_modes} modes of exp(L {T_ref}) ({info_p['timesteps']} Taylor steps of "
+                        f"degree 5), cylinder {nchi}x{neta}, Ritz residual {tol:g}",
+            "batched_s": info_b["seconds"], "plain_s": info_p["seconds"],
+            "batched_speedup": info_p["seconds"] / info_b["seconds"], "block": block,
+            "propagations": {"batched": info_b["nops"], "plain": info_p["nops"]},
+            "s_per_vector_propagation": {"batched": info_b["seconds"] / info_b["nops"],
+                                         "plain": info_p["seconds"] / info_p["nops"]},
+            "resid_rel": rel, "converged": {k: bool(max(v) <= tol) for k, v in rel.items()},
+            "eigenvalues_agree_rel": agree,
+            "eigenvalues": [[float(np.real(a)), float(np.imag(a))] for a in lam_p]}
+
+
 def run_reference(args, world, rank):
     """--impl reference: the reference's CPU path (restated, the oracle) on host cores."""
     if rank != 0:
@@ -353,6 +387,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--no-matvec", action="store_true")
+    ap.add_argument("--solve", action="store_true", help="add the solve-level timing (minutes)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_env()
@@ -458,6 +493,8 @@ def main():
         if not args.no_matvec:
             line["matvec"] = matvec_numbers(sol, cs, fp64_peak.value, hbm,
                                             cpu=not args.no_cpu_baseline and world == 1)
+        if args.solve:
+            line["solve"] = solve_numbers()
         print(json.dumps(line), flush=True)
     sol.close()
     if dist is not None:

@@ -121,3 +121,90 @@ def krylov_schur(ctx, n: int, apply_op, nev: int, ncv: int, tol: float = 1e-8, m
     V.free()
     w.free()
     return theta, resid, nops
+
+
+def block_krylov_schur(ctx, n: int, apply_block, nev: int, ncv: int, block: int, tol: float = 1e-8,
+                       maxit: int = 200, seed: int = 3, symmetric: bool = False, start_mask=None):
+    """Block Krylov-Schur: the Krylov basis grows `block` vectors at a time, so that every
+    operator application propagates a whole block in one batched call (Zhou and Saad,
+    "Block Krylov-Schur method for large symmetric eigenvalue problems", Numer. Algorithms 47
+    (2008) 341-359; the non-symmetric restart is Stewart's, as in krylov_schur).
+
+    apply_block(src_addr, dst_addr, k) writes OP(v_i) for k contiguous device vectors of
+    length n. Each new vector is orthogonalised (classical Gram-Schmidt, twice, on the
+    device) against the basis and the block's earlier vectors, so the projected matrix is
+    block upper Hessenberg with `block` subdiagonals: A V[:, :m] = V[:, :m+block] H.
+    Returns (theta, resid, nops) like krylov_schur; nops counts single-vector
+    applications (block per call). start_mask (length n, optional) multiplies the random
+    start block, e.g. to keep it on a subspace the operator leaves invariant."""
+    b = int(block)
+    if b < 1 or not (0 < nev < ncv) or ncv < nev + 2 * b:
+        raise HymorError(-1, "need block >= 1 and 0 < nev, nev + 2 block <= ncv")
+    L = ctx.L
+    cap = ncv + 2 * b  # a cycle may grow up to block - 1 columns past ncv
+    V = DeviceBuffer(ctx, 8 * n * cap)
+    W = DeviceBuffer(ctx, 8 * n * b)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    X0 = rng.standard_normal((b, n))
+    if start_mask is not None:
+        X0 *= np.asarray(start_mask, dtype=np.float64)[None, :]
+    W.upload(X0.ravel())
+    h = np.empty(cap + 2)
+    for i in range(b):  # orthonormal start block
+        ctx.check(L.hymor_krylov_orthogonalize(ctx.h, n, i, V.ptr, n, W.addr(i * n), dp(h), i))
+        if h[i] == 0:
+            raise HymorError(-3, "start block is rank deficient")
+    H = np.zeros((cap, cap))
+    p = 0
+    nops = 0
+    theta = resid = None
+    for it in range(maxit):
+        m = p + b * max(1, -(-(ncv - p) // b))
+        for j in range(p, m, b):
+            apply_block(V.addr(j * n), W.addr(), b)
+            nops += b
+            for i in range(b):
+                J = j + b + i  # orthonormal basis vectors so far
+                ctx.check(L.hymor_krylov_orthogonalize(ctx.h, n, J, V.ptr, n, W.addr(i * n), dp(h), J))
+                H[:J, j + i] = h[:J]
+                H[J, j + i] = h[J]
+                if h[J] == 0:
+                    raise HymorError(-3, "Krylov breakdown (invariant subspace found)")
+        Hm = H[:m, :m]
+        B = H[m:m + b, :m]
+        if symmetric:
+            vals, Y = np.linalg.eigh(0.5 * (Hm + Hm.T))
+        else:
+            vals, Y = np.linalg.eig(Hm)
+        order = np.argsort(-np.abs(vals))
+        vals, Y = vals[order], Y[:, order]
+        if not symmetric:
+            Y = Y / np.linalg.norm(Y, axis=0)
+        res = np.linalg.norm(B @ Y, axis=0)
+        theta, resid = vals[:nev], res[:nev]
+        if np.all(resid <= tol * np.abs(theta)):
+            break
+        # restart: keep the wanted Schur vectors, leave room for the residual block
+        keep = min(nev + max(2, (m - nev) // 2), m - b)
+        if symmetric:
+            T = np.diag(vals[:keep])
+            Q = Y[:, :keep]
+        else:
+            thr = np.sort(np.abs(vals))[::-1][keep - 1]
+            Tfull, Qfull, sdim = sla.schur(Hm, output="real", sort=lambda re, im: np.hypot(re, im) >= thr * (1 - 1e-12))
+            keep = max(1, min(sdim, m - b))
+            if keep < m and Tfull[keep, keep - 1] != 0:
+                keep -= 1  # never split a 2 x 2 block of a complex pair
+            T = Tfull[:keep, :keep]
+            Q = Qfull[:, :keep]
+        ctx.check(L.hymor_krylov_rotate(ctx.h, n, m, keep, V.ptr, n, dp(np.asfortranarray(Q))))
+        # the residual block becomes columns keep .. keep + b - 1 (keep + b <= m: no overlap)
+        ctx.check(L.hymor_memcpy_d2d(ctx.h, V.addr(keep * n), V.addr(m * n), 8 * n * b))
+        Hn = np.zeros_like(H)
+        Hn[:keep, :keep] = T
+        Hn[keep:keep + b, :keep] = B @ Q
+        H = Hn
+        p = keep
+    V.free()
+    W.free()
+    return theta, resid, nops

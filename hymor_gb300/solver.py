@@ -210,25 +210,52 @@ def _expm_op(s: Solution, dt: float, nsteps: int, order: int, transpose: int = 0
     return apply
 
 
+def _expm_block_op(s: Solution, dt: float, nsteps: int, order: int, transpose: int = 0):
+    """The propagator over k contiguous device vectors in one batched call."""
+    L, h = s.ctx.L, s.ctx.h
+
+    def apply(src, dst, k):
+        s.ctx.check(L.hymor_expm_apply_dev(h, int(k), float(dt), int(nsteps), int(order), src, dst, int(transpose)))
+    return apply
+
+
 def EIGENVALUES(L: LinearOperatorGPU, s: Solution, n_modes: int, T_ref: float = 0.5, ncv: int | None = None,
-                tol: float = 1e-8, order: int = 5, method: str = "device", seed: int = 3, maxit: int = 300):
+                tol: float = 1e-8, order: int = 5, method: str = "device", seed: int = 3, maxit: int = 300,
+                block: int = 1, flow_start: bool = False):
     """EIGENVALUES_GPU_ARNOLDI (Eigenvalues/EIGENVALUES.jl:112-205): the n_modes eigenvalues of
     largest magnitude of exp(L T_ref) (Taylor-`order` steps of the CFL dt), mapped back as
     lambda = log(mu) / (dt * timesteps).
 
     method "device": Krylov-Schur with the basis in HBM (hymor_gb300/krylov.py).
     method "host":   the reference's structure, ARPACK on the host calling one GPU
-                     propagation per Krylov vector with a host round trip."""
+                     propagation per Krylov vector with a host round trip.
+    block > 1 (device): block Krylov-Schur, `block` vectors propagated per batched call.
+    flow_start: random start vectors that vanish outside the flow cells. The residual is
+    masked by the flow cells, so the operator has zero rows there and leaves the flow-cell
+    subspace invariant; the other cells only add the trivial eigenvalue mu = 1 (lambda = 0),
+    which this excludes exactly."""
     import time
     dt = CFL_TIMESTEP(s)
     timesteps = int(round(T_ref / dt))
     n = 4 * s.N
-    ncv = ncv or max(2 * n_modes + 1, 20)
+    ncv = ncv or max(2 * n_modes + 1, 20, n_modes + 4 * block)
+    mask = None
+    if flow_start and s.cfg.shock_enabled and s.cfg.shock_feedback:
+        st = s.get_state()
+        flow = (np.arange(1, s.cfg.neta + 1)[None, :] < st["cell_idx"][:, None]).ravel(order="F")
+        mask = np.tile(flow.astype(np.float64), 4)
     t0 = time.perf_counter()
-    if method == "device":
+    if method == "device" and block > 1:
+        from .krylov import block_krylov_schur
+        mu, resid, nops = block_krylov_schur(s.ctx, n, _expm_block_op(s, dt, timesteps, order), n_modes, ncv,
+                                             block, tol=tol, maxit=maxit, seed=seed, start_mask=mask)
+    elif method == "device":
         from .krylov import krylov_schur
+        v0 = None
+        if mask is not None:
+            v0 = np.random.Generator(np.random.PCG64(seed)).standard_normal(n) * mask
         mu, resid, nops = krylov_schur(s.ctx, n, _expm_op(s, dt, timesteps, order), n_modes, ncv, tol=tol,
-                                       maxit=maxit, seed=seed)
+                                       maxit=maxit, seed=seed, v0=v0)
     elif method == "host":
         from scipy.sparse.linalg import LinearOperator, eigs
         count = [0]
@@ -299,15 +326,17 @@ def chu_blocks_from_state(cfg, vol, qflat, cell_idx, norms=(1, 1, 1, 1)):
 
 
 def TRANSIENT_GROWTH_DOWNSTREAM(L: LinearOperatorGPU, s: Solution, n_modes: int, T: float, ncv: int | None = None,
-                                tol: float = 1e-8, order: int = 5, seed: int = 4, maxit: int = 300):
+                                tol: float = 1e-8, order: int = 5, seed: int = 4, maxit: int = 300,
+                                block: int = 1):
     """TRANSIENT_GROWTH_DOWNSTREAM (TRANSIENT_GROWTH_DOWNSTREAM.jl:34-153): optimal energy gains
     G(T), the largest eigenvalues of exp(Lᵀ T) R'MR exp(L T) x = G R'M^R x. The generalised
     symmetric problem is reduced with the per-cell Cholesky factor of R'M^R (D = K Kᵀ) to
     K^{-1} Pᵀ C0 P K^{-ᵀ} y = G y and solved by Krylov-Schur (Lanczos with full
     reorthogonalisation) on the device; the forward propagation P and its adjoint Pᵀ are
-    Taylor-`order` steps of dt = T / round(T / dt_CFL)."""
+    Taylor-`order` steps of dt = T / round(T / dt_CFL). block > 1: block Krylov-Schur, the
+    operator applied to `block` vectors per batched call."""
     import time
-    from .krylov import DeviceBuffer, krylov_schur
+    from .krylov import DeviceBuffer, block_krylov_schur, krylov_schur
     dt_cfl = CFL_TIMESTEP(s)
     n_t = int(round(T / dt_cfl))
     dt = T / n_t
@@ -319,18 +348,23 @@ def TRANSIENT_GROWTH_DOWNSTREAM(L: LinearOperatorGPU, s: Solution, n_modes: int,
     bufs = [DeviceBuffer(s.ctx, 8 * s.N * 16) for _ in range(3)]
     for b, arr in zip(bufs, (C0, Kinv, KinvT)):
         b.upload(np.ascontiguousarray(arr.reshape(-1)))
-    t1, t2 = DeviceBuffer(s.ctx, 8 * n), DeviceBuffer(s.ctx, 8 * n)
+    t1, t2 = DeviceBuffer(s.ctx, 8 * n * block), DeviceBuffer(s.ctx, 8 * n * block)
     Lh, h = s.ctx.L, s.ctx.h
 
-    def apply(src, dst):
-        s.ctx.check(Lh.hymor_block4_apply_dev(h, 1, bufs[2].ptr, src, t1.ptr))            # x = K^-T y
-        s.ctx.check(Lh.hymor_expm_apply_dev(h, 1, dt, n_t, order, t1.ptr, t2.ptr, 0))      # P x
-        s.ctx.check(Lh.hymor_block4_apply_dev(h, 1, bufs[0].ptr, t2.ptr, t1.ptr))          # C0 P x
-        s.ctx.check(Lh.hymor_expm_apply_dev(h, 1, dt, n_t, order, t1.ptr, t2.ptr, 1))      # Pᵀ C0 P x
-        s.ctx.check(Lh.hymor_block4_apply_dev(h, 1, bufs[1].ptr, t2.ptr, dst))             # K^-1 (...)
-    ncv = ncv or max(2 * n_modes + 1, 16)
+    def apply_k(src, dst, k):
+        s.ctx.check(Lh.hymor_block4_apply_dev(h, k, bufs[2].ptr, src, t1.ptr))            # x = K^-T y
+        s.ctx.check(Lh.hymor_expm_apply_dev(h, k, dt, n_t, order, t1.ptr, t2.ptr, 0))      # P x
+        s.ctx.check(Lh.hymor_block4_apply_dev(h, k, bufs[0].ptr, t2.ptr, t1.ptr))          # C0 P x
+        s.ctx.check(Lh.hymor_expm_apply_dev(h, k, dt, n_t, order, t1.ptr, t2.ptr, 1))      # Pᵀ C0 P x
+        s.ctx.check(Lh.hymor_block4_apply_dev(h, k, bufs[1].ptr, t2.ptr, dst))             # K^-1 (...)
+    ncv = ncv or max(2 * n_modes + 1, 16, n_modes + 4 * block)
     t0 = time.perf_counter()
-    gains, resid, nops = krylov_schur(s.ctx, n, apply, n_modes, ncv, tol=tol, maxit=maxit, seed=seed, symmetric=True)
+    if block > 1:
+        gains, resid, nops = block_krylov_schur(s.ctx, n, apply_k, n_modes, ncv, block, tol=tol, maxit=maxit,
+                                                seed=seed, symmetric=True)
+    else:
+        gains, resid, nops = krylov_schur(s.ctx, n, lambda a, b: apply_k(a, b, 1), n_modes, ncv, tol=tol,
+                                          maxit=maxit, seed=seed, symmetric=True)
     elapsed = time.perf_counter() - t0
     for b in bufs + [t1, t2]:
         b.free()

@@ -74,6 +74,30 @@ def test_transient_growth_device_vs_oracle(require_gpu):
     assert np.allclose(np.sort(G)[::-1], Go, rtol=1e-6, atol=0)
 
 
+def test_block_eigenvalues_match_single_vector(require_gpu):
+    """Block Krylov-Schur (4 vectors per batched propagation) finds the same eigenvalues
+    as the single-vector Krylov-Schur, to 1e-8 of the spectrum's scale."""
+    cfg, cs, sol, orc = _setup(30, 20)
+    _, L = S.LINEARIZE_L(sol)
+    lam1, info1 = S.EIGENVALUES(L, sol, 4, T_ref=0.02, ncv=24, tol=1e-11)
+    lam4, info4 = S.EIGENVALUES(L, sol, 4, T_ref=0.02, ncv=28, tol=1e-10, block=4)
+    scale = np.max(np.abs(lam1))
+    for a in lam4:
+        assert np.min(np.abs(lam1 - a)) <= 1e-8 * scale
+    assert np.all(info4["resid"] <= 1e-10 * np.abs(info4["mu"]))
+    assert info4["nops"] % 4 == 0
+
+
+def test_block_transient_growth_matches_single_vector(require_gpu):
+    """Block Lanczos (Krylov-Schur, symmetric) on the transient-growth operator gives the
+    single-vector gains to 1e-6."""
+    cfg, cs, sol, orc = _setup(24, 24)
+    _, L = S.LINEARIZE_L(sol)
+    G1, _ = S.TRANSIENT_GROWTH_DOWNSTREAM(L, sol, 2, 0.01, ncv=16, tol=1e-11)
+    G4, _ = S.TRANSIENT_GROWTH_DOWNSTREAM(L, sol, 2, 0.01, ncv=20, tol=1e-10, block=4)
+    assert np.allclose(np.sort(G4)[::-1], np.sort(G1)[::-1], rtol=1e-6, atol=0)
+
+
 def test_propagator_adjoint_identity(require_gpu):
     """<P x, y> = <x, Pᵀ y> for the Taylor propagator and its adjoint (the dot-product test)."""
     cfg, cs, sol, orc = _setup(30, 20, steps=5)
