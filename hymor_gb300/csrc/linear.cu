@@ -29,6 +29,17 @@ void launch_shock_bc_flags(const DevCtx& d, bool on_S, bool copy_pts, bool do_sh
 namespace {
 
 constexpr int kMvThreads = 256;
+
+// Threads per block of a matvec over `items` work items: 256, or fewer when that would
+// leave SMs idle. One vector on a 100 x 80 grid is 8000 items: in 256-thread blocks they
+// sit on 32 SMs, whose FP64 pipes then bound the matvec; in 64-thread blocks they spread
+// over 125.
+int mv_threads(long items, int sms) {
+  if (items >= (long)sms * kMvThreads) return kMvThreads;
+  const long per_sm = (items + sms - 1) / sms;
+  const long t = ((per_sm + 31) / 32) * 32;
+  return (int)(t < 32 ? 32 : t);
+}
 constexpr int kVecChunk = 4;
 
 struct Wrap {
@@ -374,7 +385,9 @@ void launch_matvec(const DevCtx& d, int k, const double* X, double* Y, int trans
   a.N = d.N;
   a.k = k;
   a.transpose = transpose;
-  k_matvec<<<grid_for(d.N * ((k + kVecChunk - 1) / kVecChunk), kMvThreads), kMvThreads, 0, st>>>(a);
+  const long items = d.N * ((k + kVecChunk - 1) / kVecChunk);
+  const int th = mv_threads(items, d.sms);
+  k_matvec<<<grid_for(items, th), th, 0, st>>>(a);
 }
 
 // POWER_METHOD! (Eigenvalues/ARNOLDI_POWER_GPU.jl:64-82): per step vout = v,
@@ -383,6 +396,8 @@ void launch_matvec(const DevCtx& d, int k, const double* X, double* Y, int trans
 static void launch_expm_body(const DevCtx& d, int k, double dt, int nsteps, int order, double* v, double* t1,
                              double* t2, double* vout, int transpose, cudaStream_t st) {
   const long n = 4 * d.N * (long)k;
+  const long items = d.N * ((k + kVecChunk - 1) / kVecChunk);
+  const int th = mv_threads(items, d.sms);
   MvArgs a;
   a.coef = d.coef;
   a.w = make_wrap(d.cfg);
@@ -400,7 +415,7 @@ static void launch_expm_body(const DevCtx& d, int k, double dt, int nsteps, int 
       a.X = src;
       a.Y = dst;
       a.c_acc = 1.0 / (double)fact;
-      k_matvec<<<grid_for(d.N * ((k + kVecChunk - 1) / kVecChunk), kMvThreads), kMvThreads, 0, st>>>(a);
+      k_matvec<<<grid_for(items, th), th, 0, st>>>(a);
       src = dst;
     }
     k_copy<<<grid_for(n, 256), 256, 0, st>>>(vout, v, n);
@@ -547,7 +562,10 @@ int expm_cooperative(hymor_ctx* ctx, int k, double dt, int nsteps, int order, co
   if (!blocks_per_sm &&
       (r = cuda_check(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_expm_coop, kMvThreads, 0))))
     return r;
-  const long want = (d.N * ((k + kVecChunk - 1) / kVecChunk) + kMvThreads - 1) / kMvThreads;
+  const long items = d.N * ((k + kVecChunk - 1) / kVecChunk);
+  const int th = mv_threads(items, d.sms);
+  const long want = (items + th - 1) / th;
+  // co-resident: blocks of th <= 256 threads need no more than a 256-thread block
   const int grid = (int)std::min<long>(want, (long)blocks_per_sm * d.sms);
   MvArgs base;
   base.coef = d.coef;
@@ -563,7 +581,7 @@ int expm_cooperative(hymor_ctx* ctx, int k, double dt, int nsteps, int order, co
   if ((r = cuda_check(ctx, cudaMemcpyAsync(v, dX, sizeof(double) * n, cudaMemcpyDeviceToDevice, st)))) return r;
   if ((r = cuda_check(ctx, cudaMemcpyAsync(vout, dX, sizeof(double) * n, cudaMemcpyDeviceToDevice, st)))) return r;
   void* args[] = {&base, &nsteps, &order, &v, &t1, &t2, &vout};
-  if ((r = cuda_check(ctx, cudaLaunchCooperativeKernel((const void*)k_expm_coop, grid, kMvThreads, args, 0, st))))
+  if ((r = cuda_check(ctx, cudaLaunchCooperativeKernel((const void*)k_expm_coop, grid, th, args, 0, st))))
     return r;
   return cuda_check(ctx, cudaMemcpyAsync(dY, vout, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
 }
