@@ -148,6 +148,11 @@ struct MvArgs {
   double* Y;
   double* acc;
   double scale, c_acc;
+  // a term of the previous matvec to add into acc first (acc += c_prev acc_prev), or null:
+  // the propagator accumulates each Taylor term one matvec late, so that the first matvec
+  // of a step can read acc as its input without a copy
+  const double* acc_prev;
+  double c_prev;
   Wrap w;
   long N;
   int k, transpose;
@@ -157,7 +162,73 @@ struct MvArgs {
 // kVecChunk vectors) pairs, cell fastest, over a grid-stride loop: a batch of vectors on
 // a small grid still spreads over every SM (a 100 x 80 grid is 8000 cells, 64 vectors are
 // 16 chunks of it), and neighbouring threads read neighbouring cells.
-__device__ __forceinline__ void matvec_cells(const MvArgs& a) {
+// One vector (k = 1): one thread per (cell, output component), the same FMA chain per
+// output as matvec_multi (bit-identical). On GB300 one warp issues one FP64 instruction per
+// ~76 cycles of its SM sub-partition, so a warp per 32 cells (148 FP64 instructions each)
+// would bound a small grid's matvec by its own issue rate; four threads per cell spread the
+// work over four times the warps. The next neighbour block's coefficients and inputs are
+// loaded while the current block's FMAs run.
+__device__ __forceinline__ void matvec_one(const MvArgs& a) {
+  const long N = a.N;
+  for (long w = blockIdx.x * (long)blockDim.x + threadIdx.x; w < 4 * N; w += (long)gridDim.x * blockDim.x) {
+    const long m = w % N;
+    const int comp = (int)(w / N);  // output component (v_out, or v_in of the transpose)
+    const int i = (int)(m % a.w.nchi), j = (int)(m / a.w.nchi);
+    double y = 0;
+    double B[2][4], X[2][4];
+    bool ok[2];
+    auto load = [&](int q, int slot) {
+      const int b = q / 3 - 1, aa = q % 3 - 1;
+      long n, cell;  // input cell, and the cell that owns the block
+      if (!a.transpose) {
+        n = a.w.nbr(i, j, aa, b);
+        cell = m;
+      } else {
+        // m is the input cell of output cell n = m - (aa, b); block slot of (aa, b)
+        n = a.w.nbr(i, j, -aa, -b);
+        cell = n;
+      }
+      ok[slot] = n >= 0;
+      if (n >= 0) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          // row comp of the block (columns e), or column comp of it for the transpose
+          const int plane = a.transpose ? q * 16 + e * 4 + comp : q * 16 + comp * 4 + e;
+          B[slot][e] = a.coef[(long)plane * N + cell];
+          X[slot][e] = a.X[e * N + n];
+        }
+      }
+    };
+    load(0, 0);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      const int c = q & 1;
+      if (q + 1 < 9) load(q + 1, c ^ 1);
+      if (!ok[c]) continue;
+      y = fma(B[c][0], X[c][0], fma(B[c][1], X[c][1], fma(B[c][2], X[c][2], fma(B[c][3], X[c][3], y))));
+    }
+    const double val = a.scale * y;
+    a.Y[comp * N + m] = val;
+    if (a.acc) {
+      double r = a.acc[comp * N + m];
+      if (a.acc_prev) r = fma(a.acc_prev[comp * N + m], a.c_prev, r);
+      a.acc[comp * N + m] = fma(val, a.c_acc, r);
+    }
+  }
+}
+
+// The one-vector path (matvec_one) for grids with fewer cells than 32 per warp slot of 8
+// warps on every SM sub-partition; a larger grid already fills them with one thread per
+// cell (matvec_multi, whose single pass over the 144 coefficients is then cheaper).
+bool mv_one(long N, int k, int sms) { return k == 1 && N < 8L * 32 * 4 * sms; }
+
+// Work items of a matvec over k vectors: (cell, output component) on the one-vector path,
+// (cell, chunk of kVecChunk vectors) otherwise.
+long mv_items(long N, int k, int sms) {
+  return mv_one(N, k, sms) ? 4 * N : N * ((k + kVecChunk - 1) / kVecChunk);
+}
+
+__device__ __forceinline__ void matvec_multi(const MvArgs& a) {
   const long N = a.N;
   const long n4 = 4 * N;
   const int chunks = (a.k + kVecChunk - 1) / kVecChunk;
@@ -216,7 +287,9 @@ __device__ __forceinline__ void matvec_cells(const MvArgs& a) {
           yo[c * N + m] = val;
           if (a.acc) {
             double* ac = a.acc + (long)(v0 + v) * n4;
-            ac[c * N + m] = fma(val, a.c_acc, ac[c * N + m]);
+            double r = ac[c * N + m];
+            if (a.acc_prev) r = fma(a.acc_prev[(long)(v0 + v) * n4 + c * N + m], a.c_prev, r);
+            ac[c * N + m] = fma(val, a.c_acc, r);
           }
         }
       }
@@ -224,31 +297,54 @@ __device__ __forceinline__ void matvec_cells(const MvArgs& a) {
   }
 }
 
-__global__ void __launch_bounds__(kMvThreads) k_matvec(MvArgs a) { matvec_cells(a); }
+// ONE: the one-vector path (its own kernel, so that its registers do not lower the
+// occupancy of the batched path)
+template <bool ONE>
+__device__ __forceinline__ void matvec_cells(const MvArgs& a) {
+  if (ONE) matvec_one(a);
+  else matvec_multi(a);
+}
+
+template <bool ONE>
+__global__ void __launch_bounds__(kMvThreads) k_matvec(MvArgs a) { matvec_cells<ONE>(a); }
 
 // The whole Taylor propagation in one cooperative launch: the blocks are co-resident
 // (cudaLaunchCooperativeKernel) and meet at a grid barrier after every matvec, instead of
 // one kernel per matvec. Same per-cell arithmetic, in the same order, as launch_expm.
+template <bool ONE>
 __global__ void __launch_bounds__(kMvThreads) k_expm_coop(MvArgs base, int nsteps, int order, double* v, double* t1,
                                                           double* t2, double* vout) {
   cg::grid_group grid = cg::this_grid();
   const long n = 4 * base.N * (long)base.k;
   for (int s = 0; s < nsteps; ++s) {
-    const double* src = v;
+    // order >= 2: the first matvec reads vout itself and adds nothing to it, the second
+    // adds the first term before its own (the same additions in the same order as adding
+    // each term in its own matvec), so no copy vout -> v closes the step
+    const bool late = order >= 2;
+    const double* src = late ? vout : v;
+    const double* prev = nullptr;
+    double c_prev = 0;
     long fact = 1;
     for (int j = 1; j <= order; ++j) {
       fact *= j;
       MvArgs a = base;
       a.X = src;
       a.Y = (j % 2) ? t1 : t2;
-      a.acc = vout;
+      a.acc = (late && j == 1) ? nullptr : vout;
+      a.acc_prev = prev;
+      a.c_prev = c_prev;
       a.c_acc = 1.0 / (double)fact;
-      matvec_cells(a);
+      matvec_cells<ONE>(a);
       grid.sync();
       src = a.Y;
+      prev = (late && j == 1) ? a.Y : nullptr;
+      c_prev = a.c_acc;
     }
-    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) v[q] = vout[q];
-    grid.sync();
+    if (!late) {
+      for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
+        v[q] = vout[q];
+      grid.sync();
+    }
   }
 }
 
@@ -375,6 +471,8 @@ int grid_for(long n, int threads) {
 void launch_matvec(const DevCtx& d, int k, const double* X, double* Y, int transpose, double scale,
                    cudaStream_t st) {
   MvArgs a;
+  a.acc_prev = nullptr;
+  a.c_prev = 0;
   a.coef = d.coef;
   a.X = X;
   a.Y = Y;
@@ -385,9 +483,10 @@ void launch_matvec(const DevCtx& d, int k, const double* X, double* Y, int trans
   a.N = d.N;
   a.k = k;
   a.transpose = transpose;
-  const long items = d.N * ((k + kVecChunk - 1) / kVecChunk);
+  const long items = mv_items(d.N, k, d.sms);
   const int th = mv_threads(items, d.sms);
-  k_matvec<<<grid_for(items, th), th, 0, st>>>(a);
+  if (mv_one(d.N, k, d.sms)) k_matvec<true><<<grid_for(items, th), th, 0, st>>>(a);
+  else k_matvec<false><<<grid_for(items, th), th, 0, st>>>(a);
 }
 
 // POWER_METHOD! (Eigenvalues/ARNOLDI_POWER_GPU.jl:64-82): per step vout = v,
@@ -396,29 +495,39 @@ void launch_matvec(const DevCtx& d, int k, const double* X, double* Y, int trans
 static void launch_expm_body(const DevCtx& d, int k, double dt, int nsteps, int order, double* v, double* t1,
                              double* t2, double* vout, int transpose, cudaStream_t st) {
   const long n = 4 * d.N * (long)k;
-  const long items = d.N * ((k + kVecChunk - 1) / kVecChunk);
+  const long items = mv_items(d.N, k, d.sms);
   const int th = mv_threads(items, d.sms);
   MvArgs a;
+  a.acc_prev = nullptr;
+  a.c_prev = 0;
   a.coef = d.coef;
   a.w = make_wrap(d.cfg);
   a.N = d.N;
   a.k = k;
   a.transpose = transpose;
   a.scale = dt;
-  a.acc = vout;
+  const bool late = order >= 2;  // as k_expm_coop: the first term is added one matvec late
   for (int s = 0; s < nsteps; ++s) {
-    const double* src = v;
+    const double* src = late ? vout : v;
+    const double* prev = nullptr;
+    double c_prev = 0;
     long fact = 1;
     for (int j = 1; j <= order; ++j) {
       fact *= j;
       double* dst = (j % 2) ? t1 : t2;
       a.X = src;
       a.Y = dst;
+      a.acc = (late && j == 1) ? nullptr : vout;
+      a.acc_prev = prev;
+      a.c_prev = c_prev;
       a.c_acc = 1.0 / (double)fact;
-      k_matvec<<<grid_for(items, th), th, 0, st>>>(a);
+      if (mv_one(d.N, k, d.sms)) k_matvec<true><<<grid_for(items, th), th, 0, st>>>(a);
+      else k_matvec<false><<<grid_for(items, th), th, 0, st>>>(a);
       src = dst;
+      prev = (late && j == 1) ? dst : nullptr;
+      c_prev = a.c_acc;
     }
-    k_copy<<<grid_for(n, 256), 256, 0, st>>>(vout, v, n);
+    if (!late) k_copy<<<grid_for(n, 256), 256, 0, st>>>(vout, v, n);
   }
 }
 
@@ -558,16 +667,21 @@ int expm_cooperative(hymor_ctx* ctx, int k, double dt, int nsteps, int order, co
   double* t1 = c.buf + n;
   double* t2 = c.buf + 2 * n;
   double* vout = c.buf + 3 * n;
-  static int blocks_per_sm = 0;  // co-resident blocks of k_expm_coop (same on every GB300)
-  if (!blocks_per_sm &&
-      (r = cuda_check(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_expm_coop, kMvThreads, 0))))
+  // co-resident blocks of the two k_expm_coop variants (the same on every GB300)
+  static int blocks_per_sm[2] = {0, 0};
+  const bool one = mv_one(d.N, k, d.sms);
+  const void* kern = one ? (const void*)k_expm_coop<true> : (const void*)k_expm_coop<false>;
+  if (!blocks_per_sm[one] &&
+      (r = cuda_check(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm[one], kern, kMvThreads, 0))))
     return r;
-  const long items = d.N * ((k + kVecChunk - 1) / kVecChunk);
+  const long items = mv_items(d.N, k, d.sms);
   const int th = mv_threads(items, d.sms);
   const long want = (items + th - 1) / th;
   // co-resident: blocks of th <= 256 threads need no more than a 256-thread block
-  const int grid = (int)std::min<long>(want, (long)blocks_per_sm * d.sms);
+  const int grid = (int)std::min<long>(want, (long)blocks_per_sm[one] * d.sms);
   MvArgs base;
+  base.acc_prev = nullptr;
+  base.c_prev = 0;
   base.coef = d.coef;
   base.w = make_wrap(d.cfg);
   base.N = d.N;
@@ -581,7 +695,7 @@ int expm_cooperative(hymor_ctx* ctx, int k, double dt, int nsteps, int order, co
   if ((r = cuda_check(ctx, cudaMemcpyAsync(v, dX, sizeof(double) * n, cudaMemcpyDeviceToDevice, st)))) return r;
   if ((r = cuda_check(ctx, cudaMemcpyAsync(vout, dX, sizeof(double) * n, cudaMemcpyDeviceToDevice, st)))) return r;
   void* args[] = {&base, &nsteps, &order, &v, &t1, &t2, &vout};
-  if ((r = cuda_check(ctx, cudaLaunchCooperativeKernel((const void*)k_expm_coop, grid, th, args, 0, st))))
+  if ((r = cuda_check(ctx, cudaLaunchCooperativeKernel(kern, grid, th, args, 0, st))))
     return r;
   return cuda_check(ctx, cudaMemcpyAsync(dY, vout, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
 }
