@@ -112,6 +112,25 @@ def test_propagator_adjoint_identity(require_gpu):
     assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
 
 
+def test_adjoint_identities_at_600x300(require_gpu):
+    """The transient-growth case's checks at its size (600 x 300 cylinder, 720 000
+    unknowns): the seeded dot-product test <L x, y> = <x, Lᵀ y> for the matvec and for the
+    Taylor propagator (50 steps of the CFL dt), to 1e-12."""
+    cfg = C.cylinder_config(600, 300)
+    sol = S.Solution(C.initial_state(cfg))
+    S.ADVECT_FLOW(sol, 5)
+    _, L = S.LINEARIZE_L(sol)
+    rng = np.random.Generator(np.random.PCG64(4))
+    n = 4 * cfg.nchi * cfg.neta
+    x, y = rng.standard_normal(n), rng.standard_normal(n)
+    lhs, rhs = np.dot(L @ x, y), np.dot(x, L.T @ y)
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+    dt = S.CFL_TIMESTEP(sol)
+    lhs, rhs = np.dot(L.expm(x, dt, 50), y), np.dot(x, L.T.expm(y, dt, 50))
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+    sol.close()
+
+
 def test_linearisation_matches_residual_differences(require_gpu):
     """CHECK_LINEARIZATION_L.jl:33-130 on the GPU: L q ~ f(x + q) - f(x) (central, h = 1e-7)."""
     cfg, cs, sol, orc = _setup(30, 20, steps=10)
