@@ -637,6 +637,7 @@ struct KrylovScratch {
 struct LinearState {
   ExpmCache expm;
   KrylovScratch kry;
+  int coop_blocks[2] = {0, 0};  // co-resident blocks per SM of k_expm_coop<false>, <true>
 };
 LinearState& linear_state(hymor_ctx* ctx) {
   void*& slot = ctx_linear_state(ctx);
@@ -667,8 +668,7 @@ int expm_cooperative(hymor_ctx* ctx, int k, double dt, int nsteps, int order, co
   double* t1 = c.buf + n;
   double* t2 = c.buf + 2 * n;
   double* vout = c.buf + 3 * n;
-  // co-resident blocks of the two k_expm_coop variants (the same on every GB300)
-  static int blocks_per_sm[2] = {0, 0};
+  int* blocks_per_sm = linear_state(ctx).coop_blocks;
   const bool one = mv_one(d.N, k, d.sms);
   const void* kern = one ? (const void*)k_expm_coop<true> : (const void*)k_expm_coop<false>;
   if (!blocks_per_sm[one] &&
