@@ -355,7 +355,6 @@ int check_err_words(hymor_ctx* ctx, const unsigned* h) {
     return fail(ctx, HYMOR_ERR_SHOCK_RANGE, "shocked cell outside rows 2..Neta-1 (the shock left the mesh)");
   if (h[kErrFlags] & kBitNumeric)
     return fail(ctx, HYMOR_ERR_NUMERIC, "non-positive density or pressure, or NaN, in the flow field");
-  if (h[kErrFlags] & kBitTimeout) return fail(ctx, HYMOR_ERR_TIMEOUT, "bounded device wait gave up");
   return 0;
 }
 

@@ -72,7 +72,6 @@ enum ErrWord {
 enum ErrBit : unsigned {
   kBitNumeric = 1u,
   kBitShockRange = 2u,
-  kBitTimeout = 4u,
 };
 
 __host__ __device__ inline int gidx(int i, int j, int nchi) { return i + j * (nchi + 2); }  // 0-based ghosted

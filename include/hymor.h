@@ -26,7 +26,7 @@ extern "C" {
 #define HYMOR_ERR_CUDA (-2)         /* CUDA runtime error                           */
 #define HYMOR_ERR_NUMERIC (-3)      /* NaN / non-positive density or pressure seen  */
 #define HYMOR_ERR_SHOCK_RANGE (-4)  /* shocked cell too close to the domain top     */
-#define HYMOR_ERR_TIMEOUT (-5)      /* a bounded device wait gave up                */
+#define HYMOR_ERR_TIMEOUT (-5)      /* reserved: no kernel of this library waits on a flag */
 #define HYMOR_ERR_NOT_READY (-6)    /* e.g. matvec before a Jacobian exists         */
 
 /* Boundary conditions (names of utils/Operators/APPLY_BOUNDARY_CONDITIONS.jl). */
