@@ -458,10 +458,9 @@ int enqueue_download(hymor_ctx* ctx, double* q, bool with_err) {
   const size_t G = d.G, n = d.nchi, Gp = state_pitch(G);
   cudaStream_t st = ctx->stream;
   if (q) CU(cudaMemcpy2DAsync(q, G * 8, d.S.rho, Gp * 8, G * 8, 4, cudaMemcpyDeviceToHost, st));
-  CU(cudaMemcpyAsync(ctx->stage, d.Sp.x, header_doubles(n) * 8, cudaMemcpyDeviceToHost, st));
-  if (with_err)
-    CU(cudaMemcpyAsync(ctx->stage + header_doubles(n) * 8, d.err, kErrCount * sizeof(unsigned),
-                       cudaMemcpyDeviceToHost, st));
+  // the error words follow the header on the device as in the staging buffer: one copy
+  CU(cudaMemcpyAsync(ctx->stage, d.Sp.x, with_err ? stage_bytes(n) : header_doubles(n) * 8,
+                     cudaMemcpyDeviceToHost, st));
   return 0;
 }
 
@@ -586,20 +585,21 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
     return bail(r);
   for (int v = 0; v < 4; ++v)
     if ((r = dalloc(ctx, &d.F[v], d.N)) || (r = dalloc(ctx, &d.SF[v], d.N))) return bail(r);
-  {  // shock points of S, the scalars and the cell indices in one block, laid out like the
-     // pinned staging buffer, so that they move in one copy
+  {  // shock points of S, the scalars, the cell indices and the error words in one block,
+     // laid out like the pinned staging buffer, so that they move in one copy
     const size_t np = state_pitch(d.nchi);
     double* b = nullptr;
-    if ((r = dalloc(ctx, &b, header_doubles(d.nchi)))) return bail(r);
+    if ((r = dalloc(ctx, &b, header_doubles(d.nchi) + (kErrCount + 1) / 2))) return bail(r);
     d.Sp = ShockPts{b, b + np, b + 2 * np, b + 3 * np};
     d.scal = b + 4 * np;
     d.cell_idx = reinterpret_cast<int*>(b + 4 * np + kScalPitch);
+    d.err = reinterpret_cast<unsigned*>(b + header_doubles(d.nchi));
   }
   if ((r = pts(d.Yp))) return bail(r);
   if ((r = dalloc(ctx, &d.beta, d.nchi)) ||
       (r = dalloc(ctx, &d.speed_x, d.nchi)) || (r = dalloc(ctx, &d.speed_y, d.nchi)) ||
       (r = dalloc(ctx, &d.rel, d.nchi)) || (r = dalloc(ctx, &d.spl, 17 * (long)d.nchi + 16)) ||
-      (r = dalloc(ctx, &d.err, (long)kErrCount)) || (r = dalloc(ctx, &d.tiles, 2 + 2 * (long)flux_tiles(d))) ||
+      (r = dalloc(ctx, &d.tiles, 2 + 2 * (long)flux_tiles(d))) ||
       (r = dalloc(ctx, &d.ticket, 2L)) ||
       (r = dalloc(ctx, &d.cflw, d.NLR + d.NBT)))
     return bail(r);
