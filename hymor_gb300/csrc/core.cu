@@ -30,10 +30,8 @@ namespace {
 
 constexpr int TX = 31;           // cells per tile along chi (TX + 1 = 32 lr faces per row)
 constexpr int TY = 8;            // cells per tile along eta
-constexpr int HX = TX + 2, HY = TY + 2, NH = HX * HY;
-constexpr int CX = TX + 1, CY = TY + 1, NCOR = CX * CY;
-constexpr int NLRF = (TX + 1) * TY;  // 256
-constexpr int NBTF = TX * (TY + 1);  // 279
+constexpr int HX = TX + 2;       // halo columns
+constexpr int CX = TX + 1;       // corner columns
 constexpr int kFluxThreads = 256;
 // Tile geometry of a 31 x TYV-cell flux tile (TYV warps, one per tile row).
 template <int TYV>
