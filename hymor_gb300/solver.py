@@ -202,6 +202,49 @@ def LINEARIZE_L(s: Solution):
 # Stability drivers over the device-resident Krylov solver
 
 
+def CHECK_LINEARIZATION_L(L: LinearOperatorGPU, s: Solution, seed: int | None = None, verbose: bool = True) -> float:
+    """CHECK_LINEARIZATION_L (Modal_stability_analysis/CHECK_LINEARIZATION_L.jl:33-130):
+    the linearised response L q against the finite difference f(x + q) - f(x) of the
+    nonlinear residual, for a random perturbation q of every conserved variable (scaled by
+    perturbation_magnitude, masked by the flow cells like the reference), both residuals on
+    copies of `s`. Returns (and prints) the reference's error measure
+    ||(L q - dq) / (|L q| + 1e-8)|| / sqrt(144 N); below ~1e-3 means consistent."""
+    cfg, N = s.cfg, s.N
+    nchi, neta = cfg.nchi, cfg.neta
+    eps = cfg.perturbation_magnitude
+    st = s.get_state()
+    rng = np.random.default_rng(seed)
+    shock = bool(cfg.shock_enabled)
+    flow = ((np.arange(1, neta + 1)[None, :] < st["cell_idx"][:, None]).astype(np.float64)
+            if shock else np.ones((nchi, neta)))  # (nchi, neta), chi fastest when raveled "F"
+    q = np.zeros(4 * N)
+    qs = np.asarray(st["q"], dtype=np.float64).reshape(4, -1).copy()
+    for v in range(4):
+        P = rng.standard_normal((nchi, neta))
+        dv = (flow * P if shock else P) * eps
+        blk = qs[v].reshape(nchi + 2, neta + 2, order="F")
+        blk[1:-1, 1:-1] += dv
+        qs[v] = blk.ravel(order="F")
+        # the reference masks q for rho only (:52-96); the masked Jacobian ignores the rest
+        q[v * N:(v + 1) * N] = (dv if v == 0 else P * eps).ravel(order="F")
+    pts = (st["pts_x"], st["pts_y"], st["pts_chi"], st["pts_eta"])
+    base, pert = Solution(s.case), Solution(s.case)
+    try:
+        base.set_state(np.asarray(st["q"]), *pts, st["cell_idx"], st["t"])
+        pert.set_state(qs.ravel(), *pts, st["cell_idx"], st["t"])
+        f0, f1 = PDE(base), PDE(pert)
+        mask = np.tile(flow.ravel(order="F"), 4) if shock else 1.0
+        dq = (f1 - f0) * mask
+    finally:
+        base.close()
+        pert.close()
+    dq_lin = L @ q
+    err = float(np.linalg.norm((dq_lin - dq) / (np.abs(dq_lin) + 1e-8)) / np.sqrt(9 * 4 * 4 * N))
+    if verbose:
+        print(f"Error of linearization: {err:e} .")
+    return err
+
+
 def _expm_op(s: Solution, dt: float, nsteps: int, order: int, transpose: int = 0):
     L, h = s.ctx.L, s.ctx.h
 

@@ -131,6 +131,15 @@ def test_adjoint_identities_at_600x300(require_gpu):
     sol.close()
 
 
+def test_check_linearization_l(require_gpu):
+    """CHECK_LINEARIZATION_L, the reference's own consistency measure (below ~1e-3 means a
+    consistent linearisation), on the GPU operator and residual."""
+    cfg, cs, sol, orc = _setup(30, 20, steps=10)
+    _, L = S.LINEARIZE_L(sol)
+    err = S.CHECK_LINEARIZATION_L(L, sol, seed=7)
+    assert err < 1e-3
+
+
 def test_linearisation_matches_residual_differences(require_gpu):
     """CHECK_LINEARIZATION_L.jl:33-130 on the GPU: L q ~ f(x + q) - f(x) (central, h = 1e-7)."""
     cfg, cs, sol, orc = _setup(30, 20, steps=10)
