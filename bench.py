@@ -322,8 +322,9 @@ def solve_numbers(nchi: int = 100, neta: int = 80, n_modes: int = 4, T_ref: floa
     S.ADVECT_FLOW(sol, steps)
     _, Lop = S.LINEARIZE_L(sol)
     lam_b, info_b = S.EIGENVALUES(Lop, sol, n_modes, T_ref=T_ref, tol=tol, block=block, flow_start=True,
-                                  maxit=maxit)
-    lam_p, info_p = S.EIGENVALUES(Lop, sol, n_modes, T_ref=T_ref, tol=tol, flow_start=True, maxit=maxit)
+                                  maxit=maxit, keep_unconverged=True)
+    lam_p, info_p = S.EIGENVALUES(Lop, sol, n_modes, T_ref=T_ref, tol=tol, flow_start=True, maxit=maxit,
+                                  keep_unconverged=True)
     scale = float(np.max(np.abs(lam_p)))
     agree = max(float(np.min(np.abs(lam_p - a))) for a in lam_b) / scale
     sol.close()

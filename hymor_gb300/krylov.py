@@ -52,13 +52,29 @@ class DeviceBuffer:
             pass
 
 
+def ritz_vectors(ctx, V, n: int, m: int, Y: np.ndarray) -> np.ndarray:
+    """Ritz vectors V[:, :m] Y (columns of unit norm when Y's are) on the device. A complex Y
+    goes as its real and imaginary parts in one rotation of the basis (V[:, :2k] =
+    V[:, :m] [Re Y, Im Y]), which overwrites the basis: call it last."""
+    k = Y.shape[1]
+    cplx = np.iscomplexobj(Y)
+    Q = np.hstack([Y.real, Y.imag]) if cplx else np.asarray(Y, dtype=np.float64)
+    if Q.shape[1] > m:
+        raise HymorError(-1, "too many Ritz vectors for the basis")
+    ctx.check(ctx.L.hymor_krylov_rotate(ctx.h, n, m, Q.shape[1], V.ptr, n, dp(np.asfortranarray(Q))))
+    X = V.download(n * Q.shape[1]).reshape(Q.shape[1], n).T
+    return X[:, :k] + 1j * X[:, k:] if cplx else X.copy()
+
+
 def krylov_schur(ctx, n: int, apply_op, nev: int, ncv: int, tol: float = 1e-8, maxit: int = 200,
-                 seed: int = 3, symmetric: bool = False, v0: np.ndarray | None = None):
+                 seed: int = 3, symmetric: bool = False, v0: np.ndarray | None = None,
+                 want_vectors: bool = False):
     """Largest-magnitude eigenpairs of a real operator held on the device.
 
     apply_op(src_addr, dst_addr) writes OP(v) for device vectors of length n.
     Returns (theta, resid, nops): Ritz values, their residual norms ||OP x - theta x||
-    (x of unit norm) and the number of operator applications."""
+    (x of unit norm) and the number of operator applications; with want_vectors also the
+    Ritz vectors (n x nev, complex unless symmetric), or None when tol was not reached."""
     if not (0 < nev < ncv):
         raise HymorError(-1, "need 0 < nev < ncv")
     L = ctx.L
@@ -71,7 +87,7 @@ def krylov_schur(ctx, n: int, apply_op, nev: int, ncv: int, tol: float = 1e-8, m
     h = np.empty(ncv + 2)
     p = 0       # columns of the current Krylov decomposition already built
     nops = 0
-    theta = resid = None
+    theta = resid = X = None
     for it in range(maxit):
         for j in range(p, ncv):
             apply_op(V.addr(j * n), w.addr())
@@ -97,6 +113,8 @@ def krylov_schur(ctx, n: int, apply_op, nev: int, ncv: int, tol: float = 1e-8, m
             res = np.abs(b @ Y)
         theta, resid = vals[:nev], res[:nev]
         if np.all(resid <= tol * np.abs(theta)):
+            if want_vectors:
+                X = ritz_vectors(ctx, V, n, ncv, Y[:, :nev])
             break
         # Krylov-Schur restart: keep the wanted Schur vectors
         keep = min(nev + max(2, (ncv - nev) // 2), ncv - 1)
@@ -120,11 +138,12 @@ def krylov_schur(ctx, n: int, apply_op, nev: int, ncv: int, tol: float = 1e-8, m
         p = keep
     V.free()
     w.free()
-    return theta, resid, nops
+    return (theta, resid, nops, X) if want_vectors else (theta, resid, nops)
 
 
 def block_krylov_schur(ctx, n: int, apply_block, nev: int, ncv: int, block: int, tol: float = 1e-8,
-                       maxit: int = 200, seed: int = 3, symmetric: bool = False, start_mask=None):
+                       maxit: int = 200, seed: int = 3, symmetric: bool = False, start_mask=None,
+                       want_vectors: bool = False):
     """Block Krylov-Schur: the Krylov basis grows `block` vectors at a time, so that every
     operator application propagates a whole block in one batched call (Zhou and Saad,
     "Block Krylov-Schur method for large symmetric eigenvalue problems", Numer. Algorithms 47
@@ -135,8 +154,9 @@ def block_krylov_schur(ctx, n: int, apply_block, nev: int, ncv: int, block: int,
     device) against the basis and the block's earlier vectors, so the projected matrix is
     block upper Hessenberg with `block` subdiagonals: A V[:, :m] = V[:, :m+block] H.
     Returns (theta, resid, nops) like krylov_schur; nops counts single-vector
-    applications (block per call). start_mask (length n, optional) multiplies the random
-    start block, e.g. to keep it on a subspace the operator leaves invariant."""
+    applications (block per call); with want_vectors also the Ritz vectors, as
+    krylov_schur. start_mask (length n, optional) multiplies the random start block, e.g.
+    to keep it on a subspace the operator leaves invariant."""
     b = int(block)
     if b < 1 or not (0 < nev < ncv) or ncv < nev + 2 * b:
         raise HymorError(-1, "need block >= 1 and 0 < nev, nev + 2 block <= ncv")
@@ -157,7 +177,7 @@ def block_krylov_schur(ctx, n: int, apply_block, nev: int, ncv: int, block: int,
     H = np.zeros((cap, cap))
     p = 0
     nops = 0
-    theta = resid = None
+    theta = resid = X = None
     for it in range(maxit):
         m = p + b * max(1, -(-(ncv - p) // b))
         for j in range(p, m, b):
@@ -183,6 +203,8 @@ def block_krylov_schur(ctx, n: int, apply_block, nev: int, ncv: int, block: int,
         res = np.linalg.norm(B @ Y, axis=0)
         theta, resid = vals[:nev], res[:nev]
         if np.all(resid <= tol * np.abs(theta)):
+            if want_vectors:
+                X = ritz_vectors(ctx, V, n, m, Y[:, :nev])
             break
         # restart: keep the wanted Schur vectors, leave room for the residual block
         keep = min(nev + max(2, (m - nev) // 2), m - b)
@@ -207,4 +229,4 @@ def block_krylov_schur(ctx, n: int, apply_block, nev: int, ncv: int, block: int,
         p = keep
     V.free()
     W.free()
-    return theta, resid, nops
+    return (theta, resid, nops, X) if want_vectors else (theta, resid, nops)

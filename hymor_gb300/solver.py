@@ -264,10 +264,15 @@ def _expm_block_op(s: Solution, dt: float, nsteps: int, order: int, transpose: i
 
 def EIGENVALUES(L: LinearOperatorGPU, s: Solution, n_modes: int, T_ref: float = 0.5, ncv: int | None = None,
                 tol: float = 1e-8, order: int = 5, method: str = "device", seed: int = 3, maxit: int = 300,
-                block: int = 1, flow_start: bool = False):
+                block: int = 1, flow_start: bool = False, modes: bool = False, keep_unconverged: bool = False):
     """EIGENVALUES_GPU_ARNOLDI (Eigenvalues/EIGENVALUES.jl:112-205): the n_modes eigenvalues of
     largest magnitude of exp(L T_ref) (Taylor-`order` steps of the CFL dt), mapped back as
     lambda = log(mu) / (dt * timesteps).
+
+    modes: also the eigenvectors (info["modes"], 4 Nchi Neta x n_modes, complex, unit
+    norm; the reference's V). When the solve does not reach tol, the reference warns and
+    returns NaN (EIGENVALUES.jl:184-204); so does this, unless keep_unconverged, which
+    returns the last Ritz values (and no modes) with info["converged"] False.
 
     method "device": Krylov-Schur with the basis in HBM (hymor_gb300/krylov.py).
     method "host":   the reference's structure, ARPACK on the host calling one GPU
@@ -288,35 +293,53 @@ def EIGENVALUES(L: LinearOperatorGPU, s: Solution, n_modes: int, T_ref: float = 
         flow = (np.arange(1, s.cfg.neta + 1)[None, :] < st["cell_idx"][:, None]).ravel(order="F")
         mask = np.tile(flow.astype(np.float64), 4)
     t0 = time.perf_counter()
+    X = None
     if method == "device" and block > 1:
         from .krylov import block_krylov_schur
-        mu, resid, nops = block_krylov_schur(s.ctx, n, _expm_block_op(s, dt, timesteps, order), n_modes, ncv,
-                                             block, tol=tol, maxit=maxit, seed=seed, start_mask=mask)
+        mu, resid, nops, X = block_krylov_schur(s.ctx, n, _expm_block_op(s, dt, timesteps, order), n_modes, ncv,
+                                                block, tol=tol, maxit=maxit, seed=seed, start_mask=mask,
+                                                want_vectors=True)
+        converged = bool(np.all(resid <= tol * np.abs(mu)))
     elif method == "device":
         from .krylov import krylov_schur
         v0 = None
         if mask is not None:
             v0 = np.random.Generator(np.random.PCG64(seed)).standard_normal(n) * mask
-        mu, resid, nops = krylov_schur(s.ctx, n, _expm_op(s, dt, timesteps, order), n_modes, ncv, tol=tol,
-                                       maxit=maxit, seed=seed, v0=v0)
+        mu, resid, nops, X = krylov_schur(s.ctx, n, _expm_op(s, dt, timesteps, order), n_modes, ncv, tol=tol,
+                                          maxit=maxit, seed=seed, v0=v0, want_vectors=True)
+        converged = bool(np.all(resid <= tol * np.abs(mu)))
     elif method == "host":
-        from scipy.sparse.linalg import LinearOperator, eigs
+        from scipy.sparse.linalg import ArpackNoConvergence, LinearOperator, eigs
         count = [0]
 
         def mv(x):
             count[0] += 1
             return L.expm(np.ascontiguousarray(x, dtype=np.float64).ravel(), dt, timesteps, order)
         rng = np.random.Generator(np.random.PCG64(seed))
-        mu = eigs(LinearOperator((n, n), matvec=mv, dtype=np.float64), k=n_modes, which="LM", tol=tol, ncv=ncv,
-                  v0=rng.standard_normal(n), maxiter=maxit * n_modes, return_eigenvectors=False)
-        mu = mu[np.argsort(-np.abs(mu))]
+        try:
+            mu, X = eigs(LinearOperator((n, n), matvec=mv, dtype=np.float64), k=n_modes, which="LM", tol=tol,
+                         ncv=ncv, v0=rng.standard_normal(n), maxiter=maxit * n_modes, return_eigenvectors=True)
+            order_ = np.argsort(-np.abs(mu))
+            mu, X = mu[order_], X[:, order_]
+            converged = True
+        except ArpackNoConvergence as e:
+            mu, X, converged = np.asarray(e.eigenvalues), None, False
         resid = np.full(len(mu), np.nan)
         nops = count[0]
     else:
         raise HymorError(-1, f"unknown method {method!r}")
     elapsed = time.perf_counter() - t0
     lam = np.log(mu.astype(complex)) / (dt * timesteps)
-    return lam, dict(mu=mu, resid=resid, dt=dt, timesteps=timesteps, nops=nops, seconds=elapsed)
+    if not converged and not keep_unconverged:
+        import warnings
+        warnings.warn(f"eigen solve did not reach tol {tol:g} in {maxit} restarts; returning NaN")
+        lam = np.full(n_modes, np.nan + 1j * np.nan)
+        mu = np.full(n_modes, np.nan + 1j * np.nan)
+        X = np.full((n, n_modes), np.nan + 1j * np.nan) if modes else None
+    info = dict(mu=mu, resid=resid, dt=dt, timesteps=timesteps, nops=nops, seconds=elapsed, converged=converged)
+    if modes:
+        info["modes"] = X
+    return lam, info
 
 
 def chu_blocks(s: Solution, norms=(1, 1, 1, 1)):
@@ -370,14 +393,17 @@ def chu_blocks_from_state(cfg, vol, qflat, cell_idx, norms=(1, 1, 1, 1)):
 
 def TRANSIENT_GROWTH_DOWNSTREAM(L: LinearOperatorGPU, s: Solution, n_modes: int, T: float, ncv: int | None = None,
                                 tol: float = 1e-8, order: int = 5, seed: int = 4, maxit: int = 300,
-                                block: int = 1):
+                                block: int = 1, modes: bool = False, keep_unconverged: bool = False):
     """TRANSIENT_GROWTH_DOWNSTREAM (TRANSIENT_GROWTH_DOWNSTREAM.jl:34-153): optimal energy gains
     G(T), the largest eigenvalues of exp(Lᵀ T) R'MR exp(L T) x = G R'M^R x. The generalised
     symmetric problem is reduced with the per-cell Cholesky factor of R'M^R (D = K Kᵀ) to
     K^{-1} Pᵀ C0 P K^{-ᵀ} y = G y and solved by Krylov-Schur (Lanczos with full
     reorthogonalisation) on the device; the forward propagation P and its adjoint Pᵀ are
     Taylor-`order` steps of dt = T / round(T / dt_CFL). block > 1: block Krylov-Schur, the
-    operator applied to `block` vectors per batched call."""
+    operator applied to `block` vectors per batched call. modes: also the optimal initial
+    conditions x = K^-T y (info["modes"], 4 Nchi Neta x n_modes, x' R'M^R x = 1; the
+    reference's V). Non-convergence warns and returns NaN, as the reference
+    (TRANSIENT_GROWTH_DOWNSTREAM.jl:131-135), unless keep_unconverged."""
     import time
     from .krylov import DeviceBuffer, block_krylov_schur, krylov_schur
     dt_cfl = CFL_TIMESTEP(s)
@@ -403,12 +429,28 @@ def TRANSIENT_GROWTH_DOWNSTREAM(L: LinearOperatorGPU, s: Solution, n_modes: int,
     ncv = ncv or max(2 * n_modes + 1, 16, n_modes + 4 * block)
     t0 = time.perf_counter()
     if block > 1:
-        gains, resid, nops = block_krylov_schur(s.ctx, n, apply_k, n_modes, ncv, block, tol=tol, maxit=maxit,
-                                                seed=seed, symmetric=True)
+        gains, resid, nops, Y = block_krylov_schur(s.ctx, n, apply_k, n_modes, ncv, block, tol=tol, maxit=maxit,
+                                                   seed=seed, symmetric=True, want_vectors=True)
     else:
-        gains, resid, nops = krylov_schur(s.ctx, n, lambda a, b: apply_k(a, b, 1), n_modes, ncv, tol=tol,
-                                          maxit=maxit, seed=seed, symmetric=True)
+        gains, resid, nops, Y = krylov_schur(s.ctx, n, lambda a, b: apply_k(a, b, 1), n_modes, ncv, tol=tol,
+                                             maxit=maxit, seed=seed, symmetric=True, want_vectors=True)
     elapsed = time.perf_counter() - t0
     for b in bufs + [t1, t2]:
         b.free()
-    return np.real(gains), dict(resid=resid, dt=dt, n_t=n_t, T_opt=n_t * dt, nops=nops, seconds=elapsed)
+    gains = np.real(gains)
+    converged = bool(np.all(resid <= tol * np.abs(gains)))
+    X = None
+    if modes and Y is not None:
+        N = s.N
+        # x = K^-T y per cell: y as [rho; rho_u; rho_v; rho_E] blocks of N
+        Yc = Y.reshape(4, N, -1).transpose(1, 0, 2)                    # (N, 4, k)
+        X = np.einsum("nij,njk->nik", KinvT, Yc).transpose(1, 0, 2).reshape(n, -1)
+    if not converged and not keep_unconverged:
+        import warnings
+        warnings.warn(f"transient-growth solve did not reach tol {tol:g} in {maxit} restarts; returning NaN")
+        gains = np.full(n_modes, np.nan)
+        X = np.full((n, n_modes), np.nan) if modes else None
+    info = dict(resid=resid, dt=dt, n_t=n_t, T_opt=n_t * dt, nops=nops, seconds=elapsed, converged=converged)
+    if modes:
+        info["modes"] = X
+    return gains, info

@@ -74,6 +74,47 @@ def test_transient_growth_device_vs_oracle(require_gpu):
     assert np.allclose(np.sort(G)[::-1], Go, rtol=1e-6, atol=0)
 
 
+def test_eigenvalue_modes_and_nonconvergence(require_gpu):
+    """modes=True returns the eigenvectors (the reference's V): exp(L T) x = mu x for each;
+    a solve that stops short of tol warns and returns NaN, as the reference does, unless
+    keep_unconverged."""
+    cfg, cs, sol, orc = _setup(30, 20)
+    _, L = S.LINEARIZE_L(sol)
+    for block in (1, 4):
+        lam, info = S.EIGENVALUES(L, sol, 4, T_ref=0.02, ncv=28, tol=1e-10, block=block, modes=True)
+        X, mu = info["modes"], info["mu"]
+        assert X.shape == (4 * cfg.nchi * cfg.neta, 4)
+        dt, nt = info["dt"], info["timesteps"]
+        for i in range(4):
+            x = X[:, i]
+            Px = L.expm(np.ascontiguousarray(x.real), dt, nt) + 1j * L.expm(np.ascontiguousarray(x.imag), dt, nt)
+            assert np.linalg.norm(Px - mu[i] * x) <= 1e-8 * abs(mu[i])
+    with pytest.warns(UserWarning):
+        lam, info = S.EIGENVALUES(L, sol, 4, T_ref=0.02, ncv=24, tol=1e-15, maxit=2, modes=True)
+    assert np.all(np.isnan(lam)) and np.all(np.isnan(info["modes"])) and not info["converged"]
+    lam, info = S.EIGENVALUES(L, sol, 4, T_ref=0.02, ncv=24, tol=1e-15, maxit=2, keep_unconverged=True)
+    assert np.all(np.isfinite(lam)) and not info["converged"]
+
+
+def test_transient_growth_modes(require_gpu):
+    """modes=True returns the optimal initial conditions x (the reference's V), D-normalised
+    (x' R'M^R x = 1) with Rayleigh quotient (P x)' R'MR (P x) = G."""
+    cfg, cs, sol, orc = _setup(24, 24)
+    _, L = S.LINEARIZE_L(sol)
+    G, info = S.TRANSIENT_GROWTH_DOWNSTREAM(L, sol, 2, 0.01, ncv=16, tol=1e-11, modes=True)
+    X = info["modes"]
+    C0, D = S.chu_blocks(sol)
+    N = cfg.nchi * cfg.neta
+
+    def blk(B, x):
+        return np.einsum("nij,nj->ni", B, x.reshape(4, N).T).T.ravel()
+    for i in range(2):
+        x = np.ascontiguousarray(X[:, i])
+        assert abs(x @ blk(D, x) - 1) < 1e-10
+        Px = L.expm(x, info["dt"], info["n_t"])
+        assert abs(Px @ blk(C0, Px) - G[i]) <= 1e-8 * abs(G[i])
+
+
 def test_block_eigenvalues_match_single_vector(require_gpu):
     """Block Krylov-Schur (4 vectors per batched propagation) finds the same eigenvalues
     as the single-vector Krylov-Schur, to 1e-8 of the spectrum's scale."""

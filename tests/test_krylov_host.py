@@ -137,3 +137,26 @@ def test_block_krylov_schur_rejects_small_basis():
     ctx = _Ctx()
     with pytest.raises(K.HymorError):
         K.block_krylov_schur(ctx, 50, None, 4, ncv=10, block=4)
+
+
+@pytest.mark.parametrize("symmetric", [False, True])
+@pytest.mark.parametrize("block", [0, 3])
+def test_ritz_vectors_are_eigenvectors(symmetric, block):
+    """want_vectors: the Ritz vectors come back with unit norm and A x = theta x to the
+    residual the solve reached (block 0: the single-vector driver)."""
+    n, nev = 240, 5
+    A, _ = _matrix(n, symmetric, 11)
+    ctx = _Ctx()
+    one, blk = _op(A, ctx)
+    if block:
+        theta, resid, nops, X = K.block_krylov_schur(ctx, n, blk, nev, ncv=30, block=block, tol=1e-10,
+                                                     maxit=400, seed=5, symmetric=symmetric, want_vectors=True)
+    else:
+        theta, resid, nops, X = K.krylov_schur(ctx, n, one, nev, 30, tol=1e-10, maxit=400, seed=5,
+                                               symmetric=symmetric, want_vectors=True)
+    assert X.shape == (n, nev)
+    assert np.iscomplexobj(X) == (not symmetric)
+    for i in range(nev):
+        x = X[:, i]
+        assert abs(np.linalg.norm(x) - 1) < 1e-12
+        assert np.linalg.norm(A @ x - theta[i] * x) <= 1e-9 * abs(theta[i])
