@@ -34,7 +34,8 @@ struct hymor_ctx_s {
   cudaGraphExec_t gexec = nullptr;
   int step_kernels = 0;  // kernel nodes of the step graph
   // flux-kernel profiling: event-record nodes around the flux launches of the 4 stages
-  // (2 launches per stage: interior tiles, then the shock/boundary tiles)
+  // (2 launches per stage: the interior tiles on the main stream, the shock/boundary tiles
+  // on their own stream)
   bool profile = false;
   // 4 k .. 4 k + 3: around the two flux launches of stage k; 16 + k: start of stage k's
   // stage update; 20: step start; 21: step end (main stream)

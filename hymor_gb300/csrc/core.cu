@@ -1,23 +1,22 @@
 // Residual, shock fitting, boundary conditions and time-marching kernels (sm_103a).
 //
 // One RK4 step (ADVECT_FLOW_EXPLICIT, utils/Time_marching/ADVECT_FLOW_EXPLICIT.jl:36-81)
-// is this launch sequence on one stream (captured once into a CUDA graph):
+// is one CUDA graph of these kernels over four streams (api.cu, enqueue_step):
 //
-//   flow_cells      UPDATE_FLOW_CELLS on S: shocked-cell detection, upstream fill,
-//                   extrapolation (one thread per chi column)
-//   sound_cmax      sound speed of S, max|a|                       (all ghosted cells)
-//   cfl             CFL_TIMESTEP maxima, dt on the device           (all cells)
-//   4 x { update_thermo   stage update of Y and S, p/T of Y       (all ghosted cells)
-//         shock_bc        spline + R-H jump + extrapolation + MOVE_SHOCK, then the
-//                         ghost-cell boundary conditions           (one CTA)
-//         flux            FV residual of Y                         (31x8-cell tiles) }
-//   update_thermo   last S update, p/T of S
-//   shock_bc        UPDATE_SHOCK_BC + APPLY_BOUNDARY_CONDITIONS on S (one CTA)
-//   fill_minrho     UPDATE_FIELD_UPSTREAM + MIN_RHO on S, t += dt
+//   k_flow_cells        UPDATE_FLOW_CELLS on S (a warp per chi column)
+//   k_classify_tiles    the step's flux tile lists (interior / shock and boundary)
+//   k_sound_cmax, k_cfl_faces, k_cfl, k_cfl_final   CFL_TIMESTEP, dt on the device
+//   k_update_thermo     the stage copy and stage updates of Y and S, p and T
+//   k_spline_rows, k_spline_fit   the smoothing-spline fit of the shock points (one CTA)
+//   k_shock_columns     R-H jump, extrapolation, MOVE_SHOCK (a thread per column)
+//   k_move_shock        MOVE_SHOCK of the first stage, once dt is known (one CTA)
+//   k_bc_edges          ghost-cell boundary conditions (chi edges, then eta edges)
+//   k_flux              the FV residual of a stage, 31x8-cell tiles, in two launches
+//   k_fill_minrho       UPDATE_FIELD_UPSTREAM + MIN_RHO on S, t += dt
 //
-// The flux kernel dominates. It is FP64-bound on GB300 (about 1.9 DFMA/clk/SM):
-// geometry-only factors are precomputed per face (common.cuh), every face flux is
-// evaluated once per tile in shared memory, and divisions are replaced by
+// The flux kernel dominates. It is FP64-bound on GB300 (the DFMA rate is about 1.7 per
+// clock per SM): geometry-only factors are precomputed per face (common.cuh), every face
+// flux is evaluated once per tile in shared memory, and divisions are replaced by
 // reciprocal multiplies (frcp).
 #include <cmath>
 #include <cstdio>
