@@ -20,7 +20,7 @@ struct hymor_ctx_s {
   DevCtx d;
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;      // high-priority stream of the shock/BC chain inside the step graph
-  cudaStream_t fit = nullptr;       // the step's first spline fit, beside the flow cells and the CFL
+  cudaStream_t fit = nullptr;       // the first spline fit and the first jump kernels of a step
   cudaStream_t c1 = nullptr;        // the shock/boundary-class flux, beside the interior-class flux
   cudaEvent_t fork_ev[8] = {}, join_ev[8] = {};
   cudaEvent_t fit_fork = nullptr, fit_join = nullptr;
@@ -49,7 +49,7 @@ struct hymor_ctx_s {
   // L2 flush scratch of hymor_bench_steps
   void* flush_buf = nullptr;
   uint64_t flush_bytes = 0;
-  // state of the linear entry points: replayed propagator graphs, Krylov scratch (linear.cu)
+  // state of the linear entry points: propagator work vectors, Krylov scratch (linear.cu)
   void* linear_state = nullptr;
   // pinned host staging of the small state arrays (shock points, cell indices, scalars),
   // so that set_state / get_state move them by DMA instead of pageable staged copies
