@@ -34,7 +34,8 @@ EXPORTS = [
     "hymor_memcpy_h2d", "hymor_memcpy_d2h", "hymor_bench_steps", "hymor_dot_dev",
     "hymor_krylov_orthogonalize", "hymor_krylov_rotate", "hymor_block4_apply_dev", "hymor_memcpy_d2d",
     "hymor_expm_apply_dev_noalloc", "hymor_step_kernels", "hymor_fp64_peak",
-    "hymor_profile_phases", "hymor_advect", "hymor_bench_matvec",
+    "hymor_profile_phases", "hymor_advect", "hymor_bench_matvec", "hymor_operator_size",
+    "hymor_shock_blocks_get", "hymor_shock_blocks_set", "hymor_shock_fields", "hymor_block4_apply_ext_dev",
 ]
 
 
@@ -97,6 +98,11 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "hymor_krylov_orthogonalize": [vp, ctypes.c_int64, i, vp, ctypes.c_int64, vp, dp, i],
         "hymor_krylov_rotate": [vp, ctypes.c_int64, i, i, vp, ctypes.c_int64, dp],
         "hymor_block4_apply_dev": [vp, i, vp, vp, vp],
+        "hymor_block4_apply_ext_dev": [vp, i, ctypes.c_int64, vp, vp, vp, vp],
+        "hymor_operator_size": [vp, ctypes.POINTER(ctypes.c_int64)],
+        "hymor_shock_blocks_get": [vp, ip, dp, dp, dp],
+        "hymor_shock_blocks_set": [vp, ip, dp, dp, dp],
+        "hymor_shock_fields": [vp, dp, dp],
     }
     for name, args in sig.items():
         f = getattr(L, name)

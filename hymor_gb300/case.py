@@ -55,7 +55,7 @@ class ConfigStruct(ctypes.Structure):
         ("shock_enabled", ctypes.c_int32), ("shock_feedback", ctypes.c_int32),
         ("shock_interp", ctypes.c_int32), ("shock_eulerian", ctypes.c_int32),
         ("mapping", ctypes.c_int32), ("rk_variant", ctypes.c_int32),
-        ("viscosity_model", ctypes.c_int32), ("pad0", ctypes.c_int32),
+        ("viscosity_model", ctypes.c_int32), ("perturb_shock", ctypes.c_int32),
         ("gamma", ctypes.c_double), ("Pr", ctypes.c_double), ("Re", ctypes.c_double),
         ("Mach", ctypes.c_double),
         ("Tw_chi0", ctypes.c_double), ("Tw_eta0", ctypes.c_double), ("Tw_eta1", ctypes.c_double),
@@ -125,6 +125,7 @@ class Config:
     viscosity: str = "constant"          # "constant" (reference CPG) or "sutherland"
     sutherland_S: float = 110.4 / 300.0
     perturbation_magnitude: float = 1e-8
+    perturb_shock: bool = False          # stability_analysis.perturb_shock: shock-position unknowns
     disturbance_k: tuple = (1.0, 1.0)
     disturbance_amplitude: tuple = (0.0, 0.0, 0.0, 0.0)
 
@@ -189,6 +190,7 @@ def config_struct(cfg: Config) -> ConfigStruct:
     c.eta_refinement_power = mp.eta_refinement_power
     c.rho_min, c.CFL, c.max_dt = cfg.rho_min, cfg.CFL, cfg.max_dt
     c.perturbation_magnitude = cfg.perturbation_magnitude
+    c.perturb_shock = int(cfg.perturb_shock)
     c.sutherland_S = cfg.sutherland_S
     return c
 

@@ -597,7 +597,7 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
     d.err = reinterpret_cast<unsigned*>(b + header_doubles(d.nchi));
   }
   if ((r = pts(d.Yp))) return bail(r);
-  if ((r = dalloc(ctx, &d.beta, d.nchi)) ||
+  if ((r = dalloc(ctx, &d.beta, 2L * d.nchi)) ||
       (r = dalloc(ctx, &d.speed_x, d.nchi)) || (r = dalloc(ctx, &d.speed_y, d.nchi)) ||
       (r = dalloc(ctx, &d.rel, d.nchi)) || (r = dalloc(ctx, &d.spl, 17 * (long)d.nchi + 16)) ||
       (r = dalloc(ctx, &d.tiles, 2 + 2 * (long)flux_tiles(d))) ||
@@ -608,6 +608,7 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
     return bail(fail(ctx, HYMOR_ERR_CUDA, "multiprocessor count"));
   d.coef = nullptr;
   d.jwork = nullptr;
+  d.sj = ShockJac{};
   d.sf_zero = 1;  // the flux arrays are allocated zeroed
   for (int k = 0; k < hymor_ctx_s::kEv; ++k)
     if (cudaEventCreate(&ctx->cap_ev[k]) != cudaSuccess) return bail(fail(ctx, HYMOR_ERR_CUDA, "event"));

@@ -849,6 +849,10 @@ __global__ void __launch_bounds__(128) k_shock_columns(ColArgs A) {
     cb = fabs(dot) * ir;
   }
   if (i == 0 && c.bc_chi0 == HYMOR_BC_SYMMETRY) { sb = 1.0; cb = 0.0; }  // beta = pi/2, UPDATE_SHOCK_BC.jl:31-34
+  if (A.on_S) {  // s["shock"]["beta"], read by the shock-position linearisation
+    A.beta[i] = sb;
+    A.beta[nchi + i] = cb;
+  }
   // UPDATE_SHOCK_JUMP_PROPERTIES.jl:324-522 and EXTRAPOLATE_CELLS_SHOCK.jl:39-176
   const int sc = A.cell_idx[i];
   if (sc < 2 || sc > neta - 1) {

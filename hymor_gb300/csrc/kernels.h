@@ -5,6 +5,24 @@
 
 namespace hymor {
 
+// Shock-position blocks of the linearised operator (stability_analysis.perturb_shock,
+// LINEARIZE_EQUATIONS_NO_DISCONTINUITY.jl:140-274). With them the operator acts on
+// n = 4 Nchi Neta + Nchi unknowns: [rho; rho_u; rho_v; rho_E; r], r the normal
+// displacements of the shock points, and
+//   [A11 A12] with A12 writing only the flux rows (i, sc_i - 1) of every column,
+//   [A21 A22]      A21 reading only the cells (i, sc_i - 1), (i, sc_i - 2) of column i.
+struct ShockJac {
+  int on;          // the operator carries the shock unknowns
+  int* rows;       // Nchi: 1-based shocked row sc_i of each column at linearisation
+  double* a21;     // Nchi x 8, row-major: d speed_i / d q_v(i, sc_i - j) at (j - 1) * 4 + v
+  double* a12;     // 4 Nchi x Nchi, row-major, row v Nchi + i: d flux_v(i, sc_i - 1) / d r_p
+  double* a22;     // Nchi x Nchi, row-major: d speed_i / d r_p
+  double* a12t;    // transposes of a12 (Nchi x 4 Nchi) and a22, read by the transposed operator
+  double* a22t;
+  double* rel_b;   // Nchi: shock speeds of the base evaluation
+  double* dir;     // 2 x Nchi: PERTURB_SHOCK direction (cos ang, sin ang) of each point
+};
+
 struct DevCtx {
   hymor_config cfg;
   int nchi, neta, NI, NJ;
@@ -22,7 +40,8 @@ struct DevCtx {
   int sf_zero;     // SF is still all zero (nothing has written it since creation)
   ShockPts Sp, Yp, Ycp;  // shock points of S, Y and the classical snapshot
   int* cell_idx;   // 1-based shocked rows (Nchi)
-  double *beta, *speed_x, *speed_y, *rel;  // Nchi
+  double* beta;    // 2 x Nchi: sin and cos of the shock angle of the last shock update of S
+  double *speed_x, *speed_y, *rel;  // Nchi
   double* spl;     // spline workspace (device, sized for Nchi)
   double* cflw;    // CFL face rates (NLR + NBT)
   double* scal;    // Scalar block
@@ -32,7 +51,11 @@ struct DevCtx {
   // Jacobian
   double* coef;    // N * 144 stencil blocks (or null)
   double* jwork;   // linearisation workspace
+  ShockJac sj;
 };
+
+// Unknowns of the linearised operator: 4N, plus Nchi with the shock blocks.
+inline long op_size(const DevCtx& d) { return 4 * d.N + (d.sj.on ? d.nchi : 0); }
 
 // ---- core.cu ----
 // mode: 0 = Y <- S (all ghosted cells), thermo(Y); 1 = Y += wY F, S += wS F (interior,

@@ -7,6 +7,7 @@
 // addresses. hymor_jacobian_get/set convert to the per-cell block layout of
 // include/hymor.h.
 #include <cmath>
+#include <cstdio>
 #include <vector>
 
 #include <cooperative_groups.h>
@@ -62,7 +63,9 @@ Wrap make_wrap(const hymor_config& c) {
 
 // Y = S with variable `var` of every interior cell of colour `colour` (1..9, the
 // pattern of GET_PERTURBATION_MATRIX, LINEARIZE_EQUATIONS_NO_DISCONTINUITY.jl:959-983)
-// raised by flow_cells * eps; then p, T of Y.
+// raised by flow_cells * eps; then p, T of Y. shock_row = j > 0 raises instead the
+// cell (i, sc_i - j) of every column by eps (the flow-to-shock-speed perturbations,
+// :140-258).
 struct PertArgs {
   Cons S, Y;
   double *p, *T;
@@ -70,7 +73,7 @@ struct PertArgs {
   int nrcbc;
   const int* cell_idx;
   double eps, gm1;
-  int nchi, neta, var, colour, shock;
+  int nchi, neta, var, colour, shock, shock_row;
 };
 
 __global__ void k_perturb_thermo(PertArgs a) {
@@ -82,9 +85,13 @@ __global__ void k_perturb_thermo(PertArgs a) {
     const int i = (int)(k % NI), j = (int)(k / NI);
     double v[4] = {a.S.rho[k], a.S.ru[k], a.S.rv[k], a.S.rE[k]};
     if (a.var >= 0 && i >= 1 && i <= a.nchi && j >= 1 && j <= a.neta) {
-      const bool hit = (i >= si) && ((i - si) % 3 == 0) && (j >= sj) && ((j - sj) % 3 == 0);
-      const double flow = (!a.shock || j < a.cell_idx[i - 1]) ? 1.0 : 0.0;
-      v[a.var] = v[a.var] + flow * (hit ? 1.0 : 0.0) * a.eps;
+      if (a.shock_row) {
+        if (j == a.cell_idx[i - 1] - a.shock_row) v[a.var] += a.eps;
+      } else {
+        const bool hit = (i >= si) && ((i - si) % 3 == 0) && (j >= sj) && ((j - sj) % 3 == 0);
+        const double flow = (!a.shock || j < a.cell_idx[i - 1]) ? 1.0 : 0.0;
+        v[a.var] = v[a.var] + flow * (hit ? 1.0 : 0.0) * a.eps;
+      }
     }
     a.Y.rho[k] = v[0]; a.Y.ru[k] = v[1]; a.Y.rv[k] = v[2]; a.Y.rE[k] = v[3];
     const double ir = 1.0 / v[0];
@@ -155,6 +162,7 @@ struct MvArgs {
   double c_prev;
   Wrap w;
   long N;
+  long ld;  // vector stride (4N, or 4N + Nchi with the shock unknowns)
   int k, transpose;
 };
 
@@ -230,7 +238,7 @@ long mv_items(long N, int k, int sms) {
 
 __device__ __forceinline__ void matvec_multi(const MvArgs& a) {
   const long N = a.N;
-  const long n4 = 4 * N;
+  const long n4 = a.ld;
   const int chunks = (a.k + kVecChunk - 1) / kVecChunk;
   const long items = N * chunks;
   for (long w = blockIdx.x * (long)blockDim.x + threadIdx.x; w < items; w += (long)gridDim.x * blockDim.x) {
@@ -460,6 +468,160 @@ __global__ void k_block4(const double* B, const double* x, double* y, long N, in
   }
 }
 
+// Tail of vectors of 4N + nt entries: y = B x on the cells (k_block4), y = t x on the tail.
+__global__ void k_block4_tail(const double* B, const double* tail, const double* x, double* y, long N, long nt,
+                              int k) {
+  const long ld = 4 * N + nt;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < N * k; t += (long)gridDim.x * blockDim.x) {
+    const long m = t % N;
+    const long col = t / N;
+    const double* xc = x + col * ld;
+    double* yc = y + col * ld;
+    const double x0 = xc[m], x1 = xc[N + m], x2 = xc[2 * N + m], x3 = xc[3 * N + m];
+    const double* b = B + m * 16;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) yc[r * N + m] = fma(b[4 * r], x0, fma(b[4 * r + 1], x1, fma(b[4 * r + 2], x2, b[4 * r + 3] * x3)));
+    if (m < nt) yc[4 * N + m] = tail[m] * xc[4 * N + m];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Shock-position blocks (perturb_shock, LINEARIZE_EQUATIONS_NO_DISCONTINUITY.jl:140-274).
+
+// PERTURB_SHOCK (:906-913) direction of every point: ang = beta - pi/2 - phi with
+// phi = atan(rho_v_0, rho_u_0), so (cos ang, sin ang) = (sin(beta - phi), -cos(beta - phi)),
+// from the sine and cosine of beta that the last shock update of S stored.
+__global__ void k_shock_dir(const double* beta, double* dir, int nchi, double cph, double sph) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nchi) return;
+  const double sb = beta[i], cb = beta[nchi + i];
+  dir[i] = sb * cph - cb * sph;
+  dir[nchi + i] = -(cb * cph + sb * sph);
+}
+
+// Y's shock points = S's, point p displaced by eps along its PERTURB_SHOCK direction.
+__global__ void k_perturb_point(ShockPts S, ShockPts Y, const double* dir, int nchi, int p, double eps) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nchi) return;
+  double x = S.x[i], y = S.y[i];
+  if (i == p) {
+    x = x + eps * dir[i];
+    y = y + eps * dir[nchi + i];
+  }
+  Y.x[i] = x;
+  Y.y[i] = y;
+  Y.chi[i] = S.chi[i];
+  Y.eta[i] = S.eta[i];
+}
+
+// A21 column (j, var) of every point: (speed_i(x + eps e) - speed_i(x)) / eps
+// (GET_OUTPUT_INDEXING_A21, :800-820; REMOVE_BASE_OUTPUT, :935-946)
+__global__ void k_gather_a21(const double* rel, const double* rel_b, double* a21, int nchi, int col, double eps) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nchi) return;
+  a21[i * 8 + col] = (rel[i] - rel_b[i]) / eps;
+}
+
+// A12 and A22 columns of point p (GET_OUTPUT_INDEXING_A12_A22, :854-903): the flux of the
+// cells (i, sc_i - 1) and the shock speeds of every column.
+struct Flux4 {
+  const double* v[4];
+};
+__global__ void k_gather_a12(Flux4 Fp, Flux4 Fb, const double* rel, const double* rel_b, const int* rows,
+                             double* a12, double* a22, int nchi, int p, double eps) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nchi) return;
+  const long m = i + (long)(rows[i] - 2) * nchi;
+#pragma unroll
+  for (int v = 0; v < 4; ++v) a12[((long)v * nchi + i) * nchi + p] = (Fp.v[v][m] - Fb.v[v][m]) / eps;
+  a22[(long)i * nchi + p] = (rel[i] - rel_b[i]) / eps;
+}
+
+// out (cols x rows) = in (rows x cols) transposed, both row-major
+__global__ void k_transpose(const double* in, double* out, long rows, long cols) {
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < rows * cols; t += (long)gridDim.x * blockDim.x) {
+    const long r = t / cols, c = t % cols;
+    out[c * rows + r] = in[t];
+  }
+}
+
+struct ShockMvArgs {
+  ShockJac sj;
+  const double* X;
+  double* Y;
+  long N, ld;
+  double scale;
+  int nchi, k, transpose;
+};
+
+// The shock-block part of y = scale A x (after the stencil matvec has written y's cell
+// rows): one warp per output row, lanes over the row's entries, a fixed shuffle tree.
+//   forward:   rows (v, i) of A12 add scale (A12 r) into the flux rows (i, sc_i - 1);
+//              speed rows i set y_r = scale (A21 q + A22 r).
+//   transpose: speed rows p set y_r = scale (A12ᵀ q + A22ᵀ r); lanes 0-7 of the same warp
+//              add scale A21ᵀ r into the cells (p, sc_p - j).
+__global__ void __launch_bounds__(256) k_shock_mv(ShockMvArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int nchi = a.nchi;
+  const long N = a.N;
+  const int* rows = a.sj.rows;
+  const long per = a.transpose ? nchi : 5L * nchi;
+  const long warps = (long)gridDim.x * (blockDim.x / 32);
+  for (long w = (blockIdx.x * (long)blockDim.x + threadIdx.x) / 32; w < per * a.k; w += warps) {
+    const long col = w / per;
+    const int r = (int)(w % per);
+    const double* x = a.X + col * a.ld;
+    double* y = a.Y + col * a.ld;
+    const double* xr = x + 4 * N;
+    double s = 0;
+    if (!a.transpose) {
+      if (r < 4 * nchi) {
+        const double* row = a.sj.a12 + (long)r * nchi;
+        for (int p = lane; p < nchi; p += 32) s = fma(row[p], xr[p], s);
+        s = warp_sum(s);
+        if (lane == 0) {
+          const int v = r / nchi, i = r % nchi;
+          const long m = i + (long)(rows[i] - 2) * nchi;
+          y[v * N + m] += a.scale * s;
+        }
+      } else {
+        const int i = r - 4 * nchi;
+        const double* row = a.sj.a22 + (long)i * nchi;
+        for (int p = lane; p < nchi; p += 32) s = fma(row[p], xr[p], s);
+        if (lane < 8) {
+          const int j = lane / 4 + 1, v = lane % 4;
+          const long m = i + (long)(rows[i] - 1 - j) * nchi;
+          s = fma(a.sj.a21[i * 8 + lane], x[v * N + m], s);
+        }
+        s = warp_sum(s);
+        if (lane == 0) y[4 * N + i] = a.scale * s;
+      }
+    } else {
+      const int p = r;
+      const double* row = a.sj.a12t + (long)p * 4 * nchi;
+      for (int q = lane; q < 4 * nchi; q += 32) {
+        const int v = q / nchi, i = q % nchi;
+        s = fma(row[q], x[v * N + i + (long)(rows[i] - 2) * nchi], s);
+      }
+      const double* row2 = a.sj.a22t + (long)p * nchi;
+      for (int i = lane; i < nchi; i += 32) s = fma(row2[i], xr[i], s);
+      s = warp_sum(s);
+      if (lane == 0) y[4 * N + p] = a.scale * s;
+      if (lane < 8) {
+        const int j = lane / 4 + 1, v = lane % 4;
+        const long m = p + (long)(rows[p] - 1 - j) * nchi;
+        y[v * N + m] += a.scale * (a.sj.a21[p * 8 + lane] * xr[p]);
+      }
+    }
+  }
+}
+
+// acc += c t (n entries)
+__global__ void k_axpy(double* acc, const double* t, double c, long n) {
+  for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
+    acc[q] = fma(t[q], c, acc[q]);
+}
+
 int grid_for(long n, int threads) {
   long b = (n + threads - 1) / threads;
   const long cap = 152L * 16;
@@ -468,6 +630,24 @@ int grid_for(long n, int threads) {
 
 }  // namespace
 
+void launch_shock_mv(const DevCtx& d, int k, const double* X, double* Y, int transpose, double scale,
+                     cudaStream_t st) {
+  ShockMvArgs a;
+  a.sj = d.sj;
+  a.X = X;
+  a.Y = Y;
+  a.N = d.N;
+  a.ld = op_size(d);
+  a.scale = scale;
+  a.nchi = d.nchi;
+  a.k = k;
+  a.transpose = transpose;
+  const long warps = (transpose ? 1L : 5L) * d.nchi * k;
+  k_shock_mv<<<grid_for(warps * 32, 256), 256, 0, st>>>(a);
+}
+
+// y = scale A x over k vectors of op_size(d) entries: the stencil blocks, then the
+// shock-position blocks when the operator has them.
 void launch_matvec(const DevCtx& d, int k, const double* X, double* Y, int transpose, double scale,
                    cudaStream_t st) {
   MvArgs a;
@@ -481,12 +661,14 @@ void launch_matvec(const DevCtx& d, int k, const double* X, double* Y, int trans
   a.c_acc = 0;
   a.w = make_wrap(d.cfg);
   a.N = d.N;
+  a.ld = op_size(d);
   a.k = k;
   a.transpose = transpose;
   const long items = mv_items(d.N, k, d.sms);
   const int th = mv_threads(items, d.sms);
   if (mv_one(d.N, k, d.sms)) k_matvec<true><<<grid_for(items, th), th, 0, st>>>(a);
   else k_matvec<false><<<grid_for(items, th), th, 0, st>>>(a);
+  if (d.sj.on) launch_shock_mv(d, k, X, Y, transpose, scale, st);
 }
 
 // POWER_METHOD! (Eigenvalues/ARNOLDI_POWER_GPU.jl:64-82): per step vout = v,
@@ -494,7 +676,23 @@ void launch_matvec(const DevCtx& d, int k, const double* X, double* Y, int trans
 // already hold the input.
 static void launch_expm_body(const DevCtx& d, int k, double dt, int nsteps, int order, double* v, double* t1,
                              double* t2, double* vout, int transpose, cudaStream_t st) {
-  const long n = 4 * d.N * (long)k;
+  const long n = op_size(d) * (long)k;
+  if (d.sj.on) {
+    // with the shock blocks every term is a full operator application, then vout += term / j!
+    for (int s = 0; s < nsteps; ++s) {
+      const double* src = v;
+      long fact = 1;
+      for (int j = 1; j <= order; ++j) {
+        fact *= j;
+        double* dst = (j % 2) ? t1 : t2;
+        launch_matvec(d, k, src, dst, transpose, dt, st);
+        k_axpy<<<grid_for(n, 256), 256, 0, st>>>(vout, dst, 1.0 / (double)fact, n);
+        src = dst;
+      }
+      k_copy<<<grid_for(n, 256), 256, 0, st>>>(vout, v, n);
+    }
+    return;
+  }
   const long items = mv_items(d.N, k, d.sms);
   const int th = mv_threads(items, d.sms);
   MvArgs a;
@@ -503,6 +701,7 @@ static void launch_expm_body(const DevCtx& d, int k, double dt, int nsteps, int 
   a.coef = d.coef;
   a.w = make_wrap(d.cfg);
   a.N = d.N;
+  a.ld = n / k;
   a.k = k;
   a.transpose = transpose;
   a.scale = dt;
@@ -533,13 +732,58 @@ static void launch_expm_body(const DevCtx& d, int k, double dt, int nsteps, int 
 
 void launch_expm(const DevCtx& d, int k, double dt, int nsteps, int order, const double* X, double* Yout,
                  int transpose, double* work, cudaStream_t st) {
-  const long n = 4 * d.N * (long)k;
+  const long n = op_size(d) * (long)k;
   double* v = work;
   double* t1 = work + n;
   double* t2 = work + 2 * n;
   k_copy<<<grid_for(n, 256), 256, 0, st>>>(X, v, n);
   k_copy<<<grid_for(n, 256), 256, 0, st>>>(X, Yout, n);
   launch_expm_body(d, k, dt, nsteps, order, v, t1, t2, Yout, transpose, st);
+}
+
+// The shock-position blocks (perturb_shock), after the A11 assembly has left the base
+// flux in Fb and the base shock speeds in sj.rel_b, on the shocked rows d.cell_idx:
+//   A21 (LINEARIZE_EQUATIONS_NO_DISCONTINUITY.jl:140-258): the shock speed of column i
+//     reads only the cells (i, sc_i - 1) and (i, sc_i - 2) of its own column
+//     (UPDATE_SHOCK_JUMP_PROPERTIES.jl:354-405), so raising the cell (i, sc_i - j) of every
+//     column at once gives each column's speed the same inputs, and the same result, as the
+//     reference's one perturbed cell per residual; the reference's other entries of such
+//     a column are exact zeros. 8 residuals (j = 1, 2; 4 variables), no flux needed.
+//   A12, A22 (:262-274): one residual per shock point, the point moved by eps along the
+//     PERTURB_SHOCK direction (the smoothing spline couples every point to every other).
+void launch_shock_assemble(DevCtx& d, const double* const Fb[4], double* const Fp[4], PertArgs pa,
+                           cudaStream_t st) {
+  const hymor_config& c = d.cfg;
+  const int nchi = d.nchi;
+  const int cb = (nchi + 127) / 128;
+  const double eps = c.perturbation_magnitude;
+  const double h = std::hypot(c.rho_u_0, c.rho_v_0);
+  k_shock_dir<<<cb, 128, 0, st>>>(d.beta, d.sj.dir, nchi, c.rho_u_0 / h, c.rho_v_0 / h);
+  cudaMemcpyAsync(d.sj.rows, d.cell_idx, sizeof(int) * nchi, cudaMemcpyDeviceToDevice, st);
+  for (int j = 1; j <= 2; ++j)
+    for (int var = 0; var < 4; ++var) {
+      pa.var = var;
+      pa.shock_row = j;
+      k_perturb_thermo<<<grid_for(d.G, 256), 256, 0, st>>>(pa);
+      launch_shock_bc_flags(d, false, true, true, false, 0, st);
+      k_gather_a21<<<cb, 128, 0, st>>>(d.rel, d.sj.rel_b, d.sj.a21, nchi, (j - 1) * 4 + var, eps);
+    }
+  Flux4 fp, fb;
+  for (int v = 0; v < 4; ++v) {
+    fp.v[v] = Fp[v];
+    fb.v[v] = Fb[v];
+  }
+  pa.var = -1;
+  pa.shock_row = 0;
+  for (int p = 0; p < nchi; ++p) {
+    k_perturb_thermo<<<grid_for(d.G, 256), 256, 0, st>>>(pa);
+    k_perturb_point<<<cb, 128, 0, st>>>(d.Sp, d.Yp, d.sj.dir, nchi, p, eps);
+    launch_shock_bc_flags(d, false, false, true, true, 0, st);
+    launch_flux(d, false, Fp, st);
+    k_gather_a12<<<cb, 128, 0, st>>>(fp, fb, d.rel, d.sj.rel_b, d.sj.rows, d.sj.a12, d.sj.a22, nchi, p, eps);
+  }
+  k_transpose<<<grid_for(4L * nchi * nchi, 256), 256, 0, st>>>(d.sj.a12, d.sj.a12t, 4L * nchi, nchi);
+  k_transpose<<<grid_for((long)nchi * nchi, 256), 256, 0, st>>>(d.sj.a22, d.sj.a22t, nchi, nchi);
 }
 
 void launch_jacobian_assemble(DevCtx& d, cudaStream_t st) {
@@ -551,6 +795,7 @@ void launch_jacobian_assemble(DevCtx& d, cudaStream_t st) {
     Fb[v] = d.jwork + v * N;
     Fp[v] = d.jwork + (4 + v) * N;
   }
+  const bool shock_blocks = c.shock_enabled && c.perturb_shock;
   PertArgs pa;
   pa.S = d.S;
   pa.Y = d.Y;
@@ -562,6 +807,7 @@ void launch_jacobian_assemble(DevCtx& d, cudaStream_t st) {
   pa.nchi = d.nchi;
   pa.neta = d.neta;
   pa.shock = c.shock_enabled;
+  pa.shock_row = 0;
   pa.aY = d.aY;
   pa.nrcbc = (c.bc_chi0 == HYMOR_BC_OUTFLOW_NRCBC) | ((c.bc_chi1 == HYMOR_BC_OUTFLOW_NRCBC) << 1) |
              ((c.bc_eta0 == HYMOR_BC_OUTFLOW_NRCBC) << 2) | ((c.bc_eta1 == HYMOR_BC_OUTFLOW_NRCBC) << 3);
@@ -571,6 +817,8 @@ void launch_jacobian_assemble(DevCtx& d, cudaStream_t st) {
   k_perturb_thermo<<<grid_for(d.G, 256), 256, 0, st>>>(pa);
   launch_shock_bc_flags(d, false, true, c.shock_enabled, true, 0, st);
   launch_flux(d, false, Fb, st);
+  if (shock_blocks)
+    cudaMemcpyAsync(d.sj.rel_b, d.rel, sizeof(double) * d.nchi, cudaMemcpyDeviceToDevice, st);
   cudaMemsetAsync(d.coef, 0, sizeof(double) * 144 * N, st);
   ScatArgs sa;
   for (int v = 0; v < 4; ++v) { sa.Fp[v] = Fp[v]; sa.Fb[v] = Fb[v]; }
@@ -589,6 +837,7 @@ void launch_jacobian_assemble(DevCtx& d, cudaStream_t st) {
       sa.colour = colour;
       k_scatter<<<grid_for(N, 256), 256, 0, st>>>(sa);
     }
+  if (shock_blocks) launch_shock_assemble(d, Fb, Fp, pa, st);
 }
 
 }  // namespace hymor
@@ -596,6 +845,42 @@ void launch_jacobian_assemble(DevCtx& d, cudaStream_t st) {
 using namespace hymor;
 
 namespace {
+// Storage of the shock-position blocks (one allocation of doubles, one of the rows).
+int ensure_shock(hymor_ctx* ctx) {
+  DevCtx& d = ctx_dev(ctx);
+  if (d.sj.a12) return 0;
+  const long n = d.nchi;
+  void* p = nullptr;
+  if (cudaMalloc(&p, sizeof(double) * (8 * n + 10 * n * n + 3 * n)) != cudaSuccess)
+    return ctx_fail(ctx, HYMOR_ERR_CUDA, "shock-block allocation failed");
+  ctx_allocs(ctx).push_back(p);
+  double* b = static_cast<double*>(p);
+  ShockJac& j = d.sj;
+  j.a21 = b;
+  j.a12 = j.a21 + 8 * n;
+  j.a22 = j.a12 + 4 * n * n;
+  j.a12t = j.a22 + n * n;
+  j.a22t = j.a12t + 4 * n * n;
+  j.rel_b = j.a22t + n * n;
+  j.dir = j.rel_b + n;
+  if (cudaMalloc(&p, sizeof(int) * n) != cudaSuccess) return ctx_fail(ctx, HYMOR_ERR_CUDA, "shock-block allocation failed");
+  ctx_allocs(ctx).push_back(p);
+  j.rows = static_cast<int*>(p);
+  return 0;
+}
+
+// The A21 block reads the cells (i, sc_i - 2): a shocked row below 3 has no such cell (the
+// reference's column index i + (sc_i - 3) Nchi would be out of range).
+int check_shock_rows_for_blocks(hymor_ctx* ctx, const int* rows, int nchi, int neta) {
+  for (int i = 0; i < nchi; ++i)
+    if (rows[i] < 3 || rows[i] > neta - 1) {
+      char msg[200];
+      snprintf(msg, sizeof msg, "perturb_shock: shocked row %d of column %d outside 3..%d", rows[i], i + 1, neta - 1);
+      return ctx_fail(ctx, HYMOR_ERR_SHOCK_RANGE, msg);
+    }
+  return 0;
+}
+
 int ensure_linear(hymor_ctx* ctx) {
   DevCtx& d = ctx_dev(ctx);
   if (!d.coef) {
@@ -685,6 +970,7 @@ int expm_cooperative(hymor_ctx* ctx, int k, double dt, int nsteps, int order, co
   base.coef = d.coef;
   base.w = make_wrap(d.cfg);
   base.N = d.N;
+  base.ld = 4 * d.N;
   base.k = k;
   base.transpose = transpose;
   base.scale = dt;
@@ -719,6 +1005,9 @@ int hymor_linearize(hymor_ctx* ctx) {
   if (r) return r;
   DevCtx& d = ctx_dev(ctx);
   cudaStream_t st = ctx_stream(ctx);
+  const bool shock_blocks = d.cfg.shock_enabled && d.cfg.perturb_shock;
+  if (shock_blocks && (r = ensure_shock(ctx))) return r;
+  d.sj.on = 0;
   // LINEARIZE_L.jl:43-56: flow cells and shock BC, thermo, sound speed, boundary conditions
   if (d.cfg.shock_enabled) {
     launch_flow_cells(d, st);
@@ -729,9 +1018,79 @@ int hymor_linearize(hymor_ctx* ctx) {
   launch_update_thermo(d, 3, 0, 0, st);
   launch_sound_cmax(d, true, st);
   launch_shock_bc_flags(d, true, false, false, true, 1, st);
+  if (shock_blocks) {
+    std::vector<int> rows(d.nchi);
+    cudaMemcpyAsync(rows.data(), d.cell_idx, sizeof(int) * d.nchi, cudaMemcpyDeviceToHost, st);
+    if ((r = cuda_check(ctx, cudaStreamSynchronize(st)))) return r;
+    if ((r = check_shock_rows_for_blocks(ctx, rows.data(), d.nchi, d.neta))) return r;
+  }
   launch_jacobian_assemble(d, st);
   if ((r = cuda_check(ctx, cudaGetLastError()))) return r;
+  if ((r = cuda_check(ctx, cudaStreamSynchronize(st)))) return r;
+  d.sj.on = shock_blocks;
+  return 0;
+}
+
+int hymor_operator_size(hymor_ctx* ctx, int64_t* n) {
+  if (!ctx || !n) return HYMOR_ERR_INVALID;
+  *n = op_size(ctx_dev(ctx));
+  return 0;
+}
+
+int hymor_shock_blocks_get(hymor_ctx* ctx, int32_t* rows, double* a21, double* a12, double* a22) {
+  if (!ctx || !rows || !a21 || !a12 || !a22) return HYMOR_ERR_INVALID;
+  DevCtx& d = ctx_dev(ctx);
+  if (!d.sj.on) return ctx_fail(ctx, HYMOR_ERR_NOT_READY, "no shock blocks: linearise with perturb_shock");
+  cudaStream_t st = ctx_stream(ctx);
+  const long n = d.nchi;
+  cudaMemcpyAsync(rows, d.sj.rows, sizeof(int) * n, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(a21, d.sj.a21, sizeof(double) * 8 * n, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(a12, d.sj.a12, sizeof(double) * 4 * n * n, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(a22, d.sj.a22, sizeof(double) * n * n, cudaMemcpyDeviceToHost, st);
   return cuda_check(ctx, cudaStreamSynchronize(st));
+}
+
+int hymor_shock_blocks_set(hymor_ctx* ctx, const int32_t* rows, const double* a21, const double* a12,
+                           const double* a22) {
+  if (!ctx) return HYMOR_ERR_INVALID;
+  DevCtx& d = ctx_dev(ctx);
+  if (!rows) {
+    d.sj.on = 0;
+    return 0;
+  }
+  if (!a21 || !a12 || !a22) return HYMOR_ERR_INVALID;
+  if (!d.cfg.shock_enabled) return ctx_fail(ctx, HYMOR_ERR_INVALID, "shock blocks need shock fitting");
+  if (!d.coef) return ctx_fail(ctx, HYMOR_ERR_NOT_READY, "no Jacobian: call hymor_linearize or hymor_jacobian_set");
+  int r;
+  if ((r = check_shock_rows_for_blocks(ctx, rows, d.nchi, d.neta))) return r;
+  if ((r = ensure_shock(ctx))) return r;
+  cudaStream_t st = ctx_stream(ctx);
+  const long n = d.nchi;
+  cudaMemcpyAsync(d.sj.rows, rows, sizeof(int) * n, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(d.sj.a21, a21, sizeof(double) * 8 * n, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(d.sj.a12, a12, sizeof(double) * 4 * n * n, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(d.sj.a22, a22, sizeof(double) * n * n, cudaMemcpyHostToDevice, st);
+  k_transpose<<<grid_for(4 * n * n, 256), 256, 0, st>>>(d.sj.a12, d.sj.a12t, 4 * n, n);
+  k_transpose<<<grid_for(n * n, 256), 256, 0, st>>>(d.sj.a22, d.sj.a22t, n, n);
+  if ((r = cuda_check(ctx, cudaGetLastError()))) return r;
+  if ((r = cuda_check(ctx, cudaStreamSynchronize(st)))) return r;
+  d.sj.on = 1;
+  return 0;
+}
+
+int hymor_shock_fields(hymor_ctx* ctx, double* beta, double* rel_vel) {
+  if (!ctx) return HYMOR_ERR_INVALID;
+  DevCtx& d = ctx_dev(ctx);
+  cudaStream_t st = ctx_stream(ctx);
+  const long n = d.nchi;
+  std::vector<double> sc(2 * n);
+  cudaMemcpyAsync(sc.data(), d.beta, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, st);
+  if (rel_vel) cudaMemcpyAsync(rel_vel, d.rel, sizeof(double) * n, cudaMemcpyDeviceToHost, st);
+  int r = cuda_check(ctx, cudaStreamSynchronize(st));
+  if (r) return r;
+  if (beta)
+    for (long i = 0; i < n; ++i) beta[i] = std::atan2(sc[i], sc[n + i]);
+  return 0;
 }
 
 int hymor_jacobian_get(hymor_ctx* ctx, double* coef) {
@@ -777,7 +1136,7 @@ int hymor_matvec(hymor_ctx* ctx, int k, const double* X, double* Y, int transpos
   DevCtx& d = ctx_dev(ctx);
   if (!d.coef) return ctx_fail(ctx, HYMOR_ERR_NOT_READY, "no Jacobian: call hymor_linearize or hymor_jacobian_set");
   cudaStream_t st = ctx_stream(ctx);
-  const size_t bytes = sizeof(double) * 4 * d.N * (size_t)k;
+  const size_t bytes = sizeof(double) * op_size(d) * (size_t)k;
   double *dx = nullptr, *dy = nullptr;
   int r;
   if ((r = cuda_check(ctx, cudaMallocAsync((void**)&dx, bytes, st)))) return r;
@@ -804,7 +1163,7 @@ int hymor_bench_matvec(hymor_ctx* ctx, int k, const double* dX, double* dY, int 
     cudaEventDestroy(e0);
     return r;
   }
-  const long n4 = 4 * d.N;
+  const long n4 = op_size(d);
   cudaEventRecord(e0, st);
   for (int rep = 0; rep < reps; ++rep) {
     if (per_vector) {
@@ -828,8 +1187,11 @@ int hymor_expm_apply_dev(hymor_ctx* ctx, int k, double dt, int nsteps, int order
   DevCtx& d = ctx_dev(ctx);
   if (!d.coef) return ctx_fail(ctx, HYMOR_ERR_NOT_READY, "no Jacobian: call hymor_linearize or hymor_jacobian_set");
   cudaStream_t st = ctx_stream(ctx);
-  if ((long)nsteps * (order + 1) >= kExpmCoopMinLaunches) return expm_cooperative(ctx, k, dt, nsteps, order, dX, dY, transpose);
-  const size_t n = 4 * d.N * (size_t)k;
+  // the cooperative kernel covers the stencil operator; with the shock blocks each term
+  // is a launch sequence (launch_expm_body)
+  if (!d.sj.on && (long)nsteps * (order + 1) >= kExpmCoopMinLaunches)
+    return expm_cooperative(ctx, k, dt, nsteps, order, dX, dY, transpose);
+  const size_t n = op_size(d) * (size_t)k;
   double* work = nullptr;
   int r;
   if ((r = cuda_check(ctx, cudaMallocAsync((void**)&work, 3 * n * sizeof(double), st)))) return r;
@@ -843,7 +1205,7 @@ int hymor_expm_apply(hymor_ctx* ctx, int k, double dt, int nsteps, int order, co
   if (!ctx || k < 1 || !X || !Y) return HYMOR_ERR_INVALID;
   DevCtx& d = ctx_dev(ctx);
   cudaStream_t st = ctx_stream(ctx);
-  const size_t bytes = sizeof(double) * 4 * d.N * (size_t)k;
+  const size_t bytes = sizeof(double) * op_size(d) * (size_t)k;
   double *dx = nullptr, *dy = nullptr;
   int r;
   if ((r = cuda_check(ctx, cudaMallocAsync((void**)&dx, bytes, st)))) return r;
@@ -946,6 +1308,15 @@ int hymor_krylov_rotate(hymor_ctx* ctx, int64_t n, int m, int kk, double* dV, in
     cudaMemcpyAsync(dV + (long)c * ldv, k.tmp + (long)c * n, sizeof(double) * n, cudaMemcpyDeviceToDevice, st);
   if ((r = cuda_check(ctx, cudaGetLastError()))) return r;
   return cuda_check(ctx, cudaStreamSynchronize(st));
+}
+
+int hymor_block4_apply_ext_dev(hymor_ctx* ctx, int k, int64_t ntail, const double* dB, const double* dTail,
+                               const double* dX, double* dY) {
+  if (!ctx || k < 1 || ntail < 0 || !dB || (ntail && !dTail) || !dX || !dY) return HYMOR_ERR_INVALID;
+  DevCtx& d = ctx_dev(ctx);
+  if (ntail > d.N) return ctx_fail(ctx, HYMOR_ERR_INVALID, "block4 tail longer than the cell count");
+  k_block4_tail<<<grid_for(d.N * k, 256), 256, 0, ctx_stream(ctx)>>>(dB, dTail, dX, dY, d.N, ntail, k);
+  return cuda_check(ctx, cudaGetLastError());
 }
 
 int hymor_block4_apply_dev(hymor_ctx* ctx, int k, const double* dB, const double* dX, double* dY) {

@@ -11,9 +11,10 @@
 // Limits and sharing rules:
 //   * the array holds 3 x kNoAllocVec doubles (24 MiB) and is held by every GPU
 //     that loads libhymor until the process exits;
-//   * one call needs 3 work vectors of 4 * Nchi * Neta * k doubles, so
-//     4 * Nchi * Neta * k <= kNoAllocVec (1 048 576), e.g. Nchi * Neta <= 262 144 for
-//     one vector; larger requests return HYMOR_ERR_INVALID before any device work;
+//   * one call needs 3 work vectors of n * k doubles (n = 4 * Nchi * Neta, plus Nchi
+//     with the shock-position unknowns), so n * k <= kNoAllocVec (1 048 576), e.g.
+//     Nchi * Neta <= 262 144 for one vector; larger requests return HYMOR_ERR_INVALID
+//     before any device work;
 //   * all calls in the process share the array and it keeps the last call's
 //     contents; nothing in it has to start at zero (each call first copies its input
 //     into the work vectors). Calls whose GPU work overlaps (other streams, other
@@ -69,11 +70,11 @@ extern "C" int hymor_expm_apply_dev_noalloc(hymor_ctx* ctx, int k, double dt, in
   if (!ctx || k < 1 || nsteps < 0 || order < 1 || order > 20 || !dX || !dY) return HYMOR_ERR_INVALID;
   DevCtx& d = ctx_dev(ctx);
   if (!d.coef) return ctx_fail(ctx, HYMOR_ERR_NOT_READY, "no Jacobian: call hymor_linearize or hymor_jacobian_set");
-  const long n = 4 * d.N * (long)k;
+  const long n = op_size(d) * (long)k;
   if (n > kNoAllocVec) {
     char msg[256];
     snprintf(msg, sizeof msg,
-             "allocation-free propagator: 4 * Nchi * Neta * k = %ld exceeds its fixed work size of %ld doubles; "
+             "allocation-free propagator: (operator size) * k = %ld exceeds its fixed work size of %ld doubles; "
              "use hymor_expm_apply_dev",
              n, kNoAllocVec);
     return ctx_fail(ctx, HYMOR_ERR_INVALID, msg);

@@ -91,6 +91,20 @@ class Solution:
         self.ctx.check(self.ctx.L.hymor_counters(self.ctx.h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
 
+    def shock_fields(self) -> tuple[np.ndarray, np.ndarray]:
+        """(s["shock"]["beta"] of the last shock update of the solution, the relative shock
+        speeds of the last shock update), Nchi each."""
+        beta, rel = np.empty(self.nchi), np.empty(self.nchi)
+        self.ctx.check(self.ctx.L.hymor_shock_fields(self.ctx.h, dp(beta), dp(rel)))
+        return beta, rel
+
+    def operator_size(self) -> int:
+        """Unknowns of the linearised operator: 4 Nchi Neta, plus Nchi with the shock-position
+        blocks (perturb_shock)."""
+        n = ctypes.c_int64()
+        self.ctx.check(self.ctx.L.hymor_operator_size(self.ctx.h, ctypes.byref(n)))
+        return n.value
+
     def step_kernels(self) -> int:
         """Kernel launches one ADVECT_FLOW step makes (the kernel nodes of its graph)."""
         n = ctypes.c_int32()
@@ -141,14 +155,16 @@ def CFL_TIMESTEP(s: Solution) -> float:
 
 
 class LinearOperatorGPU:
-    """The linearised operator L (a Nchi*Neta*144 stencil-block Jacobian on the GPU).
+    """The linearised operator L (a Nchi*Neta*144 stencil-block Jacobian on the GPU, plus the
+    shock-position blocks when linearised with perturb_shock).
 
     Stands in for the reference's SparseMatrixCSC `L` of LINEARIZE_L: ``L @ x``,
-    ``L.T @ x`` and the Taylor propagator act on 4N-vectors (or 4N x k blocks)."""
+    ``L.T @ x`` and the Taylor propagator act on n-vectors (or n x k blocks), n = 4N, or
+    4N + Nchi with the shock unknowns (the reference's 4*Nchi*Neta + Nchi)."""
 
     def __init__(self, s: Solution, transpose: bool = False):
         self.s = s
-        self.n = 4 * s.N
+        self.n = s.operator_size()
         self.shape = (self.n, self.n)
         self.dtype = np.float64
         self._t = transpose
@@ -190,6 +206,27 @@ class LinearOperatorGPU:
         coef = np.ascontiguousarray(coef, dtype=np.float64)
         self.s.ctx.check(self.s.ctx.L.hymor_jacobian_set(self.s.ctx.h, dp(coef)))
 
+    def shock_blocks(self):
+        """(rows, a21, a12, a22) of the shock-position unknowns (include/hymor.h layouts:
+        Nchi; Nchi x 8; 4 Nchi x Nchi; Nchi x Nchi)."""
+        n = self.s.nchi
+        rows = np.empty(n, dtype=np.int32)
+        a21, a12, a22 = np.empty((n, 8)), np.empty((4 * n, n)), np.empty((n, n))
+        self.s.ctx.check(self.s.ctx.L.hymor_shock_blocks_get(self.s.ctx.h, ip(rows), dp(a21), dp(a12), dp(a22)))
+        return rows, a21, a12, a22
+
+    def set_shock_blocks(self, blocks):
+        """Sets the shock-position blocks (None turns the shock unknowns off)."""
+        L, h = self.s.ctx.L, self.s.ctx.h
+        if blocks is None:
+            self.s.ctx.check(L.hymor_shock_blocks_set(h, None, None, None, None))
+        else:
+            rows, a21, a12, a22 = blocks
+            rows = np.ascontiguousarray(rows, dtype=np.int32)
+            a21, a12, a22 = (np.ascontiguousarray(b, dtype=np.float64) for b in (a21, a12, a22))
+            self.s.ctx.check(L.hymor_shock_blocks_set(h, ip(rows), dp(a21), dp(a12), dp(a22)))
+        self.n = self.s.operator_size()
+
 
 def LINEARIZE_L(s: Solution):
     """LINEARIZE_L (LINEARIZE_L.jl:34-69): coloured finite-difference Jacobian of the
@@ -207,7 +244,8 @@ def CHECK_LINEARIZATION_L(L: LinearOperatorGPU, s: Solution, seed: int | None = 
     the linearised response L q against the finite difference f(x + q) - f(x) of the
     nonlinear residual, for a random perturbation q of every conserved variable (scaled by
     perturbation_magnitude, masked by the flow cells like the reference), both residuals on
-    copies of `s`. Returns (and prints) the reference's error measure
+    copies of `s`; with the shock unknowns the shock points move too and the shock speeds
+    are compared as well. Returns (and prints) the reference's error measure
     ||(L q - dq) / (|L q| + 1e-8)|| / sqrt(144 N); below ~1e-3 means consistent."""
     cfg, N = s.cfg, s.N
     nchi, neta = cfg.nchi, cfg.neta
@@ -228,13 +266,25 @@ def CHECK_LINEARIZATION_L(L: LinearOperatorGPU, s: Solution, seed: int | None = 
         # the reference masks q for rho only (:52-96); the masked Jacobian ignores the rest
         q[v * N:(v + 1) * N] = (dv if v == 0 else P * eps).ravel(order="F")
     pts = (st["pts_x"], st["pts_y"], st["pts_chi"], st["pts_eta"])
+    pts_p = pts
+    shock_unknowns = L.n > 4 * N
+    if shock_unknowns:
+        # the shock points move along PERTURB_SHOCK's direction by eps * randn (:92-100)
+        vp = rng.standard_normal(nchi)
+        beta, _ = s.shock_fields()
+        ang = beta - np.pi / 2 - np.arctan2(s._cs.rho_v_0, s._cs.rho_u_0)
+        pts_p = (st["pts_x"] + eps * np.cos(ang) * vp, st["pts_y"] + eps * np.sin(ang) * vp,
+                 st["pts_chi"], st["pts_eta"])
+        q = np.concatenate([q, eps * vp])
     base, pert = Solution(s.case), Solution(s.case)
     try:
         base.set_state(np.asarray(st["q"]), *pts, st["cell_idx"], st["t"])
-        pert.set_state(qs.ravel(), *pts, st["cell_idx"], st["t"])
+        pert.set_state(qs.ravel(), *pts_p, st["cell_idx"], st["t"])
         f0, f1 = PDE(base), PDE(pert)
         mask = np.tile(flow.ravel(order="F"), 4) if shock else 1.0
         dq = (f1 - f0) * mask
+        if shock_unknowns:
+            dq = np.concatenate([dq, pert.shock_fields()[1] - base.shock_fields()[1]])
     finally:
         base.close()
         pert.close()
@@ -280,18 +330,19 @@ def EIGENVALUES(L: LinearOperatorGPU, s: Solution, n_modes: int, T_ref: float = 
     block > 1 (device): block Krylov-Schur, `block` vectors propagated per batched call.
     flow_start: random start vectors that vanish outside the flow cells. The residual is
     masked by the flow cells, so the operator has zero rows there and leaves the flow-cell
-    subspace invariant; the other cells only add the trivial eigenvalue mu = 1 (lambda = 0),
-    which this excludes exactly."""
+    subspace invariant (with the shock unknowns too, which read and write only flow cells);
+    the other cells only add the trivial eigenvalue mu = 1 (lambda = 0), which this excludes
+    exactly."""
     import time
     dt = CFL_TIMESTEP(s)
     timesteps = int(round(T_ref / dt))
-    n = 4 * s.N
+    n = L.n
     ncv = ncv or max(2 * n_modes + 1, 20, n_modes + 4 * block)
     mask = None
     if flow_start and s.cfg.shock_enabled and s.cfg.shock_feedback:
         st = s.get_state()
         flow = (np.arange(1, s.cfg.neta + 1)[None, :] < st["cell_idx"][:, None]).ravel(order="F")
-        mask = np.tile(flow.astype(np.float64), 4)
+        mask = np.concatenate([np.tile(flow.astype(np.float64), 4), np.ones(n - 4 * s.N)])
     t0 = time.perf_counter()
     X = None
     if method == "device" and block > 1:
@@ -413,19 +464,34 @@ def TRANSIENT_GROWTH_DOWNSTREAM(L: LinearOperatorGPU, s: Solution, n_modes: int,
     K = np.linalg.cholesky(D)
     Kinv = np.linalg.inv(K)
     KinvT = np.transpose(Kinv, (0, 2, 1))
-    n = 4 * s.N
+    n = L.n
+    ntail = n - 4 * s.N
+    # shock-position unknowns: R is the identity on them (CONSTRUCT_R.jl:109-118), M has no
+    # entries there (CONSTRUCT_M.jl:88-92) and M^ weighs them by bt_area[i, sc_i] / 2
+    # (CONSTRUCT_M_HAT.jl:77-90), so C0 is 0 and K is sqrt(bt_area / 2) on the tail
+    tail_k = np.ones(1)
+    if ntail:
+        ci = s.get_state()["cell_idx"]
+        d_tail = np.asarray(s.case.mesh["bt_a"])[np.arange(s.nchi), ci - 1] / 2
+        tail_k = 1.0 / np.sqrt(d_tail)
     bufs = [DeviceBuffer(s.ctx, 8 * s.N * 16) for _ in range(3)]
     for b, arr in zip(bufs, (C0, Kinv, KinvT)):
         b.upload(np.ascontiguousarray(arr.reshape(-1)))
+    tails = [DeviceBuffer(s.ctx, 8 * max(ntail, 1)) for _ in range(2)]
+    tails[0].upload(np.zeros(max(ntail, 1)))
+    tails[1].upload(np.ascontiguousarray(tail_k if ntail else np.ones(1)))
     t1, t2 = DeviceBuffer(s.ctx, 8 * n * block), DeviceBuffer(s.ctx, 8 * n * block)
     Lh, h = s.ctx.L, s.ctx.h
 
+    def b4(k, B, tail, src, dst):
+        s.ctx.check(Lh.hymor_block4_apply_ext_dev(h, k, ntail, B.ptr, tail.ptr, src, dst))
+
     def apply_k(src, dst, k):
-        s.ctx.check(Lh.hymor_block4_apply_dev(h, k, bufs[2].ptr, src, t1.ptr))            # x = K^-T y
+        b4(k, bufs[2], tails[1], src, t1.ptr)                                              # x = K^-T y
         s.ctx.check(Lh.hymor_expm_apply_dev(h, k, dt, n_t, order, t1.ptr, t2.ptr, 0))      # P x
-        s.ctx.check(Lh.hymor_block4_apply_dev(h, k, bufs[0].ptr, t2.ptr, t1.ptr))          # C0 P x
+        b4(k, bufs[0], tails[0], t2.ptr, t1.ptr)                                           # C0 P x
         s.ctx.check(Lh.hymor_expm_apply_dev(h, k, dt, n_t, order, t1.ptr, t2.ptr, 1))      # Pᵀ C0 P x
-        s.ctx.check(Lh.hymor_block4_apply_dev(h, k, bufs[1].ptr, t2.ptr, dst))             # K^-1 (...)
+        b4(k, bufs[1], tails[1], t2.ptr, dst)                                              # K^-1 (...)
     ncv = ncv or max(2 * n_modes + 1, 16, n_modes + 4 * block)
     t0 = time.perf_counter()
     if block > 1:
@@ -435,16 +501,18 @@ def TRANSIENT_GROWTH_DOWNSTREAM(L: LinearOperatorGPU, s: Solution, n_modes: int,
         gains, resid, nops, Y = krylov_schur(s.ctx, n, lambda a, b: apply_k(a, b, 1), n_modes, ncv, tol=tol,
                                              maxit=maxit, seed=seed, symmetric=True, want_vectors=True)
     elapsed = time.perf_counter() - t0
-    for b in bufs + [t1, t2]:
+    for b in bufs + tails + [t1, t2]:
         b.free()
     gains = np.real(gains)
     converged = bool(np.all(resid <= tol * np.abs(gains)))
     X = None
     if modes and Y is not None:
         N = s.N
-        # x = K^-T y per cell: y as [rho; rho_u; rho_v; rho_E] blocks of N
-        Yc = Y.reshape(4, N, -1).transpose(1, 0, 2)                    # (N, 4, k)
-        X = np.einsum("nij,njk->nik", KinvT, Yc).transpose(1, 0, 2).reshape(n, -1)
+        # x = K^-T y per cell: y as [rho; rho_u; rho_v; rho_E] blocks of N (and the tail)
+        Yc = Y[:4 * N].reshape(4, N, -1).transpose(1, 0, 2)            # (N, 4, k)
+        X = np.einsum("nij,njk->nik", KinvT, Yc).transpose(1, 0, 2).reshape(4 * N, -1)
+        if ntail:
+            X = np.concatenate([X, Y[4 * N:] * tail_k[:, None]])
     if not converged and not keep_unconverged:
         import warnings
         warnings.warn(f"transient-growth solve did not reach tol {tol:g} in {maxit} restarts; returning NaN")

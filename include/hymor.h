@@ -58,7 +58,8 @@ typedef struct {
   int32_t mapping;                      /* HYMOR_MAP_*                                       */
   int32_t rk_variant;                   /* 0 reference Julia stages, 1 classical RK4         */
   int32_t viscosity_model;              /* 0 constant (reference CPG), 1 Sutherland          */
-  int32_t pad0;
+  int32_t perturb_shock;                /* stability_analysis.perturb_shock: the linearised   */
+                                        /* operator adds the Nchi shock-position unknowns    */
   double gamma, Pr, Re, Mach;
   double Tw_chi0, Tw_eta0, Tw_eta1;     /* wall temperature / freestream temperature         */
   double cv, energy_factor;             /* freestream cv, energy factor                      */
@@ -168,8 +169,32 @@ int hymor_linearize(hymor_ctx* ctx);
 /* Copy the blocks out (Nchi*Neta*144 doubles) / in. */
 int hymor_jacobian_get(hymor_ctx* ctx, double* coef);
 int hymor_jacobian_set(hymor_ctx* ctx, const double* coef);
-/* Y = L X (transpose 0) or Lᵀ X (transpose 1) for k vectors (4N x k, column-major),
- * host pointers. Replaces the CuSparse SpMV `mul!(term, A, v)` of
+
+/* Shock-position unknowns (stability_analysis.perturb_shock,
+ * LINEARIZE_EQUATIONS_NO_DISCONTINUITY.jl:140-274). hymor_linearize with cfg.perturb_shock
+ * also assembles, on the device, the blocks that couple the flow to the normal displacements
+ * r of the Nchi shock points; the operator then acts on n = 4 Nchi Neta + Nchi unknowns
+ * [rho; rho_u; rho_v; rho_E; r] (the reference's 4*Nchi*Neta + Nchi), and every matvec,
+ * propagator and vector length below uses that n. With sc_i the 1-based shocked row of
+ * column i at linearisation:
+ *   rows[i] = sc_i                                                         (Nchi)
+ *   a21[i*8 + (j-1)*4 + v] = d speed_i / d q_v(i, sc_i - j), j = 1, 2        (Nchi x 8)
+ *   a12[(v*Nchi + i)*Nchi + p] = d flux_v(i, sc_i - 1) / d r_p              (4 Nchi x Nchi)
+ *   a22[i*Nchi + p] = d speed_i / d r_p                                      (Nchi x Nchi)
+ * (speed = s["shock"]["relative_increase_velocity"]); every other entry of the reference's
+ * blocks is zero. Requires 3 <= sc_i <= Neta - 1. */
+int hymor_operator_size(hymor_ctx* ctx, int64_t* n);
+int hymor_shock_blocks_get(hymor_ctx* ctx, int32_t* rows, double* a21, double* a12, double* a22);
+/* Sets the blocks (after a Jacobian exists) and turns the shock unknowns on; rows == NULL
+ * turns them off (n = 4 Nchi Neta). */
+int hymor_shock_blocks_set(hymor_ctx* ctx, const int32_t* rows, const double* a21, const double* a12,
+                           const double* a22);
+/* s["shock"]["beta"] of the last shock update of the solution (Nchi angles) and the
+ * relative shock speeds of the last shock update (Nchi); either pointer may be NULL. */
+int hymor_shock_fields(hymor_ctx* ctx, double* beta, double* rel_vel);
+
+/* Y = L X (transpose 0) or Lᵀ X (transpose 1) for k vectors (n x k, column-major, n =
+ * hymor_operator_size), host pointers. Replaces the CuSparse SpMV `mul!(term, A, v)` of
  * Eigenvalues/ARNOLDI_POWER_GPU.jl:73 (and its transpose, TRANSIENT_GROWTH_DOWNSTREAM.jl:75). */
 int hymor_matvec(hymor_ctx* ctx, int k, const double* X, double* Y, int transpose);
 /* Same on device pointers (no copies). */
@@ -195,7 +220,7 @@ int hymor_expm_apply_dev(hymor_ctx* ctx, int k, double dt, int nsteps, int order
  * allocations: requires 4*Nchi*Neta*k <= 1048576 (else HYMOR_ERR_INVALID). All calls
  * share that array, so calls whose GPU work overlaps race; nothing in it needs to start
  * at zero. The first call on a device looks up the array's address: make it before any
- * stream capture. */
+ * stream capture. With the shock unknowns the limit is hymor_operator_size * k <= 1048576. */
 int hymor_expm_apply_dev_noalloc(hymor_ctx* ctx, int k, double dt, int nsteps, int order,
                                  const double* dX, double* dY, int transpose);
 
@@ -217,6 +242,10 @@ int hymor_krylov_rotate(hymor_ctx* ctx, int64_t n, int m, int k, double* dV, int
  * the Chu-norm weights R'MR and R'M^R of CONSTRUCT_R/M/M_HAT (Transient_growth_downstream/
  * CONSTRUCT_R.jl:24-133, CONSTRUCT_M.jl:27-94, CONSTRUCT_M_HAT.jl:25-105). */
 int hymor_block4_apply_dev(hymor_ctx* ctx, int k, const double* dB, const double* dX, double* dY);
+/* Same for k vectors of 4N + ntail entries: the cells as above, the tail scaled by dTail
+ * (ntail <= N doubles) — the shock-position entries of R'M^R (CONSTRUCT_M_HAT.jl:78-90). */
+int hymor_block4_apply_ext_dev(hymor_ctx* ctx, int k, int64_t ntail, const double* dB, const double* dTail,
+                               const double* dX, double* dY);
 
 /* Device buffer helpers for the *_dev entry points. */
 int hymor_device_alloc(hymor_ctx* ctx, uint64_t bytes, void** dptr);

@@ -70,7 +70,7 @@ typedef struct {
   int32_t mapping;            // ORC_MAP_*
   int32_t rk_variant;         // 0 = reference Julia (aliased stages), 1 = classical RK4
   int32_t viscosity_model;    // 0 = constant (reference CPG), 1 = Sutherland (extension)
-  int32_t pad0;
+  int32_t perturb_shock;      // stability_analysis.perturb_shock
   double gamma, Pr, Re, Mach;
   double Tw_chi0, Tw_eta0, Tw_eta1;  // wall temperature ratios (T_w / T_inf)
   double cv, energy_factor;          // freestream cv and energy factor (SET_FREESTREAM_PROPERTIES)
@@ -1233,6 +1233,105 @@ void linearize_equations(const orc_config& c, const Mesh& m, const State& s, dou
   }
 }
 
+// utils/Stability_analysis/Modal_stability_analysis/LINEARIZE_EQUATIONS_NO_DISCONTINUITY.jl:140-274
+// (perturb_shock = true), on the prepared state s (its beta from the last UPDATE_SHOCK_BC).
+//   rows[i] = sc_i (shock["cell_indices"]).
+//   a21_full: the reference's A21 columns as assembled. Per-point strategy when
+//     spline_param != 1 (:143-205): one residual per cell (i, sc_i - j), j = 1, 2, per
+//     variable; its column holds the change of every point's speed,
+//     a21_full[((v * 2 + j - 1) * Nchi + i) * Nchi + idx] (GET_OUTPUT_INDEXING_A21, :800-820).
+//     All-at-once strategy otherwise (:207-258): one residual per (v, j) raising the cell
+//     (i, sc_i - j) of every column; only the entries idx = i are assembled
+//     (GET_OUTPUT_INDEXING_A21_ALL, :829-850).
+//   a12[(v * Nchi + i) * Nchi + p], a22[i * Nchi + p]: one residual per shock point p moved by
+//     PERTURB_SHOCK (:906-913); the flux of cell (i, sc_i - 1) and every point's speed
+//     (GET_OUTPUT_INDEXING_A12_A22, :854-903).
+// Every difference is REMOVE_BASE_OUTPUT's (f(x + eps e) - f(x)) / eps (:935-946).
+void linearize_shock_blocks(const orc_config& c, const Mesh& m, const State& s, int* rows, double* a21_full,
+                            double* a12, double* a22) {
+  const int nchi = c.nchi;
+  const Dims d{nchi, c.neta};
+  const double eps = c.perturbation_magnitude;
+  State base = s;
+  non_linear_dynamics(c, m, base);
+  for (int i = 0; i < nchi; ++i) rows[i] = s.cell_idx[i];
+  std::memset(a21_full, 0, sizeof(double) * 8 * (size_t)nchi * nchi);
+  auto var_of = [](State& st, int v) -> vec& {
+    return v == 0 ? st.rho : v == 1 ? st.rho_u : v == 2 ? st.rho_v : st.rho_E;
+  };
+  auto speed_diff = [&](const State& sp, int idx) { return (sp.rel_vel[idx] - base.rel_vel[idx]) / eps; };
+  for (int v = 0; v < 4; ++v)
+    for (int j = 1; j <= 2; ++j) {
+      if (c.spline_param != 1) {
+        for (int i = 1; i <= nchi; ++i) {
+          State sp = s;
+          var_of(sp, v)[d.gi(i + 1, s.cell_idx[i - 1] - j + 1)] += eps;
+          non_linear_dynamics(c, m, sp);
+          double* col = a21_full + ((size_t)(v * 2 + j - 1) * nchi + (i - 1)) * nchi;
+          for (int idx = 0; idx < nchi; ++idx) col[idx] = speed_diff(sp, idx);
+        }
+      } else {
+        State sp = s;
+        for (int i = 1; i <= nchi; ++i) var_of(sp, v)[d.gi(i + 1, s.cell_idx[i - 1] - j + 1)] += eps;
+        non_linear_dynamics(c, m, sp);
+        for (int idx = 0; idx < nchi; ++idx)
+          a21_full[((size_t)(v * 2 + j - 1) * nchi + idx) * nchi + idx] = speed_diff(sp, idx);
+      }
+    }
+  const double phi = std::atan2(c.rho_v_0, c.rho_u_0);
+  for (int p = 0; p < nchi; ++p) {
+    State sp = s;
+    const double ang = s.beta[p] - M_PI / 2 - phi;
+    sp.pts_x[p] += eps * std::cos(ang);
+    sp.pts_y[p] += eps * std::sin(ang);
+    non_linear_dynamics(c, m, sp);
+    const vec* fp[4] = {&sp.flux_rho, &sp.flux_rho_u, &sp.flux_rho_v, &sp.flux_rho_E};
+    const vec* fb[4] = {&base.flux_rho, &base.flux_rho_u, &base.flux_rho_v, &base.flux_rho_E};
+    for (int i = 1; i <= nchi; ++i) {
+      const int k = d.ci(i, s.cell_idx[i - 1] - 1);
+      for (int v = 0; v < 4; ++v)
+        a12[((size_t)v * nchi + (i - 1)) * nchi + p] = ((*fp[v])[k] - (*fb[v])[k]) / eps;
+      a22[(size_t)(i - 1) * nchi + p] = speed_diff(sp, i - 1);
+    }
+  }
+}
+
+// The shock-block part of y = A x on vectors [q (4N); r (Nchi)], after stencil_matvec has
+// written y's first 4N entries; a21 compact (Nchi x 8, entry (j - 1) * 4 + v).
+void shock_matvec(const orc_config& c, const int* rows, const double* a21, const double* a12, const double* a22,
+                  const double* x, double* y, int transpose) {
+  const int nchi = c.nchi;
+  const size_t N = (size_t)nchi * c.neta;
+  const double* xr = x + 4 * N;
+  double* yr = y + 4 * N;
+  auto cell = [&](int i, int row1) { return (size_t)i + (size_t)(row1 - 1) * nchi; };  // 0-based i, 1-based row
+  if (!transpose) {
+    for (int i = 0; i < nchi; ++i) {
+      for (int v = 0; v < 4; ++v) {
+        double acc = 0;
+        for (int p = 0; p < nchi; ++p) acc += a12[((size_t)v * nchi + i) * nchi + p] * xr[p];
+        y[v * N + cell(i, rows[i] - 1)] += acc;
+      }
+      double acc = 0;
+      for (int j = 1; j <= 2; ++j)
+        for (int v = 0; v < 4; ++v) acc += a21[i * 8 + (j - 1) * 4 + v] * x[v * N + cell(i, rows[i] - j)];
+      for (int p = 0; p < nchi; ++p) acc += a22[(size_t)i * nchi + p] * xr[p];
+      yr[i] = acc;
+    }
+  } else {
+    for (int p = 0; p < nchi; ++p) {
+      double acc = 0;
+      for (int v = 0; v < 4; ++v)
+        for (int i = 0; i < nchi; ++i) acc += a12[((size_t)v * nchi + i) * nchi + p] * x[v * N + cell(i, rows[i] - 1)];
+      for (int i = 0; i < nchi; ++i) acc += a22[(size_t)i * nchi + p] * xr[i];
+      yr[p] = acc;
+    }
+    for (int i = 0; i < nchi; ++i)
+      for (int j = 1; j <= 2; ++j)
+        for (int v = 0; v < 4; ++v) y[v * N + cell(i, rows[i] - j)] += a21[i * 8 + (j - 1) * 4 + v] * xr[i];
+  }
+}
+
 // y = L x (transpose = 0) or y = Lᵀ x (transpose = 1) with the stencil blocks;
 // vectors ordered [rho; rho_u; rho_v; rho_E], each Nchi*Neta chi-fastest
 // (CHECK_LINEARIZATION_L.jl:52).
@@ -1427,6 +1526,11 @@ static void copy_flux_out(orc_ctx* c, double* flux) {
 // The entry points that run the shock chain return 0, or -1 with orc_last_error() set
 // when the reference would have raised (a shocked row out of range).
 static thread_local std::string g_orc_error;
+// s["shock"]["relative_increase_velocity"] of the last shock update (Nchi).
+void orc_get_rel_vel(orc_ctx* c, double* rel) {
+  for (int i = 0; i < c->c.nchi; ++i) rel[i] = i < (int)c->s.rel_vel.size() ? c->s.rel_vel[i] : 0.0;
+}
+
 const char* orc_last_error() { return g_orc_error.c_str(); }
 #define ORC_GUARD(body)                     \
   try {                                     \
@@ -1505,6 +1609,48 @@ void orc_jacobian(orc_ctx* c, double* coef) { linearize_equations(c->c, c->m, c-
 
 void orc_matvec(const orc_config* cfg, const double* coef, const double* x, double* y, int transpose) {
   stencil_matvec(*cfg, coef, x, y, transpose);
+}
+
+// Shock-position blocks of the prepared state (run orc_linearize first; see
+// linearize_shock_blocks for the layouts).
+int orc_shock_blocks(orc_ctx* c, int32_t* rows, double* a21_full, double* a12, double* a22) {
+  ORC_GUARD(linearize_shock_blocks(c->c, c->m, c->s, rows, a21_full, a12, a22));
+}
+
+// y = A x on the extended vectors (4N + Nchi), a21 compact (Nchi x 8).
+void orc_matvec_ext(const orc_config* cfg, const double* coef, const int32_t* rows, const double* a21,
+                    const double* a12, const double* a22, const double* x, double* y, int transpose) {
+  stencil_matvec(*cfg, coef, x, y, transpose);
+  shock_matvec(*cfg, rows, a21, a12, a22, x, y, transpose);
+}
+
+// POWER_METHOD! with the extended operator: term = (A dt) v (A dt scaled entry by entry, as
+// CuSparseMatrixCSC(A * dt)), v = term, vout += v / j!; v = vout after each step.
+void orc_expm_ext(const orc_config* cfg, const double* coef, const int32_t* rows, const double* a21,
+                  const double* a12, const double* a22, double dt, int nsteps, int order, const double* x,
+                  double* y, int transpose) {
+  const size_t nchi = cfg->nchi;
+  const size_t n = (size_t)4 * cfg->nchi * cfg->neta + nchi;
+  const size_t nc = (size_t)cfg->nchi * cfg->neta * 144;
+  vec cdt(nc), b21(8 * nchi), b12(4 * nchi * nchi), b22(nchi * nchi);
+  for (size_t k = 0; k < nc; ++k) cdt[k] = coef[k] * dt;
+  for (size_t k = 0; k < b21.size(); ++k) b21[k] = a21[k] * dt;
+  for (size_t k = 0; k < b12.size(); ++k) b12[k] = a12[k] * dt;
+  for (size_t k = 0; k < b22.size(); ++k) b22[k] = a22[k] * dt;
+  vec v(x, x + n), vout(x, x + n), term(n);
+  for (int st = 0; st < nsteps; ++st) {
+    long long fact = 1;
+    for (int j = 1; j <= order; ++j) {
+      stencil_matvec(*cfg, cdt.data(), v.data(), term.data(), transpose);
+      shock_matvec(*cfg, rows, b21.data(), b12.data(), b22.data(), v.data(), term.data(), transpose);
+      v = term;
+      fact = j * fact;
+      double r = 1.0 / (double)fact;
+      for (size_t k = 0; k < n; ++k) vout[k] += v[k] * r;
+    }
+    v = vout;
+  }
+  std::memcpy(y, vout.data(), n * 8);
 }
 
 // POWER_METHOD! (ARNOLDI_POWER_GPU.jl:64-82): x <- (Σ_{j<=order} (A dt)^j / j!)^nsteps x,

@@ -46,6 +46,11 @@ def lib() -> ctypes.CDLL:
         L.orc_expm.argtypes = [vp, dp, ctypes.c_double, ctypes.c_int, ctypes.c_int, dp, dp,
                                ctypes.c_int]
         L.orc_set_threads.argtypes = [ctypes.c_int]
+        L.orc_shock_blocks.argtypes = [vp, ip, dp, dp, dp]
+        L.orc_get_rel_vel.argtypes = [vp, dp]
+        L.orc_matvec_ext.argtypes = [vp, dp, ip, dp, dp, dp, dp, dp, ctypes.c_int]
+        L.orc_expm_ext.argtypes = [vp, dp, ip, dp, dp, dp, ctypes.c_double, ctypes.c_int, ctypes.c_int, dp, dp,
+                                   ctypes.c_int]
         _lib = L
     return _lib
 
@@ -148,12 +153,58 @@ class Oracle:
         lib().orc_matvec(ctypes.byref(self.cs), dptr(coef), dptr(x), dptr(y), int(transpose))
         return y
 
+    def rel_vel(self) -> np.ndarray:
+        """s["shock"]["relative_increase_velocity"] of the last shock update."""
+        r = np.empty(self.cs.nchi)
+        lib().orc_get_rel_vel(self.h, dptr(r))
+        return r
+
+    def shock_blocks(self):
+        """The shock-position blocks of the prepared state (after linearize()): rows (Nchi),
+        a21_full (8 Nchi x Nchi: the reference's A21 columns, column (v*2 + j-1)*Nchi + i),
+        a12 (4 Nchi x Nchi), a22 (Nchi x Nchi)."""
+        n = self.cs.nchi
+        rows = np.empty(n, dtype=np.int32)
+        a21 = np.empty(8 * n * n)
+        a12 = np.empty(4 * n * n)
+        a22 = np.empty(n * n)
+        _check(lib().orc_shock_blocks(self.h, _ip(rows), dptr(a21), dptr(a12), dptr(a22)))
+        return rows, a21.reshape(8 * n, n), a12.reshape(4 * n, n), a22.reshape(n, n)
+
+    def matvec_ext(self, coef, blocks, x, transpose=False):
+        rows, a21, a12, a22 = (np.ascontiguousarray(b) for b in blocks)
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty(4 * self.N + self.cs.nchi)
+        lib().orc_matvec_ext(ctypes.byref(self.cs), dptr(coef), _ip(rows), dptr(a21), dptr(a12), dptr(a22),
+                             dptr(x), dptr(y), int(transpose))
+        return y
+
+    def expm_ext(self, coef, blocks, dt, nsteps, x, order=5, transpose=False):
+        rows, a21, a12, a22 = (np.ascontiguousarray(b) for b in blocks)
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty(4 * self.N + self.cs.nchi)
+        lib().orc_expm_ext(ctypes.byref(self.cs), dptr(coef), _ip(rows), dptr(a21), dptr(a12), dptr(a22),
+                           float(dt), int(nsteps), int(order), dptr(x), dptr(y), int(transpose))
+        return y
+
     def expm(self, coef, dt, nsteps, x, order=5, transpose=False):
         x = np.ascontiguousarray(x, dtype=np.float64)
         y = np.empty(4 * self.N)
         lib().orc_expm(ctypes.byref(self.cs), dptr(coef), float(dt), int(nsteps), int(order),
                        dptr(x), dptr(y), int(transpose))
         return y
+
+
+def compact_a21(rows, a21_full):
+    """The stencil-compact A21 (Nchi x 8, entry (j-1)*4 + v) of the reference's columns: the
+    column of cell (i, sc_i - j), variable v, contributes its entry for point i."""
+    n = len(rows)
+    F = np.asarray(a21_full).reshape(4, 2, n, n)       # (v, j-1, perturbed column i, point idx)
+    out = np.empty((n, 8))
+    for v in range(4):
+        for j in range(2):
+            out[:, j * 4 + v] = F[v, j, np.arange(n), np.arange(n)]
+    return out
 
 
 def spline(xs, ys, lam, t):
