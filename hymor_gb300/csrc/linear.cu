@@ -555,62 +555,76 @@ struct ShockMvArgs {
 };
 
 // The shock-block part of y = scale A x (after the stencil matvec has written y's cell
-// rows): one warp per output row, lanes over the row's entries, a fixed shuffle tree.
+// rows). Block (bx, col) stages what every row of vector col reads — r, and for the
+// transpose the cells (i, sc_i - 1) of q — in shared memory, then gives each of its warps
+// whole output rows: lanes over the row's entries (coalesced), a fixed shuffle tree.
 //   forward:   rows (v, i) of A12 add scale (A12 r) into the flux rows (i, sc_i - 1);
 //              speed rows i set y_r = scale (A21 q + A22 r).
 //   transpose: speed rows p set y_r = scale (A12ᵀ q + A22ᵀ r); lanes 0-7 of the same warp
 //              add scale A21ᵀ r into the cells (p, sc_p - j).
-__global__ void __launch_bounds__(256) k_shock_mv(ShockMvArgs a) {
+constexpr int kShockThreads = 128;
+__host__ __device__ inline long shock_mv_smem(int nchi, int transpose) {
+  return (long)(transpose ? 5 : 1) * nchi * (long)sizeof(double);
+}
+
+// Σ_p a[p] b[p] over the lane's entries p = lane, lane + 32, ... (one FMA chain: the FP64
+// pipe, not the loads, bounds these rows; partial sums would add FP64 instructions)
+__device__ __forceinline__ double lane_dot(const double* __restrict__ a, const double* b, int n, int lane) {
+  double t = 0;
+  for (int p = lane; p < n; p += 32) t = fma(a[p], b[p], t);
+  return t;
+}
+
+__global__ void __launch_bounds__(kShockThreads) k_shock_mv(ShockMvArgs a) {
+  extern __shared__ double sh[];
   const int lane = threadIdx.x & 31;
   const int nchi = a.nchi;
   const long N = a.N;
   const int* rows = a.sj.rows;
-  const long per = a.transpose ? nchi : 5L * nchi;
-  const long warps = (long)gridDim.x * (blockDim.x / 32);
-  for (long w = (blockIdx.x * (long)blockDim.x + threadIdx.x) / 32; w < per * a.k; w += warps) {
-    const long col = w / per;
-    const int r = (int)(w % per);
-    const double* x = a.X + col * a.ld;
-    double* y = a.Y + col * a.ld;
-    const double* xr = x + 4 * N;
+  const long col = blockIdx.y;
+  const double* x = a.X + col * a.ld;
+  double* y = a.Y + col * a.ld;
+  const double* xr = x + 4 * N;
+  double* sr = sh;  // r
+  if (a.transpose) {
+    sr = sh + 4 * nchi;
+    for (int t = threadIdx.x; t < 4 * nchi; t += blockDim.x) {
+      const int v = t / nchi, i = t % nchi;
+      sh[t] = x[v * N + i + (long)(rows[i] - 2) * nchi];
+    }
+  }
+  for (int t = threadIdx.x; t < nchi; t += blockDim.x) sr[t] = xr[t];
+  __syncthreads();
+  const int per = a.transpose ? nchi : 5 * nchi;
+  const int wpb = blockDim.x / 32;
+  for (int r = blockIdx.x * wpb + (threadIdx.x >> 5); r < per; r += gridDim.x * wpb) {
     double s = 0;
     if (!a.transpose) {
       if (r < 4 * nchi) {
-        const double* row = a.sj.a12 + (long)r * nchi;
-        for (int p = lane; p < nchi; p += 32) s = fma(row[p], xr[p], s);
-        s = warp_sum(s);
+        s = warp_sum(lane_dot(a.sj.a12 + (long)r * nchi, sr, nchi, lane));
         if (lane == 0) {
           const int v = r / nchi, i = r % nchi;
-          const long m = i + (long)(rows[i] - 2) * nchi;
-          y[v * N + m] += a.scale * s;
+          y[v * N + i + (long)(rows[i] - 2) * nchi] += a.scale * s;
         }
       } else {
         const int i = r - 4 * nchi;
-        const double* row = a.sj.a22 + (long)i * nchi;
-        for (int p = lane; p < nchi; p += 32) s = fma(row[p], xr[p], s);
+        s = lane_dot(a.sj.a22 + (long)i * nchi, sr, nchi, lane);
         if (lane < 8) {
           const int j = lane / 4 + 1, v = lane % 4;
-          const long m = i + (long)(rows[i] - 1 - j) * nchi;
-          s = fma(a.sj.a21[i * 8 + lane], x[v * N + m], s);
+          s = fma(a.sj.a21[i * 8 + lane], x[v * N + i + (long)(rows[i] - 1 - j) * nchi], s);
         }
         s = warp_sum(s);
         if (lane == 0) y[4 * N + i] = a.scale * s;
       }
     } else {
       const int p = r;
-      const double* row = a.sj.a12t + (long)p * 4 * nchi;
-      for (int q = lane; q < 4 * nchi; q += 32) {
-        const int v = q / nchi, i = q % nchi;
-        s = fma(row[q], x[v * N + i + (long)(rows[i] - 2) * nchi], s);
-      }
-      const double* row2 = a.sj.a22t + (long)p * nchi;
-      for (int i = lane; i < nchi; i += 32) s = fma(row2[i], xr[i], s);
+      s = lane_dot(a.sj.a12t + (long)p * 4 * nchi, sh, 4 * nchi, lane);
+      s += lane_dot(a.sj.a22t + (long)p * nchi, sr, nchi, lane);
       s = warp_sum(s);
       if (lane == 0) y[4 * N + p] = a.scale * s;
       if (lane < 8) {
         const int j = lane / 4 + 1, v = lane % 4;
-        const long m = p + (long)(rows[p] - 1 - j) * nchi;
-        y[v * N + m] += a.scale * (a.sj.a21[p * 8 + lane] * xr[p]);
+        y[v * N + p + (long)(rows[p] - 1 - j) * nchi] += a.scale * (a.sj.a21[p * 8 + lane] * sr[p]);
       }
     }
   }
@@ -642,8 +656,13 @@ void launch_shock_mv(const DevCtx& d, int k, const double* X, double* Y, int tra
   a.nchi = d.nchi;
   a.k = k;
   a.transpose = transpose;
-  const long warps = (transpose ? 1L : 5L) * d.nchi * k;
-  k_shock_mv<<<grid_for(warps * 32, 256), 256, 0, st>>>(a);
+  // enough blocks per vector to spread the rows over the SMs, few enough that staging
+  // the vector into each block stays small next to the blocks' reads of A12 and A22
+  const long per = (transpose ? 1L : 5L) * d.nchi;
+  const long wpb = kShockThreads / 32;
+  const long cap = std::max(1L, 8L * d.sms / k);
+  const int bx = (int)std::max(1L, std::min((per + wpb - 1) / wpb, cap));
+  k_shock_mv<<<dim3(bx, k), kShockThreads, shock_mv_smem(d.nchi, transpose), st>>>(a);
 }
 
 // y = scale A x over k vectors of op_size(d) entries: the stencil blocks, then the
@@ -866,6 +885,11 @@ int ensure_shock(hymor_ctx* ctx) {
   if (cudaMalloc(&p, sizeof(int) * n) != cudaSuccess) return ctx_fail(ctx, HYMOR_ERR_CUDA, "shock-block allocation failed");
   ctx_allocs(ctx).push_back(p);
   j.rows = static_cast<int*>(p);
+  // the transposed shock matvec stages 5 Nchi doubles per block
+  const long smem = shock_mv_smem(d.nchi, 1);
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(k_shock_mv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return ctx_fail(ctx, HYMOR_ERR_INVALID, "perturb_shock: Nchi too large for the shock matvec's shared memory");
   return 0;
 }
 
