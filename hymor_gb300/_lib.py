@@ -36,6 +36,7 @@ EXPORTS = [
     "hymor_expm_apply_dev_noalloc", "hymor_step_kernels", "hymor_fp64_peak",
     "hymor_profile_phases", "hymor_advect", "hymor_bench_matvec", "hymor_operator_size",
     "hymor_shock_blocks_get", "hymor_shock_blocks_set", "hymor_shock_fields", "hymor_block4_apply_ext_dev",
+    "hymor_expm_apply_multi_dev",
 ]
 
 
@@ -88,6 +89,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "hymor_expm_apply": [vp, i, d, i, i, dp, dp, i],
         "hymor_expm_apply_dev": [vp, i, d, i, i, vp, vp, i],
         "hymor_expm_apply_dev_noalloc": [vp, i, d, i, i, vp, vp, i],
+        "hymor_expm_apply_multi_dev": [vp, i, dp, ip, i, vp, vp, i],
         "hymor_device_alloc": [vp, ctypes.c_uint64, ctypes.POINTER(vp)],
         "hymor_device_free": [vp, vp],
         "hymor_memcpy_h2d": [vp, vp, vp, ctypes.c_uint64],

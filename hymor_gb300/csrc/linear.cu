@@ -160,6 +160,9 @@ struct MvArgs {
   // of a step can read acc as its input without a copy
   const double* acc_prev;
   double c_prev;
+  // per-vector scale (k entries) replacing `scale`, or null: a batch of propagations with
+  // different time steps (transient-growth horizons)
+  const double* vscale;
   Wrap w;
   long N;
   long ld;  // vector stride (4N, or 4N + Nchi with the shock unknowns)
@@ -170,18 +173,23 @@ struct MvArgs {
 // kVecChunk vectors) pairs, cell fastest, over a grid-stride loop: a batch of vectors on
 // a small grid still spreads over every SM (a 100 x 80 grid is 8000 cells, 64 vectors are
 // 16 chunks of it), and neighbouring threads read neighbouring cells.
-// One vector (k = 1): one thread per (cell, output component), the same FMA chain per
-// output as matvec_multi (bit-identical). On GB300 one warp issues one FP64 instruction per
-// ~76 cycles of its SM sub-partition, so a warp per 32 cells (148 FP64 instructions each)
-// would bound a small grid's matvec by its own issue rate; four threads per cell spread the
-// work over four times the warps. The next neighbour block's coefficients and inputs are
-// loaded while the current block's FMAs run.
+// Few cells x vectors (a small grid, one or a few vectors): one thread per (cell, output
+// component, vector), the same FMA chain per output as matvec_multi (bit-identical). On
+// GB300 one warp issues one FP64 instruction per ~76 cycles of its SM sub-partition, so a
+// warp per 32 cells (148 FP64 instructions each, per vector) would bound a small grid's
+// matvec by its own issue rate; a thread per output spreads the work over four times the
+// warps per vector. The next neighbour block's coefficients and inputs are loaded while
+// the current block's FMAs run.
 __device__ __forceinline__ void matvec_one(const MvArgs& a) {
   const long N = a.N;
-  for (long w = blockIdx.x * (long)blockDim.x + threadIdx.x; w < 4 * N; w += (long)gridDim.x * blockDim.x) {
+  const long outs = 4 * N;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < outs * a.k; t += (long)gridDim.x * blockDim.x) {
+    const long vec = t / outs;
+    const long w = t - vec * outs;
     const long m = w % N;
     const int comp = (int)(w / N);  // output component (v_out, or v_in of the transpose)
     const int i = (int)(m % a.w.nchi), j = (int)(m / a.w.nchi);
+    const double* xv = a.X + vec * a.ld;
     double y = 0;
     double B[2][4], X[2][4];
     bool ok[2];
@@ -203,7 +211,7 @@ __device__ __forceinline__ void matvec_one(const MvArgs& a) {
           // row comp of the block (columns e), or column comp of it for the transpose
           const int plane = a.transpose ? q * 16 + e * 4 + comp : q * 16 + comp * 4 + e;
           B[slot][e] = a.coef[(long)plane * N + cell];
-          X[slot][e] = a.X[e * N + n];
+          X[slot][e] = xv[e * N + n];
         }
       }
     };
@@ -215,25 +223,28 @@ __device__ __forceinline__ void matvec_one(const MvArgs& a) {
       if (!ok[c]) continue;
       y = fma(B[c][0], X[c][0], fma(B[c][1], X[c][1], fma(B[c][2], X[c][2], fma(B[c][3], X[c][3], y))));
     }
-    const double val = a.scale * y;
-    a.Y[comp * N + m] = val;
+    const double val = (a.vscale ? a.vscale[vec] : a.scale) * y;
+    const long o = vec * a.ld + comp * N + m;
+    a.Y[o] = val;
     if (a.acc) {
-      double r = a.acc[comp * N + m];
-      if (a.acc_prev) r = fma(a.acc_prev[comp * N + m], a.c_prev, r);
-      a.acc[comp * N + m] = fma(val, a.c_acc, r);
+      double r = a.acc[o];
+      if (a.acc_prev) r = fma(a.acc_prev[o], a.c_prev, r);
+      a.acc[o] = fma(val, a.c_acc, r);
     }
   }
 }
 
-// The one-vector path (matvec_one) for grids with fewer cells than 32 per warp slot of 8
-// warps on every SM sub-partition; a larger grid already fills them with one thread per
-// cell (matvec_multi, whose single pass over the 144 coefficients is then cheaper).
-bool mv_one(long N, int k, int sms) { return k == 1 && N < 8L * 32 * 4 * sms; }
+// The thread-per-output path (matvec_one) when the cells x vectors are fewer than 32 per
+// warp slot of 8 warps on every SM sub-partition; more of them already fill those slots
+// with one thread per (cell, chunk of vectors) (matvec_multi, whose single pass over the
+// 144 coefficients for a chunk of vectors is then cheaper).
+__host__ __device__ inline long mv_one_limit(int sms) { return 8L * 32 * 4 * sms; }
+bool mv_one(long N, int k, int sms) { return N * k < mv_one_limit(sms); }
 
-// Work items of a matvec over k vectors: (cell, output component) on the one-vector path,
-// (cell, chunk of kVecChunk vectors) otherwise.
+// Work items of a matvec over k vectors: (cell, output component, vector) on the
+// thread-per-output path, (cell, chunk of kVecChunk vectors) otherwise.
 long mv_items(long N, int k, int sms) {
-  return mv_one(N, k, sms) ? 4 * N : N * ((k + kVecChunk - 1) / kVecChunk);
+  return mv_one(N, k, sms) ? 4 * N * k : N * ((k + kVecChunk - 1) / kVecChunk);
 }
 
 __device__ __forceinline__ void matvec_multi(const MvArgs& a) {
@@ -289,9 +300,10 @@ __device__ __forceinline__ void matvec_multi(const MvArgs& a) {
         }
       for (int v = 0; v < nv; ++v) {
         double* yo = a.Y + (long)(v0 + v) * n4;
+        const double sc = a.vscale ? a.vscale[v0 + v] : a.scale;
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
-          const double val = a.scale * y[v][c];
+          const double val = sc * y[v][c];
           yo[c * N + m] = val;
           if (a.acc) {
             double* ac = a.acc + (long)(v0 + v) * n4;
@@ -319,12 +331,20 @@ __global__ void __launch_bounds__(kMvThreads) k_matvec(MvArgs a) { matvec_cells<
 // The whole Taylor propagation in one cooperative launch: the blocks are co-resident
 // (cudaLaunchCooperativeKernel) and meet at a grid barrier after every matvec, instead of
 // one kernel per matvec. Same per-cell arithmetic, in the same order, as launch_expm.
+// vsteps (k entries, non-increasing, or null): vector c takes vsteps[c] steps, so that at
+// step s only the first #{c : vsteps[c] > s} vectors advance (a contiguous prefix).
 template <bool ONE>
-__global__ void __launch_bounds__(kMvThreads) k_expm_coop(MvArgs base, int nsteps, int order, double* v, double* t1,
-                                                          double* t2, double* vout) {
+__global__ void __launch_bounds__(kMvThreads, 2) k_expm_coop(MvArgs base, int nsteps, int order, double* v,
+                                                             double* t1, double* t2, double* vout,
+                                                             const int* vsteps) {
   cg::grid_group grid = cg::this_grid();
-  const long n = 4 * base.N * (long)base.k;
   for (int s = 0; s < nsteps; ++s) {
+    if (vsteps) {
+      int ka = 0;
+      while (ka < base.k && vsteps[ka] > s) ++ka;
+      base.k = ka;
+    }
+    const long n = 4 * base.N * (long)base.k;
     // order >= 2: the first matvec reads vout itself and adds nothing to it, the second
     // adds the first term before its own (the same additions in the same order as adding
     // each term in its own matvec), so no copy vout -> v closes the step
@@ -672,6 +692,7 @@ void launch_matvec(const DevCtx& d, int k, const double* X, double* Y, int trans
   MvArgs a;
   a.acc_prev = nullptr;
   a.c_prev = 0;
+  a.vscale = nullptr;
   a.coef = d.coef;
   a.X = X;
   a.Y = Y;
@@ -717,6 +738,7 @@ static void launch_expm_body(const DevCtx& d, int k, double dt, int nsteps, int 
   MvArgs a;
   a.acc_prev = nullptr;
   a.c_prev = 0;
+  a.vscale = nullptr;
   a.coef = d.coef;
   a.w = make_wrap(d.cfg);
   a.N = d.N;
@@ -956,22 +978,24 @@ LinearState& linear_state(hymor_ctx* ctx) {
 ExpmCache& expm_cache(hymor_ctx* ctx) { return linear_state(ctx).expm; }
 constexpr int kExpmCoopMinLaunches = 16;
 
+// hdts, hsteps (host, k entries, hsteps non-increasing), or null: vector c is propagated
+// hsteps[c] steps of hdts[c] instead of nsteps of dt.
 int expm_cooperative(hymor_ctx* ctx, int k, double dt, int nsteps, int order, const double* dX, double* dY,
-                     int transpose) {
+                     int transpose, const double* hdts = nullptr, const int* hsteps = nullptr) {
   DevCtx& d = ctx_dev(ctx);
   cudaStream_t st = ctx_stream(ctx);
   ExpmCache& c = expm_cache(ctx);
   const long n = 4 * d.N * (long)k;
   int r;
-  if (4 * n > c.cap) {
+  if (4 * n + 2 * k > c.cap) {
     if ((r = cuda_check(ctx, cudaStreamSynchronize(st)))) return r;
     if (c.buf) cudaFree(c.buf);
     c.buf = nullptr;
     c.cap = 0;
     void* p = nullptr;
-    if ((r = cuda_check(ctx, cudaMalloc(&p, sizeof(double) * 4 * n)))) return r;
+    if ((r = cuda_check(ctx, cudaMalloc(&p, sizeof(double) * (4 * n + 2 * k))))) return r;
     c.buf = static_cast<double*>(p);
-    c.cap = 4 * n;
+    c.cap = 4 * n + 2 * k;
   }
   double* v = c.buf;
   double* t1 = c.buf + n;
@@ -991,6 +1015,7 @@ int expm_cooperative(hymor_ctx* ctx, int k, double dt, int nsteps, int order, co
   MvArgs base;
   base.acc_prev = nullptr;
   base.c_prev = 0;
+  base.vscale = nullptr;
   base.coef = d.coef;
   base.w = make_wrap(d.cfg);
   base.N = d.N;
@@ -1002,9 +1027,18 @@ int expm_cooperative(hymor_ctx* ctx, int k, double dt, int nsteps, int order, co
   base.Y = nullptr;
   base.acc = nullptr;
   base.c_acc = 0;
+  int* vsteps = nullptr;
+  if (hdts && hsteps) {
+    double* vscale = c.buf + 4 * n;
+    vsteps = reinterpret_cast<int*>(c.buf + 4 * n + k);
+    if ((r = cuda_check(ctx, cudaMemcpyAsync(vscale, hdts, sizeof(double) * k, cudaMemcpyHostToDevice, st)))) return r;
+    if ((r = cuda_check(ctx, cudaMemcpyAsync(vsteps, hsteps, sizeof(int) * k, cudaMemcpyHostToDevice, st)))) return r;
+    base.vscale = vscale;
+    nsteps = hsteps[0];
+  }
   if ((r = cuda_check(ctx, cudaMemcpyAsync(v, dX, sizeof(double) * n, cudaMemcpyDeviceToDevice, st)))) return r;
   if ((r = cuda_check(ctx, cudaMemcpyAsync(vout, dX, sizeof(double) * n, cudaMemcpyDeviceToDevice, st)))) return r;
-  void* args[] = {&base, &nsteps, &order, &v, &t1, &t2, &vout};
+  void* args[] = {&base, &nsteps, &order, &v, &t1, &t2, &vout, &vsteps};
   if ((r = cuda_check(ctx, cudaLaunchCooperativeKernel(kern, grid, th, args, 0, st))))
     return r;
   return cuda_check(ctx, cudaMemcpyAsync(dY, vout, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
@@ -1222,6 +1256,26 @@ int hymor_expm_apply_dev(hymor_ctx* ctx, int k, double dt, int nsteps, int order
   launch_expm(d, k, dt, nsteps, order, dX, dY, transpose, work, st);
   cudaFreeAsync(work, st);
   return cuda_check(ctx, cudaGetLastError());
+}
+
+int hymor_expm_apply_multi_dev(hymor_ctx* ctx, int k, const double* dts, const int32_t* nsteps, int order,
+                               const double* dX, double* dY, int transpose) {
+  if (!ctx || k < 1 || !dts || !nsteps || order < 1 || order > 20 || !dX || !dY) return HYMOR_ERR_INVALID;
+  DevCtx& d = ctx_dev(ctx);
+  if (!d.coef) return ctx_fail(ctx, HYMOR_ERR_NOT_READY, "no Jacobian: call hymor_linearize or hymor_jacobian_set");
+  for (int c = 0; c < k; ++c)
+    if (nsteps[c] < 0 || (c > 0 && nsteps[c] > nsteps[c - 1]))
+      return ctx_fail(ctx, HYMOR_ERR_INVALID, "per-vector step counts must be non-negative and non-increasing");
+  if (d.sj.on) {
+    // the shock-position operator has no cooperative propagator: one vector at a time
+    const long n = op_size(d);
+    for (int c = 0; c < k; ++c) {
+      const int r = hymor_expm_apply_dev(ctx, 1, dts[c], nsteps[c], order, dX + c * n, dY + c * n, transpose);
+      if (r) return r;
+    }
+    return 0;
+  }
+  return expm_cooperative(ctx, k, 0.0, nsteps[0], order, dX, dY, transpose, dts, nsteps);
 }
 
 int hymor_expm_apply(hymor_ctx* ctx, int k, double dt, int nsteps, int order, const double* X, double* Y,

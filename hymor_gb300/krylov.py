@@ -75,6 +75,49 @@ def krylov_schur(ctx, n: int, apply_op, nev: int, ncv: int, tol: float = 1e-8, m
     Returns (theta, resid, nops): Ritz values, their residual norms ||OP x - theta x||
     (x of unit norm) and the number of operator applications; with want_vectors also the
     Ritz vectors (n x nev, complex unless symmetric), or None when tol was not reached."""
+    steps = krylov_schur_steps(ctx, n, nev, ncv, tol, maxit, seed, symmetric, v0, want_vectors)
+    try:
+        req = next(steps)
+        while True:
+            apply_op(*req)
+            req = steps.send(None)
+    except StopIteration as done:
+        return done.value
+
+
+def krylov_schur_many(ctx, n: int, apply_many, problems: list[dict]):
+    """Several Krylov-Schur solves in lockstep, so that each round applies the operators of
+    all unfinished solves in one batched call.
+
+    problems: keyword arguments of krylov_schur (nev, ncv, tol, maxit, seed, symmetric, v0,
+    want_vectors) per solve. apply_many(idx, srcs, dsts) applies operator idx[c] to the
+    device vector at srcs[c] into dsts[c] for every c; idx is increasing. Each solve makes
+    the same operations, in the same order, as its own krylov_schur call. Returns the
+    results of krylov_schur, one per problem."""
+    gens = [krylov_schur_steps(ctx, n, **p) for p in problems]
+    results: list = [None] * len(gens)
+    pending = {}
+    for i, g in enumerate(gens):
+        try:
+            pending[i] = next(g)
+        except StopIteration as done:
+            results[i] = done.value
+    while pending:
+        idx = sorted(pending)
+        apply_many(idx, [pending[i][0] for i in idx], [pending[i][1] for i in idx])
+        for i in idx:
+            try:
+                pending[i] = gens[i].send(None)
+            except StopIteration as done:
+                results[i] = done.value
+                del pending[i]
+    return results
+
+
+def krylov_schur_steps(ctx, n: int, nev: int, ncv: int, tol: float = 1e-8, maxit: int = 200, seed: int = 3,
+                       symmetric: bool = False, v0: np.ndarray | None = None, want_vectors: bool = False):
+    """krylov_schur as a generator: yields (src_addr, dst_addr) whenever it needs the
+    operator applied, and returns krylov_schur's result."""
     if not (0 < nev < ncv):
         raise HymorError(-1, "need 0 < nev < ncv")
     L = ctx.L
@@ -90,7 +133,7 @@ def krylov_schur(ctx, n: int, apply_op, nev: int, ncv: int, tol: float = 1e-8, m
     theta = resid = X = None
     for it in range(maxit):
         for j in range(p, ncv):
-            apply_op(V.addr(j * n), w.addr())
+            yield V.addr(j * n), w.addr()
             nops += 1
             ctx.check(L.hymor_krylov_orthogonalize(ctx.h, n, j + 1, V.ptr, n, w.ptr, dp(h), j + 1))
             H[: j + 1, j] = h[: j + 1]

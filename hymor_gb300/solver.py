@@ -442,6 +442,51 @@ def chu_blocks_from_state(cfg, vol, qflat, cell_idx, norms=(1, 1, 1, 1)):
     return C0, D
 
 
+class _ChuWeights:
+    """The weight operators of transient growth on the device: C0 = R'MR, K^-1 and K^-T with
+    D = R'M^R = K Kᵀ per cell (CONSTRUCT_R/M/M_HAT), and their shock-position tails: R is
+    the identity on those unknowns (CONSTRUCT_R.jl:109-118), M has no entries there
+    (CONSTRUCT_M.jl:88-92) and M^ weighs them by bt_area[i, sc_i] / 2
+    (CONSTRUCT_M_HAT.jl:77-90), so C0 is 0 and K is sqrt(bt_area / 2) on the tail."""
+
+    def __init__(self, L: LinearOperatorGPU, s: Solution):
+        from .krylov import DeviceBuffer
+        self.s, self.N = s, s.N
+        C0, D = chu_blocks(s)
+        Kinv = np.linalg.inv(np.linalg.cholesky(D))
+        self.KinvT = np.transpose(Kinv, (0, 2, 1))
+        self.ntail = L.n - 4 * s.N
+        self.tail_k = np.ones(1)
+        if self.ntail:
+            ci = s.get_state()["cell_idx"]
+            self.tail_k = 1.0 / np.sqrt(np.asarray(s.case.mesh["bt_a"])[np.arange(s.nchi), ci - 1] / 2)
+        self.blocks = [DeviceBuffer(s.ctx, 8 * s.N * 16) for _ in range(3)]
+        for b, arr in zip(self.blocks, (C0, Kinv, self.KinvT)):
+            b.upload(np.ascontiguousarray(arr.reshape(-1)))
+        self.tails = [DeviceBuffer(s.ctx, 8 * max(self.ntail, 1)) for _ in range(2)]
+        self.tails[0].upload(np.zeros(max(self.ntail, 1)))
+        self.tails[1].upload(np.ascontiguousarray(self.tail_k))
+
+    def apply(self, which: str, k: int, src, dst):
+        """which: "C0", "Kinv" or "KinvT", on k contiguous device vectors."""
+        b, t = {"C0": (0, 0), "Kinv": (1, 1), "KinvT": (2, 1)}[which]
+        self.s.ctx.check(self.s.ctx.L.hymor_block4_apply_ext_dev(self.s.ctx.h, int(k), self.ntail, self.blocks[b].ptr,
+                                                                 self.tails[t].ptr, src, dst))
+
+    def initial_conditions(self, Y: np.ndarray) -> np.ndarray:
+        """x = K^-T y per cell (and on the tail), y as [rho; rho_u; rho_v; rho_E; r] columns."""
+        N = self.N
+        Yc = Y[:4 * N].reshape(4, N, -1).transpose(1, 0, 2)            # (N, 4, k)
+        X = np.einsum("nij,njk->nik", self.KinvT, Yc).transpose(1, 0, 2).reshape(4 * N, -1)
+        if self.ntail:
+            X = np.concatenate([X, Y[4 * N:] * self.tail_k[:, None]])
+        return X
+
+    def free(self):
+        for b in self.blocks + self.tails:
+            b.free()
+
+
 def TRANSIENT_GROWTH_DOWNSTREAM(L: LinearOperatorGPU, s: Solution, n_modes: int, T: float, ncv: int | None = None,
                                 tol: float = 1e-8, order: int = 5, seed: int = 4, maxit: int = 300,
                                 block: int = 1, modes: bool = False, keep_unconverged: bool = False):
@@ -452,46 +497,25 @@ def TRANSIENT_GROWTH_DOWNSTREAM(L: LinearOperatorGPU, s: Solution, n_modes: int,
     reorthogonalisation) on the device; the forward propagation P and its adjoint Pᵀ are
     Taylor-`order` steps of dt = T / round(T / dt_CFL). block > 1: block Krylov-Schur, the
     operator applied to `block` vectors per batched call. modes: also the optimal initial
-    conditions x = K^-T y (info["modes"], 4 Nchi Neta x n_modes, x' R'M^R x = 1; the
-    reference's V). Non-convergence warns and returns NaN, as the reference
+    conditions x = K^-T y (info["modes"], n x n_modes, x' R'M^R x = 1; the reference's V).
+    Non-convergence warns and returns NaN, as the reference
     (TRANSIENT_GROWTH_DOWNSTREAM.jl:131-135), unless keep_unconverged."""
     import time
     from .krylov import DeviceBuffer, block_krylov_schur, krylov_schur
     dt_cfl = CFL_TIMESTEP(s)
     n_t = int(round(T / dt_cfl))
     dt = T / n_t
-    C0, D = chu_blocks(s)
-    K = np.linalg.cholesky(D)
-    Kinv = np.linalg.inv(K)
-    KinvT = np.transpose(Kinv, (0, 2, 1))
     n = L.n
-    ntail = n - 4 * s.N
-    # shock-position unknowns: R is the identity on them (CONSTRUCT_R.jl:109-118), M has no
-    # entries there (CONSTRUCT_M.jl:88-92) and M^ weighs them by bt_area[i, sc_i] / 2
-    # (CONSTRUCT_M_HAT.jl:77-90), so C0 is 0 and K is sqrt(bt_area / 2) on the tail
-    tail_k = np.ones(1)
-    if ntail:
-        ci = s.get_state()["cell_idx"]
-        d_tail = np.asarray(s.case.mesh["bt_a"])[np.arange(s.nchi), ci - 1] / 2
-        tail_k = 1.0 / np.sqrt(d_tail)
-    bufs = [DeviceBuffer(s.ctx, 8 * s.N * 16) for _ in range(3)]
-    for b, arr in zip(bufs, (C0, Kinv, KinvT)):
-        b.upload(np.ascontiguousarray(arr.reshape(-1)))
-    tails = [DeviceBuffer(s.ctx, 8 * max(ntail, 1)) for _ in range(2)]
-    tails[0].upload(np.zeros(max(ntail, 1)))
-    tails[1].upload(np.ascontiguousarray(tail_k if ntail else np.ones(1)))
+    W = _ChuWeights(L, s)
     t1, t2 = DeviceBuffer(s.ctx, 8 * n * block), DeviceBuffer(s.ctx, 8 * n * block)
     Lh, h = s.ctx.L, s.ctx.h
 
-    def b4(k, B, tail, src, dst):
-        s.ctx.check(Lh.hymor_block4_apply_ext_dev(h, k, ntail, B.ptr, tail.ptr, src, dst))
-
     def apply_k(src, dst, k):
-        b4(k, bufs[2], tails[1], src, t1.ptr)                                              # x = K^-T y
+        W.apply("KinvT", k, src, t1.ptr)                                                   # x = K^-T y
         s.ctx.check(Lh.hymor_expm_apply_dev(h, k, dt, n_t, order, t1.ptr, t2.ptr, 0))      # P x
-        b4(k, bufs[0], tails[0], t2.ptr, t1.ptr)                                           # C0 P x
+        W.apply("C0", k, t2.ptr, t1.ptr)                                                   # C0 P x
         s.ctx.check(Lh.hymor_expm_apply_dev(h, k, dt, n_t, order, t1.ptr, t2.ptr, 1))      # Pᵀ C0 P x
-        b4(k, bufs[1], tails[1], t2.ptr, dst)                                              # K^-1 (...)
+        W.apply("Kinv", k, t2.ptr, dst)                                                    # K^-1 (...)
     ncv = ncv or max(2 * n_modes + 1, 16, n_modes + 4 * block)
     t0 = time.perf_counter()
     if block > 1:
@@ -501,18 +525,12 @@ def TRANSIENT_GROWTH_DOWNSTREAM(L: LinearOperatorGPU, s: Solution, n_modes: int,
         gains, resid, nops, Y = krylov_schur(s.ctx, n, lambda a, b: apply_k(a, b, 1), n_modes, ncv, tol=tol,
                                              maxit=maxit, seed=seed, symmetric=True, want_vectors=True)
     elapsed = time.perf_counter() - t0
-    for b in bufs + tails + [t1, t2]:
+    for b in (t1, t2):
         b.free()
     gains = np.real(gains)
     converged = bool(np.all(resid <= tol * np.abs(gains)))
-    X = None
-    if modes and Y is not None:
-        N = s.N
-        # x = K^-T y per cell: y as [rho; rho_u; rho_v; rho_E] blocks of N (and the tail)
-        Yc = Y[:4 * N].reshape(4, N, -1).transpose(1, 0, 2)            # (N, 4, k)
-        X = np.einsum("nij,njk->nik", KinvT, Yc).transpose(1, 0, 2).reshape(4 * N, -1)
-        if ntail:
-            X = np.concatenate([X, Y[4 * N:] * tail_k[:, None]])
+    X = W.initial_conditions(Y) if (modes and Y is not None) else None
+    W.free()
     if not converged and not keep_unconverged:
         import warnings
         warnings.warn(f"transient-growth solve did not reach tol {tol:g} in {maxit} restarts; returning NaN")
@@ -522,3 +540,65 @@ def TRANSIENT_GROWTH_DOWNSTREAM(L: LinearOperatorGPU, s: Solution, n_modes: int,
     if modes:
         info["modes"] = X
     return gains, info
+
+
+def TRANSIENT_GROWTH_HORIZONS(L: LinearOperatorGPU, s: Solution, n_modes: int, Ts, ncv: int | None = None,
+                              tol: float = 1e-8, order: int = 5, seed: int = 4, maxit: int = 300,
+                              keep_unconverged: bool = False):
+    """TRANSIENT_GROWTH_DOWNSTREAM for several time horizons at once: one Krylov-Schur solve
+    per horizon, run in lockstep (krylov_schur_many), so that each round propagates one
+    vector per unfinished horizon in one batched call (hymor_expm_apply_multi_dev: each
+    vector with its own dt = T / round(T / dt_CFL) and step count, the longer horizons
+    first). Each horizon's solve makes the same operations as TRANSIENT_GROWTH_DOWNSTREAM(T)
+    with the same seed. Returns (gains, infos): gains[h] the n_modes gains of Ts[h], infos[h]
+    as TRANSIENT_GROWTH_DOWNSTREAM's info (seconds: the whole batched solve)."""
+    import time
+    from .krylov import DeviceBuffer, krylov_schur_many
+    Ts = [float(T) for T in Ts]
+    dt_cfl = CFL_TIMESTEP(s)
+    steps = [int(round(T / dt_cfl)) for T in Ts]
+    dts = [T / nt for T, nt in zip(Ts, steps)]
+    order_h = sorted(range(len(Ts)), key=lambda h: -steps[h])        # longest horizon first
+    H, n = len(Ts), L.n
+    W = _ChuWeights(L, s)
+    bufs = [DeviceBuffer(s.ctx, 8 * n * H) for _ in range(4)]
+    Lh, h = s.ctx.L, s.ctx.h
+
+    def apply_many(idx, srcs, dsts):
+        k = len(idx)
+        hs = [order_h[i] for i in idx]
+        dt_k = np.array([dts[j] for j in hs])
+        st_k = np.array([steps[j] for j in hs], dtype=np.int32)
+        for c, src in enumerate(srcs):
+            s.ctx.check(Lh.hymor_memcpy_d2d(h, bufs[0].addr(c * n), src, 8 * n))
+        def expm(src, dst, transpose):
+            s.ctx.check(Lh.hymor_expm_apply_multi_dev(h, k, dp(dt_k), ip(st_k), int(order), src, dst, transpose))
+        W.apply("KinvT", k, bufs[0].ptr, bufs[1].ptr)       # x = K^-T y
+        expm(bufs[1].ptr, bufs[2].ptr, 0)                  # P x
+        W.apply("C0", k, bufs[2].ptr, bufs[3].ptr)          # C0 P x
+        expm(bufs[3].ptr, bufs[2].ptr, 1)                  # Pᵀ C0 P x
+        W.apply("Kinv", k, bufs[2].ptr, bufs[0].ptr)        # K^-1 (...)
+        for c, dst in enumerate(dsts):
+            s.ctx.check(Lh.hymor_memcpy_d2d(h, dst, bufs[0].addr(c * n), 8 * n))
+    ncv = ncv or max(2 * n_modes + 1, 16)
+    problems = [dict(nev=n_modes, ncv=ncv, tol=tol, maxit=maxit, seed=seed, symmetric=True) for _ in Ts]
+    t0 = time.perf_counter()
+    res = krylov_schur_many(s.ctx, n, apply_many, problems)
+    elapsed = time.perf_counter() - t0
+    for b in bufs:
+        b.free()
+    W.free()
+    gains = np.full((H, n_modes), np.nan)
+    infos: list = [None] * H
+    for i, j in enumerate(order_h):
+        g, resid, nops = res[i]
+        g = np.real(g)
+        converged = bool(np.all(resid <= tol * np.abs(g)))
+        if converged or keep_unconverged:
+            gains[j] = g
+        infos[j] = dict(resid=resid, dt=dts[j], n_t=steps[j], T_opt=steps[j] * dts[j], nops=nops, seconds=elapsed,
+                        converged=converged)
+    if not all(inf["converged"] for inf in infos) and not keep_unconverged:
+        import warnings
+        warnings.warn(f"transient-growth solves of some horizons did not reach tol {tol:g}; their gains are NaN")
+    return gains, infos

@@ -212,6 +212,12 @@ int hymor_expm_apply(hymor_ctx* ctx, int k, double dt, int nsteps, int order, co
                      double* Y, int transpose);
 int hymor_expm_apply_dev(hymor_ctx* ctx, int k, double dt, int nsteps, int order,
                          const double* dX, double* dY, int transpose);
+/* k propagations of different lengths in one batched call: vector c gets nsteps[c] steps
+ * of dt[c] (host arrays of k; nsteps non-increasing, so the vectors still advancing are a
+ * prefix). Device pointers. The transient-growth horizons of one solve batch (no
+ * counterpart in the reference, which propagates one horizon per call). */
+int hymor_expm_apply_multi_dev(hymor_ctx* ctx, int k, const double* dts, const int32_t* nsteps, int order,
+                               const double* dX, double* dY, int transpose);
 
 /* Allocation-free variant of hymor_expm_apply_dev (no counterpart in the reference). For
  * callers that must not allocate device memory during the call, e.g. code running

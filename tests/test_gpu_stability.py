@@ -204,3 +204,44 @@ def test_linearisation_matches_residual_differences(require_gpu):
     df = (residual_at(+1) - residual_at(-1)) / (2 * h)
     Lq = L @ dq
     assert np.linalg.norm(Lq - df) / np.linalg.norm(df) < 1e-3
+
+
+def test_expm_multi_matches_single_propagations(require_gpu):
+    """hymor_expm_apply_multi_dev: k propagations with their own dt and step counts in one
+    batched call equal the k one-vector propagations (the same FMA chains per output)."""
+    import ctypes
+    from hymor_gb300.krylov import DeviceBuffer
+    cfg, cs, sol, orc = _setup(30, 20, steps=5)
+    _, L = S.LINEARIZE_L(sol)
+    n = L.n
+    rng = np.random.Generator(np.random.PCG64(8))
+    X = rng.standard_normal((3, n))
+    dts = np.array([1.1e-3, 0.9e-3, 1.3e-3])
+    steps = np.array([40, 25, 7], dtype=np.int32)
+    bx, by = DeviceBuffer(sol.ctx, 8 * n * 3), DeviceBuffer(sol.ctx, 8 * n * 3)
+    bx.upload(X.ravel())
+    Lh, h = sol.ctx.L, sol.ctx.h
+    for tr in (0, 1):
+        sol.ctx.check(Lh.hymor_expm_apply_multi_dev(h, 3, dts.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                                    steps.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), 5,
+                                                    bx.ptr, by.ptr, tr))
+        Y = by.download(3 * n).reshape(3, n)
+        P = L.T if tr else L
+        for c in range(3):
+            ref = P.expm(X[c], dts[c], int(steps[c]))
+            assert np.max(np.abs(Y[c] - ref)) <= 1e-14 * np.max(np.abs(ref))
+    bx.free()
+    by.free()
+
+
+def test_transient_growth_horizons_batched(require_gpu):
+    """TRANSIENT_GROWTH_HORIZONS (the horizons of one solve propagated together, lockstep
+    Krylov-Schur) gives each horizon's TRANSIENT_GROWTH_DOWNSTREAM gains."""
+    cfg, cs, sol, orc = _setup(24, 24)
+    _, L = S.LINEARIZE_L(sol)
+    Ts = [0.004, 0.016, 0.008]
+    G, infos = S.TRANSIENT_GROWTH_HORIZONS(L, sol, 2, Ts, ncv=16, tol=1e-11)
+    for h, T in enumerate(Ts):
+        g1, info1 = S.TRANSIENT_GROWTH_DOWNSTREAM(L, sol, 2, T, ncv=16, tol=1e-11)
+        assert np.allclose(G[h], g1, rtol=1e-9, atol=0)
+        assert infos[h]["n_t"] == info1["n_t"] and infos[h]["converged"]

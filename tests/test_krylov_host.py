@@ -160,3 +160,27 @@ def test_ritz_vectors_are_eigenvectors(symmetric, block):
         x = X[:, i]
         assert abs(np.linalg.norm(x) - 1) < 1e-12
         assert np.linalg.norm(A @ x - theta[i] * x) <= 1e-9 * abs(theta[i])
+
+
+def test_lockstep_solves_match_separate_solves():
+    """krylov_schur_many runs one solve per operator in lockstep (one batched application
+    per round): each solve gives exactly its own krylov_schur result, also when the solves
+    converge after different numbers of restarts."""
+    n, nev = 200, 3
+    mats = [_matrix(n, True, seed)[0] * scale for seed, scale in ((21, 1.0), (22, 3.0), (23, 0.5))]
+    ctx = _Ctx()
+    separate = []
+    for i, A in enumerate(mats):
+        one, _ = _op(A, ctx)
+        separate.append(K.krylov_schur(ctx, n, one, nev, ncv=14, tol=1e-10, maxit=300, seed=7 + i, symmetric=True))
+    calls = []
+
+    def apply_many(idx, srcs, dsts):
+        calls.append(len(idx))
+        for i, src, dst in zip(idx, srcs, dsts):
+            ctx.L._view(dst, n)[:] = mats[i] @ ctx.L._view(src, n)
+    probs = [dict(nev=nev, ncv=14, tol=1e-10, maxit=300, seed=7 + i, symmetric=True) for i in range(3)]
+    together = K.krylov_schur_many(ctx, n, apply_many, probs)
+    for (t1, r1, n1), (t2, r2, n2) in zip(separate, together):
+        assert np.array_equal(t1, t2) and np.array_equal(r1, r2) and n1 == n2
+    assert max(calls) == 3 and sum(calls) == sum(s[2] for s in separate)
