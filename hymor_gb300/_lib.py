@@ -36,7 +36,8 @@ EXPORTS = [
     "hymor_expm_apply_dev_noalloc", "hymor_step_kernels", "hymor_fp64_peak",
     "hymor_profile_phases", "hymor_advect", "hymor_bench_matvec", "hymor_operator_size",
     "hymor_shock_blocks_get", "hymor_shock_blocks_set", "hymor_shock_fields", "hymor_block4_apply_ext_dev",
-    "hymor_expm_apply_multi_dev",
+    "hymor_expm_apply_multi_dev", "hymor_linearize_b", "hymor_b_get", "hymor_b_set", "hymor_recept_size",
+    "hymor_recept_apply_dev", "hymor_recept_expm_dev",
 ]
 
 
@@ -105,6 +106,12 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "hymor_shock_blocks_get": [vp, ip, dp, dp, dp],
         "hymor_shock_blocks_set": [vp, ip, dp, dp, dp],
         "hymor_shock_fields": [vp, dp, dp],
+        "hymor_linearize_b": [vp],
+        "hymor_b_get": [vp, ip, dp, dp],
+        "hymor_b_set": [vp, ip, dp, dp],
+        "hymor_recept_size": [vp, i, ctypes.POINTER(ctypes.c_int64)],
+        "hymor_recept_apply_dev": [vp, i, i, dp, d, vp, vp, i],
+        "hymor_recept_expm_dev": [vp, i, i, dp, d, i, i, vp, vp, i],
     }
     for name, args in sig.items():
         f = getattr(L, name)

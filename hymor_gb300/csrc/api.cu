@@ -609,6 +609,11 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
   d.coef = nullptr;
   d.jwork = nullptr;
   d.sj = ShockJac{};
+  d.up_cols = nullptr;
+  d.bq = nullptr;
+  d.bs = nullptr;
+  d.brows = nullptr;
+  d.bwork = nullptr;
   d.sf_zero = 1;  // the flux arrays are allocated zeroed
   for (int k = 0; k < hymor_ctx_s::kEv; ++k)
     if (cudaEventCreate(&ctx->cap_ev[k]) != cudaSuccess) return bail(fail(ctx, HYMOR_ERR_CUDA, "event"));

@@ -195,15 +195,25 @@ __device__ double spline_g(int n, const double* ih, const double* ys, const doub
   return ys[r] - lam * qg;
 }
 
-// Freestream state seen by shock point i (COMPUTE_UPSTREAM_CONDITIONS.jl:31-112).
+// Freestream state seen by shock point i (COMPUTE_UPSTREAM_CONDITIONS.jl:31-112): the
+// (disturbed) freestream, or with cols (4 x Nchi: rho, rho_u, rho_v, rho_E per column) the
+// prescribed per-column upstream state of `rho_0_upstream_p` (:87-91).
 __device__ void upstream(const hymor_config& c, double t, double px, double py, bool first, double& p_inf,
-                         double& u_inf, double& v_inf, double& rho_inf) {
-  const double u_y = c.rho_v_0 / c.rho_0, u_x = c.rho_u_0 / c.rho_0;
-  const double pert = cos(2.0 * M_PI * c.dist_ky * (py - u_y * t)) * sin(2.0 * M_PI * c.dist_kx * (px - u_x * t));
-  const double rho = c.rho_0 + pert * c.dist_amp[0];
-  const double ru = c.rho_u_0 + pert * c.dist_amp[1];
-  double rv = c.rho_v_0 + pert * c.dist_amp[2];
-  const double rE = c.rho_E_0 + pert * c.dist_amp[3];
+                         double& u_inf, double& v_inf, double& rho_inf, const double* cols = nullptr, int i = 0) {
+  double rho, ru, rv, rE;
+  if (cols) {
+    rho = cols[i];
+    ru = cols[c.nchi + i];
+    rv = cols[2 * c.nchi + i];
+    rE = cols[3 * c.nchi + i];
+  } else {
+    const double u_y = c.rho_v_0 / c.rho_0, u_x = c.rho_u_0 / c.rho_0;
+    const double pert = cos(2.0 * M_PI * c.dist_ky * (py - u_y * t)) * sin(2.0 * M_PI * c.dist_kx * (px - u_x * t));
+    rho = c.rho_0 + pert * c.dist_amp[0];
+    ru = c.rho_u_0 + pert * c.dist_amp[1];
+    rv = c.rho_v_0 + pert * c.dist_amp[2];
+    rE = c.rho_E_0 + pert * c.dist_amp[3];
+  }
   if (c.axisymmetric && first) rv = 0;
   v_inf = rv / rho;
   u_inf = ru / rho;
@@ -776,6 +786,7 @@ struct ColArgs {
   unsigned* err;
   DevMesh m;
   double cY, cS;
+  const double* up_cols;                  // per-column upstream state (4 x Nchi) or null
   int move, on_S;
   int disturbed;                          // any freestream disturbance amplitude non-zero
   double p_inf, u_inf, v_inf, rho_inf;    // undisturbed freestream (COMPUTE_UPSTREAM_CONDITIONS.jl)
@@ -838,7 +849,8 @@ __global__ void __launch_bounds__(128) k_shock_columns(ColArgs A) {
   element_space(c, xv, yv, ch, et);
   A.pts.x[i] = xv; A.pts.y[i] = yv; A.pts.chi[i] = ch; A.pts.eta[i] = et;
   double p_inf = A.p_inf, u_inf = A.u_inf, v_inf = A.v_inf, rho_inf = A.rho_inf;
-  if (A.disturbed || (c.axisymmetric && i == 0)) upstream(c, t, xv, yv, i == 0, p_inf, u_inf, v_inf, rho_inf);
+  const bool local_up = A.disturbed || A.up_cols || (c.axisymmetric && i == 0);
+  if (local_up) upstream(c, t, xv, yv, i == 0, p_inf, u_inf, v_inf, rho_inf, A.up_cols, i);
   const double cross = xd * v_inf - yd * u_inf;
   const double dot = xd * u_inf + yd * v_inf;
   // beta = atan2(|cross|, |dot|) enters only through its sine and cosine, |cross| / r and |dot| / r
@@ -887,7 +899,7 @@ __global__ void __launch_bounds__(128) k_shock_columns(ColArgs A) {
   const double e_s = p_s * A.igm1 * irho_s;
   // ang_inf = beta - atan2(v_inf, u_inf): sine and cosine by the angle-difference identity
   double vmag = A.vmag, cph = A.cph, sph = A.sph;
-  if (A.disturbed || (c.axisymmetric && i == 0)) {
+  if (local_up) {
     vmag = sqrt(u_inf * u_inf + v_inf * v_inf);
     const double ivm = frcp(vmag);
     cph = u_inf * ivm;
@@ -1750,6 +1762,7 @@ void launch_columns_bc(const DevCtx& d, bool on_S, bool move, double cY, double 
     ca.m = d.m;
     ca.cY = cY;
     ca.cS = cS;
+    ca.up_cols = d.up_cols;
     ca.move = move;
     ca.on_S = on_S;
     ca.disturbed = c.dist_amp[0] != 0 || c.dist_amp[1] != 0 || c.dist_amp[2] != 0 || c.dist_amp[3] != 0;

@@ -52,6 +52,15 @@ struct DevCtx {
   double* coef;    // N * 144 stencil blocks (or null)
   double* jwork;   // linearisation workspace
   ShockJac sj;
+  // prescribed per-column upstream state (4 x Nchi) of the shock chain, or null: set only
+  // while the upstream-boundary operator B is assembled (rho_0_upstream_p)
+  const double* up_cols;
+  // upstream-boundary operator B (LINEARIZE_B): per column m, for the input column
+  // n = m + d (d = -1, 0, 1), bq[((m*3 + d+1)*4 + vout)*4 + vin] = d flux_vout(m, sc_m - 1) /
+  // d upstream_vin(n) and bs[(m*3 + d+1)*4 + vin] = d speed_m / d upstream_vin(n)
+  double *bq, *bs;
+  int* brows;      // Nchi: the shocked rows sc_m of B's flux rows
+  double* bwork;   // 5 x Nchi: the per-column upstream state and the base shock speeds
 };
 
 // Unknowns of the linearised operator: 4N, plus Nchi with the shock blocks.
@@ -103,8 +112,9 @@ void launch_classical_stage(const DevCtx& d, double cY, cudaStream_t st);
 
 // ---- linear.cu ----
 void launch_jacobian_assemble(DevCtx& d, cudaStream_t st);
+void launch_b_assemble(DevCtx& d, cudaStream_t st);
 void launch_matvec(const DevCtx& d, int k, const double* X, double* Y, int transpose, double scale,
-                   cudaStream_t st);
+                   cudaStream_t st, long ld = 0);
 void launch_expm(const DevCtx& d, int k, double dt, int nsteps, int order, const double* X,
                  double* Y, int transpose, double* work, cudaStream_t st);
 

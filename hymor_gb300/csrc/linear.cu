@@ -501,7 +501,10 @@ __global__ void k_block4_tail(const double* B, const double* tail, const double*
     const double* b = B + m * 16;
 #pragma unroll
     for (int r = 0; r < 4; ++r) yc[r * N + m] = fma(b[4 * r], x0, fma(b[4 * r + 1], x1, fma(b[4 * r + 2], x2, b[4 * r + 3] * x3)));
-    if (m < nt) yc[4 * N + m] = tail[m] * xc[4 * N + m];
+  }
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < nt * k; t += (long)gridDim.x * blockDim.x) {
+    const long m = t % nt, col = t / nt;
+    y[col * ld + 4 * N + m] = tail[m] * x[col * ld + 4 * N + m];
   }
 }
 
@@ -650,6 +653,127 @@ __global__ void __launch_bounds__(kShockThreads) k_shock_mv(ShockMvArgs a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Upstream-boundary operator B (freestream receptivity, Freestream_receptivity/LINEARIZE_B.jl).
+
+// Per-column upstream state: the freestream, with variable `var` of the columns i = colour
+// (mod 3) raised by eps (LINEARIZE_B.jl:49-70; var < 0: the unperturbed state).
+__global__ void k_up_cols(double* cols, int nchi, double r0, double ru0, double rv0, double rE0, int var,
+                          int colour, double eps) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nchi) return;
+  const double f[4] = {r0, ru0, rv0, rE0};
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    const double hit = (v == var && i % 3 == colour) ? 1.0 : 0.0;
+    cols[v * nchi + i] = f[v] + eps * hit;
+  }
+}
+
+// GET_BLOCK (LINEARIZE_B.jl:186-253): the raised column n = m + d (d in -1, 0, 1) of output
+// column m is the one of this colour; its entries are the flux change of the cell
+// (m, sc_m - 1) and the change of speed m over eps.
+__global__ void k_gather_b(Flux4 Fp, Flux4 Fb, const double* rel, const double* rel_b, const int* rows, double* bq,
+                           double* bs, int nchi, int var, int colour, double eps) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= nchi) return;
+  int d = 2;  // the offset in -1..1 whose column has this colour
+  for (int dd = -1; dd <= 1; ++dd)
+    if (((m + dd) % 3 + 3) % 3 == colour) d = dd;
+  const int n = m + d;
+  if (d == 2 || n < 0 || n >= nchi) return;
+  const long cell = m + (long)(rows[m] - 2) * nchi;
+#pragma unroll
+  for (int vo = 0; vo < 4; ++vo)
+    bq[((m * 3 + d + 1) * 4 + vo) * 4 + var] = (Fp.v[vo][cell] - Fb.v[vo][cell]) / eps;
+  if (bs) bs[(m * 3 + d + 1) * 4 + var] = (rel[m] - rel_b[m]) / eps;
+}
+
+struct RecArgs {
+  const double* X;
+  double* Y;
+  const double *bq, *bs, *w;
+  const int* rows;
+  long N, ld, nop;  // vector stride; nop = start of the freestream blocks
+  double scale;
+  int nchi, nw, k, adjoint, shock;
+};
+
+// The freestream part of the receptivity operator L_ = [L, B ... B; 0, diag(-i w_k I)]
+// (LINEARIZE_L_.jl:60-68) on k complex vectors, each stored as its real and imaginary
+// parts (real vectors 2c and 2c + 1 of stride ld), after the matvec with L has written the
+// downstream rows. Forward: the flux rows (m, sc_m - 1) (and speed rows) add B (sum_k u_k);
+// the freestream rows are -i w_k u_k. Adjoint (the conjugate transpose): every freestream
+// block gets B^T q + i w_k u_k.
+__global__ void __launch_bounds__(256) k_recept_mv(RecArgs a) {
+  const int nchi = a.nchi;
+  const long p4 = 4L * nchi;
+  const long nre = 2L * a.k;
+  const long items = a.adjoint ? nre * p4 : nre * nchi + nre * a.nw * p4;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < items; t += (long)gridDim.x * blockDim.x) {
+    if (a.adjoint) {
+      const long r = t / p4;
+      const int e = (int)(t % p4), vin = e / nchi, n = e % nchi;
+      const double* x = a.X + r * a.ld;
+      const double* xo = a.X + (r ^ 1) * a.ld;
+      double* y = a.Y + r * a.ld;
+      double bt = 0;
+      for (int m = max(n - 1, 0); m <= min(n + 1, nchi - 1); ++m) {
+        const int slot = (m * 3 + (n - m) + 1) * 4;
+        const long cell = m + (long)(a.rows[m] - 2) * nchi;
+#pragma unroll
+        for (int vo = 0; vo < 4; ++vo) bt = fma(a.bq[(slot + vo) * 4 + vin], x[vo * a.N + cell], bt);
+        if (a.shock) bt = fma(a.bs[slot + vin], x[4 * a.N + m], bt);
+      }
+      const double sg = (r & 1) ? 1.0 : -1.0;  // i w u: real part -w u_im, imaginary part +w u_re
+      for (int kk = 0; kk < a.nw; ++kk) {
+        const long idx = a.nop + kk * p4 + e;
+        y[idx] = a.scale * fma(sg * a.w[kk], xo[idx], bt);
+      }
+    } else if (t < nre * nchi) {
+      const long r = t / nchi;
+      const int m = (int)(t % nchi);
+      const double* x = a.X + r * a.ld;
+      double* y = a.Y + r * a.ld;
+      double acc[4] = {0, 0, 0, 0}, accs = 0;
+      for (int dd = -1; dd <= 1; ++dd) {
+        const int n = m + dd;
+        if (n < 0 || n >= nchi) continue;
+        const int slot = (m * 3 + dd + 1) * 4;
+#pragma unroll
+        for (int vin = 0; vin < 4; ++vin) {
+          double u = 0;
+          for (int kk = 0; kk < a.nw; ++kk) u += x[a.nop + kk * p4 + vin * nchi + n];
+#pragma unroll
+          for (int vo = 0; vo < 4; ++vo) acc[vo] = fma(a.bq[(slot + vo) * 4 + vin], u, acc[vo]);
+          accs = fma(a.bs[slot + vin], u, accs);
+        }
+      }
+      const long cell = m + (long)(a.rows[m] - 2) * nchi;
+#pragma unroll
+      for (int vo = 0; vo < 4; ++vo) y[vo * a.N + cell] += a.scale * acc[vo];
+      if (a.shock) y[4 * a.N + m] += a.scale * accs;
+    } else {
+      const long u = t - nre * nchi;
+      const long r = u / (a.nw * p4);
+      const long f = u % (a.nw * p4);
+      const int kk = (int)(f / p4);
+      const long idx = a.nop + f;
+      const double sg = (r & 1) ? -1.0 : 1.0;  // -i w u: real part +w u_im, imaginary part -w u_re
+      a.Y[r * a.ld + idx] = a.scale * (sg * a.w[kk] * a.X[(r ^ 1) * a.ld + idx]);
+    }
+  }
+}
+
+// t *= c, acc += t (n entries): one term of EXPONENTIAL!'s recurrence (CONSTRUCT_C.jl:78-111)
+__global__ void k_scale_acc(double* t, double* acc, double c, long n) {
+  for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+    const double v = t[q] * c;
+    t[q] = v;
+    acc[q] += v;
+  }
+}
+
 // acc += c t (n entries)
 __global__ void k_axpy(double* acc, const double* t, double c, long n) {
   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
@@ -665,13 +789,13 @@ int grid_for(long n, int threads) {
 }  // namespace
 
 void launch_shock_mv(const DevCtx& d, int k, const double* X, double* Y, int transpose, double scale,
-                     cudaStream_t st) {
+                     cudaStream_t st, long ld) {
   ShockMvArgs a;
   a.sj = d.sj;
   a.X = X;
   a.Y = Y;
   a.N = d.N;
-  a.ld = op_size(d);
+  a.ld = ld;
   a.scale = scale;
   a.nchi = d.nchi;
   a.k = k;
@@ -685,10 +809,11 @@ void launch_shock_mv(const DevCtx& d, int k, const double* X, double* Y, int tra
   k_shock_mv<<<dim3(bx, k), kShockThreads, shock_mv_smem(d.nchi, transpose), st>>>(a);
 }
 
-// y = scale A x over k vectors of op_size(d) entries: the stencil blocks, then the
-// shock-position blocks when the operator has them.
+// y = scale A x over k vectors of op_size(d) entries (stride ld, 0: op_size(d)): the stencil
+// blocks, then the shock-position blocks when the operator has them.
 void launch_matvec(const DevCtx& d, int k, const double* X, double* Y, int transpose, double scale,
-                   cudaStream_t st) {
+                   cudaStream_t st, long ld) {
+  if (ld <= 0) ld = op_size(d);
   MvArgs a;
   a.acc_prev = nullptr;
   a.c_prev = 0;
@@ -701,14 +826,61 @@ void launch_matvec(const DevCtx& d, int k, const double* X, double* Y, int trans
   a.c_acc = 0;
   a.w = make_wrap(d.cfg);
   a.N = d.N;
-  a.ld = op_size(d);
+  a.ld = ld;
   a.k = k;
   a.transpose = transpose;
   const long items = mv_items(d.N, k, d.sms);
   const int th = mv_threads(items, d.sms);
   if (mv_one(d.N, k, d.sms)) k_matvec<true><<<grid_for(items, th), th, 0, st>>>(a);
   else k_matvec<false><<<grid_for(items, th), th, 0, st>>>(a);
-  if (d.sj.on) launch_shock_mv(d, k, X, Y, transpose, scale, st);
+  if (d.sj.on) launch_shock_mv(d, k, X, Y, transpose, scale, st, ld);
+}
+
+long recept_size(const DevCtx& d, int nw) { return op_size(d) + (long)nw * 4 * d.nchi; }
+
+// y = scale L_ x (or scale L_^H x) for k complex vectors ([re; im] of recept_size each)
+void launch_recept_apply(const DevCtx& d, int k, int nw, const double* dw, const double* X, double* Y, int adjoint,
+                         double scale, cudaStream_t st) {
+  const long ld = recept_size(d, nw);
+  launch_matvec(d, 2 * k, X, Y, adjoint, scale, st, ld);
+  RecArgs a;
+  a.X = X;
+  a.Y = Y;
+  a.bq = d.bq;
+  a.bs = d.bs;
+  a.w = dw;
+  a.rows = d.brows;
+  a.N = d.N;
+  a.ld = ld;
+  a.nop = op_size(d);
+  a.scale = scale;
+  a.nchi = d.nchi;
+  a.nw = nw;
+  a.k = k;
+  a.adjoint = adjoint;
+  a.shock = d.sj.on;
+  const long items = adjoint ? 8L * k * d.nchi : 2L * k * d.nchi + 8L * k * nw * d.nchi;
+  k_recept_mv<<<grid_for(items, 256), 256, 0, st>>>(a);
+}
+
+// EXPONENTIAL! (Transient_growth_downstream/CONSTRUCT_C.jl:78-111) with L_: per step term =
+// vout, then term = (L_ dt) term / j and vout += term for j = 1..order. work: 2 x 2k x ld.
+void launch_recept_expm(const DevCtx& d, int k, int nw, const double* dw, double dt, int nsteps, int order,
+                        const double* X, double* Y, int adjoint, double* work, cudaStream_t st) {
+  const long n = 2L * k * recept_size(d, nw);
+  double* term = work;
+  double* t2 = work + n;
+  k_copy<<<grid_for(n, 256), 256, 0, st>>>(X, Y, n);
+  for (int s = 0; s < nsteps; ++s) {
+    k_copy<<<grid_for(n, 256), 256, 0, st>>>(Y, term, n);
+    double* src = term;
+    double* dst = t2;
+    for (int j = 1; j <= order; ++j) {
+      launch_recept_apply(d, k, nw, dw, src, dst, adjoint, dt, st);
+      k_scale_acc<<<grid_for(n, 256), 256, 0, st>>>(dst, Y, 1.0 / (double)j, n);
+      std::swap(src, dst);
+    }
+  }
 }
 
 // POWER_METHOD! (Eigenvalues/ARNOLDI_POWER_GPU.jl:64-82): per step vout = v,
@@ -827,16 +999,8 @@ void launch_shock_assemble(DevCtx& d, const double* const Fb[4], double* const F
   k_transpose<<<grid_for((long)nchi * nchi, 256), 256, 0, st>>>(d.sj.a22, d.sj.a22t, nchi, nchi);
 }
 
-void launch_jacobian_assemble(DevCtx& d, cudaStream_t st) {
+static PertArgs pert_args(const DevCtx& d) {
   const hymor_config& c = d.cfg;
-  const long N = d.N;
-  double* Fb[4];
-  double* Fp[4];
-  for (int v = 0; v < 4; ++v) {
-    Fb[v] = d.jwork + v * N;
-    Fp[v] = d.jwork + (4 + v) * N;
-  }
-  const bool shock_blocks = c.shock_enabled && c.perturb_shock;
   PertArgs pa;
   pa.S = d.S;
   pa.Y = d.Y;
@@ -852,9 +1016,23 @@ void launch_jacobian_assemble(DevCtx& d, cudaStream_t st) {
   pa.aY = d.aY;
   pa.nrcbc = (c.bc_chi0 == HYMOR_BC_OUTFLOW_NRCBC) | ((c.bc_chi1 == HYMOR_BC_OUTFLOW_NRCBC) << 1) |
              ((c.bc_eta0 == HYMOR_BC_OUTFLOW_NRCBC) << 2) | ((c.bc_eta1 == HYMOR_BC_OUTFLOW_NRCBC) << 3);
-  // base output: NON_LINEAR_DYNAMICS(deepcopy(s))
   pa.var = -1;
   pa.colour = 1;
+  return pa;
+}
+
+void launch_jacobian_assemble(DevCtx& d, cudaStream_t st) {
+  const hymor_config& c = d.cfg;
+  const long N = d.N;
+  double* Fb[4];
+  double* Fp[4];
+  for (int v = 0; v < 4; ++v) {
+    Fb[v] = d.jwork + v * N;
+    Fp[v] = d.jwork + (4 + v) * N;
+  }
+  const bool shock_blocks = c.shock_enabled && c.perturb_shock;
+  PertArgs pa = pert_args(d);
+  // base output: NON_LINEAR_DYNAMICS(deepcopy(s))
   k_perturb_thermo<<<grid_for(d.G, 256), 256, 0, st>>>(pa);
   launch_shock_bc_flags(d, false, true, c.shock_enabled, true, 0, st);
   launch_flux(d, false, Fb, st);
@@ -879,6 +1057,45 @@ void launch_jacobian_assemble(DevCtx& d, cudaStream_t st) {
       k_scatter<<<grid_for(N, 256), 256, 0, st>>>(sa);
     }
   if (shock_blocks) launch_shock_assemble(d, Fb, Fp, pa, st);
+}
+
+// LINEARIZE_B (Freestream_receptivity/LINEARIZE_B.jl:40-170): the residual with a prescribed
+// per-column upstream state (rho_0_upstream_p), once unperturbed and once per variable and
+// colour of columns (i = colour mod 3 raised by eps): 13 residuals. Each output column m has
+// exactly one raised column among m - 1, m, m + 1 per colour.
+void launch_b_assemble(DevCtx& d, cudaStream_t st) {
+  const hymor_config& c = d.cfg;
+  const long N = d.N;
+  const int nchi = d.nchi, cb = (nchi + 127) / 128;
+  const double eps = c.perturbation_magnitude;
+  double* Fb[4];
+  double* Fp[4];
+  Flux4 fb, fp;
+  for (int v = 0; v < 4; ++v) {
+    Fb[v] = d.jwork + v * N;
+    Fp[v] = d.jwork + (4 + v) * N;
+    fb.v[v] = Fb[v];
+    fp.v[v] = Fp[v];
+  }
+  double* cols = d.bwork;
+  double* rel_b = d.bwork + 4 * nchi;
+  const PertArgs pa = pert_args(d);
+  cudaMemcpyAsync(d.brows, d.cell_idx, sizeof(int) * nchi, cudaMemcpyDeviceToDevice, st);
+  cudaMemsetAsync(d.bq, 0, sizeof(double) * 48 * nchi, st);
+  cudaMemsetAsync(d.bs, 0, sizeof(double) * 12 * nchi, st);
+  d.up_cols = cols;
+  for (int var = -1; var < 4; ++var)
+    for (int colour = 0; colour < (var < 0 ? 1 : 3); ++colour) {
+      k_up_cols<<<cb, 128, 0, st>>>(cols, nchi, c.rho_0, c.rho_u_0, c.rho_v_0, c.rho_E_0, var, colour, eps);
+      k_perturb_thermo<<<grid_for(d.G, 256), 256, 0, st>>>(pa);
+      launch_shock_bc_flags(d, false, true, true, true, 0, st);
+      launch_flux(d, false, var < 0 ? Fb : Fp, st);
+      if (var < 0)
+        cudaMemcpyAsync(rel_b, d.rel, sizeof(double) * nchi, cudaMemcpyDeviceToDevice, st);
+      else
+        k_gather_b<<<cb, 128, 0, st>>>(fp, fb, d.rel, rel_b, d.brows, d.bq, d.bs, nchi, var, colour, eps);
+    }
+  d.up_cols = nullptr;
 }
 
 }  // namespace hymor
@@ -922,6 +1139,36 @@ int check_shock_rows_for_blocks(hymor_ctx* ctx, const int* rows, int nchi, int n
     if (rows[i] < 3 || rows[i] > neta - 1) {
       char msg[200];
       snprintf(msg, sizeof msg, "perturb_shock: shocked row %d of column %d outside 3..%d", rows[i], i + 1, neta - 1);
+      return ctx_fail(ctx, HYMOR_ERR_SHOCK_RANGE, msg);
+    }
+  return 0;
+}
+
+// Storage of the upstream-boundary operator B.
+int ensure_b(hymor_ctx* ctx) {
+  DevCtx& d = ctx_dev(ctx);
+  if (d.bq) return 0;
+  void* p = nullptr;
+  if (cudaMalloc(&p, sizeof(double) * 65 * (long)d.nchi) != cudaSuccess)
+    return ctx_fail(ctx, HYMOR_ERR_CUDA, "upstream-boundary operator allocation failed");
+  ctx_allocs(ctx).push_back(p);
+  d.bq = static_cast<double*>(p);
+  d.bs = d.bq + 48 * d.nchi;
+  d.bwork = d.bs + 12 * d.nchi;
+  if (cudaMalloc(&p, sizeof(int) * d.nchi) != cudaSuccess)
+    return ctx_fail(ctx, HYMOR_ERR_CUDA, "upstream-boundary operator allocation failed");
+  ctx_allocs(ctx).push_back(p);
+  d.brows = static_cast<int*>(p);
+  return 0;
+}
+
+// B's flux rows are the cells (m, sc_m - 1): sc_m must leave one flow cell below it.
+int check_b_rows(hymor_ctx* ctx, const int* rows, int nchi, int neta) {
+  for (int i = 0; i < nchi; ++i)
+    if (rows[i] < 2 || rows[i] > neta - 1) {
+      char msg[200];
+      snprintf(msg, sizeof msg, "upstream-boundary operator: shocked row %d of column %d outside 2..%d", rows[i], i + 1,
+               neta - 1);
       return ctx_fail(ctx, HYMOR_ERR_SHOCK_RANGE, msg);
     }
   return 0;
@@ -1388,11 +1635,95 @@ int hymor_krylov_rotate(hymor_ctx* ctx, int64_t n, int m, int kk, double* dV, in
   return cuda_check(ctx, cudaStreamSynchronize(st));
 }
 
+int hymor_linearize_b(hymor_ctx* ctx) {
+  if (!ctx) return HYMOR_ERR_INVALID;
+  DevCtx& d = ctx_dev(ctx);
+  if (!d.cfg.shock_enabled) return ctx_fail(ctx, HYMOR_ERR_INVALID, "the upstream-boundary operator needs shock fitting");
+  int r = ensure_linear(ctx);
+  if (r || (r = ensure_b(ctx))) return r;
+  cudaStream_t st = ctx_stream(ctx);
+  std::vector<int> rows(d.nchi);
+  cudaMemcpyAsync(rows.data(), d.cell_idx, sizeof(int) * d.nchi, cudaMemcpyDeviceToHost, st);
+  if ((r = cuda_check(ctx, cudaStreamSynchronize(st)))) return r;
+  if ((r = check_b_rows(ctx, rows.data(), d.nchi, d.neta))) return r;
+  launch_b_assemble(d, st);
+  if ((r = cuda_check(ctx, cudaGetLastError()))) return r;
+  return cuda_check(ctx, cudaStreamSynchronize(st));
+}
+
+int hymor_b_get(hymor_ctx* ctx, int32_t* rows, double* bq, double* bs) {
+  if (!ctx || !rows || !bq) return HYMOR_ERR_INVALID;
+  DevCtx& d = ctx_dev(ctx);
+  if (!d.bq) return ctx_fail(ctx, HYMOR_ERR_NOT_READY, "no upstream-boundary operator: call hymor_linearize_b");
+  cudaStream_t st = ctx_stream(ctx);
+  cudaMemcpyAsync(rows, d.brows, sizeof(int) * d.nchi, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(bq, d.bq, sizeof(double) * 48 * d.nchi, cudaMemcpyDeviceToHost, st);
+  if (bs) cudaMemcpyAsync(bs, d.bs, sizeof(double) * 12 * d.nchi, cudaMemcpyDeviceToHost, st);
+  return cuda_check(ctx, cudaStreamSynchronize(st));
+}
+
+int hymor_b_set(hymor_ctx* ctx, const int32_t* rows, const double* bq, const double* bs) {
+  if (!ctx || !rows || !bq || !bs) return HYMOR_ERR_INVALID;
+  DevCtx& d = ctx_dev(ctx);
+  int r;
+  if ((r = check_b_rows(ctx, rows, d.nchi, d.neta)) || (r = ensure_b(ctx))) return r;
+  cudaStream_t st = ctx_stream(ctx);
+  cudaMemcpyAsync(d.brows, rows, sizeof(int) * d.nchi, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(d.bq, bq, sizeof(double) * 48 * d.nchi, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(d.bs, bs, sizeof(double) * 12 * d.nchi, cudaMemcpyHostToDevice, st);
+  return cuda_check(ctx, cudaStreamSynchronize(st));
+}
+
+int hymor_recept_size(hymor_ctx* ctx, int nw, int64_t* n) {
+  if (!ctx || nw < 0 || !n) return HYMOR_ERR_INVALID;
+  *n = recept_size(ctx_dev(ctx), nw);
+  return 0;
+}
+
+// the frequencies on the device for one call (freed in stream order)
+static int recept_prep(hymor_ctx* ctx, int k, int nw, const double* w, const double* dX, double* dY, double** dw) {
+  if (!ctx || k < 1 || nw < 1 || !w || !dX || !dY) return HYMOR_ERR_INVALID;
+  DevCtx& d = ctx_dev(ctx);
+  if (!d.coef) return ctx_fail(ctx, HYMOR_ERR_NOT_READY, "no Jacobian: call hymor_linearize or hymor_jacobian_set");
+  if (!d.bq) return ctx_fail(ctx, HYMOR_ERR_NOT_READY, "no upstream-boundary operator: call hymor_linearize_b");
+  cudaStream_t st = ctx_stream(ctx);
+  int r;
+  if ((r = cuda_check(ctx, cudaMallocAsync((void**)dw, sizeof(double) * nw, st)))) return r;
+  return cuda_check(ctx, cudaMemcpyAsync(*dw, w, sizeof(double) * nw, cudaMemcpyHostToDevice, st));
+}
+
+int hymor_recept_apply_dev(hymor_ctx* ctx, int k, int nw, const double* w, double scale, const double* dX, double* dY,
+                           int adjoint) {
+  double* dw = nullptr;
+  int r = recept_prep(ctx, k, nw, w, dX, dY, &dw);
+  if (r) return r;
+  cudaStream_t st = ctx_stream(ctx);
+  launch_recept_apply(ctx_dev(ctx), k, nw, dw, dX, dY, adjoint, scale, st);
+  cudaFreeAsync(dw, st);
+  return cuda_check(ctx, cudaGetLastError());
+}
+
+int hymor_recept_expm_dev(hymor_ctx* ctx, int k, int nw, const double* w, double dt, int nsteps, int order,
+                          const double* dX, double* dY, int adjoint) {
+  if (nsteps < 0 || order < 1 || order > 20) return HYMOR_ERR_INVALID;
+  double* dw = nullptr;
+  int r = recept_prep(ctx, k, nw, w, dX, dY, &dw);
+  if (r) return r;
+  DevCtx& d = ctx_dev(ctx);
+  cudaStream_t st = ctx_stream(ctx);
+  double* work = nullptr;
+  const long n = 2L * k * recept_size(d, nw);
+  if ((r = cuda_check(ctx, cudaMallocAsync((void**)&work, sizeof(double) * 2 * n, st)))) return r;
+  launch_recept_expm(d, k, nw, dw, dt, nsteps, order, dX, dY, adjoint, work, st);
+  cudaFreeAsync(work, st);
+  cudaFreeAsync(dw, st);
+  return cuda_check(ctx, cudaGetLastError());
+}
+
 int hymor_block4_apply_ext_dev(hymor_ctx* ctx, int k, int64_t ntail, const double* dB, const double* dTail,
                                const double* dX, double* dY) {
   if (!ctx || k < 1 || ntail < 0 || !dB || (ntail && !dTail) || !dX || !dY) return HYMOR_ERR_INVALID;
   DevCtx& d = ctx_dev(ctx);
-  if (ntail > d.N) return ctx_fail(ctx, HYMOR_ERR_INVALID, "block4 tail longer than the cell count");
   k_block4_tail<<<grid_for(d.N * k, 256), 256, 0, ctx_stream(ctx)>>>(dB, dTail, dX, dY, d.N, ntail, k);
   return cuda_check(ctx, cudaGetLastError());
 }

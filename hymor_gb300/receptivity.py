@@ -1,0 +1,239 @@
+"""Freestream receptivity over libhymor (utils/Stability_analysis/Freestream_receptivity).
+
+The reference extends the linearised operator with the upstream state of every column and
+one block of freestream unknowns per disturbance frequency (LINEARIZE_L_.jl:36-71),
+
+    L_ = [L,  B, ..., B;  0, diag(-i w_k I_{4 Nchi})],
+
+and finds the freestream disturbances of largest energy gain over a horizon T: the
+generalised Hermitian eigenproblem C x = G D x with C = Z exp(L_ T)^H R'MR exp(L_ T) Z (Z
+zeroes the downstream cells, CONSTRUCT_C.jl:55-76) and D = R_' M_infty_ R_
+(FREESTREAM_RECEPTIVITY.jl:37-162). Here B is assembled on the device (hymor_linearize_b),
+L_ and its conjugate transpose act on the device (hymor_recept_apply_dev / _expm_dev), and
+the eigenproblem is solved by the device Krylov-Schur on the real form of the unknowns the
+initial condition may carry (the shock displacements and the freestream blocks), reduced
+with the per-block Cholesky factor of D. The weights (R, M, M_infty, a handful of 4 x 4
+blocks per column) are host-side set-up, as in the reference.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from ._lib import dp, ip
+from .krylov import DeviceBuffer, krylov_schur
+from .solver import CFL_TIMESTEP, LinearOperatorGPU, Solution, chu_blocks
+
+
+def GET_T_REF(s: Solution) -> float:
+    """GET_T_REF (GET_T_REF.jl:20-48): the downstream mass over the mass flux through the
+    shock, sum(rho flow vol) / sum_i bt_area(i, sc_i) |rho_u_0 n_x + rho_v_0 n_y|."""
+    st = s.get_state()
+    c, m = s._cs, s.case.mesh
+    nchi, neta = s.nchi, s.neta
+    rho = np.asarray(st["q"]).reshape(4, -1)[0].reshape(nchi + 2, neta + 2, order="F")[1:-1, 1:-1]
+    ci = st["cell_idx"]
+    flow = (np.arange(1, neta + 1)[None, :] < ci[:, None]).astype(float)
+    mass = float(np.sum(rho * flow * np.asarray(m["vol"])))
+    i = np.arange(nchi)
+    j = ci - 1
+    flux = np.abs(c.rho_u_0 * np.asarray(m["bt_xn"])[i, j] + c.rho_v_0 * np.asarray(m["bt_yn"])[i, j])
+    return mass / float(np.sum(np.asarray(m["bt_a"])[i, j] * flux))
+
+
+def freestream_blocks(s: Solution) -> np.ndarray:
+    """R_infty (CONSTRUCT_R_.jl:59-142): the 4 x 4 map from the conserved freestream
+    perturbation to (p, u, v, S) at the uniform freestream state."""
+    c = s._cs
+    g = c.gamma
+    rho, u, v, p = c.rho_0, c.rho_u_0 / c.rho_0, c.rho_v_0 / c.rho_0, c.p_0
+    return np.array([
+        [(g - 1) * (u**2 + v**2) / 2, -u * (g - 1), -v * (g - 1), g - 1],
+        [-u / rho, 1 / rho, 0, 0],
+        [-v / rho, 0, 1 / rho, 0],
+        [(u**2 + v**2) / (2 * p) - g / (g - 1) / rho, -u / p, -v / p, 1 / p]])
+
+
+def freestream_weights(s: Solution, w_infty, norms=(1, 1, 1, 1)) -> np.ndarray:
+    """The freestream blocks of D = R_' M_infty_ R_ (CONSTRUCT_M_INFTY_.jl:31-52 and
+    :63-160 with scaling_non_temporal, i.e. scaled by GET_T_REF): per frequency k and
+    column i, R_inf' diag(m) R_inf with the Chu weights of the freestream times the
+    column's shock arc length bt_area |n . V_inf / |V_inf||, halved for w_k != 0.
+    Returns (Nw, Nchi, 4, 4)."""
+    c, m = s._cs, s.case.mesh
+    g, rho, p = c.gamma, c.rho_0, c.p_0
+    a = s.case.fs["a_0"]
+    ci = s.get_state()["cell_idx"]
+    i, j = np.arange(s.nchi), ci - 1
+    vm = np.hypot(c.rho_u_0, c.rho_v_0)
+    proj = np.asarray(m["bt_xn"])[i, j] * (c.rho_u_0 / vm) + np.asarray(m["bt_yn"])[i, j] * (c.rho_v_0 / vm)
+    arc = np.asarray(m["bt_a"])[i, j] * np.abs(proj)
+    wv = np.array([rho * a**2 / (2 * (g * p) ** 2), rho / 2, rho / 2, (g - 1) * p / (2 * g)]) * np.asarray(norms)
+    Rinf = freestream_blocks(s)
+    T_ref = GET_T_REF(s)
+    out = np.empty((len(w_infty), s.nchi, 4, 4))
+    for k, w in enumerate(w_infty):
+        f = 1.0 if w == 0 else 0.5
+        mw = wv[None, :] * arc[:, None] * T_ref * f                    # (Nchi, 4)
+        out[k] = np.einsum("vi,nv,vj->nij", Rinf, mw, Rinf)
+    return out
+
+
+class ReceptivityOperator:
+    """L_ of LINEARIZE_L_ on the device for the frequencies w_infty: ``apply`` and ``expm``
+    on complex host vectors of n = hymor_recept_size unknowns [q; r; u_1; ...; u_Nw]."""
+
+    def __init__(self, L: LinearOperatorGPU, s: Solution, w_infty):
+        self.L, self.s = L, s
+        self.w = np.ascontiguousarray(w_infty, dtype=np.float64)
+        n = ctypes.c_int64()
+        s.ctx.check(s.ctx.L.hymor_recept_size(s.ctx.h, len(self.w), ctypes.byref(n)))
+        self.n = n.value
+        self.n_down = 4 * s.N
+
+    def _run(self, fn, x, *args):
+        X = np.asarray(x, dtype=complex).reshape(self.n, -1)
+        k = X.shape[1]
+        buf = np.empty((k, 2, self.n))
+        buf[:, 0], buf[:, 1] = X.real.T, X.imag.T
+        bx, by = DeviceBuffer(self.s.ctx, buf.nbytes), DeviceBuffer(self.s.ctx, buf.nbytes)
+        try:
+            bx.upload(buf.ravel())
+            fn(k, bx.ptr, by.ptr, *args)
+            out = by.download(buf.size).reshape(k, 2, self.n)
+        finally:
+            bx.free()
+            by.free()
+        Y = (out[:, 0] + 1j * out[:, 1]).T
+        return Y[:, 0] if np.ndim(x) == 1 else Y
+
+    def apply(self, x, adjoint: bool = False, scale: float = 1.0):
+        """scale L_ x, or scale L_^H x."""
+        c = self.s.ctx
+
+        def fn(k, src, dst):
+            c.check(c.L.hymor_recept_apply_dev(c.h, k, len(self.w), dp(self.w), float(scale), src, dst,
+                                               int(adjoint)))
+        return self._run(fn, x)
+
+    def expm(self, x, dt: float, nsteps: int, adjoint: bool = False, order: int = 5):
+        """EXPONENTIAL!'s Taylor propagation of x by nsteps steps of L_ dt (or L_^H dt)."""
+        c = self.s.ctx
+
+        def fn(k, src, dst):
+            c.check(c.L.hymor_recept_expm_dev(c.h, k, len(self.w), dp(self.w), float(dt), int(nsteps), int(order),
+                                              src, dst, int(adjoint)))
+        return self._run(fn, x)
+
+
+def LINEARIZE_B(s: Solution):
+    """LINEARIZE_B (LINEARIZE_B.jl:40-296) on the device; returns (rows, bq, bs) as
+    hymor_b_get lays them out: bq (Nchi, 3, 4, 4), bs (Nchi, 3, 4)."""
+    s.ctx.check(s.ctx.L.hymor_linearize_b(s.ctx.h))
+    n = s.nchi
+    rows = np.empty(n, dtype=np.int32)
+    bq, bs = np.empty(48 * n), np.empty(12 * n)
+    s.ctx.check(s.ctx.L.hymor_b_get(s.ctx.h, ip(rows), dp(bq), dp(bs)))
+    return rows, bq.reshape(n, 3, 4, 4), bs.reshape(n, 3, 4)
+
+
+def LINEARIZE_L_(L: LinearOperatorGPU, s: Solution, w_infty):
+    """LINEARIZE_L_ (LINEARIZE_L_.jl:36-71): B on the device and the extended operator L_
+    for the frequencies w_infty. Call after LINEARIZE_L. Returns (s, L_)."""
+    s.ctx.check(s.ctx.L.hymor_linearize_b(s.ctx.h))
+    return s, ReceptivityOperator(L, s, w_infty)
+
+
+def FREESTREAM_RECEPTIVITY(L_: ReceptivityOperator, s: Solution, n_modes: int, T: float, ncv: int | None = None,
+                           tol: float = 1e-8, order: int = 5, seed: int = 5, maxit: int = 300,
+                           modes: bool = False, keep_unconverged: bool = False):
+    """FREESTREAM_RECEPTIVITY (FREESTREAM_RECEPTIVITY.jl:37-162): the n_modes largest gains
+    G of Z P^H R'MR P Z x = G D x over the horizon T_opt = n_t dt (dt = T / round(T /
+    dt_CFL)), P the Taylor propagation of L_ (EXPONENTIAL!). The initial condition carries
+    no downstream cells (Z); its unknowns are the shock displacements (with the shock
+    unknowns, D = bt_area / 2 there) and the freestream blocks (D = R_inf' M_infty R_inf,
+    halved for w != 0). The problem is reduced with the block Cholesky factor K of D and
+    solved by the device Krylov-Schur on the real form (real and imaginary parts) of the
+    reduced complex Hermitian operator, which has the same eigenvalues; as the reference,
+    the gains are the eigenvalues / 2 (FREESTREAM_RECEPTIVITY.jl:113-116).
+
+    Returns (V, D, T_opt) like the reference: V the modes (n x n_modes complex, with modes
+    True, else None), D the gains; NaN with a warning when tol is not reached (:136-140),
+    unless keep_unconverged."""
+    import time
+    import warnings
+    dt_cfl = CFL_TIMESTEP(s)
+    n_t = int(round(T / dt_cfl))
+    dt = T / n_t
+    n, n4 = L_.n, L_.n_down
+    nr = L_.L.n - n4                     # shock displacements (0 without the shock unknowns)
+    nw, p = len(L_.w), 4 * s.nchi
+    # D on the free unknowns: the shock tail, then per frequency and column a 4 x 4 block
+    ci = s.get_state()["cell_idx"]
+    d_r = np.asarray(s.case.mesh["bt_a"])[np.arange(s.nchi), ci - 1] / 2 if nr else np.zeros(0)
+    Dk = freestream_weights(s, L_.w)                                   # (Nw, Nchi, 4, 4)
+    Kinv = np.linalg.inv(np.linalg.cholesky(Dk))
+    kr = 1 / np.sqrt(d_r)
+    nf = nr + nw * p                                                  # free unknowns (complex)
+
+    def k_inv_t(y):   # x = K^-H y on the free unknowns (K real)
+        x = np.empty_like(y)
+        x[:nr] = kr * y[:nr]
+        U = y[nr:].reshape(nw, 4, s.nchi)
+        x[nr:] = np.einsum("knji,kjn->kin", Kinv, U).reshape(-1)
+        return x
+
+    def k_inv(y):     # K^-1 y
+        x = np.empty_like(y)
+        x[:nr] = kr * y[:nr]
+        U = y[nr:].reshape(nw, 4, s.nchi)
+        x[nr:] = np.einsum("knij,kjn->kin", Kinv, U).reshape(-1)
+        return x
+    C0, _ = chu_blocks(s)
+    bC0 = DeviceBuffer(s.ctx, 8 * s.N * 16)
+    bC0.upload(np.ascontiguousarray(C0.reshape(-1)))
+    tail0 = DeviceBuffer(s.ctx, 8 * (n - n4))
+    tail0.upload(np.zeros(n - n4))
+    bz = [DeviceBuffer(s.ctx, 8 * 2 * n) for _ in range(2)]
+    c = s.ctx
+    count = [0]
+
+    def apply_op(src, dst):
+        count[0] += 1
+        y = np.empty(2 * nf)
+        c.check(c.L.hymor_memcpy_d2h(c.h, y.ctypes.data, src, y.nbytes))
+        x = k_inv_t(y[:nf] + 1j * y[nf:])
+        z = np.zeros((2, n))
+        z[0, n4:], z[1, n4:] = x.real, x.imag
+        bz[0].upload(z.ravel())
+        c.check(c.L.hymor_recept_expm_dev(c.h, 1, nw, dp(L_.w), dt, n_t, order, bz[0].ptr, bz[1].ptr, 0))
+        c.check(c.L.hymor_block4_apply_ext_dev(c.h, 2, n - n4, bC0.ptr, tail0.ptr, bz[1].ptr, bz[0].ptr))
+        c.check(c.L.hymor_recept_expm_dev(c.h, 1, nw, dp(L_.w), dt, n_t, order, bz[0].ptr, bz[1].ptr, 1))
+        out = bz[1].download(2 * n).reshape(2, n)
+        r = k_inv(out[0, n4:] + 1j * out[1, n4:])
+        res = np.concatenate([r.real, r.imag])
+        c.check(c.L.hymor_memcpy_h2d(c.h, dst, res.ctypes.data, res.nbytes))
+    ncv = ncv or max(2 * n_modes + 1, 16)
+    t0 = time.perf_counter()
+    try:
+        lam, resid, nops, Y = krylov_schur(c, 2 * nf, apply_op, n_modes, ncv, tol=tol, maxit=maxit, seed=seed,
+                                           symmetric=True, want_vectors=True)
+    finally:
+        for b in [bC0, tail0] + bz:
+            b.free()
+    elapsed = time.perf_counter() - t0
+    lam = np.real(lam)
+    converged = bool(np.all(resid <= tol * np.abs(lam)))
+    gains = lam / 2
+    V = None
+    if modes and Y is not None:
+        V = np.zeros((n, n_modes), dtype=complex)
+        for m_ in range(n_modes):
+            V[n4:, m_] = k_inv_t(Y[:nf, m_] + 1j * Y[nf:, m_])
+    if not converged and not keep_unconverged:
+        warnings.warn(f"receptivity solve did not reach tol {tol:g} in {maxit} restarts; returning NaN")
+        gains = np.full(n_modes, np.nan)
+        V = np.full((n, n_modes), np.nan + 0j) if modes else None
+    info = dict(resid=resid, dt=dt, n_t=n_t, nops=nops, seconds=elapsed, converged=converged, applications=count[0])
+    return V, gains, n_t * dt, info

@@ -230,6 +230,32 @@ int hymor_expm_apply_multi_dev(hymor_ctx* ctx, int k, const double* dts, const i
 int hymor_expm_apply_dev_noalloc(hymor_ctx* ctx, int k, double dt, int nsteps, int order,
                                  const double* dX, double* dY, int transpose);
 
+/* ---- Freestream receptivity (utils/Stability_analysis/Freestream_receptivity) ----
+ * LINEARIZE_B (LINEARIZE_B.jl:40-296): the upstream-boundary operator B, the response of
+ * the residual to a per-column upstream state (rho_0_upstream_p) [rho; rho_u; rho_v; rho_E]
+ * (4 x Nchi), assembled on the device with 13 residuals (3 colours of columns per
+ * variable). With sc_m the 1-based shocked row of column m at assembly and n = m + d,
+ * d = -1, 0, 1:
+ *   rows[m] = sc_m,
+ *   bq[((m*3 + d+1)*4 + vout)*4 + vin] = d flux_vout(m, sc_m - 1) / d upstream_vin(n),
+ *   bs[(m*3 + d+1)*4 + vin] = d speed_m / d upstream_vin(n)   (rows of the shock unknowns).
+ * Needs shock fitting and 2 <= sc_m <= Neta - 1; call after hymor_linearize. */
+int hymor_linearize_b(hymor_ctx* ctx);
+int hymor_b_get(hymor_ctx* ctx, int32_t* rows, double* bq, double* bs);
+int hymor_b_set(hymor_ctx* ctx, const int32_t* rows, const double* bq, const double* bs);
+/* The extended operator of LINEARIZE_L_ (LINEARIZE_L_.jl:36-71) for nw frequencies w (host
+ * array): L_ = [L, B ... B; 0, diag(-i w_k I_{4 Nchi})], n_ = hymor_operator_size + nw*4*Nchi
+ * unknowns (hymor_recept_size). Complex vectors are stored as their real part followed by
+ * their imaginary part (2 n_ doubles each); k of them back to back. */
+int hymor_recept_size(hymor_ctx* ctx, int nw, int64_t* n);
+/* Y = scale L_ X, or scale L_^H X (adjoint: the conjugate transpose). Device pointers. */
+int hymor_recept_apply_dev(hymor_ctx* ctx, int k, int nw, const double* w, double scale, const double* dX,
+                           double* dY, int adjoint);
+/* EXPONENTIAL! (Transient_growth_downstream/CONSTRUCT_C.jl:78-111) with L_ (or L_^H): per
+ * step term = Y, then term = (L_ dt) term / j and Y += term for j = 1..order. */
+int hymor_recept_expm_dev(hymor_ctx* ctx, int k, int nw, const double* w, double dt, int nsteps, int order,
+                          const double* dX, double* dY, int adjoint);
+
 /* ---- Device-resident Krylov building blocks (replace the host Arpack loop around the
  * GPU matvec, Eigenvalues/EIGENVALUES.jl:159 and TRANSIENT_GROWTH_DOWNSTREAM.jl:103).
  * Reductions are deterministic (fixed block partition, fixed-order trees). */
@@ -249,7 +275,8 @@ int hymor_krylov_rotate(hymor_ctx* ctx, int64_t n, int m, int k, double* dV, int
  * CONSTRUCT_R.jl:24-133, CONSTRUCT_M.jl:27-94, CONSTRUCT_M_HAT.jl:25-105). */
 int hymor_block4_apply_dev(hymor_ctx* ctx, int k, const double* dB, const double* dX, double* dY);
 /* Same for k vectors of 4N + ntail entries: the cells as above, the tail scaled by dTail
- * (ntail <= N doubles) — the shock-position entries of R'M^R (CONSTRUCT_M_HAT.jl:78-90). */
+ * (ntail doubles) — the shock-position entries of R'M^R (CONSTRUCT_M_HAT.jl:78-90), or
+ * the freestream blocks of the receptivity operator. */
 int hymor_block4_apply_ext_dev(hymor_ctx* ctx, int k, int64_t ntail, const double* dB, const double* dTail,
                                const double* dX, double* dY);
 

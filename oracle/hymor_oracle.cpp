@@ -120,6 +120,9 @@ struct State {
   vec flow;                   // Nchi x Neta, shock["flow_cells"]
   vec beta, speed_x, speed_y, rel_vel;
   vec flux_rho, flux_rho_u, flux_rho_v, flux_rho_E;  // Nchi x Neta
+  // prescribed per-column upstream state (s["rho_0_upstream_p"] with freestream
+  // rho_0_p, rho_u_0_p, rho_v_0_p, rho_E_0_p, 4 x Nchi), empty when absent
+  vec up_cols;
   double t = 0, dt = 0;
   int rho_limited = 0;
   int rh_warnings = 0;
@@ -409,6 +412,12 @@ void compute_upstream_conditions(const orc_config& c, const State& s, vec& p_inf
     double rho_u = c.rho_u_0 + pert * c.dist_amp[1];
     double rho_v = c.rho_v_0 + pert * c.dist_amp[2];
     double rho_E = c.rho_E_0 + pert * c.dist_amp[3];
+    if (!s.up_cols.empty()) {  // :87-91
+      rho = s.up_cols[i];
+      rho_u = s.up_cols[n + i];
+      rho_v = s.up_cols[2 * n + i];
+      rho_E = s.up_cols[3 * n + i];
+    }
     if (c.axisymmetric && i == 0) rho_v = 0;
     double vi = rho_v / rho;
     double ui = rho_u / rho;
@@ -448,6 +457,14 @@ void update_field_upstream(const orc_config& c, const Mesh& m, State& s) {
     int sc = s.cell_idx[i - 1];
     for (int jg = sc + 3; jg <= c.neta + 2; ++jg) {
       int k = d.gi(i + 1, jg);
+      if (!s.up_cols.empty()) {  // prescribed per-column upstream state (:75-90)
+        const int n = c.nchi;
+        s.rho[k] = s.up_cols[i - 1];
+        s.rho_u[k] = s.up_cols[n + i - 1];
+        s.rho_v[k] = s.up_cols[2 * n + i - 1];
+        s.rho_E[k] = s.up_cols[3 * n + i - 1];
+        continue;
+      }
       double pert = std::cos(two_pi_ky * (m.y_ext[k] - u_y_t)) * std::sin(two_pi_kx * (m.x_ext[k] - u_x_t));
       s.rho[k] = c.rho_0 + pert * c.dist_amp[0];
       s.rho_u[k] = c.rho_u_0 + pert * c.dist_amp[1];
@@ -1296,6 +1313,56 @@ void linearize_shock_blocks(const orc_config& c, const Mesh& m, const State& s, 
   }
 }
 
+// utils/Stability_analysis/Freestream_receptivity/LINEARIZE_B.jl:40-296: the response of the
+// residual to the per-column upstream state, column-wise finite differences with 3 colours
+// (LINEARIZE_B.jl:49-170) and GET_BLOCK's left / middle / right neighbours (:186-253).
+// rows[m] = sc_m; bq[((m*3 + d+1)*4 + vout)*4 + vin] and bs[(m*3 + d+1)*4 + vin] for the
+// input column n = m + d (0-based), as include/hymor.h documents for hymor_b_get.
+void linearize_b(const orc_config& c, const Mesh& m, const State& s0, int* rows, double* bq, double* bs) {
+  const int nchi = c.nchi;
+  const Dims d{nchi, c.neta};
+  const double eps = c.perturbation_magnitude;
+  State s = s0;
+  s.up_cols.assign(4 * (size_t)nchi, 0.0);
+  const double fs[4] = {c.rho_0, c.rho_u_0, c.rho_v_0, c.rho_E_0};
+  for (int v = 0; v < 4; ++v)
+    for (int i = 0; i < nchi; ++i) s.up_cols[(size_t)v * nchi + i] = fs[v];
+  orc_config cz = c;  // the disturbance amplitude is set to zero (:45)
+  for (int v = 0; v < 4; ++v) cz.dist_amp[v] = 0;
+  State base = s;
+  non_linear_dynamics(cz, m, base);
+  for (int i = 0; i < nchi; ++i) rows[i] = s.cell_idx[i];
+  std::memset(bq, 0, sizeof(double) * 48 * nchi);
+  std::memset(bs, 0, sizeof(double) * 12 * nchi);
+  for (int var = 0; var < 4; ++var)
+    for (int iter = 1; iter <= 3; ++iter) {
+      State sp = s;
+      for (int i = iter; i <= nchi; i += 3) sp.up_cols[(size_t)var * nchi + i - 1] += eps * 1.0;
+      non_linear_dynamics(cz, m, sp);
+      // GET_BLOCK's (output column pert_m, input column pert_n) pairs, 1-based
+      auto block = [&](const std::vector<int>& pm, const std::vector<int>& pn) {
+        for (size_t k = 0; k < pm.size(); ++k) {
+          const int mo = pm[k] - 1, ni = pn[k] - 1, dd = ni - mo;
+          const int cell = d.ci(pm[k], s.cell_idx[mo] - 1);
+          const vec* fp[4] = {&sp.flux_rho, &sp.flux_rho_u, &sp.flux_rho_v, &sp.flux_rho_E};
+          const vec* fb[4] = {&base.flux_rho, &base.flux_rho_u, &base.flux_rho_v, &base.flux_rho_E};
+          for (int vo = 0; vo < 4; ++vo)
+            bq[((mo * 3 + dd + 1) * 4 + vo) * 4 + var] = ((*fp[vo])[cell] - (*fb[vo])[cell]) / eps;
+          bs[(mo * 3 + dd + 1) * 4 + var] = (sp.rel_vel[mo] - base.rel_vel[mo]) / eps;
+        }
+      };
+      std::vector<int> pm, pn;
+      for (int x = (iter == 1 ? iter + 2 : iter - 1); x <= nchi - 1; x += 3) { pm.push_back(x); pn.push_back(x + 1); }
+      block(pm, pn);
+      pm.clear(); pn.clear();
+      for (int x = iter; x <= nchi; x += 3) { pm.push_back(x); pn.push_back(x); }
+      block(pm, pn);
+      pm.clear(); pn.clear();
+      for (int x = iter + 1; x <= nchi; x += 3) { pm.push_back(x); pn.push_back(x - 1); }
+      block(pm, pn);
+    }
+}
+
 // The shock-block part of y = A x on vectors [q (4N); r (Nchi)], after stencil_matvec has
 // written y's first 4N entries; a21 compact (Nchi x 8, entry (j - 1) * 4 + v).
 void shock_matvec(const orc_config& c, const int* rows, const double* a21, const double* a12, const double* a22,
@@ -1609,6 +1676,18 @@ void orc_jacobian(orc_ctx* c, double* coef) { linearize_equations(c->c, c->m, c-
 
 void orc_matvec(const orc_config* cfg, const double* coef, const double* x, double* y, int transpose) {
   stencil_matvec(*cfg, coef, x, y, transpose);
+}
+
+// LINEARIZE_B of the prepared state (run orc_linearize first).
+int orc_linearize_b(orc_ctx* c, int32_t* rows, double* bq, double* bs) {
+  ORC_GUARD(linearize_b(c->c, c->m, c->s, rows, bq, bs));
+}
+
+// Per-column upstream state of the context (4 x Nchi; NULL removes it), for residuals with
+// a prescribed upstream state (CHECK_LINEARIZATION_B).
+void orc_set_upstream(orc_ctx* c, const double* cols) {
+  if (!cols) c->s.up_cols.clear();
+  else c->s.up_cols.assign(cols, cols + 4 * (size_t)c->c.nchi);
 }
 
 // Shock-position blocks of the prepared state (run orc_linearize first; see

@@ -48,6 +48,8 @@ def lib() -> ctypes.CDLL:
         L.orc_set_threads.argtypes = [ctypes.c_int]
         L.orc_shock_blocks.argtypes = [vp, ip, dp, dp, dp]
         L.orc_get_rel_vel.argtypes = [vp, dp]
+        L.orc_linearize_b.argtypes = [vp, ip, dp, dp]
+        L.orc_set_upstream.argtypes = [vp, dp]
         L.orc_matvec_ext.argtypes = [vp, dp, ip, dp, dp, dp, dp, dp, ctypes.c_int]
         L.orc_expm_ext.argtypes = [vp, dp, ip, dp, dp, dp, ctypes.c_double, ctypes.c_int, ctypes.c_int, dp, dp,
                                    ctypes.c_int]
@@ -158,6 +160,23 @@ class Oracle:
         r = np.empty(self.cs.nchi)
         lib().orc_get_rel_vel(self.h, dptr(r))
         return r
+
+    def linearize_b(self):
+        """LINEARIZE_B of the prepared state: rows (Nchi), bq (Nchi x 3 x 4 x 4: output column,
+        input column offset + 1, vout, vin), bs (Nchi x 3 x 4)."""
+        n = self.cs.nchi
+        rows = np.empty(n, dtype=np.int32)
+        bq, bs = np.empty(48 * n), np.empty(12 * n)
+        _check(lib().orc_linearize_b(self.h, _ip(rows), dptr(bq), dptr(bs)))
+        return rows, bq.reshape(n, 3, 4, 4), bs.reshape(n, 3, 4)
+
+    def set_upstream(self, cols):
+        """Prescribed per-column upstream state (4 x Nchi), or None."""
+        if cols is None:
+            lib().orc_set_upstream(self.h, None)
+        else:
+            cols = np.ascontiguousarray(cols, dtype=np.float64).ravel()
+            lib().orc_set_upstream(self.h, dptr(cols))
 
     def shock_blocks(self):
         """The shock-position blocks of the prepared state (after linearize()): rows (Nchi),

@@ -1,0 +1,182 @@
+"""Freestream receptivity (utils/Stability_analysis/Freestream_receptivity): the oracle's
+LINEARIZE_B against the reference's own consistency measure (CHECK_LINEARIZATION_B.jl) on
+the CPU; on the GPU the device B against the oracle's, the extended operator L_ and its
+propagation against a sparse restatement built from the same blocks, and
+FREESTREAM_RECEPTIVITY's gains against eigsh on that restatement."""
+import numpy as np
+import pytest
+
+from hymor_gb300 import case as C
+from oracle import oracle as O
+
+from helpers import rel_err
+
+
+def _oracle_case(nchi=30, neta=24, steps=5):
+    cfg = C.cylinder_config(nchi, neta)
+    cs = C.initial_state(cfg)
+    orc = O.Oracle(cs)
+    orc.advect(steps)
+    co = orc.linearize()
+    return cfg, cs, orc, co
+
+
+def b_apply(cfg, rows, bq, P):
+    """B P on the flux rows (m, sc_m - 1): P (4, Nchi) per-column upstream perturbation."""
+    nchi, N = cfg.nchi, cfg.nchi * cfg.neta
+    y = np.zeros(4 * N)
+    for m in range(nchi):
+        cell = m + (rows[m] - 2) * nchi
+        for d in (-1, 0, 1):
+            n = m + d
+            if 0 <= n < nchi:
+                y[np.arange(4) * N + cell] += bq[m, d + 1] @ P[:, n]
+    return y
+
+
+def test_linearize_b_consistency():
+    """CHECK_LINEARIZATION_B: B q matches the change of the masked residual when the
+    per-column upstream state moves by q (every column at once, 1e-7 * randn)."""
+    cfg, cs, orc, co = _oracle_case()
+    rows, bq, bs = orc.linearize_b()
+    st = orc.get_state()
+    fs = np.array([orc.cs.rho_0, orc.cs.rho_u_0, orc.cs.rho_v_0, orc.cs.rho_E_0])
+    base_cols = np.repeat(fs[:, None], cfg.nchi, axis=1)
+    P = 1e-7 * np.random.Generator(np.random.PCG64(12)).standard_normal((4, cfg.nchi))
+    f = []
+    for cols in (base_cols, base_cols + P):
+        o = O.Oracle(cs)
+        o.set_state(st["q"], st["pts_x"], st["pts_y"], st["pts_chi"], st["pts_eta"], st["cell_idx"], st["t"])
+        o.set_upstream(cols)
+        f.append(o.residual())
+    flow = np.tile((np.arange(1, cfg.neta + 1)[None, :] < st["cell_idx"][:, None]).ravel(order="F"), 4)
+    df = (f[1] - f[0]) * flow
+    Bq = b_apply(cfg, rows, bq, P)
+    assert np.linalg.norm(df) > 0
+    assert np.linalg.norm(Bq - df) < 1e-4 * np.linalg.norm(df)
+    # B couples each column to its neighbours only, and the uniform state is a no-op
+    assert np.all(bq[0, 0] == 0) and np.all(bq[-1, 2] == 0)
+
+
+# ---------------------------------------------------------------------------
+# GPU, through the C ABI
+
+
+def _gpu_case(nchi=24, neta=20, steps=20):
+    from hymor_gb300 import solver as S
+    cfg = C.cylinder_config(nchi, neta)
+    cs = C.initial_state(cfg)
+    sol, orc = S.Solution(cs), O.Oracle(cs)
+    S.ADVECT_FLOW(sol, steps)
+    orc.advect(steps)
+    _, L = S.LINEARIZE_L(sol)
+    co = orc.linearize()
+    return cfg, cs, sol, orc, L, co
+
+
+def _sparse_recept(cfg, coef, rows, bq, w):
+    """L_ = [L, B ... B; 0, diag(-i w_k I)] as a scipy sparse matrix from the blocks."""
+    import scipy.sparse as sp
+    nchi, N = cfg.nchi, cfg.nchi * cfg.neta
+    L = O.stencil_to_csr(cfg, coef)
+    r, c, v = [], [], []
+    for m in range(nchi):
+        cell = m + (rows[m] - 2) * nchi
+        for d in (-1, 0, 1):
+            n = m + d
+            if 0 <= n < nchi:
+                for vo in range(4):
+                    for vi in range(4):
+                        r.append(vo * N + cell)
+                        c.append(vi * nchi + n)
+                        v.append(bq[m, d + 1, vo, vi])
+    B = sp.csr_matrix((v, (r, c)), shape=(4 * N, 4 * nchi))
+    p = 4 * nchi
+    top = sp.hstack([L] + [B] * len(w))
+    bot = sp.hstack([sp.csr_matrix((len(w) * p, 4 * N)), sp.kron(sp.diags(-1j * np.asarray(w)), sp.eye(p))])
+    return sp.vstack([top, bot]).tocsr().astype(complex)
+
+
+def _exponential(A, x, dt, n_t, order=5):
+    """EXPONENTIAL!'s Taylor recurrence (CONSTRUCT_C.jl:78-111) with the matrix A dt."""
+    Adt = A * dt
+    vout = x.copy()
+    for _ in range(n_t):
+        term = vout.copy()
+        for j in range(1, order + 1):
+            term = (Adt @ term) * (1.0 / j)
+            vout = vout + term
+    return vout
+
+
+@pytest.mark.gpu
+def test_b_parity(require_gpu):
+    """The device's LINEARIZE_B against the oracle's (finite differences with eps = 1e-8 of
+    residuals that agree to ~1e-13: agreement to the FD rounding)."""
+    from hymor_gb300 import receptivity as R
+    cfg, cs, sol, orc, L, co = _gpu_case()
+    rows, bq, bs = R.LINEARIZE_B(sol)
+    rows_o, bq_o, bs_o = orc.linearize_b()
+    assert np.array_equal(rows, rows_o)
+    assert rel_err(bq, bq_o) < 1e-5
+    assert rel_err(bs, bs_o) < 1e-5
+
+
+@pytest.mark.gpu
+def test_receptivity_operator_parity(require_gpu):
+    """L_ and L_^H (hymor_recept_apply_dev) and their Taylor propagation against the sparse
+    restatement from the device's own blocks: 1e-12."""
+    from hymor_gb300 import receptivity as R
+    cfg, cs, sol, orc, L, co = _gpu_case()
+    w = [0.0, 1.5, 4.0]
+    _, Lr = R.LINEARIZE_L_(L, sol, w)
+    rows, bq, _ = R.LINEARIZE_B(sol)
+    A = _sparse_recept(cfg, L.blocks(), rows, bq, w)
+    assert A.shape == (Lr.n, Lr.n)
+    rng = np.random.Generator(np.random.PCG64(6))
+    X = rng.standard_normal((Lr.n, 2)) + 1j * rng.standard_normal((Lr.n, 2))
+    for adj, M in ((False, A), (True, A.conj().T.tocsr())):
+        Y = Lr.apply(X, adjoint=adj)
+        for j in range(2):
+            ref = M @ X[:, j]
+            assert np.max(np.abs(Y[:, j] - ref)) <= 1e-12 * np.max(np.abs(ref))
+        P = Lr.expm(X[:, 0], 2e-3, 7, adjoint=adj)
+        ref = _exponential(M, X[:, 0], 2e-3, 7)
+        assert np.max(np.abs(P - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+@pytest.mark.gpu
+def test_freestream_receptivity_vs_eigsh(require_gpu):
+    """FREESTREAM_RECEPTIVITY (device Krylov-Schur on the real form of the reduced Hermitian
+    problem) against eigsh on the complex Hermitian operator composed from the sparse
+    restatement, the same weights and the same propagation: gains to 1e-6."""
+    sla = pytest.importorskip("scipy.sparse.linalg")
+    from hymor_gb300 import receptivity as R
+    from hymor_gb300 import solver as S
+    cfg, cs, sol, orc, L, co = _gpu_case()
+    w = [0.0, 2.0]
+    _, Lr = R.LINEARIZE_L_(L, sol, w)
+    V, G, T_opt, info = R.FREESTREAM_RECEPTIVITY(Lr, sol, 2, 0.01, ncv=16, tol=1e-10, modes=True)
+    rows, bq, _ = R.LINEARIZE_B(sol)
+    A = _sparse_recept(cfg, L.blocks(), rows, bq, w)
+    AH = A.conj().T.tocsr()
+    N, p = cfg.nchi * cfg.neta, 4 * cfg.nchi
+    C0, _ = S.chu_blocks(sol)
+    Ki = np.linalg.inv(np.linalg.cholesky(R.freestream_weights(sol, w)))   # (Nw, Nchi, 4, 4)
+    dt, nt = info["dt"], info["n_t"]
+
+    def mv(y):
+        y = np.asarray(y).ravel()
+        x = np.einsum("knji,kjn->kin", Ki, y.reshape(len(w), 4, cfg.nchi)).ravel()
+        z = np.concatenate([np.zeros(4 * N, dtype=complex), x])
+        z = _exponential(A, z, dt, nt)
+        q = z[:4 * N].reshape(4, N).T
+        z = np.concatenate([np.einsum("nij,nj->ni", C0, q).T.ravel(), np.zeros(len(w) * p)])
+        z = _exponential(AH, z, dt, nt)
+        return np.einsum("knij,kjn->kin", Ki, z[4 * N:].reshape(len(w), 4, cfg.nchi)).ravel()
+    nf = len(w) * p
+    op = sla.LinearOperator((nf, nf), matvec=mv, dtype=complex)
+    lam = np.sort(np.real(sla.eigsh(op, k=2, which="LA", tol=1e-12, return_eigenvectors=False)))[::-1] / 2
+    assert np.allclose(np.sort(G)[::-1], lam, rtol=1e-6, atol=0)
+    assert info["converged"] and V.shape == (Lr.n, 2)
+    assert np.all(V[:4 * N] == 0)
