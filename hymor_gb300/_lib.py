@@ -37,7 +37,7 @@ EXPORTS = [
     "hymor_profile_phases", "hymor_advect", "hymor_bench_matvec", "hymor_operator_size",
     "hymor_shock_blocks_get", "hymor_shock_blocks_set", "hymor_shock_fields", "hymor_block4_apply_ext_dev",
     "hymor_expm_apply_multi_dev", "hymor_linearize_b", "hymor_b_get", "hymor_b_set", "hymor_recept_size",
-    "hymor_recept_apply_dev", "hymor_recept_expm_dev",
+    "hymor_recept_apply_dev", "hymor_recept_expm_dev", "hymor_set_upstream",
 ]
 
 
@@ -107,6 +107,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "hymor_shock_blocks_set": [vp, ip, dp, dp, dp],
         "hymor_shock_fields": [vp, dp, dp],
         "hymor_linearize_b": [vp],
+        "hymor_set_upstream": [vp, dp],
         "hymor_b_get": [vp, ip, dp, dp],
         "hymor_b_set": [vp, ip, dp, dp],
         "hymor_recept_size": [vp, i, ctypes.POINTER(ctypes.c_int64)],

@@ -613,6 +613,7 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
   d.bq = nullptr;
   d.bs = nullptr;
   d.brows = nullptr;
+  d.res_up = nullptr;
   d.bwork = nullptr;
   d.sf_zero = 1;  // the flux arrays are allocated zeroed
   for (int k = 0; k < hymor_ctx_s::kEv; ++k)
@@ -654,6 +655,7 @@ int hymor_ctx_destroy(hymor_ctx* ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   linear_state_release(ctx->linear_state);
+  if (ctx->d.res_up) cudaFree(ctx->d.res_up);
   if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
   if (ctx->graph) cudaGraphDestroy(ctx->graph);
   for (auto e : ctx->cap_ev)
@@ -732,7 +734,9 @@ int hymor_residual(hymor_ctx* ctx, double* flux) {
   launch_update_thermo(d, 3, 0, 0, st);
   launch_sound_cmax(d, true, st);
   ctx->a_stale = false;
+  d.up_cols = d.res_up;  // rho_0_upstream_p of the reference's Dict, when set
   launch_shock_bc(d, true, false, false, 0, 0, 1, st);
+  d.up_cols = nullptr;
   double* const SF[4] = {d.SF[0], d.SF[1], d.SF[2], d.SF[3]};
   launch_flux(d, true, SF, st);
   stored_flux_written(ctx);
@@ -741,6 +745,24 @@ int hymor_residual(hymor_ctx* ctx, double* flux) {
     for (int v = 0; v < 4; ++v)
       CU(cudaMemcpyAsync(flux + v * d.N, d.SF[v], d.N * 8, cudaMemcpyDeviceToHost, st));
   return read_err(ctx);
+}
+
+int hymor_set_upstream(hymor_ctx* ctx, const double* cols) {
+  if (!ctx) return HYMOR_ERR_INVALID;
+  TRY(set_device(ctx));
+  DevCtx& d = ctx->d;
+  if (!cols) {
+    if (d.res_up) {
+      CU(cudaStreamSynchronize(ctx->stream));
+      CU(cudaFree(d.res_up));
+    }
+    d.res_up = nullptr;
+    return 0;
+  }
+  if (!d.res_up) CU(cudaMalloc(&d.res_up, sizeof(double) * 4 * d.nchi));
+  CU(cudaMemcpyAsync(d.res_up, cols, sizeof(double) * 4 * d.nchi, cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return 0;
 }
 
 int hymor_set_flux(hymor_ctx* ctx, const double* flux) {

@@ -59,6 +59,7 @@ struct DevCtx {
   // n = m + d (d = -1, 0, 1), bq[((m*3 + d+1)*4 + vout)*4 + vin] = d flux_vout(m, sc_m - 1) /
   // d upstream_vin(n) and bs[(m*3 + d+1)*4 + vin] = d speed_m / d upstream_vin(n)
   double *bq, *bs;
+  double* res_up;  // 4 x Nchi upstream state of hymor_residual (hymor_set_upstream), or null
   int* brows;      // Nchi: the shocked rows sc_m of B's flux rows
   double* bwork;   // 5 x Nchi: the per-column upstream state and the base shock speeds
 };

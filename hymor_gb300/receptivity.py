@@ -138,6 +138,52 @@ def LINEARIZE_B(s: Solution):
     return rows, bq.reshape(n, 3, 4, 4), bs.reshape(n, 3, 4)
 
 
+def CHECK_LINEARIZATION_B(B, s: Solution, seed: int | None = None, verbose: bool = True) -> float:
+    """CHECK_LINEARIZATION_B (CHECK_LINEARIZATION_B.jl:20-89): B q against the change of the
+    masked residual (and of the shock speeds with the shock unknowns) when the per-column
+    upstream state moves by q = perturbation_magnitude * randn, both residuals on copies of
+    `s` with a prescribed upstream state. B = (rows, bq, bs) of LINEARIZE_B. Returns (and
+    prints) the reference's measure ||(B q - dq) / (|B q| + 1e-8)|| / sqrt(48 Nchi)."""
+    rows, bq, bs = B
+    c, nchi, N = s._cs, s.nchi, s.N
+    eps = c.perturbation_magnitude
+    rng = np.random.default_rng(seed)
+    P = eps * rng.standard_normal((4, nchi))
+    fs = np.array([c.rho_0, c.rho_u_0, c.rho_v_0, c.rho_E_0])
+    cols0 = np.ascontiguousarray(np.repeat(fs[:, None], nchi, axis=1))
+    st = s.get_state()
+    pts = (st["pts_x"], st["pts_y"], st["pts_chi"], st["pts_eta"])
+    shock_rows = s.operator_size() > 4 * N
+    out = []
+    for cols in (cols0, np.ascontiguousarray(cols0 + P)):
+        x = Solution(s.case)
+        try:
+            x.set_state(np.asarray(st["q"]), *pts, st["cell_idx"], st["t"])
+            x.ctx.check(x.ctx.L.hymor_set_upstream(x.ctx.h, dp(cols.ravel())))
+            from .solver import PDE
+            out.append((PDE(x), x.shock_fields()[1]))
+        finally:
+            x.close()
+    flow = np.tile((np.arange(1, s.neta + 1)[None, :] < st["cell_idx"][:, None]).ravel(order="F"), 4)
+    dq = (out[1][0] - out[0][0]) * flow
+    Bq = np.zeros(4 * N)
+    Bs = np.zeros(nchi)
+    for m in range(nchi):
+        cell = m + (rows[m] - 2) * nchi
+        for d in (-1, 0, 1):
+            n = m + d
+            if 0 <= n < nchi:
+                Bq[np.arange(4) * N + cell] += bq[m, d + 1] @ P[:, n]
+                Bs[m] += bs[m, d + 1] @ P[:, n]
+    if shock_rows:
+        dq = np.concatenate([dq, out[1][1] - out[0][1]])
+        Bq = np.concatenate([Bq, Bs])
+    err = float(np.linalg.norm((Bq - dq) / (np.abs(Bq) + 1e-8)) / np.sqrt(3 * 4 * 4 * nchi))
+    if verbose:
+        print(f"Error of linearization: {err:e} .")
+    return err
+
+
 def LINEARIZE_L_(L: LinearOperatorGPU, s: Solution, w_infty):
     """LINEARIZE_L_ (LINEARIZE_L_.jl:36-71): B on the device and the extended operator L_
     for the frequencies w_infty. Call after LINEARIZE_L. Returns (s, L_)."""

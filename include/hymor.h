@@ -111,6 +111,11 @@ int hymor_get_state(hymor_ctx* ctx, double* q, double* pts_x, double* pts_y, dou
  * like the reference mutates `s` (ghost cells, shocked cells, shock points). Writes
  * the context's flux (read by the CFL dt2 term) and, if flux != NULL, copies it out. */
 int hymor_residual(hymor_ctx* ctx, double* flux);
+/* A prescribed upstream state per column for hymor_residual (the Dict's rho_0_upstream_p
+ * with freestream rho_0_p, rho_u_0_p, rho_v_0_p, rho_E_0_p: 4 x Nchi, COMPUTE_UPSTREAM_
+ * CONDITIONS.jl:87-91), as CHECK_LINEARIZATION_B uses it; NULL restores the freestream.
+ * The RK step never reads it. */
+int hymor_set_upstream(hymor_ctx* ctx, const double* cols);
 /* Sets the context's persistent flux arrays (the Dict's s["flux"]). */
 int hymor_set_flux(hymor_ctx* ctx, const double* flux);
 

@@ -180,3 +180,30 @@ def test_freestream_receptivity_vs_eigsh(require_gpu):
     assert np.allclose(np.sort(G)[::-1], lam, rtol=1e-6, atol=0)
     assert info["converged"] and V.shape == (Lr.n, 2)
     assert np.all(V[:4 * N] == 0)
+
+
+@pytest.mark.gpu
+def test_residual_with_upstream_state(require_gpu):
+    """hymor_set_upstream: the residual with a prescribed per-column upstream state against
+    the oracle's (rho_0_upstream_p), to 1e-12 of the flux scale; and the device B passes
+    the reference's CHECK_LINEARIZATION_B measure (< 1e-3)."""
+    from hymor_gb300 import receptivity as R
+    from hymor_gb300 import solver as S
+    from hymor_gb300._lib import dp
+    from helpers import residual_rel
+    cfg, cs, sol, orc, L, co = _gpu_case()
+    st = sol.get_state()
+    fs = np.array([orc.cs.rho_0, orc.cs.rho_u_0, orc.cs.rho_v_0, orc.cs.rho_E_0])
+    cols = np.ascontiguousarray(fs[:, None] * (1 + 1e-3 * np.random.Generator(np.random.PCG64(9)).standard_normal(
+        (4, cfg.nchi))))
+    pts = (st["pts_x"], st["pts_y"], st["pts_chi"], st["pts_eta"])
+    o = O.Oracle(cs)
+    o.set_state(st["q"], *pts, st["cell_idx"], st["t"])
+    o.set_upstream(cols)
+    s2 = S.Solution(cs)
+    s2.set_state(np.asarray(st["q"]), *pts, st["cell_idx"], st["t"])
+    s2.ctx.check(s2.ctx.L.hymor_set_upstream(s2.ctx.h, dp(cols.ravel())))
+    assert max(residual_rel(S.PDE(s2), o.residual(), cs)) < 1e-12
+    s2.close()
+    err = R.CHECK_LINEARIZATION_B(R.LINEARIZE_B(sol), sol, seed=3, verbose=False)
+    assert err < 1e-3
