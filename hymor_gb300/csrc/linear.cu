@@ -863,6 +863,30 @@ void launch_recept_apply(const DevCtx& d, int k, int nw, const double* dw, const
   k_recept_mv<<<grid_for(items, 256), 256, 0, st>>>(a);
 }
 
+// Runs `step` (the launches of one Taylor step, the same every step) nsteps times: captured
+// once into a CUDA graph and replayed, so that the dozen small launches of a step cost one
+// graph launch; launched directly when the stream is already being captured by the caller
+// or the capture fails.
+template <class Step>
+static void repeat_steps(int nsteps, cudaStream_t st, Step step) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t ge = nullptr;
+  if (nsteps > 1 && cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone &&
+      cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    step();
+    if (cudaStreamEndCapture(st, &g) == cudaSuccess && g && cudaGraphInstantiate(&ge, g, 0) == cudaSuccess) {
+      for (int s = 0; s < nsteps; ++s) cudaGraphLaunch(ge, st);
+      cudaGraphExecDestroy(ge);
+      cudaGraphDestroy(g);
+      return;
+    }
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();  // a failed capture leaves nothing launched: run the steps directly
+  }
+  for (int s = 0; s < nsteps; ++s) step();
+}
+
 // EXPONENTIAL! (Transient_growth_downstream/CONSTRUCT_C.jl:78-111) with L_: per step term =
 // vout, then term = (L_ dt) term / j and vout += term for j = 1..order. work: 2 x 2k x ld.
 void launch_recept_expm(const DevCtx& d, int k, int nw, const double* dw, double dt, int nsteps, int order,
@@ -871,7 +895,7 @@ void launch_recept_expm(const DevCtx& d, int k, int nw, const double* dw, double
   double* term = work;
   double* t2 = work + n;
   k_copy<<<grid_for(n, 256), 256, 0, st>>>(X, Y, n);
-  for (int s = 0; s < nsteps; ++s) {
+  repeat_steps(nsteps, st, [&]() {
     k_copy<<<grid_for(n, 256), 256, 0, st>>>(Y, term, n);
     double* src = term;
     double* dst = t2;
@@ -880,7 +904,7 @@ void launch_recept_expm(const DevCtx& d, int k, int nw, const double* dw, double
       k_scale_acc<<<grid_for(n, 256), 256, 0, st>>>(dst, Y, 1.0 / (double)j, n);
       std::swap(src, dst);
     }
-  }
+  });
 }
 
 // POWER_METHOD! (Eigenvalues/ARNOLDI_POWER_GPU.jl:64-82): per step vout = v,
@@ -891,7 +915,7 @@ static void launch_expm_body(const DevCtx& d, int k, double dt, int nsteps, int 
   const long n = op_size(d) * (long)k;
   if (d.sj.on) {
     // with the shock blocks every term is a full operator application, then vout += term / j!
-    for (int s = 0; s < nsteps; ++s) {
+    repeat_steps(nsteps, st, [&]() {
       const double* src = v;
       long fact = 1;
       for (int j = 1; j <= order; ++j) {
@@ -902,7 +926,7 @@ static void launch_expm_body(const DevCtx& d, int k, double dt, int nsteps, int 
         src = dst;
       }
       k_copy<<<grid_for(n, 256), 256, 0, st>>>(vout, v, n);
-    }
+    });
     return;
   }
   const long items = mv_items(d.N, k, d.sms);
