@@ -62,9 +62,9 @@ def test_linearize_b_consistency():
 # GPU, through the C ABI
 
 
-def _gpu_case(nchi=24, neta=20, steps=20):
+def _gpu_case(nchi=24, neta=20, steps=20, cone=False):
     from hymor_gb300 import solver as S
-    cfg = C.cylinder_config(nchi, neta)
+    cfg = (C.blunt_cone_config if cone else C.cylinder_config)(nchi, neta)
     cs = C.initial_state(cfg)
     sol, orc = S.Solution(cs), O.Oracle(cs)
     S.ADVECT_FLOW(sol, steps)
@@ -110,11 +110,13 @@ def _exponential(A, x, dt, n_t, order=5):
 
 
 @pytest.mark.gpu
-def test_b_parity(require_gpu):
+@pytest.mark.parametrize("cone", [False, True])
+def test_b_parity(require_gpu, cone):
     """The device's LINEARIZE_B against the oracle's (finite differences with eps = 1e-8 of
-    residuals that agree to ~1e-13: agreement to the FD rounding)."""
+    residuals that agree to ~1e-13: agreement to the FD rounding), on the cylinder and the
+    axisymmetric sphere-cone."""
     from hymor_gb300 import receptivity as R
-    cfg, cs, sol, orc, L, co = _gpu_case()
+    cfg, cs, sol, orc, L, co = _gpu_case(48, 24, steps=5, cone=True) if cone else _gpu_case()
     rows, bq, bs = R.LINEARIZE_B(sol)
     rows_o, bq_o, bs_o = orc.linearize_b()
     assert np.array_equal(rows, rows_o)

@@ -98,9 +98,10 @@ def test_shock_operator_adjoint_identity():
 # GPU, through the C ABI
 
 
-def _gpu_case(nchi=30, neta=24, steps=5):
+def _gpu_case(nchi=30, neta=24, steps=5, cone=False):
     from hymor_gb300 import solver as S
-    cfg = C.cylinder_config(nchi, neta, perturb_shock=True)
+    make = C.blunt_cone_config if cone else C.cylinder_config
+    cfg = make(nchi, neta, perturb_shock=True)
     cs = C.initial_state(cfg)
     sol, orc = S.Solution(cs), O.Oracle(cs)
     S.ADVECT_FLOW(sol, steps)
@@ -112,11 +113,13 @@ def _gpu_case(nchi=30, neta=24, steps=5):
 
 
 @pytest.mark.gpu
-def test_shock_blocks_parity(require_gpu):
-    """The device's shock blocks against the oracle's per-point restatement. Entries are
-    finite differences with eps = 1e-8 of residuals that agree to ~1e-13, so they agree to
-    the FD rounding, as the A11 blocks do."""
-    cfg, cs, sol, orc, L, co, ob = _gpu_case()
+@pytest.mark.parametrize("cone", [False, True])
+def test_shock_blocks_parity(require_gpu, cone):
+    """The device's shock blocks against the oracle's per-point restatement, on the
+    cylinder and the axisymmetric sphere-cone (shocked rows varying between columns).
+    Entries are finite differences with eps = 1e-8 of residuals that agree to ~1e-13, so
+    they agree to the FD rounding, as the A11 blocks do."""
+    cfg, cs, sol, orc, L, co, ob = _gpu_case(48, 24, cone=True) if cone else _gpu_case()
     assert L.n == 4 * cfg.nchi * cfg.neta + cfg.nchi
     rows, a21, a12, a22 = L.shock_blocks()
     assert np.array_equal(rows, ob[0])
