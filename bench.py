@@ -251,7 +251,49 @@ def matvec_numbers(sol, cs, fp64_peak_tflops: float, hbm_gbs: float, cpu: bool, 
                                "sample": f"{nv} vectors through the oracle's stencil matvec"}
     del dX, dY
     out["propagator"] = propagator_numbers(fp64_peak_tflops)
+    try:
+        out["shock_unknowns"] = extended_numbers(cs)
+    except Exception as e:  # reported, never fatal to the bench line
+        out["shock_unknowns"] = {"error": str(e)}
     return out
+
+
+def extended_numbers(cs, reps: int = 10):
+    """The same 800 x 400 case linearised with the shock-position unknowns (perturb_shock):
+    the device assembly (36 + 8 + Nchi residuals, host clock), the matvec on one vector of
+    4N + Nchi unknowns forward and transposed (device time, CUDA events), and LINEARIZE_B
+    (13 residuals, host clock)."""
+    import dataclasses
+    import torch
+    from hymor_gb300 import solver as S
+    case = dataclasses.replace(cs, cfg=dataclasses.replace(cs.cfg, perturb_shock=True))
+    sol = S.Solution(case)
+    try:
+        S.ADVECT_FLOW(sol, 20)
+        L, h = sol.ctx.L, sol.ctx.h
+        sol.ctx.check(L.hymor_linearize(h))  # warm-up
+        t0 = time.perf_counter()
+        sol.ctx.check(L.hymor_linearize(h))
+        asm = time.perf_counter() - t0
+        n = sol.operator_size()
+        x = torch.from_numpy(np.random.Generator(np.random.PCG64(2)).standard_normal(n)).cuda()
+        y = torch.empty_like(x)
+        torch.cuda.synchronize()
+        xp, yp = ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(y.data_ptr())
+        ms = ctypes.c_float()
+        res = {"workload": f"perturb_shock, {NCHI}x{NETA}: {n} unknowns", "assembly_s": asm}
+        for tr, key in ((0, "matvec_ms"), (1, "transpose_matvec_ms")):
+            sol.ctx.check(L.hymor_bench_matvec(h, 1, xp, yp, tr, 0, 1, ctypes.byref(ms)))
+            sol.ctx.check(L.hymor_bench_matvec(h, 1, xp, yp, tr, 0, reps, ctypes.byref(ms)))
+            res[key] = ms.value / reps
+        sol.ctx.check(L.hymor_linearize_b(h))  # warm-up
+        t0 = time.perf_counter()
+        sol.ctx.check(L.hymor_linearize_b(h))
+        res["linearize_b_ms"] = (time.perf_counter() - t0) * 1e3
+        del x, y
+        return res
+    finally:
+        sol.close()
 
 
 def propagator_numbers(fp64_peak_tflops: float, nchi: int = 100, neta: int = 80, k: int = 64,
