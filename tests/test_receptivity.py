@@ -209,3 +209,56 @@ def test_residual_with_upstream_state(require_gpu):
     s2.close()
     err = R.CHECK_LINEARIZATION_B(R.LINEARIZE_B(sol), sol, seed=3, verbose=False)
     assert err < 1e-3
+
+
+@pytest.mark.gpu
+def test_receptivity_operator_with_shock_unknowns(require_gpu):
+    """L_ with the shock-position unknowns (perturb_shock): the downstream part is the
+    extended operator [A11 A12; A21 A22] and B has speed rows; apply and adjoint against the
+    sparse restatement from the device's own blocks, 1e-12."""
+    import scipy.sparse as sp
+    from hymor_gb300 import receptivity as R
+    from hymor_gb300 import solver as S
+    cfg = C.cylinder_config(24, 20, perturb_shock=True)
+    cs = C.initial_state(cfg)
+    sol = S.Solution(cs)
+    S.ADVECT_FLOW(sol, 5)
+    _, L = S.LINEARIZE_L(sol)
+    w = [0.0, 3.0]
+    _, Lr = R.LINEARIZE_L_(L, sol, w)
+    rows_b, bq, bs = R.LINEARIZE_B(sol)
+    rows, a21, a12, a22 = L.shock_blocks()
+    nchi, N = cfg.nchi, cfg.nchi * cfg.neta
+    n_down = 4 * N + nchi
+    assert Lr.n == n_down + len(w) * 4 * nchi
+    A11 = O.stencil_to_csr(cfg, L.blocks())
+    r, c, v = [], [], []
+    for i in range(nchi):
+        for vv in range(4):
+            for p in range(nchi):
+                r.append(vv * N + i + (rows[i] - 2) * nchi); c.append(4 * N + p); v.append(a12[vv * nchi + i, p])
+            for j in (1, 2):
+                r.append(4 * N + i); c.append(vv * N + i + (rows[i] - 1 - j) * nchi); v.append(a21[i, (j - 1) * 4 + vv])
+        for p in range(nchi):
+            r.append(4 * N + i); c.append(4 * N + p); v.append(a22[i, p])
+    Ld = sp.csr_matrix((v, (r, c)), shape=(n_down, n_down)) + sp.block_diag([A11, sp.csr_matrix((nchi, nchi))])
+    r, c, v = [], [], []
+    for m in range(nchi):
+        cell = m + (rows_b[m] - 2) * nchi
+        for d in (-1, 0, 1):
+            n = m + d
+            if 0 <= n < nchi:
+                for vi in range(4):
+                    for vo in range(4):
+                        r.append(vo * N + cell); c.append(vi * nchi + n); v.append(bq[m, d + 1, vo, vi])
+                    r.append(4 * N + m); c.append(vi * nchi + n); v.append(bs[m, d + 1, vi])
+    B = sp.csr_matrix((v, (r, c)), shape=(n_down, 4 * nchi))
+    p4 = 4 * nchi
+    A = sp.vstack([sp.hstack([Ld] + [B] * len(w)),
+                   sp.hstack([sp.csr_matrix((len(w) * p4, n_down)),
+                              sp.kron(sp.diags(-1j * np.asarray(w)), sp.eye(p4))])]).tocsr().astype(complex)
+    rng = np.random.Generator(np.random.PCG64(7))
+    x = rng.standard_normal(Lr.n) + 1j * rng.standard_normal(Lr.n)
+    for adj, M in ((False, A), (True, A.conj().T.tocsr())):
+        ref = M @ x
+        assert np.max(np.abs(Lr.apply(x, adjoint=adj) - ref)) <= 1e-12 * np.max(np.abs(ref))
