@@ -15,7 +15,14 @@ of four kinds, each recorded with where it comes from:
 - oracle_*.npz: outputs of the C++ restatement (oracle/) for small seeded cases:
   the residual (PDE) and the state after ten RK4 steps (ADVECT_FLOW). These are
   regression vectors: they pin the oracle and the CUDA path to the outputs the
-  oracle produced when the fixtures were made.
+  oracle produced when the fixtures were made;
+- oracle_linear_cylinder_24x20.npz: the oracle's finite-difference operators that
+  the reference assembles beside the stencil Jacobian, on the 24 x 20 cylinder after
+  five RK4 steps: the shock-position blocks of perturb_shock
+  (LINEARIZE_EQUATIONS_NO_DISCONTINUITY.jl:140-274) and the upstream-boundary operator B
+  (LINEARIZE_B.jl:40-296). Regression vectors as well.
+
+Each part can be made on its own: python tests/golden/make_golden.py linear
 """
 from __future__ import annotations
 
@@ -88,8 +95,29 @@ def oracle_fixtures():
                             pts_x=st["pts_x"], pts_y=st["pts_y"], cell_idx=st["cell_idx"], steps=steps)
 
 
+def linear_fixture():
+    from hymor_gb300 import case as C
+    from oracle import oracle as O
+
+    cfg = C.cylinder_config(24, 20, perturb_shock=True)
+    cs = C.initial_state(cfg, seed=1, noise=1e-6)
+    o = O.Oracle(cs)
+    o.advect(5)
+    o.linearize()
+    rows, a21f, a12, a22 = o.shock_blocks()
+    brows, bq, bs = o.linearize_b()
+    np.savez_compressed(os.path.join(HERE, "oracle_linear_cylinder_24x20.npz"), steps=5, rows=rows,
+                        a21=O.compact_a21(rows, a21f), a12=a12, a22=a22, b_rows=brows, bq=bq, bs=bs)
+
+
 if __name__ == "__main__":
-    spline_fixture()
-    known_answers()
-    oracle_fixtures()
+    parts = sys.argv[1:] or ["spline", "known", "oracle", "linear"]
+    if "spline" in parts:
+        spline_fixture()
+    if "known" in parts:
+        known_answers()
+    if "oracle" in parts:
+        oracle_fixtures()
+    if "linear" in parts:
+        linear_fixture()
     print("fixtures written to", HERE)

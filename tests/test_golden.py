@@ -78,3 +78,42 @@ def test_cuda_path_reproduces_fixtures(require_gpu, stem):
     assert rel_err(st["pts_x"], g["pts_x"]) < STATE_TOL
     assert abs(st["t"] - float(g["t"])) < 1e-13 * max(1.0, abs(float(g["t"])))
     sol.close()
+
+
+def _linear_case():
+    g = np.load(os.path.join(GOLDEN, "oracle_linear_cylinder_24x20.npz"))
+    cs = C.initial_state(C.cylinder_config(24, 20, perturb_shock=True), seed=1, noise=1e-6)
+    return cs, int(g["steps"]), g
+
+
+def test_oracle_reproduces_linear_fixture():
+    """The oracle's shock-position blocks and upstream-boundary operator B against the
+    stored ones (finite differences: 1e-9 of each block's scale)."""
+    cs, steps, g = _linear_case()
+    o = O.Oracle(cs)
+    o.advect(steps)
+    o.linearize()
+    rows, a21f, a12, a22 = o.shock_blocks()
+    brows, bq, bs = o.linearize_b()
+    assert np.array_equal(rows, g["rows"]) and np.array_equal(brows, g["b_rows"])
+    for got, key in ((O.compact_a21(rows, a21f), "a21"), (a12, "a12"), (a22, "a22"), (bq, "bq"), (bs, "bs")):
+        assert rel_err(got, g[key]) < 1e-9, key
+
+
+@pytest.mark.gpu
+def test_cuda_path_reproduces_linear_fixture(require_gpu):
+    """The device's shock-position blocks and B against the stored vectors (1e-5, the FD
+    agreement of the device and the oracle)."""
+    from hymor_gb300 import receptivity as R
+    from hymor_gb300 import solver as S
+
+    cs, steps, g = _linear_case()
+    sol = S.Solution(cs)
+    S.ADVECT_FLOW(sol, steps)
+    _, L = S.LINEARIZE_L(sol)
+    rows, a21, a12, a22 = L.shock_blocks()
+    brows, bq, bs = R.LINEARIZE_B(sol)
+    assert np.array_equal(rows, g["rows"]) and np.array_equal(brows, g["b_rows"])
+    for got, key in ((a21, "a21"), (a12, "a12"), (a22, "a22"), (bq, "bq"), (bs, "bs")):
+        assert rel_err(got, g[key]) < 1e-5, key
+    sol.close()
