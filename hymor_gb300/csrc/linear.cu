@@ -1012,11 +1012,15 @@ void launch_shock_assemble(DevCtx& d, const double* const Fb[4], double* const F
   }
   pa.var = -1;
   pa.shock_row = 0;
+  // only the flux of the cells (i, sc_i - 1) is read: the tiles whose halo the shock and
+  // boundary kernels write (class 1 of the step's tile lists) hold them all, and compute
+  // them with the same per-cell arithmetic as the whole grid
+  launch_classify_tiles(d, st);
   for (int p = 0; p < nchi; ++p) {
     k_perturb_thermo<<<grid_for(d.G, 256), 256, 0, st>>>(pa);
     k_perturb_point<<<cb, 128, 0, st>>>(d.Sp, d.Yp, d.sj.dir, nchi, p, eps);
     launch_shock_bc_flags(d, false, false, true, true, 0, st);
-    launch_flux(d, false, Fp, st);
+    launch_flux_class(d, false, Fp, 1, st);
     k_gather_a12<<<cb, 128, 0, st>>>(fp, fb, d.rel, d.sj.rel_b, d.sj.rows, d.sj.a12, d.sj.a22, nchi, p, eps);
   }
   k_transpose<<<grid_for(4L * nchi * nchi, 256), 256, 0, st>>>(d.sj.a12, d.sj.a12t, 4L * nchi, nchi);
