@@ -262,3 +262,19 @@ def test_receptivity_operator_with_shock_unknowns(require_gpu):
     for adj, M in ((False, A), (True, A.conj().T.tocsr())):
         ref = M @ x
         assert np.max(np.abs(Lr.apply(x, adjoint=adj) - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+def test_linearize_b_axisymmetric_first_column():
+    """On an axisymmetric case the reference zeroes rho_v of the first column's upstream
+    state (COMPUTE_UPSTREAM_CONDITIONS.jl:105-108), so B has no entries for that input;
+    the other inputs of the first column act."""
+    cfg = C.blunt_cone_config(48, 24)
+    cs = C.initial_state(cfg)
+    orc = O.Oracle(cs)
+    orc.advect(2)
+    orc.linearize()
+    rows, bq, bs = orc.linearize_b()
+    # input column n = 0 is reached from output columns m = 0 (d = 0) and m = 1 (d = -1)
+    assert np.all(bq[0, 1, :, 2] == 0) and np.all(bq[1, 0, :, 2] == 0)
+    assert np.all(bs[0, 1, 2] == 0) and np.all(bs[1, 0, 2] == 0)
+    assert np.max(np.abs(bq[0, 1, :, 0])) > 0 and np.max(np.abs(bq[2, 1, :, 2])) > 0
