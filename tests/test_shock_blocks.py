@@ -11,8 +11,8 @@ from oracle import oracle as O
 from helpers import rel_err
 
 
-def _oracle_case(nchi=30, neta=24, steps=5):
-    cfg = C.cylinder_config(nchi, neta, perturb_shock=True)
+def _oracle_case(nchi=30, neta=24, steps=5, **kw):
+    cfg = C.cylinder_config(nchi, neta, perturb_shock=True, **kw)
     cs = C.initial_state(cfg)
     orc = O.Oracle(cs)
     orc.advect(steps)
@@ -60,12 +60,14 @@ def test_a21_is_column_local():
     assert np.all(rows == orc.get_state()["cell_idx"])
 
 
-def test_shock_linearization_consistency():
+@pytest.mark.parametrize("spline_param", [None, 1.0])
+def test_shock_linearization_consistency(spline_param):
     """CHECK_LINEARIZATION_L with the shock unknowns: [A11 A12; A21 A22] [q; r] matches the
     change of the masked residual and of the shock speeds when the cells move by q and the
-    shock points by r along their normals. Without A12 the flux response misses the shock's
-    share by orders of magnitude more."""
-    cfg, cs, orc, co = _oracle_case()
+    shock points by r along their normals, with the smoothing spline (A21 one cell per
+    residual) and without it (spline_param = 1: all columns at once, :207-258). Without A12
+    the flux response misses the shock's share by orders of magnitude more."""
+    cfg, cs, orc, co = _oracle_case(**({} if spline_param is None else {"spline_param": spline_param}))
     rows, a21f, a12, a22 = orc.shock_blocks()
     blocks = (rows, O.compact_a21(rows, a21f), a12, a22)
     n, N = cfg.nchi, cfg.nchi * cfg.neta
