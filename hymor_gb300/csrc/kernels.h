@@ -116,7 +116,9 @@ void launch_jacobian_assemble(DevCtx& d, cudaStream_t st);
 void launch_b_assemble(DevCtx& d, cudaStream_t st);
 void launch_matvec(const DevCtx& d, int k, const double* X, double* Y, int transpose, double scale,
                    cudaStream_t st, long ld = 0);
+// graph_ok: with the shock blocks, the Taylor steps may be captured once into a CUDA graph
+// and replayed (false: every step is launched directly, nothing is instantiated).
 void launch_expm(const DevCtx& d, int k, double dt, int nsteps, int order, const double* X,
-                 double* Y, int transpose, double* work, cudaStream_t st);
+                 double* Y, int transpose, double* work, cudaStream_t st, bool graph_ok = true);
 
 }  // namespace hymor

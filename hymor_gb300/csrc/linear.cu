@@ -867,12 +867,13 @@ void launch_recept_apply(const DevCtx& d, int k, int nw, const double* dw, const
 // once into a CUDA graph and replayed, so that the dozen small launches of a step cost one
 // graph launch; launched directly when the stream is already being captured by the caller
 // or the capture fails.
+// graph_ok false: always launch directly (the allocation-free propagator builds no graph).
 template <class Step>
-static void repeat_steps(int nsteps, cudaStream_t st, Step step) {
+static void repeat_steps(int nsteps, cudaStream_t st, Step step, bool graph_ok = true) {
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   cudaGraph_t g = nullptr;
   cudaGraphExec_t ge = nullptr;
-  if (nsteps > 1 && cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone &&
+  if (graph_ok && nsteps > 1 && cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone &&
       cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
     step();
     if (cudaStreamEndCapture(st, &g) == cudaSuccess && g && cudaGraphInstantiate(&ge, g, 0) == cudaSuccess) {
@@ -911,7 +912,7 @@ void launch_recept_expm(const DevCtx& d, int k, int nw, const double* dw, double
 // term_j = (A dt) term_{j-1}, vout += term_j / j!, v = vout. The body assumes v and vout
 // already hold the input.
 static void launch_expm_body(const DevCtx& d, int k, double dt, int nsteps, int order, double* v, double* t1,
-                             double* t2, double* vout, int transpose, cudaStream_t st) {
+                             double* t2, double* vout, int transpose, cudaStream_t st, bool graph_ok) {
   const long n = op_size(d) * (long)k;
   if (d.sj.on) {
     // with the shock blocks every term is a full operator application, then vout += term / j!
@@ -926,7 +927,7 @@ static void launch_expm_body(const DevCtx& d, int k, double dt, int nsteps, int 
         src = dst;
       }
       k_copy<<<grid_for(n, 256), 256, 0, st>>>(vout, v, n);
-    });
+    }, graph_ok);
     return;
   }
   const long items = mv_items(d.N, k, d.sms);
@@ -968,14 +969,14 @@ static void launch_expm_body(const DevCtx& d, int k, double dt, int nsteps, int 
 }
 
 void launch_expm(const DevCtx& d, int k, double dt, int nsteps, int order, const double* X, double* Yout,
-                 int transpose, double* work, cudaStream_t st) {
+                 int transpose, double* work, cudaStream_t st, bool graph_ok) {
   const long n = op_size(d) * (long)k;
   double* v = work;
   double* t1 = work + n;
   double* t2 = work + 2 * n;
   k_copy<<<grid_for(n, 256), 256, 0, st>>>(X, v, n);
   k_copy<<<grid_for(n, 256), 256, 0, st>>>(X, Yout, n);
-  launch_expm_body(d, k, dt, nsteps, order, v, t1, t2, Yout, transpose, st);
+  launch_expm_body(d, k, dt, nsteps, order, v, t1, t2, Yout, transpose, st, graph_ok);
 }
 
 // The shock-position blocks (perturb_shock), after the A11 assembly has left the base

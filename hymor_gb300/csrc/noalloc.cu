@@ -1,12 +1,13 @@
 // Allocation-free variant of the Taylor propagator (hymor_expm_apply_dev).
 //
-// Who needs it: callers that must not allocate device memory while they run, for
-// example a host framework that invokes this library from inside its own CUDA
-// stream capture (where cudaMalloc is not allowed), or a service that reserves its
-// whole device-memory budget at start-up and treats any allocation during a solve
-// as a failure. hymor_expm_apply_dev allocates its three work vectors on every
-// call; this entry point takes them from one fixed, file-scope device array
-// instead, so the call itself never allocates or frees.
+// Who needs it: callers that cannot call cudaMalloc while they run, for example a
+// service that reserves its whole device-memory budget at start-up and treats any
+// allocation during a solve as a failure, or a host runtime whose own pool allocator
+// owns the device memory and must not see a second allocator take from it.
+// hymor_expm_apply_dev allocates work vectors (and, with the shock-position unknowns,
+// instantiates a CUDA graph of one Taylor step); this entry point takes its work
+// vectors from one fixed, file-scope device array and launches every Taylor step
+// directly, so the call itself allocates nothing.
 //
 // Limits and sharing rules:
 //   * the array holds 3 x kNoAllocVec doubles (24 MiB) and is held by every GPU
@@ -21,9 +22,13 @@
 //     contexts on the same device, other host threads) race on the array: serialise
 //     them;
 //   * the device address of the array is looked up once per device, on the first
-//     call made with that device current (cudaGetSymbolAddress). Make that first
-//     call before any stream capture.
+//     call for a context on that device (cudaGetSymbolAddress, with the context's
+//     device made current first). Make that first call before any stream capture.
+//     The lookup is guarded by a mutex, so first calls from several host threads are
+//     safe.
+#include <atomic>
 #include <cstdio>
+#include <mutex>
 
 #include "kernels.h"
 
@@ -31,6 +36,7 @@ namespace hymor {
 DevCtx& ctx_dev(hymor_ctx* c);
 cudaStream_t ctx_stream(hymor_ctx* c);
 int ctx_fail(hymor_ctx* c, int code, const char* msg);
+int ctx_select_device(hymor_ctx* c);
 }  // namespace hymor
 
 using namespace hymor;
@@ -42,24 +48,32 @@ constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) double g_expm_scratch[3 * kNoAllocVec];
 
-// device address of g_expm_scratch, per device (nullptr until the first call there)
-double* g_scratch_addr[kMaxDevices] = {};
+// device address of g_expm_scratch, per device (null until the first call there)
+std::atomic<double*> g_scratch_addr[kMaxDevices];
+std::mutex g_scratch_mu;
 
-int scratch_for_current_device(hymor_ctx* ctx, double** out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
-    return ctx_fail(ctx, HYMOR_ERR_CUDA, "no current CUDA device for the allocation-free propagator");
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_expm_scratch);
-    if (e != cudaSuccess || !p) {
-      char msg[256];
-      snprintf(msg, sizeof msg, "cudaGetSymbolAddress of the propagator scratch failed: %s", cudaGetErrorString(e));
-      return ctx_fail(ctx, HYMOR_ERR_CUDA, msg);
+// Makes the context's device current and returns the array's address on it.
+int scratch_for_ctx_device(hymor_ctx* ctx, double** out) {
+  int dev = -1;
+  if (ctx_select_device(ctx) || cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+    return ctx_fail(ctx, HYMOR_ERR_CUDA, "cannot make the context's device current for the allocation-free propagator");
+  double* p = g_scratch_addr[dev].load(std::memory_order_acquire);
+  if (!p) {
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    p = g_scratch_addr[dev].load(std::memory_order_relaxed);
+    if (!p) {
+      void* a = nullptr;
+      const cudaError_t e = cudaGetSymbolAddress(&a, g_expm_scratch);
+      if (e != cudaSuccess || !a) {
+        char msg[256];
+        snprintf(msg, sizeof msg, "cudaGetSymbolAddress of the propagator scratch failed: %s", cudaGetErrorString(e));
+        return ctx_fail(ctx, HYMOR_ERR_CUDA, msg);
+      }
+      p = static_cast<double*>(a);
+      g_scratch_addr[dev].store(p, std::memory_order_release);
     }
-    g_scratch_addr[dev] = static_cast<double*>(p);
   }
-  *out = g_scratch_addr[dev];
+  *out = p;
   return 0;
 }
 
@@ -80,10 +94,11 @@ extern "C" int hymor_expm_apply_dev_noalloc(hymor_ctx* ctx, int k, double dt, in
     return ctx_fail(ctx, HYMOR_ERR_INVALID, msg);
   }
   double* work = nullptr;
-  int r = scratch_for_current_device(ctx, &work);
+  int r = scratch_for_ctx_device(ctx, &work);
   if (r) return r;
-  // launch_expm uses work[0, 3n): v, and the two alternating Taylor terms
-  launch_expm(d, k, dt, nsteps, order, dX, dY, transpose, work, ctx_stream(ctx));
+  // launch_expm uses work[0, 3n): v, and the two alternating Taylor terms; every Taylor
+  // step is launched directly (graph_ok false), also with the shock-position blocks
+  launch_expm(d, k, dt, nsteps, order, dX, dY, transpose, work, ctx_stream(ctx), false);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return ctx_fail(ctx, HYMOR_ERR_CUDA, cudaGetErrorString(e));
   return 0;

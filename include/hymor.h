@@ -2,7 +2,7 @@
  * hymor.h — C ABI of the GB300-native HYMOR hot path (libhymor.so).
  *
  * The reference (AdrianAA00/HYMOR) is Julia; its hot path is the Julia API
- * below, which a Julia host binds with `ccall` (see INTEGRATION.md). Every entry
+ * below, which a Julia host binds with `ccall`. Every entry
  * point returns 0 on success or a negative HYMOR_ERR_* code; hymor_last_error()
  * gives the message. Arrays use the reference layout: column-major with chi (i)
  * fastest; conserved variables are ghosted (Nchi+2) x (Neta+2) and stored back
@@ -224,14 +224,18 @@ int hymor_expm_apply_dev(hymor_ctx* ctx, int k, double dt, int nsteps, int order
 int hymor_expm_apply_multi_dev(hymor_ctx* ctx, int k, const double* dts, const int32_t* nsteps, int order,
                                const double* dX, double* dY, int transpose);
 
-/* Allocation-free variant of hymor_expm_apply_dev (no counterpart in the reference). For
- * callers that must not allocate device memory during the call, e.g. code running
- * inside the caller's own stream capture, or a service with a fixed device-memory budget.
- * The work vectors come from one fixed 24 MiB device array instead of per-call
- * allocations: requires 4*Nchi*Neta*k <= 1048576 (else HYMOR_ERR_INVALID). All calls
- * share that array, so calls whose GPU work overlaps race; nothing in it needs to start
- * at zero. The first call on a device looks up the array's address: make it before any
- * stream capture. With the shock unknowns the limit is hymor_operator_size * k <= 1048576. */
+/* Allocation-free variant of hymor_expm_apply_dev. It has no counterpart in the reference.
+ * For callers that cannot call cudaMalloc during a solve: a service that reserves its whole
+ * device-memory budget at start-up and treats any later allocation as a failure, or a host
+ * runtime whose own pool allocator owns the device memory. hymor_expm_apply_dev allocates
+ * work vectors per call (and, with the shock unknowns, instantiates a CUDA graph of one
+ * Taylor step); this variant takes its work vectors from one fixed 24 MiB device array that
+ * every GPU loading the library holds until exit, and launches every Taylor step directly.
+ * Requires hymor_operator_size * k <= 1048576 (else HYMOR_ERR_INVALID, before any device
+ * work). All calls share the array and it keeps the last call's contents (nothing in it
+ * needs to start at zero): calls whose GPU work overlaps race, so serialise them. The first
+ * call for a context on a device makes that device current and looks up the array's
+ * address there: make that first call before any stream capture. */
 int hymor_expm_apply_dev_noalloc(hymor_ctx* ctx, int k, double dt, int nsteps, int order,
                                  const double* dX, double* dY, int transpose);
 
