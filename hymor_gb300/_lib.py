@@ -37,8 +37,16 @@ EXPORTS = [
     "hymor_profile_phases", "hymor_advect", "hymor_bench_matvec", "hymor_operator_size",
     "hymor_shock_blocks_get", "hymor_shock_blocks_set", "hymor_shock_fields", "hymor_block4_apply_ext_dev",
     "hymor_expm_apply_multi_dev", "hymor_linearize_b", "hymor_b_get", "hymor_b_set", "hymor_recept_size",
-    "hymor_recept_apply_dev", "hymor_recept_expm_dev", "hymor_set_upstream",
+    "hymor_recept_apply_dev", "hymor_recept_expm_dev", "hymor_set_upstream", "hymor_eigs", "hymor_tg_gain",
+    "hymor_dense_schur", "hymor_dense_symeig",
 ]
+
+
+class KrylovOpts(ctypes.Structure):
+    """hymor_krylov_opts (include/hymor.h)."""
+    _fields_ = [("nev", ctypes.c_int32), ("ncv", ctypes.c_int32), ("maxit", ctypes.c_int32),
+                ("block", ctypes.c_int32), ("order", ctypes.c_int32), ("flow_start", ctypes.c_int32),
+                ("seed", ctypes.c_uint64), ("tol", ctypes.c_double)]
 
 
 class HymorError(RuntimeError):
@@ -113,6 +121,10 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "hymor_recept_size": [vp, i, ctypes.POINTER(ctypes.c_int64)],
         "hymor_recept_apply_dev": [vp, i, i, dp, d, vp, vp, i],
         "hymor_recept_expm_dev": [vp, i, i, dp, d, i, i, vp, vp, i],
+        "hymor_eigs": [vp, vp, d, i, dp, dp, dp, dp, ip, vp],
+        "hymor_tg_gain": [vp, vp, i, dp, dp, dp, dp, ip, dp, ip, vp],
+        "hymor_dense_schur": [i, dp, i, dp, dp, dp, dp, ip],
+        "hymor_dense_symeig": [i, dp, dp, dp],
     }
     for name, args in sig.items():
         f = getattr(L, name)

@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libhymor.so")
-SOURCES = ["core.cu", "linear.cu", "api.cu", "noalloc.cu", "peak.cu"]
+SOURCES = ["core.cu", "linear.cu", "api.cu", "noalloc.cu", "peak.cu", "krylov.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xptxas", "-v"]

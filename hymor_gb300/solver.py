@@ -143,6 +143,60 @@ def RUN_SIMULATION(s: Solution, N_iter: int) -> Solution:
     return ADVECT_FLOW(s, N_iter)
 
 
+def RESIDUAL(s: Solution, q_save: np.ndarray, cell_idx: np.ndarray | None = None) -> np.ndarray:
+    """RESIDUAL of the MATLAB twin (utils/Time_marching/ADVECT_FLOW_EXPLICIT.m:92-110): per
+    conserved variable, rms of the change since q_save over the flow cells divided by the rms
+    of the variable there (interior cells; flow cells j < cell_idx[i] with shock fitting).
+    q_save is a state as Solution.get_state()["q"] returns it."""
+    st = s.get_state()
+    shape = (s.nchi + 2, s.neta + 2)
+    qa = st["q"].reshape(4, -1)
+    qb = np.asarray(q_save).reshape(4, -1)
+    ci = st["cell_idx"] if cell_idx is None else cell_idx
+    if s.cfg.shock_enabled:
+        mask = (np.arange(1, s.neta + 1)[None, :] < np.asarray(ci)[:, None])
+    else:
+        mask = np.ones((s.nchi, s.neta), dtype=bool)
+    out = np.empty(4)
+    for v in range(4):
+        a = qa[v].reshape(shape, order="F")[1:-1, 1:-1][mask]
+        b = qb[v].reshape(shape, order="F")[1:-1, 1:-1][mask]
+        out[v] = np.sqrt(np.mean((a - b) ** 2)) / np.sqrt(np.mean(a**2))
+    return out
+
+
+def MARCH_TO_RESIDUAL(s: Solution, tol: float = 1e-10, max_steps: int = 10**7, check_every: int = 2000,
+                      max_seconds: float | None = None, log=None) -> dict:
+    """RUN_SIMULATION's time loop (RUN_SIMULATION.jl:77-80) until the step residual of the
+    MATLAB twin (RESIDUAL, max over the four variables) falls below tol. The residual of
+    one step is measured every check_every steps; the march stops at tol, at max_steps or
+    after max_seconds of wall time. Returns the step count, the last residual and the
+    history [(step, t, residual)]."""
+    import time
+    t0 = time.perf_counter()
+    steps, hist = 0, []
+    res = np.full(4, np.inf)
+    while steps < max_steps:
+        q_save = s.get_state()["q"]
+        ADVECT_FLOW(s, 1)
+        steps += 1
+        res = RESIDUAL(s, q_save)
+        st_t = s.get_state()["t"]
+        hist.append((steps, st_t, float(np.max(res))))
+        if log:
+            log(f"step {steps} t {st_t:.4f} residual {np.max(res):.3e} ({time.perf_counter() - t0:.0f} s)")
+        if np.max(res) < tol:
+            break
+        if max_seconds is not None and time.perf_counter() - t0 > max_seconds:
+            break
+        n = min(check_every - 1, max_steps - steps)
+        if n > 0:
+            ADVECT_FLOW(s, n)
+            steps += n
+    return dict(steps=steps, residual=res, converged=bool(np.max(res) < tol), history=hist,
+                seconds=time.perf_counter() - t0)
+
+
 def UPDATE_FLOW_CELLS(s: Solution) -> Solution:
     s.ctx.check(s.ctx.L.hymor_update_flow_cells(s.ctx.h))
     return s
@@ -312,6 +366,14 @@ def _expm_block_op(s: Solution, dt: float, nsteps: int, order: int, transpose: i
     return apply
 
 
+def _krylov_opts(nev: int, ncv: int, tol: float, maxit: int, block: int, order: int, seed: int = 0,
+                 flow_start: bool = False):
+    o = _lib.KrylovOpts()
+    o.nev, o.ncv, o.maxit, o.block, o.order = int(nev), int(ncv), int(maxit), int(block), int(order)
+    o.flow_start, o.seed, o.tol = int(flow_start), int(seed), float(tol)
+    return o
+
+
 def EIGENVALUES(L: LinearOperatorGPU, s: Solution, n_modes: int, T_ref: float = 0.5, ncv: int | None = None,
                 tol: float = 1e-8, order: int = 5, method: str = "device", seed: int = 3, maxit: int = 300,
                 block: int = 1, flow_start: bool = False, modes: bool = False, keep_unconverged: bool = False):
@@ -319,15 +381,17 @@ def EIGENVALUES(L: LinearOperatorGPU, s: Solution, n_modes: int, T_ref: float = 
     largest magnitude of exp(L T_ref) (Taylor-`order` steps of the CFL dt), mapped back as
     lambda = log(mu) / (dt * timesteps).
 
-    modes: also the eigenvectors (info["modes"], 4 Nchi Neta x n_modes, complex, unit
-    norm; the reference's V). When the solve does not reach tol, the reference warns and
-    returns NaN (EIGENVALUES.jl:184-204); so does this, unless keep_unconverged, which
-    returns the last Ritz values (and no modes) with info["converged"] False.
+    modes: also the eigenvectors (info["modes"], n x n_modes, complex, unit norm; the
+    reference's V). When the solve does not reach tol, the reference warns and returns NaN
+    (EIGENVALUES.jl:184-204); so does this, unless keep_unconverged, which returns the last
+    Ritz values (and no modes) with info["converged"] False.
 
-    method "device": Krylov-Schur with the basis in HBM (hymor_gb300/krylov.py).
+    method "device": hymor_eigs, the Krylov-Schur solver behind the C ABI (basis in HBM;
+                     block > 1: `block` vectors propagated per batched call).
+    method "python": the same Krylov-Schur restart driven from Python (hymor_gb300/krylov.py)
+                     over the device building blocks, with LAPACK's dense steps.
     method "host":   the reference's structure, ARPACK on the host calling one GPU
                      propagation per Krylov vector with a host round trip.
-    block > 1 (device): block Krylov-Schur, `block` vectors propagated per batched call.
     flow_start: random start vectors that vanish outside the flow cells. The residual is
     masked by the flow cells, so the operator has zero rows there and leaves the flow-cell
     subspace invariant (with the shock unknowns too, which read and write only flow cells);
@@ -343,21 +407,41 @@ def EIGENVALUES(L: LinearOperatorGPU, s: Solution, n_modes: int, T_ref: float = 
         st = s.get_state()
         flow = (np.arange(1, s.cfg.neta + 1)[None, :] < st["cell_idx"][:, None]).ravel(order="F")
         mask = np.concatenate([np.tile(flow.astype(np.float64), 4), np.ones(n - 4 * s.N)])
+    rng = np.random.Generator(np.random.PCG64(seed))
     t0 = time.perf_counter()
     X = None
-    if method == "device" and block > 1:
+    if method == "device":
+        from .krylov import DeviceBuffer
+        x0 = rng.standard_normal((block, n))
+        if mask is not None:
+            x0 *= mask[None, :]
+        x0 = np.ascontiguousarray(x0.ravel())
+        mr, mi, resid = np.empty(n_modes), np.empty(n_modes), np.empty(n_modes)
+        info3 = np.zeros(3, dtype=np.int32)
+        want = modes and 2 * n_modes <= ncv
+        vb = DeviceBuffer(s.ctx, 8 * n * 2 * n_modes) if want else None
+        o = _krylov_opts(n_modes, ncv, tol, maxit, block, order)
+        s.ctx.check(s.ctx.L.hymor_eigs(s.ctx.h, ctypes.byref(o), float(dt), int(timesteps), dp(x0), dp(mr), dp(mi),
+                                       dp(resid), ip(info3), vb.ptr if vb else None))
+        mu = mr + 1j * mi
+        if vb is not None:
+            Xr = vb.download(2 * n * n_modes).reshape(2 * n_modes, n).T
+            X = Xr[:, :n_modes] + 1j * Xr[:, n_modes:]
+            vb.free()
+        nops, converged = int(info3[0]), bool(info3[2])
+    elif method == "python" and block > 1:
         from .krylov import block_krylov_schur
         mu, resid, nops, X = block_krylov_schur(s.ctx, n, _expm_block_op(s, dt, timesteps, order), n_modes, ncv,
                                                 block, tol=tol, maxit=maxit, seed=seed, start_mask=mask,
                                                 want_vectors=True)
         converged = bool(np.all(resid <= tol * np.abs(mu)))
-    elif method == "device":
+    elif method == "python":
         from .krylov import krylov_schur
-        v0 = None
+        v0 = rng.standard_normal(n)
         if mask is not None:
-            v0 = np.random.Generator(np.random.PCG64(seed)).standard_normal(n) * mask
+            v0 = v0 * mask
         mu, resid, nops, X = krylov_schur(s.ctx, n, _expm_op(s, dt, timesteps, order), n_modes, ncv, tol=tol,
-                                          maxit=maxit, seed=seed, v0=v0, want_vectors=True)
+                                          maxit=maxit, v0=v0, want_vectors=True)
         converged = bool(np.all(resid <= tol * np.abs(mu)))
     elif method == "host":
         from scipy.sparse.linalg import ArpackNoConvergence, LinearOperator, eigs
@@ -366,7 +450,6 @@ def EIGENVALUES(L: LinearOperatorGPU, s: Solution, n_modes: int, T_ref: float = 
         def mv(x):
             count[0] += 1
             return L.expm(np.ascontiguousarray(x, dtype=np.float64).ravel(), dt, timesteps, order)
-        rng = np.random.Generator(np.random.PCG64(seed))
         try:
             mu, X = eigs(LinearOperator((n, n), matvec=mv, dtype=np.float64), k=n_modes, which="LM", tol=tol,
                          ncv=ncv, v0=rng.standard_normal(n), maxiter=maxit * n_modes, return_eigenvectors=True)
@@ -489,7 +572,8 @@ class _ChuWeights:
 
 def TRANSIENT_GROWTH_DOWNSTREAM(L: LinearOperatorGPU, s: Solution, n_modes: int, T: float, ncv: int | None = None,
                                 tol: float = 1e-8, order: int = 5, seed: int = 4, maxit: int = 300,
-                                block: int = 1, modes: bool = False, keep_unconverged: bool = False):
+                                block: int = 1, modes: bool = False, keep_unconverged: bool = False,
+                                method: str = "device"):
     """TRANSIENT_GROWTH_DOWNSTREAM (TRANSIENT_GROWTH_DOWNSTREAM.jl:34-153): optimal energy gains
     G(T), the largest eigenvalues of exp(Lᵀ T) R'MR exp(L T) x = G R'M^R x. The generalised
     symmetric problem is reduced with the per-cell Cholesky factor of R'M^R (D = K Kᵀ) to
@@ -499,7 +583,50 @@ def TRANSIENT_GROWTH_DOWNSTREAM(L: LinearOperatorGPU, s: Solution, n_modes: int,
     operator applied to `block` vectors per batched call. modes: also the optimal initial
     conditions x = K^-T y (info["modes"], n x n_modes, x' R'M^R x = 1; the reference's V).
     Non-convergence warns and returns NaN, as the reference
-    (TRANSIENT_GROWTH_DOWNSTREAM.jl:131-135), unless keep_unconverged."""
+    (TRANSIENT_GROWTH_DOWNSTREAM.jl:131-135), unless keep_unconverged.
+
+    method "device": hymor_tg_gain (the solver behind the C ABI, weights built on the device
+    context's state); "python": the Krylov-Schur driven from Python (krylov.py) with the
+    weights built by numpy."""
+    ncv = ncv or max(2 * n_modes + 1, 16, n_modes + 4 * block)
+    if method == "python":
+        return _tg_python(L, s, n_modes, T, ncv, tol, order, seed, maxit, block, modes, keep_unconverged)
+    import time
+    from .krylov import DeviceBuffer
+    n = L.n
+    rng = np.random.Generator(np.random.PCG64(seed))
+    x0 = np.ascontiguousarray(rng.standard_normal((block, n)).ravel())
+    G = np.empty(n_modes)
+    resid = np.empty(n_modes)
+    info3 = np.zeros(3, dtype=np.int32)
+    dt_o, nt_o = np.empty(1), np.zeros(1, dtype=np.int32)
+    vb = DeviceBuffer(s.ctx, 8 * n * n_modes) if modes else None
+    o = _krylov_opts(n_modes, ncv, tol, maxit, block, order)
+    Ts = np.array([float(T)])
+    t0 = time.perf_counter()
+    s.ctx.check(s.ctx.L.hymor_tg_gain(s.ctx.h, ctypes.byref(o), 1, dp(Ts), dp(x0), dp(G), dp(resid), ip(info3),
+                                      dp(dt_o), ip(nt_o), vb.ptr if vb else None))
+    elapsed = time.perf_counter() - t0
+    X = None
+    if vb is not None:
+        X = vb.download(n * n_modes).reshape(n_modes, n).T.copy()
+        vb.free()
+    converged = bool(info3[2])
+    if not converged and not keep_unconverged:
+        import warnings
+        warnings.warn(f"transient-growth solve did not reach tol {tol:g} in {maxit} restarts; returning NaN")
+        G = np.full(n_modes, np.nan)
+        X = np.full((n, n_modes), np.nan) if modes else None
+    dt, n_t = float(dt_o[0]), int(nt_o[0])
+    info = dict(resid=resid, dt=dt, n_t=n_t, T_opt=n_t * dt, nops=int(info3[0]), seconds=elapsed,
+                converged=converged)
+    if modes:
+        info["modes"] = X
+    return G, info
+
+
+def _tg_python(L, s, n_modes, T, ncv, tol, order, seed, maxit, block, modes, keep_unconverged):
+    """TRANSIENT_GROWTH_DOWNSTREAM with the Krylov-Schur driven from Python (krylov.py)."""
     import time
     from .krylov import DeviceBuffer, block_krylov_schur, krylov_schur
     dt_cfl = CFL_TIMESTEP(s)
@@ -516,7 +643,6 @@ def TRANSIENT_GROWTH_DOWNSTREAM(L: LinearOperatorGPU, s: Solution, n_modes: int,
         W.apply("C0", k, t2.ptr, t1.ptr)                                                   # C0 P x
         s.ctx.check(Lh.hymor_expm_apply_dev(h, k, dt, n_t, order, t1.ptr, t2.ptr, 1))      # Pᵀ C0 P x
         W.apply("Kinv", k, t2.ptr, dst)                                                    # K^-1 (...)
-    ncv = ncv or max(2 * n_modes + 1, 16, n_modes + 4 * block)
     t0 = time.perf_counter()
     if block > 1:
         gains, resid, nops, Y = block_krylov_schur(s.ctx, n, apply_k, n_modes, ncv, block, tol=tol, maxit=maxit,
@@ -544,14 +670,48 @@ def TRANSIENT_GROWTH_DOWNSTREAM(L: LinearOperatorGPU, s: Solution, n_modes: int,
 
 def TRANSIENT_GROWTH_HORIZONS(L: LinearOperatorGPU, s: Solution, n_modes: int, Ts, ncv: int | None = None,
                               tol: float = 1e-8, order: int = 5, seed: int = 4, maxit: int = 300,
-                              keep_unconverged: bool = False):
+                              keep_unconverged: bool = False, method: str = "device"):
     """TRANSIENT_GROWTH_DOWNSTREAM for several time horizons at once: one Krylov-Schur solve
-    per horizon, run in lockstep (krylov_schur_many), so that each round propagates one
-    vector per unfinished horizon in one batched call (hymor_expm_apply_multi_dev: each
-    vector with its own dt = T / round(T / dt_CFL) and step count, the longer horizons
-    first). Each horizon's solve makes the same operations as TRANSIENT_GROWTH_DOWNSTREAM(T)
-    with the same seed. Returns (gains, infos): gains[h] the n_modes gains of Ts[h], infos[h]
-    as TRANSIENT_GROWTH_DOWNSTREAM's info (seconds: the whole batched solve)."""
+    per horizon, run in lockstep, so that each round propagates one vector per unfinished
+    horizon in one batched call (hymor_expm_apply_multi_dev: each vector with its own
+    dt = T / round(T / dt_CFL) and step count, the longer horizons first). Each horizon's
+    solve makes the same operations as TRANSIENT_GROWTH_DOWNSTREAM(T) with the same seed.
+    Returns (gains, infos): gains[h] the n_modes gains of Ts[h], infos[h] as
+    TRANSIENT_GROWTH_DOWNSTREAM's info (seconds: the whole batched solve).
+
+    method "device": hymor_tg_gain with nh horizons (the lockstep behind the C ABI);
+    "python": krylov_schur_many driven from Python."""
+    ncv = ncv or max(2 * n_modes + 1, 16)
+    if method == "python":
+        return _tg_horizons_python(L, s, n_modes, Ts, ncv, tol, order, seed, maxit, keep_unconverged)
+    import time
+    Ts = np.array([float(T) for T in Ts])
+    H, n = len(Ts), L.n
+    x0 = np.ascontiguousarray(np.random.Generator(np.random.PCG64(seed)).standard_normal(n))
+    G = np.empty((H, n_modes))
+    resid = np.empty((H, n_modes))
+    info3 = np.zeros(3 * H, dtype=np.int32)
+    dts, nts = np.empty(H), np.zeros(H, dtype=np.int32)
+    o = _krylov_opts(n_modes, ncv, tol, maxit, 1, order)
+    t0 = time.perf_counter()
+    s.ctx.check(s.ctx.L.hymor_tg_gain(s.ctx.h, ctypes.byref(o), H, dp(Ts), dp(x0), dp(G), dp(resid), ip(info3),
+                                      dp(dts), ip(nts), None))
+    elapsed = time.perf_counter() - t0
+    infos = []
+    for h in range(H):
+        converged = bool(info3[3 * h + 2])
+        if not converged and not keep_unconverged:
+            G[h] = np.nan
+        infos.append(dict(resid=resid[h], dt=float(dts[h]), n_t=int(nts[h]), T_opt=int(nts[h]) * float(dts[h]),
+                          nops=int(info3[3 * h]), seconds=elapsed, converged=converged))
+    if not all(inf["converged"] for inf in infos) and not keep_unconverged:
+        import warnings
+        warnings.warn(f"transient-growth solves of some horizons did not reach tol {tol:g}; their gains are NaN")
+    return G, infos
+
+
+def _tg_horizons_python(L, s, n_modes, Ts, ncv, tol, order, seed, maxit, keep_unconverged):
+    """TRANSIENT_GROWTH_HORIZONS with the lockstep Krylov-Schur driven from Python."""
     import time
     from .krylov import DeviceBuffer, krylov_schur_many
     Ts = [float(T) for T in Ts]
@@ -580,7 +740,6 @@ def TRANSIENT_GROWTH_HORIZONS(L: LinearOperatorGPU, s: Solution, n_modes: int, T
         W.apply("Kinv", k, bufs[2].ptr, bufs[0].ptr)        # K^-1 (...)
         for c, dst in enumerate(dsts):
             s.ctx.check(Lh.hymor_memcpy_d2d(h, dst, bufs[0].addr(c * n), 8 * n))
-    ncv = ncv or max(2 * n_modes + 1, 16)
     problems = [dict(nev=n_modes, ncv=ncv, tol=tol, maxit=maxit, seed=seed, symmetric=True) for _ in Ts]
     t0 = time.perf_counter()
     res = krylov_schur_many(s.ctx, n, apply_many, problems)

@@ -289,6 +289,51 @@ int hymor_block4_apply_dev(hymor_ctx* ctx, int k, const double* dB, const double
 int hymor_block4_apply_ext_dev(hymor_ctx* ctx, int k, int64_t ntail, const double* dB, const double* dTail,
                                const double* dX, double* dY);
 
+/* ---- Device-resident eigen and transient-growth solvers (Krylov-Schur on the device
+ * basis; the host handles only the projected matrix, at most (ncv + 2 block)^2). ---- */
+typedef struct {
+  int32_t nev;        /* eigenvalues / gains wanted (the reference's n_modes)                    */
+  int32_t ncv;        /* basis size; 0 picks max(2 nev + 1, 20, nev + 4 block)                   */
+  int32_t maxit;      /* Krylov-Schur cycles (restarts + 1)                                      */
+  int32_t block;      /* vectors per batched propagation; 1 = Krylov-Schur, > 1 = block variant  */
+  int32_t order;      /* Taylor degree of one propagator step (5: POWER_METHOD!, 4: RK4 substeps) */
+  int32_t flow_start; /* start vectors vanish outside the flow cells (when x0 is NULL)            */
+  uint64_t seed;      /* start vectors when x0 is NULL (deterministic normal variates)            */
+  double tol;         /* converged when every Ritz residual <= tol |theta|                        */
+} hymor_krylov_opts;
+/* EIGENVALUES_GPU_ARNOLDI (Stability_analysis/Eigenvalues/EIGENVALUES.jl:112-205, the Arpack
+ * call of :152-162 with the matvec closure of ARNOLDI_POWER_GPU.jl:36-82): the nev eigenvalues
+ * mu of largest modulus of P = exp(L dt nsteps) (nsteps Taylor steps of degree order), in
+ * decreasing modulus (lambda = log(mu) / (dt nsteps) is the caller's mapping, as the
+ * reference's :166). x0: host start block (n x block, n = hymor_operator_size) or NULL.
+ * resid: Ritz residual norms (may be NULL). info[3]: operator applications (vectors),
+ * restarts, converged (1/0). dvecs: NULL, or a device buffer of n x 2 nev receiving the unit
+ * eigenvectors' real parts (first nev columns) and imaginary parts (needs 2 nev <= ncv). A
+ * solve that stops at maxit returns 0 with info[2] = 0: the reference then warns and returns
+ * NaN (EIGENVALUES.jl:184-204), which is the caller's choice here. */
+int hymor_eigs(hymor_ctx* ctx, const hymor_krylov_opts* opts, double dt, int nsteps, const double* x0, double* mu_re,
+               double* mu_im, double* resid, int32_t* info, double* dvecs);
+/* TRANSIENT_GROWTH_DOWNSTREAM (Stability_analysis/Transient_growth_downstream/
+ * TRANSIENT_GROWTH_DOWNSTREAM.jl:34-153, the Arpack call of :96-106 with CONSTRUCT_C.jl's
+ * operator): the nev largest optimal energy gains G(T) of exp(L' T) R'MR exp(L T) x = G R'M^R x
+ * for nh horizons T[h], with R, M, M^ built on the device context's solution (CONSTRUCT_R.jl,
+ * CONSTRUCT_M.jl, CONSTRUCT_M_HAT.jl) and the problem reduced by the per-cell Cholesky factor
+ * of R'M^R. Each horizon uses steps = round(T / dt_CFL) Taylor steps of dt = T / steps (:40-44;
+ * dt_out, nsteps_out per horizon, may be NULL). Several horizons (nh > 1, block 1) run in
+ * lockstep, one batched propagation per round for all unfinished horizons (no counterpart in
+ * the reference, which solves one horizon per call). gains, resid: nh x nev; info: nh x 3 as
+ * hymor_eigs. dvecs (nh = 1 only): NULL or a device buffer of n x nev receiving the optimal
+ * initial conditions x (x' R'M^R x = 1), the reference's V. */
+int hymor_tg_gain(hymor_ctx* ctx, const hymor_krylov_opts* opts, int nh, const double* T, const double* x0,
+                  double* gains, double* resid, int32_t* info, double* dt_out, int32_t* nsteps_out, double* dvecs);
+/* The dense steps of the two solvers, exposed for testing and for callers with their own
+ * Krylov loops (no counterpart in the reference, whose dense steps are Arpack's LAPACK calls):
+ * real Schur form A = Z T Z' (column-major n x n, n <= 1024) with the nsel eigenvalues of
+ * largest modulus leading (whole conjugate pairs; *nlead = rows they fill), wr/wi the
+ * eigenvalues in T's order; and the symmetric eigen-decomposition A = V diag(w) V'. */
+int hymor_dense_schur(int n, const double* A, int nsel, double* T, double* Z, double* wr, double* wi, int32_t* nlead);
+int hymor_dense_symeig(int n, const double* A, double* w, double* V);
+
 /* Device buffer helpers for the *_dev entry points. */
 int hymor_device_alloc(hymor_ctx* ctx, uint64_t bytes, void** dptr);
 int hymor_device_free(hymor_ctx* ctx, void* dptr);

@@ -1407,28 +1407,38 @@ void stencil_matvec(const orc_config& c, const double* coef, const double* x, do
   const size_t N = (size_t)nchi * neta;
   const bool per_chi = c.bc_chi0 == ORC_BC_PERIODIC && c.bc_chi1 == ORC_BC_PERIODIC;
   const bool per_eta = c.bc_eta0 == ORC_BC_PERIODIC && c.bc_eta1 == ORC_BC_PERIODIC;
-  std::memset(y, 0, sizeof(double) * 4 * N);
+  // Each output entry is summed by the one thread that owns its cell. Forward: output
+  // cell m sums its 9 neighbour blocks (b, a ascending). Transpose: output cell n sums the
+  // blocks of the cells m = n - (a, b) whose stencil reaches n (b, a descending, the order
+  // in which a scatter over m ascending would add them).
+#pragma omp parallel for schedule(static)
   for (int j = 1; j <= neta; ++j)
     for (int i = 1; i <= nchi; ++i) {
-      size_t mo = (size_t)(i - 1) + (size_t)(j - 1) * nchi;
-      for (int b = -1; b <= 1; ++b)
-        for (int a = -1; a <= 1; ++a) {
-          int in = i + a, jn = j + b;
+      const size_t me = (size_t)(i - 1) + (size_t)(j - 1) * nchi;
+      double acc[4] = {0.0, 0.0, 0.0, 0.0};
+      for (int bb = 0; bb < 3; ++bb)
+        for (int aa = 0; aa < 3; ++aa) {
+          const int b = transpose ? 1 - bb : bb - 1;
+          const int a = transpose ? 1 - aa : aa - 1;
+          // forward: the neighbour (i + a, j + b); transpose: the cell (i - a, j - b)
+          int in = transpose ? i - a : i + a, jn = transpose ? j - b : j + b;
           bool wi = in < 1 || in > nchi, wj = jn < 1 || jn > neta;
           if ((wi && !per_chi) || (wj && !per_eta) || (wi && wj)) continue;
           if (wi) in = in < 1 ? in + nchi : in - nchi;
           if (wj) jn = jn < 1 ? jn + neta : jn - neta;
-          size_t n = (size_t)(in - 1) + (size_t)(jn - 1) * nchi;
-          int q = (b + 1) * 3 + (a + 1);
-          const double* B = coef + (mo * 9 + q) * 16;
-          for (int vo = 0; vo < 4; ++vo)
-            for (int vi = 0; vi < 4; ++vi) {
-              if (!transpose)
-                y[vo * N + mo] += B[vo * 4 + vi] * x[vi * N + n];
-              else
-                y[vi * N + n] += B[vo * 4 + vi] * x[vo * N + mo];
-            }
+          const size_t other = (size_t)(in - 1) + (size_t)(jn - 1) * nchi;
+          const int q = (b + 1) * 3 + (a + 1);
+          if (!transpose) {
+            const double* B = coef + (me * 9 + q) * 16;
+            for (int vo = 0; vo < 4; ++vo)
+              for (int vi = 0; vi < 4; ++vi) acc[vo] += B[vo * 4 + vi] * x[vi * N + other];
+          } else {
+            const double* B = coef + (other * 9 + q) * 16;
+            for (int vo = 0; vo < 4; ++vo)
+              for (int vi = 0; vi < 4; ++vi) acc[vi] += B[vo * 4 + vi] * x[vo * N + other];
+          }
         }
+      for (int v = 0; v < 4; ++v) y[v * N + me] = acc[v];
     }
 }
 
@@ -1722,10 +1732,11 @@ void orc_expm_ext(const orc_config* cfg, const double* coef, const int32_t* rows
     for (int j = 1; j <= order; ++j) {
       stencil_matvec(*cfg, cdt.data(), v.data(), term.data(), transpose);
       shock_matvec(*cfg, rows, b21.data(), b12.data(), b22.data(), v.data(), term.data(), transpose);
-      v = term;
+      v.swap(term);
       fact = j * fact;
       double r = 1.0 / (double)fact;
-      for (size_t k = 0; k < n; ++k) vout[k] += v[k] * r;
+#pragma omp parallel for schedule(static)
+      for (long k = 0; k < (long)n; ++k) vout[k] += v[k] * r;
     }
     v = vout;
   }
@@ -1746,10 +1757,11 @@ void orc_expm(const orc_config* cfg, const double* coef, double dt, int nsteps, 
     long long fact = 1;
     for (int j = 1; j <= order; ++j) {
       stencil_matvec(*cfg, cdt.data(), v.data(), term.data(), transpose);
-      v = term;
+      v.swap(term);
       fact = j * fact;
       double r = 1.0 / (double)fact;
-      for (size_t k = 0; k < n; ++k) vout[k] += v[k] * r;
+#pragma omp parallel for schedule(static)
+      for (long k = 0; k < (long)n; ++k) vout[k] += v[k] * r;
     }
     v = vout;
   }

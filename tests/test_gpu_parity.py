@@ -181,17 +181,20 @@ def test_stored_flux_enters_cfl_and_steps(require_gpu):
 @pytest.mark.slow
 def test_cylinder_2000_steps_parity(require_gpu):
     """The 100 x 80 shock-fitted cylinder marched 2000 RK4 steps at CFL 0.5: residual and
-    shock position match the oracle."""
+    shock position match the oracle. Measured on GB300: state 1.7e-13 (rho_v; the others
+    3e-14 .. 7e-14) and residual 1.2e-15 of the flux scale; the tolerances are ~10x those."""
     cfg = C.cylinder_config(100, 80)
     cs, sol, orc = both(cfg)
     S.ADVECT_FLOW(sol, 2000)
     orc.advect(2000)
-    errs = compare_state(sol, orc, 1e-9)
+    errs = compare_state(sol, orc, 2e-12)
     st = sol.get_state()
     assert np.isfinite(st["q"]).all()
     # residual of the marched state
     fg, fo = S.PDE(sol), orc.residual()
-    assert max(residual_rel(fg, fo, cs)) < 1e-8, errs
+    res = residual_rel(fg, fo, cs)
+    print(f"\n2000-step parity: state {errs}, residual {res}")
+    assert max(res) < 1.5e-14, (errs, res)
 
 
 def test_jacobian_parity(require_gpu):

@@ -245,3 +245,144 @@ def test_transient_growth_horizons_batched(require_gpu):
         g1, info1 = S.TRANSIENT_GROWTH_DOWNSTREAM(L, sol, 2, T, ncv=16, tol=1e-11)
         assert np.allclose(G[h], g1, rtol=1e-9, atol=0)
         assert infos[h]["n_t"] == info1["n_t"] and infos[h]["converged"]
+
+
+@pytest.mark.slow
+def test_channel_eigenvalue_pin_device(require_gpu):
+    """tutorials/channel_flow/README.md:164-168, through the device: the channel (180 x 60,
+    Re 7500, M 0.05) linearised by LINEARIZE_L on the GPU has the leading eigenvalue
+    0.000247 + 0.248408i, the reference's printed answer, held to the oracle's 5e-6 (the FD
+    Jacobian's rounding moves it by ~1e-5 at M 0.05). Shift-invert on the host, as the
+    tutorial's main.jl:69-81."""
+    import json
+    import os
+    sla = pytest.importorskip("scipy.sparse.linalg")
+    cfg = C.channel_config()
+    cs = C.initial_state(cfg, noise=0.0)
+    sol = S.Solution(cs)
+    _, L = S.LINEARIZE_L(sol)
+    A = O.stencil_to_csr(cfg, L.blocks())
+    lam = sla.eigs(A.astype(complex), k=1, sigma=0.25j, return_eigenvectors=False)[0]
+    ka = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "known_answers.json")))
+    pin = ka["channel_eigenvalue"]
+    assert abs(lam.real - pin["re"]) < 5e-6, lam
+    assert abs(lam.imag - pin["im"]) < 5e-6, lam
+    sol.close()
+
+
+@pytest.mark.slow
+def test_eigenvalues_sphere_cone_degree4(require_gpu):
+    """The batched-modal-analysis configuration's shape at reduced size: the axisymmetric
+    7-degree sphere-cone (M 6, Re 2e4) at 240 x 80, exp(L dt_50) built from 50 Taylor steps
+    of degree 4 (the RK4-substep form of the propagator), start vector on the flow cells.
+    The device Krylov-Schur eigenvalues match ARPACK on the oracle's propagator to 1e-8 of
+    the spectrum's scale, with the same Jacobian blocks."""
+    sla = pytest.importorskip("scipy.sparse.linalg")
+    cfg = C.blunt_cone_config(240, 80)
+    cs = C.initial_state(cfg)
+    sol, orc = S.Solution(cs), O.Oracle(cs)
+    S.ADVECT_FLOW(sol, 20)
+    orc.advect(20)
+    _, L = S.LINEARIZE_L(sol)
+    co = orc.linearize()
+    L.set_blocks(co)
+    dt = S.CFL_TIMESTEP(sol)
+    lam, info = S.EIGENVALUES(L, sol, 4, T_ref=50 * dt, order=4, ncv=30, tol=1e-11, flow_start=True)
+    assert info["timesteps"] == 50 and info["converged"]
+    n = 4 * cfg.nchi * cfg.neta
+    st = sol.get_state()
+    flow = (np.arange(1, cfg.neta + 1)[None, :] < st["cell_idx"][:, None]).ravel(order="F")
+    v0 = np.random.Generator(np.random.PCG64(3)).standard_normal(n) * np.tile(flow, 4)
+    op = sla.LinearOperator((n, n), matvec=lambda x: orc.expm(co, info["dt"], 50, np.ascontiguousarray(x).ravel(),
+                                                             order=4), dtype=np.float64)
+    mu = sla.eigs(op, k=4, which="LM", tol=1e-12, ncv=30, v0=v0, return_eigenvectors=False)
+    lam_o = np.log(mu.astype(complex)) / (info["dt"] * 50)
+    scale = np.max(np.abs(lam_o))
+    for a in lam:
+        assert np.min(np.abs(lam_o - a)) <= 1e-8 * scale, (lam, lam_o)
+    sol.close()
+
+
+@pytest.mark.slow
+def test_transient_growth_cylinder_T1(require_gpu):
+    """The transient-growth configuration's family at reduced size: the cylinder with the
+    same wall-normal stretch at 80 x 40 and a horizon of one freestream time unit (T = 1,
+    1126 Taylor steps of the CFL dt). The device gains match eigsh on the oracle's forward
+    and adjoint propagators to 1e-6, with the same Jacobian blocks."""
+    sla = pytest.importorskip("scipy.sparse.linalg")
+    cfg, cs, sol, orc = _setup(80, 40)
+    _, L = S.LINEARIZE_L(sol)
+    co = orc.linearize()
+    L.set_blocks(co)
+    G, info = S.TRANSIENT_GROWTH_DOWNSTREAM(L, sol, 2, 1.0, ncv=16, tol=1e-11)
+    assert info["n_t"] > 1000 and info["converged"]
+    st = sol.get_state()
+    C0, D = S.chu_blocks_from_state(cfg, cs.mesh["vol"], st["q"], st["cell_idx"])
+    Ki = np.linalg.inv(np.linalg.cholesky(D))
+    N = cfg.nchi * cfg.neta
+
+    def blk(B, x):
+        return np.einsum("nij,nj->ni", B, x.reshape(4, N).T).T.ravel()
+    dt, nt = info["dt"], info["n_t"]
+
+    def mv(y):
+        x = blk(np.transpose(Ki, (0, 2, 1)), np.ascontiguousarray(y).ravel())
+        z = blk(C0, orc.expm(co, dt, nt, x))
+        return blk(Ki, orc.expm(co, dt, nt, z, transpose=True))
+    op = sla.LinearOperator((4 * N, 4 * N), matvec=mv, dtype=np.float64)
+    Go = np.sort(sla.eigsh(op, k=2, which="LA", tol=1e-12, ncv=16, return_eigenvectors=False))[::-1]
+    assert np.allclose(np.sort(G)[::-1], Go, rtol=1e-6, atol=0), (G, Go)
+    sol.close()
+
+
+def test_cabi_solvers_match_python_driver(require_gpu):
+    """hymor_eigs and hymor_tg_gain (the Krylov-Schur solvers behind the C ABI, with their own
+    dense steps) give the eigenvalues and gains of the same Krylov-Schur driven from Python
+    with LAPACK's dense steps (krylov.py), on the same device operator and start vectors:
+    the two differ only in the rounding of the projected-matrix steps."""
+    cfg, cs, sol, orc = _setup(30, 20)
+    _, L = S.LINEARIZE_L(sol)
+    for block in (1, 3):
+        lam_c, ic = S.EIGENVALUES(L, sol, 4, T_ref=0.02, ncv=24, tol=1e-11, block=block)
+        lam_p, ip_ = S.EIGENVALUES(L, sol, 4, T_ref=0.02, ncv=24, tol=1e-11, block=block, method="python")
+        assert ic["converged"] and ip_["converged"]
+        scale = np.max(np.abs(lam_p))
+        for a in lam_c:
+            assert np.min(np.abs(lam_p - a)) <= 1e-9 * scale, (block, lam_c, lam_p)
+    G_c, ic = S.TRANSIENT_GROWTH_DOWNSTREAM(L, sol, 2, 0.01, ncv=16, tol=1e-11, modes=True)
+    G_p, ip_ = S.TRANSIENT_GROWTH_DOWNSTREAM(L, sol, 2, 0.01, ncv=16, tol=1e-11, modes=True, method="python")
+    assert np.allclose(G_c, G_p, rtol=1e-9, atol=0), (G_c, G_p)
+    for i in range(2):  # the same optimal initial conditions up to sign
+        a, b = ic["modes"][:, i], ip_["modes"][:, i]
+        assert min(np.linalg.norm(a - b), np.linalg.norm(a + b)) <= 1e-7 * np.linalg.norm(b)
+    Ts = [0.004, 0.016, 0.008]
+    Gh_c, _ = S.TRANSIENT_GROWTH_HORIZONS(L, sol, 2, Ts, ncv=16, tol=1e-11)
+    Gh_p, _ = S.TRANSIENT_GROWTH_HORIZONS(L, sol, 2, Ts, ncv=16, tol=1e-11, method="python")
+    assert np.allclose(Gh_c, Gh_p, rtol=1e-9, atol=0)
+
+
+def test_cabi_eigs_seeded_start_and_errors(require_gpu):
+    """hymor_eigs called as a C caller would: no start vector (the library's seeded normal
+    start, masked to the flow cells), the converged flag, and the errors before a Jacobian
+    exists or with inconsistent options."""
+    import ctypes
+    from hymor_gb300 import _lib
+    from hymor_gb300._lib import dp, ip
+    cfg, cs, sol, orc = _setup(30, 20)
+    Lh, h = sol.ctx.L, sol.ctx.h
+    o = S._krylov_opts(4, 24, 1e-10, 300, 1, 5, seed=11, flow_start=True)
+    mr, mi, res = np.empty(4), np.empty(4), np.empty(4)
+    info = np.zeros(3, dtype=np.int32)
+    dt = S.CFL_TIMESTEP(sol)
+    assert Lh.hymor_eigs(h, ctypes.byref(o), dt, 40, None, dp(mr), dp(mi), dp(res), ip(info), None) == -6
+    _, L = S.LINEARIZE_L(sol)
+    sol.ctx.check(Lh.hymor_eigs(h, ctypes.byref(o), dt, 40, None, dp(mr), dp(mi), dp(res), ip(info), None))
+    assert info[2] == 1 and info[0] > 0
+    assert np.all(res <= 1e-10 * np.abs(mr + 1j * mi))
+    lam_ref, _ = S.EIGENVALUES(L, sol, 4, T_ref=40 * dt, ncv=24, tol=1e-10, flow_start=True)
+    lam = np.log((mr + 1j * mi).astype(complex)) / (dt * 40)
+    for a in lam:
+        assert np.min(np.abs(lam_ref - a)) <= 1e-8 * np.max(np.abs(lam_ref))
+    bad = S._krylov_opts(10, 11, 1e-10, 300, 1, 5)
+    assert Lh.hymor_eigs(h, ctypes.byref(bad), dt, 40, None, dp(mr), dp(mi), None, None, None) == -1
+    assert "nev + 2 block <= ncv" in Lh.hymor_last_error(h).decode()
