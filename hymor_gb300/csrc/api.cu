@@ -7,6 +7,8 @@
 #include <string>
 #include <vector>
 
+#include <cudaTypedefs.h>  // PFN_cuTensorMapEncodeTiled
+
 #include "kernels.h"
 
 namespace hymor {
@@ -57,6 +59,8 @@ struct hymor_ctx_s {
   // the persistent sound speed has not been computed for the state set last (set_state
   // without it); the next call that reads it computes it first
   bool a_stale = false;
+  // the flux halo can be staged by TMA (descriptors made at creation)
+  int tma_able = 0;
 };
 
 namespace {
@@ -268,7 +272,7 @@ int enqueue_step(hymor_ctx* ctx, bool with_events) {
       CU(cudaEventRecord(ctx->c1_fork[k], sj));
       CU(cudaStreamWaitEvent(ctx->c1, ctx->c1_fork[k], 0));
       TRY(ev_on(4 * k + 2, ctx->c1));
-      launch_flux_class(d, false, F, 1, ctx->c1);
+      launch_flux_class(d, false, F, 1, ctx->c1, 0, d.step_ffv != 0);
       TRY(ev_on(4 * k + 3, ctx->c1));
       CU(cudaEventRecord(ctx->c1_join[k], ctx->c1));
       if (k == 0) {
@@ -281,7 +285,7 @@ int enqueue_step(hymor_ctx* ctx, bool with_events) {
       // the interior flux leaves one block slot per SM to the side-stream kernels and the
       // shock/boundary-class flux
       if (k == 0) CU(cudaStreamWaitEvent(st, ctx->cls_ev, 0));
-      launch_flux_class(d, false, F, 0, st, 1);
+      launch_flux_class(d, false, F, 0, st, d.flux_spare, d.step_ffv != 0);
       TRY(ev(4 * k + 1));
       CU(cudaStreamWaitEvent(st, ctx->c1_join[k], 0));
       if (k == 0) CU(cudaStreamWaitEvent(st, ctx->cfl_ev, 0));  // dt, for the next stage update
@@ -298,7 +302,7 @@ int enqueue_step(hymor_ctx* ctx, bool with_events) {
     launch_update_thermo(d, 0, 0, 0, st);
     launch_shock_bc(d, false, true, shock, 0.0, wA[0], 0, st);
     TRY(ev(0));
-    launch_flux(d, false, F, st);
+    launch_flux_class(d, false, F, -1, st, 0, d.step_ffv != 0);
     TRY(ev(1));
     TRY(ev(2));
     TRY(ev(3));
@@ -308,7 +312,7 @@ int enqueue_step(hymor_ctx* ctx, bool with_events) {
       launch_update_thermo(d, 5, 0, wA[k - 1], st);
       launch_shock_bc(d, false, false, shock, 0.0, wA[k], 0, st);
       TRY(ev(4 * k));
-      launch_flux(d, false, F, st);
+      launch_flux_class(d, false, F, -1, st, 0, d.step_ffv != 0);
       TRY(ev(4 * k + 1));
       TRY(ev(4 * k + 2));
       TRY(ev(4 * k + 3));
@@ -351,7 +355,46 @@ int build_graph(hymor_ctx* ctx) {
   return 0;
 }
 
+// TMA descriptors of the ghosted planes the flux halo reads (kernels.h, DevCtx::tmS ..): 2-D
+// (Nchi + 2) x (Neta + 2) FP64 planes, boxes of 36 x (rows + 2) for tiles of 8 and 16 rows.
+// The encoder is the driver's cuTensorMapEncodeTiled, reached through the runtime's entry-
+// point query (no link against libcuda). Returns 1 when every descriptor was made.
+int make_flux_maps(DevCtx& d) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+      return 0;
+    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  const cuuint64_t pitch = (cuuint64_t)(d.nchi + 2) * sizeof(double);
+  if (pitch % 16) return 0;  // the row pitch of a TMA tensor is a multiple of 16 bytes
+  const cuuint64_t dims[2] = {(cuuint64_t)d.nchi + 2, (cuuint64_t)d.neta + 2};
+  const cuuint64_t strides[1] = {pitch};
+  const cuuint32_t estr[2] = {1, 1};
+  const int rows[2] = {8, 16};
+  auto one = [&](CUtensorMap* m, const double* base, int r) {
+    const cuuint32_t box[2] = {36, (cuuint32_t)r + 2};
+    return encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<double*>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  };
+  for (int ri = 0; ri < 2; ++ri) {
+    const double* sp[4] = {d.S.rho, d.S.ru, d.S.rv, d.S.rE};
+    const double* yp[4] = {d.Y.rho, d.Y.ru, d.Y.rv, d.Y.rE};
+    for (int v = 0; v < 4; ++v)
+      if (!one(&d.tmS[ri][v], sp[v], rows[ri]) || !one(&d.tmY[ri][v], yp[v], rows[ri])) return 0;
+    if (!one(&d.tmP[ri], d.p, rows[ri]) || !one(&d.tmT[ri], d.T, rows[ri])) return 0;
+  }
+  return 1;
+}
+
 int check_err_words(hymor_ctx* ctx, const unsigned* h) {
+  if (h[kErrFlags] & kBitTimeout)
+    return fail(ctx, HYMOR_ERR_TIMEOUT, "a bounded wait for a TMA transfer of the flux halo gave up");
   if (h[kErrFlags] & kBitShockRange)
     return fail(ctx, HYMOR_ERR_SHOCK_RANGE, "shocked cell outside rows 2..Neta-1 (the shock left the mesh)");
   if (h[kErrFlags] & kBitNumeric)
@@ -379,11 +422,18 @@ size_t state_pitch(size_t n) { return (n + 31) & ~size_t(31); }
 size_t header_doubles(size_t n) { return 4 * state_pitch(n) + kScalPitch + (n + 1) / 2; }
 size_t stage_bytes(int n) { return header_doubles(n) * sizeof(double) + kErrCount * sizeof(unsigned); }
 
+void drop_step_graph(hymor_ctx* ctx);
+
 // The stored flux s["flux"] is no longer all zero: a step graph captured while it was
 // (whose CFL kernel skips the stored-flux term) is dropped and captured again.
 void stored_flux_written(hymor_ctx* ctx) {
   if (!ctx->d.sf_zero) return;
   ctx->d.sf_zero = 0;
+  drop_step_graph(ctx);
+}
+
+// The next step captures its graph again (its launches changed).
+void drop_step_graph(hymor_ctx* ctx) {
   if (ctx->gexec) {
     cudaStreamSynchronize(ctx->stream);
     cudaGraphExecDestroy(ctx->gexec);
@@ -537,6 +587,34 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
   {
     std::vector<double> lrg, btg, rvol, rxl, rxb, gvis;
     face_geometry(*cfg, *mesh, lrg, btg, rvol, rxl, rxb, gvis);
+    {  // float-float copies of the planes the viscous terms read: nx, ny, g1, g2/4, 1/(4 len)
+      const long NLR = (long)(cfg->nchi + 1) * cfg->neta, NBT = (long)cfg->nchi * (cfg->neta + 1);
+      const int planes[5] = {0, 1, 3, 4, 5};
+      auto split = [](const std::vector<double>& g, long nf, const int* pl) {
+        std::vector<float2> out(5 * nf);
+        for (int q = 0; q < 5; ++q)
+          for (long f = 0; f < nf; ++f) {
+            const double x = g[pl[q] * nf + f];
+            const float h = (float)x;
+            out[q * nf + f] = make_float2(h, (float)(x - (double)h));
+          }
+        return out;
+      };
+      const std::vector<float2> lf = split(lrg, NLR, planes), bf = split(btg, NBT, planes);
+      float2 *q1 = nullptr, *q2 = nullptr;
+      if (cudaMalloc(&q1, sizeof(float2) * lf.size()) != cudaSuccess ||
+          cudaMalloc(&q2, sizeof(float2) * bf.size()) != cudaSuccess) {
+        if (q1) cudaFree(q1);
+        return bail(fail(ctx, HYMOR_ERR_CUDA, "float-float geometry allocation failed"));
+      }
+      ctx->allocs.push_back(q1);
+      ctx->allocs.push_back(q2);
+      if (cudaMemcpy(q1, lf.data(), sizeof(float2) * lf.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+          cudaMemcpy(q2, bf.data(), sizeof(float2) * bf.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        return bail(fail(ctx, HYMOR_ERR_CUDA, "float-float geometry upload failed"));
+      m.lrf = q1;
+      m.btf = q2;
+    }
     double *p1, *p2, *p3, *p4, *p5, *p6;
     if ((r = upload(ctx, &p1, lrg.data(), lrg.size(), "lr geometry"))) return bail(r);
     if ((r = upload(ctx, &p2, btg.data(), btg.size(), "bt geometry"))) return bail(r);
@@ -600,7 +678,7 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
   if ((r = dalloc(ctx, &d.beta, 2L * d.nchi)) ||
       (r = dalloc(ctx, &d.speed_x, d.nchi)) || (r = dalloc(ctx, &d.speed_y, d.nchi)) ||
       (r = dalloc(ctx, &d.rel, d.nchi)) || (r = dalloc(ctx, &d.spl, 17 * (long)d.nchi + 16)) ||
-      (r = dalloc(ctx, &d.tiles, 2 + 2 * (long)flux_tiles(d))) ||
+      (r = dalloc(ctx, &d.tiles, 2 + 2 * (long)flux_tiles_max(d))) ||
       (r = dalloc(ctx, &d.ticket, 2L)) ||
       (r = dalloc(ctx, &d.cflw, d.NLR + d.NBT)))
     return bail(r);
@@ -616,6 +694,11 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
   d.res_up = nullptr;
   d.bwork = nullptr;
   d.sf_zero = 1;  // the flux arrays are allocated zeroed
+  d.step_ffv = 1;
+  d.flux_rows = 8;
+  d.flux_spare = 1;
+  d.tma = make_flux_maps(d);
+  ctx->tma_able = d.tma;
   for (int k = 0; k < hymor_ctx_s::kEv; ++k)
     if (cudaEventCreate(&ctx->cap_ev[k]) != cudaSuccess) return bail(fail(ctx, HYMOR_ERR_CUDA, "event"));
   for (int k = 0; k < 8; ++k)  // 5 forks and 5 joins per step
@@ -838,6 +921,103 @@ int hymor_bench_steps(hymor_ctx* ctx, int nsteps, uint64_t flush_bytes, float* m
   return read_err(ctx);
 }
 
+int hymor_autotune(hymor_ctx* ctx, int steps, int32_t* choice, float* ms_per_step) {
+  if (!ctx || steps < 1 || !choice) return HYMOR_ERR_INVALID;
+  TRY(set_device(ctx));
+  DevCtx& d = ctx->d;
+  cudaStream_t st = ctx->stream;
+  // what a step changes, saved so that every candidate starts from the same state and the
+  // context leaves the tuning as it entered it
+  struct Part {
+    void* p;
+    size_t bytes;
+  };
+  const size_t n = (size_t)d.nchi;
+  const Part parts[] = {
+      {d.S.rho, sizeof(double) * d.G}, {d.S.ru, sizeof(double) * d.G}, {d.S.rv, sizeof(double) * d.G},
+      {d.S.rE, sizeof(double) * d.G},  {d.aS, sizeof(double) * d.G},   {d.Sp.x, sizeof(double) * n},
+      {d.Sp.y, sizeof(double) * n},    {d.Sp.chi, sizeof(double) * n}, {d.Sp.eta, sizeof(double) * n},
+      {d.cell_idx, sizeof(int) * n},   {d.beta, sizeof(double) * 2 * n}, {d.speed_x, sizeof(double) * n},
+      {d.speed_y, sizeof(double) * n}, {d.rel, sizeof(double) * n},    {d.scal, sizeof(double) * kCount},
+      {d.err, sizeof(unsigned) * kErrCount}};
+  size_t total = 0;
+  for (const Part& q : parts) total += (q.bytes + 255) & ~(size_t)255;
+  unsigned char* save = nullptr;
+  CU(cudaMalloc(&save, total));
+  auto copy = [&](bool store) -> int {
+    size_t off = 0;
+    for (const Part& q : parts) {
+      unsigned char* dst = store ? save + off : static_cast<unsigned char*>(q.p);
+      const unsigned char* src = store ? static_cast<const unsigned char*>(q.p) : save + off;
+      CU(cudaMemcpyAsync(dst, src, q.bytes, cudaMemcpyDeviceToDevice, st));
+      off += (q.bytes + 255) & ~(size_t)255;
+    }
+    return 0;
+  };
+  const bool stale = ctx->a_stale;
+  const int rows0 = d.flux_rows, spare0 = d.flux_spare, tma0 = d.tma;
+  int r = copy(true);
+  // candidates: halo by TMA or by thread loads x tile rows x spare block slots per SM of the
+  // interior grid (without TMA descriptors only the thread-load half)
+  const int rows_c[2] = {8, 16}, spare_c[3] = {0, 1, 2};
+  float best = 0;
+  int bi = -1, c = 0;
+  for (int a = 0; a < 4 && !r; ++a)
+    for (int b = 0; b < 3 && !r; ++b, ++c) {
+      if (ms_per_step) ms_per_step[c] = 0;
+      if ((a >> 1) && !ctx->tma_able) continue;
+      d.tma = a >> 1;
+      d.flux_rows = rows_c[a & 1];
+      d.flux_spare = spare_c[b];
+      drop_step_graph(ctx);
+      float ms = 0;
+      if ((r = copy(false))) break;
+      ctx->a_stale = stale;
+      if ((r = hymor_bench_steps(ctx, 1, 0, &ms))) break;  // capture and warm up
+      if ((r = copy(false))) break;
+      ctx->a_stale = stale;
+      if ((r = hymor_bench_steps(ctx, steps, 0, &ms))) break;
+      ms /= steps;
+      if (ms_per_step) ms_per_step[c] = ms;
+      if (bi < 0 || ms < best) {
+        best = ms;
+        bi = c;
+      }
+    }
+  if (!r) r = copy(false);
+  cudaStreamSynchronize(st);
+  cudaFree(save);
+  ctx->a_stale = stale;
+  if (r || bi < 0) {
+    d.flux_rows = rows0;
+    d.flux_spare = spare0;
+    d.tma = tma0;
+    drop_step_graph(ctx);
+    return r ? r : fail(ctx, HYMOR_ERR_CUDA, "autotune: no candidate ran");
+  }
+  d.tma = bi / 6;
+  d.flux_rows = rows_c[(bi / 3) & 1];
+  d.flux_spare = spare_c[bi % 3];
+  drop_step_graph(ctx);
+  choice[0] = d.flux_rows;
+  choice[1] = d.flux_spare;
+  choice[2] = d.tma;
+  return 0;
+}
+
+int hymor_set_flux_tiling(hymor_ctx* ctx, int rows, int spare, int tma) {
+  if (!ctx || (rows != 8 && rows != 16) || spare < 0 || spare > 4 || tma < 0 || tma > 1) return HYMOR_ERR_INVALID;
+  if (tma && !ctx->tma_able) return fail(ctx, HYMOR_ERR_INVALID, "no TMA descriptors for this grid (Nchi odd)");
+  TRY(set_device(ctx));
+  if (ctx->d.flux_rows != rows || ctx->d.flux_spare != spare || ctx->d.tma != tma) {
+    ctx->d.flux_rows = rows;
+    ctx->d.flux_spare = spare;
+    ctx->d.tma = tma;
+    drop_step_graph(ctx);
+  }
+  return 0;
+}
+
 int hymor_update_flow_cells(hymor_ctx* ctx) {
   if (!ctx) return HYMOR_ERR_INVALID;
   TRY(set_device(ctx));
@@ -874,6 +1054,16 @@ int hymor_counters(hymor_ctx* ctx, int32_t* rho_limited, int32_t* rh_warnings) {
   CU(cudaStreamSynchronize(ctx->stream));
   if (rho_limited) *rho_limited = (int32_t)h[kRhoLimited];
   if (rh_warnings) *rh_warnings = (int32_t)h[kRhWarn];
+  return 0;
+}
+
+int hymor_set_step_viscous(hymor_ctx* ctx, int mode) {
+  if (!ctx || mode < 0 || mode > 1) return HYMOR_ERR_INVALID;
+  if (ctx->d.step_ffv != mode) {
+    TRY(set_device(ctx));
+    ctx->d.step_ffv = mode;
+    drop_step_graph(ctx);
+  }
   return 0;
 }
 

@@ -9,6 +9,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda.h>  // CUtensorMap (the TMA descriptors of the flux halo)
 #include <cuda_runtime.h>
 
 #include "../../include/hymor.h"
@@ -42,6 +43,11 @@ struct DevMesh {
   const double* gvis;   // kv 2 (A_xi^2 + A_eta^2) / vol^2 per cell, kv = max(4/3, gamma/Pr) / Re
                         // (viscous CFL rate over the volume, CFL_TIMESTEP.jl:110-113)
   const double *xt, *yt;  // x_ext, y_ext transposed: ghosted (i, j) at i * (Neta + 2) + j
+  // float-float copies (high, low) of the lr / bt face planes nx, ny, s g1 (s h1), s g2/4
+  // (s h2/4), s/(4 len), 5 x NLR and 5 x NBT, for the float-float viscous terms of the
+  // RK-step flux
+  const float2* lrf;
+  const float2* btf;
 };
 
 struct Cons {
@@ -72,6 +78,13 @@ enum ErrWord {
 enum ErrBit : unsigned {
   kBitNumeric = 1u,
   kBitShockRange = 2u,
+  kBitTimeout = 4u,  // a bounded wait on a TMA transfer gave up
+};
+
+// TMA descriptors of the six halo planes a flux launch reads (rho, rho_u, rho_v, rho_E, p, T
+// of the array evaluated), passed by value as a __grid_constant__ kernel parameter.
+struct FluxMaps {
+  CUtensorMap m[6];
 };
 
 __host__ __device__ inline int gidx(int i, int j, int nchi) { return i + j * (nchi + 2); }  // 0-based ghosted

@@ -20,7 +20,9 @@
 // reciprocal multiplies (frcp).
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 
+#include "ff.cuh"
 #include "kernels.h"
 
 namespace hymor {
@@ -31,16 +33,40 @@ constexpr int TX = 31;           // cells per tile along chi (TX + 1 = 32 lr fac
 constexpr int TY = 8;            // cells per tile along eta
 constexpr int HX = TX + 2;       // halo columns
 constexpr int CX = TX + 1;       // corner columns
-constexpr int kFluxThreads = 256;
-// Tile geometry of a 31 x TYV-cell flux tile (TYV warps, one per tile row).
-template <int TYV>
+// Tile geometry of a 31 x TYV-cell flux tile (TYV warps, one per tile row). With TMA the
+// halo rows are staged 36 doubles wide (kTmaBoxX: the 33 halo columns from an even first
+// column, the 16-byte rule of a TMA box's x coordinate) and each staged plane starts on a
+// 128-byte boundary.
+constexpr int kTmaBoxX = 36;
+template <int TYV, bool TMA = false>
 struct TileGeo {
   static constexpr int NH = HX * (TYV + 2);        // halo cells
+  static constexpr int HP = TMA ? kTmaBoxX : HX;   // halo row pitch in shared memory
+  static constexpr int PS = TMA ? (HP * (TYV + 2) + 15) / 16 * 16 : NH;  // halo plane stride
   static constexpr int NCOR = CX * (TYV + 1);      // corners
   static constexpr int NLRF = (TX + 1) * TYV;      // lr faces
   static constexpr int NBTF = TX * (TYV + 1);      // bt faces
   static constexpr int THREADS = 32 * TYV;
 };
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+// Waits for the mbarrier phase `parity` to complete, for at most ~2^22 polls. Returns
+// whether it completed.
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+  for (int it = 0; it < (1 << 22); ++it) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
 // ceiling of the flux kernels' dynamic shared memory (above the 48 KB default)
 constexpr size_t kFluxMaxSmem = 120 * 1024;
 
@@ -1032,6 +1058,8 @@ struct FluxArgs {
   // heat flux k gamma / (Re Pr) dT/dn (CPG: mu* = k* = 1; Sutherland: both times mu_f).
   double kpr;
   double suthS, Tinf_inv;
+  float2 kprf, c23f;       // kpr and 2/3 as float-float (the float-float viscous variant)
+  unsigned* err;           // device error word (TMA wait timeouts)
   int nchi, neta;
   int mask;                // shock fitting with feedback: zero flux at j >= sc
   int shock;
@@ -1050,21 +1078,21 @@ struct FluxArgs {
 // rows (zero flux under the NON_LINEAR_DYNAMICS mask, never read by the stage update)
 // are left out. lists: [count0, count1, class 0 tiles (ntiles), class 1 tiles (ntiles)].
 __global__ void k_classify_tiles(const int* __restrict__ cell_idx, int* lists, int nchi, int neta, int tiles_x,
-                                 int ntiles, int shock, int mask) {
+                                 int ntiles, int shock, int mask, int ty) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntiles) return;
-  const int i0 = (t % tiles_x) * TX, j0 = (t / tiles_x) * TY;
+  const int i0 = (t % tiles_x) * TX, j0 = (t / tiles_x) * ty;
   if (mask) {
     int sc = 0;
     for (int c = i0; c < i0 + TX && c < nchi; ++c) sc = max(sc, cell_idx[c]);
     if (j0 + 1 >= sc) return;
   }
-  bool inner = i0 >= 1 && i0 + TX + 1 <= nchi && j0 >= 1 && j0 + TY + 1 <= neta;
+  bool inner = i0 >= 1 && i0 + TX + 1 <= nchi && j0 >= 1 && j0 + ty + 1 <= neta;
   if (shock) {
     int scmin = 0x7fffffff;
     for (int c = i0 - 1; c <= i0 + TX; ++c)
       if (c >= 0 && c < nchi) scmin = min(scmin, cell_idx[c]);
-    inner = inner && (j0 + TY + 1 < scmin);
+    inner = inner && (j0 + ty + 1 < scmin);
   }
   const int cls = inner ? 0 : 1;
   lists[2 + cls * ntiles + atomicAdd(&lists[cls], 1)] = t;
@@ -1072,28 +1100,88 @@ __global__ void k_classify_tiles(const int* __restrict__ cell_idx, int* lists, i
 
 // One 31 x TYV-cell tile (bx, by) of the residual, TYV warps (one per tile row); every
 // thread of the block takes part.
-template <bool AXI, bool SUTH, int TYV>
-__device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, double* sm) {
-  using G = TileGeo<TYV>;
+// The viscous part of one face in float-float arithmetic (the FP64 form, with its
+// derivation, is in flux_tile): u, v, T of the two cells A (left / bottom) and B (right /
+// top) and the corner sums at the face's two ends (lo, hi), the face's float-float planes
+// (nx, ny, s g1, s g2/4, s/(4 len)). LR: an lr face (sg = 1), else a bt face (sg = -1).
+// Returns twice the traction (tx, ty), twice the heat flux qn, and for the axisymmetric
+// hoop stress -2/3 div + 2 u_f / x_f (the caller scales it by mu_f / 2).
+template <bool LR, bool AXI>
+__device__ __forceinline__ void visc_face_ff(const ff* fu, const ff* fv, const ff* fT, int A, int B, const ff* fuc,
+                                             const ff* fvc, const ff* fTc, int lo, int hi, const float2* pl, long NF,
+                                             long f, double rxd, float2 kprf, float2 c23f, double& tx, double& ty,
+                                             double& qn, double& hoop) {
+  const ff nx = *reinterpret_cast<const ff*>(pl + f), ny = *reinterpret_cast<const ff*>(pl + NF + f);
+  const ff g1 = *reinterpret_cast<const ff*>(pl + 2 * NF + f), g2 = *reinterpret_cast<const ff*>(pl + 3 * NF + f);
+  const ff il = *reinterpret_cast<const ff*>(pl + 4 * NF + f);
+  const ff dUc = ff_sub(fuc[hi], fuc[lo]), dVc = ff_sub(fvc[hi], fvc[lo]), dTc = ff_sub(fTc[hi], fTc[lo]);
+  const ff du_dn = ff_add(ff_mul(g1, ff_sub(fu[B], fu[A])), ff_mul(g2, dUc));
+  const ff dv_dn = ff_add(ff_mul(g1, ff_sub(fv[B], fv[A])), ff_mul(g2, dVc));
+  const ff dT_dn = ff_add(ff_mul(g1, ff_sub(fT[B], fT[A])), ff_mul(g2, dTc));
+  ff du_dt = ff_mul(dUc, il), dv_dt = ff_mul(dVc, il);
+  if (!LR) {
+    du_dt = ff_neg(du_dt);
+    dv_dt = ff_neg(dv_dt);
+  }
+  const ff Dn = ff_add(ff_mul(du_dn, nx), ff_mul(dv_dn, ny));
+  const ff En = ff_add(ff_mul(du_dt, nx), ff_mul(dv_dt, ny));
+  const ff Et = ff_sub(ff_mul(du_dt, ny), ff_mul(dv_dt, nx));
+  ff div = LR ? ff_sub(Et, Dn) : ff_add(Et, Dn);
+  ff uf{0.f, 0.f}, rx{0.f, 0.f};
+  if (AXI) {
+    rx = ff_from_double(rxd);
+    uf = ff_scale2(ff_add(fu[B], fu[A]), 0.5f);
+    div = ff_add(div, ff_mul(uf, rx));
+  }
+  const ff c23 = *reinterpret_cast<const ff*>(&c23f);
+  const ff al = ff_add(ff_mul(LR ? c23 : ff_neg(c23), div), Dn);
+  const ff Ey = ff_mul(En, ny), Ex = ff_mul(En, nx);
+  const ff txf = ff_add(ff_mul(al, nx), LR ? ff_sub(du_dn, Ey) : ff_add(du_dn, Ey));
+  const ff tyf = ff_add(ff_mul(al, ny), LR ? ff_add(dv_dn, Ex) : ff_sub(dv_dn, Ex));
+  const ff qf = ff_mul(*reinterpret_cast<const ff*>(&kprf), dT_dn);
+  tx = ff_to_double(txf);
+  ty = ff_to_double(tyf);
+  qn = ff_to_double(qf);
+  if (AXI) hoop = ff_to_double(ff_add(ff_mul(ff_neg(c23), div), ff_mul(ff_scale2(uf, 2.f), rx)));
+}
+
+// Returns false when a TMA wait gave up (the block then stops).
+template <bool AXI, bool SUTH, int TYV, bool FFV, bool TMA>
+__device__ __forceinline__ bool flux_tile(const FluxArgs& a, const FluxMaps& tm, int bx, int by, double* sm,
+                                          uint64_t* bar, unsigned& phase) {
+  using G = TileGeo<TYV, TMA>;
+  // halo planes; with TMA the first six are the staged copies of the ghosted planes
   double* s_r = sm;
-  double* s_u = s_r + G::NH;   // u = rho_u / rho
-  double* s_v = s_u + G::NH;
-  double* s_ru = s_v + G::NH;
-  double* s_rv = s_ru + G::NH;
-  double* s_rE = s_rv + G::NH;
-  double* s_p = s_rE + G::NH;
-  double* s_T = s_p + G::NH;
-  double* s_uc = s_T + G::NH;
+  double* s_ru = s_r + G::PS;
+  double* s_rv = s_ru + G::PS;
+  double* s_rE = s_rv + G::PS;
+  double* s_p = s_rE + G::PS;
+  double* s_T = s_p + G::PS;
+  double* s_u = s_T + G::PS;   // u = rho_u / rho
+  double* s_v = s_u + G::PS;
+  double* s_uc = s_v + G::PS;
   double* s_vc = s_uc + G::NCOR;
   double* s_Tc = s_vc + G::NCOR;
   double* f_lr = s_Tc + G::NCOR;                // 4 x G::NLRF
   double* f_bt = f_lr + 4 * G::NLRF;            // 4 x G::NBTF
   double* t_lr = f_bt + 4 * G::NBTF;            // AXI hoop stress on faces
   double* t_bt = t_lr + (AXI ? G::NLRF : 0);
+  // the float-float variant keeps u, v, T and the corner sums as float-float pairs in the
+  // same shared slots (8 bytes per entry either way)
+  ff* fu = reinterpret_cast<ff*>(s_u);
+  ff* fv = reinterpret_cast<ff*>(s_v);
+  ff* fT = reinterpret_cast<ff*>(s_T);
+  ff* fuc = reinterpret_cast<ff*>(s_uc);
+  ff* fvc = reinterpret_cast<ff*>(s_vc);
+  ff* fTc = reinterpret_cast<ff*>(s_Tc);
 
   const int nchi = a.nchi, neta = a.neta;
   const int i0 = bx * TX, j0 = by * TYV;  // first interior cell (0-based)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // shared index of halo cell (hx, hy) = ghosted (i0 + hx, j0 + hy); with TMA the staged rows
+  // start at the even column i0 - (i0 & 1)
+  const int xo = TMA ? (i0 & 1) : 0;
+  auto hid = [&](int hx, int hy) { return hx + xo + hy * G::HP; };
 
   if (a.tile_class >= 0 && !a.list) {
     // the halo (ghosted columns i0..i0+TX+1, rows j0..j0+TYV+1) avoids every ghost cell and
@@ -1109,7 +1197,7 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, dou
       for (int o = 16; o > 0; o >>= 1) scmin = min(scmin, __shfl_xor_sync(0xffffffffu, scmin, o));
       inner = inner && (j0 + TYV + 1 < scmin);
     }
-    if (inner != (a.tile_class == 0)) return;
+    if (inner != (a.tile_class == 0)) return true;
   }
 
   // whole tile at or above the shocked rows: flux is zero (NON_LINEAR_DYNAMICS mask)
@@ -1124,23 +1212,61 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, dou
         const long c = (long)ci + (long)cj * nchi;
         a.o0[c] = 0; a.o1[c] = 0; a.o2[c] = 0; a.o3[c] = 0;
       }
-      return;
+      return true;
     }
   }
 
+  if (TMA) {
+    // (1a) the six halo planes by TMA: boxes of 36 x (TYV + 2) doubles from the even column
+    // i0 - xo and row j0 (cells past the ghost layer read as zero and are never used)
+    if (tid == 0) {
+      const unsigned b = smem_u32(bar);
+      // earlier generic-proxy reads of these buffers come before the async-proxy writes
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b),
+                   "r"((unsigned)(6 * G::HP * (TYV + 2) * sizeof(double)))
+                   : "memory");
+      double* dst[6] = {s_r, s_ru, s_rv, s_rE, s_p, s_T};
+#pragma unroll
+      for (int q = 0; q < 6; ++q)
+        asm volatile(
+            "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+            "[%4];" ::"r"(smem_u32(dst[q])),
+            "l"(&tm.m[q]), "r"(i0 - xo), "r"(j0), "r"(b)
+            : "memory");
+    }
+    const bool ok = mbar_wait(smem_u32(bar), phase);
+    phase ^= 1u;
+    if (!__syncthreads_and(ok)) {
+      if (tid == 0) atomicOr(a.err, kBitTimeout);
+      return false;
+    }
+  }
   // (1) halo cells: ghosted (i0 + hx, j0 + hy)
-  for (int h = tid; h < G::NH; h += G::THREADS) {
-    const int hx = h % HX, hy = h / HX;
+  for (int h0 = tid; h0 < G::NH; h0 += G::THREADS) {
+    const int hx = h0 % HX, hy = h0 / HX;
+    const int h = hid(hx, hy);
     const int gi = i0 + hx, gj = j0 + hy;
     if (gi <= nchi + 1 && gj <= neta + 1) {
-      const long g = (long)gi + (long)gj * (nchi + 2);
-      const double r = a.rho[g], ru = a.ru[g], rv = a.rv[g];
+      double r, ru, rv, T;
+      if (TMA) {
+        r = s_r[h]; ru = s_ru[h]; rv = s_rv[h]; T = s_T[h];
+      } else {
+        const long g = (long)gi + (long)gj * (nchi + 2);
+        r = a.rho[g]; ru = a.ru[g]; rv = a.rv[g];
+        s_r[h] = r; s_ru[h] = ru; s_rv[h] = rv; s_rE[h] = a.rE[g];
+        s_p[h] = a.p[g];
+        T = a.T[g];
+      }
       const double ir = frcp(r);
-      s_r[h] = r; s_ru[h] = ru; s_rv[h] = rv; s_rE[h] = a.rE[g];
-      s_u[h] = ru * ir; s_v[h] = rv * ir;
-      s_p[h] = a.p[g];
-      const double T = a.T[g];
-      s_T[h] = T;
+      if (FFV) {
+        fu[h] = ff_from_double(ru * ir);
+        fv[h] = ff_from_double(rv * ir);
+        fT[h] = ff_from_double(T);
+      } else {
+        s_u[h] = ru * ir; s_v[h] = rv * ir;
+        s_T[h] = T;
+      }
     }
   }
   __syncthreads();
@@ -1148,11 +1274,17 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, dou
   for (int cidx = tid; cidx < G::NCOR; cidx += G::THREADS) {
     const int cx = cidx % CX, cy = cidx / CX;
     if (i0 + cx <= nchi && j0 + cy <= neta) {
-      const int h00 = cx + cy * HX, h10 = h00 + 1, h01 = h00 + HX, h11 = h01 + 1;
+      const int h00 = hid(cx, cy), h10 = h00 + 1, h01 = h00 + G::HP, h11 = h01 + 1;
       // four times the corner averages: the 1/4 is folded into the g2/h2 and 1/len planes
-      s_uc[cidx] = s_u[h00] + s_u[h10] + s_u[h01] + s_u[h11];
-      s_vc[cidx] = s_v[h00] + s_v[h10] + s_v[h01] + s_v[h11];
-      s_Tc[cidx] = s_T[h00] + s_T[h10] + s_T[h01] + s_T[h11];
+      if (FFV) {
+        fuc[cidx] = ff_add(ff_add(fu[h00], fu[h10]), ff_add(fu[h01], fu[h11]));
+        fvc[cidx] = ff_add(ff_add(fv[h00], fv[h10]), ff_add(fv[h01], fv[h11]));
+        fTc[cidx] = ff_add(ff_add(fT[h00], fT[h10]), ff_add(fT[h01], fT[h11]));
+      } else {
+        s_uc[cidx] = s_u[h00] + s_u[h10] + s_u[h01] + s_u[h11];
+        s_vc[cidx] = s_v[h00] + s_v[h10] + s_v[h01] + s_v[h11];
+        s_Tc[cidx] = s_T[h00] + s_T[h10] + s_T[h01] + s_T[h11];
+      }
     }
   }
   __syncthreads();
@@ -1164,55 +1296,66 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, dou
     if (gi <= nchi && gj < neta) {
       const long f = (long)gi + (long)gj * (nchi + 1);
       const double nx = a.m.lrg[f], ny = a.m.lrg[NLR + f], Ah = a.m.lrg[2 * NLR + f];
-      const double g1 = a.m.lrg[3 * NLR + f], g2 = a.m.lrg[4 * NLR + f], il = a.m.lrg[5 * NLR + f];
-      const int L = fx + (fy + 1) * HX, R = L + 1;
+      const int L = hid(fx, fy + 1), R = L + 1;
       const int clo = fx + fy * CX, chi_ = clo + CX;
       const double Sr = s_r[L] + s_r[R], Su = s_ru[L] + s_ru[R], Sv = s_rv[L] + s_rv[R];
       const double SE = s_rE[L] + s_rE[R], Sp = s_p[L] + s_p[R];
       const double ir = frcp(Sr);
       const double m2 = fma(Su, nx, Sv * ny);
       const double Vn = m2 * ir;
-      // viscous (VISCOUS_FLUX.jl:98-133)
-      const double dUc = s_uc[chi_] - s_uc[clo], dVc = s_vc[chi_] - s_vc[clo], dTc = s_Tc[chi_] - s_Tc[clo];
-      const double du_dn = fma(g1, s_u[R] - s_u[L], g2 * dUc);
-      const double dv_dn = fma(g1, s_v[R] - s_v[L], g2 * dVc);
-      const double dT_dn = fma(g1, s_T[R] - s_T[L], g2 * dTc);
-      const double du_dt = dUc * il, dv_dt = dVc * il;
-      // With D = (du_dn, dv_dn), E = (du_dt, dv_dt), n and t = (ny, -nx) the face frame of
-      // VISCOUS_FLUX.jl:98-133 has dun_dn = -D.n, dut_dn = D.t, dun_dt = -E.n, dut_dt = E.t,
-      // and the traction t = -tau11 n + tau12 t with tau11 = mu (2 dun_dn - 2/3 div),
-      // tau12 = mu (dun_dt + dut_dn) is, expanding D in the (n, t) basis,
-      //   t = mu (D + (D.n + 2/3 div) n - (E.n) t),   div = E.t - D.n (+ u/x axisymmetric)
-      const double Dn = fma(du_dn, nx, dv_dn * ny);
-      const double En = fma(du_dt, nx, dv_dt * ny);
-      const double Et = fma(du_dt, ny, -dv_dt * nx);
-      double div = Et - Dn;
-      double kpr = a.kpr;  // gamma / Pr: the heat flux from the 2/Re-scaled temperature gradient
-      double mu_f = 1;
-      if (SUTH) {  // Sutherland at the face temperature
-        const double Ts = (s_T[L] + s_T[R]) * 0.5 * a.Tinf_inv;
-        mu_f = Ts * sqrt(Ts) * (1 + a.suthS) * frcp(Ts + a.suthS);
-        kpr *= mu_f;
+      double tx, ty, qn, hoop = 0, mu_f = 1;
+      if (FFV) {
+        visc_face_ff<true, AXI>(fu, fv, fT, L, R, fuc, fvc, fTc, clo, chi_, a.m.lrf, NLR, f,
+                                AXI ? a.m.rx_lr[f] : 0.0, a.kprf, a.c23f, tx, ty, qn, hoop);
+        if (SUTH) {  // Sutherland at the face temperature
+          const double Ts = (ff_to_double(fT[L]) + ff_to_double(fT[R])) * 0.5 * a.Tinf_inv;
+          mu_f = Ts * sqrt(Ts) * (1 + a.suthS) * frcp(Ts + a.suthS);
+          tx *= mu_f; ty *= mu_f; qn *= mu_f;
+        }
+      } else {
+        const double g1 = a.m.lrg[3 * NLR + f], g2 = a.m.lrg[4 * NLR + f], il = a.m.lrg[5 * NLR + f];
+        // viscous (VISCOUS_FLUX.jl:98-133)
+        const double dUc = s_uc[chi_] - s_uc[clo], dVc = s_vc[chi_] - s_vc[clo], dTc = s_Tc[chi_] - s_Tc[clo];
+        const double du_dn = fma(g1, s_u[R] - s_u[L], g2 * dUc);
+        const double dv_dn = fma(g1, s_v[R] - s_v[L], g2 * dVc);
+        const double dT_dn = fma(g1, s_T[R] - s_T[L], g2 * dTc);
+        const double du_dt = dUc * il, dv_dt = dVc * il;
+        // With D = (du_dn, dv_dn), E = (du_dt, dv_dt), n and t = (ny, -nx) the face frame of
+        // VISCOUS_FLUX.jl:98-133 has dun_dn = -D.n, dut_dn = D.t, dun_dt = -E.n, dut_dt = E.t,
+        // and the traction t = -tau11 n + tau12 t with tau11 = mu (2 dun_dn - 2/3 div),
+        // tau12 = mu (dun_dt + dut_dn) is, expanding D in the (n, t) basis,
+        //   t = mu (D + (D.n + 2/3 div) n - (E.n) t),   div = E.t - D.n (+ u/x axisymmetric)
+        const double Dn = fma(du_dn, nx, dv_dn * ny);
+        const double En = fma(du_dt, nx, dv_dt * ny);
+        const double Et = fma(du_dt, ny, -dv_dt * nx);
+        double div = Et - Dn;
+        double kpr = a.kpr;  // gamma / Pr: the heat flux from the 2/Re-scaled temperature gradient
+        if (SUTH) {  // Sutherland at the face temperature
+          const double Ts = (s_T[L] + s_T[R]) * 0.5 * a.Tinf_inv;
+          mu_f = Ts * sqrt(Ts) * (1 + a.suthS) * frcp(Ts + a.suthS);
+          kpr *= mu_f;
+        }
+        double uf = 0, rx = 0;
+        if (AXI) {
+          rx = a.m.rx_lr[f];
+          uf = (s_u[R] + s_u[L]) * 0.5;
+          div = fma(uf, rx, div);
+        }
+        // twice the traction, the work and the heat flux: (2 t) (A/2) = t A
+        const double al = fma(2.0 / 3.0, div, Dn);
+        tx = fma(al, nx, fma(-En, ny, du_dn));
+        ty = fma(al, ny, fma(En, nx, dv_dn));
+        if (SUTH) { tx *= mu_f; ty *= mu_f; }
+        qn = kpr * dT_dn;
+        if (AXI) hoop = fma(-2.0 / 3.0, div, 2 * uf * rx);
       }
-      double uf = 0, rx = 0;
-      if (AXI) {
-        rx = a.m.rx_lr[f];
-        uf = (s_u[R] + s_u[L]) * 0.5;
-        div = fma(uf, rx, div);
-      }
-      // twice the traction, the work and the heat flux: (2 t) (A/2) = t A
-      const double al = fma(2.0 / 3.0, div, Dn);
-      double tx = fma(al, nx, fma(-En, ny, du_dn));
-      double ty = fma(al, ny, fma(En, nx, dv_dn));
-      if (SUTH) { tx *= mu_f; ty *= mu_f; }
       const double w = fma(Su, tx, Sv * ty) * ir;
-      const double qn = kpr * dT_dn;
       const int o = fx + fy * (TX + 1);
       f_lr[o] = m2 * Ah;
       f_lr[G::NLRF + o] = fma(Su, Vn, fma(Sp, nx, tx)) * Ah;
       f_lr[2 * G::NLRF + o] = fma(Sv, Vn, fma(Sp, ny, ty)) * Ah;
       f_lr[3 * G::NLRF + o] = fma(SE + Sp, Vn, w + qn) * Ah;
-      if (AXI) t_lr[o] = (0.5 * mu_f) * fma(-2.0 / 3.0, div, 2 * uf * rx);
+      if (AXI) t_lr[o] = (0.5 * mu_f) * hoop;
     }
   }
   // (3b) bt faces: TX x (TYV + 1)
@@ -1223,50 +1366,61 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, dou
     if (gi < nchi && gj <= neta) {
       const long f = (long)gi + (long)gj * nchi;
       const double nx = a.m.btg[f], ny = a.m.btg[NBT + f], Ah = a.m.btg[2 * NBT + f];
-      const double h1 = a.m.btg[3 * NBT + f], h2 = a.m.btg[4 * NBT + f], il = a.m.btg[5 * NBT + f];
-      const int B = (fx + 1) + fy * HX, Tt = B + HX;
+      const int B = hid(fx + 1, fy), Tt = B + G::HP;
       const int clo = fx + fy * CX, chi_ = clo + 1;
       const double Sr = s_r[B] + s_r[Tt], Su = s_ru[B] + s_ru[Tt], Sv = s_rv[B] + s_rv[Tt];
       const double SE = s_rE[B] + s_rE[Tt], Sp = s_p[B] + s_p[Tt];
       const double ir = frcp(Sr);
       const double m2 = fma(Su, nx, Sv * ny);
       const double Vn = m2 * ir;
-      const double dUc = s_uc[chi_] - s_uc[clo], dVc = s_vc[chi_] - s_vc[clo], dTc = s_Tc[chi_] - s_Tc[clo];
-      const double du_dn = fma(h1, s_u[Tt] - s_u[B], h2 * dUc);
-      const double dv_dn = fma(h1, s_v[Tt] - s_v[B], h2 * dVc);
-      const double dT_dn = fma(h1, s_T[Tt] - s_T[B], h2 * dTc);
-      const double du_dt = -dUc * il, dv_dt = -dVc * il;
-      // bt frame: dun_dn = D.n, dut_dn = D.t, dun_dt = E.n, dut_dt = E.t, traction
-      // tau22 n + tau21 t = mu (D + (D.n - 2/3 div) n + (E.n) t), div = E.t + D.n
-      const double Dn = fma(du_dn, nx, dv_dn * ny);
-      const double En = fma(du_dt, nx, dv_dt * ny);
-      const double Et = fma(du_dt, ny, -dv_dt * nx);
-      double div = Et + Dn;
-      double kpr = a.kpr;
-      double mu_f = 1;
-      if (SUTH) {
-        const double Ts = (s_T[B] + s_T[Tt]) * 0.5 * a.Tinf_inv;
-        mu_f = Ts * sqrt(Ts) * (1 + a.suthS) * frcp(Ts + a.suthS);
-        kpr *= mu_f;
+      double tx, ty, qn, hoop = 0, mu_f = 1;
+      if (FFV) {
+        visc_face_ff<false, AXI>(fu, fv, fT, B, Tt, fuc, fvc, fTc, clo, chi_, a.m.btf, NBT, f,
+                                 AXI ? a.m.rx_bt[f] : 0.0, a.kprf, a.c23f, tx, ty, qn, hoop);
+        if (SUTH) {
+          const double Ts = (ff_to_double(fT[B]) + ff_to_double(fT[Tt])) * 0.5 * a.Tinf_inv;
+          mu_f = Ts * sqrt(Ts) * (1 + a.suthS) * frcp(Ts + a.suthS);
+          tx *= mu_f; ty *= mu_f; qn *= mu_f;
+        }
+      } else {
+        const double h1 = a.m.btg[3 * NBT + f], h2 = a.m.btg[4 * NBT + f], il = a.m.btg[5 * NBT + f];
+        const double dUc = s_uc[chi_] - s_uc[clo], dVc = s_vc[chi_] - s_vc[clo], dTc = s_Tc[chi_] - s_Tc[clo];
+        const double du_dn = fma(h1, s_u[Tt] - s_u[B], h2 * dUc);
+        const double dv_dn = fma(h1, s_v[Tt] - s_v[B], h2 * dVc);
+        const double dT_dn = fma(h1, s_T[Tt] - s_T[B], h2 * dTc);
+        const double du_dt = -dUc * il, dv_dt = -dVc * il;
+        // bt frame: dun_dn = D.n, dut_dn = D.t, dun_dt = E.n, dut_dt = E.t, traction
+        // tau22 n + tau21 t = mu (D + (D.n - 2/3 div) n + (E.n) t), div = E.t + D.n
+        const double Dn = fma(du_dn, nx, dv_dn * ny);
+        const double En = fma(du_dt, nx, dv_dt * ny);
+        const double Et = fma(du_dt, ny, -dv_dt * nx);
+        double div = Et + Dn;
+        double kpr = a.kpr;
+        if (SUTH) {
+          const double Ts = (s_T[B] + s_T[Tt]) * 0.5 * a.Tinf_inv;
+          mu_f = Ts * sqrt(Ts) * (1 + a.suthS) * frcp(Ts + a.suthS);
+          kpr *= mu_f;
+        }
+        double uf = 0, rx = 0;
+        if (AXI) {
+          rx = a.m.rx_bt[f];
+          uf = (s_u[Tt] + s_u[B]) * 0.5;
+          div = fma(uf, rx, div);
+        }
+        const double al = fma(-2.0 / 3.0, div, Dn);
+        tx = fma(al, nx, fma(En, ny, du_dn));
+        ty = fma(al, ny, fma(-En, nx, dv_dn));
+        if (SUTH) { tx *= mu_f; ty *= mu_f; }
+        qn = kpr * dT_dn;
+        if (AXI) hoop = fma(-2.0 / 3.0, div, 2 * uf * rx);
       }
-      double uf = 0, rx = 0;
-      if (AXI) {
-        rx = a.m.rx_bt[f];
-        uf = (s_u[Tt] + s_u[B]) * 0.5;
-        div = fma(uf, rx, div);
-      }
-      const double al = fma(-2.0 / 3.0, div, Dn);
-      double tx = fma(al, nx, fma(En, ny, du_dn));
-      double ty = fma(al, ny, fma(-En, nx, dv_dn));
-      if (SUTH) { tx *= mu_f; ty *= mu_f; }
       const double w = fma(Su, tx, Sv * ty) * ir;
-      const double qn = kpr * dT_dn;
       const int o = fx + fy * TX;
       f_bt[o] = m2 * Ah;
       f_bt[G::NBTF + o] = fma(Su, Vn, fma(Sp, nx, -tx)) * Ah;
       f_bt[2 * G::NBTF + o] = fma(Sv, Vn, fma(Sp, ny, -ty)) * Ah;
       f_bt[3 * G::NBTF + o] = fma(SE + Sp, Vn, -(w + qn)) * Ah;
-      if (AXI) t_bt[o] = (0.5 * mu_f) * fma(-2.0 / 3.0, div, 2 * uf * rx);
+      if (AXI) t_bt[o] = (0.5 * mu_f) * hoop;
     }
   }
   __syncthreads();
@@ -1287,7 +1441,7 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, dou
         double v2 = f_lr[2 * G::NLRF + w] - f_lr[2 * G::NLRF + e] + f_bt[2 * G::NBTF + s] - f_bt[2 * G::NBTF + n];
         if (AXI) {
           // FLUX_MOMENTUM_3D.jl:120-122: front/back pressure with sign(y) of the cell centre
-          const double pc = s_p[(cx + 1) + (cy + 1) * HX];
+          const double pc = s_p[hid(cx + 1, cy + 1)];
           const double ycell = a.m.y_ext[(long)(ci + 1) + (long)(cj + 1) * (nchi + 2)];
           v2 += (pc * a.m.fb_yn_front - pc * a.m.fb_yn_back) * a.m.fb_area[c] * jsign(ycell);
           // VISCOUS_FLUX_3D.jl:154-177: hoop stress, radius = x of the cell centre
@@ -1301,28 +1455,41 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, dou
       a.o0[c] = r0; a.o1[c] = r1; a.o2[c] = r2; a.o3[c] = r3;
     }
   }
+  return true;
 }
 
 // Tile grid (no list), or a persistent grid striding over the compact tile list of a class.
-template <bool AXI, bool SUTH, int TYV>
-__global__ void __launch_bounds__(32 * TYV, 32 / TYV) k_flux(FluxArgs a) {
-  extern __shared__ double sm[];
+template <bool AXI, bool SUTH, int TYV, bool FFV, bool TMA>
+__global__ void __launch_bounds__(32 * TYV, 32 / TYV) k_flux(FluxArgs a, const __grid_constant__ FluxMaps tm) {
+  extern __shared__ double sm_raw[];
+  __shared__ uint64_t bar;  // completion of the halo TMA transfers of a tile
+  // TMA destinations start on a 128-byte boundary (128 bytes of slack in the launch's size)
+  double* sm = TMA ? reinterpret_cast<double*>((reinterpret_cast<uintptr_t>(sm_raw) + 127) & ~uintptr_t(127)) : sm_raw;
+  unsigned phase = 0;
+  if (TMA) {
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar)) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+  }
   if (!a.list) {
-    flux_tile<AXI, SUTH, TYV>(a, blockIdx.x, blockIdx.y, sm);
+    flux_tile<AXI, SUTH, TYV, FFV, TMA>(a, tm, blockIdx.x, blockIdx.y, sm, &bar, phase);
     return;
   }
   const int n = *a.count;
   for (int k = blockIdx.x; k < n; k += gridDim.x) {
     const int t = a.list[k];
-    flux_tile<AXI, SUTH, TYV>(a, t % a.tiles_x, t / a.tiles_x, sm);
+    if (!flux_tile<AXI, SUTH, TYV, FFV, TMA>(a, tm, t % a.tiles_x, t / a.tiles_x, sm, &bar, phase)) return;
     __syncthreads();  // the next tile reuses the shared arrays
   }
 }
 
-template <bool AXI, bool SUTH, int TYV = TY>
+template <bool AXI, bool SUTH, int TYV = TY, bool TMA = false>
 size_t flux_smem() {
-  using G = TileGeo<TYV>;
-  return sizeof(double) * (8 * G::NH + 3 * G::NCOR + 4 * G::NLRF + 4 * G::NBTF + (AXI ? G::NLRF + G::NBTF : 0));
+  using G = TileGeo<TYV, TMA>;
+  return sizeof(double) * (8 * G::PS + 3 * G::NCOR + 4 * G::NLRF + 4 * G::NBTF + (AXI ? G::NLRF + G::NBTF : 0)) +
+         (TMA ? 128 : 0);
 }
 
 // ---------------------------------------------------------------------------
@@ -1845,31 +2012,56 @@ void launch_shock_bc_flags(const DevCtx& d, bool on_S, bool copy_pts, bool do_sh
   launch_shock_bc_impl(d, on_S, copy_pts, false, 0, 0, a_mode, do_shock, do_bc, st);
 }
 
-// resident flux blocks per SM of each variant (index 2 axisymmetric + Sutherland)
-int g_flux_blocks_per_sm[4] = {3, 3, 3, 3};
+// resident flux blocks per SM of each variant (index 16 TMA + 8 (16-row tiles) + 4 float-float +
+// 2 axisymmetric + Sutherland)
+int g_flux_blocks_per_sm[32];
 
+// a double as a float-float pair (high: nearest float, low: the nearest float to the rest)
+float2 host_ff(double x) {
+  const float h = (float)x;
+  return make_float2(h, (float)(x - (double)h));
+}
+
+int flux_rows(const DevCtx& d) { return d.flux_rows == 16 ? 16 : TY; }
 int flux_tiles_x(const DevCtx& d) { return (d.nchi + TX - 1) / TX; }
-int flux_tiles(const DevCtx& d) { return flux_tiles_x(d) * ((d.neta + TY - 1) / TY); }
+int flux_tiles(const DevCtx& d) { return flux_tiles_x(d) * ((d.neta + flux_rows(d) - 1) / flux_rows(d)); }
+int flux_tiles_max(const DevCtx& d) { return flux_tiles_x(d) * ((d.neta + TY - 1) / TY); }
 
 void launch_classify_tiles(const DevCtx& d, cudaStream_t st) {
   const int nt = flux_tiles(d);
   cudaMemsetAsync(d.tiles, 0, 2 * sizeof(int), st);
   k_classify_tiles<<<(nt + 127) / 128, 128, 0, st>>>(d.cell_idx, d.tiles, d.nchi, d.neta, flux_tiles_x(d), nt,
-                                                   d.cfg.shock_enabled, d.cfg.shock_enabled && d.cfg.shock_feedback);
+                                                   d.cfg.shock_enabled, d.cfg.shock_enabled && d.cfg.shock_feedback,
+                                                   flux_rows(d));
 }
 
-template <bool AXI, bool SUTH>
-void flux_launch(const FluxArgs& a, int tile_class, dim3 grid, const DevCtx& d, cudaStream_t st) {
+template <bool AXI, bool SUTH, bool FFV, int TYV, bool TMA>
+void flux_launch_rows(const FluxArgs& a, const FluxMaps& tm, int tile_class, dim3 grid, const DevCtx& d,
+                      cudaStream_t st) {
+  const size_t smem = flux_smem<AXI, SUTH, TYV, TMA>();
   if (tile_class == 1 && a.list) {
     // the shock/boundary class: a persistent grid of one block per SM over its few tiles
-    k_flux<AXI, SUTH, TY><<<d.sms, kFluxThreads, flux_smem<AXI, SUTH>(), st>>>(a);
+    k_flux<AXI, SUTH, TYV, FFV, TMA><<<d.sms, 32 * TYV, smem, st>>>(a, tm);
   } else {
-    k_flux<AXI, SUTH, TY><<<grid, kFluxThreads, flux_smem<AXI, SUTH>(), st>>>(a);
+    k_flux<AXI, SUTH, TYV, FFV, TMA><<<grid, 32 * TYV, smem, st>>>(a, tm);
+  }
+}
+
+template <bool AXI, bool SUTH, bool FFV>
+void flux_launch(const FluxArgs& a, const FluxMaps& tm, int tile_class, dim3 grid, const DevCtx& d,
+                 cudaStream_t st) {
+  const bool r16 = flux_rows(d) == 16;
+  if (d.tma) {
+    if (r16) flux_launch_rows<AXI, SUTH, FFV, 16, true>(a, tm, tile_class, grid, d, st);
+    else flux_launch_rows<AXI, SUTH, FFV, TY, true>(a, tm, tile_class, grid, d, st);
+  } else {
+    if (r16) flux_launch_rows<AXI, SUTH, FFV, 16, false>(a, tm, tile_class, grid, d, st);
+    else flux_launch_rows<AXI, SUTH, FFV, TY, false>(a, tm, tile_class, grid, d, st);
   }
 }
 
 void launch_flux_class(const DevCtx& d, bool on_S, double* const out[4], int tile_class, cudaStream_t st,
-                       int spare) {
+                       int spare, bool ffv) {
   FluxArgs a;
   a.tile_class = tile_class;
   a.list = nullptr;
@@ -1882,15 +2074,29 @@ void launch_flux_class(const DevCtx& d, bool on_S, double* const out[4], int til
   a.o0 = out[0]; a.o1 = out[1]; a.o2 = out[2]; a.o3 = out[3];
   a.cell_idx = d.cell_idx;
   a.m = d.m;
+  a.err = d.err;
+  FluxMaps tm;
+  if (d.tma) {
+    const int ri = flux_rows(d) == 16;
+    const CUtensorMap* q4 = on_S ? d.tmS[ri] : d.tmY[ri];
+    for (int v = 0; v < 4; ++v) tm.m[v] = q4[v];
+    tm.m[4] = d.tmP[ri];
+    tm.m[5] = d.tmT[ri];
+  } else {
+    memset(&tm, 0, sizeof tm);
+  }
   const hymor_config& c = d.cfg;
   a.kpr = c.gamma / c.Pr;
+  a.kprf = host_ff(a.kpr);
+  a.c23f = host_ff(2.0 / 3.0);
   a.suthS = c.sutherland_S;
   a.Tinf_inv = c.energy_factor / c.cv;
   a.nchi = d.nchi;
   a.neta = d.neta;
   a.shock = c.shock_enabled;
   a.mask = c.shock_enabled && c.shock_feedback;
-  dim3 grid((d.nchi + TX - 1) / TX, (d.neta + TY - 1) / TY);
+  const int rows = flux_rows(d);
+  dim3 grid((d.nchi + TX - 1) / TX, (d.neta + rows - 1) / rows);
   const bool axi = c.axisymmetric, suth = c.viscosity_model == 1;
   if (tile_class >= 0 && d.tiles) {
     // the compact list of the class over a persistent grid (the interior tiles at full
@@ -1898,33 +2104,53 @@ void launch_flux_class(const DevCtx& d, bool on_S, double* const out[4], int til
     const int nt = flux_tiles(d);
     a.count = d.tiles + tile_class;
     a.list = d.tiles + 2 + tile_class * nt;
-    const int b = g_flux_blocks_per_sm[axi * 2 + suth];
+    const int b = g_flux_blocks_per_sm[(d.tma ? 16 : 0) + (rows == 16) * 8 + ffv * 4 + axi * 2 + suth];
     grid = dim3((b > spare + 1 ? b - spare : 1) * d.sms, 1);
   }
-  if (!axi && !suth) flux_launch<false, false>(a, tile_class, grid, d, st);
-  else if (axi && !suth) flux_launch<true, false>(a, tile_class, grid, d, st);
-  else if (!axi && suth) flux_launch<false, true>(a, tile_class, grid, d, st);
-  else flux_launch<true, true>(a, tile_class, grid, d, st);
+  if (ffv) {
+    if (!axi && !suth) flux_launch<false, false, true>(a, tm, tile_class, grid, d, st);
+    else if (axi && !suth) flux_launch<true, false, true>(a, tm, tile_class, grid, d, st);
+    else if (!axi && suth) flux_launch<false, true, true>(a, tm, tile_class, grid, d, st);
+    else flux_launch<true, true, true>(a, tm, tile_class, grid, d, st);
+  } else {
+    if (!axi && !suth) flux_launch<false, false, false>(a, tm, tile_class, grid, d, st);
+    else if (axi && !suth) flux_launch<true, false, false>(a, tm, tile_class, grid, d, st);
+    else if (!axi && suth) flux_launch<false, true, false>(a, tm, tile_class, grid, d, st);
+    else flux_launch<true, true, false>(a, tm, tile_class, grid, d, st);
+  }
 }
 
 void launch_flux(const DevCtx& d, bool on_S, double* const out[4], cudaStream_t st) {
   launch_flux_class(d, on_S, out, -1, st);
 }
 
-void flux_kernel_setup() {
-  cudaFuncSetAttribute(k_flux<false, false, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxMaxSmem);
-  cudaFuncSetAttribute(k_flux<true, false, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxMaxSmem);
-  cudaFuncSetAttribute(k_flux<false, true, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxMaxSmem);
-  cudaFuncSetAttribute(k_flux<true, true, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxMaxSmem);
+template <bool FFV, int TYV, bool TMA>
+void flux_setup_variant() {
   auto occ = [](auto kern, size_t smem) {
     int b = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kFluxThreads, smem) != cudaSuccess || b < 1) b = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, 32 * TYV, smem) != cudaSuccess || b < 1) b = 1;
     return b;
   };
-  g_flux_blocks_per_sm[0] = occ(k_flux<false, false, TY>, flux_smem<false, false>());
-  g_flux_blocks_per_sm[1] = occ(k_flux<false, true, TY>, flux_smem<false, true>());
-  g_flux_blocks_per_sm[2] = occ(k_flux<true, false, TY>, flux_smem<true, false>());
-  g_flux_blocks_per_sm[3] = occ(k_flux<true, true, TY>, flux_smem<true, true>());
+  const int base = (TMA ? 16 : 0) + (TYV == 16) * 8 + FFV * 4;
+  auto one = [&](auto kern, size_t smem, int idx) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxMaxSmem);
+    g_flux_blocks_per_sm[base + idx] = occ(kern, smem);
+  };
+  one(k_flux<false, false, TYV, FFV, TMA>, flux_smem<false, false, TYV, TMA>(), 0);
+  one(k_flux<false, true, TYV, FFV, TMA>, flux_smem<false, true, TYV, TMA>(), 1);
+  one(k_flux<true, false, TYV, FFV, TMA>, flux_smem<true, false, TYV, TMA>(), 2);
+  one(k_flux<true, true, TYV, FFV, TMA>, flux_smem<true, true, TYV, TMA>(), 3);
+}
+
+void flux_kernel_setup() {
+  flux_setup_variant<false, TY, false>();
+  flux_setup_variant<true, TY, false>();
+  flux_setup_variant<false, 16, false>();
+  flux_setup_variant<true, 16, false>();
+  flux_setup_variant<false, TY, true>();
+  flux_setup_variant<true, TY, true>();
+  flux_setup_variant<false, 16, true>();
+  flux_setup_variant<true, 16, true>();
   cudaFuncSetAttribute(k_spline_fit, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)sizeof(float) * kSplineArrays * spline_stride(4096));
 }

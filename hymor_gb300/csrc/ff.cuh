@@ -1,0 +1,88 @@
+// Float-float arithmetic on the FP32 pipe for the viscous terms of the RK-step flux.
+//
+// On GB300 one FP64 warp instruction issues per ~70 cycles of an SM sub-partition and one
+// FP32 warp instruction per cycle, so an FP64 operation costs as much as ~70 FP32 ones. A
+// float-float value is the unevaluated sum h + l of two floats with |l| <= ulp(h) / 2,
+// about 48 significant bits (Dekker, "A floating-point technique for extending the
+// available precision", Numer. Math. 18 (1971) 224-242): an addition is Knuth's TwoSum of
+// the high parts plus the low parts, a product is the exact product of the high parts
+// (TwoProduct, with a fused multiply-add) plus the cross terms; each is renormalised by
+// the fast two-sum. These are the "sloppy" forms: their error is ~2^-47 of the operands'
+// magnitude, which is all the viscous fluxes need (their rounding then stays ~1e-15 of
+// the face-flux scale).
+//
+// Conversions go through the bit patterns on the integer pipe, so that the FP64 pipe only
+// sees the one addition that joins a result back into a double (a cvt between f32 and f64
+// issues on the FP64 pipe at the DFMA rate on this GPU).
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace hymor {
+
+struct __align__(8) ff {
+  float h, l;
+};
+
+__device__ __forceinline__ ff ff_fast_two_sum(float a, float b) {  // |a| >= |b| or a == 0
+  const float s = a + b;
+  return ff{s, b - (s - a)};
+}
+
+__device__ __forceinline__ ff ff_two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return ff{s, (a - (s - bb)) + (b - bb)};
+}
+
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+  const ff s = ff_two_sum(a.h, b.h);
+  return ff_fast_two_sum(s.h, s.l + (a.l + b.l));
+}
+
+__device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.h, -a.l}; }
+
+__device__ __forceinline__ ff ff_sub(ff a, ff b) { return ff_add(a, ff_neg(b)); }
+
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+  const float p = a.h * b.h;
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, e));
+  return ff_fast_two_sum(p, e);
+}
+
+// a * 2^k for a power of two: exact, no renormalisation
+__device__ __forceinline__ ff ff_scale2(ff a, float p2) { return ff{a.h * p2, a.l * p2}; }
+
+// double -> float-float: h is x with its 29 low mantissa bits cleared (an exact float),
+// l the remaining 29 bits truncated to 24. |x| must lie in the float normal range; zero
+// (and anything below 2^-126) gives zero.
+__device__ __forceinline__ ff ff_from_double(double x) {
+  const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
+  const unsigned sign = hw & 0x80000000u;
+  const int e = (int)((hw >> 20) & 0x7ffu);
+  const unsigned hb = sign | ((unsigned)(e - 896) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29);
+  const unsigned m = lw & 0x1fffffffu;
+  const int p = 31 - __clz((int)m);                                // leading bit of m, -1 if m == 0
+  const unsigned mant = p > 23 ? (m >> (p - 23)) : (m << (23 - p));
+  const int el = e - 948 + p;                                      // biased float exponent of l
+  const unsigned lb = sign | ((unsigned)el << 23) | (mant & 0x7fffffu);
+  ff r;
+  r.h = e > 896 ? __uint_as_float(hb) : 0.0f;
+  r.l = (e > 896 && m != 0u && el > 0) ? __uint_as_float(lb) : 0.0f;
+  return r;
+}
+
+// exact float -> double widening of a normal float (or zero) through the bit pattern
+__device__ __forceinline__ double ff_widen(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned ef = (b >> 23) & 0xffu;
+  const unsigned hw = (b & 0x80000000u) | (ef ? (((ef + 896u) << 20) | ((b & 0x7fffffu) >> 3)) : 0u);
+  const unsigned lw = ef ? (b << 29) : 0u;
+  return __hiloint2double((int)hw, (int)lw);
+}
+
+// float-float -> double: one FP64 addition
+__device__ __forceinline__ double ff_to_double(ff a) { return ff_widen(a.h) + ff_widen(a.l); }
+
+}  // namespace hymor

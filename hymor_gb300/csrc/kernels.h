@@ -62,6 +62,18 @@ struct DevCtx {
   double* res_up;  // 4 x Nchi upstream state of hymor_residual (hymor_set_upstream), or null
   int* brows;      // Nchi: the shocked rows sc_m of B's flux rows
   double* bwork;   // 5 x Nchi: the per-column upstream state and the base shock speeds
+  // the RK step's flux forms the viscous terms in float-float arithmetic (1, the default)
+  // or in FP64 (0); the residual entry point and the Jacobian always use FP64
+  int step_ffv;
+  // flux tiling of the RK step (hymor_autotune): tile rows (8 or 16) and the block slots per
+  // SM the persistent interior-tile grid leaves to the side streams
+  int flux_rows, flux_spare;
+  // TMA descriptors of the ghosted planes for the flux halo, per tile height (8, 16 rows):
+  // S and Y conserved planes, p, T. tma: 1 when they are used (they exist when (Nchi + 2) * 8
+  // bytes is a multiple of 16, the TMA row-pitch rule); else the flux loads its halo thread
+  // by thread.
+  CUtensorMap tmS[2][4], tmY[2][4], tmP[2], tmT[2];
+  int tma;
 };
 
 // Unknowns of the linearised operator: 4N, plus Nchi with the shock blocks.
@@ -93,11 +105,13 @@ void launch_flux(const DevCtx& d, bool on_S, double* const out[4], cudaStream_t 
 // With the step's tile lists (d.tiles) each class runs over its compact list, and tiles
 // wholly above the shock are not evaluated (their flux is never read by the stage update).
 // spare: resident block slots per SM the persistent interior-tile grid leaves to other streams
+// ffv: the viscous terms in float-float arithmetic (the RK step), else FP64
 void launch_flux_class(const DevCtx& d, bool on_S, double* const out[4], int tile_class, cudaStream_t st,
-                       int spare = 0);
+                       int spare = 0, bool ffv = false);
 // Classifies the flux tiles of the current shocked rows into d.tiles.
 void launch_classify_tiles(const DevCtx& d, cudaStream_t st);
 int flux_tiles(const DevCtx& d);
+int flux_tiles_max(const DevCtx& d);  // the tile count of the smallest tile height (list sizes)
 // UPDATE_FLOW_CELLS part 1: detect shocked cells, upstream fill, extrapolation (on S).
 void launch_flow_cells(const DevCtx& d, cudaStream_t st);
 // Sound speed of S (recompute) and max|a| into scal[kCmax]; recompute=false only reduces aS.
@@ -112,8 +126,6 @@ void launch_snapshot(const DevCtx& d, cudaStream_t st);
 void launch_classical_stage(const DevCtx& d, double cY, cudaStream_t st);
 
 // ---- linear.cu ----
-void launch_jacobian_assemble(DevCtx& d, cudaStream_t st);
-void launch_b_assemble(DevCtx& d, cudaStream_t st);
 void launch_matvec(const DevCtx& d, int k, const double* X, double* Y, int transpose, double scale,
                    cudaStream_t st, long ld = 0);
 // graph_ok: with the shock blocks, the Taylor steps may be captured once into a CUDA graph

@@ -105,6 +105,11 @@ class Solution:
         self.ctx.check(self.ctx.L.hymor_operator_size(self.ctx.h, ctypes.byref(n)))
         return n.value
 
+    def set_step_viscous(self, mode: int):
+        """Arithmetic of the viscous terms in the RK step's flux: 1 float-float (default),
+        0 FP64 (hymor_set_step_viscous). PDE and the Jacobian always use FP64."""
+        self.ctx.check(self.ctx.L.hymor_set_step_viscous(self.ctx.h, int(mode)))
+
     def step_kernels(self) -> int:
         """Kernel launches one ADVECT_FLOW step makes (the kernel nodes of its graph)."""
         n = ctypes.c_int32()
@@ -410,6 +415,7 @@ def EIGENVALUES(L: LinearOperatorGPU, s: Solution, n_modes: int, T_ref: float = 
     rng = np.random.Generator(np.random.PCG64(seed))
     t0 = time.perf_counter()
     X = None
+    restarts = None
     if method == "device":
         from .krylov import DeviceBuffer
         x0 = rng.standard_normal((block, n))
@@ -428,7 +434,7 @@ def EIGENVALUES(L: LinearOperatorGPU, s: Solution, n_modes: int, T_ref: float = 
             Xr = vb.download(2 * n * n_modes).reshape(2 * n_modes, n).T
             X = Xr[:, :n_modes] + 1j * Xr[:, n_modes:]
             vb.free()
-        nops, converged = int(info3[0]), bool(info3[2])
+        nops, converged, restarts = int(info3[0]), bool(info3[2]), int(info3[1])
     elif method == "python" and block > 1:
         from .krylov import block_krylov_schur
         mu, resid, nops, X = block_krylov_schur(s.ctx, n, _expm_block_op(s, dt, timesteps, order), n_modes, ncv,
@@ -470,7 +476,8 @@ def EIGENVALUES(L: LinearOperatorGPU, s: Solution, n_modes: int, T_ref: float = 
         lam = np.full(n_modes, np.nan + 1j * np.nan)
         mu = np.full(n_modes, np.nan + 1j * np.nan)
         X = np.full((n, n_modes), np.nan + 1j * np.nan) if modes else None
-    info = dict(mu=mu, resid=resid, dt=dt, timesteps=timesteps, nops=nops, seconds=elapsed, converged=converged)
+    info = dict(mu=mu, resid=resid, dt=dt, timesteps=timesteps, nops=nops, seconds=elapsed, converged=converged,
+                restarts=restarts)
     if modes:
         info["modes"] = X
     return lam, info
@@ -619,7 +626,7 @@ def TRANSIENT_GROWTH_DOWNSTREAM(L: LinearOperatorGPU, s: Solution, n_modes: int,
         X = np.full((n, n_modes), np.nan) if modes else None
     dt, n_t = float(dt_o[0]), int(nt_o[0])
     info = dict(resid=resid, dt=dt, n_t=n_t, T_opt=n_t * dt, nops=int(info3[0]), seconds=elapsed,
-                converged=converged)
+                converged=converged, restarts=int(info3[1]))
     if modes:
         info["modes"] = X
     return G, info
@@ -703,7 +710,8 @@ def TRANSIENT_GROWTH_HORIZONS(L: LinearOperatorGPU, s: Solution, n_modes: int, T
         if not converged and not keep_unconverged:
             G[h] = np.nan
         infos.append(dict(resid=resid[h], dt=float(dts[h]), n_t=int(nts[h]), T_opt=int(nts[h]) * float(dts[h]),
-                          nops=int(info3[3 * h]), seconds=elapsed, converged=converged))
+                          nops=int(info3[3 * h]), seconds=elapsed, converged=converged,
+                          restarts=int(info3[3 * h + 1])))
     if not all(inf["converged"] for inf in infos) and not keep_unconverged:
         import warnings
         warnings.warn(f"transient-growth solves of some horizons did not reach tol {tol:g}; their gains are NaN")

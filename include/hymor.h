@@ -26,7 +26,7 @@ extern "C" {
 #define HYMOR_ERR_CUDA (-2)         /* CUDA runtime error                           */
 #define HYMOR_ERR_NUMERIC (-3)      /* NaN / non-positive density or pressure seen  */
 #define HYMOR_ERR_SHOCK_RANGE (-4)  /* shocked cell too close to the domain top     */
-#define HYMOR_ERR_TIMEOUT (-5)      /* reserved: no kernel of this library waits on a flag */
+#define HYMOR_ERR_TIMEOUT (-5)      /* a bounded device wait (TMA transfer) gave up        */
 #define HYMOR_ERR_NOT_READY (-6)    /* e.g. matvec before a Jacobian exists         */
 
 /* Boundary conditions (names of utils/Operators/APPLY_BOUNDARY_CONDITIONS.jl). */
@@ -118,6 +118,28 @@ int hymor_residual(hymor_ctx* ctx, double* flux);
 int hymor_set_upstream(hymor_ctx* ctx, const double* cols);
 /* Sets the context's persistent flux arrays (the Dict's s["flux"]). */
 int hymor_set_flux(hymor_ctx* ctx, const double* flux);
+
+/* Arithmetic of the viscous terms in the RK step's flux (no counterpart in the reference,
+ * whose arithmetic is FP64 throughout). mode 1 (the default): the gradients, stresses and heat
+ * flux of VISCOUS_FLUX.jl:36-210 in float-float arithmetic (pairs of FP32 values, ~48-bit
+ * significands, on the FP32 pipe, which GB300 issues ~70x faster than FP64), joined back into
+ * FP64 before they enter the face fluxes; mode 0: FP64. hymor_residual and the Jacobian
+ * (hymor_linearize, hymor_linearize_b) always use FP64. The next hymor_step re-captures its
+ * graph. */
+int hymor_set_step_viscous(hymor_ctx* ctx, int mode);
+
+/* Tile-shape autotuner of the RK step's flux (no counterpart in the reference): times `steps`
+ * steps (CUDA events, after a warm-up step) for each flux configuration — the tile halo staged
+ * by TMA (cp.async.bulk.tensor) or loaded thread by thread, tiles of 31 x 8 or 31 x 16 cells,
+ * and 0, 1 or 2 block slots per SM that the persistent interior-tile grid leaves to the side
+ * streams — each from the same saved state, restores the state, and keeps the fastest.
+ * choice[3] = (rows, spare, tma); ms_per_step[12] (or NULL) = the candidates' times, index
+ * 6 tma + 3 (rows == 16) + spare (0 where a TMA candidate could not run: Nchi odd). Every
+ * configuration gives bit-identical fluxes (each face flux has the same arithmetic whichever
+ * tile computes it, and the staged halo holds the same values). hymor_set_flux_tiling sets one
+ * directly (default: TMA when Nchi is even, 8 rows, 1 spare slot). */
+int hymor_autotune(hymor_ctx* ctx, int steps, int32_t* choice, float* ms_per_step);
+int hymor_set_flux_tiling(hymor_ctx* ctx, int rows, int spare, int tma);
 
 /* nsteps x ADVECT_FLOW (utils/Time_marching/ADVECT_FLOW.jl:30-39 ->
  * ADVECT_FLOW_EXPLICIT.jl:36-81), all on the device (one CUDA graph per step). */

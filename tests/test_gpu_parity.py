@@ -178,6 +178,33 @@ def test_stored_flux_enters_cfl_and_steps(require_gpu):
     compare_state(sol, orc, 1e-11)
 
 
+@pytest.mark.parametrize("name", ["cylinder_100x80", "cylinder_sutherland", "blunt_cone_axisym",
+                                  "cylinder_interp1_eulerian"])
+def test_step_viscous_float_float(require_gpu, name):
+    """The RK step with the viscous terms in float-float arithmetic (the default) and in FP64
+    (hymor_set_step_viscous(0)) both match the oracle after 10 steps to the 10-step tolerance;
+    their difference is the float-float rounding (~2^-47 of the viscous terms)."""
+    cfg = CASES[name]()
+    cs = C.initial_state(cfg, seed=1, noise=1e-6)
+    a, b, orc = S.Solution(cs), S.Solution(cs), O.Oracle(cs)
+    b.set_step_viscous(0)
+    S.ADVECT_FLOW(a, 10)
+    S.ADVECT_FLOW(b, 10)
+    orc.advect(10)
+    ea = compare_state(a, orc, STATE_TOL.get(name, 1e-11))
+    eb = compare_state(b, orc, STATE_TOL.get(name, 1e-11))
+    dab = state_rel(a.get_state()["q"], b.get_state()["q"])
+    print(f"\n{name}: float-float {max(ea):.2e}, FP64 {max(eb):.2e}, between them {max(dab):.2e}")
+    assert max(dab) < 1e-12
+    # the residual entry point stays FP64 whatever the step uses: bit-identical on one state
+    st = orc.get_state()
+    for sol in (a, b):
+        sol.set_state(st["q"], st["pts_x"], st["pts_y"], st["pts_chi"], st["pts_eta"], st["cell_idx"], st["t"])
+    assert np.array_equal(S.PDE(a), S.PDE(b))
+    a.close()
+    b.close()
+
+
 @pytest.mark.slow
 def test_cylinder_2000_steps_parity(require_gpu):
     """The 100 x 80 shock-fitted cylinder marched 2000 RK4 steps at CFL 0.5: residual and
@@ -310,3 +337,53 @@ def test_shock_range_error_is_reported(require_gpu):
         sol = S.Solution(cs)
         sol.set_state(cs.q_flat(), cs.pts_x, cs.pts_y, cs.pts_chi, cs.pts_eta, bad, 0.0)
     assert e.value.code == -4
+
+
+def test_flux_tilings_bit_identical(require_gpu):
+    """Every flux configuration (halo by TMA or thread loads, tiles of 31 x 8 or 31 x 16 cells,
+    0..2 spare block slots) gives bit-identical RK steps and residuals: each face flux has the
+    same arithmetic whichever tile computes it, from the same halo values."""
+    cfg = C.cylinder_config(100, 80)
+    cs = C.initial_state(cfg, seed=1, noise=1e-6)
+    ref = S.Solution(cs)
+    S.ADVECT_FLOW(ref, 5)
+    q_ref = ref.get_state()
+    f_ref = S.PDE(ref)  # PDE mutates its solution: evaluate each solution once
+    for rows, spare, tma in ((16, 0, 1), (16, 2, 0), (8, 0, 0), (8, 1, 1)):
+        sol = S.Solution(cs)
+        sol.ctx.check(sol.ctx.L.hymor_set_flux_tiling(sol.ctx.h, rows, spare, tma))
+        S.ADVECT_FLOW(sol, 5)
+        st = sol.get_state()
+        assert np.array_equal(st["q"], q_ref["q"]), (rows, spare)
+        assert np.array_equal(st["pts_x"], q_ref["pts_x"]) and st["t"] == q_ref["t"]
+        assert np.array_equal(S.PDE(sol), f_ref), (rows, spare, tma)
+        sol.close()
+    ref.close()
+
+
+def test_autotune_restores_state_and_picks_a_tiling(require_gpu):
+    """hymor_autotune times every flux configuration from the same saved state, restores it,
+    and keeps the fastest: the state after tuning is the state before, bit for bit, and the
+    steps after it equal an untuned context's."""
+    import ctypes
+    cfg = C.cylinder_config(200, 100)
+    cs = C.initial_state(cfg, seed=1, noise=1e-6)
+    a, b = S.Solution(cs), S.Solution(cs)
+    S.ADVECT_FLOW(a, 3)
+    S.ADVECT_FLOW(b, 3)
+    before = a.get_state()
+    choice = np.zeros(3, dtype=np.int32)
+    ms = (ctypes.c_float * 12)()
+    a.ctx.check(a.ctx.L.hymor_autotune(a.ctx.h, 5, choice.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), ms))
+    assert choice[0] in (8, 16) and choice[1] in (0, 1, 2) and choice[2] in (0, 1)
+    assert all(m > 0 for m in ms)  # 200 x 100: Nchi even, the TMA candidates run too
+    after = a.get_state()
+    for k in ("q", "pts_x", "pts_y", "pts_chi", "pts_eta", "cell_idx"):
+        assert np.array_equal(after[k], before[k]), k
+    assert after["t"] == before["t"]
+    assert a.counters() == b.counters()
+    S.ADVECT_FLOW(a, 4)
+    S.ADVECT_FLOW(b, 4)
+    assert np.array_equal(a.get_state()["q"], b.get_state()["q"])
+    a.close()
+    b.close()
