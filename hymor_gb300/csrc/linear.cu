@@ -979,6 +979,61 @@ void launch_expm(const DevCtx& d, int k, double dt, int nsteps, int order, const
   launch_expm_body(d, k, dt, nsteps, order, v, t1, t2, Yout, transpose, st, graph_ok);
 }
 
+// Workspaces of the perturbed residuals of a linearisation (the A11 colours, the shock-point
+// residuals, LINEARIZE_B's columns): each lane has its own stage array, p, T, edge sound
+// speed, shock points, spline workspace, shock speeds, prescribed upstream columns and flux,
+// and its own stream, so that the residuals of different perturbations run concurrently. The
+// base state, the mesh, the base flux and the assembled blocks are shared: read-only, or
+// written at entries no other perturbation writes, with the same arithmetic as one after
+// another, so the result does not depend on the lanes.
+constexpr int kJacLanes = 8;
+static PertArgs pert_args(const DevCtx& d);
+struct JacLane {
+  cudaStream_t st = nullptr;
+  cudaEvent_t done = nullptr;
+  double* mem = nullptr;
+  Cons Y;
+  double *p, *T, *aY, *spl, *speed_x, *speed_y, *rel, *cols;
+  ShockPts Yp;
+  double* F[4];
+};
+struct JacLanes {
+  std::vector<JacLane> lane;
+  cudaEvent_t fork = nullptr;
+};
+
+// The lane's view of the context: its own buffers in place of the shared ones. TMA
+// descriptors name the context's own stage array, so a lane loads its halo thread by thread
+// (the same values, the same arithmetic).
+DevCtx lane_ctx(const DevCtx& d, const JacLane& l) {
+  DevCtx ld = d;
+  ld.Y = l.Y;
+  ld.p = l.p;
+  ld.T = l.T;
+  ld.aY = l.aY;
+  ld.spl = l.spl;
+  ld.speed_x = l.speed_x;
+  ld.speed_y = l.speed_y;
+  ld.rel = l.rel;
+  ld.Yp = l.Yp;
+  ld.tma = 0;
+  if (d.up_cols) ld.up_cols = l.cols;
+  return ld;
+}
+
+// every lane waits for the work enqueued on st so far
+void lanes_fork(JacLanes& L, cudaStream_t st) {
+  cudaEventRecord(L.fork, st);
+  for (JacLane& l : L.lane) cudaStreamWaitEvent(l.st, L.fork, 0);
+}
+// st waits for every lane
+void lanes_join(JacLanes& L, cudaStream_t st) {
+  for (JacLane& l : L.lane) {
+    cudaEventRecord(l.done, l.st);
+    cudaStreamWaitEvent(st, l.done, 0);
+  }
+}
+
 // The shock-position blocks (perturb_shock), after the A11 assembly has left the base
 // flux in Fb and the base shock speeds in sj.rel_b, on the shocked rows d.cell_idx:
 //   A21 (LINEARIZE_EQUATIONS_NO_DISCONTINUITY.jl:140-258): the shock speed of column i
@@ -989,41 +1044,50 @@ void launch_expm(const DevCtx& d, int k, double dt, int nsteps, int order, const
 //     a column are exact zeros. 8 residuals (j = 1, 2; 4 variables), no flux needed.
 //   A12, A22 (:262-274): one residual per shock point, the point moved by eps along the
 //     PERTURB_SHOCK direction (the smoothing spline couples every point to every other).
-void launch_shock_assemble(DevCtx& d, const double* const Fb[4], double* const Fp[4], PertArgs pa,
-                           cudaStream_t st) {
+void launch_shock_assemble(DevCtx& d, const double* const Fb[4], PertArgs pa, JacLanes& L, cudaStream_t st) {
   const hymor_config& c = d.cfg;
   const int nchi = d.nchi;
   const int cb = (nchi + 127) / 128;
   const double eps = c.perturbation_magnitude;
   const double h = std::hypot(c.rho_u_0, c.rho_v_0);
+  const int K = (int)L.lane.size();
   k_shock_dir<<<cb, 128, 0, st>>>(d.beta, d.sj.dir, nchi, c.rho_u_0 / h, c.rho_v_0 / h);
   cudaMemcpyAsync(d.sj.rows, d.cell_idx, sizeof(int) * nchi, cudaMemcpyDeviceToDevice, st);
-  for (int j = 1; j <= 2; ++j)
-    for (int var = 0; var < 4; ++var) {
-      pa.var = var;
-      pa.shock_row = j;
-      k_perturb_thermo<<<grid_for(d.G, 256), 256, 0, st>>>(pa);
-      launch_shock_bc_flags(d, false, true, true, false, 0, st);
-      k_gather_a21<<<cb, 128, 0, st>>>(d.rel, d.sj.rel_b, d.sj.a21, nchi, (j - 1) * 4 + var, eps);
-    }
-  Flux4 fp, fb;
-  for (int v = 0; v < 4; ++v) {
-    fp.v[v] = Fp[v];
-    fb.v[v] = Fb[v];
-  }
-  pa.var = -1;
-  pa.shock_row = 0;
   // only the flux of the cells (i, sc_i - 1) is read: the tiles whose halo the shock and
   // boundary kernels write (class 1 of the step's tile lists) hold them all, and compute
   // them with the same per-cell arithmetic as the whole grid
   launch_classify_tiles(d, st);
-  for (int p = 0; p < nchi; ++p) {
-    k_perturb_thermo<<<grid_for(d.G, 256), 256, 0, st>>>(pa);
-    k_perturb_point<<<cb, 128, 0, st>>>(d.Sp, d.Yp, d.sj.dir, nchi, p, eps);
-    launch_shock_bc_flags(d, false, false, true, true, 0, st);
-    launch_flux_class(d, false, Fp, 1, st);
-    k_gather_a12<<<cb, 128, 0, st>>>(fp, fb, d.rel, d.sj.rel_b, d.sj.rows, d.sj.a12, d.sj.a22, nchi, p, eps);
+  lanes_fork(L, st);
+  int q = 0;
+  for (int j = 1; j <= 2; ++j)
+    for (int var = 0; var < 4; ++var, ++q) {
+      const JacLane& l = L.lane[q % K];
+      const DevCtx ld = lane_ctx(d, l);
+      PertArgs pl = pert_args(ld);
+      pl.var = var;
+      pl.shock_row = j;
+      k_perturb_thermo<<<grid_for(d.G, 256), 256, 0, l.st>>>(pl);
+      launch_shock_bc_flags(ld, false, true, true, false, 0, l.st);
+      k_gather_a21<<<cb, 128, 0, l.st>>>(ld.rel, d.sj.rel_b, d.sj.a21, nchi, (j - 1) * 4 + var, eps);
+    }
+  Flux4 fb;
+  for (int v = 0; v < 4; ++v) fb.v[v] = Fb[v];
+  for (int p = 0; p < nchi; ++p, ++q) {
+    const JacLane& l = L.lane[q % K];
+    const DevCtx ld = lane_ctx(d, l);
+    PertArgs pl = pert_args(ld);
+    pl.var = -1;
+    pl.shock_row = 0;
+    Flux4 fp;
+    for (int v = 0; v < 4; ++v) fp.v[v] = l.F[v];
+    double* const Fp[4] = {l.F[0], l.F[1], l.F[2], l.F[3]};
+    k_perturb_thermo<<<grid_for(d.G, 256), 256, 0, l.st>>>(pl);
+    k_perturb_point<<<cb, 128, 0, l.st>>>(d.Sp, ld.Yp, d.sj.dir, nchi, p, eps);
+    launch_shock_bc_flags(ld, false, false, true, true, 0, l.st);
+    launch_flux_class(ld, false, Fp, 1, l.st);
+    k_gather_a12<<<cb, 128, 0, l.st>>>(fp, fb, ld.rel, d.sj.rel_b, d.sj.rows, d.sj.a12, d.sj.a22, nchi, p, eps);
   }
+  lanes_join(L, st);
   k_transpose<<<grid_for(4L * nchi * nchi, 256), 256, 0, st>>>(d.sj.a12, d.sj.a12t, 4L * nchi, nchi);
   k_transpose<<<grid_for((long)nchi * nchi, 256), 256, 0, st>>>(d.sj.a22, d.sj.a22t, nchi, nchi);
 }
@@ -1050,15 +1114,11 @@ static PertArgs pert_args(const DevCtx& d) {
   return pa;
 }
 
-void launch_jacobian_assemble(DevCtx& d, cudaStream_t st) {
+void launch_jacobian_assemble(DevCtx& d, cudaStream_t st, JacLanes& L) {
   const hymor_config& c = d.cfg;
   const long N = d.N;
   double* Fb[4];
-  double* Fp[4];
-  for (int v = 0; v < 4; ++v) {
-    Fb[v] = d.jwork + v * N;
-    Fp[v] = d.jwork + (4 + v) * N;
-  }
+  for (int v = 0; v < 4; ++v) Fb[v] = d.jwork + v * N;
   const bool shock_blocks = c.shock_enabled && c.perturb_shock;
   PertArgs pa = pert_args(d);
   // base output: NON_LINEAR_DYNAMICS(deepcopy(s))
@@ -1069,61 +1129,82 @@ void launch_jacobian_assemble(DevCtx& d, cudaStream_t st) {
     cudaMemcpyAsync(d.sj.rel_b, d.rel, sizeof(double) * d.nchi, cudaMemcpyDeviceToDevice, st);
   cudaMemsetAsync(d.coef, 0, sizeof(double) * 144 * N, st);
   ScatArgs sa;
-  for (int v = 0; v < 4; ++v) { sa.Fp[v] = Fp[v]; sa.Fb[v] = Fb[v]; }
+  for (int v = 0; v < 4; ++v) sa.Fb[v] = Fb[v];
   sa.coef = d.coef;
   sa.w = make_wrap(c);
   sa.eps = c.perturbation_magnitude;
   sa.N = N;
+  // the 36 colour x variable residuals, spread over the lanes
+  const int K = (int)L.lane.size();
+  lanes_fork(L, st);
+  int q = 0;
   for (int var = 0; var < 4; ++var)
-    for (int colour = 1; colour <= 9; ++colour) {
-      pa.var = var;
-      pa.colour = colour;
-      k_perturb_thermo<<<grid_for(d.G, 256), 256, 0, st>>>(pa);
-      launch_shock_bc_flags(d, false, true, c.shock_enabled, true, 0, st);
-      launch_flux(d, false, Fp, st);
-      sa.var = var;
-      sa.colour = colour;
-      k_scatter<<<grid_for(N, 256), 256, 0, st>>>(sa);
+    for (int colour = 1; colour <= 9; ++colour, ++q) {
+      const JacLane& l = L.lane[q % K];
+      const DevCtx ld = lane_ctx(d, l);
+      PertArgs pl = pert_args(ld);
+      pl.var = var;
+      pl.colour = colour;
+      double* const Fp[4] = {l.F[0], l.F[1], l.F[2], l.F[3]};
+      k_perturb_thermo<<<grid_for(d.G, 256), 256, 0, l.st>>>(pl);
+      launch_shock_bc_flags(ld, false, true, c.shock_enabled, true, 0, l.st);
+      launch_flux(ld, false, Fp, l.st);
+      ScatArgs sl = sa;
+      for (int v = 0; v < 4; ++v) sl.Fp[v] = l.F[v];
+      sl.var = var;
+      sl.colour = colour;
+      k_scatter<<<grid_for(N, 256), 256, 0, l.st>>>(sl);
     }
-  if (shock_blocks) launch_shock_assemble(d, Fb, Fp, pa, st);
+  lanes_join(L, st);
+  if (shock_blocks) launch_shock_assemble(d, Fb, pa, L, st);
 }
 
 // LINEARIZE_B (Freestream_receptivity/LINEARIZE_B.jl:40-170): the residual with a prescribed
 // per-column upstream state (rho_0_upstream_p), once unperturbed and once per variable and
 // colour of columns (i = colour mod 3 raised by eps): 13 residuals. Each output column m has
 // exactly one raised column among m - 1, m, m + 1 per colour.
-void launch_b_assemble(DevCtx& d, cudaStream_t st) {
+void launch_b_assemble(DevCtx& d, cudaStream_t st, JacLanes& L) {
   const hymor_config& c = d.cfg;
   const long N = d.N;
   const int nchi = d.nchi, cb = (nchi + 127) / 128;
   const double eps = c.perturbation_magnitude;
   double* Fb[4];
-  double* Fp[4];
-  Flux4 fb, fp;
+  Flux4 fb;
   for (int v = 0; v < 4; ++v) {
     Fb[v] = d.jwork + v * N;
-    Fp[v] = d.jwork + (4 + v) * N;
     fb.v[v] = Fb[v];
-    fp.v[v] = Fp[v];
   }
   double* cols = d.bwork;
   double* rel_b = d.bwork + 4 * nchi;
-  const PertArgs pa = pert_args(d);
   cudaMemcpyAsync(d.brows, d.cell_idx, sizeof(int) * nchi, cudaMemcpyDeviceToDevice, st);
   cudaMemsetAsync(d.bq, 0, sizeof(double) * 48 * nchi, st);
   cudaMemsetAsync(d.bs, 0, sizeof(double) * 12 * nchi, st);
   d.up_cols = cols;
-  for (int var = -1; var < 4; ++var)
-    for (int colour = 0; colour < (var < 0 ? 1 : 3); ++colour) {
-      k_up_cols<<<cb, 128, 0, st>>>(cols, nchi, c.rho_0, c.rho_u_0, c.rho_v_0, c.rho_E_0, var, colour, eps);
-      k_perturb_thermo<<<grid_for(d.G, 256), 256, 0, st>>>(pa);
-      launch_shock_bc_flags(d, false, true, true, true, 0, st);
-      launch_flux(d, false, var < 0 ? Fb : Fp, st);
-      if (var < 0)
-        cudaMemcpyAsync(rel_b, d.rel, sizeof(double) * nchi, cudaMemcpyDeviceToDevice, st);
-      else
-        k_gather_b<<<cb, 128, 0, st>>>(fp, fb, d.rel, rel_b, d.brows, d.bq, d.bs, nchi, var, colour, eps);
+  // base: the uniform upstream state
+  k_up_cols<<<cb, 128, 0, st>>>(cols, nchi, c.rho_0, c.rho_u_0, c.rho_v_0, c.rho_E_0, -1, 0, eps);
+  k_perturb_thermo<<<grid_for(d.G, 256), 256, 0, st>>>(pert_args(d));
+  launch_shock_bc_flags(d, false, true, true, true, 0, st);
+  launch_flux(d, false, Fb, st);
+  cudaMemcpyAsync(rel_b, d.rel, sizeof(double) * nchi, cudaMemcpyDeviceToDevice, st);
+  // one residual per variable and colour of columns, spread over the lanes (each with its own
+  // upstream columns)
+  const int K = (int)L.lane.size();
+  lanes_fork(L, st);
+  int q = 0;
+  for (int var = 0; var < 4; ++var)
+    for (int colour = 0; colour < 3; ++colour, ++q) {
+      const JacLane& l = L.lane[q % K];
+      const DevCtx ld = lane_ctx(d, l);
+      Flux4 fp;
+      for (int v = 0; v < 4; ++v) fp.v[v] = l.F[v];
+      double* const Fp[4] = {l.F[0], l.F[1], l.F[2], l.F[3]};
+      k_up_cols<<<cb, 128, 0, l.st>>>(l.cols, nchi, c.rho_0, c.rho_u_0, c.rho_v_0, c.rho_E_0, var, colour, eps);
+      k_perturb_thermo<<<grid_for(d.G, 256), 256, 0, l.st>>>(pert_args(ld));
+      launch_shock_bc_flags(ld, false, true, true, true, 0, l.st);
+      launch_flux(ld, false, Fp, l.st);
+      k_gather_b<<<cb, 128, 0, l.st>>>(fp, fb, ld.rel, rel_b, d.brows, d.bq, d.bs, nchi, var, colour, eps);
     }
+  lanes_join(L, st);
   d.up_cols = nullptr;
 }
 
@@ -1245,6 +1326,7 @@ struct LinearState {
   ExpmCache expm;
   KrylovScratch kry;
   int coop_blocks[2] = {0, 0};  // co-resident blocks per SM of k_expm_coop<false>, <true>
+  JacLanes lanes;               // workspaces of the linearisations' perturbed residuals
 };
 LinearState& linear_state(hymor_ctx* ctx) {
   void*& slot = ctx_linear_state(ctx);
@@ -1252,6 +1334,45 @@ LinearState& linear_state(hymor_ctx* ctx) {
   return *static_cast<LinearState*>(slot);
 }
 ExpmCache& expm_cache(hymor_ctx* ctx) { return linear_state(ctx).expm; }
+
+// The linearisation lanes, made on first use (kJacLanes x ~(7 G + 4 N) doubles).
+int ensure_lanes(hymor_ctx* ctx, JacLanes** out) {
+  JacLanes& L = linear_state(ctx).lanes;
+  *out = &L;
+  if (!L.lane.empty()) return 0;
+  const DevCtx& d = ctx_dev(ctx);
+  const size_t G = d.G, N = d.N, n = d.nchi;
+  auto pad = [](size_t k) { return (k + 31) & ~size_t(31); };  // 256-byte aligned parts
+  const size_t total = 7 * pad(G) + 4 * pad(N) + 4 * pad(n) + pad(17 * n + 16) + 3 * pad(n) + pad(4 * n);
+  if (cudaEventCreateWithFlags(&L.fork, cudaEventDisableTiming) != cudaSuccess)
+    return ctx_fail(ctx, HYMOR_ERR_CUDA, "linearisation lane event");
+  L.lane.resize(kJacLanes);
+  for (JacLane& l : L.lane) {
+    if (cudaStreamCreateWithFlags(&l.st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&l.done, cudaEventDisableTiming) != cudaSuccess ||
+        cudaMalloc(&l.mem, sizeof(double) * total) != cudaSuccess)
+      return ctx_fail(ctx, HYMOR_ERR_CUDA, "linearisation lane allocation failed");
+    cudaMemset(l.mem, 0, sizeof(double) * total);
+    double* b = l.mem;
+    auto take = [&](size_t k) {
+      double* r = b;
+      b += pad(k);
+      return r;
+    };
+    l.Y = Cons{take(G), take(G), take(G), take(G)};
+    l.p = take(G);
+    l.T = take(G);
+    l.aY = take(G);
+    for (int v = 0; v < 4; ++v) l.F[v] = take(N);
+    l.Yp = ShockPts{take(n), take(n), take(n), take(n)};
+    l.spl = take(17 * n + 16);
+    l.speed_x = take(n);
+    l.speed_y = take(n);
+    l.rel = take(n);
+    l.cols = take(4 * n);
+  }
+  return 0;
+}
 constexpr int kExpmCoopMinLaunches = 16;
 
 // hdts, hsteps (host, k entries, hsteps non-increasing), or null: vector c is propagated
@@ -1327,6 +1448,12 @@ void linear_state_release(void* p) {
   if (!p) return;
   LinearState* s = static_cast<LinearState*>(p);
   if (s->expm.buf) cudaFree(s->expm.buf);
+  for (JacLane& l : s->lanes.lane) {
+    if (l.st) cudaStreamDestroy(l.st);
+    if (l.done) cudaEventDestroy(l.done);
+    if (l.mem) cudaFree(l.mem);
+  }
+  if (s->lanes.fork) cudaEventDestroy(s->lanes.fork);
   delete s;  // the Krylov buffers are context allocations, freed with the context
 }
 }  // namespace hymor
@@ -1358,7 +1485,9 @@ int hymor_linearize(hymor_ctx* ctx) {
     if ((r = cuda_check(ctx, cudaStreamSynchronize(st)))) return r;
     if ((r = check_shock_rows_for_blocks(ctx, rows.data(), d.nchi, d.neta))) return r;
   }
-  launch_jacobian_assemble(d, st);
+  JacLanes* L = nullptr;
+  if ((r = ensure_lanes(ctx, &L))) return r;
+  launch_jacobian_assemble(d, st, *L);
   if ((r = cuda_check(ctx, cudaGetLastError()))) return r;
   if ((r = cuda_check(ctx, cudaStreamSynchronize(st)))) return r;
   d.sj.on = shock_blocks;
@@ -1675,7 +1804,9 @@ int hymor_linearize_b(hymor_ctx* ctx) {
   cudaMemcpyAsync(rows.data(), d.cell_idx, sizeof(int) * d.nchi, cudaMemcpyDeviceToHost, st);
   if ((r = cuda_check(ctx, cudaStreamSynchronize(st)))) return r;
   if ((r = check_b_rows(ctx, rows.data(), d.nchi, d.neta))) return r;
-  launch_b_assemble(d, st);
+  JacLanes* L = nullptr;
+  if ((r = ensure_lanes(ctx, &L))) return r;
+  launch_b_assemble(d, st, *L);
   if ((r = cuda_check(ctx, cudaGetLastError()))) return r;
   return cuda_check(ctx, cudaStreamSynchronize(st));
 }
