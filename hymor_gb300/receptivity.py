@@ -191,6 +191,88 @@ def LINEARIZE_L_(L: LinearOperatorGPU, s: Solution, w_infty):
     return s, ReceptivityOperator(L, s, w_infty)
 
 
+class _ReceptivityProblem:
+    """The reduced receptivity operator of one case, y -> K^-1 Z P^H R'MR P Z K^-H y on the
+    real form of the free unknowns (FREESTREAM_RECEPTIVITY.jl:80-116), split into the host
+    step that stages the input (begin), the device propagations, which it only enqueues on
+    the case's stream (launch), and the host step that reads the result (end)."""
+
+    def __init__(self, L_: ReceptivityOperator, s: Solution, T: float, order: int):
+        dt_cfl = CFL_TIMESTEP(s)
+        self.n_t = int(round(T / dt_cfl))
+        self.dt = T / self.n_t
+        self.L_, self.s, self.order = L_, s, order
+        self.n, self.n4 = L_.n, L_.n_down
+        self.nr = L_.L.n - self.n4                # shock displacements (0 without the shock unknowns)
+        self.nw, self.p = len(L_.w), 4 * s.nchi
+        # D on the free unknowns: the shock tail, then per frequency and column a 4 x 4 block
+        ci = s.get_state()["cell_idx"]
+        d_r = np.asarray(s.case.mesh["bt_a"])[np.arange(s.nchi), ci - 1] / 2 if self.nr else np.zeros(0)
+        Dk = freestream_weights(s, L_.w)                               # (Nw, Nchi, 4, 4)
+        self.Kinv = np.linalg.inv(np.linalg.cholesky(Dk))
+        self.kr = 1 / np.sqrt(d_r)
+        self.nf = self.nr + self.nw * self.p      # free unknowns (complex)
+        C0, _ = chu_blocks(s)
+        self.bC0 = DeviceBuffer(s.ctx, 8 * s.N * 16)
+        self.bC0.upload(np.ascontiguousarray(C0.reshape(-1)))
+        self.tail0 = DeviceBuffer(s.ctx, 8 * (self.n - self.n4))
+        self.tail0.upload(np.zeros(self.n - self.n4))
+        self.bz = [DeviceBuffer(s.ctx, 8 * 2 * self.n) for _ in range(2)]
+        self.count = 0
+
+    def k_inv_t(self, y):   # x = K^-H y on the free unknowns (K real)
+        x = np.empty_like(y)
+        nr = self.nr
+        x[:nr] = self.kr * y[:nr]
+        U = y[nr:].reshape(self.nw, 4, self.s.nchi)
+        x[nr:] = np.einsum("knji,kjn->kin", self.Kinv, U).reshape(-1)
+        return x
+
+    def k_inv(self, y):     # K^-1 y
+        x = np.empty_like(y)
+        nr = self.nr
+        x[:nr] = self.kr * y[:nr]
+        U = y[nr:].reshape(self.nw, 4, self.s.nchi)
+        x[nr:] = np.einsum("knij,kjn->kin", self.Kinv, U).reshape(-1)
+        return x
+
+    def begin(self, src):
+        c = self.s.ctx
+        self.count += 1
+        y = np.empty(2 * self.nf)
+        c.check(c.L.hymor_memcpy_d2h(c.h, y.ctypes.data, src, y.nbytes))
+        x = self.k_inv_t(y[:self.nf] + 1j * y[self.nf:])
+        z = np.zeros((2, self.n))
+        z[0, self.n4:], z[1, self.n4:] = x.real, x.imag
+        self.bz[0].upload(z.ravel())
+
+    def launch(self):
+        """Enqueues P, R'MR and P^H on the case's stream (returns before they run)."""
+        c, w, n, n4 = self.s.ctx, self.L_.w, self.n, self.n4
+        nw, dt, n_t, order = len(w), self.dt, self.n_t, self.order
+        c.check(c.L.hymor_recept_expm_dev(c.h, 1, nw, dp(w), dt, n_t, order, self.bz[0].ptr, self.bz[1].ptr, 0))
+        c.check(c.L.hymor_block4_apply_ext_dev(c.h, 2, n - n4, self.bC0.ptr, self.tail0.ptr, self.bz[1].ptr,
+                                               self.bz[0].ptr))
+        c.check(c.L.hymor_recept_expm_dev(c.h, 1, nw, dp(w), dt, n_t, order, self.bz[0].ptr, self.bz[1].ptr, 1))
+
+    def end(self, dst):
+        c, n, n4 = self.s.ctx, self.n, self.n4
+        out = self.bz[1].download(2 * n).reshape(2, n)
+        r = self.k_inv(out[0, n4:] + 1j * out[1, n4:])
+        res = np.concatenate([r.real, r.imag])
+        c.check(c.L.hymor_memcpy_h2d(c.h, dst, res.ctypes.data, res.nbytes))
+
+    def modes(self, Y, n_modes):
+        V = np.zeros((self.n, n_modes), dtype=complex)
+        for m_ in range(n_modes):
+            V[self.n4:, m_] = self.k_inv_t(Y[:self.nf, m_] + 1j * Y[self.nf:, m_])
+        return V
+
+    def free(self):
+        for b in [self.bC0, self.tail0] + self.bz:
+            b.free()
+
+
 def FREESTREAM_RECEPTIVITY(L_: ReceptivityOperator, s: Solution, n_modes: int, T: float, ncv: int | None = None,
                            tol: float = 1e-8, order: int = 5, seed: int = 5, maxit: int = 300,
                            modes: bool = False, keep_unconverged: bool = False):
@@ -209,77 +291,86 @@ def FREESTREAM_RECEPTIVITY(L_: ReceptivityOperator, s: Solution, n_modes: int, T
     unless keep_unconverged."""
     import time
     import warnings
-    dt_cfl = CFL_TIMESTEP(s)
-    n_t = int(round(T / dt_cfl))
-    dt = T / n_t
-    n, n4 = L_.n, L_.n_down
-    nr = L_.L.n - n4                     # shock displacements (0 without the shock unknowns)
-    nw, p = len(L_.w), 4 * s.nchi
-    # D on the free unknowns: the shock tail, then per frequency and column a 4 x 4 block
-    ci = s.get_state()["cell_idx"]
-    d_r = np.asarray(s.case.mesh["bt_a"])[np.arange(s.nchi), ci - 1] / 2 if nr else np.zeros(0)
-    Dk = freestream_weights(s, L_.w)                                   # (Nw, Nchi, 4, 4)
-    Kinv = np.linalg.inv(np.linalg.cholesky(Dk))
-    kr = 1 / np.sqrt(d_r)
-    nf = nr + nw * p                                                  # free unknowns (complex)
-
-    def k_inv_t(y):   # x = K^-H y on the free unknowns (K real)
-        x = np.empty_like(y)
-        x[:nr] = kr * y[:nr]
-        U = y[nr:].reshape(nw, 4, s.nchi)
-        x[nr:] = np.einsum("knji,kjn->kin", Kinv, U).reshape(-1)
-        return x
-
-    def k_inv(y):     # K^-1 y
-        x = np.empty_like(y)
-        x[:nr] = kr * y[:nr]
-        U = y[nr:].reshape(nw, 4, s.nchi)
-        x[nr:] = np.einsum("knij,kjn->kin", Kinv, U).reshape(-1)
-        return x
-    C0, _ = chu_blocks(s)
-    bC0 = DeviceBuffer(s.ctx, 8 * s.N * 16)
-    bC0.upload(np.ascontiguousarray(C0.reshape(-1)))
-    tail0 = DeviceBuffer(s.ctx, 8 * (n - n4))
-    tail0.upload(np.zeros(n - n4))
-    bz = [DeviceBuffer(s.ctx, 8 * 2 * n) for _ in range(2)]
-    c = s.ctx
-    count = [0]
+    pb = _ReceptivityProblem(L_, s, T, order)
 
     def apply_op(src, dst):
-        count[0] += 1
-        y = np.empty(2 * nf)
-        c.check(c.L.hymor_memcpy_d2h(c.h, y.ctypes.data, src, y.nbytes))
-        x = k_inv_t(y[:nf] + 1j * y[nf:])
-        z = np.zeros((2, n))
-        z[0, n4:], z[1, n4:] = x.real, x.imag
-        bz[0].upload(z.ravel())
-        c.check(c.L.hymor_recept_expm_dev(c.h, 1, nw, dp(L_.w), dt, n_t, order, bz[0].ptr, bz[1].ptr, 0))
-        c.check(c.L.hymor_block4_apply_ext_dev(c.h, 2, n - n4, bC0.ptr, tail0.ptr, bz[1].ptr, bz[0].ptr))
-        c.check(c.L.hymor_recept_expm_dev(c.h, 1, nw, dp(L_.w), dt, n_t, order, bz[0].ptr, bz[1].ptr, 1))
-        out = bz[1].download(2 * n).reshape(2, n)
-        r = k_inv(out[0, n4:] + 1j * out[1, n4:])
-        res = np.concatenate([r.real, r.imag])
-        c.check(c.L.hymor_memcpy_h2d(c.h, dst, res.ctypes.data, res.nbytes))
+        pb.begin(src)
+        pb.launch()
+        pb.end(dst)
     ncv = ncv or max(2 * n_modes + 1, 16)
     t0 = time.perf_counter()
     try:
-        lam, resid, nops, Y = krylov_schur(c, 2 * nf, apply_op, n_modes, ncv, tol=tol, maxit=maxit, seed=seed,
-                                           symmetric=True, want_vectors=True)
+        lam, resid, nops, Y = krylov_schur(s.ctx, 2 * pb.nf, apply_op, n_modes, ncv, tol=tol, maxit=maxit,
+                                           seed=seed, symmetric=True, want_vectors=True)
+        elapsed = time.perf_counter() - t0
+        lam = np.real(lam)
+        converged = bool(np.all(resid <= tol * np.abs(lam)))
+        gains = lam / 2
+        V = pb.modes(Y, n_modes) if (modes and Y is not None) else None
     finally:
-        for b in [bC0, tail0] + bz:
-            b.free()
-    elapsed = time.perf_counter() - t0
-    lam = np.real(lam)
-    converged = bool(np.all(resid <= tol * np.abs(lam)))
-    gains = lam / 2
-    V = None
-    if modes and Y is not None:
-        V = np.zeros((n, n_modes), dtype=complex)
-        for m_ in range(n_modes):
-            V[n4:, m_] = k_inv_t(Y[:nf, m_] + 1j * Y[nf:, m_])
+        pb.free()
     if not converged and not keep_unconverged:
         warnings.warn(f"receptivity solve did not reach tol {tol:g} in {maxit} restarts; returning NaN")
         gains = np.full(n_modes, np.nan)
-        V = np.full((n, n_modes), np.nan + 0j) if modes else None
-    info = dict(resid=resid, dt=dt, n_t=n_t, nops=nops, seconds=elapsed, converged=converged, applications=count[0])
-    return V, gains, n_t * dt, info
+        V = np.full((pb.n, n_modes), np.nan + 0j) if modes else None
+    info = dict(resid=resid, dt=pb.dt, n_t=pb.n_t, nops=nops, seconds=elapsed, converged=converged,
+                applications=pb.count)
+    return V, gains, pb.n_t * pb.dt, info
+
+
+def FREESTREAM_RECEPTIVITY_BATCH(cases, n_modes: int, T: float, ncv: int | None = None, tol: float = 1e-8,
+                                 order: int = 5, seed: int = 5, maxit: int = 300, keep_unconverged: bool = False):
+    """FREESTREAM_RECEPTIVITY for several cases at once: cases = [(L_, s), ...], each its own
+    context and grid (sizes may differ), each L_ with its own frequencies. One Krylov-Schur
+    solve per case in lockstep (each makes the operations of its own FREESTREAM_RECEPTIVITY
+    with the same seed, so the gains are the same): every round stages each unfinished case's
+    vector, then enqueues all their propagations before waiting for any, so the cases'
+    propagations run concurrently on their streams, then reads the results. The reference
+    solves one case per FREESTREAM_RECEPTIVITY call. Returns [(gains, info)] per case (info
+    seconds: the whole batched solve)."""
+    import time
+    import warnings
+    from .krylov import krylov_schur_steps
+    probs = [_ReceptivityProblem(L_, s, T, order) for (L_, s) in cases]
+    ncv = ncv or max(2 * n_modes + 1, 16)
+    gens = [krylov_schur_steps(s.ctx, 2 * pb.nf, n_modes, ncv, tol, maxit, seed, True, None, False)
+            for pb, (_, s) in zip(probs, cases)]
+    results: list = [None] * len(gens)
+    pending = {}
+    t0 = time.perf_counter()
+    try:
+        for i, g in enumerate(gens):
+            try:
+                pending[i] = next(g)
+            except StopIteration as done:
+                results[i] = done.value
+        while pending:
+            idx = sorted(pending)
+            for i in idx:
+                probs[i].begin(pending[i][0])
+            for i in idx:
+                probs[i].launch()
+            for i in idx:
+                probs[i].end(pending[i][1])
+            for i in idx:
+                try:
+                    pending[i] = gens[i].send(None)
+                except StopIteration as done:
+                    results[i] = done.value
+                    del pending[i]
+        elapsed = time.perf_counter() - t0
+    finally:
+        for pb in probs:
+            pb.free()
+    out = []
+    for pb, res in zip(probs, results):
+        lam, resid, nops = res
+        lam = np.real(lam)
+        converged = bool(np.all(resid <= tol * np.abs(lam)))
+        gains = lam / 2
+        if not converged and not keep_unconverged:
+            warnings.warn(f"receptivity solve did not reach tol {tol:g}; its gains are NaN")
+            gains = np.full(n_modes, np.nan)
+        out.append((gains, dict(resid=resid, dt=pb.dt, n_t=pb.n_t, nops=nops, seconds=elapsed, converged=converged,
+                                applications=pb.count)))
+    return out

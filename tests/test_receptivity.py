@@ -278,3 +278,31 @@ def test_linearize_b_axisymmetric_first_column():
     assert np.all(bq[0, 1, :, 2] == 0) and np.all(bq[1, 0, :, 2] == 0)
     assert np.all(bs[0, 1, 2] == 0) and np.all(bs[1, 0, 2] == 0)
     assert np.max(np.abs(bq[0, 1, :, 0])) > 0 and np.max(np.abs(bq[2, 1, :, 2])) > 0
+
+
+@pytest.mark.gpu
+def test_receptivity_batch_uneven_grids(require_gpu):
+    """FREESTREAM_RECEPTIVITY_BATCH: three cases of different grids, Mach numbers and
+    frequency sets solved together (lockstep Krylov-Schur, the cases' propagations enqueued
+    together on their own streams) give each case's own FREESTREAM_RECEPTIVITY gains: the
+    same operations in the same order, so to rounding of nothing (1e-12 allowed)."""
+    from hymor_gb300 import receptivity as R
+    from hymor_gb300 import solver as S
+    specs = [(24, 20, 5.0, 1e4, [0.0, 2.0]), (36, 24, 6.0, 2e4, [0.5, 1.0, 3.0]), (28, 28, 4.0, 5e3, [1.0])]
+    cases, sols = [], []
+    for nchi, neta, M, Re, w in specs:
+        cs = C.initial_state(C.cylinder_config(nchi, neta, Mach=M, Re=Re))
+        sol = S.Solution(cs)
+        S.ADVECT_FLOW(sol, 20)
+        _, L = S.LINEARIZE_L(sol)
+        _, Lr = R.LINEARIZE_L_(L, sol, w)
+        cases.append((Lr, sol))
+        sols.append(sol)
+    batch = R.FREESTREAM_RECEPTIVITY_BATCH(cases, 2, 0.01, ncv=16, tol=1e-10)
+    for (Lr, sol), (G, info) in zip(cases, batch):
+        _, G1, _, info1 = R.FREESTREAM_RECEPTIVITY(Lr, sol, 2, 0.01, ncv=16, tol=1e-10)
+        assert info["converged"] and info1["converged"]
+        assert np.allclose(G, G1, rtol=1e-12, atol=0), (G, G1)
+        assert info["nops"] == info1["nops"]
+    for sol in sols:
+        sol.close()
