@@ -200,6 +200,14 @@ def matvec_numbers(sol, cs, fp64_peak_tflops: float, hbm_gbs: float, cpu: bool, 
     oracle's single-vector matvec on the host."""
     import torch
     from hymor_gb300._lib import dp
+    from hymor_gb300 import baseflow as B
+    base, rec = B.solution("cylinder_800x400"), B.load("cylinder_800x400")
+    state = "synthetic start (no converged base flow cached)"
+    if base is not None:
+        # the Jacobian of the converged base flow (its own, taller domain); the matvec's
+        # work per cell does not depend on the state
+        sol, cs = base, B.case_of(rec, "cylinder_800x400")
+        state = f"converged base flow, step residual {float(rec['residual']):.2e} at t = {float(rec['t']):.1f}"
     L, h = sol.ctx.L, sol.ctx.h
     t0 = time.perf_counter()
     sol.ctx.check(L.hymor_linearize(h))
@@ -231,7 +239,7 @@ def matvec_numbers(sol, cs, fp64_peak_tflops: float, hbm_gbs: float, cpu: bool, 
                 "flop_per_cell_matvec": MATVEC_FLOP}
 
     out = {"workload": f"linearised-residual matvec, {k} seeded unit-norm vectors x {n} ({NCHI}x{NETA})",
-           "vectors": k, "batched_ms": t_b * 1e3, "plain_ms": t_p * 1e3, "transpose_batched_ms": t_t * 1e3,
+           "state": state, "vectors": k, "batched_ms": t_b * 1e3, "plain_ms": t_p * 1e3, "transpose_batched_ms": t_t * 1e3,
            "batched_speedup": t_p / t_b,
            "per_vector_us": {"batched": t_b / k * 1e6, "plain": t_p / k * 1e6},
            "roofline": roof(t_b, k), "plain_roofline": roof(t_p, 1),
@@ -250,6 +258,8 @@ def matvec_numbers(sol, cs, fp64_peak_tflops: float, hbm_gbs: float, cpu: bool, 
         out["cpu_baseline"] = {"ms_per_vector": el * 1e3, "cores": 1, "kind": "port",
                                "sample": f"{nv} vectors through the oracle's stencil matvec"}
     del dX, dY
+    if base is not None:
+        base.close()
     out["propagator"] = propagator_numbers(fp64_peak_tflops)
     try:
         out["shock_unknowns"] = extended_numbers(cs)
@@ -348,39 +358,146 @@ def propagator_numbers(fp64_peak_tflops: float, nchi: int = 100, neta: int = 80,
             "gpu_launches": {"batched": 1, "plain": k}}
 
 
-def solve_numbers(nchi: int = 100, neta: int = 80, n_modes: int = 4, T_ref: float = 0.5, tol: float = 1e-8,
-                  block: int = 8, steps: int = 20, maxit: int = 200):
-    """Solve level (--solve, minutes): the n_modes eigenvalues of largest magnitude of
-    exp(L T_ref) on the cylinder (after `steps` RK4 steps of the synthetic start), by the
-    block Krylov-Schur (`block` vectors per batched propagation) and by the one-vector
-    Krylov-Schur, both to Ritz residual tol or maxit restarts, from start vectors on the
-    flow cells (the masked operator's other directions only carry the trivial eigenvalue
-    0); host clock around each solve. Reports the residuals reached: on a clustered
-    spectrum neither solve may reach tol within maxit."""
-    from hymor_gb300 import case as C
+def _base_solution(name: str):
+    """The converged base flow of `name` (hymor_gb300/_cache, made by `python -m
+    hymor_gb300.baseflow name`), or None."""
+    from hymor_gb300 import baseflow as B
+    return B.solution(name), B.load(name)
+
+
+def solve_eigen(n_modes: int = 12, ncv: int = 60, substeps: int = 50, order: int = 4, tol: float = 1e-8,
+                block: int = 6, maxit: int = 300):
+    """Solve level, modal analysis (sphere-cone 1200 x 400, M 6, Re 2e4, on its converged
+    base flow): the n_modes eigenvalues of largest modulus of exp(L dt_50), built from
+    `substeps` Taylor steps of degree `order` of the CFL dt, Krylov basis ncv, Ritz residual
+    tol, start vectors on the flow cells; the one-vector Krylov-Schur against the block
+    Krylov-Schur (`block` vectors per batched propagation), both through hymor_eigs. Host
+    clock around each solve."""
     from hymor_gb300 import solver as S
-    cfg = C.cylinder_config(nchi, neta)
-    sol = S.Solution(C.initial_state(cfg))
-    S.ADVECT_FLOW(sol, steps)
+    sol, rec = _base_solution("sphere_cone_1200x400")
+    if sol is None:
+        return {"unavailable": "no converged sphere-cone base flow: run python -m hymor_gb300.baseflow "
+                               "sphere_cone_1200x400"}
     _, Lop = S.LINEARIZE_L(sol)
-    lam_b, info_b = S.EIGENVALUES(Lop, sol, n_modes, T_ref=T_ref, tol=tol, block=block, flow_start=True,
-                                  maxit=maxit, keep_unconverged=True)
-    lam_p, info_p = S.EIGENVALUES(Lop, sol, n_modes, T_ref=T_ref, tol=tol, flow_start=True, maxit=maxit,
-                                  keep_unconverged=True)
-    scale = float(np.max(np.abs(lam_p)))
-    agree = max(float(np.min(np.abs(lam_p - a))) for a in lam_b) / scale
+    dt = S.CFL_TIMESTEP(sol)
+    out = {"workload": f"EIGENVALUES: {n_modes} eigenvalues of exp(L {substeps} dt), {substeps} Taylor steps of "
+                       f"degree {order}, Krylov {ncv}, sphere-cone 1200x400 M6 Re2e4, Ritz residual {tol:g}",
+           "base_flow": {"residual": float(rec["residual"]), "t": float(rec["t"]),
+                         "levels": rec["levels"].tolist()},
+           "n": Lop.n, "dt": dt}
+    arms = {}
+    for name, b in (("plain", 1), ("batched", block)):
+        lam, info = S.EIGENVALUES(Lop, sol, n_modes, T_ref=substeps * dt, ncv=ncv, tol=tol, order=order,
+                                  block=b, flow_start=True, maxit=maxit, keep_unconverged=True)
+        rel = info["resid"] / np.abs(info["mu"])
+        arms[name] = dict(seconds=info["seconds"], block=b, converged=info["converged"], restarts=info["restarts"],
+                          vector_propagations=info["nops"], max_resid_rel=float(np.max(rel)),
+                          s_per_vector_propagation=info["seconds"] / max(info["nops"], 1),
+                          eigenvalues=[[float(np.real(a)), float(np.imag(a))] for a in lam])
+    la = np.array([complex(*e) for e in arms["plain"]["eigenvalues"]])
+    lb = np.array([complex(*e) for e in arms["batched"]["eigenvalues"]])
+    out.update(arms)
+    out["batched_speedup"] = arms["plain"]["seconds"] / arms["batched"]["seconds"]
+    out["eigenvalues_agree_rel"] = float(max(np.min(np.abs(la - x)) for x in lb) / np.max(np.abs(la)))
     sol.close()
-    rel = {k: [float(r) for r in i["resid"] / np.abs(i["mu"])] for k, i in (("batched", info_b), ("plain", info_p))}
-    return {"workload": f"EIGENVALUES, {n_modes} modes of exp(L {T_ref}) ({info_p['timesteps']} Taylor steps of "
-                        f"degree 5), cylinder {nchi}x{neta}, Ritz residual {tol:g}",
-            "batched_s": info_b["seconds"], "plain_s": info_p["seconds"],
-            "batched_speedup": info_p["seconds"] / info_b["seconds"], "block": block,
-            "propagations": {"batched": info_b["nops"], "plain": info_p["nops"]},
-            "s_per_vector_propagation": {"batched": info_b["seconds"] / info_b["nops"],
-                                         "plain": info_p["seconds"] / info_p["nops"]},
-            "resid_rel": rel, "converged": {k: bool(max(v) <= tol) for k, v in rel.items()},
-            "eigenvalues_agree_rel": agree,
-            "eigenvalues": [[float(np.real(a)), float(np.imag(a))] for a in lam_p]}
+    return out
+
+
+def solve_tg(Ts=(0.0625, 0.125, 0.25, 0.5), n_modes: int = 2, tol: float = 1e-8, maxit: int = 300):
+    """Solve level, transient growth (cylinder 600 x 300, M 5, on its converged base flow):
+    the optimal gains of the horizons Ts, solved together (hymor_tg_gain with every horizon:
+    one batched forward and one batched adjoint propagation per round) against one horizon
+    after another, gains matched to 1e-6. Host clock around each solve."""
+    from hymor_gb300 import solver as S
+    sol, rec = _base_solution("cylinder_600x300")
+    if sol is None:
+        return {"unavailable": "no converged 600x300 cylinder base flow: run python -m hymor_gb300.baseflow "
+                               "cylinder_600x300"}
+    _, Lop = S.LINEARIZE_L(sol)
+    dt = S.CFL_TIMESTEP(sol)
+    Gb, infos = S.TRANSIENT_GROWTH_HORIZONS(Lop, sol, n_modes, Ts, tol=tol, maxit=maxit, keep_unconverged=True)
+    t_batched = infos[0]["seconds"]
+    t_plain, Gp, conv_p = 0.0, [], []
+    for T in Ts:
+        g, info = S.TRANSIENT_GROWTH_DOWNSTREAM(Lop, sol, n_modes, T, tol=tol, maxit=maxit, keep_unconverged=True)
+        t_plain += info["seconds"]
+        Gp.append(g)
+        conv_p.append(info["converged"])
+    Gp = np.array(Gp)
+    sol.close()
+    return {"workload": f"TRANSIENT_GROWTH_DOWNSTREAM: {n_modes} gains for T in {list(Ts)}, cylinder 600x300 M5 "
+                        f"Re1e4, Ritz residual {tol:g}",
+            "base_flow": {"residual": float(rec["residual"]), "t": float(rec["t"]), "levels": rec["levels"].tolist()},
+            "dt_cfl": dt, "taylor_steps": [inf["n_t"] for inf in infos],
+            "batched": {"seconds": t_batched, "converged": [inf["converged"] for inf in infos],
+                        "vector_applications": [inf["nops"] for inf in infos]},
+            "plain": {"seconds": t_plain, "converged": conv_p},
+            "batched_speedup": t_plain / t_batched,
+            "gains": Gb.tolist(),
+            "gains_agree_rel": float(np.max(np.abs(Gb - Gp) / np.abs(Gp)))}
+
+
+def solve_receptivity(ncases: int = 16, nw: int = 24, T: float = 0.01, n_modes: int = 1, tol: float = 1e-8,
+                      steps: int = 200, seed: int = 6, grid_lo=(80, 40), grid_hi=(240, 96)):
+    """Batched receptivity over uneven grids (the fifth benchmark configuration, at reduced
+    sizes): `ncases` shock-fitted CPG cases, blunt wedge (cylinder nose) and axisymmetric
+    blunt cone alternately, grids drawn by seed between grid_lo and grid_hi, Mach uniform in
+    4-8, Re log-uniform in 5e3-5e4, `steps` RK4 steps from the synthetic start, each with nw
+    freestream wavenumbers k in logspace(-1, 1.5, nw) (convected at the freestream speed:
+    w = k). The optimal freestream disturbances of every case: FREESTREAM_RECEPTIVITY_BATCH
+    (all cases in lockstep, their propagations concurrent) against one FREESTREAM_RECEPTIVITY
+    after another, gains matched."""
+    from hymor_gb300 import baseflow as B
+    from hymor_gb300 import case as C
+    from hymor_gb300 import receptivity as R
+    from hymor_gb300 import solver as S
+    rng = np.random.Generator(np.random.PCG64(seed))
+    w = np.logspace(-1, 1.5, nw)
+    cases, meta = [], []
+    t_setup = time.perf_counter()
+    for i in range(ncases):
+        nchi = int(rng.integers(grid_lo[0], grid_hi[0] + 1)) // 2 * 2
+        neta = int(rng.integers(grid_lo[1], grid_hi[1] + 1))
+        M, Re = float(rng.uniform(4, 8)), float(10 ** rng.uniform(np.log10(5e3), np.log10(5e4)))
+        # the cylinders on the taller domain of the base-flow cases (the bow shock of a slow
+        # case stands off further than the default domain reaches); first-order extrapolation
+        # above the shock through the start-up transient, as the base-flow marches
+        make = B.cylinder if i % 2 == 0 else C.blunt_cone_config
+        sol = S.Solution(C.initial_state(make(nchi, neta, Mach=M, Re=Re, shock_interp="1st")))
+        S.ADVECT_FLOW(sol, steps)
+        _, L = S.LINEARIZE_L(sol)
+        _, Lr = R.LINEARIZE_L_(L, sol, w)
+        cases.append((Lr, sol))
+        meta.append({"geometry": "blunt wedge" if i % 2 == 0 else "blunt cone", "grid": [nchi, neta],
+                     "Mach": round(M, 3), "Re": round(Re, 1), "unknowns": Lr.n})
+    t_setup = time.perf_counter() - t_setup
+    batch = R.FREESTREAM_RECEPTIVITY_BATCH(cases, n_modes, T, tol=tol, keep_unconverged=True)
+    t_batched = batch[0][1]["seconds"]
+    t_plain, worst = 0.0, 0.0
+    for (Lr, sol), (G, info), m in zip(cases, batch):
+        _, G1, _, info1 = R.FREESTREAM_RECEPTIVITY(Lr, sol, n_modes, T, tol=tol, keep_unconverged=True)
+        t_plain += info1["seconds"]
+        worst = max(worst, float(np.max(np.abs(G - G1) / np.abs(G1))))
+        m.update(gain=float(G[0]), converged=info["converged"], taylor_steps=info["n_t"], applications=info["nops"])
+    for _, sol in cases:
+        sol.close()
+    return {"workload": f"FREESTREAM_RECEPTIVITY of {ncases} uneven cases x {nw} wavenumbers, T = {T:g}, "
+                        f"{n_modes} gain each, tol {tol:g}",
+            "cases": meta, "setup_s": t_setup, "batched_s": t_batched, "plain_s": t_plain,
+            "batched_speedup": t_plain / t_batched, "gains_agree_rel": worst,
+            "note": f"synthetic states after {steps} RK4 steps (no converged base flows for these grids); "
+                    "grids reduced from 200x100..1000x400 so that both arms finish in minutes"}
+
+
+def solve_numbers(which: str):
+    out = {}
+    if which in ("all", "eigen"):
+        out["eigen"] = solve_eigen()
+    if which in ("all", "tg"):
+        out["transient_growth"] = solve_tg()
+    if which in ("all", "recept"):
+        out["receptivity"] = solve_receptivity()
+    return out
 
 
 def run_reference(args, world, rank):
@@ -430,7 +547,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--no-matvec", action="store_true")
-    ap.add_argument("--solve", action="store_true", help="add the solve-level timing (minutes)")
+    ap.add_argument("--solve", nargs="?", const="all", default=None, choices=["all", "eigen", "tg", "recept"],
+                    help="add the solve-level timing on the converged base flows (minutes)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_env()
@@ -451,6 +569,16 @@ def main():
     # warm-up (graph capture happens on the first step)
     ms = ctypes.c_float()
     sol.ctx.check(L.hymor_bench_steps(h, args.warmup, FLUSH_BYTES, ctypes.byref(ms)))
+    # the flux configuration picked by the library's autotuner on this case (state restored after)
+    choice = np.zeros(3, dtype=np.int32)
+    tune_ms = (ctypes.c_float * 12)()
+    sol.ctx.check(L.hymor_autotune(h, 20, ip(choice), tune_ms))
+    autotune = {"flux_tile": f"31x{int(choice[0])}", "interior_spare_blocks_per_sm": int(choice[1]),
+                "halo": "TMA" if choice[2] else "thread loads",
+                "candidates_ms_per_step": {f"{'tma' if t else 'ld'}/31x{r}/spare{sp}":
+                                           round(tune_ms[6 * t + 3 * (r == 16) + sp], 4)
+                                           for t in (0, 1) for r in (8, 16) for sp in (0, 1, 2)}}
+    sol.ctx.check(L.hymor_bench_steps(h, 2, FLUSH_BYTES, ctypes.byref(ms)))
     # timed region: K steps, flux-kernel events on
     sol.ctx.check(L.hymor_profile_flux(h, 1, None, None))
     torch.cuda.synchronize()
@@ -467,6 +595,14 @@ def main():
     t_dev = max_over_ranks(dist, ms.value / 1e3)
     total_cell_stages = CELLS * STAGES * args.steps * world
     value = total_cell_stages / t_dev / 1e6
+    # the same steps with the viscous terms in FP64 instead of float-float (a reported
+    # comparison; the state marches on from where the timed steps left it)
+    n64 = max(50, args.steps // 4)
+    sol.set_step_viscous(0)
+    sol.ctx.check(L.hymor_bench_steps(h, 3, FLUSH_BYTES, ctypes.byref(ms)))
+    sol.ctx.check(L.hymor_bench_steps(h, n64, FLUSH_BYTES, ctypes.byref(ms)))
+    value_fp64_viscous = CELLS * STAGES * n64 * world / max_over_ranks(dist, ms.value / 1e3) / 1e6
+    sol.set_step_viscous(1)
 
     # end-to-end through the public API with pinned host buffers
     G = (NCHI + 2) * (NETA + 2)
@@ -529,6 +665,10 @@ def main():
                                "stage_fields": ["update", "flux_interior", "start_shock_bc_after_interior", "flux_shock_bc"],
                                "end": round(phases[17] * 1e3, 1)},
             "clocks": clk.summary(),
+            "viscous_arithmetic": "float-float (FP32 pairs, ~48-bit) for the viscous gradients, stresses and "
+                                  "heat flux of the step; FP64 everywhere else",
+            "value_fp64_viscous": value_fp64_viscous,
+            "autotune": autotune,
         }
         if not args.no_cpu_baseline and world == 1:
             line["cpu_baseline"] = cpu_baseline_sample(cs)
@@ -538,7 +678,7 @@ def main():
             line["matvec"] = matvec_numbers(sol, cs, fp64_peak.value, hbm,
                                             cpu=not args.no_cpu_baseline and world == 1)
         if args.solve:
-            line["solve"] = solve_numbers()
+            line["solve"] = solve_numbers(args.solve)
         print(json.dumps(line), flush=True)
     sol.close()
     if dist is not None:
