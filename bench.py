@@ -493,6 +493,10 @@ def solve_numbers(which: str):
     out = {}
     if which in ("all", "eigen"):
         out["eigen"] = solve_eigen()
+    if which in ("all", "eigen4"):
+        # the same operator over a ten times longer horizon (500 degree-4 steps), 4 eigenvalues:
+        # exp(L 50 dt) puts the whole stable spectrum within ~1 % of |mu| = 1
+        out["eigen_4_modes_500_steps"] = solve_eigen(n_modes=4, substeps=500, maxit=150)
     if which in ("all", "tg"):
         out["transient_growth"] = solve_tg()
     if which in ("all", "recept"):
@@ -547,7 +551,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--no-matvec", action="store_true")
-    ap.add_argument("--solve", nargs="?", const="all", default=None, choices=["all", "eigen", "tg", "recept"],
+    ap.add_argument("--solve", nargs="?", const="all", default=None, choices=["all", "eigen", "eigen4", "tg", "recept"],
                     help="add the solve-level timing on the converged base flows (minutes)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
