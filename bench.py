@@ -496,7 +496,7 @@ def solve_numbers(which: str):
     if which in ("all", "eigen4"):
         # the same operator over a ten times longer horizon (500 degree-4 steps), 4 eigenvalues:
         # exp(L 50 dt) puts the whole stable spectrum within ~1 % of |mu| = 1
-        out["eigen_4_modes_500_steps"] = solve_eigen(n_modes=4, substeps=500, maxit=150)
+        out["eigen_4_modes_500_steps"] = solve_eigen(n_modes=4, substeps=500, maxit=60)
     if which in ("all", "tg"):
         out["transient_growth"] = solve_tg()
     if which in ("all", "recept"):
