@@ -24,10 +24,11 @@ struct hymor_ctx_s {
   cudaStream_t side = nullptr;      // high-priority stream of the shock/BC chain inside the step graph
   cudaStream_t fit = nullptr;       // the first spline fit and the first jump kernels of a step
   cudaStream_t c1 = nullptr;        // the shock/boundary-class flux, beside the interior-class flux
+  cudaStream_t cfl = nullptr;       // the step's CFL reduction, at the lowest priority
   cudaEvent_t fork_ev[8] = {}, join_ev[8] = {};
   cudaEvent_t fit_fork = nullptr, fit_join = nullptr;
   cudaEvent_t c1_fork[4] = {}, c1_join[4] = {};
-  cudaEvent_t u0_ev = nullptr, cfl_ev = nullptr, cls_ev = nullptr;
+  cudaEvent_t u0_ev = nullptr, cfl_ev = nullptr, cls_ev = nullptr, cfl_fork = nullptr;
   int device = 0;
   std::string err;
   std::vector<void*> allocs;
@@ -244,11 +245,17 @@ int enqueue_step(hymor_ctx* ctx, bool with_events) {
     TRY(fork());
     launch_classify_tiles(d, sx);
     CU(cudaEventRecord(ctx->cls_ev, sx));
-    // with shock fitting the step recomputes the sound speed for the CFL maximum only
-    // (and the outflow_NRCBC lines); the full field is recomputed when next needed
-    launch_sound_cmax(d, shock, sx, true);
-    launch_cfl(d, sx);
-    CU(cudaEventRecord(ctx->cfl_ev, sx));
+    // The CFL reduction on a stream of the lowest priority: its full-grid kernels would
+    // otherwise take the block slots that the interior flux leaves free ahead of the first
+    // stage's jump and boundary kernels, which the boundary-class flux waits for; dt is
+    // needed only by the first MOVE_SHOCK and the second stage update. With shock fitting
+    // the step recomputes the sound speed for the CFL maximum only (and the outflow_NRCBC
+    // lines); the full field is recomputed when next needed.
+    CU(cudaEventRecord(ctx->cfl_fork, st));
+    CU(cudaStreamWaitEvent(ctx->cfl, ctx->cfl_fork, 0));
+    launch_sound_cmax(d, shock, ctx->cfl, true);
+    launch_cfl(d, ctx->cfl);
+    CU(cudaEventRecord(ctx->cfl_ev, ctx->cfl));
     TRY(ev(16));
     launch_update_thermo(d, 0, 0, 0, st);
     for (int k = 0; k < 4; ++k) {
@@ -277,6 +284,7 @@ int enqueue_step(hymor_ctx* ctx, bool with_events) {
       CU(cudaEventRecord(ctx->c1_join[k], ctx->c1));
       if (k == 0) {
         CU(cudaStreamWaitEvent(sx, ctx->c1_fork[0], 0));
+        CU(cudaStreamWaitEvent(sx, ctx->cfl_ev, 0));
         launch_move_shock(d, false, wY[0], wA[0], sx);
       }
       // next fit (stage k+1 on Y, or the step-end fit on S) overlaps this stage's remaining work
@@ -587,12 +595,13 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
   {
     std::vector<double> lrg, btg, rvol, rxl, rxb, gvis;
     face_geometry(*cfg, *mesh, lrg, btg, rvol, rxl, rxb, gvis);
-    {  // float-float copies of the planes the viscous terms read: nx, ny, g1, g2/4, 1/(4 len)
+    {  // float-float copies of the planes the viscous terms read: nx, ny, g1, g2/4, 1/(4 len),
+       // and the half area that scales them
       const long NLR = (long)(cfg->nchi + 1) * cfg->neta, NBT = (long)cfg->nchi * (cfg->neta + 1);
-      const int planes[5] = {0, 1, 3, 4, 5};
+      const int planes[6] = {0, 1, 3, 4, 5, 2};
       auto split = [](const std::vector<double>& g, long nf, const int* pl) {
-        std::vector<float2> out(5 * nf);
-        for (int q = 0; q < 5; ++q)
+        std::vector<float2> out(6 * nf);
+        for (int q = 0; q < 6; ++q)
           for (long f = 0; f < nf; ++f) {
             const double x = g[pl[q] * nf + f];
             const float h = (float)x;
@@ -614,6 +623,20 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
         return bail(fail(ctx, HYMOR_ERR_CUDA, "float-float geometry upload failed"));
       m.lrf = q1;
       m.btf = q2;
+      // the normals times the half area, rounded once
+      auto fold = [](const std::vector<double>& g, long nf) {
+        std::vector<double> out(2 * nf);
+        for (int q = 0; q < 2; ++q)
+          for (long f = 0; f < nf; ++f) out[q * nf + f] = g[q * nf + f] * g[2 * nf + f];
+        return out;
+      };
+      const std::vector<double> la = fold(lrg, NLR), ba = fold(btg, NBT);
+      double *a1 = nullptr, *a2 = nullptr;
+      if ((r = upload(ctx, &a1, la.data(), la.size(), "lr n A/2")) ||
+          (r = upload(ctx, &a2, ba.data(), ba.size(), "bt n A/2")))
+        return bail(r);
+      m.lra = a1;
+      m.bta = a2;
     }
     double *p1, *p2, *p3, *p4, *p5, *p6;
     if ((r = upload(ctx, &p1, lrg.data(), lrg.size(), "lr geometry"))) return bail(r);
@@ -710,6 +733,7 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
     cudaDeviceGetStreamPriorityRange(&lo, &hi);
     if (cudaStreamCreateWithPriority(&ctx->side, cudaStreamNonBlocking, hi) != cudaSuccess ||
         cudaStreamCreateWithPriority(&ctx->fit, cudaStreamNonBlocking, hi) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&ctx->cfl, cudaStreamNonBlocking, lo) != cudaSuccess ||
         cudaStreamCreateWithPriority(&ctx->c1, cudaStreamNonBlocking, hi) != cudaSuccess)
       return bail(fail(ctx, HYMOR_ERR_CUDA, "side stream creation failed"));
     for (int k = 0; k < 4; ++k)
@@ -720,7 +744,8 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
         cudaEventCreateWithFlags(&ctx->fit_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->u0_ev, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->cfl_ev, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&ctx->cls_ev, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&ctx->cls_ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->cfl_fork, cudaEventDisableTiming) != cudaSuccess)
       return bail(fail(ctx, HYMOR_ERR_CUDA, "event"));
   }
   if (cudaMallocHost(&ctx->stage, stage_bytes(d.nchi)) != cudaSuccess)
@@ -752,12 +777,14 @@ int hymor_ctx_destroy(hymor_ctx* ctx) {
   if (ctx->u0_ev) cudaEventDestroy(ctx->u0_ev);
   if (ctx->cfl_ev) cudaEventDestroy(ctx->cfl_ev);
   if (ctx->cls_ev) cudaEventDestroy(ctx->cls_ev);
+  if (ctx->cfl_fork) cudaEventDestroy(ctx->cfl_fork);
   for (auto e : ctx->c1_fork)
     if (e) cudaEventDestroy(e);
   for (auto e : ctx->c1_join)
     if (e) cudaEventDestroy(e);
   if (ctx->side) cudaStreamDestroy(ctx->side);
   if (ctx->fit) cudaStreamDestroy(ctx->fit);
+  if (ctx->cfl) cudaStreamDestroy(ctx->cfl);
   if (ctx->c1) cudaStreamDestroy(ctx->c1);
   for (auto e : ctx->prof_ev) cudaEventDestroy(e);
   if (ctx->t0) cudaEventDestroy(ctx->t0);

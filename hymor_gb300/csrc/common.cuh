@@ -44,10 +44,14 @@ struct DevMesh {
                         // (viscous CFL rate over the volume, CFL_TIMESTEP.jl:110-113)
   const double *xt, *yt;  // x_ext, y_ext transposed: ghosted (i, j) at i * (Neta + 2) + j
   // float-float copies (high, low) of the lr / bt face planes nx, ny, s g1 (s h1), s g2/4
-  // (s h2/4), s/(4 len), 5 x NLR and 5 x NBT, for the float-float viscous terms of the
+  // (s h2/4), s/(4 len), A/2, 6 x NLR and 6 x NBT, for the float-float viscous terms of the
   // RK-step flux
   const float2* lrf;
   const float2* btf;
+  // nx A/2, ny A/2 (FP64, 2 x NLR and 2 x NBT): the inviscid face fluxes of the RK step with
+  // the area folded into the normal
+  const double* lra;
+  const double* bta;
 };
 
 struct Cons {

@@ -1105,12 +1105,12 @@ __global__ void k_classify_tiles(const int* __restrict__ cell_idx, int* lists, i
 // top) and the corner sums at the face's two ends (lo, hi), the face's float-float planes
 // (nx, ny, s g1, s g2/4, s/(4 len)). LR: an lr face (sg = 1), else a bt face (sg = -1).
 // Returns twice the traction (tx, ty), twice the heat flux qn, and for the axisymmetric
-// hoop stress -2/3 div + 2 u_f / x_f (the caller scales it by mu_f / 2).
+// hoop stress -2/3 div + 2 u_f / x_f (the caller scales it by mu_f / 2), all float-float.
 template <bool LR, bool AXI>
 __device__ __forceinline__ void visc_face_ff(const ff* fu, const ff* fv, const ff* fT, int A, int B, const ff* fuc,
                                              const ff* fvc, const ff* fTc, int lo, int hi, const float2* pl, long NF,
-                                             long f, double rxd, float2 kprf, float2 c23f, double& tx, double& ty,
-                                             double& qn, double& hoop) {
+                                             long f, double rxd, float2 kprf, float2 c23f, ff& txf, ff& tyf, ff& qf,
+                                             ff& hoop) {
   const ff nx = *reinterpret_cast<const ff*>(pl + f), ny = *reinterpret_cast<const ff*>(pl + NF + f);
   const ff g1 = *reinterpret_cast<const ff*>(pl + 2 * NF + f), g2 = *reinterpret_cast<const ff*>(pl + 3 * NF + f);
   const ff il = *reinterpret_cast<const ff*>(pl + 4 * NF + f);
@@ -1136,13 +1136,51 @@ __device__ __forceinline__ void visc_face_ff(const ff* fu, const ff* fv, const f
   const ff c23 = *reinterpret_cast<const ff*>(&c23f);
   const ff al = ff_add(ff_mul(LR ? c23 : ff_neg(c23), div), Dn);
   const ff Ey = ff_mul(En, ny), Ex = ff_mul(En, nx);
-  const ff txf = ff_add(ff_mul(al, nx), LR ? ff_sub(du_dn, Ey) : ff_add(du_dn, Ey));
-  const ff tyf = ff_add(ff_mul(al, ny), LR ? ff_add(dv_dn, Ex) : ff_sub(dv_dn, Ex));
-  const ff qf = ff_mul(*reinterpret_cast<const ff*>(&kprf), dT_dn);
-  tx = ff_to_double(txf);
-  ty = ff_to_double(tyf);
-  qn = ff_to_double(qf);
-  if (AXI) hoop = ff_to_double(ff_add(ff_mul(ff_neg(c23), div), ff_mul(ff_scale2(uf, 2.f), rx)));
+  txf = ff_add(ff_mul(al, nx), LR ? ff_sub(du_dn, Ey) : ff_add(du_dn, Ey));
+  tyf = ff_add(ff_mul(al, ny), LR ? ff_add(dv_dn, Ex) : ff_sub(dv_dn, Ex));
+  qf = ff_mul(*reinterpret_cast<const ff*>(&kprf), dT_dn);
+  if (AXI) hoop = ff_add(ff_mul(ff_neg(c23), div), ff_mul(ff_scale2(uf, 2.f), rx));
+}
+
+// The flux of one face with the viscous terms in float-float (the RK step's form). A, B:
+// the halo cells left / right (lr face, LR) or bottom / top (bt face); lo, hi: the corner
+// sums at its ends; gA: the FP64 planes nx A/2, ny A/2; pl: the float-float planes (the
+// five of visc_face_ff, then A/2). Writes the four fluxes (stride fs) of the FP64 form in
+// flux_tile, i.e. (Vn (S) + p n + s t) A/2 with s = 1 (lr) or -1 (bt) and the energy's
+// s (w + qn) A/2, and for the axisymmetric the hoop term mu_f hoop / 2. The inviscid parts
+// are FP64 with the area folded into n; the traction, the heat flux and the work term
+// w = (S_u tx + S_v ty) / S_rho are scaled by s A/2 (and mu_f) in float-float and join the
+// FP64 sums through one addition each.
+template <bool LR, bool AXI, bool SUTH>
+__device__ __forceinline__ void face_flux_ff(const FluxArgs& a, const double* s_r, const double* s_ru,
+                                             const double* s_rv, const double* s_rE, const double* s_p, const ff* fu,
+                                             const ff* fv, const ff* fT, const ff* fuc, const ff* fvc, const ff* fTc,
+                                             int A, int B, int lo, int hi, const double* gA, const float2* pl, long NF,
+                                             long f, double rxd, double* out, int fs, double* hoop_out) {
+  const double Sr = s_r[A] + s_r[B], Su = s_ru[A] + s_ru[B], Sv = s_rv[A] + s_rv[B];
+  const double SE = s_rE[A] + s_rE[B], Sp = s_p[A] + s_p[B];
+  const double ir = frcp(Sr);
+  const double nxA = gA[f], nyA = gA[NF + f];
+  const double m2A = fma(Su, nxA, Sv * nyA);  // (S_u nx + S_v ny) A/2
+  const double VnA = m2A * ir;
+  ff txf, tyf, qf, hpf;
+  visc_face_ff<LR, AXI>(fu, fv, fT, A, B, fuc, fvc, fTc, lo, hi, pl, NF, f, rxd, a.kprf, a.c23f, txf, tyf, qf, hpf);
+  ff fac = *reinterpret_cast<const ff*>(pl + 5 * NF + f);
+  if (!LR) fac = ff_neg(fac);
+  ff muf{1.f, 0.f};
+  if (SUTH) {  // Sutherland at the face temperature
+    const double Ts = (ff_to_double(fT[A]) + ff_to_double(fT[B])) * 0.5 * a.Tinf_inv;
+    muf = ff_from_double(Ts * sqrt(Ts) * (1 + a.suthS) * frcp(Ts + a.suthS));
+    fac = ff_mul(fac, muf);
+  }
+  const ff txA = ff_mul(txf, fac), tyA = ff_mul(tyf, fac);
+  const ff wA = ff_mul(ff_add(ff_mul(ff_from_double(Su), txA), ff_mul(ff_from_double(Sv), tyA)), ff_from_double(ir));
+  const ff wqA = ff_add(wA, ff_mul(qf, fac));
+  out[0] = m2A;
+  out[fs] = fma(Su, VnA, fma(Sp, nxA, ff_to_double(txA)));
+  out[2 * fs] = fma(Sv, VnA, fma(Sp, nyA, ff_to_double(tyA)));
+  out[3 * fs] = fma(SE + Sp, VnA, ff_to_double(wqA));
+  if (AXI) *hoop_out = ff_to_double(ff_scale2(SUTH ? ff_mul(hpf, muf) : hpf, 0.5f));
 }
 
 // Returns false when a TMA wait gave up (the block then stops).
@@ -1258,12 +1296,13 @@ __device__ __forceinline__ bool flux_tile(const FluxArgs& a, const FluxMaps& tm,
         s_p[h] = a.p[g];
         T = a.T[g];
       }
-      const double ir = frcp(r);
-      if (FFV) {
-        fu[h] = ff_from_double(ru * ir);
-        fv[h] = ff_from_double(rv * ir);
+      if (FFV) {  // u, v as float-float quotients: no FP64 work per halo cell
+        const ff iv = ff_rcp(ff_from_double(r));
+        fu[h] = ff_mul(ff_from_double(ru), iv);
+        fv[h] = ff_mul(ff_from_double(rv), iv);
         fT[h] = ff_from_double(T);
       } else {
+        const double ir = frcp(r);
         s_u[h] = ru * ir; s_v[h] = rv * ir;
         s_T[h] = T;
       }
@@ -1293,7 +1332,14 @@ __device__ __forceinline__ bool flux_tile(const FluxArgs& a, const FluxMaps& tm,
   {
     const int fx = lane, fy = warp;
     const int gi = i0 + fx, gj = j0 + fy;  // face (gi, gj) 0-based: between ghosted (gi, gj+1), (gi+1, gj+1)
-    if (gi <= nchi && gj < neta) {
+    const int o = fx + fy * (TX + 1);
+    if (FFV && gi <= nchi && gj < neta) {
+      const long f = (long)gi + (long)gj * (nchi + 1);
+      const int L = hid(fx, fy + 1);
+      face_flux_ff<true, AXI, SUTH>(a, s_r, s_ru, s_rv, s_rE, s_p, fu, fv, fT, fuc, fvc, fTc, L, L + 1,
+                                    fx + fy * CX, fx + fy * CX + CX, a.m.lra, a.m.lrf, NLR, f,
+                                    AXI ? a.m.rx_lr[f] : 0.0, f_lr + o, G::NLRF, t_lr + o);
+    } else if (gi <= nchi && gj < neta) {
       const long f = (long)gi + (long)gj * (nchi + 1);
       const double nx = a.m.lrg[f], ny = a.m.lrg[NLR + f], Ah = a.m.lrg[2 * NLR + f];
       const int L = hid(fx, fy + 1), R = L + 1;
@@ -1304,15 +1350,7 @@ __device__ __forceinline__ bool flux_tile(const FluxArgs& a, const FluxMaps& tm,
       const double m2 = fma(Su, nx, Sv * ny);
       const double Vn = m2 * ir;
       double tx, ty, qn, hoop = 0, mu_f = 1;
-      if (FFV) {
-        visc_face_ff<true, AXI>(fu, fv, fT, L, R, fuc, fvc, fTc, clo, chi_, a.m.lrf, NLR, f,
-                                AXI ? a.m.rx_lr[f] : 0.0, a.kprf, a.c23f, tx, ty, qn, hoop);
-        if (SUTH) {  // Sutherland at the face temperature
-          const double Ts = (ff_to_double(fT[L]) + ff_to_double(fT[R])) * 0.5 * a.Tinf_inv;
-          mu_f = Ts * sqrt(Ts) * (1 + a.suthS) * frcp(Ts + a.suthS);
-          tx *= mu_f; ty *= mu_f; qn *= mu_f;
-        }
-      } else {
+      {
         const double g1 = a.m.lrg[3 * NLR + f], g2 = a.m.lrg[4 * NLR + f], il = a.m.lrg[5 * NLR + f];
         // viscous (VISCOUS_FLUX.jl:98-133)
         const double dUc = s_uc[chi_] - s_uc[clo], dVc = s_vc[chi_] - s_vc[clo], dTc = s_Tc[chi_] - s_Tc[clo];
@@ -1350,7 +1388,6 @@ __device__ __forceinline__ bool flux_tile(const FluxArgs& a, const FluxMaps& tm,
         if (AXI) hoop = fma(-2.0 / 3.0, div, 2 * uf * rx);
       }
       const double w = fma(Su, tx, Sv * ty) * ir;
-      const int o = fx + fy * (TX + 1);
       f_lr[o] = m2 * Ah;
       f_lr[G::NLRF + o] = fma(Su, Vn, fma(Sp, nx, tx)) * Ah;
       f_lr[2 * G::NLRF + o] = fma(Sv, Vn, fma(Sp, ny, ty)) * Ah;
@@ -1363,7 +1400,14 @@ __device__ __forceinline__ bool flux_tile(const FluxArgs& a, const FluxMaps& tm,
     const int fx = b & 31, fy = b >> 5;
     if (fx >= TX) continue;
     const int gi = i0 + fx, gj = j0 + fy;  // face (gi, gj): between ghosted (gi+1, gj), (gi+1, gj+1)
-    if (gi < nchi && gj <= neta) {
+    const int o = fx + fy * TX;
+    if (FFV && gi < nchi && gj <= neta) {
+      const long f = (long)gi + (long)gj * nchi;
+      const int B = hid(fx + 1, fy);
+      face_flux_ff<false, AXI, SUTH>(a, s_r, s_ru, s_rv, s_rE, s_p, fu, fv, fT, fuc, fvc, fTc, B, B + G::HP,
+                                     fx + fy * CX, fx + fy * CX + 1, a.m.bta, a.m.btf, NBT, f,
+                                     AXI ? a.m.rx_bt[f] : 0.0, f_bt + o, G::NBTF, t_bt + o);
+    } else if (gi < nchi && gj <= neta) {
       const long f = (long)gi + (long)gj * nchi;
       const double nx = a.m.btg[f], ny = a.m.btg[NBT + f], Ah = a.m.btg[2 * NBT + f];
       const int B = hid(fx + 1, fy), Tt = B + G::HP;
@@ -1374,15 +1418,7 @@ __device__ __forceinline__ bool flux_tile(const FluxArgs& a, const FluxMaps& tm,
       const double m2 = fma(Su, nx, Sv * ny);
       const double Vn = m2 * ir;
       double tx, ty, qn, hoop = 0, mu_f = 1;
-      if (FFV) {
-        visc_face_ff<false, AXI>(fu, fv, fT, B, Tt, fuc, fvc, fTc, clo, chi_, a.m.btf, NBT, f,
-                                 AXI ? a.m.rx_bt[f] : 0.0, a.kprf, a.c23f, tx, ty, qn, hoop);
-        if (SUTH) {
-          const double Ts = (ff_to_double(fT[B]) + ff_to_double(fT[Tt])) * 0.5 * a.Tinf_inv;
-          mu_f = Ts * sqrt(Ts) * (1 + a.suthS) * frcp(Ts + a.suthS);
-          tx *= mu_f; ty *= mu_f; qn *= mu_f;
-        }
-      } else {
+      {
         const double h1 = a.m.btg[3 * NBT + f], h2 = a.m.btg[4 * NBT + f], il = a.m.btg[5 * NBT + f];
         const double dUc = s_uc[chi_] - s_uc[clo], dVc = s_vc[chi_] - s_vc[clo], dTc = s_Tc[chi_] - s_Tc[clo];
         const double du_dn = fma(h1, s_u[Tt] - s_u[B], h2 * dUc);
@@ -1415,7 +1451,6 @@ __device__ __forceinline__ bool flux_tile(const FluxArgs& a, const FluxMaps& tm,
         if (AXI) hoop = fma(-2.0 / 3.0, div, 2 * uf * rx);
       }
       const double w = fma(Su, tx, Sv * ty) * ir;
-      const int o = fx + fy * TX;
       f_bt[o] = m2 * Ah;
       f_bt[G::NBTF + o] = fma(Su, Vn, fma(Sp, nx, -tx)) * Ah;
       f_bt[2 * G::NBTF + o] = fma(Sv, Vn, fma(Sp, ny, -ty)) * Ah;

@@ -13,7 +13,10 @@
 //
 // Conversions go through the bit patterns on the integer pipe, so that the FP64 pipe only
 // sees the one addition that joins a result back into a double (a cvt between f32 and f64
-// issues on the FP64 pipe at the DFMA rate on this GPU).
+// issues on the FP64 pipe at the DFMA rate on this GPU). The halo velocities u = rho_u / rho
+// are float-float quotients too (ff_rcp), and the face area and the viscous work term are
+// applied in float-float before the join, so that the FP64 pipe sees only the inviscid
+// fluxes and the cell sums.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -53,6 +56,20 @@ __device__ __forceinline__ ff ff_mul(ff a, ff b) {
 
 // a * 2^k for a power of two: exact, no renormalisation
 __device__ __forceinline__ ff ff_scale2(ff a, float p2) { return ff{a.h * p2, a.l * p2}; }
+
+// 1 / b for b > 0 in the float normal range: Newton-Raphson from the hardware's float
+// reciprocal y0 (rcp.approx, within one ulp), with the correction carried past float
+// precision. e = 1 - b y0 is formed exactly to ~2^-48 (1 - p is exact since p = b.h y0 lies
+// within 2^-22 of 1, and p + pe = b.h y0 exactly by the FMA), and 1 / b = y0 (1 + e + e^2
+// + ...), whose cubic term is below 2^-69. Relative error ~2^-46.
+__device__ __forceinline__ ff ff_rcp(ff b) {
+  float y0;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y0) : "f"(b.h));
+  const float p = b.h * y0;
+  const float pe = __fmaf_rn(b.h, y0, -p);
+  const float e = __fmaf_rn(-b.l, y0, (1.0f - p) - pe);
+  return ff_fast_two_sum(y0, y0 * __fmaf_rn(e, e, e));
+}
 
 // double -> float-float: h is x with its 29 low mantissa bits cleared (an exact float),
 // l the remaining 29 bits truncated to 24. |x| must lie in the float normal range; zero
