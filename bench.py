@@ -78,7 +78,8 @@ class ClockSampler:
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,clocks.mem,"
+              "clocks.max.mem")
 
     def __init__(self, gpu_index: int):
         self.gpu = gpu_index
@@ -109,7 +110,7 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
-        sm, mx, reasons = [], None, set()
+        sm, mx, reasons, mem, mem_max = [], None, set(), [], None
         for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
@@ -119,14 +120,22 @@ class ClockSampler:
                 mx = float(parts[2])
             except ValueError:
                 continue
+            try:  # the memory clock, which latency-bound kernels follow too
+                mem.append(float(parts[9]))
+                mem_max = float(parts[10])
+            except (ValueError, IndexError):
+                pass
             names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
             for n, v in zip(names, parts[5:9]):
                 if v.lower() == "active":
                     reasons.add(n)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+        if mem:
+            out["mem_mhz"] = statistics.median(mem)
+            out["mem_max_mhz"] = mem_max
+        return out
 
 
 def dist_env():
@@ -246,6 +255,8 @@ def matvec_numbers(sol, cs, fp64_peak_tflops: float, hbm_gbs: float, cpu: bool, 
            "jacobian_assembly_s": jac_s, "gpu_launches": {"batched": reps, "plain": reps * k}}
     if cpu:
         from oracle import oracle as O
+        threads = os.cpu_count() or 1
+        O.lib().orc_set_threads(threads)
         coef = np.empty(CELLS * 144)
         sol.ctx.check(L.hymor_jacobian_get(h, dp(coef)))
         o = O.Oracle(cs)
@@ -255,8 +266,8 @@ def matvec_numbers(sol, cs, fp64_peak_tflops: float, hbm_gbs: float, cpu: bool, 
             o.matvec(coef, X[nv])
             nv += 1
         el = (time.perf_counter() - t0) / nv
-        out["cpu_baseline"] = {"ms_per_vector": el * 1e3, "cores": 1, "kind": "port",
-                               "sample": f"{nv} vectors through the oracle's stencil matvec"}
+        out["cpu_baseline"] = {"ms_per_vector": el * 1e3, "cores": threads, "kind": "port",
+                               "sample": f"{nv} vectors through the oracle's stencil matvec (OpenMP)"}
     del dX, dY
     if base is not None:
         base.close()
