@@ -253,8 +253,12 @@ int enqueue_step(hymor_ctx* ctx, bool with_events) {
     // lines); the full field is recomputed when next needed.
     CU(cudaEventRecord(ctx->cfl_fork, st));
     CU(cudaStreamWaitEvent(ctx->cfl, ctx->cfl_fork, 0));
-    launch_sound_cmax(d, shock, ctx->cfl, true);
-    launch_cfl(d, ctx->cfl);
+    if (shock && d.cfl_screen) {
+      launch_cfl_screened(d, ctx->cfl);
+    } else {
+      launch_sound_cmax(d, shock, ctx->cfl, true);
+      launch_cfl(d, ctx->cfl);
+    }
     CU(cudaEventRecord(ctx->cfl_ev, ctx->cfl));
     TRY(ev(16));
     launch_update_thermo(d, 0, 0, 0, st);
@@ -702,7 +706,7 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
       (r = dalloc(ctx, &d.speed_x, d.nchi)) || (r = dalloc(ctx, &d.speed_y, d.nchi)) ||
       (r = dalloc(ctx, &d.rel, d.nchi)) || (r = dalloc(ctx, &d.spl, 17 * (long)d.nchi + 16)) ||
       (r = dalloc(ctx, &d.tiles, 2 + 2 * (long)flux_tiles_max(d))) ||
-      (r = dalloc(ctx, &d.ticket, 2L)) ||
+      (r = dalloc(ctx, &d.ticket, 6L)) ||
       (r = dalloc(ctx, &d.cflw, d.NLR + d.NBT)))
     return bail(r);
   if (cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess || d.sms < 1)
@@ -718,6 +722,7 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
   d.bwork = nullptr;
   d.sf_zero = 1;  // the flux arrays are allocated zeroed
   d.step_ffv = 1;
+  d.cfl_screen = 1;
   d.flux_rows = 8;
   d.flux_spare = 1;
   d.tma = make_flux_maps(d);
@@ -1089,6 +1094,16 @@ int hymor_set_step_viscous(hymor_ctx* ctx, int mode) {
   if (ctx->d.step_ffv != mode) {
     TRY(set_device(ctx));
     ctx->d.step_ffv = mode;
+    drop_step_graph(ctx);
+  }
+  return 0;
+}
+
+int hymor_set_cfl_screen(hymor_ctx* ctx, int on) {
+  if (!ctx || on < 0 || on > 1) return HYMOR_ERR_INVALID;
+  if (ctx->d.cfl_screen != on) {
+    TRY(set_device(ctx));
+    ctx->d.cfl_screen = on;
     drop_step_graph(ctx);
   }
   return 0;

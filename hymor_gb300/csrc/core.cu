@@ -1624,29 +1624,35 @@ struct SoundArgs {
   int nchi, neta, mode, isothermal_eta0, nrcbc;
 };
 
+// gamma p / rho of ghosted cell k = (i, j) of S; the isothermal wall's ghost row takes the
+// pressure extrapolated from the first two rows (UPDATE_THERMODYNAMIC_PROPERTIES.jl:28-31)
+__device__ __forceinline__ double cell_c2(const SoundArgs& A, long k, int i, int j) {
+  const double gm1 = A.gamma - 1;
+  auto pres_r = [&](long q, double ir) {
+    const double u = A.S.ru[q], v = A.S.rv[q], e = A.S.rE[q];
+    return fma(-0.5, fma(u, u, v * v) * ir, e) * gm1;
+  };
+  auto pres = [&](long q) { return pres_r(q, frcp(A.S.rho[q])); };
+  double p;
+  const double ir = frcp(A.S.rho[k]);
+  if (j == 0 && A.isothermal_eta0)
+    p = 2 * pres(gidx(i, 1, A.nchi)) - pres(gidx(i, 2, A.nchi));
+  else
+    p = pres_r(k, ir);
+  return A.gamma * p * ir;
+}
+
 __global__ void __launch_bounds__(256) k_sound_cmax(SoundArgs A) {
   const int NI = A.nchi + 2, NJ = A.neta + 2;
   const long G = (long)NI * NJ;
   double mx = 0;
-  const double gm1 = A.gamma - 1;
-  auto pres_r = [&](long k, double ir) {
-    const double u = A.S.ru[k], v = A.S.rv[k], e = A.S.rE[k];
-    return fma(-0.5, fma(u, u, v * v) * ir, e) * gm1;
-  };
-  auto pres = [&](long k) { return pres_r(k, frcp(A.S.rho[k])); };
   for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < G; k += (long)gridDim.x * blockDim.x) {
     if (A.mode == 0) {
       mx = fmax(mx, fabs(A.aS[k]));
       continue;
     }
     const int i = (int)(k % NI), j = (int)(k / NI);
-    double p;
-    const double ir = frcp(A.S.rho[k]);
-    if (j == 0 && A.isothermal_eta0)
-      p = 2 * pres(gidx(i, 1, A.nchi)) - pres(gidx(i, 2, A.nchi));
-    else
-      p = pres_r(k, ir);
-    const double c2 = A.gamma * p * ir;
+    const double c2 = cell_c2(A, k, i, j);
     if (A.mode == 1) {
       const double a = sqrt(c2);
       A.aS[k] = a;
@@ -1701,6 +1707,30 @@ struct CflArgs {
   int sf_zero;      // the stored flux is zero everywhere: its dt term is +inf, skip it
 };
 
+// Convective rate (|V_n| + c_max) A of the face between ghosted cells L and R of S.
+__device__ __forceinline__ double face_rate(const Cons& S, long L, long R, double nx, double ny, double Af,
+                                            double cmax) {
+  const double rs = S.rho[L] + S.rho[R];
+  const double Vn = fabs(fma(S.ru[L] + S.ru[R], nx, (S.rv[L] + S.rv[R]) * ny)) * frcp(rs);
+  return (Vn + cmax) * Af;
+}
+
+// CFL rate of interior cell c (ghosted g, ir = 1 / rho) from its west, east, south and
+// north face rates: the larger of opposite faces, summed, over the volume, plus the viscous
+// rate 2 max(4/3, gamma/Pr) (A_xi^2 + A_eta^2) / (rho Re_flow vol^2).
+__device__ __forceinline__ double cell_rate(const CflArgs& A, long c, long g, double lw, double le, double ls,
+                                            double ln, double ir) {
+  const double lam_c = fmax(lw, le) + fmax(ls, ln);
+  // viscous rate over the volume: gvis carries max(4/3, gamma/Pr) / Re and 1/vol^2
+  double lam_v = A.m.gvis[c] * ir;
+  if (A.suth) {  // Re_flow = Re / mu* (UPDATE_CHEMISTRY_EQUILIBRIUM.jl:99-101); mu* = 1 for CPG
+    const double e = fma(-0.5, fma(A.S.ru[g], A.S.ru[g], A.S.rv[g] * A.S.rv[g]) * ir, A.S.rE[g]) * ir;
+    const double Ts = e * A.Tinf_inv;
+    lam_v *= Ts * sqrt(Ts) * (1 + A.suthS) * frcp(Ts + A.suthS);
+  }
+  return fma(lam_c, A.m.rvol[c], lam_v);
+}
+
 __global__ void __launch_bounds__(256) k_cfl_faces(CflArgs A) {
   const int nchi = A.nchi, neta = A.neta;
   const long NLR = (long)(nchi + 1) * neta, NBT = (long)nchi * (neta + 1);
@@ -1721,9 +1751,7 @@ __global__ void __launch_bounds__(256) k_cfl_faces(CflArgs A) {
       R = L + (nchi + 2);
       nx = A.m.btg[g]; ny = A.m.btg[NBT + g]; Af = 2 * A.m.btg[2 * NBT + g];
     }
-    const double rs = A.S.rho[L] + A.S.rho[R];
-    const double Vn = fabs(fma(A.S.ru[L] + A.S.ru[R], nx, (A.S.rv[L] + A.S.rv[R]) * ny)) * frcp(rs);
-    const double lam = (Vn + cmax) * Af;
+    const double lam = face_rate(A.S, L, R, nx, ny, Af, cmax);
     if (f < NLR) A.lam_lr[f] = lam; else A.lam_bt[f - NLR] = lam;
   }
 }
@@ -1737,18 +1765,9 @@ __global__ void __launch_bounds__(256) k_cfl(CflArgs A) {
     const bool flow = !A.shock || (j + 1 < A.cell_idx[i]);
     if (flow) {
       const long fw = i + (long)j * (nchi + 1), fs = i + (long)j * nchi;
-      const double lam_c = fmax(A.lam_lr[fw], A.lam_lr[fw + 1]) + fmax(A.lam_bt[fs], A.lam_bt[fs + nchi]);
       const long g = gidx(i + 1, j + 1, nchi);
-      const double r = A.S.rho[g];
-      const double ir = frcp(r);
-      // viscous rate over the volume: gvis carries max(4/3, gamma/Pr) / Re and 1/vol^2
-      double lam_v = A.m.gvis[c] * ir;
-      if (A.suth) {  // Re_flow = Re / mu* (UPDATE_CHEMISTRY_EQUILIBRIUM.jl:99-101); mu* = 1 for CPG
-        const double e = fma(-0.5, fma(A.S.ru[g], A.S.ru[g], A.S.rv[g] * A.S.rv[g]) * ir, A.S.rE[g]) * ir;
-        const double Ts = e * A.Tinf_inv;
-        lam_v *= Ts * sqrt(Ts) * (1 + A.suthS) * frcp(Ts + A.suthS);
-      }
-      mlam = fmax(mlam, fma(lam_c, A.m.rvol[c], lam_v));
+      const double ir = frcp(A.S.rho[g]);
+      mlam = fmax(mlam, cell_rate(A, c, g, A.lam_lr[fw], A.lam_lr[fw + 1], A.lam_bt[fs], A.lam_bt[fs + nchi], ir));
       if (!A.sf_zero) {
         const double t_u = (fabs(A.SF2[c]) + fabs(A.SF1[c])) * ir;
         const double t_r = fabs(A.SF0[c] * ir);
@@ -1774,10 +1793,229 @@ __global__ void __launch_bounds__(256) k_cfl(CflArgs A) {
   }
 }
 
+__device__ __forceinline__ double cfl_dt(double max_lam, double max_flux, double CFL, double max_dt) {
+  const double dt1 = CFL / max_lam;
+  const double dt2 = CFL / max_flux;  // +inf when the stored flux is zero
+  return fmin(dt1, fmin(dt2, max_dt));
+}
+
 __global__ void k_cfl_final(double* scal, double CFL, double max_dt) {
-  const double dt1 = CFL / scal[kMaxLam];
-  const double dt2 = CFL / scal[kMaxFlux];  // +inf when the stored flux is zero
-  scal[kDt] = fmin(dt1, fmin(dt2, max_dt));
+  scal[kDt] = cfl_dt(scal[kMaxLam], scal[kMaxFlux], CFL, max_dt);
+}
+
+// ---------------------------------------------------------------------------
+// The RK step's CFL reduction, screened: the same maxima as k_sound_cmax (mode 2) and
+// k_cfl_faces + k_cfl, bit for bit, with ~1 % of their FP64 work. A first pass evaluates
+// every cell's value in FP32 from its inputs truncated to float through their bit patterns
+// (integer pipe: a cvt between f64 and f32 issues on the FP64 pipe) and reduces the FP32
+// maximum M; a second pass evaluates in FP64, with the expressions of the full kernels
+// (cell_c2, face_rate, cell_rate), only the cells whose FP32 value is at least
+// M (1 - 2^-8), and reduces their maximum. The FP32 value of a cell is within a relative
+// ~1e-6 x (its cancellation factor) of its FP64 value, so the cell that attains the FP64
+// maximum is always among those evaluated, for cancellation factors below ~10^3 (the
+// pressure's rho E / (rho e), 1 + gamma (gamma - 1) M^2 / 2 at local Mach number M, is 113
+// at M = 20). Cells whose inputs are not finite floats, or whose FP32 value is NaN, are
+// always evaluated in FP64. The last block of each second pass takes the root (c_max) or
+// forms dt, and resets the FP32 maximum and its block counter for the next step.
+constexpr float kScreenKeep = 1.0f - 1.0f / 256;
+
+// x as a float with its mantissa truncated to 23 bits, from the bit pattern; zero below the
+// float normal range; sets bad beyond it (and for infinities and NaN).
+__device__ __forceinline__ float trunc_float(double x, bool& bad) {
+  const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
+  const unsigned e = (hw >> 20) & 0x7ffu;
+  bad |= e >= 1151u;
+  const unsigned fb = (hw & 0x80000000u) | ((e - 896u) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29);
+  return e > 896u ? __uint_as_float(fb) : 0.0f;
+}
+
+// block maximum of non-negative floats into *slot (bit patterns order as unsigned integers)
+__device__ __forceinline__ void block_max_f32(float v, unsigned* slot) {
+  __shared__ float red[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    float w = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) w = fmaxf(w, __shfl_xor_sync(0xffffffffu, w, o));
+    if (threadIdx.x == 0) atomicMax(slot, __float_as_uint(fmaxf(w, 0.0f)));
+  }
+}
+
+// FP64 block maximum into scal[slot]; true in thread 0 of the block that arrives last at
+// *ticket (every block's maximum is then in)
+__device__ __forceinline__ bool block_max_f64_last(double v, double* slot, unsigned* ticket) {
+  __shared__ double red[32];
+  __shared__ bool last;
+  v = warp_max(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double w = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    w = warp_max(w);
+    if (threadIdx.x == 0) {
+      atomic_max_nonneg(slot, w);
+      __threadfence();
+      last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+  }
+  __syncthreads();
+  return last && threadIdx.x == 0;
+}
+
+// scr: [0] FP32 max of gamma p / rho, [1] FP32 max of the cell rates, [2], [3] block counters
+__global__ void __launch_bounds__(256) k_cmax_screen(SoundArgs A, float* c2f, unsigned* scr) {
+  const int NI = A.nchi + 2, NJ = A.neta + 2;
+  const long G = (long)NI * NJ;
+  const float gm1 = (float)(A.gamma - 1), gam = (float)A.gamma;
+  float mx = 0.0f;
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < G; k += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(k % NI), j = (int)(k / NI);
+    bool bad = false;
+    auto pres = [&](long q, float& r) {
+      r = trunc_float(A.S.rho[q], bad);
+      const float u = trunc_float(A.S.ru[q], bad), v = trunc_float(A.S.rv[q], bad);
+      const float e = trunc_float(A.S.rE[q], bad);
+      return __fmaf_rn(-0.5f, __fdividef(__fmaf_rn(u, u, v * v), r), e) * gm1;
+    };
+    float r, p;
+    if (j == 0 && A.isothermal_eta0) {
+      float r1, r2;
+      p = 2.0f * pres(gidx(i, 1, A.nchi), r1) - pres(gidx(i, 2, A.nchi), r2);
+      r = trunc_float(A.S.rho[k], bad);
+    } else {
+      p = pres(k, r);
+    }
+    float c2 = __fdividef(gam * p, r);
+    if (bad) c2 = __int_as_float(0x7f800000);  // evaluated in FP64, kept out of the FP32 maximum
+    else mx = fmaxf(mx, c2);
+    c2f[k] = c2;
+  }
+  block_max_f32(mx, &scr[0]);
+}
+
+__global__ void __launch_bounds__(256) k_cmax_exact(SoundArgs A, const float* c2f, unsigned* scr) {
+  const int NI = A.nchi + 2, NJ = A.neta + 2;
+  const long G = (long)NI * NJ;
+  const float M = __uint_as_float(scr[0]);
+  const float keep = M > 0.0f ? M * kScreenKeep : -__int_as_float(0x7f800000);
+  double mx = 0;
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < G; k += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(k % NI), j = (int)(k / NI);
+    const bool nb = ((A.nrcbc & 1) && i == 1) || ((A.nrcbc & 2) && i == NI - 2) ||
+                    ((A.nrcbc & 4) && j == 1) || ((A.nrcbc & 8) && j == NJ - 2);
+    if (!(c2f[k] < keep) || nb) {
+      const double c2 = cell_c2(A, k, i, j);
+      if (nb) A.aS[k] = sqrt(c2);
+      mx = fmax(mx, c2);
+    }
+  }
+  if (block_max_f64_last(mx, &A.scal[kCmax], &scr[2])) {
+    unsigned long long* bits = reinterpret_cast<unsigned long long*>(&A.scal[kCmax]);
+    A.scal[kCmax] = sqrt(__longlong_as_double((long long)atomicAdd(bits, 0ull)));
+    scr[0] = 0;
+    scr[2] = 0;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_cfl_screen(CflArgs A, float* rf, unsigned* scr) {
+  const int nchi = A.nchi, neta = A.neta;
+  const long N = (long)nchi * neta, NLR = (long)(nchi + 1) * neta, NBT = (long)nchi * (neta + 1);
+  bool bad_c = false;
+  const float cmax = trunc_float(A.scal[kCmax], bad_c);
+  float mx = 0.0f;
+  for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N; c += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(c % nchi), j = (int)(c / nchi);
+    if (A.shock && !(j + 1 < A.cell_idx[i])) continue;
+    bool bad = bad_c;
+    const long g = gidx(i + 1, j + 1, nchi);
+    const long nb[5] = {g, g - 1, g + 1, g - (nchi + 2), g + (nchi + 2)};  // cell, W, E, S, N
+    float r[5], u[5], v[5];
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+      r[q] = trunc_float(A.S.rho[nb[q]], bad);
+      u[q] = trunc_float(A.S.ru[nb[q]], bad);
+      v[q] = trunc_float(A.S.rv[nb[q]], bad);
+    }
+    // the planes' high floats: nx, ny (planes 0, 1) and A/2 (plane 5)
+    auto rate = [&](const float2* pl, long NF, long f, int a, int b) {
+      const float nx = pl[f].x, ny = pl[NF + f].x, Ah = pl[5 * NF + f].x;
+      const float Vn = fabsf(__fmaf_rn(u[a] + u[b], nx, (v[a] + v[b]) * ny)) * __fdividef(1.0f, r[a] + r[b]);
+      return (Vn + cmax) * (2.0f * Ah);
+    };
+    const long fw = i + (long)j * (nchi + 1), fs = i + (long)j * nchi;
+    const float lw = rate(A.m.lrf, NLR, fw, 1, 0), le = rate(A.m.lrf, NLR, fw + 1, 0, 2);
+    const float ls = rate(A.m.btf, NBT, fs, 3, 0), ln = rate(A.m.btf, NBT, fs + nchi, 0, 4);
+    const float ir = __fdividef(1.0f, r[0]);
+    float lam_v = trunc_float(A.m.gvis[c], bad) * ir;
+    if (A.suth) {
+      const float e = __fmaf_rn(-0.5f, __fmaf_rn(u[0], u[0], v[0] * v[0]) * ir, trunc_float(A.S.rE[g], bad)) * ir;
+      const float Ts = e * (float)A.Tinf_inv, S = (float)A.suthS;
+      lam_v *= Ts * sqrtf(Ts) * (1.0f + S) * __fdividef(1.0f, Ts + S);
+    }
+    float rate_c = __fmaf_rn(fmaxf(lw, le) + fmaxf(ls, ln), trunc_float(A.m.rvol[c], bad), lam_v);
+    if (bad) rate_c = __int_as_float(0x7f800000);
+    else mx = fmaxf(mx, rate_c);
+    rf[c] = rate_c;
+  }
+  block_max_f32(mx, &scr[1]);
+}
+
+__global__ void __launch_bounds__(256) k_cfl_exact(CflArgs A, const float* rf, unsigned* scr, double CFL,
+                                                   double max_dt) {
+  const int nchi = A.nchi, neta = A.neta;
+  const long N = (long)nchi * neta, NLR = (long)(nchi + 1) * neta, NBT = (long)nchi * (neta + 1);
+  const float M = __uint_as_float(scr[1]);
+  const float keep = M > 0.0f ? M * kScreenKeep : -__int_as_float(0x7f800000);
+  const double cmax = A.scal[kCmax];
+  double mlam = 0, mflux = 0;
+  for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N; c += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(c % nchi), j = (int)(c / nchi);
+    if (A.shock && !(j + 1 < A.cell_idx[i])) continue;
+    const long g = gidx(i + 1, j + 1, nchi);
+    const bool eval = !(rf[c] < keep);
+    if (!eval && A.sf_zero) continue;
+    const double ir = frcp(A.S.rho[g]);
+    if (eval) {
+      // the face rates of k_cfl_faces: lr face f between ghosted (i, j+1) and (i+1, j+1),
+      // bt face f between (i+1, j) and (i+1, j+1)
+      const long fw = i + (long)j * (nchi + 1), fs = i + (long)j * nchi;
+      auto lr = [&](long f, long L) {
+        return face_rate(A.S, L, L + 1, A.m.lrg[f], A.m.lrg[NLR + f], 2 * A.m.lrg[2 * NLR + f], cmax);
+      };
+      auto bt = [&](long f, long L) {
+        return face_rate(A.S, L, L + (nchi + 2), A.m.btg[f], A.m.btg[NBT + f], 2 * A.m.btg[2 * NBT + f], cmax);
+      };
+      mlam = fmax(mlam, cell_rate(A, c, g, lr(fw, g - 1), lr(fw + 1, g), bt(fs, g - (nchi + 2)),
+                                  bt(fs + nchi, g), ir));
+    }
+    if (!A.sf_zero) {
+      const double t_u = (fabs(A.SF2[c]) + fabs(A.SF1[c])) * ir;
+      const double t_r = fabs(A.SF0[c] * ir);
+      const double t_E = fabs(A.SF3[c] * frcp(A.S.rE[g]));
+      mflux = fmax(mflux, fmax(t_u, fmax(t_r, t_E)));
+    }
+  }
+  // the stored-flux maximum first (no counter), then the rates with the block counter
+  mflux = warp_max(mflux);
+  __shared__ double rfx[32];
+  if ((threadIdx.x & 31) == 0) rfx[threadIdx.x >> 5] = mflux;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double w = threadIdx.x < (blockDim.x >> 5) ? rfx[threadIdx.x] : 0.0;
+    w = warp_max(w);
+    if (threadIdx.x == 0) atomic_max_nonneg(&A.scal[kMaxFlux], w);
+  }
+  if (block_max_f64_last(mlam, &A.scal[kMaxLam], &scr[3])) {
+    unsigned long long* lam = reinterpret_cast<unsigned long long*>(&A.scal[kMaxLam]);
+    unsigned long long* flx = reinterpret_cast<unsigned long long*>(&A.scal[kMaxFlux]);
+    A.scal[kDt] = cfl_dt(__longlong_as_double((long long)atomicAdd(lam, 0ull)),
+                         __longlong_as_double((long long)atomicAdd(flx, 0ull)), CFL, max_dt);
+    scr[1] = 0;
+    scr[3] = 0;
+  }
 }
 
 // Step end on S: UPDATE_FIELD_UPSTREAM (after APPLY_BOUNDARY_CONDITIONS), MIN_RHO, t += dt.
@@ -2238,6 +2476,47 @@ void launch_cfl(const DevCtx& d, cudaStream_t st) {
   k_cfl_faces<<<grid_for(d.NLR + d.NBT, 256), 256, 0, st>>>(A);
   k_cfl<<<grid_for(d.N, 256), 256, 0, st>>>(A);
   k_cfl_final<<<1, 1, 0, st>>>(d.scal, d.cfg.CFL, d.cfg.max_dt);
+}
+
+// The step's CFL reduction with the FP32 screen (with shock fitting: the sound-speed
+// maximum is recomputed from S, as launch_sound_cmax(d, true, st, true) followed by
+// launch_cfl(d, st)); the FP32 values go to the face-rate buffer.
+void launch_cfl_screened(const DevCtx& d, cudaStream_t st) {
+  SoundArgs S;
+  S.S = d.S;
+  S.aS = d.aS;
+  S.scal = d.scal;
+  S.ticket = d.ticket;
+  S.gamma = d.cfg.gamma;
+  S.nchi = d.nchi;
+  S.neta = d.neta;
+  S.mode = 2;
+  S.nrcbc = (d.cfg.bc_chi0 == HYMOR_BC_OUTFLOW_NRCBC) | ((d.cfg.bc_chi1 == HYMOR_BC_OUTFLOW_NRCBC) << 1) |
+            ((d.cfg.bc_eta0 == HYMOR_BC_OUTFLOW_NRCBC) << 2) | ((d.cfg.bc_eta1 == HYMOR_BC_OUTFLOW_NRCBC) << 3);
+  S.isothermal_eta0 = d.cfg.bc_eta0 == HYMOR_BC_NO_SLIP_ISOTHERMAL;
+  CflArgs A;
+  A.S = d.S;
+  A.SF0 = d.SF[0]; A.SF1 = d.SF[1]; A.SF2 = d.SF[2]; A.SF3 = d.SF[3];
+  A.m = d.m;
+  A.cell_idx = d.cell_idx;
+  A.scal = d.scal;
+  A.gamma = d.cfg.gamma;
+  A.suthS = d.cfg.sutherland_S;
+  A.Tinf_inv = d.cfg.energy_factor / d.cfg.cv;
+  A.suth = d.cfg.viscosity_model == 1;
+  A.nchi = d.nchi;
+  A.neta = d.neta;
+  A.shock = d.cfg.shock_enabled;
+  A.lam_lr = d.cflw;
+  A.lam_bt = d.cflw + d.NLR;
+  A.sf_zero = d.sf_zero;
+  float* c2f = reinterpret_cast<float*>(d.cflw);  // G floats
+  float* rf = c2f + d.G;                          // N floats (G + N floats fit in NLR + NBT doubles)
+  unsigned* scr = d.ticket + 2;
+  k_cmax_screen<<<grid_for(d.G, 256), 256, 0, st>>>(S, c2f, scr);
+  k_cmax_exact<<<grid_for(d.G, 256), 256, 0, st>>>(S, c2f, scr);
+  k_cfl_screen<<<grid_for(d.N, 256), 256, 0, st>>>(A, rf, scr);
+  k_cfl_exact<<<grid_for(d.N, 256), 256, 0, st>>>(A, rf, scr, d.cfg.CFL, d.cfg.max_dt);
 }
 
 void launch_fill_minrho(const DevCtx& d, bool advance_time, cudaStream_t st) {

@@ -47,7 +47,8 @@ struct DevCtx {
   double* scal;    // Scalar block
   unsigned* err;   // ErrWord block
   int* tiles;      // flux tile lists of the RK step (launch_classify_tiles)
-  unsigned* ticket;  // block counters: [0] k_sound_cmax (mode 2), [1] k_fill_minrho
+  unsigned* ticket;  // [0] k_sound_cmax (mode 2) and [1] k_fill_minrho block counters; [2..5] the
+                     // screened CFL reduction's FP32 maxima and block counters
   // Jacobian
   double* coef;    // N * 144 stencil blocks (or null)
   double* jwork;   // linearisation workspace
@@ -65,6 +66,8 @@ struct DevCtx {
   // the RK step's flux forms the viscous terms in float-float arithmetic (1, the default)
   // or in FP64 (0); the residual entry point and the Jacobian always use FP64
   int step_ffv;
+  // the step's CFL maxima through the FP32 screen (1, the default) or in FP64 over every cell
+  int cfl_screen;
   // flux tiling of the RK step (hymor_autotune): tile rows (8 or 16) and the block slots per
   // SM the persistent interior-tile grid leaves to the side streams
   int flux_rows, flux_spare;
@@ -119,6 +122,7 @@ void launch_flow_cells(const DevCtx& d, cudaStream_t st);
 void launch_sound_cmax(const DevCtx& d, bool recompute, cudaStream_t st, bool max_only = false);
 // CFL maxima and dt (scal[kDt]).
 void launch_cfl(const DevCtx& d, cudaStream_t st);
+void launch_cfl_screened(const DevCtx& d, cudaStream_t st);
 // Step end: upstream fill + MIN_RHO on S, t += dt.
 void launch_fill_minrho(const DevCtx& d, bool advance_time, cudaStream_t st);
 // Classical RK4: snapshot S -> Yc (cells and shock points); restore Y <- Yc + c*dt*F.

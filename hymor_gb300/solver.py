@@ -110,6 +110,11 @@ class Solution:
         0 FP64 (hymor_set_step_viscous). PDE and the Jacobian always use FP64."""
         self.ctx.check(self.ctx.L.hymor_set_step_viscous(self.ctx.h, int(mode)))
 
+    def set_cfl_screen(self, on: int):
+        """Reduction of the RK step's CFL maxima: 1 through the exact FP32 screen (default),
+        0 FP64 over every cell (hymor_set_cfl_screen); dt is the same bit for bit."""
+        self.ctx.check(self.ctx.L.hymor_set_cfl_screen(self.ctx.h, int(on)))
+
     def step_kernels(self) -> int:
         """Kernel launches one ADVECT_FLOW step makes (the kernel nodes of its graph)."""
         n = ctypes.c_int32()

@@ -128,6 +128,13 @@ int hymor_set_flux(hymor_ctx* ctx, const double* flux);
  * graph. */
 int hymor_set_step_viscous(hymor_ctx* ctx, int mode);
 
+/* Reduction of the RK step's CFL maxima (CFL_TIMESTEP.jl:80-130; no counterpart in the
+ * reference, which evaluates them in FP64). on = 1 (the default): every cell is screened in
+ * FP32 and only the cells within 2^-8 of the FP32 maximum are evaluated in FP64, which gives
+ * the FP64 maxima, and dt, bit for bit with ~1 % of the FP64 work; on = 0: every cell in
+ * FP64. Only the step with shock fitting screens. The next hymor_step re-captures its graph. */
+int hymor_set_cfl_screen(hymor_ctx* ctx, int on);
+
 /* Tile-shape autotuner of the RK step's flux (no counterpart in the reference): times `steps`
  * steps (CUDA events, after a warm-up step) for each flux configuration — the tile halo staged
  * by TMA (cp.async.bulk.tensor) or loaded thread by thread, tiles of 31 x 8 or 31 x 16 cells,

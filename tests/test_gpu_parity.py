@@ -178,6 +178,28 @@ def test_stored_flux_enters_cfl_and_steps(require_gpu):
     compare_state(sol, orc, 1e-11)
 
 
+@pytest.mark.parametrize("name", list(CASES))
+def test_step_cfl_screen_is_exact(require_gpu, name):
+    """The RK step reduces its CFL maxima through an FP32 screen and an FP64 pass over the
+    cells near the FP32 maximum (the default); its dt, and so the marched state, must equal
+    bit for bit those of the step that reduces every cell in FP64, step after step, and with
+    the stored flux set."""
+    cs = C.initial_state(CASES[name](), seed=3, noise=1e-6)
+    a, b = S.Solution(cs), S.Solution(cs)
+    b.set_cfl_screen(0)
+    for k in range(5):
+        if k == 2:
+            for s in (a, b):
+                S.PDE(s)  # the stored flux enters dt2 from here on
+        S.ADVECT_FLOW(a, 1)
+        S.ADVECT_FLOW(b, 1)
+        sa, sb = a.get_state(), b.get_state()
+        assert sa["dt"] == sb["dt"], (k, sa["dt"], sb["dt"])
+        assert np.array_equal(sa["q"], sb["q"]) and np.array_equal(sa["pts_x"], sb["pts_x"]), k
+    a.close()
+    b.close()
+
+
 @pytest.mark.parametrize("name", ["cylinder_100x80", "cylinder_sutherland", "blunt_cone_axisym",
                                   "cylinder_interp1_eulerian"])
 def test_step_viscous_float_float(require_gpu, name):
