@@ -347,7 +347,10 @@ int build_graph(hymor_ctx* ctx) {
   if (r) return r;
   if (e != cudaSuccess) return fail(ctx, HYMOR_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
   ctx->graph = g;
-  CU(cudaGraphInstantiate(&ctx->gexec, g, 0));
+  // per-node priorities: the kernels keep the priority of the stream they were captured on
+  // (the shock chain and the boundary-class flux above the interior flux, the CFL reduction
+  // below it); without the flag every node runs at the launch stream's priority
+  CU(cudaGraphInstantiate(&ctx->gexec, g, cudaGraphInstantiateFlagUseNodePriority));
   // map the event-record nodes to their flux-launch slots
   size_t nn = 0;
   CU(cudaGraphGetNodes(g, nullptr, &nn));
