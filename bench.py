@@ -269,6 +269,7 @@ def matvec_numbers(sol, cs, fp64_peak_tflops: float, hbm_gbs: float, cpu: bool, 
         out["cpu_baseline"] = {"ms_per_vector": el * 1e3, "cores": threads, "kind": "port",
                                "sample": f"{nv} vectors through the oracle's stencil matvec (OpenMP)"}
     del dX, dY
+    out["propagator_800x400"] = propagator_large(sol, fp64_peak_tflops)
     if base is not None:
         base.close()
     out["propagator"] = propagator_numbers(fp64_peak_tflops)
@@ -351,22 +352,67 @@ def propagator_numbers(fp64_peak_tflops: float, nchi: int = 100, neta: int = 80,
                                                  ctypes.c_void_p(yp + 8 * n * v), 0))
 
     res = {}
-    for name, fn in (("batched", batched), ("plain", plain)):
-        fn()  # warm-up (scratch allocation)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        fn()
-        torch.cuda.synchronize()
-        res[name] = time.perf_counter() - t0
+    for arith in (1, 0):  # float-float (the default), then FP64
+        sol.ctx.check(L.hymor_set_expm_arith(h, arith))
+        for name, fn in (("batched", batched), ("plain", plain)):
+            fn()  # warm-up (scratch allocation, the float-float copy of the blocks)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            res[(arith, name)] = time.perf_counter() - t0
     sol.close()
     flop = float(nsteps * order) * nchi * neta * MATVEC_FLOP * k
     return {"workload": f"exp(L dt): {nsteps} Taylor steps of degree {order}, {k} vectors x {n} ({nchi}x{neta})",
-            "batched_s": res["batched"], "plain_s": res["plain"],
-            "batched_speedup": res["plain"] / res["batched"],
-            "per_vector_ms": {"batched": res["batched"] / k * 1e3, "plain": res["plain"] / k * 1e3},
-            "fp64_frac": {"batched": flop / res["batched"] / 1e12 / fp64_peak_tflops,
-                          "plain": flop / res["plain"] / 1e12 / fp64_peak_tflops},
+            "arithmetic": "float-float matvecs on the FP32 pipe (default); the fp64 object times the same in FP64",
+            "batched_s": res[(1, "batched")], "plain_s": res[(1, "plain")],
+            "batched_speedup": res[(1, "plain")] / res[(1, "batched")],
+            "per_vector_ms": {"batched": res[(1, "batched")] / k * 1e3, "plain": res[(1, "plain")] / k * 1e3},
+            "fp64_equivalent_tflops": {"batched": flop / res[(1, "batched")] / 1e12,
+                                       "plain": flop / res[(1, "plain")] / 1e12},
+            "fp64": {"batched_s": res[(0, "batched")], "plain_s": res[(0, "plain")],
+                     "fp64_frac": {"batched": flop / res[(0, "batched")] / 1e12 / fp64_peak_tflops,
+                                   "plain": flop / res[(0, "plain")] / 1e12 / fp64_peak_tflops}},
+            "float_float_speedup": {"batched": res[(0, "batched")] / res[(1, "batched")],
+                                    "plain": res[(0, "plain")] / res[(1, "plain")]},
             "gpu_launches": {"batched": 1, "plain": k}}
+
+
+def propagator_large(sol, fp64_peak_tflops: float, k: int = 8, nsteps: int = 50, order: int = 4):
+    """The propagation on the bench case's own Jacobian (800 x 400, 1.28 M unknowns): 50
+    Taylor steps of degree 4 of one vector, and of 8 vectors in one call, in float-float
+    (the default) and in FP64; CUDA-synchronised host clock."""
+    import torch
+    L, h = sol.ctx.L, sol.ctx.h
+    dt = ctypes.c_double()
+    sol.ctx.check(L.hymor_cfl_timestep(h, ctypes.byref(dt)))
+    n = 4 * NCHI * NETA
+    rng = np.random.Generator(np.random.PCG64(5))
+    X = rng.standard_normal((k, n))
+    dX = torch.from_numpy(X.reshape(-1)).cuda()
+    dY = torch.empty_like(dX)
+    out = {"workload": f"exp(L dt): {nsteps} Taylor steps of degree {order}, 1 and {k} vectors x {n} "
+                       f"({NCHI}x{NETA})"}
+    for arith, name in ((1, "float_float"), (0, "fp64")):
+        sol.ctx.check(L.hymor_set_expm_arith(h, arith))
+        row = {}
+        for kk in (1, k):
+            call = lambda: sol.ctx.check(L.hymor_expm_apply_dev(h, kk, dt.value, nsteps, order,
+                                                               ctypes.c_void_p(dX.data_ptr()),
+                                                               ctypes.c_void_p(dY.data_ptr()), 0))
+            call()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            call()
+            torch.cuda.synchronize()
+            el = time.perf_counter() - t0
+            flop = float(nsteps * order) * CELLS * MATVEC_FLOP * kk
+            row[f"{kk}_vectors"] = {"s": el, "ms_per_matvec_vector": el / (nsteps * order * kk) * 1e3,
+                                    "fp64_equivalent_tflops": flop / el / 1e12}
+        out[name] = row
+    sol.ctx.check(L.hymor_set_expm_arith(h, 1))
+    out["float_float_speedup"] = {key: out["fp64"][key]["s"] / out["float_float"][key]["s"] for key in out["fp64"]}
+    return out
 
 
 def _base_solution(name: str):

@@ -39,6 +39,7 @@ EXPORTS = [
     "hymor_expm_apply_multi_dev", "hymor_linearize_b", "hymor_b_get", "hymor_b_set", "hymor_recept_size",
     "hymor_recept_apply_dev", "hymor_recept_expm_dev", "hymor_set_upstream", "hymor_eigs", "hymor_tg_gain",
     "hymor_dense_schur", "hymor_dense_symeig", "hymor_set_step_viscous", "hymor_set_cfl_screen",
+    "hymor_set_expm_arith",
     "hymor_autotune", "hymor_set_flux_tiling",
 ]
 
@@ -128,6 +129,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "hymor_dense_symeig": [i, dp, dp, dp],
         "hymor_set_step_viscous": [vp, i],
         "hymor_set_cfl_screen": [vp, i],
+        "hymor_set_expm_arith": [vp, i],
         "hymor_autotune": [vp, i, ip, ctypes.POINTER(ctypes.c_float)],
         "hymor_set_flux_tiling": [vp, i, i, i],
     }

@@ -725,6 +725,7 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
   d.bwork = nullptr;
   d.sf_zero = 1;  // the flux arrays are allocated zeroed
   d.step_ffv = 1;
+  d.expm_ff = 1;
   d.cfl_screen = 1;
   d.flux_rows = 8;
   d.flux_spare = 1;
@@ -1099,6 +1100,12 @@ int hymor_set_step_viscous(hymor_ctx* ctx, int mode) {
     ctx->d.step_ffv = mode;
     drop_step_graph(ctx);
   }
+  return 0;
+}
+
+int hymor_set_expm_arith(hymor_ctx* ctx, int mode) {
+  if (!ctx || mode < 0 || mode > 1) return HYMOR_ERR_INVALID;
+  ctx->d.expm_ff = mode;
   return 0;
 }
 

@@ -1,4 +1,5 @@
-// Float-float arithmetic on the FP32 pipe for the viscous terms of the RK-step flux.
+// Float-float arithmetic on the FP32 pipe: the viscous terms of the RK-step flux and the
+// Taylor propagator's matvecs.
 //
 // On GB300 one FP64 warp instruction issues per ~70 cycles of an SM sub-partition and one
 // FP32 warp instruction per cycle, so an FP64 operation costs as much as ~70 FP32 ones. A
@@ -54,6 +55,14 @@ __device__ __forceinline__ ff ff_mul(ff a, ff b) {
   return ff_fast_two_sum(p, e);
 }
 
+// acc + b x, with the product's high part exact (TwoProduct by FMA) and its cross terms
+// joining the low part of the sum (the FMA-chain step of a float-float dot product)
+__device__ __forceinline__ ff ff_fma(ff b, ff x, ff acc) {
+  const float p = b.h * x.h;
+  const float e = __fmaf_rn(b.h, x.l, __fmaf_rn(b.l, x.h, __fmaf_rn(b.h, x.h, -p)));
+  return ff_add(acc, ff{p, e});
+}
+
 // a * 2^k for a power of two: exact, no renormalisation
 __device__ __forceinline__ ff ff_scale2(ff a, float p2) { return ff{a.h * p2, a.l * p2}; }
 
@@ -90,13 +99,21 @@ __device__ __forceinline__ ff ff_from_double(double x) {
   return r;
 }
 
-// exact float -> double widening of a normal float (or zero) through the bit pattern
+// double -> float-float as ff_from_double, with non-finite values and values beyond the
+// float range as NaN (the propagator's inputs and coefficients)
+__device__ __forceinline__ ff ff_from_double_checked(double x) {
+  const unsigned e = ((unsigned)__double2hiint(x) >> 20) & 0x7ffu;
+  return e >= 1151u ? ff{__int_as_float(0x7fc00000), 0.0f} : ff_from_double(x);
+}
+
+// exact float -> double widening of a normal float (or zero) through the bit pattern; an
+// infinity or NaN widens to NaN
 __device__ __forceinline__ double ff_widen(float f) {
   const unsigned b = __float_as_uint(f);
   const unsigned ef = (b >> 23) & 0xffu;
   const unsigned hw = (b & 0x80000000u) | (ef ? (((ef + 896u) << 20) | ((b & 0x7fffffu) >> 3)) : 0u);
   const unsigned lw = ef ? (b << 29) : 0u;
-  return __hiloint2double((int)hw, (int)lw);
+  return ef == 0xffu ? __longlong_as_double(0x7ff8000000000000LL) : __hiloint2double((int)hw, (int)lw);
 }
 
 // float-float -> double: one FP64 addition

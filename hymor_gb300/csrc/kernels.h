@@ -51,6 +51,10 @@ struct DevCtx {
                      // screened CFL reduction's FP32 maxima and block counters
   // Jacobian
   double* coef;    // N * 144 stencil blocks (or null)
+  float2* coef_ff; // float-float copy of coef for the propagator (or null)
+  int coef_version, coef_ff_version;  // writes of coef, and the write coef_ff was split from
+  // the cooperative Taylor propagator in float-float (1, the default) or FP64 (0)
+  int expm_ff;
   double* jwork;   // linearisation workspace
   ShockJac sj;
   // prescribed per-column upstream state (4 x Nchi) of the shock chain, or null: set only

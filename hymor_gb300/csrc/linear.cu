@@ -14,6 +14,7 @@
 
 #include <algorithm>
 
+#include "ff.cuh"
 #include "kernels.h"
 
 namespace cg = cooperative_groups;
@@ -374,6 +375,178 @@ __global__ void __launch_bounds__(kMvThreads, 2) k_expm_coop(MvArgs base, int ns
       grid.sync();
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Float-float Taylor propagation (the cooperative propagator's default arithmetic). The
+// Taylor terms and their running sum are float-float pairs (ff.cuh) and the blocks a
+// float-float copy of the Jacobian (coef_ff, split once per linearisation), so that the
+// 144 multiply-adds per cell and vector run on the FP32 pipe, which this GPU issues ~70x
+// faster than FP64; only the input and output vectors are FP64. Each multiply-add is
+// ff_fma (the product's high part exact by FMA, the sum by TwoSum, renormalised), ~2^-47
+// of the largest partial sum, in the order of the FP64 chains (per neighbour block, input
+// component 3 down to 0), so that the one-vector and the batched paths give the same
+// pairs. A Taylor step of degree 4-5 at the CFL time step truncates at a far larger
+// relative level than this rounding; the Jacobian is a finite-difference one (~1e-8).
+struct MvFf {
+  const float2* coef;
+  const float2* X;
+  float2* Y;
+  float2* acc;             // the running sum, or null
+  const float2* acc_prev;  // the previous term, added into acc first (acc += c_prev acc_prev)
+  double scale;            // the time step (split on the device, as the per-vector ones)
+  ff c_acc, c_prev;
+  const double* vscale;    // per-vector time steps, or null
+  Wrap w;
+  long N, ld;
+  int k, transpose;
+};
+
+__device__ __forceinline__ ff ldff(const float2* p, long i) {
+  const float2 v = p[i];
+  return ff{v.x, v.y};
+}
+__device__ __forceinline__ void stff(float2* p, long i, ff v) { p[i] = make_float2(v.h, v.l); }
+
+// one output of a term: val = scale y into Y, and the running sum
+__device__ __forceinline__ void mvff_out(const MvFf& a, int vec, long o, ff y) {
+  const ff sc = ff_from_double(a.vscale ? a.vscale[vec] : a.scale);
+  const ff val = ff_mul(sc, y);
+  stff(a.Y, o, val);
+  if (a.acc) {
+    ff r = ldff(a.acc, o);
+    if (a.acc_prev) r = ff_add(r, ff_mul(ldff(a.acc_prev, o), a.c_prev));
+    stff(a.acc, o, ff_add(r, ff_mul(val, a.c_acc)));
+  }
+}
+
+// thread per (cell, output component, vector), as matvec_one
+__device__ __forceinline__ void matvec_one_ff(const MvFf& a) {
+  const long N = a.N;
+  const long outs = 4 * N;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < outs * a.k; t += (long)gridDim.x * blockDim.x) {
+    const long vec = t / outs;
+    const long w = t - vec * outs;
+    const long m = w % N;
+    const int comp = (int)(w / N);
+    const int i = (int)(m % a.w.nchi), j = (int)(m / a.w.nchi);
+    const float2* xv = a.X + vec * a.ld;
+    ff y{0.0f, 0.0f};
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      const int b = q / 3 - 1, aa = q % 3 - 1;
+      const long n = a.transpose ? a.w.nbr(i, j, -aa, -b) : a.w.nbr(i, j, aa, b);
+      if (n < 0) continue;
+      const long cell = a.transpose ? n : m;
+      ff B[4], X[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int plane = a.transpose ? q * 16 + e * 4 + comp : q * 16 + comp * 4 + e;
+        B[e] = ldff(a.coef, (long)plane * N + cell);
+        X[e] = ldff(xv, e * N + n);
+      }
+      y = ff_fma(B[0], X[0], ff_fma(B[1], X[1], ff_fma(B[2], X[2], ff_fma(B[3], X[3], y))));
+    }
+    mvff_out(a, (int)vec, vec * a.ld + comp * N + m, y);
+  }
+}
+
+// (cell, chunk of kVecChunk vectors) items, as matvec_multi
+__device__ __forceinline__ void matvec_multi_ff(const MvFf& a) {
+  const long N = a.N;
+  const long n4 = a.ld;
+  const int chunks = (a.k + kVecChunk - 1) / kVecChunk;
+  const long items = N * chunks;
+  for (long w = blockIdx.x * (long)blockDim.x + threadIdx.x; w < items; w += (long)gridDim.x * blockDim.x) {
+    const long m = w % N;
+    const int i = (int)(m % a.w.nchi), j = (int)(m / a.w.nchi);
+    const int v0 = (int)(w / N) * kVecChunk;
+    const int nv = min(kVecChunk, a.k - v0);
+    ff y[kVecChunk][4];
+#pragma unroll
+    for (int v = 0; v < kVecChunk; ++v)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) y[v][c] = ff{0.0f, 0.0f};
+#pragma unroll
+    for (int b = -1; b <= 1; ++b)
+#pragma unroll
+      for (int aa = -1; aa <= 1; ++aa) {
+        const long n = a.transpose ? a.w.nbr(i, j, -aa, -b) : a.w.nbr(i, j, aa, b);
+        if (n < 0) continue;
+        const long cell = a.transpose ? n : m;
+        const int q = (b + 1) * 3 + (aa + 1);
+        ff B[16];
+#pragma unroll
+        for (int e = 0; e < 16; ++e) B[e] = ldff(a.coef, (long)(q * 16 + e) * N + cell);
+        for (int v = 0; v < nv; ++v) {
+          const float2* x = a.X + (long)(v0 + v) * n4;
+          const ff x0 = ldff(x, n), x1 = ldff(x, N + n), x2 = ldff(x, 2 * N + n), x3 = ldff(x, 3 * N + n);
+          if (!a.transpose) {
+#pragma unroll
+            for (int vo = 0; vo < 4; ++vo)
+              y[v][vo] = ff_fma(B[vo * 4 + 0], x0,
+                                ff_fma(B[vo * 4 + 1], x1, ff_fma(B[vo * 4 + 2], x2, ff_fma(B[vo * 4 + 3], x3, y[v][vo]))));
+          } else {
+#pragma unroll
+            for (int vi = 0; vi < 4; ++vi)
+              y[v][vi] = ff_fma(B[0 * 4 + vi], x0,
+                                ff_fma(B[1 * 4 + vi], x1, ff_fma(B[2 * 4 + vi], x2, ff_fma(B[3 * 4 + vi], x3, y[v][vi]))));
+          }
+        }
+      }
+    for (int v = 0; v < nv; ++v)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) mvff_out(a, v0 + v, (long)(v0 + v) * n4 + c * N + m, y[v][c]);
+  }
+}
+
+// The cooperative propagation in float-float (degree >= 2, the late-sum order of
+// k_expm_coop): the input vectors are split into the running sum, and the sum is joined
+// into the FP64 output after the last step.
+template <bool ONE>
+__global__ void __launch_bounds__(kMvThreads, 2) k_expm_coop_ff(MvFf base, int nsteps, int order, const double* xin,
+                                                                double* yout, float2* t1, float2* t2, float2* vout,
+                                                                const int* vsteps) {
+  cg::grid_group grid = cg::this_grid();
+  const long nall = base.ld * (long)base.k;
+  for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < nall; q += (long)gridDim.x * blockDim.x)
+    stff(vout, q, ff_from_double_checked(xin[q]));
+  grid.sync();
+  const int kall = base.k;
+  for (int s = 0; s < nsteps; ++s) {
+    if (vsteps) {
+      int ka = 0;
+      while (ka < kall && vsteps[ka] > s) ++ka;
+      base.k = ka;
+    }
+    const float2* src = vout;
+    const float2* prev = nullptr;
+    ff c_prev{0.0f, 0.0f};
+    long fact = 1;
+    for (int j = 1; j <= order; ++j) {
+      fact *= j;
+      MvFf a = base;
+      a.X = src;
+      a.Y = (j % 2) ? t1 : t2;
+      a.acc = j == 1 ? nullptr : vout;
+      a.acc_prev = prev;
+      a.c_prev = c_prev;
+      a.c_acc = ff_from_double(1.0 / (double)fact);
+      if (ONE) matvec_one_ff(a);
+      else matvec_multi_ff(a);
+      grid.sync();
+      src = a.Y;
+      prev = j == 1 ? a.Y : nullptr;
+      c_prev = a.c_acc;
+    }
+  }
+  for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < nall; q += (long)gridDim.x * blockDim.x)
+    yout[q] = ff_to_double(ldff(vout, q));
+}
+
+__global__ void k_coef_to_ff(const double* __restrict__ c, float2* __restrict__ f, long n) {
+  for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
+    stff(f, q, ff_from_double_checked(c[q]));
 }
 
 __global__ void k_copy(const double* __restrict__ s, double* __restrict__ d, long n) {
@@ -1115,6 +1288,7 @@ static PertArgs pert_args(const DevCtx& d) {
 }
 
 void launch_jacobian_assemble(DevCtx& d, cudaStream_t st, JacLanes& L) {
+  ++d.coef_version;
   const hymor_config& c = d.cfg;
   const long N = d.N;
   double* Fb[4];
@@ -1325,7 +1499,8 @@ struct KrylovScratch {
 struct LinearState {
   ExpmCache expm;
   KrylovScratch kry;
-  int coop_blocks[2] = {0, 0};  // co-resident blocks per SM of k_expm_coop<false>, <true>
+  int coop_blocks[4] = {0, 0, 0, 0};  // co-resident blocks per SM of k_expm_coop<false>, <true>,
+                                      // k_expm_coop_ff<false>, <true>
   JacLanes lanes;               // workspaces of the linearisations' perturbed residuals
 };
 LinearState& linear_state(hymor_ctx* ctx) {
@@ -1375,6 +1550,7 @@ int ensure_lanes(hymor_ctx* ctx, JacLanes** out) {
 }
 constexpr int kExpmCoopMinLaunches = 16;
 
+
 // hdts, hsteps (host, k entries, hsteps non-increasing), or null: vector c is propagated
 // hsteps[c] steps of hdts[c] instead of nsteps of dt.
 int expm_cooperative(hymor_ctx* ctx, int k, double dt, int nsteps, int order, const double* dX, double* dY,
@@ -1398,17 +1574,31 @@ int expm_cooperative(hymor_ctx* ctx, int k, double dt, int nsteps, int order, co
   double* t1 = c.buf + n;
   double* t2 = c.buf + 2 * n;
   double* vout = c.buf + 3 * n;
+  // float-float (degree >= 2): the blocks' float-float copy, split again after each write
+  const bool ffp = d.expm_ff && order >= 2;
+  if (ffp && (!d.coef_ff || d.coef_ff_version != d.coef_version)) {
+    if (!d.coef_ff) {
+      void* p = nullptr;
+      if ((r = cuda_check(ctx, cudaMalloc(&p, sizeof(float2) * 144 * d.N)))) return r;
+      ctx_allocs(ctx).push_back(p);
+      d.coef_ff = static_cast<float2*>(p);
+    }
+    k_coef_to_ff<<<grid_for(144 * d.N, 256), 256, 0, st>>>(d.coef, d.coef_ff, 144 * d.N);
+    d.coef_ff_version = d.coef_version;
+  }
   int* blocks_per_sm = linear_state(ctx).coop_blocks;
   const bool one = mv_one(d.N, k, d.sms);
-  const void* kern = one ? (const void*)k_expm_coop<true> : (const void*)k_expm_coop<false>;
-  if (!blocks_per_sm[one] &&
-      (r = cuda_check(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm[one], kern, kMvThreads, 0))))
+  const int kind = (ffp ? 2 : 0) + (one ? 1 : 0);
+  const void* kern = ffp ? (one ? (const void*)k_expm_coop_ff<true> : (const void*)k_expm_coop_ff<false>)
+                         : (one ? (const void*)k_expm_coop<true> : (const void*)k_expm_coop<false>);
+  if (!blocks_per_sm[kind] &&
+      (r = cuda_check(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm[kind], kern, kMvThreads, 0))))
     return r;
   const long items = mv_items(d.N, k, d.sms);
   const int th = mv_threads(items, d.sms);
   const long want = (items + th - 1) / th;
   // co-resident: blocks of th <= 256 threads need no more than a 256-thread block
-  const int grid = (int)std::min<long>(want, (long)blocks_per_sm[one] * d.sms);
+  const int grid = (int)std::min<long>(want, (long)blocks_per_sm[kind] * d.sms);
   MvArgs base;
   base.acc_prev = nullptr;
   base.c_prev = 0;
@@ -1432,6 +1622,28 @@ int expm_cooperative(hymor_ctx* ctx, int k, double dt, int nsteps, int order, co
     if ((r = cuda_check(ctx, cudaMemcpyAsync(vsteps, hsteps, sizeof(int) * k, cudaMemcpyHostToDevice, st)))) return r;
     base.vscale = vscale;
     nsteps = hsteps[0];
+  }
+  if (ffp) {
+    MvFf bf;
+    bf.coef = d.coef_ff;
+    bf.X = nullptr;
+    bf.Y = nullptr;
+    bf.acc = nullptr;
+    bf.acc_prev = nullptr;
+    bf.scale = dt;
+    bf.c_acc = ff{0.0f, 0.0f};
+    bf.c_prev = ff{0.0f, 0.0f};
+    bf.vscale = base.vscale;
+    bf.w = base.w;
+    bf.N = base.N;
+    bf.ld = base.ld;
+    bf.k = k;
+    bf.transpose = transpose;
+    float2* f1 = reinterpret_cast<float2*>(t1);
+    float2* f2 = reinterpret_cast<float2*>(t2);
+    float2* fo = reinterpret_cast<float2*>(vout);
+    void* fargs[] = {&bf, &nsteps, &order, &dX, &dY, &f1, &f2, &fo, &vsteps};
+    return cuda_check(ctx, cudaLaunchCooperativeKernel(kern, grid, th, fargs, 0, st));
   }
   if ((r = cuda_check(ctx, cudaMemcpyAsync(v, dX, sizeof(double) * n, cudaMemcpyDeviceToDevice, st)))) return r;
   if ((r = cuda_check(ctx, cudaMemcpyAsync(vout, dX, sizeof(double) * n, cudaMemcpyDeviceToDevice, st)))) return r;
@@ -1581,6 +1793,7 @@ int hymor_jacobian_set(hymor_ctx* ctx, const double* coef) {
   if ((r = cuda_check(ctx, cudaMallocAsync((void**)&tmp, sizeof(double) * 144 * d.N, st)))) return r;
   r = cuda_check(ctx, cudaMemcpyAsync(tmp, coef, sizeof(double) * 144 * d.N, cudaMemcpyHostToDevice, st));
   k_blocks_to_planes<<<grid_for(d.N * 144, 256), 256, 0, st>>>(tmp, d.coef, d.N);
+  ++d.coef_version;
   cudaFreeAsync(tmp, st);
   if (r) return r;
   return cuda_check(ctx, cudaStreamSynchronize(st));

@@ -115,6 +115,11 @@ class Solution:
         0 FP64 over every cell (hymor_set_cfl_screen); dt is the same bit for bit."""
         self.ctx.check(self.ctx.L.hymor_set_cfl_screen(self.ctx.h, int(on)))
 
+    def set_expm_arith(self, mode: int):
+        """Arithmetic of the cooperative Taylor propagator's matvecs: 1 float-float on the
+        FP32 pipe (default), 0 FP64 (hymor_set_expm_arith)."""
+        self.ctx.check(self.ctx.L.hymor_set_expm_arith(self.ctx.h, int(mode)))
+
     def step_kernels(self) -> int:
         """Kernel launches one ADVECT_FLOW step makes (the kernel nodes of its graph)."""
         n = ctypes.c_int32()

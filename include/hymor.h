@@ -135,6 +135,16 @@ int hymor_set_step_viscous(hymor_ctx* ctx, int mode);
  * FP64. Only the step with shock fitting screens. The next hymor_step re-captures its graph. */
 int hymor_set_cfl_screen(hymor_ctx* ctx, int on);
 
+/* Arithmetic of the Taylor propagator's matvecs (POWER_METHOD!, ARNOLDI_POWER_GPU.jl:36-82;
+ * no counterpart in the reference, which multiplies in FP64). mode 1 (the default): the
+ * propagations that run as one cooperative launch (the stencil operator, Taylor degree >= 2,
+ * 16 launches or more) keep their Taylor terms and running sum as float-float pairs and
+ * multiply by a float-float copy of the blocks on the FP32 pipe, ~2^-47 per operation (the
+ * input and output vectors stay FP64); mode 0: FP64. hymor_matvec_dev, the propagators with
+ * the shock-position unknowns and the receptivity operator are FP64 in either mode. The
+ * eigen and transient-growth solvers (hymor_eigs, hymor_tg_gain) use the context's mode. */
+int hymor_set_expm_arith(hymor_ctx* ctx, int mode);
+
 /* Tile-shape autotuner of the RK step's flux (no counterpart in the reference): times `steps`
  * steps (CUDA events, after a warm-up step) for each flux configuration — the tile halo staged
  * by TMA (cp.async.bulk.tensor) or loaded thread by thread, tiles of 31 x 8 or 31 x 16 cells,

@@ -24,6 +24,9 @@ pytestmark = pytest.mark.gpu
 
 
 def _compare(sol, k, nsteps, order, seed, tol):
+    # both entry points in FP64 (the allocating one would otherwise run its cooperative
+    # launches in float-float)
+    sol.set_expm_arith(0)
     lib, h = sol.ctx.L, sol.ctx.h
     n = sol.operator_size() * k
     X, Y_ref, Y_new = (DeviceBuffer(sol.ctx, 8 * n) for _ in range(3))
