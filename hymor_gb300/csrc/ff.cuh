@@ -63,6 +63,25 @@ __device__ __forceinline__ ff ff_fma(ff b, ff x, ff acc) {
   return ff_add(acc, ff{p, e});
 }
 
+// y + b3 x3 + b2 x2 + b1 x1 + b0 x0 (in that order): each product's high part joins the
+// running high part by TwoSum and its rounding error and cross terms join the low part,
+// which is renormalised (TwoSum) once after the four. The loop-carried dependency is one
+// addition on each part instead of a renormalisation per term; the low part's rounding
+// over the four terms is ~2^-44 of the largest partial sum.
+__device__ __forceinline__ ff ff_dot4(const ff* b, const ff* x, ff y) {
+  float h = y.h, l = y.l;
+#pragma unroll
+  for (int e = 3; e >= 0; --e) {
+    const float p = b[e].h * x[e].h;
+    const float pe = __fmaf_rn(b[e].h, x[e].l, __fmaf_rn(b[e].l, x[e].h, __fmaf_rn(b[e].h, x[e].h, -p)));
+    const float s = h + p;
+    const float bb = s - h;
+    l += ((h - (s - bb)) + (p - bb)) + pe;
+    h = s;
+  }
+  return ff_two_sum(h, l);
+}
+
 // a * 2^k for a power of two: exact, no renormalisation
 __device__ __forceinline__ ff ff_scale2(ff a, float p2) { return ff{a.h * p2, a.l * p2}; }
 

@@ -382,11 +382,10 @@ __global__ void __launch_bounds__(kMvThreads, 2) k_expm_coop(MvArgs base, int ns
 // Taylor terms and their running sum are float-float pairs (ff.cuh) and the blocks a
 // float-float copy of the Jacobian (coef_ff, split once per linearisation), so that the
 // 144 multiply-adds per cell and vector run on the FP32 pipe, which this GPU issues ~70x
-// faster than FP64; only the input and output vectors are FP64. Each multiply-add is
-// ff_fma (the product's high part exact by FMA, the sum by TwoSum, renormalised), ~2^-47
-// of the largest partial sum, in the order of the FP64 chains (per neighbour block, input
-// component 3 down to 0), so that the one-vector and the batched paths give the same
-// pairs. A Taylor step of degree 4-5 at the CFL time step truncates at a far larger
+// faster than FP64; only the input and output vectors are FP64. Each neighbour block adds
+// its four products with ff_dot4 (the products' high parts exact by FMA, the sums by
+// TwoSum, one renormalisation per block), in the order of the FP64 chains (input component
+// 3 down to 0), so that the one-vector and the batched paths give the same pairs. A Taylor step of degree 4-5 at the CFL time step truncates at a far larger
 // relative level than this rounding; the Jacobian is a finite-difference one (~1e-8).
 struct MvFf {
   const float2* coef;
@@ -445,31 +444,36 @@ __device__ __forceinline__ void matvec_one_ff(const MvFf& a) {
         B[e] = ldff(a.coef, (long)plane * N + cell);
         X[e] = ldff(xv, e * N + n);
       }
-      y = ff_fma(B[0], X[0], ff_fma(B[1], X[1], ff_fma(B[2], X[2], ff_fma(B[3], X[3], y))));
+      y = ff_dot4(B, X, y);
     }
     mvff_out(a, (int)vec, vec * a.ld + comp * N + m, y);
   }
 }
 
-// (cell, chunk of kVecChunk vectors) items, as matvec_multi
+// (cell, chunk of KV vectors) items, as matvec_multi (KV = kVecChunk; KV = 1 for a single
+// vector on a large grid, where the smaller register set raises the occupancy of this
+// HBM-bound case: the 144 block entries are read once per cell and vector)
+template <int KV>
 __device__ __forceinline__ void matvec_multi_ff(const MvFf& a) {
   const long N = a.N;
   const long n4 = a.ld;
-  const int chunks = (a.k + kVecChunk - 1) / kVecChunk;
+  const int chunks = (a.k + KV - 1) / KV;
   const long items = N * chunks;
   for (long w = blockIdx.x * (long)blockDim.x + threadIdx.x; w < items; w += (long)gridDim.x * blockDim.x) {
     const long m = w % N;
     const int i = (int)(m % a.w.nchi), j = (int)(m / a.w.nchi);
-    const int v0 = (int)(w / N) * kVecChunk;
-    const int nv = min(kVecChunk, a.k - v0);
-    ff y[kVecChunk][4];
+    const int v0 = (int)(w / N) * KV;
+    const int nv = min(KV, a.k - v0);
+    ff y[KV][4];
 #pragma unroll
-    for (int v = 0; v < kVecChunk; ++v)
+    for (int v = 0; v < KV; ++v)
 #pragma unroll
       for (int c = 0; c < 4; ++c) y[v][c] = ff{0.0f, 0.0f};
-#pragma unroll
+    // one neighbour block at a time for a single vector (its 16 pairs in registers), all
+    // nine unrolled for a chunk
+#pragma unroll(KV == 1 ? 1 : 3)
     for (int b = -1; b <= 1; ++b)
-#pragma unroll
+#pragma unroll(KV == 1 ? 1 : 3)
       for (int aa = -1; aa <= 1; ++aa) {
         const long n = a.transpose ? a.w.nbr(i, j, -aa, -b) : a.w.nbr(i, j, aa, b);
         if (n < 0) continue;
@@ -478,33 +482,84 @@ __device__ __forceinline__ void matvec_multi_ff(const MvFf& a) {
         ff B[16];
 #pragma unroll
         for (int e = 0; e < 16; ++e) B[e] = ldff(a.coef, (long)(q * 16 + e) * N + cell);
-        for (int v = 0; v < nv; ++v) {
+        // unrolled over the chunk with a predicate, so that the pairs of y stay in registers
+#pragma unroll
+        for (int v = 0; v < KV; ++v) {
+          if (v >= nv) continue;
           const float2* x = a.X + (long)(v0 + v) * n4;
-          const ff x0 = ldff(x, n), x1 = ldff(x, N + n), x2 = ldff(x, 2 * N + n), x3 = ldff(x, 3 * N + n);
-          if (!a.transpose) {
+          const ff xs[4] = {ldff(x, n), ldff(x, N + n), ldff(x, 2 * N + n), ldff(x, 3 * N + n)};
 #pragma unroll
-            for (int vo = 0; vo < 4; ++vo)
-              y[v][vo] = ff_fma(B[vo * 4 + 0], x0,
-                                ff_fma(B[vo * 4 + 1], x1, ff_fma(B[vo * 4 + 2], x2, ff_fma(B[vo * 4 + 3], x3, y[v][vo]))));
-          } else {
-#pragma unroll
-            for (int vi = 0; vi < 4; ++vi)
-              y[v][vi] = ff_fma(B[0 * 4 + vi], x0,
-                                ff_fma(B[1 * 4 + vi], x1, ff_fma(B[2 * 4 + vi], x2, ff_fma(B[3 * 4 + vi], x3, y[v][vi]))));
+          for (int c = 0; c < 4; ++c) {
+            // row c of the block, or column c for the transpose
+            const ff bs[4] = {B[a.transpose ? c : c * 4], B[a.transpose ? 4 + c : c * 4 + 1],
+                              B[a.transpose ? 8 + c : c * 4 + 2], B[a.transpose ? 12 + c : c * 4 + 3]};
+            y[v][c] = ff_dot4(bs, xs, y[v][c]);
           }
         }
       }
-    for (int v = 0; v < nv; ++v)
 #pragma unroll
-      for (int c = 0; c < 4; ++c) mvff_out(a, v0 + v, (long)(v0 + v) * n4 + c * N + m, y[v][c]);
+    for (int v = 0; v < KV; ++v)
+      if (v < nv)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) mvff_out(a, v0 + v, (long)(v0 + v) * n4 + c * N + m, y[v][c]);
+  }
+}
+
+// (cell, output component, chunk of KV vectors) items: 4 block entries per neighbour in
+// registers instead of 16, for the occupancy that keeps the FP32 pipe busy with a batch
+// (the four threads of a cell read its inputs four times, from L1)
+template <int KV>
+__device__ __forceinline__ void matvec_comp_ff(const MvFf& a) {
+  const long N = a.N;
+  const long n4 = a.ld;
+  const int chunks = (a.k + KV - 1) / KV;
+  const long items = 4 * N * chunks;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < items; t += (long)gridDim.x * blockDim.x) {
+    const long m = t % N;
+    const long r = t / N;
+    const int comp = (int)(r % 4);
+    const int v0 = (int)(r / 4) * KV;
+    const int nv = min(KV, a.k - v0);
+    const int i = (int)(m % a.w.nchi), j = (int)(m / a.w.nchi);
+    ff y[KV];
+#pragma unroll
+    for (int v = 0; v < KV; ++v) y[v] = ff{0.0f, 0.0f};
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      const int b = q / 3 - 1, aa = q % 3 - 1;
+      const long n = a.transpose ? a.w.nbr(i, j, -aa, -b) : a.w.nbr(i, j, aa, b);
+      if (n < 0) continue;
+      const long cell = a.transpose ? n : m;
+      ff B[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int plane = a.transpose ? q * 16 + e * 4 + comp : q * 16 + comp * 4 + e;
+        B[e] = ldff(a.coef, (long)plane * N + cell);
+      }
+#pragma unroll
+      for (int v = 0; v < KV; ++v) {
+        if (v >= nv) continue;
+        const float2* x = a.X + (long)(v0 + v) * n4;
+        const ff xs[4] = {ldff(x, n), ldff(x, N + n), ldff(x, 2 * N + n), ldff(x, 3 * N + n)};
+        y[v] = ff_dot4(B, xs, y[v]);
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < KV; ++v)
+      if (v < nv) mvff_out(a, v0 + v, (long)(v0 + v) * n4 + comp * N + m, y[v]);
   }
 }
 
 // The cooperative propagation in float-float (degree >= 2, the late-sum order of
 // k_expm_coop): the input vectors are split into the running sum, and the sum is joined
-// into the FP64 output after the last step.
-template <bool ONE>
-__global__ void __launch_bounds__(kMvThreads, 2) k_expm_coop_ff(MvFf base, int nsteps, int order, const double* xin,
+// into the FP64 output after the last step. MODE 0: matvec_comp_ff<kVecChunk> (a batch on a
+// large grid), 1: matvec_one_ff (few cells x vectors), 2: matvec_multi_ff<1> (one vector on
+// a large grid), 3: matvec_multi_ff<kVecChunk> (a batch on a small grid). Measured on the
+// 800 x 400 Jacobian: 68 us per vector-matvec for one vector (MODE 2; 111 in FP64) and for
+// 8 (MODE 0; 83 with MODE 3, 91 in FP64); 64 vectors on the 100 x 80 one: 18.5 ms for 250
+// matvecs with MODE 3, 24 with MODE 0, 40 in FP64.
+template <int MODE>
+__global__ void __launch_bounds__(kMvThreads, MODE == 1 || MODE == 3 ? 2 : 3) k_expm_coop_ff(MvFf base, int nsteps, int order, const double* xin,
                                                                 double* yout, float2* t1, float2* t2, float2* vout,
                                                                 const int* vsteps) {
   cg::grid_group grid = cg::this_grid();
@@ -532,8 +587,10 @@ __global__ void __launch_bounds__(kMvThreads, 2) k_expm_coop_ff(MvFf base, int n
       a.acc_prev = prev;
       a.c_prev = c_prev;
       a.c_acc = ff_from_double(1.0 / (double)fact);
-      if (ONE) matvec_one_ff(a);
-      else matvec_multi_ff(a);
+      if (MODE == 1) matvec_one_ff(a);
+      else if (MODE == 2) matvec_multi_ff<1>(a);
+      else if (MODE == 3) matvec_multi_ff<kVecChunk>(a);
+      else matvec_comp_ff<kVecChunk>(a);
       grid.sync();
       src = a.Y;
       prev = j == 1 ? a.Y : nullptr;
@@ -1499,8 +1556,8 @@ struct KrylovScratch {
 struct LinearState {
   ExpmCache expm;
   KrylovScratch kry;
-  int coop_blocks[4] = {0, 0, 0, 0};  // co-resident blocks per SM of k_expm_coop<false>, <true>,
-                                      // k_expm_coop_ff<false>, <true>
+  int coop_blocks[6] = {0, 0, 0, 0, 0, 0};  // co-resident blocks per SM of k_expm_coop<false>,
+                                            // <true>, k_expm_coop_ff<0>, <1>, <2>, <3>
   JacLanes lanes;               // workspaces of the linearisations' perturbed residuals
 };
 LinearState& linear_state(hymor_ctx* ctx) {
@@ -1549,6 +1606,8 @@ int ensure_lanes(hymor_ctx* ctx, JacLanes** out) {
   return 0;
 }
 constexpr int kExpmCoopMinLaunches = 16;
+// grids from this many cells take the thread-per-component float-float batch
+constexpr long kFfCompCells = 65536;
 
 
 // hdts, hsteps (host, k entries, hsteps non-increasing), or null: vector c is propagated
@@ -1588,13 +1647,19 @@ int expm_cooperative(hymor_ctx* ctx, int k, double dt, int nsteps, int order, co
   }
   int* blocks_per_sm = linear_state(ctx).coop_blocks;
   const bool one = mv_one(d.N, k, d.sms);
-  const int kind = (ffp ? 2 : 0) + (one ? 1 : 0);
-  const void* kern = ffp ? (one ? (const void*)k_expm_coop_ff<true> : (const void*)k_expm_coop_ff<false>)
-                         : (one ? (const void*)k_expm_coop<true> : (const void*)k_expm_coop<false>);
+  // float-float: thread per output on few cells x vectors, one cell per thread for one vector,
+  // a thread per output component for a batch on a large grid, a chunk per thread on a small
+  const int ffmode = one ? 1 : (k == 1 ? 2 : (d.N >= kFfCompCells ? 0 : 3));
+  const int kind = ffp ? 2 + ffmode : (one ? 1 : 0);
+  const void* kerns[6] = {(const void*)k_expm_coop<false>, (const void*)k_expm_coop<true>,
+                          (const void*)k_expm_coop_ff<0>, (const void*)k_expm_coop_ff<1>,
+                          (const void*)k_expm_coop_ff<2>, (const void*)k_expm_coop_ff<3>};
+  const void* kern = kerns[kind];
   if (!blocks_per_sm[kind] &&
       (r = cuda_check(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm[kind], kern, kMvThreads, 0))))
     return r;
-  const long items = mv_items(d.N, k, d.sms);
+  // the batched float-float path takes a thread per output component
+  const long items = mv_items(d.N, k, d.sms) * (kind == 2 ? 4 : 1);
   const int th = mv_threads(items, d.sms);
   const long want = (items + th - 1) / th;
   // co-resident: blocks of th <= 256 threads need no more than a 256-thread block
