@@ -18,6 +18,7 @@
 // clock per SM): geometry-only factors are precomputed per face (common.cuh), every face
 // flux is evaluated once per tile in shared memory, and divisions are replaced by
 // reciprocal multiplies (frcp).
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -2513,10 +2514,13 @@ void launch_cfl_screened(const DevCtx& d, cudaStream_t st) {
   float* c2f = reinterpret_cast<float*>(d.cflw);  // G floats
   float* rf = c2f + d.G;                          // N floats (G + N floats fit in NLR + NBT doubles)
   unsigned* scr = d.ticket + 2;
+  // the second passes read one float per cell and evaluate a few cells: two blocks per SM,
+  // so that the blocks' atomics on the two maxima and the counter stay few
+  const int exact_grid = std::min(grid_for(d.G, 256), 2 * d.sms);
   k_cmax_screen<<<grid_for(d.G, 256), 256, 0, st>>>(S, c2f, scr);
-  k_cmax_exact<<<grid_for(d.G, 256), 256, 0, st>>>(S, c2f, scr);
+  k_cmax_exact<<<exact_grid, 256, 0, st>>>(S, c2f, scr);
   k_cfl_screen<<<grid_for(d.N, 256), 256, 0, st>>>(A, rf, scr);
-  k_cfl_exact<<<grid_for(d.N, 256), 256, 0, st>>>(A, rf, scr, d.cfg.CFL, d.cfg.max_dt);
+  k_cfl_exact<<<std::min(grid_for(d.N, 256), 2 * d.sms), 256, 0, st>>>(A, rf, scr, d.cfg.CFL, d.cfg.max_dt);
 }
 
 void launch_fill_minrho(const DevCtx& d, bool advance_time, cudaStream_t st) {
