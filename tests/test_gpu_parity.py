@@ -162,6 +162,36 @@ def test_advect_host_matches_separate_calls(require_gpu):
     b.close()
 
 
+@pytest.mark.parametrize("offset", [0, 1])
+def test_advect_host_pinned_state(require_gpu, offset):
+    """hymor_advect with the state in page-locked host memory (as the benchmark's end-to-end
+    loop holds it; offset 1 shifts the array by one double) gives exactly what pageable
+    buffers give, on an odd ghosted size too."""
+    torch = pytest.importorskip("torch")
+    for nchi, neta in ((40, 30), (33, 17)):
+        cfg = C.cylinder_config(nchi, neta)
+        cs = C.initial_state(cfg)
+        a = S.Solution(cs)
+        st = a.get_state()
+        qa = st["q"].copy()
+        pa = [st[k].copy() for k in ("pts_x", "pts_y", "pts_chi", "pts_eta")]
+        ca = st["cell_idx"].copy()
+        ta = a.advect_host(qa, *pa, ca, st["t"], 3)
+        buf = torch.empty(qa.size + 1, dtype=torch.float64).pin_memory()
+        qp = buf.numpy()[offset:offset + qa.size]
+        qp[:] = st["q"]
+        pb = [st[k].copy() for k in ("pts_x", "pts_y", "pts_chi", "pts_eta")]
+        cb = st["cell_idx"].copy()
+        b = S.Solution(cs)
+        tb = b.advect_host(qp, *pb, cb, st["t"], 3)
+        assert np.array_equal(qp, qa) and tb == ta, (nchi, neta)
+        for u, v in zip(pa, pb):
+            assert np.array_equal(u, v)
+        assert np.array_equal(ca, cb)
+        a.close()
+        b.close()
+
+
 def test_stored_flux_enters_cfl_and_steps(require_gpu):
     """The stored flux s["flux"] (set by PDE on the solution) enters CFL_TIMESTEP's dt2
     term: steps taken before and after it is first written match the oracle (the step
