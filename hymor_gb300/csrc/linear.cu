@@ -406,6 +406,12 @@ __device__ __forceinline__ ff ldff(const float2* p, long i) {
   return ff{v.x, v.y};
 }
 __device__ __forceinline__ void stff(float2* p, long i, ff v) { p[i] = make_float2(v.h, v.l); }
+// the block entries, read once per cell and chunk of vectors: streaming loads (evict-first),
+// so that they do not push the vectors, which every neighbour re-reads, out of L2
+__device__ __forceinline__ ff ldff_stream(const float2* p, long i) {
+  const float2 v = __ldcs(p + i);
+  return ff{v.x, v.y};
+}
 
 // one output of a term: val = scale y into Y, and the running sum
 __device__ __forceinline__ void mvff_out(const MvFf& a, int vec, long o, ff y) {
@@ -441,7 +447,7 @@ __device__ __forceinline__ void matvec_one_ff(const MvFf& a) {
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         const int plane = a.transpose ? q * 16 + e * 4 + comp : q * 16 + comp * 4 + e;
-        B[e] = ldff(a.coef, (long)plane * N + cell);
+        B[e] = ldff_stream(a.coef, (long)plane * N + cell);
         X[e] = ldff(xv, e * N + n);
       }
       y = ff_dot4(B, X, y);
@@ -481,7 +487,7 @@ __device__ __forceinline__ void matvec_multi_ff(const MvFf& a) {
         const int q = (b + 1) * 3 + (aa + 1);
         ff B[16];
 #pragma unroll
-        for (int e = 0; e < 16; ++e) B[e] = ldff(a.coef, (long)(q * 16 + e) * N + cell);
+        for (int e = 0; e < 16; ++e) B[e] = ldff_stream(a.coef, (long)(q * 16 + e) * N + cell);
         // unrolled over the chunk with a predicate, so that the pairs of y stay in registers
 #pragma unroll
         for (int v = 0; v < KV; ++v) {
@@ -534,7 +540,7 @@ __device__ __forceinline__ void matvec_comp_ff(const MvFf& a) {
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         const int plane = a.transpose ? q * 16 + e * 4 + comp : q * 16 + comp * 4 + e;
-        B[e] = ldff(a.coef, (long)plane * N + cell);
+        B[e] = ldff_stream(a.coef, (long)plane * N + cell);
       }
 #pragma unroll
       for (int v = 0; v < KV; ++v) {
