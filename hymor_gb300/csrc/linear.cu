@@ -170,6 +170,14 @@ struct MvArgs {
   int k, transpose;
 };
 
+// ST: the blocks exceed L2 and are read with streaming (evict-first) loads, which keep the
+// vectors that every neighbour re-reads in L2; blocks that fit stay cached from one matvec
+// of a propagation to the next (a compile-time choice: a branch per load slowed the loads)
+template <bool ST>
+__device__ __forceinline__ double ld_coef(const double* p) {
+  return ST ? __ldcs(p) : *p;
+}
+
 // y = scale * A x (or A^T x), acc += c_acc y. The work items are (cell, chunk of
 // kVecChunk vectors) pairs, cell fastest, over a grid-stride loop: a batch of vectors on
 // a small grid still spreads over every SM (a 100 x 80 grid is 8000 cells, 64 vectors are
@@ -181,6 +189,7 @@ struct MvArgs {
 // matvec by its own issue rate; a thread per output spreads the work over four times the
 // warps per vector. The next neighbour block's coefficients and inputs are loaded while
 // the current block's FMAs run.
+template <bool ST>
 __device__ __forceinline__ void matvec_one(const MvArgs& a) {
   const long N = a.N;
   const long outs = 4 * N;
@@ -211,7 +220,7 @@ __device__ __forceinline__ void matvec_one(const MvArgs& a) {
         for (int e = 0; e < 4; ++e) {
           // row comp of the block (columns e), or column comp of it for the transpose
           const int plane = a.transpose ? q * 16 + e * 4 + comp : q * 16 + comp * 4 + e;
-          B[slot][e] = a.coef[(long)plane * N + cell];
+          B[slot][e] = ld_coef<ST>(a.coef + (long)plane * N + cell);
           X[slot][e] = xv[e * N + n];
         }
       }
@@ -240,6 +249,10 @@ __device__ __forceinline__ void matvec_one(const MvArgs& a) {
 // with one thread per (cell, chunk of vectors) (matvec_multi, whose single pass over the
 // 144 coefficients for a chunk of vectors is then cheaper).
 __host__ __device__ inline long mv_one_limit(int sms) { return 8L * 32 * 4 * sms; }
+// the Jacobian's blocks (144 per cell, 8 bytes each) larger than this many bytes take
+// streaming loads in the matvecs (about a third of the L2, leaving the rest to the
+// vectors); smaller blocks stay cached from one matvec of a propagation to the next
+constexpr long kCoefStreamBytes = 48L << 20;
 bool mv_one(long N, int k, int sms) { return N * k < mv_one_limit(sms); }
 
 // Work items of a matvec over k vectors: (cell, output component, vector) on the
@@ -248,6 +261,7 @@ long mv_items(long N, int k, int sms) {
   return mv_one(N, k, sms) ? 4 * N * k : N * ((k + kVecChunk - 1) / kVecChunk);
 }
 
+template <bool ST>
 __device__ __forceinline__ void matvec_multi(const MvArgs& a) {
   const long N = a.N;
   const long n4 = a.ld;
@@ -284,7 +298,7 @@ __device__ __forceinline__ void matvec_multi(const MvArgs& a) {
           if (n < 0) continue;
           double B[16];
 #pragma unroll
-          for (int e = 0; e < 16; ++e) B[e] = a.coef[(long)(q * 16 + e) * N + cell];
+          for (int e = 0; e < 16; ++e) B[e] = ld_coef<ST>(a.coef + (long)(q * 16 + e) * N + cell);
           for (int v = 0; v < nv; ++v) {
             const double* x = a.X + (long)(v0 + v) * n4;
             const double x0 = x[n], x1 = x[N + n], x2 = x[2 * N + n], x3 = x[3 * N + n];
@@ -320,21 +334,21 @@ __device__ __forceinline__ void matvec_multi(const MvArgs& a) {
 
 // ONE: the one-vector path (its own kernel, so that its registers do not lower the
 // occupancy of the batched path)
-template <bool ONE>
+template <bool ONE, bool ST>
 __device__ __forceinline__ void matvec_cells(const MvArgs& a) {
-  if (ONE) matvec_one(a);
-  else matvec_multi(a);
+  if (ONE) matvec_one<ST>(a);
+  else matvec_multi<ST>(a);
 }
 
-template <bool ONE>
-__global__ void __launch_bounds__(kMvThreads) k_matvec(MvArgs a) { matvec_cells<ONE>(a); }
+template <bool ONE, bool ST>
+__global__ void __launch_bounds__(kMvThreads) k_matvec(MvArgs a) { matvec_cells<ONE, ST>(a); }
 
 // The whole Taylor propagation in one cooperative launch: the blocks are co-resident
 // (cudaLaunchCooperativeKernel) and meet at a grid barrier after every matvec, instead of
 // one kernel per matvec. Same per-cell arithmetic, in the same order, as launch_expm.
 // vsteps (k entries, non-increasing, or null): vector c takes vsteps[c] steps, so that at
 // step s only the first #{c : vsteps[c] > s} vectors advance (a contiguous prefix).
-template <bool ONE>
+template <bool ONE, bool ST>
 __global__ void __launch_bounds__(kMvThreads, 2) k_expm_coop(MvArgs base, int nsteps, int order, double* v,
                                                              double* t1, double* t2, double* vout,
                                                              const int* vsteps) {
@@ -363,7 +377,7 @@ __global__ void __launch_bounds__(kMvThreads, 2) k_expm_coop(MvArgs base, int ns
       a.acc_prev = prev;
       a.c_prev = c_prev;
       a.c_acc = 1.0 / (double)fact;
-      matvec_cells<ONE>(a);
+      matvec_cells<ONE, ST>(a);
       grid.sync();
       src = a.Y;
       prev = (late && j == 1) ? a.Y : nullptr;
@@ -406,10 +420,12 @@ __device__ __forceinline__ ff ldff(const float2* p, long i) {
   return ff{v.x, v.y};
 }
 __device__ __forceinline__ void stff(float2* p, long i, ff v) { p[i] = make_float2(v.h, v.l); }
-// the block entries, read once per cell and chunk of vectors: streaming loads (evict-first),
-// so that they do not push the vectors, which every neighbour re-reads, out of L2
-__device__ __forceinline__ ff ldff_stream(const float2* p, long i) {
-  const float2 v = __ldcs(p + i);
+// the block entries, read once per cell and chunk of vectors: when they exceed L2, streaming
+// loads (evict-first), so that they do not push the vectors, which every neighbour re-reads,
+// out of L2; when they fit, ordinary loads, which keep them cached across the matvecs
+template <bool ST>
+__device__ __forceinline__ ff ldff_coef(const float2* p, long i) {
+  const float2 v = ST ? __ldcs(p + i) : p[i];
   return ff{v.x, v.y};
 }
 
@@ -426,6 +442,7 @@ __device__ __forceinline__ void mvff_out(const MvFf& a, int vec, long o, ff y) {
 }
 
 // thread per (cell, output component, vector), as matvec_one
+template <bool ST>
 __device__ __forceinline__ void matvec_one_ff(const MvFf& a) {
   const long N = a.N;
   const long outs = 4 * N;
@@ -447,7 +464,7 @@ __device__ __forceinline__ void matvec_one_ff(const MvFf& a) {
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         const int plane = a.transpose ? q * 16 + e * 4 + comp : q * 16 + comp * 4 + e;
-        B[e] = ldff_stream(a.coef, (long)plane * N + cell);
+        B[e] = ldff_coef<ST>(a.coef, (long)plane * N + cell);
         X[e] = ldff(xv, e * N + n);
       }
       y = ff_dot4(B, X, y);
@@ -459,7 +476,7 @@ __device__ __forceinline__ void matvec_one_ff(const MvFf& a) {
 // (cell, chunk of KV vectors) items, as matvec_multi (KV = kVecChunk; KV = 1 for a single
 // vector on a large grid, where the smaller register set raises the occupancy of this
 // HBM-bound case: the 144 block entries are read once per cell and vector)
-template <int KV>
+template <int KV, bool ST>
 __device__ __forceinline__ void matvec_multi_ff(const MvFf& a) {
   const long N = a.N;
   const long n4 = a.ld;
@@ -487,7 +504,7 @@ __device__ __forceinline__ void matvec_multi_ff(const MvFf& a) {
         const int q = (b + 1) * 3 + (aa + 1);
         ff B[16];
 #pragma unroll
-        for (int e = 0; e < 16; ++e) B[e] = ldff_stream(a.coef, (long)(q * 16 + e) * N + cell);
+        for (int e = 0; e < 16; ++e) B[e] = ldff_coef<ST>(a.coef, (long)(q * 16 + e) * N + cell);
         // unrolled over the chunk with a predicate, so that the pairs of y stay in registers
 #pragma unroll
         for (int v = 0; v < KV; ++v) {
@@ -514,7 +531,7 @@ __device__ __forceinline__ void matvec_multi_ff(const MvFf& a) {
 // (cell, output component, chunk of KV vectors) items: 4 block entries per neighbour in
 // registers instead of 16, for the occupancy that keeps the FP32 pipe busy with a batch
 // (the four threads of a cell read its inputs four times, from L1)
-template <int KV>
+template <int KV, bool ST>
 __device__ __forceinline__ void matvec_comp_ff(const MvFf& a) {
   const long N = a.N;
   const long n4 = a.ld;
@@ -540,7 +557,7 @@ __device__ __forceinline__ void matvec_comp_ff(const MvFf& a) {
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         const int plane = a.transpose ? q * 16 + e * 4 + comp : q * 16 + comp * 4 + e;
-        B[e] = ldff_stream(a.coef, (long)plane * N + cell);
+        B[e] = ldff_coef<ST>(a.coef, (long)plane * N + cell);
       }
 #pragma unroll
       for (int v = 0; v < KV; ++v) {
@@ -564,7 +581,7 @@ __device__ __forceinline__ void matvec_comp_ff(const MvFf& a) {
 // 800 x 400 Jacobian: 68 us per vector-matvec for one vector (MODE 2; 111 in FP64) and for
 // 8 (MODE 0; 83 with MODE 3, 91 in FP64); 64 vectors on the 100 x 80 one: 18.5 ms for 250
 // matvecs with MODE 3, 24 with MODE 0, 40 in FP64.
-template <int MODE>
+template <int MODE, bool ST>
 __global__ void __launch_bounds__(kMvThreads, MODE == 1 || MODE == 3 ? 2 : 3) k_expm_coop_ff(MvFf base, int nsteps, int order, const double* xin,
                                                                 double* yout, float2* t1, float2* t2, float2* vout,
                                                                 const int* vsteps) {
@@ -593,10 +610,10 @@ __global__ void __launch_bounds__(kMvThreads, MODE == 1 || MODE == 3 ? 2 : 3) k_
       a.acc_prev = prev;
       a.c_prev = c_prev;
       a.c_acc = ff_from_double(1.0 / (double)fact);
-      if (MODE == 1) matvec_one_ff(a);
-      else if (MODE == 2) matvec_multi_ff<1>(a);
-      else if (MODE == 3) matvec_multi_ff<kVecChunk>(a);
-      else matvec_comp_ff<kVecChunk>(a);
+      if (MODE == 1) matvec_one_ff<ST>(a);
+      else if (MODE == 2) matvec_multi_ff<1, ST>(a);
+      else if (MODE == 3) matvec_multi_ff<kVecChunk, ST>(a);
+      else matvec_comp_ff<kVecChunk, ST>(a);
       grid.sync();
       src = a.Y;
       prev = j == 1 ? a.Y : nullptr;
@@ -1047,6 +1064,16 @@ void launch_shock_mv(const DevCtx& d, int k, const double* X, double* Y, int tra
 
 // y = scale A x over k vectors of op_size(d) entries (stride ld, 0: op_size(d)): the stencil
 // blocks, then the shock-position blocks when the operator has them.
+int coef_stream(const DevCtx& d) { return 144L * d.N * 8 > kCoefStreamBytes ? 1 : 0; }
+
+void launch_k_matvec(const DevCtx& d, int k, const MvArgs& a, int grid, int th, cudaStream_t st) {
+  const bool one = mv_one(d.N, k, d.sms), stream = coef_stream(d);
+  if (one && stream) k_matvec<true, true><<<grid, th, 0, st>>>(a);
+  else if (one) k_matvec<true, false><<<grid, th, 0, st>>>(a);
+  else if (stream) k_matvec<false, true><<<grid, th, 0, st>>>(a);
+  else k_matvec<false, false><<<grid, th, 0, st>>>(a);
+}
+
 void launch_matvec(const DevCtx& d, int k, const double* X, double* Y, int transpose, double scale,
                    cudaStream_t st, long ld) {
   if (ld <= 0) ld = op_size(d);
@@ -1067,8 +1094,7 @@ void launch_matvec(const DevCtx& d, int k, const double* X, double* Y, int trans
   a.transpose = transpose;
   const long items = mv_items(d.N, k, d.sms);
   const int th = mv_threads(items, d.sms);
-  if (mv_one(d.N, k, d.sms)) k_matvec<true><<<grid_for(items, th), th, 0, st>>>(a);
-  else k_matvec<false><<<grid_for(items, th), th, 0, st>>>(a);
+  launch_k_matvec(d, k, a, grid_for(items, th), th, st);
   if (d.sj.on) launch_shock_mv(d, k, X, Y, transpose, scale, st, ld);
 }
 
@@ -1194,8 +1220,7 @@ static void launch_expm_body(const DevCtx& d, int k, double dt, int nsteps, int 
       a.acc_prev = prev;
       a.c_prev = c_prev;
       a.c_acc = 1.0 / (double)fact;
-      if (mv_one(d.N, k, d.sms)) k_matvec<true><<<grid_for(items, th), th, 0, st>>>(a);
-      else k_matvec<false><<<grid_for(items, th), th, 0, st>>>(a);
+      launch_k_matvec(d, k, a, grid_for(items, th), th, st);
       src = dst;
       prev = (late && j == 1) ? dst : nullptr;
       c_prev = a.c_acc;
@@ -1562,8 +1587,9 @@ struct KrylovScratch {
 struct LinearState {
   ExpmCache expm;
   KrylovScratch kry;
-  int coop_blocks[6] = {0, 0, 0, 0, 0, 0};  // co-resident blocks per SM of k_expm_coop<false>,
-                                            // <true>, k_expm_coop_ff<0>, <1>, <2>, <3>
+  int coop_blocks[12] = {};  // co-resident blocks per SM of k_expm_coop<false>, <true>,
+                             // k_expm_coop_ff<0>, <1>, <2>, <3>, each with ordinary and
+                             // streaming block loads
   JacLanes lanes;               // workspaces of the linearisations' perturbed residuals
 };
 LinearState& linear_state(hymor_ctx* ctx) {
@@ -1657,19 +1683,23 @@ int expm_cooperative(hymor_ctx* ctx, int k, double dt, int nsteps, int order, co
   // a thread per output component for a batch on a large grid, a chunk per thread on a small
   const int ffmode = one ? 1 : (k == 1 ? 2 : (d.N >= kFfCompCells ? 0 : 3));
   const int kind = ffp ? 2 + ffmode : (one ? 1 : 0);
-  const void* kerns[6] = {(const void*)k_expm_coop<false>, (const void*)k_expm_coop<true>,
-                          (const void*)k_expm_coop_ff<0>, (const void*)k_expm_coop_ff<1>,
-                          (const void*)k_expm_coop_ff<2>, (const void*)k_expm_coop_ff<3>};
-  const void* kern = kerns[kind];
-  if (!blocks_per_sm[kind] &&
-      (r = cuda_check(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm[kind], kern, kMvThreads, 0))))
+  const int kst = 2 * kind + coef_stream(d);
+  const void* kerns[12] = {(const void*)k_expm_coop<false, false>,  (const void*)k_expm_coop<false, true>,
+                           (const void*)k_expm_coop<true, false>,   (const void*)k_expm_coop<true, true>,
+                           (const void*)k_expm_coop_ff<0, false>,   (const void*)k_expm_coop_ff<0, true>,
+                           (const void*)k_expm_coop_ff<1, false>,   (const void*)k_expm_coop_ff<1, true>,
+                           (const void*)k_expm_coop_ff<2, false>,   (const void*)k_expm_coop_ff<2, true>,
+                           (const void*)k_expm_coop_ff<3, false>,   (const void*)k_expm_coop_ff<3, true>};
+  const void* kern = kerns[kst];
+  if (!blocks_per_sm[kst] &&
+      (r = cuda_check(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm[kst], kern, kMvThreads, 0))))
     return r;
   // the batched float-float path takes a thread per output component
   const long items = mv_items(d.N, k, d.sms) * (kind == 2 ? 4 : 1);
   const int th = mv_threads(items, d.sms);
   const long want = (items + th - 1) / th;
   // co-resident: blocks of th <= 256 threads need no more than a 256-thread block
-  const int grid = (int)std::min<long>(want, (long)blocks_per_sm[kind] * d.sms);
+  const int grid = (int)std::min<long>(want, (long)blocks_per_sm[kst] * d.sms);
   MvArgs base;
   base.acc_prev = nullptr;
   base.c_prev = 0;
