@@ -49,3 +49,13 @@ def test_invalid_config_rejected(kw, text):
     assert rc == -1
     assert text in L.hymor_last_error(h).decode()
     L.hymor_ctx_destroy(h)
+
+
+@pytest.mark.parametrize("name", ["hymor_set_step_viscous", "hymor_set_cfl_screen", "hymor_set_expm_arith"])
+def test_switches_reject_bad_arguments(name):
+    """The arithmetic and schedule switches of the step and the propagator reject a null
+    context and modes other than 0 and 1 before touching a device."""
+    L = _lib.load()
+    fn = getattr(L, name)
+    for ctx, mode in ((None, 1), (None, 0), (None, 2)):
+        assert fn(ctx, mode) == -1
