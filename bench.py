@@ -560,7 +560,7 @@ def solve_numbers(which: str):
         # exp(L 50 dt) puts the whole stable spectrum within ~1 % of |mu| = 1
         out["eigen_4_modes_500_steps"] = solve_eigen(n_modes=4, substeps=500, maxit=60)
     if which == "eigen12":
-        # the benchmark spec's 12 eigenvalues and Krylov 60 over the ten times longer horizon, one-vector
+        # the sphere-cone solve's 12 eigenvalues and Krylov 60 over the ten times longer horizon, one-vector
         out["eigen_12_modes_500_steps"] = solve_eigen(n_modes=12, substeps=500, maxit=80, arms=("plain",))
     if which in ("all", "tg"):
         out["transient_growth"] = solve_tg()
