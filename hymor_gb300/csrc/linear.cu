@@ -446,13 +446,18 @@ template <bool ST>
 __device__ __forceinline__ void matvec_one_ff(const MvFf& a) {
   const long N = a.N;
   const long outs = 4 * N;
+  // 32-bit decomposition of the work item (the host keeps the items below 2^31)
+  const unsigned outs_u = (unsigned)outs, N_u = (unsigned)N, nchi_u = (unsigned)a.w.nchi;
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < outs * a.k; t += (long)gridDim.x * blockDim.x) {
-    const long vec = t / outs;
-    const long w = t - vec * outs;
-    const long m = w % N;
-    const int comp = (int)(w / N);
-    const int i = (int)(m % a.w.nchi), j = (int)(m / a.w.nchi);
-    const float2* xv = a.X + vec * a.ld;
+    const unsigned tu = (unsigned)t;
+    const unsigned vec = tu / outs_u;
+    const unsigned w = tu - vec * outs_u;
+    const unsigned comp_u = w / N_u;
+    const unsigned m = w - comp_u * N_u;
+    const int comp = (int)comp_u;
+    const unsigned j_u = m / nchi_u;
+    const int i = (int)(m - j_u * nchi_u), j = (int)j_u;
+    const float2* xv = a.X + (long)vec * a.ld;
     ff y{0.0f, 0.0f};
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
@@ -469,7 +474,7 @@ __device__ __forceinline__ void matvec_one_ff(const MvFf& a) {
       }
       y = ff_dot4(B, X, y);
     }
-    mvff_out(a, (int)vec, vec * a.ld + comp * N + m, y);
+    mvff_out(a, (int)vec, (long)vec * a.ld + comp * N + m, y);
   }
 }
 
@@ -482,10 +487,14 @@ __device__ __forceinline__ void matvec_multi_ff(const MvFf& a) {
   const long n4 = a.ld;
   const int chunks = (a.k + KV - 1) / KV;
   const long items = N * chunks;
+  const unsigned N_u = (unsigned)N, nchi_u = (unsigned)a.w.nchi;
   for (long w = blockIdx.x * (long)blockDim.x + threadIdx.x; w < items; w += (long)gridDim.x * blockDim.x) {
-    const long m = w % N;
-    const int i = (int)(m % a.w.nchi), j = (int)(m / a.w.nchi);
-    const int v0 = (int)(w / N) * KV;
+    const unsigned wu = (unsigned)w;
+    const unsigned ch = wu / N_u;
+    const unsigned m = wu - ch * N_u;
+    const unsigned j_u = m / nchi_u;
+    const int i = (int)(m - j_u * nchi_u), j = (int)j_u;
+    const int v0 = (int)ch * KV;
     const int nv = min(KV, a.k - v0);
     ff y[KV][4];
 #pragma unroll
@@ -537,13 +546,16 @@ __device__ __forceinline__ void matvec_comp_ff(const MvFf& a) {
   const long n4 = a.ld;
   const int chunks = (a.k + KV - 1) / KV;
   const long items = 4 * N * chunks;
+  const unsigned N_u = (unsigned)N, nchi_u = (unsigned)a.w.nchi;
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < items; t += (long)gridDim.x * blockDim.x) {
-    const long m = t % N;
-    const long r = t / N;
-    const int comp = (int)(r % 4);
-    const int v0 = (int)(r / 4) * KV;
+    const unsigned tu = (unsigned)t;
+    const unsigned r = tu / N_u;
+    const unsigned m = tu - r * N_u;
+    const int comp = (int)(r & 3u);
+    const int v0 = (int)(r >> 2) * KV;
     const int nv = min(KV, a.k - v0);
-    const int i = (int)(m % a.w.nchi), j = (int)(m / a.w.nchi);
+    const unsigned j_u = m / nchi_u;
+    const int i = (int)(m - j_u * nchi_u), j = (int)j_u;
     ff y[KV];
 #pragma unroll
     for (int v = 0; v < KV; ++v) y[v] = ff{0.0f, 0.0f};
@@ -1665,8 +1677,9 @@ int expm_cooperative(hymor_ctx* ctx, int k, double dt, int nsteps, int order, co
   double* t1 = c.buf + n;
   double* t2 = c.buf + 2 * n;
   double* vout = c.buf + 3 * n;
-  // float-float (degree >= 2): the blocks' float-float copy, split again after each write
-  const bool ffp = d.expm_ff && order >= 2;
+  // float-float (degree >= 2; its kernels decompose their work items in 32 bits), with the
+  // blocks' float-float copy split again after each write of the blocks
+  const bool ffp = d.expm_ff && order >= 2 && 4L * d.N * k < (1L << 31);
   if (ffp && (!d.coef_ff || d.coef_ff_version != d.coef_version)) {
     if (!d.coef_ff) {
       void* p = nullptr;
