@@ -640,13 +640,15 @@ def main():
     sol.ctx.check(L.hymor_bench_steps(h, args.warmup, FLUSH_BYTES, ctypes.byref(ms)))
     # the flux configuration picked by the library's autotuner on this case (state restored after)
     choice = np.zeros(3, dtype=np.int32)
-    tune_ms = (ctypes.c_float * 12)()
+    tune_ms = (ctypes.c_float * 18)()
     sol.ctx.check(L.hymor_autotune(h, 20, ip(choice), tune_ms))
-    autotune = {"flux_tile": f"31x{int(choice[0])}", "interior_spare_blocks_per_sm": int(choice[1]),
+    tiles = {8: "31x8", 16: "31x16", 4: "31x4+31x8"}  # 4: interior tiles 31x4, shock/boundary 31x8
+    autotune = {"flux_tile": tiles[int(choice[0])], "interior_spare_blocks_per_sm": int(choice[1]),
                 "halo": "TMA" if choice[2] else "thread loads",
-                "candidates_ms_per_step": {f"{'tma' if t else 'ld'}/31x{r}/spare{sp}":
-                                           round(tune_ms[6 * t + 3 * (r == 16) + sp], 4)
-                                           for t in (0, 1) for r in (8, 16) for sp in (0, 1, 2)}}
+                "candidates_ms_per_step": {f"{'tma' if t else 'ld'}/{tiles[r]}/spare{sp}":
+                                           round(tune_ms[9 * t + 3 * ri + sp], 4)
+                                           for t in (0, 1) for ri, r in enumerate((8, 16, 4))
+                                           for sp in (0, 1, 2)}}
     sol.ctx.check(L.hymor_bench_steps(h, 2, FLUSH_BYTES, ctypes.byref(ms)))
     # timed region: K steps, flux-kernel events on
     sol.ctx.check(L.hymor_profile_flux(h, 1, None, None))

@@ -727,8 +727,8 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
   d.step_ffv = 1;
   d.expm_ff = 1;
   d.cfl_screen = 1;
-  d.flux_rows = 8;
-  d.flux_spare = 1;
+  d.flux_rows = 4;  // the split tiling
+  d.flux_spare = 2;
   d.tma = make_flux_maps(d);
   ctx->tma_able = d.tma;
   for (int k = 0; k < hymor_ctx_s::kEv; ++k)
@@ -993,17 +993,17 @@ int hymor_autotune(hymor_ctx* ctx, int steps, int32_t* choice, float* ms_per_ste
   const bool stale = ctx->a_stale;
   const int rows0 = d.flux_rows, spare0 = d.flux_spare, tma0 = d.tma;
   int r = copy(true);
-  // candidates: halo by TMA or by thread loads x tile rows x spare block slots per SM of the
-  // interior grid (without TMA descriptors only the thread-load half)
-  const int rows_c[2] = {8, 16}, spare_c[3] = {0, 1, 2};
+  // candidates: halo by TMA or by thread loads x tile rows (8, 16, or the split 4/8) x spare
+  // block slots per SM of the interior grid (without TMA descriptors only the thread-load half)
+  const int rows_c[3] = {8, 16, 4}, spare_c[3] = {0, 1, 2};
   float best = 0;
   int bi = -1, c = 0;
-  for (int a = 0; a < 4 && !r; ++a)
+  for (int a = 0; a < 6 && !r; ++a)
     for (int b = 0; b < 3 && !r; ++b, ++c) {
       if (ms_per_step) ms_per_step[c] = 0;
-      if ((a >> 1) && !ctx->tma_able) continue;
-      d.tma = a >> 1;
-      d.flux_rows = rows_c[a & 1];
+      if (a >= 3 && !ctx->tma_able) continue;
+      d.tma = a >= 3;
+      d.flux_rows = rows_c[a % 3];
       d.flux_spare = spare_c[b];
       drop_step_graph(ctx);
       float ms = 0;
@@ -1031,8 +1031,8 @@ int hymor_autotune(hymor_ctx* ctx, int steps, int32_t* choice, float* ms_per_ste
     drop_step_graph(ctx);
     return r ? r : fail(ctx, HYMOR_ERR_CUDA, "autotune: no candidate ran");
   }
-  d.tma = bi / 6;
-  d.flux_rows = rows_c[(bi / 3) & 1];
+  d.tma = bi / 9;
+  d.flux_rows = rows_c[(bi / 3) % 3];
   d.flux_spare = spare_c[bi % 3];
   drop_step_graph(ctx);
   choice[0] = d.flux_rows;
@@ -1042,7 +1042,7 @@ int hymor_autotune(hymor_ctx* ctx, int steps, int32_t* choice, float* ms_per_ste
 }
 
 int hymor_set_flux_tiling(hymor_ctx* ctx, int rows, int spare, int tma) {
-  if (!ctx || (rows != 8 && rows != 16) || spare < 0 || spare > 4 || tma < 0 || tma > 1) return HYMOR_ERR_INVALID;
+  if (!ctx || (rows != 4 && rows != 8 && rows != 16) || spare < 0 || spare > 4 || tma < 0 || tma > 1) return HYMOR_ERR_INVALID;
   if (tma && !ctx->tma_able) return fail(ctx, HYMOR_ERR_INVALID, "no TMA descriptors for this grid (Nchi odd)");
   TRY(set_device(ctx));
   if (ctx->d.flux_rows != rows || ctx->d.flux_spare != spare || ctx->d.tma != tma) {

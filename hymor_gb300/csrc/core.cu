@@ -1077,14 +1077,17 @@ struct FluxArgs {
 // and stays below the shocked rows sc .. sc+2 of its columns, so its flux does not wait
 // for the shock/boundary kernels; 1 = the others; tiles wholly at or above the shocked
 // rows (zero flux under the NON_LINEAR_DYNAMICS mask, never read by the stage update)
-// are left out. lists: [count0, count1, class 0 tiles (ntiles), class 1 tiles (ntiles)].
+// are left out. lists: [count0, count1, class 0 tiles (cap0), class 1 tiles]. split: each
+// tile is listed as its two halves, tiles of the tiling with ty / 2 rows, in its class (a
+// half wholly above the shocked rows left out like a tile).
 __global__ void k_classify_tiles(const int* __restrict__ cell_idx, int* lists, int nchi, int neta, int tiles_x,
-                                 int ntiles, int shock, int mask, int ty) {
+                                 int ntiles, int shock, int mask, int ty, int split, int cap0) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntiles) return;
   const int i0 = (t % tiles_x) * TX, j0 = (t / tiles_x) * ty;
+  int sc = 0x7fffffff;
   if (mask) {
-    int sc = 0;
+    sc = 0;
     for (int c = i0; c < i0 + TX && c < nchi; ++c) sc = max(sc, cell_idx[c]);
     if (j0 + 1 >= sc) return;
   }
@@ -1096,7 +1099,16 @@ __global__ void k_classify_tiles(const int* __restrict__ cell_idx, int* lists, i
     inner = inner && (j0 + ty + 1 < scmin);
   }
   const int cls = inner ? 0 : 1;
-  lists[2 + cls * ntiles + atomicAdd(&lists[cls], 1)] = t;
+  int* list = lists + 2 + cls * cap0;
+  if (split) {
+    const int h = 2 * (t / tiles_x) * tiles_x + t % tiles_x;  // the lower half's index
+    const bool upper = j0 + ty / 2 + 1 < sc && j0 + ty / 2 < neta;
+    const int k = atomicAdd(&lists[cls], upper ? 2 : 1);
+    list[k] = h;
+    if (upper) list[k + 1] = h + tiles_x;
+  } else {
+    list[atomicAdd(&lists[cls], 1)] = t;
+  }
 }
 
 // One 31 x TYV-cell tile (bx, by) of the residual, TYV warps (one per tile row); every
@@ -2286,9 +2298,12 @@ void launch_shock_bc_flags(const DevCtx& d, bool on_S, bool copy_pts, bool do_sh
   launch_shock_bc_impl(d, on_S, copy_pts, false, 0, 0, a_mode, do_shock, do_bc, st);
 }
 
-// resident flux blocks per SM of each variant (index 16 TMA + 8 (16-row tiles) + 4 float-float +
-// 2 axisymmetric + Sutherland)
-int g_flux_blocks_per_sm[32];
+// resident flux blocks per SM of each variant (index flux_variant + 2 axisymmetric + Sutherland)
+int g_flux_blocks_per_sm[40];
+// 16 TMA + 8 (16-row tiles) + 4 float-float; the 4-row tiles (thread loads only) from 32
+constexpr int flux_variant(bool tma, int rows, bool ffv) {
+  return rows == TY / 2 ? 32 + ffv * 4 : tma * 16 + (rows == 16) * 8 + ffv * 4;
+}
 
 // a double as a float-float pair (high: nearest float, low: the nearest float to the rest)
 float2 host_ff(double x) {
@@ -2296,17 +2311,25 @@ float2 host_ff(double x) {
   return make_float2(h, (float)(x - (double)h));
 }
 
-int flux_rows(const DevCtx& d) { return d.flux_rows == 16 ? 16 : TY; }
+// flux_rows 4 is the split tiling: the tiles are classified at 8 rows and run as 31 x 4 halves
+// (halo by thread loads), so that a block of the shock/boundary class fits beside the
+// persistent interior grid and its tiles spread over twice the blocks; the halo re-read is
+// 6/4 of the cells instead of 10/8.
+bool flux_split(const DevCtx& d) { return d.flux_rows == TY / 2; }
+int flux_rows(const DevCtx& d) { return d.flux_rows == 16 ? 16 : TY; }  // of the classified tiles
 int flux_tiles_x(const DevCtx& d) { return (d.nchi + TX - 1) / TX; }
 int flux_tiles(const DevCtx& d) { return flux_tiles_x(d) * ((d.neta + flux_rows(d) - 1) / flux_rows(d)); }
-int flux_tiles_max(const DevCtx& d) { return flux_tiles_x(d) * ((d.neta + TY - 1) / TY); }
+int flux_tiles_max(const DevCtx& d) { return flux_tiles_x(d) * ((d.neta + TY / 2 - 1) / (TY / 2)); }
+// capacity of the class-0 list (the class-1 list follows it; each holds at most the tiles of
+// the tiling it lists)
+int flux_list0_cap(const DevCtx& d) { return flux_split(d) ? flux_tiles_max(d) : flux_tiles(d); }
 
 void launch_classify_tiles(const DevCtx& d, cudaStream_t st) {
   const int nt = flux_tiles(d);
   cudaMemsetAsync(d.tiles, 0, 2 * sizeof(int), st);
   k_classify_tiles<<<(nt + 127) / 128, 128, 0, st>>>(d.cell_idx, d.tiles, d.nchi, d.neta, flux_tiles_x(d), nt,
                                                    d.cfg.shock_enabled, d.cfg.shock_enabled && d.cfg.shock_feedback,
-                                                   flux_rows(d));
+                                                   flux_rows(d), flux_split(d), flux_list0_cap(d));
 }
 
 template <bool AXI, bool SUTH, bool FFV, int TYV, bool TMA>
@@ -2314,8 +2337,9 @@ void flux_launch_rows(const FluxArgs& a, const FluxMaps& tm, int tile_class, dim
                       cudaStream_t st) {
   const size_t smem = flux_smem<AXI, SUTH, TYV, TMA>();
   if (tile_class == 1 && a.list) {
-    // the shock/boundary class: a persistent grid of one block per SM over its few tiles
-    k_flux<AXI, SUTH, TYV, FFV, TMA><<<d.sms, 32 * TYV, smem, st>>>(a, tm);
+    // the shock/boundary class: a persistent grid of one block per SM over its few tiles (two
+    // of the half-height tiles)
+    k_flux<AXI, SUTH, TYV, FFV, TMA><<<d.sms * (TYV == TY / 2 ? 2 : 1), 32 * TYV, smem, st>>>(a, tm);
   } else {
     k_flux<AXI, SUTH, TYV, FFV, TMA><<<grid, 32 * TYV, smem, st>>>(a, tm);
   }
@@ -2323,9 +2347,11 @@ void flux_launch_rows(const FluxArgs& a, const FluxMaps& tm, int tile_class, dim
 
 template <bool AXI, bool SUTH, bool FFV>
 void flux_launch(const FluxArgs& a, const FluxMaps& tm, int tile_class, dim3 grid, const DevCtx& d,
-                 cudaStream_t st) {
-  const bool r16 = flux_rows(d) == 16;
-  if (d.tma) {
+                 cudaStream_t st, int rows, bool tma) {
+  const bool r16 = rows == 16;
+  if (rows == TY / 2) {
+    flux_launch_rows<AXI, SUTH, FFV, TY / 2, false>(a, tm, tile_class, grid, d, st);
+  } else if (tma) {
     if (r16) flux_launch_rows<AXI, SUTH, FFV, 16, true>(a, tm, tile_class, grid, d, st);
     else flux_launch_rows<AXI, SUTH, FFV, TY, true>(a, tm, tile_class, grid, d, st);
   } else {
@@ -2349,9 +2375,13 @@ void launch_flux_class(const DevCtx& d, bool on_S, double* const out[4], int til
   a.cell_idx = d.cell_idx;
   a.m = d.m;
   a.err = d.err;
+  // the split tiling's classes: half-height tiles, halo by thread loads
+  const bool half = flux_split(d) && tile_class >= 0 && d.tiles;
+  const int rows = half ? TY / 2 : flux_rows(d);
+  const bool tma = d.tma && !half;
   FluxMaps tm;
-  if (d.tma) {
-    const int ri = flux_rows(d) == 16;
+  if (tma) {
+    const int ri = rows == 16;
     const CUtensorMap* q4 = on_S ? d.tmS[ri] : d.tmY[ri];
     for (int v = 0; v < 4; ++v) tm.m[v] = q4[v];
     tm.m[4] = d.tmP[ri];
@@ -2369,28 +2399,26 @@ void launch_flux_class(const DevCtx& d, bool on_S, double* const out[4], int til
   a.neta = d.neta;
   a.shock = c.shock_enabled;
   a.mask = c.shock_enabled && c.shock_feedback;
-  const int rows = flux_rows(d);
   dim3 grid((d.nchi + TX - 1) / TX, (d.neta + rows - 1) / rows);
   const bool axi = c.axisymmetric, suth = c.viscosity_model == 1;
   if (tile_class >= 0 && d.tiles) {
     // the compact list of the class over a persistent grid (the interior tiles at full
     // occupancy)
-    const int nt = flux_tiles(d);
     a.count = d.tiles + tile_class;
-    a.list = d.tiles + 2 + tile_class * nt;
-    const int b = g_flux_blocks_per_sm[(d.tma ? 16 : 0) + (rows == 16) * 8 + ffv * 4 + axi * 2 + suth];
+    a.list = d.tiles + 2 + tile_class * flux_list0_cap(d);
+    const int b = g_flux_blocks_per_sm[flux_variant(tma, rows, ffv) + axi * 2 + suth];
     grid = dim3((b > spare + 1 ? b - spare : 1) * d.sms, 1);
   }
   if (ffv) {
-    if (!axi && !suth) flux_launch<false, false, true>(a, tm, tile_class, grid, d, st);
-    else if (axi && !suth) flux_launch<true, false, true>(a, tm, tile_class, grid, d, st);
-    else if (!axi && suth) flux_launch<false, true, true>(a, tm, tile_class, grid, d, st);
-    else flux_launch<true, true, true>(a, tm, tile_class, grid, d, st);
+    if (!axi && !suth) flux_launch<false, false, true>(a, tm, tile_class, grid, d, st, rows, tma);
+    else if (axi && !suth) flux_launch<true, false, true>(a, tm, tile_class, grid, d, st, rows, tma);
+    else if (!axi && suth) flux_launch<false, true, true>(a, tm, tile_class, grid, d, st, rows, tma);
+    else flux_launch<true, true, true>(a, tm, tile_class, grid, d, st, rows, tma);
   } else {
-    if (!axi && !suth) flux_launch<false, false, false>(a, tm, tile_class, grid, d, st);
-    else if (axi && !suth) flux_launch<true, false, false>(a, tm, tile_class, grid, d, st);
-    else if (!axi && suth) flux_launch<false, true, false>(a, tm, tile_class, grid, d, st);
-    else flux_launch<true, true, false>(a, tm, tile_class, grid, d, st);
+    if (!axi && !suth) flux_launch<false, false, false>(a, tm, tile_class, grid, d, st, rows, tma);
+    else if (axi && !suth) flux_launch<true, false, false>(a, tm, tile_class, grid, d, st, rows, tma);
+    else if (!axi && suth) flux_launch<false, true, false>(a, tm, tile_class, grid, d, st, rows, tma);
+    else flux_launch<true, true, false>(a, tm, tile_class, grid, d, st, rows, tma);
   }
 }
 
@@ -2405,7 +2433,7 @@ void flux_setup_variant() {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, 32 * TYV, smem) != cudaSuccess || b < 1) b = 1;
     return b;
   };
-  const int base = (TMA ? 16 : 0) + (TYV == 16) * 8 + FFV * 4;
+  const int base = flux_variant(TMA, TYV, FFV);
   auto one = [&](auto kern, size_t smem, int idx) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFluxMaxSmem);
     g_flux_blocks_per_sm[base + idx] = occ(kern, smem);
@@ -2425,6 +2453,8 @@ void flux_kernel_setup() {
   flux_setup_variant<true, TY, true>();
   flux_setup_variant<false, 16, true>();
   flux_setup_variant<true, 16, true>();
+  flux_setup_variant<false, TY / 2, false>();
+  flux_setup_variant<true, TY / 2, false>();
   cudaFuncSetAttribute(k_spline_fit, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)sizeof(float) * kSplineArrays * spline_stride(4096));
 }

@@ -72,8 +72,9 @@ struct DevCtx {
   int step_ffv;
   // the step's CFL maxima through the FP32 screen (1, the default) or in FP64 over every cell
   int cfl_screen;
-  // flux tiling of the RK step (hymor_autotune): tile rows (8 or 16) and the block slots per
-  // SM the persistent interior-tile grid leaves to the side streams
+  // flux tiling of the RK step (hymor_autotune): tile rows (8 or 16; 4 = the split tiling, the
+  // tiles classified at 8 rows and run as 31 x 4 halves by thread loads) and the block slots
+  // per SM the persistent interior-tile grid leaves to the side streams
   int flux_rows, flux_spare;
   // TMA descriptors of the ghosted planes for the flux halo, per tile height (8, 16 rows):
   // S and Y conserved planes, p, T. tma: 1 when they are used (they exist when (Nchi + 2) * 8

@@ -392,8 +392,8 @@ def test_shock_range_error_is_reported(require_gpu):
 
 
 def test_flux_tilings_bit_identical(require_gpu):
-    """Every flux configuration (halo by TMA or thread loads, tiles of 31 x 8 or 31 x 16 cells,
-    0..2 spare block slots) gives bit-identical RK steps and residuals: each face flux has the
+    """Every flux configuration (halo by TMA or thread loads, tiles of 31 x 8 or 31 x 16 cells or
+    the interior in 31 x 4 halves, 0..2 spare block slots) gives bit-identical RK steps and residuals: each face flux has the
     same arithmetic whichever tile computes it, from the same halo values."""
     cfg = C.cylinder_config(100, 80)
     cs = C.initial_state(cfg, seed=1, noise=1e-6)
@@ -401,7 +401,7 @@ def test_flux_tilings_bit_identical(require_gpu):
     S.ADVECT_FLOW(ref, 5)
     q_ref = ref.get_state()
     f_ref = S.PDE(ref)  # PDE mutates its solution: evaluate each solution once
-    for rows, spare, tma in ((16, 0, 1), (16, 2, 0), (8, 0, 0), (8, 1, 1)):
+    for rows, spare, tma in ((16, 0, 1), (16, 2, 0), (8, 0, 0), (8, 1, 1), (4, 0, 0), (4, 2, 1)):
         sol = S.Solution(cs)
         sol.ctx.check(sol.ctx.L.hymor_set_flux_tiling(sol.ctx.h, rows, spare, tma))
         S.ADVECT_FLOW(sol, 5)
@@ -425,9 +425,9 @@ def test_autotune_restores_state_and_picks_a_tiling(require_gpu):
     S.ADVECT_FLOW(b, 3)
     before = a.get_state()
     choice = np.zeros(3, dtype=np.int32)
-    ms = (ctypes.c_float * 12)()
+    ms = (ctypes.c_float * 18)()
     a.ctx.check(a.ctx.L.hymor_autotune(a.ctx.h, 5, choice.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), ms))
-    assert choice[0] in (8, 16) and choice[1] in (0, 1, 2) and choice[2] in (0, 1)
+    assert choice[0] in (4, 8, 16) and choice[1] in (0, 1, 2) and choice[2] in (0, 1)
     assert all(m > 0 for m in ms)  # 200 x 100: Nchi even, the TMA candidates run too
     after = a.get_state()
     for k in ("q", "pts_x", "pts_y", "pts_chi", "pts_eta", "cell_idx"):
