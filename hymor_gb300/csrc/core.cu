@@ -854,27 +854,98 @@ __device__ __forceinline__ void move_shock_point(const hymor_config& c, const Sh
   }
 }
 
-__global__ void __launch_bounds__(128) k_shock_columns(ColArgs A) {
+// k_shock_columns: 32 columns per block, the work of a column split over three warps in two
+// phases (a warp's FP64 instruction takes the sub-partition's FP64 pipe ~70 cycles whatever
+// its active lanes, so the serial chain of one column shortens only when other warps take
+// part of it):
+//   phase 1: warp 0 evaluates the x spline, warp 1 the y spline, warp 2 loads the shocked
+//            column's mesh points and states and forms the geometry and the slopes;
+//   phase 2: warp 0 maps the point to element space, warp 1 forms beta, the jump, the
+//            extrapolation and the shock speed.
+// Each quantity has the arithmetic of the one-thread-per-column form.
+constexpr int kColCols = 32;
+constexpr int kColThreads = 3 * kColCols;
+
+struct ColShared {
+  double xv[kColCols], xd[kColCols], yv[kColCols], yd[kColCols];
+  // mesh points of rows sc, sc - 1 and their differences, reciprocal distances
+  double x0[kColCols], y0[kColCols], x1[kColCols], y1[kColCols];
+  double dx01[kColCols], dy01[kColCols], dx12[kColCols], dy12[kColCols], i01[kColCols], i12[kColCols];
+  // the states of rows sc - 1 and sc - 2 (rho, rho u, rho v, rho E, p; p of sc - 2 as the
+  // extrapolation reads it) and the slopes of p, rho, rho u, rho v, rho E
+  double q1[5][kColCols], q2[5][kColCols], sl[5][kColCols];
+  int sc[kColCols];
+};
+
+__global__ void __launch_bounds__(kColThreads) k_shock_columns(ColArgs A) {
+  __shared__ ColShared sh;
   const hymor_config& c = A.cfg;
   const int nchi = c.nchi, neta = c.neta;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nchi) return;
+  const int lane = threadIdx.x % kColCols, w = threadIdx.x / kColCols;
+  const int i = blockIdx.x * kColCols + lane;
+  const bool act = i < nchi;
   const double* xs = A.ws;
   const double* cxs = A.ws + 3 * nchi;
   const double* cys = A.ws + 4 * nchi;
   const double* gxs = A.ws + 5 * nchi;
   const double* gys = A.ws + 6 * nchi;
   const double* ih = A.ws + 15 * nchi;
+  const int I = i + 1;
+  // phase 1. LEAST_SQUARES_SHOCK_POINTS.jl:60-70, COMPUTE_BETA.jl:37-50: the fitted spline
+  // and its slope at the column's abscissa
+  if (act && w < 2) {
+    double v, dv;
+    spline_at(nchi, xs, w == 0 ? gxs : gys, w == 0 ? cxs : cys, ih, A.m.chi1[i], i - 1, v, dv);
+    (w == 0 ? sh.xv : sh.yv)[lane] = v;
+    (w == 0 ? sh.xd : sh.yd)[lane] = dv;
+  } else if (act) {
+    // UPDATE_SHOCK_JUMP_PROPERTIES.jl:324-522 and EXTRAPOLATE_CELLS_SHOCK.jl:39-176: the
+    // shocked cell's column below the shock
+    const int sc = A.cell_idx[i];
+    sh.sc[lane] = sc;
+    if (sc >= 2 && sc <= neta - 1) {
+      const double x0 = A.m.x_ext[gidx(I, sc, nchi)], y0 = A.m.y_ext[gidx(I, sc, nchi)];
+      const double x1 = A.m.x_ext[gidx(I, sc - 1, nchi)], y1 = A.m.y_ext[gidx(I, sc - 1, nchi)];
+      const double x2 = A.m.x_ext[gidx(I, sc - 2, nchi)], y2 = A.m.y_ext[gidx(I, sc - 2, nchi)];
+      const double dx01 = x0 - x1, dy01 = y0 - y1, dx12 = x1 - x2, dy12 = y1 - y2;
+      const double i12 = frsqrt(dx12 * dx12 + dy12 * dy12);  // 1 / dist12
+      sh.x0[lane] = x0; sh.y0[lane] = y0; sh.x1[lane] = x1; sh.y1[lane] = y1;
+      sh.dx01[lane] = dx01; sh.dy01[lane] = dy01; sh.dx12[lane] = dx12; sh.dy12[lane] = dy12;
+      sh.i01[lane] = frsqrt(dx01 * dx01 + dy01 * dy01);  // 1 / dist01
+      sh.i12[lane] = i12;
+      const int g1 = gidx(I, sc - 1, nchi), g2 = gidx(I, sc - 2, nchi);
+      const double p_1 = A.p[g1];
+      double p_2 = A.p[g2];
+      if (sc - 2 == 0 && c.bc_eta0 == HYMOR_BC_NO_SLIP_ISOTHERMAL)
+        p_2 = 2 * A.p[gidx(I, 1, nchi)] - A.p[gidx(I, 2, nchi)];  // UPDATE_THERMODYNAMIC_PROPERTIES.jl:28-31
+      const double* arr[4] = {A.tgt.rho, A.tgt.ru, A.tgt.rv, A.tgt.rE};
+      sh.q1[4][lane] = p_1;
+      sh.q2[4][lane] = p_2;
+      sh.sl[0][lane] = (p_1 - p_2) * i12;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const double a1 = arr[v][g1], a2 = arr[v][g2];
+        sh.q1[v][lane] = a1;
+        sh.q2[v][lane] = a2;
+        sh.sl[v + 1][lane] = (a1 - a2) * i12;
+      }
+    }
+  }
+  __syncthreads();
+  if (!act || w == 2) return;
+  const double xv = sh.xv[lane], yv = sh.yv[lane];
+  if (w == 0) {
+    double ch, et;
+    element_space(c, xv, yv, ch, et);
+    A.pts.chi[i] = ch;
+    A.pts.eta[i] = et;
+    return;
+  }
+  // phase 2, warp 1
+  const double xd = sh.xd[lane], yd = sh.yd[lane];
   const double t = A.scal[kT], dt = A.scal[kDt];
   Cons q = A.tgt;
-  // LEAST_SQUARES_SHOCK_POINTS.jl:60-70, COMPUTE_BETA.jl:37-50
-  const double tc = A.m.chi1[i];
-  double xv, xd, yv, yd;
-  spline_at(nchi, xs, gxs, cxs, ih, tc, i - 1, xv, xd);
-  spline_at(nchi, xs, gys, cys, ih, tc, i - 1, yv, yd);
-  double ch, et;
-  element_space(c, xv, yv, ch, et);
-  A.pts.x[i] = xv; A.pts.y[i] = yv; A.pts.chi[i] = ch; A.pts.eta[i] = et;
+  A.pts.x[i] = xv; A.pts.y[i] = yv;
   double p_inf = A.p_inf, u_inf = A.u_inf, v_inf = A.v_inf, rho_inf = A.rho_inf;
   const bool local_up = A.disturbed || A.up_cols || (c.axisymmetric && i == 0);
   if (local_up) upstream(c, t, xv, yv, i == 0, p_inf, u_inf, v_inf, rho_inf, A.up_cols, i);
@@ -892,30 +963,17 @@ __global__ void __launch_bounds__(128) k_shock_columns(ColArgs A) {
     A.beta[i] = sb;
     A.beta[nchi + i] = cb;
   }
-  // UPDATE_SHOCK_JUMP_PROPERTIES.jl:324-522 and EXTRAPOLATE_CELLS_SHOCK.jl:39-176
-  const int sc = A.cell_idx[i];
+  const int sc = sh.sc[lane];
   if (sc < 2 || sc > neta - 1) {
     atomicOr(&A.err[kErrFlags], kBitShockRange);
     return;
   }
-  const int I = i + 1;
-  const double x0 = A.m.x_ext[gidx(I, sc, nchi)], y0 = A.m.y_ext[gidx(I, sc, nchi)];
-  const double x1 = A.m.x_ext[gidx(I, sc - 1, nchi)], y1 = A.m.y_ext[gidx(I, sc - 1, nchi)];
-  const double x2 = A.m.x_ext[gidx(I, sc - 2, nchi)], y2 = A.m.y_ext[gidx(I, sc - 2, nchi)];
-  const double i01 = frsqrt((x0 - x1) * (x0 - x1) + (y0 - y1) * (y0 - y1));  // 1 / dist01
-  const double i12 = frsqrt((x1 - x2) * (x1 - x2) + (y1 - y2) * (y1 - y2));  // 1 / dist12
-  const double dist1s = ((xv - x1) * (x1 - x2) + (yv - y1) * (y1 - y2)) * i12;
-  const double dist0s = ((xv - x0) * (x0 - x1) + (yv - y0) * (y0 - y1)) * i01;
-  const int g0 = gidx(I, sc, nchi), g1 = gidx(I, sc - 1, nchi), g2 = gidx(I, sc - 2, nchi);
-  const double p_1 = A.p[g1];
-  double p_2 = A.p[g2];
-  if (sc - 2 == 0 && c.bc_eta0 == HYMOR_BC_NO_SLIP_ISOTHERMAL)
-    p_2 = 2 * A.p[gidx(I, 1, nchi)] - A.p[gidx(I, 2, nchi)];  // UPDATE_THERMODYNAMIC_PROPERTIES.jl:28-31
-  const double slope_p = (p_1 - p_2) * i12;
-  const double slope_rho = (q.rho[g1] - q.rho[g2]) * i12;
-  const double slope_ru = (q.ru[g1] - q.ru[g2]) * i12;
-  const double slope_rv = (q.rv[g1] - q.rv[g2]) * i12;
-  const double slope_rE = (q.rE[g1] - q.rE[g2]) * i12;
+  const double i01 = sh.i01[lane], i12 = sh.i12[lane];
+  const double dist1s = ((xv - sh.x1[lane]) * sh.dx12[lane] + (yv - sh.y1[lane]) * sh.dy12[lane]) * i12;
+  const double dist0s = ((xv - sh.x0[lane]) * sh.dx01[lane] + (yv - sh.y0[lane]) * sh.dy01[lane]) * i01;
+  const int g0 = gidx(I, sc, nchi);
+  const double p_1 = sh.q1[4][lane];
+  const double slope_p = sh.sl[0][lane];
   const double p_s = slope_p * dist1s + p_1;
   const double yr = p_s * frcp(p_inf);
   if (yr < 1) atomicAdd(&A.err[kRhWarn], 1u);
@@ -955,23 +1013,39 @@ __global__ void __launch_bounds__(128) k_shock_columns(ColArgs A) {
   const double ru_s = rho_s * (vn_s * sb + vt_s * cb);
   const double rv_s = rho_s * (-vn_s * cb + vt_s * sb);
   const double rE_s = e_s * rho_s + (ru_s * ru_s + rv_s * rv_s) * (0.5 * irho_s);
-  q.rho[g0] = -slope_rho * dist0s + rho_s;
-  q.ru[g0] = -slope_ru * dist0s + ru_s;
-  q.rv[g0] = -slope_rv * dist0s + rv_s;
-  q.rE[g0] = -slope_rE * dist0s + rE_s;
-  A.p[g0] = -slope_p * dist0s + p_s;
-  const int i1 = gidx(I, sc + 1, nchi), i2 = gidx(I, sc + 2, nchi);
-  const int im1 = g1, im2 = g2;
+  // the shocked cell's state (rho, rho u, rho v, rho E, p) and its extrapolation to sc + 1, sc + 2
+  double v0[5];
+  v0[0] = -sh.sl[1][lane] * dist0s + rho_s;
+  v0[1] = -sh.sl[2][lane] * dist0s + ru_s;
+  v0[2] = -sh.sl[3][lane] * dist0s + rv_s;
+  v0[3] = -sh.sl[4][lane] * dist0s + rE_s;
+  v0[4] = -slope_p * dist0s + p_s;
   double* arr[5] = {q.rho, q.ru, q.rv, q.rE, A.p};
+  const int i1 = gidx(I, sc + 1, nchi), i2 = gidx(I, sc + 2, nchi);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) arr[v][g0] = v0[v];
   if (c.shock_interp == 1) {
-    for (int v = 0; v < 5; ++v) { arr[v][i1] = arr[v][g0]; arr[v][i2] = arr[v][g0]; }
+#pragma unroll
+    for (int v = 0; v < 5; ++v) { arr[v][i1] = v0[v]; arr[v][i2] = v0[v]; }
   } else if (c.shock_interp == 2) {
-    for (int v = 0; v < 5; ++v) arr[v][i1] = 2 * arr[v][g0] - arr[v][im1];
-    for (int v = 0; v < 4; ++v) arr[v][i2] = 2 * arr[v][i1] - arr[v][g0];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const double e1 = 2 * v0[v] - sh.q1[v][lane];
+      arr[v][i1] = e1;
+      if (v < 4) arr[v][i2] = 2 * e1 - v0[v];
+    }
   } else {
-    for (int v = 0; v < 4; ++v) arr[v][i1] = 3 * arr[v][g0] - 3 * arr[v][im1] + arr[v][im2];
-    A.p[i1] = 3 * A.p[g0] - 3 * A.p[im1] + p_2;
-    for (int v = 0; v < 4; ++v) arr[v][i2] = 3 * arr[v][i1] - 3 * arr[v][g0] + arr[v][im1];
+    // 3 a - 3 b + c with each operation rounded (no fused multiply-add), the reference's
+    // association
+    auto cubic = [](double a, double b, double c) {
+      return __dadd_rn(__dsub_rn(__dmul_rn(3.0, a), __dmul_rn(3.0, b)), c);
+    };
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const double e1 = cubic(v0[v], sh.q1[v][lane], sh.q2[v][lane]);
+      arr[v][i1] = e1;
+      if (v < 4) arr[v][i2] = cubic(e1, v0[v], sh.q1[v][lane]);
+    }
   }
   // MOVE_SHOCK; the symmetry copy pts_x[1] -> pts_x[0] runs in k_bc_edges
   if (A.move) move_shock_point(c, A.pS, A.pts, A.on_S, A.cY, A.cS, dt, spx, spy, i);
@@ -2235,7 +2309,7 @@ void launch_columns_bc(const DevCtx& d, bool on_S, bool move, double cY, double 
     ca.gp1_gm1 = (c.gamma + 1) / (c.gamma - 1);
     ca.igm1 = 1.0 / (c.gamma - 1);
     ca.two_igm1 = 2 / (c.gamma - 1);
-    k_shock_columns<<<(d.nchi + 127) / 128, 128, 0, st>>>(ca);
+    k_shock_columns<<<(d.nchi + kColCols - 1) / kColCols, kColThreads, 0, st>>>(ca);
   }
   const bool fix = shock && move && c.bc_chi0 == HYMOR_BC_SYMMETRY;
   if (do_bc || fix) {
