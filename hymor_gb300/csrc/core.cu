@@ -1617,19 +1617,37 @@ size_t flux_smem() {
 // ---------------------------------------------------------------------------
 // UPDATE_FLOW_CELLS on S: DETECT_CELLS_SHOCKED (DETECT_CELLS_SHOCKED.jl:50-65),
 // UPDATE_FIELD_UPSTREAM (UPDATE_FIELD_UPSTREAM.jl:93-109), EXTRAPOLATE_CELLS_SHOCK.
-__device__ void extrapolate_column(const hymor_config& c, Cons q, int i, int sc) {
+// x as a float with its mantissa truncated to 23 bits, from the bit pattern; zero below the
+// float normal range; sets bad beyond it (and for infinities and NaN).
+__device__ __forceinline__ float trunc_float(double x, bool& bad) {
+  const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
+  const unsigned e = (hw >> 20) & 0x7ffu;
+  bad |= e >= 1151u;
+  const unsigned fb = (hw & 0x80000000u) | ((e - 896u) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29);
+  return e > 896u ? __uint_as_float(fb) : 0.0f;
+}
+
+// EXTRAPOLATE_CELLS_SHOCK above the shocked cell sc of column i: rows sc + 1, sc + 2 of
+// variable v (the 3rd-order form with each operation rounded, the reference's association)
+__device__ void extrapolate_column(const hymor_config& c, Cons q, int i, int sc, int v) {
   const int nchi = c.nchi, I = i + 1;
   const int g0 = gidx(I, sc, nchi), i1 = gidx(I, sc + 1, nchi), i2 = gidx(I, sc + 2, nchi);
   const int im1 = gidx(I, sc - 1, nchi), im2 = gidx(I, sc - 2, nchi);
-  double* arr[4] = {q.rho, q.ru, q.rv, q.rE};
+  double* a = v == 0 ? q.rho : (v == 1 ? q.ru : (v == 2 ? q.rv : q.rE));
   if (c.shock_interp == 1) {
-    for (int v = 0; v < 4; ++v) { arr[v][i1] = arr[v][g0]; arr[v][i2] = arr[v][g0]; }
+    a[i1] = a[g0];
+    a[i2] = a[g0];
   } else if (c.shock_interp == 2) {
-    for (int v = 0; v < 4; ++v) arr[v][i1] = 2 * arr[v][g0] - arr[v][im1];
-    for (int v = 0; v < 4; ++v) arr[v][i2] = 2 * arr[v][i1] - arr[v][g0];
+    const double e1 = 2 * a[g0] - a[im1];
+    a[i1] = e1;
+    a[i2] = 2 * e1 - a[g0];
   } else {
-    for (int v = 0; v < 4; ++v) arr[v][i1] = 3 * arr[v][g0] - 3 * arr[v][im1] + arr[v][im2];
-    for (int v = 0; v < 4; ++v) arr[v][i2] = 3 * arr[v][i1] - 3 * arr[v][g0] + arr[v][im1];
+    auto cubic = [](double x, double y, double z) {
+      return __dadd_rn(__dsub_rn(__dmul_rn(3.0, x), __dmul_rn(3.0, y)), z);
+    };
+    const double e1 = cubic(a[g0], a[im1], a[im2]);
+    a[i1] = e1;
+    a[i2] = cubic(e1, a[g0], a[im1]);
   }
 }
 
@@ -1643,28 +1661,74 @@ struct FlowArgs {
   unsigned* err;
 };
 
-__global__ void __launch_bounds__(256) k_flow_cells(FlowArgs A) {
+// The nearest cell centre of a column is found by an FP32 screen: every row's squared
+// distance in FP32 from the truncated coordinates, with a bound E on its error against the
+// exact value, and the FP64 distance (rounded like the reference's unfused dx^2 + dy^2) only
+// for the rows whose interval [d - E, d + E] reaches below the smallest d + E. Every row
+// attaining the FP64 minimum is among them, so the nearest row and its ties are those of the
+// full FP64 scan. Rows whose coordinates are not finite floats are always evaluated in FP64.
+struct NearScreen {
+  float px, py;
+  bool bad;
+};
+
+// lower (lo) and upper (hi) bounds of the squared distance of the row's centre (x, y)
+__device__ __forceinline__ void near_bounds(const NearScreen& s, double x, double y, float& lo, float& hi) {
+  bool bad = s.bad;
+  const float xf = trunc_float(x, bad), yf = trunc_float(y, bad);
+  const float dx = s.px - xf, dy = s.py - yf;
+  const float d = dx * dx + dy * dy;
+  // |dx - (X - C)| <= 2^-23 (|X| + |C|) + 2^-24 |x - c| (truncation and the subtraction),
+  // taken twice over, plus the float normal range's floor
+  const float ex = 0x1p-22f * (fabsf(s.px) + fabsf(xf)) + 0x1p-23f * fabsf(dx) + 0x1p-125f;
+  const float ey = 0x1p-22f * (fabsf(s.py) + fabsf(yf)) + 0x1p-23f * fabsf(dy) + 0x1p-125f;
+  const float e = 2.0f * ((2.0f * fabsf(dx) + ex) * ex + (2.0f * fabsf(dy) + ey) * ey + 0x1p-21f * d) + 0x1p-120f;
+  lo = d - e;
+  hi = d + e;
+  if (bad || !(hi <= 3.0e38f)) { lo = 0.0f; hi = __int_as_float(0x7f800000); }  // always evaluated
+}
+
+// one warp per column (two per block, so that the columns spread over every SM)
+__global__ void __launch_bounds__(64) k_flow_cells(FlowArgs A) {
   const hymor_config& c = A.cfg;
   const int nchi = c.nchi, neta = c.neta, NJ = neta + 2;
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (i >= nchi) return;
   const double px = A.pS.x[i], py = A.pS.y[i];
   // nearest cell centre along the column; ties go to the smallest row, like the
-  // reference's sequential scan with a strict comparison
-  // (squared distance rounded like the reference's unfused dx^2 + dy^2, so that the
-  // nearest row is the same one; the transposed centres make the loads coalesced)
-  double best = INFINITY;
-  int bj = 0x7fffffff;
+  // reference's sequential scan with a strict comparison (the transposed centres make the
+  // loads coalesced)
   const double* xc = A.m.xt + (long)(i + 1) * NJ;
   const double* yc = A.m.yt + (long)(i + 1) * NJ;
+  NearScreen scr;
+  scr.bad = false;
+  scr.px = trunc_float(px, scr.bad);
+  scr.py = trunc_float(py, scr.bad);
+  float top = __int_as_float(0x7f800000);
   for (int j = 1 + lane; j <= neta; j += 32) {
-    const double dx = px - xc[j], dy = py - yc[j];
-    const double d = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
-    if (d < best) { best = d; bj = j; }
+    float lo, hi;
+    near_bounds(scr, xc[j], yc[j], lo, hi);
+    top = fminf(top, hi);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) top = fminf(top, __shfl_xor_sync(0xffffffffu, top, o));
+  // the FP64 distances of the candidates; non-negative doubles order as their bit patterns
+  unsigned long long best = 0x7ff0000000000000ull;  // +inf
+  int bj = 0x7fffffff;
+  for (int j = 1 + lane; j <= neta; j += 32) {
+    const double x = xc[j], y = yc[j];
+    float lo, hi;
+    near_bounds(scr, x, y, lo, hi);
+    if (lo <= top) {
+      const double dx = px - x, dy = py - y;
+      const double d = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+      const unsigned long long db = (unsigned long long)__double_as_longlong(d);
+      if (db < best) { best = db; bj = j; }  // NaN (above +inf) never wins, like d < best
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+    const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, o);
     const int oj = __shfl_xor_sync(0xffffffffu, bj, o);
     if (ob < best || (ob == best && oj < bj)) { best = ob; bj = oj; }
   }
@@ -1693,7 +1757,7 @@ __global__ void __launch_bounds__(256) k_flow_cells(FlowArgs A) {
     }
   }
   __syncwarp();
-  if (lane == 0) extrapolate_column(c, A.S, i, bj);
+  if (lane < 4) extrapolate_column(c, A.S, i, bj, lane);
 }
 
 // Sound speed of S, max |a| over every ghosted cell (CFL_TIMESTEP.jl:80).
@@ -1906,15 +1970,6 @@ __global__ void k_cfl_final(double* scal, double CFL, double max_dt) {
 // forms dt, and resets the FP32 maximum and its block counter for the next step.
 constexpr float kScreenKeep = 1.0f - 1.0f / 256;
 
-// x as a float with its mantissa truncated to 23 bits, from the bit pattern; zero below the
-// float normal range; sets bad beyond it (and for infinities and NaN).
-__device__ __forceinline__ float trunc_float(double x, bool& bad) {
-  const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
-  const unsigned e = (hw >> 20) & 0x7ffu;
-  bad |= e >= 1151u;
-  const unsigned fb = (hw & 0x80000000u) | ((e - 896u) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29);
-  return e > 896u ? __uint_as_float(fb) : 0.0f;
-}
 
 // block maximum of non-negative floats into *slot (bit patterns order as unsigned integers)
 __device__ __forceinline__ void block_max_f32(float v, unsigned* slot) {
@@ -2115,12 +2170,22 @@ struct FillArgs {
   unsigned* err;
   unsigned* ticket;  // blocks done; the last one advances t (every block has read t by then)
   int advance;
+  int rho_min_pos;   // rho_min > 0: the MIN_RHO test on the bit patterns
 };
 
+// x < m for m > 0 (not NaN) on the integer pipe: true for every negative x and -0, false
+// for NaN, else the order of the non-negative bit patterns
+__device__ __forceinline__ bool below_positive(double x, double m) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long a = b & 0x7fffffffffffffffull;
+  if (a > 0x7ff0000000000000ull) return false;  // NaN
+  return (b >> 63) ? true : b < (unsigned long long)__double_as_longlong(m);
+}
+
+// a 32 x 8 block of ghosted cells (columns 1 .. Nchi, every row)
 __global__ void __launch_bounds__(256) k_fill_minrho(FillArgs A) {
   const hymor_config& c = A.cfg;
   const int nchi = c.nchi, neta = c.neta, NI = nchi + 2;
-  const long G = (long)NI * (neta + 2);
   const double t = A.scal[kT];
   const bool dist = c.dist_amp[0] != 0 || c.dist_amp[1] != 0 || c.dist_amp[2] != 0 || c.dist_amp[3] != 0;
   // every FP64 instruction costs a full pass of the SM partition's FP64 pipe on GB300, so
@@ -2128,9 +2193,9 @@ __global__ void __launch_bounds__(256) k_fill_minrho(FillArgs A) {
   double u_y = 0, u_x = 0;
   if (dist) { u_y = c.rho_v_0 / c.rho_0; u_x = c.rho_u_0 / c.rho_0; }
   unsigned limited = 0;
-  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < G; k += (long)gridDim.x * blockDim.x) {
-    const int i = (int)(k % NI), j = (int)(k / NI);
-    if (i < 1 || i > nchi) continue;
+  const int i = blockIdx.x * 32 + (threadIdx.x & 31) + 1, j = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if (i <= nchi && j <= neta + 1) {
+    const long k = (long)i + (long)j * NI;
     if (c.shock_enabled && j >= A.cell_idx[i - 1] + 2) {
       if (dist) {
         const double pert =
@@ -2143,9 +2208,12 @@ __global__ void __launch_bounds__(256) k_fill_minrho(FillArgs A) {
         A.S.rho[k] = c.rho_0; A.S.ru[k] = c.rho_u_0; A.S.rv[k] = c.rho_v_0; A.S.rE[k] = c.rho_E_0;
       }
     }
-    if (j >= 1 && j <= neta && A.S.rho[k] < c.rho_min) {  // MIN_RHO.jl:16-23
-      A.S.rho[k] = c.rho_min;
-      ++limited;
+    if (j >= 1 && j <= neta) {  // MIN_RHO.jl:16-23
+      const double r = A.S.rho[k];
+      if (A.rho_min_pos ? below_positive(r, c.rho_min) : r < c.rho_min) {
+        A.S.rho[k] = c.rho_min;
+        ++limited;
+      }
     }
   }
   if (limited) atomicAdd(&A.err[kRhoLimited], limited);
@@ -2153,7 +2221,7 @@ __global__ void __launch_bounds__(256) k_fill_minrho(FillArgs A) {
     __syncthreads();
     if (threadIdx.x == 0) {
       __threadfence();
-      if (atomicAdd(A.ticket, 1u) == gridDim.x - 1) {
+      if (atomicAdd(A.ticket, 1u) == gridDim.x * gridDim.y - 1) {
         A.scal[kT] = A.scal[kT] + A.scal[kDt];
         *A.ticket = 0;
       }
@@ -2542,7 +2610,7 @@ void launch_flow_cells(const DevCtx& d, cudaStream_t st) {
   A.cell_idx = d.cell_idx;
   A.scal = d.scal;
   A.err = d.err;
-  k_flow_cells<<<(d.nchi * 32 + 255) / 256, 256, 0, st>>>(A);
+  k_flow_cells<<<(d.nchi * 32 + 63) / 64, 64, 0, st>>>(A);
 }
 
 void launch_sound_cmax(const DevCtx& d, bool recompute, cudaStream_t st, bool max_only) {
@@ -2637,7 +2705,8 @@ void launch_fill_minrho(const DevCtx& d, bool advance_time, cudaStream_t st) {
   A.err = d.err;
   A.ticket = d.ticket + 1;
   A.advance = advance_time;
-  k_fill_minrho<<<grid_for(d.G, 256), 256, 0, st>>>(A);
+  A.rho_min_pos = d.cfg.rho_min > 0;
+  k_fill_minrho<<<dim3((d.nchi + 31) / 32, (d.neta + 2 + 7) / 8), 256, 0, st>>>(A);
 }
 
 void launch_snapshot(const DevCtx& d, cudaStream_t st) {
