@@ -104,10 +104,18 @@ struct UpdArgs {
 __global__ void __launch_bounds__(256) k_update_thermo(UpdArgs a) {
   const int NI = a.nchi + 2, NJ = a.neta + 2;
   const long G = (long)NI * NJ;
-  const double dt = a.scal[kDt];
-  const double wY = a.cY * dt, wS = a.cS * dt;
+  // the stage weights once per block: an FP64 instruction costs the SM partition's FP64 pipe
+  // the same whatever its active lanes
+  __shared__ double wsh[2];
+  if (threadIdx.x == 0) {
+    const double dt = a.scal[kDt];
+    wsh[0] = a.cY * dt;
+    wsh[1] = a.cS * dt;
+  }
+  __syncthreads();
+  const double wY = wsh[0], wS = wsh[1];
   for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < G; k += (long)gridDim.x * blockDim.x) {
-    const int i = (int)(k % NI), j = (int)(k / NI);
+    const int i = (int)((unsigned)k % (unsigned)NI), j = (int)((unsigned)k / (unsigned)NI);
     const bool interior = i >= 1 && i <= a.nchi && j >= 1 && j <= a.neta;
     // Upstream of the shock band (interior rows >= sc + 3) nothing changes the stage array
     // or the solution between the step's first update and its end (the flux is masked
@@ -1802,7 +1810,7 @@ __global__ void __launch_bounds__(256) k_sound_cmax(SoundArgs A) {
       mx = fmax(mx, fabs(A.aS[k]));
       continue;
     }
-    const int i = (int)(k % NI), j = (int)(k / NI);
+    const int i = (int)((unsigned)k % (unsigned)NI), j = (int)((unsigned)k / (unsigned)NI);
     const double c2 = cell_c2(A, k, i, j);
     if (A.mode == 1) {
       const double a = sqrt(c2);
@@ -1912,7 +1920,7 @@ __global__ void __launch_bounds__(256) k_cfl(CflArgs A) {
   const long N = (long)nchi * neta;
   double mlam = 0, mflux = 0;
   for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N; c += (long)gridDim.x * blockDim.x) {
-    const int i = (int)(c % nchi), j = (int)(c / nchi);
+    const int i = (int)((unsigned)c % (unsigned)nchi), j = (int)((unsigned)c / (unsigned)nchi);
     const bool flow = !A.shock || (j + 1 < A.cell_idx[i]);
     if (flow) {
       const long fw = i + (long)j * (nchi + 1), fs = i + (long)j * nchi;
@@ -2014,7 +2022,7 @@ __global__ void __launch_bounds__(256) k_cmax_screen(SoundArgs A, float* c2f, un
   const float gm1 = (float)(A.gamma - 1), gam = (float)A.gamma;
   float mx = 0.0f;
   for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < G; k += (long)gridDim.x * blockDim.x) {
-    const int i = (int)(k % NI), j = (int)(k / NI);
+    const int i = (int)((unsigned)k % (unsigned)NI), j = (int)((unsigned)k / (unsigned)NI);
     bool bad = false;
     auto pres = [&](long q, float& r) {
       r = trunc_float(A.S.rho[q], bad);
@@ -2045,7 +2053,7 @@ __global__ void __launch_bounds__(256) k_cmax_exact(SoundArgs A, const float* c2
   const float keep = M > 0.0f ? M * kScreenKeep : -__int_as_float(0x7f800000);
   double mx = 0;
   for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < G; k += (long)gridDim.x * blockDim.x) {
-    const int i = (int)(k % NI), j = (int)(k / NI);
+    const int i = (int)((unsigned)k % (unsigned)NI), j = (int)((unsigned)k / (unsigned)NI);
     const bool nb = ((A.nrcbc & 1) && i == 1) || ((A.nrcbc & 2) && i == NI - 2) ||
                     ((A.nrcbc & 4) && j == 1) || ((A.nrcbc & 8) && j == NJ - 2);
     if (!(c2f[k] < keep) || nb) {
@@ -2069,7 +2077,7 @@ __global__ void __launch_bounds__(256) k_cfl_screen(CflArgs A, float* rf, unsign
   const float cmax = trunc_float(A.scal[kCmax], bad_c);
   float mx = 0.0f;
   for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N; c += (long)gridDim.x * blockDim.x) {
-    const int i = (int)(c % nchi), j = (int)(c / nchi);
+    const int i = (int)((unsigned)c % (unsigned)nchi), j = (int)((unsigned)c / (unsigned)nchi);
     if (A.shock && !(j + 1 < A.cell_idx[i])) continue;
     bool bad = bad_c;
     const long g = gidx(i + 1, j + 1, nchi);
@@ -2114,7 +2122,7 @@ __global__ void __launch_bounds__(256) k_cfl_exact(CflArgs A, const float* rf, u
   const double cmax = A.scal[kCmax];
   double mlam = 0, mflux = 0;
   for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N; c += (long)gridDim.x * blockDim.x) {
-    const int i = (int)(c % nchi), j = (int)(c / nchi);
+    const int i = (int)((unsigned)c % (unsigned)nchi), j = (int)((unsigned)c / (unsigned)nchi);
     if (A.shock && !(j + 1 < A.cell_idx[i])) continue;
     const long g = gidx(i + 1, j + 1, nchi);
     const bool eval = !(rf[c] < keep);
@@ -2265,7 +2273,7 @@ __global__ void k_classical_stage(ClassArgs A) {
   const long G = (long)NI * (A.neta + 2);
   const double w = A.cY * A.scal[kDt];
   for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < G; k += (long)gridDim.x * blockDim.x) {
-    const int i = (int)(k % NI), j = (int)(k / NI);
+    const int i = (int)((unsigned)k % (unsigned)NI), j = (int)((unsigned)k / (unsigned)NI);
     double r = A.Yc.rho[k], u = A.Yc.ru[k], v = A.Yc.rv[k], e = A.Yc.rE[k];
     if (i >= 1 && i <= A.nchi && j >= 1 && j <= A.neta && flow_at(A.cell_idx, A.shock, i - 1, j)) {
       const long c = (long)(i - 1) + (long)(j - 1) * A.nchi;
@@ -2284,6 +2292,8 @@ __global__ void k_classical_stage(ClassArgs A) {
 // symmetry fix of the classical stage points runs after the stage kernel
 __global__ void k_sym_fix(ShockPts p) { p.x[0] = p.x[1]; }
 
+// (a context's ghosted grid has at most 2^30 cells, so the grid-stride kernels split a cell
+// index into (i, j) by 32-bit unsigned division)
 int grid_for(long n, int threads) {
   long b = (n + threads - 1) / threads;
   const long cap = 152L * 16;
