@@ -1667,6 +1667,7 @@ struct FlowArgs {
   int* cell_idx;
   const double* scal;
   unsigned* err;
+  int disturbed;  // any freestream disturbance amplitude non-zero (set on the host)
 };
 
 // The nearest cell centre of a column is found by an FP32 screen: every row's squared
@@ -1713,6 +1714,7 @@ __global__ void __launch_bounds__(64) k_flow_cells(FlowArgs A) {
   scr.px = trunc_float(px, scr.bad);
   scr.py = trunc_float(py, scr.bad);
   float top = __int_as_float(0x7f800000);
+#pragma unroll 4
   for (int j = 1 + lane; j <= neta; j += 32) {
     float lo, hi;
     near_bounds(scr, xc[j], yc[j], lo, hi);
@@ -1723,6 +1725,7 @@ __global__ void __launch_bounds__(64) k_flow_cells(FlowArgs A) {
   // the FP64 distances of the candidates; non-negative doubles order as their bit patterns
   unsigned long long best = 0x7ff0000000000000ull;  // +inf
   int bj = 0x7fffffff;
+#pragma unroll 4
   for (int j = 1 + lane; j <= neta; j += 32) {
     const double x = xc[j], y = yc[j];
     float lo, hi;
@@ -1748,7 +1751,7 @@ __global__ void __launch_bounds__(64) k_flow_cells(FlowArgs A) {
   }
   // UPDATE_FIELD_UPSTREAM: ghosted rows >= sc + 2 of this column
   const double t = A.scal[kT];
-  const bool dist = c.dist_amp[0] != 0 || c.dist_amp[1] != 0 || c.dist_amp[2] != 0 || c.dist_amp[3] != 0;
+  const bool dist = A.disturbed;
   double u_y = 0, u_x = 0;
   if (dist) { u_y = c.rho_v_0 / c.rho_0; u_x = c.rho_u_0 / c.rho_0; }
   for (int jg = bj + 2 + lane; jg < NJ; jg += 32) {
@@ -2178,7 +2181,7 @@ struct FillArgs {
   unsigned* err;
   unsigned* ticket;  // blocks done; the last one advances t (every block has read t by then)
   int advance;
-  int rho_min_pos;   // rho_min > 0: the MIN_RHO test on the bit patterns
+  int disturbed;     // any freestream disturbance amplitude non-zero (set on the host)
 };
 
 // x < m for m > 0 (not NaN) on the integer pipe: true for every negative x and -0, false
@@ -2190,12 +2193,14 @@ __device__ __forceinline__ bool below_positive(double x, double m) {
   return (b >> 63) ? true : b < (unsigned long long)__double_as_longlong(m);
 }
 
-// a 32 x 8 block of ghosted cells (columns 1 .. Nchi, every row)
+// a 32 x 8 block of ghosted cells (columns 1 .. Nchi, every row); MINPOS: rho_min > 0, the
+// MIN_RHO test on the bit patterns
+template <bool MINPOS>
 __global__ void __launch_bounds__(256) k_fill_minrho(FillArgs A) {
   const hymor_config& c = A.cfg;
   const int nchi = c.nchi, neta = c.neta, NI = nchi + 2;
   const double t = A.scal[kT];
-  const bool dist = c.dist_amp[0] != 0 || c.dist_amp[1] != 0 || c.dist_amp[2] != 0 || c.dist_amp[3] != 0;
+  const bool dist = A.disturbed;
   // every FP64 instruction costs a full pass of the SM partition's FP64 pipe on GB300, so
   // the convection speeds of the disturbance are only formed when there is one
   double u_y = 0, u_x = 0;
@@ -2218,7 +2223,7 @@ __global__ void __launch_bounds__(256) k_fill_minrho(FillArgs A) {
     }
     if (j >= 1 && j <= neta) {  // MIN_RHO.jl:16-23
       const double r = A.S.rho[k];
-      if (A.rho_min_pos ? below_positive(r, c.rho_min) : r < c.rho_min) {
+      if (MINPOS ? below_positive(r, c.rho_min) : r < c.rho_min) {
         A.S.rho[k] = c.rho_min;
         ++limited;
       }
@@ -2620,6 +2625,8 @@ void launch_flow_cells(const DevCtx& d, cudaStream_t st) {
   A.cell_idx = d.cell_idx;
   A.scal = d.scal;
   A.err = d.err;
+  const hymor_config& c = d.cfg;
+  A.disturbed = c.dist_amp[0] != 0 || c.dist_amp[1] != 0 || c.dist_amp[2] != 0 || c.dist_amp[3] != 0;
   k_flow_cells<<<(d.nchi * 32 + 63) / 64, 64, 0, st>>>(A);
 }
 
@@ -2715,8 +2722,13 @@ void launch_fill_minrho(const DevCtx& d, bool advance_time, cudaStream_t st) {
   A.err = d.err;
   A.ticket = d.ticket + 1;
   A.advance = advance_time;
-  A.rho_min_pos = d.cfg.rho_min > 0;
-  k_fill_minrho<<<dim3((d.nchi + 31) / 32, (d.neta + 2 + 7) / 8), 256, 0, st>>>(A);
+  const hymor_config& c = d.cfg;
+  A.disturbed = c.dist_amp[0] != 0 || c.dist_amp[1] != 0 || c.dist_amp[2] != 0 || c.dist_amp[3] != 0;
+  const dim3 grid((d.nchi + 31) / 32, (d.neta + 2 + 7) / 8);
+  if (c.rho_min > 0)
+    k_fill_minrho<true><<<grid, 256, 0, st>>>(A);
+  else
+    k_fill_minrho<false><<<grid, 256, 0, st>>>(A);
 }
 
 void launch_snapshot(const DevCtx& d, cudaStream_t st) {
