@@ -140,6 +140,39 @@ def test_cfl_timestep_parity(require_gpu):
     assert abs(S.CFL_TIMESTEP(sol) - orc.cfl()) < 1e-14 * orc.cfl()
 
 
+@pytest.mark.parametrize("interp", ["1st", "2nd", "3rd"])
+def test_flow_cells_nearest_row_ties(require_gpu, interp):
+    """UPDATE_FLOW_CELLS finds each shock point's nearest cell centre along its column through
+    an FP32 screen with an error bound and FP64 distances for the rows the bound keeps. Points
+    on a cell centre, halfway between two centres (a tie in real arithmetic, broken or kept by
+    the FP64 rounding the same way in both) and at random along the column give the oracle's
+    rows, upstream fill and extrapolation, bit for bit."""
+    cfg = C.cylinder_config(64, 40, shock_interp=interp)
+    cs = C.initial_state(cfg, seed=2, noise=1e-6)
+    xe, ye = cs.mesh.arrays["x_ext"], cs.mesh.arrays["y_ext"]  # ghosted centres (Nchi+2, Neta+2)
+    rng = np.random.default_rng(5)
+    px, py = cs.pts_x.copy(), cs.pts_y.copy()
+    for i in range(cfg.nchi):
+        I, j = i + 1, int(rng.integers(4, cfg.neta - 4))
+        if i % 3 == 0:
+            px[i], py[i] = xe[I, j], ye[I, j]
+        elif i % 3 == 1:
+            px[i], py[i] = (xe[I, j] + xe[I, j + 1]) / 2, (ye[I, j] + ye[I, j + 1]) / 2
+        else:
+            f = rng.uniform()
+            px[i] = xe[I, j] + f * (xe[I, j + 1] - xe[I, j])
+            py[i] = ye[I, j] + f * (ye[I, j + 1] - ye[I, j])
+    sol, orc = S.Solution(cs), O.Oracle(cs)
+    for s in (sol, orc):
+        s.set_state(cs.q_flat(), px, py, cs.pts_chi, cs.pts_eta, cs.cell_idx, 0.0)
+    S.UPDATE_FLOW_CELLS(sol)
+    orc.update_flow_cells()
+    a, b = sol.get_state(), orc.get_state()
+    assert np.array_equal(a["cell_idx"], b["cell_idx"])
+    assert np.array_equal(a["q"], b["q"])
+    sol.close()
+
+
 def test_advect_host_matches_separate_calls(require_gpu):
     """hymor_advect (upload, steps, download in one call) gives exactly what
     hymor_set_state + hymor_step + hymor_get_state give."""
