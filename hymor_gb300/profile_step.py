@@ -27,7 +27,7 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=2)
     ap.add_argument("--viscous", choices=["ff", "fp64"], default="ff")
-    ap.add_argument("--tiling", default=None, help="rows,spare,tma (default: the library's)")
+    ap.add_argument("--tiling", default=None, help="rows,spare,tma (rows 4: the split tiling; default: the library's)")
     ap.add_argument("--linearize", action="store_true")
     ap.add_argument("--expm", type=int, default=0, help="vectors to propagate after linearising")
     ap.add_argument("--expm-steps", type=int, default=50)

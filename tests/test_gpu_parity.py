@@ -436,6 +436,8 @@ def test_flux_tilings_bit_identical(require_gpu):
     f_ref = S.PDE(ref)  # PDE mutates its solution: evaluate each solution once
     for rows, spare, tma in ((16, 0, 1), (16, 2, 0), (8, 0, 0), (8, 1, 1), (4, 0, 0), (4, 2, 1)):
         sol = S.Solution(cs)
+        for bad in ((5, 0, 0), (32, 0, 0), (4, 5, 0), (8, 0, 2)):
+            assert sol.ctx.L.hymor_set_flux_tiling(sol.ctx.h, *bad) == -1, bad
         sol.ctx.check(sol.ctx.L.hymor_set_flux_tiling(sol.ctx.h, rows, spare, tma))
         S.ADVECT_FLOW(sol, 5)
         st = sol.get_state()
