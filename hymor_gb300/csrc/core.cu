@@ -45,7 +45,6 @@ struct TileGeo {
   static constexpr int HP = TMA ? kTmaBoxX : HX;   // halo row pitch in shared memory
   static constexpr int PS = TMA ? (HP * (TYV + 2) + 15) / 16 * 16 : NH;  // halo plane stride
   static constexpr int NCOR = CX * (TYV + 1);      // corners
-  static constexpr int NLRF = (TX + 1) * TYV;      // lr faces
   static constexpr int NBTF = TX * (TYV + 1);      // bt faces
   static constexpr int THREADS = 32 * TYV;
 };
@@ -1295,10 +1294,10 @@ __device__ __forceinline__ bool flux_tile(const FluxArgs& a, const FluxMaps& tm,
   double* s_uc = s_v + G::PS;
   double* s_vc = s_uc + G::NCOR;
   double* s_Tc = s_vc + G::NCOR;
-  double* f_lr = s_Tc + G::NCOR;                // 4 x G::NLRF
-  double* f_bt = f_lr + 4 * G::NLRF;            // 4 x G::NBTF
-  double* t_lr = f_bt + 4 * G::NBTF;            // AXI hoop stress on faces
-  double* t_bt = t_lr + (AXI ? G::NLRF : 0);
+  // the lr faces stay in registers (a row's faces are one warp's lanes: a cell's east face
+  // is the next lane's west face); the bottom/top faces cross warps and go through here
+  double* f_bt = s_Tc + G::NCOR;                // 4 x G::NBTF
+  double* t_bt = f_bt + 4 * G::NBTF;            // AXI hoop stress on bt faces
   // the float-float variant keeps u, v, T and the corner sums as float-float pairs in the
   // same shared slots (8 bytes per entry either way)
   ff* fu = reinterpret_cast<ff*>(s_u);
@@ -1423,17 +1422,17 @@ __device__ __forceinline__ bool flux_tile(const FluxArgs& a, const FluxMaps& tm,
   }
   __syncthreads();
   const long NLR = (long)(nchi + 1) * neta, NBT = (long)nchi * (neta + 1);
-  // (3a) lr faces: warp = tile row fy, lane = fx (32 faces per row)
+  // (3a) lr faces: warp = tile row fy, lane = fx (32 faces per row), into registers
+  double fl[4] = {0.0, 0.0, 0.0, 0.0}, tl = 0.0;
   {
     const int fx = lane, fy = warp;
     const int gi = i0 + fx, gj = j0 + fy;  // face (gi, gj) 0-based: between ghosted (gi, gj+1), (gi+1, gj+1)
-    const int o = fx + fy * (TX + 1);
     if (FFV && gi <= nchi && gj < neta) {
       const long f = (long)gi + (long)gj * (nchi + 1);
       const int L = hid(fx, fy + 1);
       face_flux_ff<true, AXI, SUTH>(a, s_r, s_ru, s_rv, s_rE, s_p, fu, fv, fT, fuc, fvc, fTc, L, L + 1,
                                     fx + fy * CX, fx + fy * CX + CX, a.m.lra, a.m.lrf, NLR, f,
-                                    AXI ? a.m.rx_lr[f] : 0.0, f_lr + o, G::NLRF, t_lr + o);
+                                    AXI ? a.m.rx_lr[f] : 0.0, fl, 1, &tl);
     } else if (gi <= nchi && gj < neta) {
       const long f = (long)gi + (long)gj * (nchi + 1);
       const double nx = a.m.lrg[f], ny = a.m.lrg[NLR + f], Ah = a.m.lrg[2 * NLR + f];
@@ -1483,13 +1482,18 @@ __device__ __forceinline__ bool flux_tile(const FluxArgs& a, const FluxMaps& tm,
         if (AXI) hoop = fma(-2.0 / 3.0, div, 2 * uf * rx);
       }
       const double w = fma(Su, tx, Sv * ty) * ir;
-      f_lr[o] = m2 * Ah;
-      f_lr[G::NLRF + o] = fma(Su, Vn, fma(Sp, nx, tx)) * Ah;
-      f_lr[2 * G::NLRF + o] = fma(Sv, Vn, fma(Sp, ny, ty)) * Ah;
-      f_lr[3 * G::NLRF + o] = fma(SE + Sp, Vn, w + qn) * Ah;
-      if (AXI) t_lr[o] = (0.5 * mu_f) * hoop;
+      fl[0] = m2 * Ah;
+      fl[1] = fma(Su, Vn, fma(Sp, nx, tx)) * Ah;
+      fl[2] = fma(Sv, Vn, fma(Sp, ny, ty)) * Ah;
+      fl[3] = fma(SE + Sp, Vn, w + qn) * Ah;
+      if (AXI) tl = (0.5 * mu_f) * hoop;
     }
   }
+  // west minus east face of the lane's cell (the last lane's value is unused: TX = 31)
+  double dl[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) dl[k] = fl[k] - __shfl_down_sync(0xffffffffu, fl[k], 1);
+  const double tls = AXI ? tl + __shfl_down_sync(0xffffffffu, tl, 1) : 0.0;
   // (3b) bt faces: TX x (TYV + 1)
   for (int b = tid; b < (TX + 1) * (TYV + 1); b += G::THREADS) {
     const int fx = b & 31, fy = b >> 5;
@@ -1563,24 +1567,23 @@ __device__ __forceinline__ bool flux_tile(const FluxArgs& a, const FluxMaps& tm,
       double r0 = 0, r1 = 0, r2 = 0, r3 = 0;
       const bool active = !a.mask || (cj + 1 < a.cell_idx[ci]);
       if (active) {
-        const int w = cx + cy * (TX + 1), e = w + 1;
         const int s = cx + cy * TX, n = s + TX;
         const double rv = a.m.rvol[c];
-        r0 = (f_lr[w] - f_lr[e] + f_bt[s] - f_bt[n]) * rv;
-        r1 = (f_lr[G::NLRF + w] - f_lr[G::NLRF + e] + f_bt[G::NBTF + s] - f_bt[G::NBTF + n]) * rv;
-        double v2 = f_lr[2 * G::NLRF + w] - f_lr[2 * G::NLRF + e] + f_bt[2 * G::NBTF + s] - f_bt[2 * G::NBTF + n];
+        r0 = (dl[0] + f_bt[s] - f_bt[n]) * rv;
+        r1 = (dl[1] + f_bt[G::NBTF + s] - f_bt[G::NBTF + n]) * rv;
+        double v2 = dl[2] + f_bt[2 * G::NBTF + s] - f_bt[2 * G::NBTF + n];
         if (AXI) {
           // FLUX_MOMENTUM_3D.jl:120-122: front/back pressure with sign(y) of the cell centre
           const double pc = s_p[hid(cx + 1, cy + 1)];
           const double ycell = a.m.y_ext[(long)(ci + 1) + (long)(cj + 1) * (nchi + 2)];
           v2 += (pc * a.m.fb_yn_front - pc * a.m.fb_yn_back) * a.m.fb_area[c] * jsign(ycell);
           // VISCOUS_FLUX_3D.jl:154-177: hoop stress, radius = x of the cell centre
-          const double tth = (t_lr[w] + t_lr[e] + t_bt[s] + t_bt[n]) * 0.25;
+          const double tth = (tls + t_bt[s] + t_bt[n]) * 0.25;
           const double xcell = a.m.x_ext[(long)(ci + 1) + (long)(cj + 1) * (nchi + 2)];
           r1 -= tth * frcp(xcell);
         }
         r2 = v2 * rv;
-        r3 = (f_lr[3 * G::NLRF + w] - f_lr[3 * G::NLRF + e] + f_bt[3 * G::NBTF + s] - f_bt[3 * G::NBTF + n]) * rv;
+        r3 = (dl[3] + f_bt[3 * G::NBTF + s] - f_bt[3 * G::NBTF + n]) * rv;
       }
       a.o0[c] = r0; a.o1[c] = r1; a.o2[c] = r2; a.o3[c] = r3;
     }
@@ -1588,9 +1591,16 @@ __device__ __forceinline__ bool flux_tile(const FluxArgs& a, const FluxMaps& tm,
   return true;
 }
 
+// The 2-D constant-viscosity 31 x 4 kernel is held to 56 registers for nine resident blocks
+// per SM (its shared memory allows ten), so that the persistent interior grid of the split
+// tiling keeps eight beside a spare slot; the others to 64.
+template <bool AXI, bool SUTH, int TYV>
+constexpr int flux_min_blocks() { return TYV == 4 && !AXI && !SUTH ? 9 : 32 / TYV; }
+
 // Tile grid (no list), or a persistent grid striding over the compact tile list of a class.
 template <bool AXI, bool SUTH, int TYV, bool FFV, bool TMA>
-__global__ void __launch_bounds__(32 * TYV, 32 / TYV) k_flux(FluxArgs a, const __grid_constant__ FluxMaps tm) {
+__global__ void __launch_bounds__(32 * TYV, flux_min_blocks<AXI, SUTH, TYV>())
+    k_flux(FluxArgs a, const __grid_constant__ FluxMaps tm) {
   extern __shared__ double sm_raw[];
   __shared__ uint64_t bar;  // completion of the halo TMA transfers of a tile
   // TMA destinations start on a 128-byte boundary (128 bytes of slack in the launch's size)
@@ -1618,7 +1628,7 @@ __global__ void __launch_bounds__(32 * TYV, 32 / TYV) k_flux(FluxArgs a, const _
 template <bool AXI, bool SUTH, int TYV = TY, bool TMA = false>
 size_t flux_smem() {
   using G = TileGeo<TYV, TMA>;
-  return sizeof(double) * (8 * G::PS + 3 * G::NCOR + 4 * G::NLRF + 4 * G::NBTF + (AXI ? G::NLRF + G::NBTF : 0)) +
+  return sizeof(double) * (8 * G::PS + 3 * G::NCOR + 4 * G::NBTF + (AXI ? G::NBTF : 0)) +
          (TMA ? 128 : 0);
 }
 
