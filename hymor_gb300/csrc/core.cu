@@ -1,23 +1,26 @@
 // Residual, shock fitting, boundary conditions and time-marching kernels (sm_103a).
 //
 // One RK4 step (ADVECT_FLOW_EXPLICIT, utils/Time_marching/ADVECT_FLOW_EXPLICIT.jl:36-81)
-// is one CUDA graph of these kernels over four streams (api.cu, enqueue_step):
+// is one CUDA graph of these kernels over five streams (api.cu, enqueue_step):
 //
 //   k_flow_cells        UPDATE_FLOW_CELLS on S (a warp per chi column)
 //   k_classify_tiles    the step's flux tile lists (interior / shock and boundary)
-//   k_sound_cmax, k_cfl_faces, k_cfl, k_cfl_final   CFL_TIMESTEP, dt on the device
+//   k_cmax_screen, k_cmax_exact, k_cfl_screen, k_cfl_exact   CFL_TIMESTEP through an FP32
+//                       screen and an exact FP64 pass, dt on the device (k_sound_cmax,
+//                       k_cfl_faces, k_cfl, k_cfl_final: the FP64 reduction over every cell)
 //   k_update_thermo     the stage copy and stage updates of Y and S, p and T
 //   k_spline_rows, k_spline_fit   the smoothing-spline fit of the shock points (one CTA)
-//   k_shock_columns     R-H jump, extrapolation, MOVE_SHOCK (a thread per column)
+//   k_shock_columns     R-H jump, extrapolation, MOVE_SHOCK (three warps per 32 columns)
 //   k_move_shock        MOVE_SHOCK of the first stage, once dt is known (one CTA)
 //   k_bc_edges          ghost-cell boundary conditions (chi edges, then eta edges)
-//   k_flux              the FV residual of a stage, 31x8-cell tiles, in two launches
+//   k_flux              the FV residual of a stage, in two launches (interior tiles, then
+//                       the shock-band and boundary tiles)
 //   k_fill_minrho       UPDATE_FIELD_UPSTREAM + MIN_RHO on S, t += dt
 //
 // The flux kernel dominates. It is FP64-bound on GB300 (the DFMA rate is about 1.7 per
 // clock per SM): geometry-only factors are precomputed per face (common.cuh), every face
-// flux is evaluated once per tile in shared memory, and divisions are replaced by
-// reciprocal multiplies (frcp).
+// flux is evaluated once per tile, the viscous terms of the RK step in float-float on the
+// FP32 pipe (ff.cuh), and divisions are replaced by reciprocal multiplies (frcp).
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
