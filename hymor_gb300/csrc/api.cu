@@ -294,8 +294,8 @@ int enqueue_step(hymor_ctx* ctx, bool with_events) {
       // next fit (stage k+1 on Y, or the step-end fit on S) overlaps this stage's remaining work
       launch_spline(d, k == 3, false, sx);
       TRY(ev(4 * k));
-      // the interior flux leaves one block slot per SM to the side-stream kernels and the
-      // shock/boundary-class flux
+      // the interior flux leaves spare block slots per SM (flux_spare) to the side-stream
+      // kernels and the shock/boundary-class flux
       if (k == 0) CU(cudaStreamWaitEvent(st, ctx->cls_ev, 0));
       launch_flux_class(d, false, F, 0, st, d.flux_spare, d.step_ffv != 0);
       TRY(ev(4 * k + 1));
@@ -728,7 +728,7 @@ int hymor_ctx_create(const hymor_config* cfg, const hymor_mesh* mesh, hymor_ctx*
   d.expm_ff = 1;
   d.cfl_screen = 1;
   d.flux_rows = 4;  // the split tiling
-  d.flux_spare = 2;
+  d.flux_spare = 1;
   d.tma = make_flux_maps(d);
   ctx->tma_able = d.tma;
   for (int k = 0; k < hymor_ctx_s::kEv; ++k)

@@ -1132,7 +1132,7 @@ __global__ void __launch_bounds__(256) k_bc_edges(BcArgs A) {
 
 // ---------------------------------------------------------------------------
 // Residual: FLUX_MASS/MOMENTUM/TOTAL_ENERGY + VISCOUS_FLUX (and the *_3D forms),
-// fused and face-centric, one 31x8-cell tile per CTA.
+// fused and face-centric, one 31 x TYV-cell tile per CTA.
 struct FluxArgs {
   const double *rho, *ru, *rv, *rE, *p, *T;
   double *o0, *o1, *o2, *o3;

@@ -148,16 +148,17 @@ int hymor_set_expm_arith(hymor_ctx* ctx, int mode);
 /* Tile-shape autotuner of the RK step's flux (no counterpart in the reference): times `steps`
  * steps (CUDA events, after a warm-up step) for each flux configuration — the tile halo staged
  * by TMA (cp.async.bulk.tensor) or loaded thread by thread, tiles of 31 x 8 or 31 x 16 cells
- * or the split tiling (rows = 4: the interior tiles as 31 x 4 halves, by thread loads, the
- * shock/boundary tiles 31 x 8), and 0, 1 or 2 block slots per SM that the persistent
+ * or the split tiling (rows = 4: the tiles classified at 31 x 8 cells and run as 31 x 4 halves,
+ * halo by thread loads), and 0, 1 or 2 block slots per SM that the persistent
  * interior-tile grid leaves to the side streams — each from the same saved state, restores the
  * state, and keeps the fastest. choice[3] = (rows, spare, tma); ms_per_step[18] (or NULL) = the
  * candidates' times, index 9 tma + 3 r + spare with r = 0, 1, 2 for rows 8, 16, 4 (0 where a
  * TMA candidate could not run: Nchi odd). Every
  * configuration gives bit-identical fluxes (each face flux has the same arithmetic whichever
  * tile computes it, and the staged halo holds the same values). hymor_set_flux_tiling sets one
- * directly (default: the split tiling, 2 spare slots, TMA when Nchi is even: the split tiling
- * stages by TMA only the whole-grid flux of the classical RK4 scheme). */
+ * directly (default: the split tiling, 1 spare slot, TMA when Nchi is even: with the split
+ * tiling only the whole-grid flux of the residual and of the classical RK4 scheme stages its
+ * halo by TMA). */
 int hymor_autotune(hymor_ctx* ctx, int steps, int32_t* choice, float* ms_per_step);
 int hymor_set_flux_tiling(hymor_ctx* ctx, int rows, int spare, int tma);
 
